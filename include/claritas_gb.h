@@ -1,0 +1,255 @@
+/* claritas_gb.h -- C ABI of the GB300 photon-transport library (libclaritas_gb.so).
+ *
+ * This library replaces the device half of the CLARITAS forward model:
+ *   - trace_kernel          CLARITAS/CLARITAS.py:4551-5104 (234 launch arguments, launch :7638-7758)
+ *   - score_detectors_kernel CLARITAS/CLARITAS.py:4378-4436 (47 launch arguments, launch :7783-7847)
+ *   - the particle-physics precompute launched from
+ *     ClaritasForwardModel._prepare_gpu_particle_physics, CLARITAS/CLARITAS.py:6036-6965:
+ *     PSD normalisation (:3607-3635), Mie coefficients/efficiencies (:3495-3559),
+ *     theta grid (:3488-3493), phase pdf (:3561-3581), phase cdf (:3583-3592),
+ *     transport rates (:3845-3921), sediment coefficients and majorants (:3940-4038).
+ * The reference binds these through CuPy RawModule launches with positional
+ * numpy scalars and CuPy device arrays. Here the whole scene is one POD struct
+ * and every call returns an int status (0 = success, negative = error); the text
+ * of the last error is available from clr_last_error().
+ *
+ * Units: metres, kg/m^3 (= g/L), radians unless named otherwise. The coordinate
+ * frame is the reference's: z = 0 at the sensor-ring plane, the LED bore at
+ * 180 degrees launches along +y, detector j looks along (sin 10j deg, cos 10j deg).
+ *
+ * Threading: a context owns one CUDA stream and its device allocations; it must
+ * not be used from two host threads at once. Calls are synchronous from the
+ * caller's point of view.
+ */
+#ifndef CLARITAS_GB_H
+#define CLARITAS_GB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CLR_N_DETECTORS 18
+#define CLR_MAX_BINS 64            /* AGG_MAX_BINS, CLARITAS/CLARITAS.py:3599 */
+#define CLR_MIE_MAX_ORDER 4096     /* MIE_MAX_ORDER, CLARITAS/CLARITAS.py:1136 */
+#define CLR_N_STATUS 16
+#define CLR_N_FAILURE_CODES 32
+#define CLR_N_EVENT_COUNTERS 24
+#define CLR_N_CONDITIONAL_STATS 10
+
+/* status codes returned by every entry point */
+enum {
+    CLR_OK = 0,
+    CLR_ERR_INVALID_ARGUMENT = -1,
+    CLR_ERR_CUDA = -2,
+    CLR_ERR_NOT_READY = -3,
+    CLR_ERR_UNSUPPORTED = -4,
+    CLR_ERR_PRECOMPUTE = -5,   /* a precompute kernel raised its error word (reference error_flag) */
+    CLR_ERR_DEVICE_TIMEOUT = -6
+};
+
+/* random-number back-ends */
+enum {
+    CLR_RNG_REFERENCE_XORSHIFT = 0, /* the reference's per-ray xorshift32 streams, bit-exact parity mode */
+    CLR_RNG_PHILOX = 1              /* counter-based Philox4x32-10 keyed by (seed, scenario, photon) */
+};
+
+/* photon weighting */
+enum {
+    CLR_WEIGHT_ANALOG = 0,   /* reference semantics: absorption is terminal, every weight is 1 */
+    CLR_WEIGHT_IMPLICIT = 1  /* implicit capture at absorbing bins + Russian roulette below a threshold */
+};
+
+/* source models */
+enum {
+    CLR_SOURCE_REFERENCE_LED = 0,  /* Gaussian spot + Beta angular law through the 180-degree bore */
+    CLR_SOURCE_COLLIMATED_DISC = 1 /* uniform disc beam, launched at the inner wall, no collimator */
+};
+
+/* Scene description. Field names follow the ClaritasForwardModel constructor
+ * (CLARITAS/CLARITAS.py:5577-5652) after its derived quantities
+ * (zmin = -sensor_height, zmean = water_height - sensor_height, ... :5671-5699). */
+typedef struct clr_scene_params {
+    /* refractive indices */
+    float n_water, n_acrylic, n_air, bore_n, ring_face_n, bottom_external_n;
+    /* cell */
+    float rin, rout, zmin, zmean, zwall_top, bottom_disc_thickness;
+    /* sensor ring and bores */
+    float ring_in, throat_out, ring_out, source_r, throat_r, counterbore_r;
+    /* source */
+    float beam_sigma, alpha1, alpha2, legacy_accept_deg;
+    int32_t source_angular_model;   /* SOURCE_ANGULAR_MODEL_CODES :5553 */
+    int32_t source_bore_model;      /* BORE_SURFACE_MODEL_CODES :5558 */
+    int32_t detector_bore_model;
+    int32_t ring_face_model;        /* RING_FACE_SURFACE_MODEL_CODES :5559 */
+    int32_t photodiode_model;       /* PHOTODIODE_RESPONSE_MODEL_CODES :5560 */
+    int32_t max_bore_bounces, max_ring_face_bounces;
+    /* free surface */
+    int32_t free_surface_model;     /* FREE_SURFACE_MODEL_CODES :5565 */
+    float vortex_delta_h, vortex_core_radius;
+    /* particle event law */
+    float wavelength;               /* vacuum wavelength used inside particles */
+    float rough_alpha;              /* tan(particle_surface_rms_slope_deg) */
+    float spheroid_aspect, orientation_kappa;
+    int32_t orientation_model;
+    int32_t max_particle_bounces, max_cell_bounces, max_axial_bounces;
+    float max_iterations;
+    int32_t event_model;            /* EVENT_MODEL_CODES :5544 */
+    int32_t conditional_retries;    /* CONDITIONAL_MAX_TRIALS :1117 */
+    int32_t sediment_model;         /* SEDIMENT_TRANSPORT_MODEL_CODES :5570 */
+    /* new source option (no reference counterpart; ignored when source_kind == CLR_SOURCE_REFERENCE_LED) */
+    int32_t source_kind;
+    float disc_radius;              /* collimated disc beam radius */
+    float disc_height;              /* beam axis height z (same frame) */
+    int32_t reserved[4];
+} clr_scene_params;
+
+/* Particle population and the inputs of the Mie/rate precompute
+ * (_prepare_gpu_particle_physics, CLARITAS/CLARITAS.py:6036-6330). */
+typedef struct clr_particle_spec {
+    int32_t n_bins;                 /* 1..CLR_MAX_BINS */
+    int32_t n_theta;                /* mie_phase_grid_size; 2 selects the dummy 2-point table */
+    int32_t weight_mode;            /* 0 mass_fraction, 1 number_fraction */
+    int32_t moment_enabled;         /* 1 when moment_a/b/mode are supplied */
+    const double* diameter_m;
+    const double* weight;           /* PSD weights, normalised internally */
+    const double* n_real;
+    const double* k_imag;
+    const double* moment_a;         /* nullable */
+    const double* moment_b;         /* nullable */
+    const uint8_t* moment_mode;     /* nullable */
+    double concentration_kg_m3;
+    double density_kg_m3;
+    double n_medium;
+    double wavelength_m;
+    double wave_rms_height_m;
+    double hybrid_wave_scale;
+} clr_particle_spec;
+
+/* Inputs of the sediment coefficient precompute (CLARITAS/CLARITAS.py:3940-4038) and,
+ * for sediment model 3, an externally supplied (r,z) concentration-scale grid laid
+ * out [bin][ir][iz] as the reference's SED_GRID (:1537-1558). */
+typedef struct clr_sediment_spec {
+    double particle_density, water_density, water_viscosity, gravity, eddy_diffusivity;
+    int32_t n_quad, n_radial;
+    int32_t grid_nr, grid_nz;
+    const double* grid;             /* nullable unless sediment_model == 3 */
+    double grid_zmax;
+} clr_sediment_spec;
+
+/* One transport run over a contiguous range of global ray ids. The three
+ * transport seeds and the detector seed are the reference's derived seeds
+ * (simulate, CLARITAS/CLARITAS.py:7304-7306 and :7780-7782). */
+typedef struct clr_run_params {
+    int64_t n_rays;
+    uint32_t ray_offset;
+    uint32_t seed0, seed1, seed2, detector_seed;
+    int32_t rng_mode;               /* CLR_RNG_* */
+    uint64_t philox_key;            /* CLR_RNG_PHILOX: 64-bit key */
+    uint32_t scenario_id;           /* CLR_RNG_PHILOX: folded into the counter */
+    int32_t weight_mode;            /* CLR_WEIGHT_* */
+    float roulette_threshold;       /* CLR_WEIGHT_IMPLICIT only */
+    float roulette_survival;        /* weight given to survivors; probability = w / survival */
+    int32_t block_threads;          /* 0 = autotuned default */
+    int32_t rays_per_item;          /* work-queue granularity; 0 = default */
+    int32_t reserved[4];
+} clr_run_params;
+
+/* Per-ray record, written only when a record buffer is passed to clr_trace
+ * (parity tests). Integer fields are the reference's per-ray outputs
+ * (trace_kernel :5070-5103, score_detectors_kernel :4396-4411). air_* are NaN
+ * unless status == 1, as in the reference's NaN-initialised outputs (:7635). */
+typedef struct clr_ray_record {
+    int32_t status, interaction_count, geometric, wave, coherent, morphology;
+    int32_t particle_reflections, entry_reflections, internal_reflections, absorptions;
+    int32_t cell_inner_reflections, cell_outer_reflections, cell_tir;
+    int32_t top_reflections, top_tir, bottom_inner_reflections, bottom_outer_reflections, bottom_tir;
+    int32_t source_bore_interactions, source_bore_reflections, entered_water;
+    int32_t failure_code, failure_subcode;
+    int32_t native_id, mirror_id, native_bounces, mirror_bounces;
+    float air_x, air_y, air_z, air_vx, air_vy, air_vz;
+    float water_path, acrylic_path;
+} clr_ray_record;
+
+/* indices into clr_tallies.event_counts (sums of per-ray counters over the run) */
+enum {
+    CLR_EV_INTERACTIONS = 0, CLR_EV_GEOMETRIC, CLR_EV_WAVE, CLR_EV_COHERENT, CLR_EV_MORPHOLOGY,
+    CLR_EV_PARTICLE_REFLECTIONS, CLR_EV_ENTRY_REFLECTIONS, CLR_EV_INTERNAL_REFLECTIONS, CLR_EV_ABSORPTIONS,
+    CLR_EV_CELL_INNER, CLR_EV_CELL_OUTER, CLR_EV_CELL_TIR, CLR_EV_TOP, CLR_EV_TOP_TIR,
+    CLR_EV_BOTTOM_INNER, CLR_EV_BOTTOM_OUTER, CLR_EV_BOTTOM_TIR,
+    CLR_EV_SOURCE_BORE_INTERACTIONS, CLR_EV_SOURCE_BORE_REFLECTIONS, CLR_EV_ENTERED_WATER,
+    CLR_EV_WATER_STEPS,       /* free-flight steps in water (the unit of the roofline work count) */
+    CLR_EV_NULL_COLLISIONS,   /* Woodcock rejections and inaccessible-placement nulls */
+    CLR_EV_ROULETTE_KILLS,
+    CLR_EV_RESERVED
+};
+
+/* Detector tallies of one run. Integer counts are exact; float sums are FP64. */
+typedef struct clr_tallies {
+    int64_t n_rays;
+    int64_t hw_native[CLR_N_DETECTORS], hw_mirror[CLR_N_DETECTORS];
+    int64_t hw_native_direct[CLR_N_DETECTORS], hw_mirror_direct[CLR_N_DETECTORS];
+    int64_t hw_native_stray[CLR_N_DETECTORS], hw_mirror_stray[CLR_N_DETECTORS];
+    int64_t hw_native_face[CLR_N_DETECTORS], hw_mirror_face[CLR_N_DETECTORS];
+    int64_t legacy_native[CLR_N_DETECTORS], legacy_mirror[CLR_N_DETECTORS];
+    double photodiode_native[CLR_N_DETECTORS], photodiode_mirror[CLR_N_DETECTORS];
+    double incidence_native_sum[CLR_N_DETECTORS], incidence_mirror_sum[CLR_N_DETECTORS];
+    double weight_native[CLR_N_DETECTORS], weight_mirror[CLR_N_DETECTORS];
+    double weight_sq_native[CLR_N_DETECTORS], weight_sq_mirror[CLR_N_DETECTORS];
+    int64_t status_counts[CLR_N_STATUS];
+    int64_t failure_code_counts[CLR_N_FAILURE_CODES];
+    int64_t event_counts[CLR_N_EVENT_COUNTERS];
+    uint64_t conditional_stats[CLR_N_CONDITIONAL_STATS];
+    int32_t device_error;           /* nonzero if a bounded device wait gave up */
+    int32_t reserved[7];
+} clr_tallies;
+
+/* Host copies of the particle-physics tables (diagnostics and parity checks).
+ * Arrays are caller-owned; any pointer may be NULL to skip that output. */
+typedef struct clr_particle_physics {
+    double* size_parameter; double* qext; double* qsca; double* qabs; double* qback;
+    double* asym_g; double* albedo; int32_t* nstop;
+    double* radius; double* number_density;
+    double* mu_geom_bin; double* mu_sca_bin; double* mu_ext_bin; double* mu_wave_bin; double* mu_event_bin;
+    double* trace_geom_bin; double* trace_wave_bin;
+    double* geometric_cdf; double* wave_cdf; double* particle_event_cdf;
+    double* mu_scalars;            /* [8], transport_precompute_kernel :3908-3920 */
+    double* sed_majorants;         /* [4] */
+    double* theta;                 /* [n_theta] */
+    double* phase_cdf;             /* [n_bins * n_theta] */
+} clr_particle_physics;
+
+typedef struct clr_ctx clr_ctx;
+
+/* Context lifetime. Replaces ClaritasForwardModel.__init__'s RawModule build
+ * (CLARITAS/CLARITAS.py:6000-6033); kernels are compiled ahead of time. */
+int clr_create(clr_ctx** out, int device);
+int clr_destroy(clr_ctx* ctx);
+const char* clr_last_error(const clr_ctx* ctx);
+const char* clr_version(void);
+
+/* Store the scene parameters (the scalar half of the trace_kernel/score_detectors_kernel
+ * argument lists, CLARITAS/CLARITAS.py:4551-4560 and :4378-4384). */
+int clr_set_scene(clr_ctx* ctx, const clr_scene_params* scene);
+
+/* Run the whole particle-physics precompute on the device and keep its tables resident:
+ * replaces _prepare_gpu_particle_physics (CLARITAS/CLARITAS.py:6036-6965). */
+int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* particles, const clr_sediment_spec* sediment);
+
+/* Copy the resident tables back (CLARITAS/CLARITAS.py:6774, phase_table_diagnostics :7146). */
+int clr_read_particle_physics(clr_ctx* ctx, clr_particle_physics* out);
+
+/* Trace n_rays photons and score them: replaces one simulate() chunk loop
+ * (CLARITAS/CLARITAS.py:7614-7864). `records` is a DEVICE pointer to n_rays
+ * clr_ray_record entries, or NULL for the tally-only hot path. */
+int clr_trace(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* records);
+
+/* Same as clr_trace with HOST-resident record memory (copied back inside the call). */
+int clr_trace_host_records(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* host_records);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CLARITAS_GB_H */

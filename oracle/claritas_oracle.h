@@ -1,0 +1,37 @@
+/* CPU oracle API (test infrastructure only).
+ *
+ * A plain-C restatement of the reference's photon-transport hot path: the
+ * particle-physics precompute of ClaritasForwardModel._prepare_gpu_particle_physics
+ * (CLARITAS/CLARITAS.py:6036-6965), trace_kernel (:4551-5104) and
+ * score_detectors_kernel (:4378-4436), evaluated ray by ray on the host.
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it,
+ * always as the checker. The product library never links it.
+ */
+#ifndef CLARITAS_ORACLE_H
+#define CLARITAS_ORACLE_H
+
+#include "claritas_gb.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct clo_state clo_state;
+
+int clo_prepare(const clr_scene_params* scene, const clr_particle_spec* particles, const clr_sediment_spec* sediment,
+                clo_state** out);
+int clo_read_physics(clo_state* st, clr_particle_physics* out);
+int clo_n_theta(clo_state* st);
+int clo_trace(clo_state* st, const clr_run_params* run, clr_tallies* out, clr_ray_record* records, int n_threads);
+const char* clo_last_error(clo_state* st);
+void clo_free(clo_state* st);
+
+/* unit entry points used by the oracle's own tests */
+double clo_erfinv(double y);
+int clo_philox4x32_10(const uint32_t key[2], const uint32_t ctr[4], uint32_t out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,188 @@
+"""ctypes mirror of include/claritas_gb.h (the library's C ABI).
+
+Every Structure here has the same field order and C types as its C counterpart;
+tests/test_abi.py checks the sizes against the compiled library's own
+``clr_abi_sizeof`` export.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+N_DETECTORS = 18
+MAX_BINS = 64
+MIE_MAX_ORDER = 4096
+N_STATUS = 16
+N_FAILURE_CODES = 32
+N_EVENT_COUNTERS = 24
+N_CONDITIONAL_STATS = 10
+
+CLR_OK = 0
+CLR_ERR_INVALID_ARGUMENT = -1
+CLR_ERR_CUDA = -2
+CLR_ERR_NOT_READY = -3
+CLR_ERR_UNSUPPORTED = -4
+CLR_ERR_PRECOMPUTE = -5
+CLR_ERR_DEVICE_TIMEOUT = -6
+
+RNG_REFERENCE_XORSHIFT = 0
+RNG_PHILOX = 1
+WEIGHT_ANALOG = 0
+WEIGHT_IMPLICIT = 1
+SOURCE_REFERENCE_LED = 0
+SOURCE_COLLIMATED_DISC = 1
+
+EV_NAMES = [
+    "interactions", "geometric", "wave", "coherent", "morphology",
+    "particle_reflections", "entry_reflections", "internal_reflections", "absorptions",
+    "cell_inner", "cell_outer", "cell_tir", "top", "top_tir",
+    "bottom_inner", "bottom_outer", "bottom_tir",
+    "source_bore_interactions", "source_bore_reflections", "entered_water",
+    "water_steps", "null_collisions", "roulette_kills", "reserved",
+]
+
+f32, f64, i32, u32, i64, u64 = C.c_float, C.c_double, C.c_int32, C.c_uint32, C.c_int64, C.c_uint64
+PD = C.POINTER(C.c_double)
+PI32 = C.POINTER(C.c_int32)
+PU8 = C.POINTER(C.c_uint8)
+
+
+class SceneParams(C.Structure):
+    _fields_ = [
+        ("n_water", f32), ("n_acrylic", f32), ("n_air", f32), ("bore_n", f32), ("ring_face_n", f32),
+        ("bottom_external_n", f32),
+        ("rin", f32), ("rout", f32), ("zmin", f32), ("zmean", f32), ("zwall_top", f32),
+        ("bottom_disc_thickness", f32),
+        ("ring_in", f32), ("throat_out", f32), ("ring_out", f32), ("source_r", f32), ("throat_r", f32),
+        ("counterbore_r", f32),
+        ("beam_sigma", f32), ("alpha1", f32), ("alpha2", f32), ("legacy_accept_deg", f32),
+        ("source_angular_model", i32), ("source_bore_model", i32), ("detector_bore_model", i32),
+        ("ring_face_model", i32), ("photodiode_model", i32),
+        ("max_bore_bounces", i32), ("max_ring_face_bounces", i32),
+        ("free_surface_model", i32), ("vortex_delta_h", f32), ("vortex_core_radius", f32),
+        ("wavelength", f32), ("rough_alpha", f32), ("spheroid_aspect", f32), ("orientation_kappa", f32),
+        ("orientation_model", i32), ("max_particle_bounces", i32), ("max_cell_bounces", i32),
+        ("max_axial_bounces", i32),
+        ("max_iterations", f32),
+        ("event_model", i32), ("conditional_retries", i32), ("sediment_model", i32),
+        ("source_kind", i32), ("disc_radius", f32), ("disc_height", f32),
+        ("reserved", i32 * 4),
+    ]
+
+
+class ParticleSpec(C.Structure):
+    _fields_ = [
+        ("n_bins", i32), ("n_theta", i32), ("weight_mode", i32), ("moment_enabled", i32),
+        ("diameter_m", PD), ("weight", PD), ("n_real", PD), ("k_imag", PD),
+        ("moment_a", PD), ("moment_b", PD), ("moment_mode", PU8),
+        ("concentration_kg_m3", f64), ("density_kg_m3", f64), ("n_medium", f64), ("wavelength_m", f64),
+        ("wave_rms_height_m", f64), ("hybrid_wave_scale", f64),
+    ]
+
+
+class SedimentSpec(C.Structure):
+    _fields_ = [
+        ("particle_density", f64), ("water_density", f64), ("water_viscosity", f64), ("gravity", f64),
+        ("eddy_diffusivity", f64),
+        ("n_quad", i32), ("n_radial", i32), ("grid_nr", i32), ("grid_nz", i32),
+        ("grid", PD), ("grid_zmax", f64),
+    ]
+
+
+class RunParams(C.Structure):
+    _fields_ = [
+        ("n_rays", i64), ("ray_offset", u32), ("seed0", u32), ("seed1", u32), ("seed2", u32),
+        ("detector_seed", u32), ("rng_mode", i32), ("philox_key", u64), ("scenario_id", u32),
+        ("weight_mode", i32), ("roulette_threshold", f32), ("roulette_survival", f32),
+        ("block_threads", i32), ("rays_per_item", i32), ("reserved", i32 * 4),
+    ]
+
+
+class RayRecord(C.Structure):
+    _fields_ = [(n, i32) for n in (
+        "status", "interaction_count", "geometric", "wave", "coherent", "morphology",
+        "particle_reflections", "entry_reflections", "internal_reflections", "absorptions",
+        "cell_inner_reflections", "cell_outer_reflections", "cell_tir",
+        "top_reflections", "top_tir", "bottom_inner_reflections", "bottom_outer_reflections", "bottom_tir",
+        "source_bore_interactions", "source_bore_reflections", "entered_water",
+        "failure_code", "failure_subcode", "native_id", "mirror_id", "native_bounces", "mirror_bounces",
+    )] + [(n, f32) for n in ("air_x", "air_y", "air_z", "air_vx", "air_vy", "air_vz", "water_path",
+                            "acrylic_path")]
+
+
+RECORD_INT_FIELDS = [n for n, t in RayRecord._fields_ if t is i32]
+RECORD_FLOAT_FIELDS = [n for n, t in RayRecord._fields_ if t is f32]
+
+
+class Tallies(C.Structure):
+    _fields_ = [
+        ("n_rays", i64),
+        ("hw_native", i64 * N_DETECTORS), ("hw_mirror", i64 * N_DETECTORS),
+        ("hw_native_direct", i64 * N_DETECTORS), ("hw_mirror_direct", i64 * N_DETECTORS),
+        ("hw_native_stray", i64 * N_DETECTORS), ("hw_mirror_stray", i64 * N_DETECTORS),
+        ("hw_native_face", i64 * N_DETECTORS), ("hw_mirror_face", i64 * N_DETECTORS),
+        ("legacy_native", i64 * N_DETECTORS), ("legacy_mirror", i64 * N_DETECTORS),
+        ("photodiode_native", f64 * N_DETECTORS), ("photodiode_mirror", f64 * N_DETECTORS),
+        ("incidence_native_sum", f64 * N_DETECTORS), ("incidence_mirror_sum", f64 * N_DETECTORS),
+        ("weight_native", f64 * N_DETECTORS), ("weight_mirror", f64 * N_DETECTORS),
+        ("weight_sq_native", f64 * N_DETECTORS), ("weight_sq_mirror", f64 * N_DETECTORS),
+        ("status_counts", i64 * N_STATUS),
+        ("failure_code_counts", i64 * N_FAILURE_CODES),
+        ("event_counts", i64 * N_EVENT_COUNTERS),
+        ("conditional_stats", u64 * N_CONDITIONAL_STATS),
+        ("device_error", i32), ("reserved", i32 * 7),
+    ]
+
+    def as_dict(self) -> dict:
+        import numpy as np
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            if hasattr(v, "_length_"):
+                out[name] = np.ctypeslib.as_array(v).copy()
+            else:
+                out[name] = v
+        return out
+
+
+class ParticlePhysics(C.Structure):
+    _fields_ = [(n, PD) for n in (
+        "size_parameter", "qext", "qsca", "qabs", "qback", "asym_g", "albedo")] + [("nstop", PI32)] + [
+        (n, PD) for n in (
+            "radius", "number_density", "mu_geom_bin", "mu_sca_bin", "mu_ext_bin", "mu_wave_bin", "mu_event_bin",
+            "trace_geom_bin", "trace_wave_bin", "geometric_cdf", "wave_cdf", "particle_event_cdf",
+            "mu_scalars", "sed_majorants", "theta", "phase_cdf")]
+
+
+PHYSICS_BIN_FIELDS = [
+    "size_parameter", "qext", "qsca", "qabs", "qback", "asym_g", "albedo", "radius", "number_density",
+    "mu_geom_bin", "mu_sca_bin", "mu_ext_bin", "mu_wave_bin", "mu_event_bin", "trace_geom_bin",
+    "trace_wave_bin", "geometric_cdf", "wave_cdf", "particle_event_cdf",
+]
+
+
+def alloc_physics(n_bins: int, n_theta: int):
+    """Allocate numpy outputs for clr_read_particle_physics and a struct pointing at them."""
+    import numpy as np
+    arrays = {k: np.zeros(n_bins, dtype=np.float64) for k in PHYSICS_BIN_FIELDS}
+    arrays["nstop"] = np.zeros(n_bins, dtype=np.int32)
+    arrays["mu_scalars"] = np.zeros(8, dtype=np.float64)
+    arrays["sed_majorants"] = np.zeros(4, dtype=np.float64)
+    arrays["theta"] = np.zeros(n_theta, dtype=np.float64)
+    arrays["phase_cdf"] = np.zeros(n_bins * n_theta, dtype=np.float64)
+    pp = ParticlePhysics()
+    for k, a in arrays.items():
+        setattr(pp, k, a.ctypes.data_as(PI32 if k == "nstop" else PD))
+    return pp, arrays
+
+
+def records_to_numpy(buf, n: int):
+    """View a RayRecord buffer (ctypes array or bytes-like) as a structured numpy array."""
+    import numpy as np
+    dt = np.dtype([(nm, np.int32) for nm in RECORD_INT_FIELDS] + [(nm, np.float32) for nm in RECORD_FLOAT_FIELDS])
+    assert dt.itemsize == C.sizeof(RayRecord)
+    return np.frombuffer(buf, dtype=dt, count=n)
+
+
+def record_dtype():
+    import numpy as np
+    return np.dtype([(nm, np.int32) for nm in RECORD_INT_FIELDS] + [(nm, np.float32) for nm in RECORD_FLOAT_FIELDS])
