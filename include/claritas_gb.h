@@ -151,7 +151,7 @@ typedef struct clr_run_params {
     int32_t weight_mode;            /* CLR_WEIGHT_* */
     float roulette_threshold;       /* CLR_WEIGHT_IMPLICIT only */
     float roulette_survival;        /* weight given to survivors; probability = w / survival */
-    int32_t block_threads;          /* 0 = autotuned default */
+    int32_t max_blocks;             /* 0 = occupancy-derived grid; >0 caps the resident blocks (tuning, tests) */
     int32_t rays_per_item;          /* work-queue granularity; 0 = default */
     int32_t reserved[4];
 } clr_run_params;
@@ -247,6 +247,11 @@ int clr_trace(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray
 
 /* Same as clr_trace with HOST-resident record memory (copied back inside the call). */
 int clr_trace_host_records(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* host_records);
+
+/* Sizes of the ABI structs as compiled into the library (0 scene, 1 particle spec, 2 sediment spec,
+ * 3 run params, 4 ray record, 5 tallies, 6 particle physics); -1 for an unknown index.
+ * No reference counterpart: lets a binding check its struct mirror against the library. */
+int64_t clr_abi_sizeof(int which);
 
 #ifdef __cplusplus
 }

@@ -93,7 +93,7 @@ class RunParams(C.Structure):
         ("n_rays", i64), ("ray_offset", u32), ("seed0", u32), ("seed1", u32), ("seed2", u32),
         ("detector_seed", u32), ("rng_mode", i32), ("philox_key", u64), ("scenario_id", u32),
         ("weight_mode", i32), ("roulette_threshold", f32), ("roulette_survival", f32),
-        ("block_threads", i32), ("rays_per_item", i32), ("reserved", i32 * 4),
+        ("max_blocks", i32), ("rays_per_item", i32), ("reserved", i32 * 4),
     ]
 
 

@@ -1,0 +1,353 @@
+// C ABI of libclaritas_gb.so (declared in include/claritas_gb.h).
+//
+// A context owns one CUDA stream, the resident particle tables of the current
+// scene, and the small per-run buffers (work counter, device tallies). All
+// entry points return 0 or a negative CLR_ERR_* code; clr_last_error() gives
+// the message. Configuration errors that the reference raises as ValueError in
+// its constructor are rejected by the Python layer before reaching here; the
+// checks below guard the ABI itself.
+#include <cstdio>
+#include <cstring>
+#include <cstdarg>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include <cuda_runtime.h>
+#include "claritas_gb.h"
+#include "kernels.h"
+
+using namespace clr;
+
+struct clr_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    bool scene_set = false, built = false;
+    clr_scene_params sp{};
+    ParticleBuffers pb{};
+    std::vector<void*> allocs;
+    // per-run device buffers (single scenario)
+    DevScene* d_scene = nullptr;
+    long long* d_chunk_begin = nullptr;
+    DevTally* d_tally = nullptr;
+    unsigned long long* d_work = nullptr;
+    int num_sms = 0;
+};
+
+static int fail(clr_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+#define CU(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return fail(ctx, CLR_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+static cudaError_t dalloc(clr_ctx* ctx, void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e == cudaSuccess) ctx->allocs.push_back(*p);
+    return e;
+}
+static void free_particles(clr_ctx* ctx) {
+    for (void* p : ctx->allocs) cudaFree(p);
+    ctx->allocs.clear();
+    ctx->pb = ParticleBuffers{};
+    ctx->built = false;
+}
+
+extern "C" {
+
+const char* clr_version(void) { return "claritas_gb 0.1 (sm_103a)"; }
+
+const char* clr_last_error(const clr_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int clr_create(clr_ctx** out, int device) {
+    if (!out) return CLR_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n <= device || device < 0) return CLR_ERR_CUDA;
+    clr_ctx* ctx = new clr_ctx();
+    ctx->device = device;
+    CU(cudaSetDevice(device));
+    CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    CU(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+    CU(cudaMalloc(&ctx->d_scene, sizeof(DevScene)));
+    CU(cudaMalloc(&ctx->d_chunk_begin, 2 * sizeof(long long)));
+    CU(cudaMalloc(&ctx->d_tally, sizeof(DevTally)));
+    CU(cudaMalloc(&ctx->d_work, sizeof(unsigned long long)));
+    *out = ctx;
+    return CLR_OK;
+}
+
+int clr_destroy(clr_ctx* ctx) {
+    if (!ctx) return CLR_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_particles(ctx);
+    cudaFree(ctx->d_scene);
+    cudaFree(ctx->d_chunk_begin);
+    cudaFree(ctx->d_tally);
+    cudaFree(ctx->d_work);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return CLR_OK;
+}
+
+int clr_set_scene(clr_ctx* ctx, const clr_scene_params* scene) {
+    if (!ctx || !scene) return CLR_ERR_INVALID_ARGUMENT;
+    const clr_scene_params& s = *scene;
+    if (!(0 < s.rin && s.rin < s.rout && s.rout < s.ring_in && s.ring_in < s.throat_out &&
+          s.throat_out <= s.source_r && s.source_r <= s.ring_out))
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "TARDIIS radial/source geometry is inconsistent");
+    if (!(s.zwall_top > s.zmean && s.zmean > s.zmin))
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "wall top must lie above the water domain");
+    if (s.free_surface_model < 0 || s.free_surface_model > 2 || s.sediment_model < 0 || s.sediment_model > 3 ||
+        s.event_model < 0 || s.event_model > 5)
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "model code out of range");
+    if (s.source_kind != CLR_SOURCE_REFERENCE_LED && s.source_kind != CLR_SOURCE_COLLIMATED_DISC)
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "unknown source_kind %d", s.source_kind);
+    ctx->sp = s;
+    ctx->scene_set = true;
+    ctx->built = false;
+    return CLR_OK;
+}
+
+int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sediment_spec* ss) {
+    if (!ctx || !ps || !ss) return CLR_ERR_INVALID_ARGUMENT;
+    if (!ctx->scene_set) return fail(ctx, CLR_ERR_NOT_READY, "clr_set_scene must be called first");
+    const int n = ps->n_bins;
+    if (n < 1 || n > CLR_MAX_BINS) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "n_bins must be 1..%d", CLR_MAX_BINS);
+    const clr_scene_params& sp = ctx->sp;
+    const bool hybrid = sp.event_model == 3 || sp.event_model == 4 || sp.event_model == 5;
+    const int nt = hybrid ? ps->n_theta : 2;
+    if (hybrid && nt < 257) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "n_theta must be >= 257");
+    if (!ps->diameter_m || !ps->weight || !ps->n_real || !ps->k_imag)
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "particle arrays must not be null");
+    if (ss->n_radial < 65 || ss->n_quad < 64) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "sediment lookup sizes too small");
+    // sediment precompute argument checks (error codes 31-33 of the reference kernel, :3958-3967)
+    if (sp.sediment_model != 0) {
+        if (!(ss->particle_density > ss->water_density) || !(ss->water_density > 0.0) || !(ss->water_viscosity > 0.0) ||
+            !(ss->gravity > 0.0) || !(ss->eddy_diffusivity > 0.0) || !(sp.rin > 0.0f))
+            return fail(ctx, CLR_ERR_PRECOMPUTE, "sediment transport precompute failed with error code 31");
+        if ((sp.vortex_delta_h > 0.0f && sp.free_surface_model == 0) ||
+            (sp.free_surface_model == 2 && !(sp.vortex_core_radius > 0.0f)))
+            return fail(ctx, CLR_ERR_PRECOMPUTE, "sediment transport precompute failed with error code 32");
+        if (!((double)sp.zmean - (double)sp.zmin > 0.0))
+            return fail(ctx, CLR_ERR_PRECOMPUTE, "sediment transport precompute failed with error code 33");
+        if (sp.sediment_model == 3 && (!ss->grid || ss->grid_nr < 2 || ss->grid_nz < 2))
+            return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "sediment model 3 needs a [bins][nr][nz] grid");
+    }
+    CU(cudaSetDevice(ctx->device));
+    free_particles(ctx);
+    ParticleBuffers& pb = ctx->pb;
+    pb.n = n; pb.nt = nt; pb.n_radial = ss->n_radial;
+    pb.grid_nr = sp.sediment_model == 3 ? ss->grid_nr : 2;
+    pb.grid_nz = sp.sediment_model == 3 ? ss->grid_nz : 2;
+    pb.grid_zmax = ss->grid_zmax;
+    auto D = [&](double** p, size_t cnt) { return dalloc(ctx, (void**)p, cnt * sizeof(double)); };
+    auto F = [&](float** p, size_t cnt) { return dalloc(ctx, (void**)p, cnt * sizeof(float)); };
+    double** darr[] = {&pb.d, &pb.w, &pb.nidx, &pb.kidx, &pb.x, &pb.qext, &pb.qsca, &pb.qabs, &pb.qback, &pb.g,
+                       &pb.albedo, &pb.radius, &pb.nden, &pb.mug, &pb.mus, &pb.mue, &pb.muw, &pb.muev, &pb.gcdf,
+                       &pb.wcdf, &pb.pcdf, &pb.moment_a, &pb.moment_b, &pb.trace_geom, &pb.trace_wave, &pb.sedA,
+                       &pb.sedB, &pb.sed_norm, &pb.sed_max};
+    for (double** p : darr) CU(D(p, n));
+    float** farr[] = {&pb.gcdf_f, &pb.wcdf_f, &pb.pn_f, &pb.pk_f, &pb.prad_f};
+    for (float** p : farr) CU(F(p, n));
+    CU(dalloc(ctx, (void**)&pb.nstop, n * sizeof(int)));
+    CU(dalloc(ctx, (void**)&pb.moment_mode, n));
+    CU(dalloc(ctx, (void**)&pb.err, sizeof(int)));
+    CU(D(&pb.ab, (size_t)n * CLR_MIE_MAX_ORDER * 4));
+    CU(D(&pb.theta, nt));
+    CU(F(&pb.theta_f, nt));
+    CU(D(&pb.pdf, (size_t)n * nt));
+    CU(D(&pb.phase_cdf, (size_t)n * nt));
+    CU(F(&pb.phase_cdf_f, (size_t)n * nt));
+    CU(D(&pb.muscal, 8));
+    CU(D(&pb.sed_major, 4));
+    CU(D(&pb.sed_radial_log, (size_t)n * ss->n_radial));
+    CU(D(&pb.sed_wr, (size_t)n * ss->n_radial));
+    const size_t grid_cells = (size_t)pb.grid_nr * pb.grid_nz * (sp.sediment_model == 3 ? n : 1);
+    CU(D(&pb.sed_grid, grid_cells));
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemcpyAsync(pb.d, ps->diameter_m, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(pb.w, ps->weight, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(pb.nidx, ps->n_real, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(pb.kidx, ps->k_imag, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    std::vector<double> ma(n, 1.0), mb(n, 0.0);
+    std::vector<uint8_t> mm(n, 0);
+    pb.any_moment = 0;
+    if (ps->moment_enabled && ps->moment_a && ps->moment_b && ps->moment_mode) {
+        for (int i = 0; i < n; ++i) {
+            ma[i] = ps->moment_a[i]; mb[i] = ps->moment_b[i]; mm[i] = ps->moment_mode[i];
+            pb.any_moment |= mm[i] ? 1 : 0;
+        }
+    }
+    CU(cudaMemcpyAsync(pb.moment_a, ma.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(pb.moment_b, mb.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(pb.moment_mode, mm.data(), n, cudaMemcpyHostToDevice, st));
+    if (sp.sediment_model == 3) {
+        CU(cudaMemcpyAsync(pb.sed_grid, ss->grid, grid_cells * sizeof(double), cudaMemcpyHostToDevice, st));
+    } else {
+        const double one[4] = {1.0, 1.0, 1.0, 1.0};
+        CU(cudaMemcpyAsync(pb.sed_grid, one, sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    CU(enqueue_particle_precompute(pb, sp, *ps, *ss, nullptr, st));
+    int herr = 0;
+    CU(cudaMemcpyAsync(&herr, pb.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (herr) return fail(ctx, CLR_ERR_PRECOMPUTE, "particle precompute failed with error code %d", herr);
+    ctx->built = true;
+    return CLR_OK;
+}
+
+int clr_read_particle_physics(clr_ctx* ctx, clr_particle_physics* o) {
+    if (!ctx || !o) return CLR_ERR_INVALID_ARGUMENT;
+    if (!ctx->built) return fail(ctx, CLR_ERR_NOT_READY, "particles not built");
+    const ParticleBuffers& pb = ctx->pb;
+    const int n = pb.n;
+    CU(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    struct Pair { double* dst; const double* src; size_t cnt; };
+    Pair pairs[] = {{o->size_parameter, pb.x, (size_t)n}, {o->qext, pb.qext, (size_t)n}, {o->qsca, pb.qsca, (size_t)n},
+                    {o->qabs, pb.qabs, (size_t)n}, {o->qback, pb.qback, (size_t)n}, {o->asym_g, pb.g, (size_t)n},
+                    {o->albedo, pb.albedo, (size_t)n}, {o->radius, pb.radius, (size_t)n},
+                    {o->number_density, pb.nden, (size_t)n}, {o->mu_geom_bin, pb.mug, (size_t)n},
+                    {o->mu_sca_bin, pb.mus, (size_t)n}, {o->mu_ext_bin, pb.mue, (size_t)n},
+                    {o->mu_wave_bin, pb.muw, (size_t)n}, {o->mu_event_bin, pb.muev, (size_t)n},
+                    {o->trace_geom_bin, pb.trace_geom, (size_t)n}, {o->trace_wave_bin, pb.trace_wave, (size_t)n},
+                    {o->geometric_cdf, pb.gcdf, (size_t)n}, {o->wave_cdf, pb.wcdf, (size_t)n},
+                    {o->particle_event_cdf, pb.pcdf, (size_t)n}, {o->mu_scalars, pb.muscal, 8},
+                    {o->sed_majorants, pb.sed_major, 4}, {o->theta, pb.theta, (size_t)pb.nt},
+                    {o->phase_cdf, pb.phase_cdf, (size_t)n * pb.nt}};
+    for (const Pair& p : pairs)
+        if (p.dst) CU(cudaMemcpyAsync(p.dst, p.src, p.cnt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (o->nstop) CU(cudaMemcpyAsync(o->nstop, pb.nstop, n * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return CLR_OK;
+}
+
+}  // extern "C"
+
+// Fill the device scene description for the current tables and a run.
+static void fill_scene(const clr_ctx* ctx, const clr_run_params* run, DevScene* s) {
+    const ParticleBuffers& pb = ctx->pb;
+    memset(s, 0, sizeof *s);
+    s->P = ctx->sp;
+    s->gcdf = pb.gcdf_f; s->wcdf = pb.wcdf_f; s->phase_cdf = pb.phase_cdf_f; s->theta = pb.theta_f;
+    s->pn = pb.pn_f; s->pk = pb.pk_f; s->prad = pb.prad_f;
+    s->k = pb.kidx; s->qsca = pb.qsca; s->qext = pb.qext;
+    s->moment_a = pb.moment_a; s->moment_b = pb.moment_b; s->moment_mode = pb.moment_mode;
+    s->trace_geom = pb.trace_geom; s->trace_wave = pb.trace_wave;
+    s->sedA = pb.sedA; s->sedB = pb.sedB; s->sed_norm = pb.sed_norm; s->sed_radial_log = pb.sed_radial_log;
+    s->sed_grid = pb.sed_grid; s->mu_channels = pb.muscal; s->sed_major = pb.sed_major;
+    s->n_bins = pb.n; s->nt = pb.nt; s->n_radial = pb.n_radial; s->grid_nr = pb.grid_nr; s->grid_nz = pb.grid_nz;
+    s->any_moment = pb.any_moment; s->grid_zmax = (float)pb.grid_zmax;
+    s->seed0 = run->seed0; s->seed1 = run->seed1; s->seed2 = run->seed2; s->det_seed = run->detector_seed;
+    s->ray_offset = run->ray_offset; s->scenario_id = run->scenario_id; s->philox_key = run->philox_key;
+    s->n_rays = run->n_rays; s->weight_mode = run->weight_mode;
+    s->roulette_threshold = run->roulette_threshold; s->roulette_survival = run->roulette_survival;
+}
+
+static void tally_to_host(const DevTally& t, clr_tallies* out, int64_t n_rays) {
+    memset(out, 0, sizeof *out);
+    out->n_rays = n_rays;
+    for (int j = 0; j < CLR_N_DETECTORS; ++j) {
+        out->hw_native[j] = (int64_t)t.hw[0][j]; out->hw_mirror[j] = (int64_t)t.hw[1][j];
+        out->hw_native_direct[j] = (int64_t)t.hw[2][j]; out->hw_mirror_direct[j] = (int64_t)t.hw[3][j];
+        out->hw_native_stray[j] = (int64_t)t.hw[4][j]; out->hw_mirror_stray[j] = (int64_t)t.hw[5][j];
+        out->hw_native_face[j] = (int64_t)t.hw[6][j]; out->hw_mirror_face[j] = (int64_t)t.hw[7][j];
+        out->legacy_native[j] = (int64_t)t.hw[8][j]; out->legacy_mirror[j] = (int64_t)t.hw[9][j];
+        out->photodiode_native[j] = t.sums[0][j]; out->photodiode_mirror[j] = t.sums[1][j];
+        out->incidence_native_sum[j] = t.sums[2][j]; out->incidence_mirror_sum[j] = t.sums[3][j];
+        out->weight_native[j] = t.sums[4][j]; out->weight_mirror[j] = t.sums[5][j];
+        out->weight_sq_native[j] = t.sums[6][j]; out->weight_sq_mirror[j] = t.sums[7][j];
+    }
+    for (int k = 0; k < CLR_N_STATUS; ++k) out->status_counts[k] = (int64_t)t.status[k];
+    for (int k = 0; k < CLR_N_FAILURE_CODES; ++k) out->failure_code_counts[k] = (int64_t)t.failure[k];
+    for (int k = 0; k < CLR_N_EVENT_COUNTERS; ++k) out->event_counts[k] = (int64_t)t.events[k];
+    for (int k = 0; k < CLR_N_CONDITIONAL_STATS; ++k) out->conditional_stats[k] = t.cstats[k];
+    out->device_error = (t.n_done == (unsigned long long)n_rays) ? 0 : 1;
+}
+
+static int trace_impl(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* d_records) {
+    if (!ctx || !run || !out) return CLR_ERR_INVALID_ARGUMENT;
+    if (!ctx->built) return fail(ctx, CLR_ERR_NOT_READY, "clr_build_particles must succeed before clr_trace");
+    if (run->n_rays < 0 || (uint64_t)run->ray_offset + (uint64_t)run->n_rays > (1ull << 32))
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "ray range exceeds uint32 global ids");
+    if (run->rng_mode != CLR_RNG_REFERENCE_XORSHIFT && run->rng_mode != CLR_RNG_PHILOX)
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "unknown rng_mode %d", run->rng_mode);
+    if (run->weight_mode == CLR_WEIGHT_IMPLICIT && run->rng_mode != CLR_RNG_PHILOX)
+        return fail(ctx, CLR_ERR_UNSUPPORTED, "implicit-capture weighting runs on the Philox stream only");
+    CU(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    DevScene hs;
+    fill_scene(ctx, run, &hs);
+    const int chunk = run->rays_per_item > 0 ? run->rays_per_item : 256;
+    long long cb[2] = {0, (run->n_rays + chunk - 1) / chunk};
+    CU(cudaMemcpyAsync(ctx->d_scene, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->d_chunk_begin, cb, sizeof cb, cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(ctx->d_tally, 0, sizeof(DevTally), st));
+    CU(cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long), st));
+    LaunchArgs a;
+    a.scenes = ctx->d_scene; a.chunk_begin = ctx->d_chunk_begin; a.n_scen = 1; a.n_chunks = cb[1];
+    a.chunk_rays = chunk; a.work = ctx->d_work; a.tallies = ctx->d_tally; a.records = d_records;
+    a.stream = st; a.rng_mode = run->rng_mode; a.weighted = run->weight_mode == CLR_WEIGHT_IMPLICIT;
+    int occ = photon_kernel_occupancy(a.rng_mode, d_records != nullptr, a.weighted);
+    if (occ < 1) occ = 1;
+    long long want = (long long)ctx->num_sms * occ;
+    long long warps_needed = (cb[1] + 0);  // one chunk per warp is the finest useful split
+    long long blocks_needed = (warps_needed * 32 + CLR_TRACE_THREADS - 1) / CLR_TRACE_THREADS;
+    a.grid = (int)std::max(1LL, std::min(want, blocks_needed));
+    if (run->max_blocks > 0) a.grid = std::max(1, std::min(a.grid, run->max_blocks));
+    if (cb[1] > 0) CU(launch_photon_kernel(a));
+    DevTally ht;
+    CU(cudaMemcpyAsync(&ht, ctx->d_tally, sizeof ht, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    tally_to_host(ht, out, run->n_rays);
+    return CLR_OK;
+}
+
+extern "C" {
+
+int clr_trace(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* records) {
+    return trace_impl(ctx, run, out, records);
+}
+
+int clr_trace_host_records(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* host_records) {
+    if (!ctx || !run || !out) return CLR_ERR_INVALID_ARGUMENT;
+    if (!host_records) return trace_impl(ctx, run, out, nullptr);
+    CU(cudaSetDevice(ctx->device));
+    clr_ray_record* d = nullptr;
+    const size_t bytes = (size_t)run->n_rays * sizeof(clr_ray_record);
+    CU(cudaMalloc(&d, bytes ? bytes : 16));
+    int rc = trace_impl(ctx, run, out, d);
+    if (rc == CLR_OK) {
+        cudaError_t e = cudaMemcpy(host_records, d, bytes, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) rc = fail(ctx, CLR_ERR_CUDA, "record copy: %s", cudaGetErrorString(e));
+    }
+    cudaFree(d);
+    return rc;
+}
+
+/* sizes of the ABI structs as compiled, for the Python mirror's self-check */
+int64_t clr_abi_sizeof(int which) {
+    switch (which) {
+        case 0: return (int64_t)sizeof(clr_scene_params);
+        case 1: return (int64_t)sizeof(clr_particle_spec);
+        case 2: return (int64_t)sizeof(clr_sediment_spec);
+        case 3: return (int64_t)sizeof(clr_run_params);
+        case 4: return (int64_t)sizeof(clr_ray_record);
+        case 5: return (int64_t)sizeof(clr_tallies);
+        case 6: return (int64_t)sizeof(clr_particle_physics);
+        default: return -1;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,59 @@
+// Device-resident description of one scenario: the scene scalars plus pointers
+// to its particle tables, as consumed by the photon kernel. Built by the
+// precompute path (precompute.cu) and uploaded once per scenario.
+#pragma once
+#include <cstdint>
+#include "claritas_gb.h"
+
+namespace clr {
+
+struct DevScene {
+    clr_scene_params P;
+    // particle tables (float copies are exact casts of the FP64 tables, which is what the
+    // reference compares against: CLARITAS/CLARITAS.py:2628, :2633-2637)
+    const float* gcdf;
+    const float* wcdf;
+    const float* phase_cdf;     // [n_bins][nt]
+    const float* theta;         // [nt]
+    const float* pn;            // (float)n_real
+    const float* pk;            // (float)k_imag
+    const float* prad;          // (float)radius
+    const double* k;            // k_imag
+    const double* qsca;
+    const double* qext;
+    const double* moment_a;
+    const double* moment_b;
+    const uint8_t* moment_mode;
+    const double* trace_geom;   // channel rates per bin (:6362-6375)
+    const double* trace_wave;
+    const double* sedA;
+    const double* sedB;
+    const double* sed_norm;
+    const double* sed_radial_log;
+    const double* sed_grid;
+    const double* mu_channels;  // [8] transport_precompute_kernel output
+    const double* sed_major;    // [4]
+    int32_t n_bins, nt, n_radial, grid_nr, grid_nz, any_moment;
+    float grid_zmax;
+    // run description of this scenario
+    uint32_t seed0, seed1, seed2, det_seed, ray_offset, scenario_id;
+    uint64_t philox_key;
+    int64_t n_rays;
+    int32_t weight_mode;
+    float roulette_threshold, roulette_survival;
+    int32_t pad;
+};
+
+// Per-scenario tallies in device memory (64-bit counters, FP64 sums).
+struct DevTally {
+    unsigned long long hw[10][CLR_N_DETECTORS];   // native, mirror, nat direct, mir direct, nat stray, mir stray,
+                                                  // nat face, mir face, legacy native, legacy mirror
+    double sums[8][CLR_N_DETECTORS];              // photodiode nat/mir, incidence nat/mir, weight nat/mir, w^2 nat/mir
+    unsigned long long status[CLR_N_STATUS];
+    unsigned long long failure[CLR_N_FAILURE_CODES];
+    unsigned long long events[CLR_N_EVENT_COUNTERS];
+    unsigned long long cstats[CLR_N_CONDITIONAL_STATS];
+    unsigned long long n_done;
+};
+
+}  // namespace clr

@@ -1,0 +1,65 @@
+// Internal launch interface between the C ABI (clr_api.cu) and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "device_scene.cuh"
+
+#define CLR_TRACE_THREADS 256
+
+namespace clr {
+
+struct LaunchArgs {
+    const DevScene* scenes;
+    const long long* chunk_begin;  // [n_scen + 1] first work chunk of each scenario
+    int n_scen;
+    long long n_chunks;
+    int chunk_rays;
+    unsigned long long* work;      // global chunk counter (zeroed before launch)
+    DevTally* tallies;             // [n_scen]
+    clr_ray_record* records;       // nullable; single-scenario parity runs only
+    int grid;
+    cudaStream_t stream;
+    int rng_mode;
+    bool weighted;
+};
+
+cudaError_t launch_xor(const LaunchArgs& a);
+cudaError_t launch_philox(const LaunchArgs& a);
+int occupancy_xor(bool records);
+int occupancy_philox(bool records);
+inline cudaError_t launch_photon_kernel(const LaunchArgs& a) {
+    return a.rng_mode == CLR_RNG_PHILOX ? launch_philox(a) : launch_xor(a);
+}
+inline int photon_kernel_occupancy(int rng_mode, bool records, bool /*weighted*/) {
+    return rng_mode == CLR_RNG_PHILOX ? occupancy_philox(records) : occupancy_xor(records);
+}
+
+// Device buffers of one scenario's particle physics (all FP64 unless named _f).
+struct ParticleBuffers {
+    int n = 0, nt = 0, n_radial = 0, grid_nr = 2, grid_nz = 2;
+    double grid_zmax = 0.0;
+    double *d = nullptr, *w = nullptr, *nidx = nullptr, *kidx = nullptr;
+    int* nstop = nullptr;
+    double *x = nullptr, *qext = nullptr, *qsca = nullptr, *qabs = nullptr, *qback = nullptr, *g = nullptr,
+           *albedo = nullptr;
+    double* ab = nullptr;  // Mie a_n, b_n scratch: [n][CLR_MIE_MAX_ORDER][4] (a.re, a.im, b.re, b.im)
+    double *theta = nullptr, *pdf = nullptr, *phase_cdf = nullptr;
+    float *theta_f = nullptr, *phase_cdf_f = nullptr;
+    double *radius = nullptr, *nden = nullptr, *mug = nullptr, *mus = nullptr, *mue = nullptr, *muw = nullptr,
+           *muev = nullptr, *gcdf = nullptr, *wcdf = nullptr, *pcdf = nullptr, *muscal = nullptr;
+    float *gcdf_f = nullptr, *wcdf_f = nullptr, *pn_f = nullptr, *pk_f = nullptr, *prad_f = nullptr;
+    double *moment_a = nullptr, *moment_b = nullptr;
+    uint8_t* moment_mode = nullptr;
+    int any_moment = 0;
+    double *trace_geom = nullptr, *trace_wave = nullptr;
+    double *sedA = nullptr, *sedB = nullptr, *sed_norm = nullptr, *sed_max = nullptr, *sed_radial_log = nullptr,
+           *sed_wr = nullptr, *sed_major = nullptr, *sed_grid = nullptr;
+    int* err = nullptr;
+};
+
+// Enqueue the whole precompute on `stream`. Host inputs are copied in; error codes land in pb.err.
+// `ab_scratch` may supply the Mie a_n/b_n scratch (n*CLR_MIE_MAX_ORDER*4 doubles); when null, pb.ab is used.
+cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,
+                                        const clr_sediment_spec& ss, double* ab_scratch, cudaStream_t stream);
+
+}  // namespace clr

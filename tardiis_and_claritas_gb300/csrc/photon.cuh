@@ -1,0 +1,547 @@
+// Photon history as a resumable state machine.
+//
+// The reference traces each ray start-to-finish in one thread (trace_kernel,
+// CLARITAS/CLARITAS.py:4551-5104) and scores it in a second kernel
+// (score_detectors_kernel :4378-4436). Here a history is split into
+// resumable steps -- the launch segment (source, collimator, acrylic entry,
+// :4650-4732) and one water free-flight step (one iteration of :4734-5066) --
+// so a persistent warp can hand a finished lane a fresh photon immediately.
+// Within each step the arithmetic, random-draw order and branch structure are
+// the reference's, so per-ray integer outcomes are reproduced exactly in the
+// xorshift parity mode.
+#pragma once
+#include "physics_b.cuh"
+#include "device_scene.cuh"
+
+namespace clr {
+namespace {  // header-only device code: internal linkage in every translation unit
+
+enum : int { PHASE_LAUNCH = 0, PHASE_WATER = 1 };
+
+struct Ray {
+    float x, y, z, vx, vy, vz, wp, ap, w;
+    int phase, step, st, pf, pfs;
+    int ic, gic, wic, wcoh, wmorph, cir, cor, ctir, tr, ttir, bir, bor, btir, sbi, sbr, entered;
+    o_pcount pc;
+    int steps, nulls;
+};
+
+// Small per-history counters that the reference keeps in registers; summed into tallies at the end.
+__device__ __forceinline__ void ray_reset(Ray& r) {
+    r.x = r.y = r.z = 0.f; r.vx = 0.f; r.vy = 1.f; r.vz = 0.f; r.wp = 0.f; r.ap = 0.f; r.w = 1.f;
+    r.phase = PHASE_LAUNCH; r.step = 0; r.st = 0; r.pf = 0; r.pfs = 0;
+    r.ic = r.gic = r.wic = r.wcoh = r.wmorph = 0;
+    r.cir = r.cor = r.ctir = r.tr = r.ttir = r.bir = r.bor = r.btir = r.sbi = r.sbr = r.entered = 0;
+    r.pc.reflections = r.pc.entry_reflections = r.pc.internal_reflections = r.pc.absorptions = 0;
+    r.steps = r.nulls = 0;
+}
+
+// per-warp shared tally region (64-bit counters; flushed to the owning scenario's DevTally)
+struct WarpTally {
+    unsigned long long hw[10][CLR_N_DETECTORS];
+    double sums[8][CLR_N_DETECTORS];
+    unsigned long long status[CLR_N_STATUS];
+    unsigned long long failure[CLR_N_FAILURE_CODES];
+    unsigned long long events[CLR_N_EVENT_COUNTERS];
+    unsigned long long cstats[CLR_N_CONDITIONAL_STATS];
+    unsigned long long n_done;
+};
+static_assert(sizeof(WarpTally) == sizeof(DevTally), "tally layouts must match");
+
+// offsets inside WarpTally/DevTally counter space (in units of unsigned long long after hw)
+#define CLR_OFF_HW(k, j) ((k) * CLR_N_DETECTORS + (j))
+#define CLR_OFF_STATUS (10 * CLR_N_DETECTORS + 8 * CLR_N_DETECTORS)
+#define CLR_OFF_FAIL (CLR_OFF_STATUS + CLR_N_STATUS)
+#define CLR_OFF_EV (CLR_OFF_FAIL + CLR_N_FAILURE_CODES)
+#define CLR_OFF_CS (CLR_OFF_EV + CLR_N_EVENT_COUNTERS)
+#define CLR_OFF_DONE (CLR_OFF_CS + CLR_N_CONDITIONAL_STATS)
+
+// ---------------- conditional closure (:4479-4536) ----------------
+struct Hist {
+    float x, y, z, vx, vy, vz, path;
+    o_pcount pc;
+    int status, channel, macro, micro, failure, subcode;
+};
+
+template <class S>
+__device__ __forceinline__ void conditional_body(
+    S* s, Hist* out, int pidx, double qs, double qe, float nm, float nr, float ki, float wl, float rough,
+    float radius, float aspect, int orientation, float kappa, int max_bounces, float coherent, const float* cdf,
+    const float* theta, int nt, float x, float y, float z, float vx, float vy, float vz, float rin, float zmin,
+    float zmean, int surface, float delta, float core, int max_trials, unsigned long long* stats) {
+    Hist h;
+    memset(&h, 0, sizeof h);
+    h.failure = OP_OTHER; h.subcode = 9002;
+    double tol = 1e-10 * fmax(1.0, fmax(fabs(qs), fabs(qe)));
+    if (max_trials == 0) { h.subcode = 9001; ++stats[9]; *out = h; return; }
+    if (!isfinite(qs) || !isfinite(qe) || qe <= 0.0 || qs < -tol || qs > qe + tol || max_trials < 1) { ++stats[8]; *out = h; return; }
+    double albedo = (ki == 0.0f && fabs(qe - qs) <= tol) ? 1.0 : fmin(fmax(qs / qe, 0.0), 1.0);
+    double pabs = (ki == 0.0f && fabs(qe - qs) <= tol) ? 0.0 : fmin(fmax((qe - qs) / qe, 0.0), 1.0);
+    const double MINP = 2.3283064365386962890625e-10;
+    if ((ki > 0.0f && (pabs <= 0.0 || albedo >= 1.0)) || (albedo > 0.0 && albedo < MINP) || (pabs > 0.0 && pabs < MINP)) {
+        h.subcode = 9003; ++stats[8]; *out = h; return;
+    }
+    int target_absorbed = (albedo < 1.0 && uniform53(s) >= albedo);
+    double wave = qs > 0.0 ? fmax(qs - 1.0, 0.0) / qs : 0.0;
+    for (int trial = 0; trial < max_trials; ++trial) {
+        ++stats[0];
+        memset(&h, 0, sizeof h);
+        h.x = x; h.y = y; h.z = z; h.vx = vx; h.vy = vy; h.vz = vz;
+        h.channel = (uniform53(s) < wave) ? ((coherent >= 1.0f || uniform53(s) < coherent) ? 1 : 2) : 0;
+        if (h.channel == 1) {
+            o_mie_direction(s, cdf, theta, nt, pidx, &h.vx, &h.vy, &h.vz);
+            h.status = 1;
+        } else if (h.channel == 2) {
+            float fr = sqrtf(x * x + y * y), fx = 1, fy = 0;
+            if (fr > 1e-12f) { fx = -y / fr; fy = x / fr; }
+            h.status = o_spheroid_event(s, nm, nr, ki, wl, rough, radius, aspect, orientation, kappa, fx, fy, 0,
+                                        max_bounces, &h.vx, &h.vy, &h.vz, &h.path, &h.pc, &h.failure, &h.subcode,
+                                        &h.macro, &h.micro);
+        } else {
+            float rho, phi, gx, gy, gz;
+            o_sphere_geometry(s, radius, x, y, z, vx, vy, vz, &rho, &phi, &gx, &gy, &gz);
+            double dcx = (double)x - (double)radius * gx, dcy = (double)y - (double)radius * gy,
+                   dcz = (double)z - (double)radius * gz;
+            if (!o_sphere_accessible(dcx, dcy, dcz, radius, rin, zmin, zmean, surface, delta, core)) { ++stats[2]; continue; }
+            h.status = o_sphere_sampled(s, nm, nr, ki, wl, rough, radius, max_bounces, gx, gy, gz, dcx, dcy, dcz, &h.x,
+                                        &h.y, &h.z, &h.vx, &h.vy, &h.vz, &h.path, &h.pc, &h.failure, &h.subcode,
+                                        &h.macro, &h.micro);
+        }
+        if (h.status != 1 && h.status != 2) { ++stats[8]; *out = h; return; }
+        if ((h.status == 2) != target_absorbed) { ++stats[1]; continue; }
+        ++stats[3 + h.channel];
+        ++stats[h.status == 2 ? 6 : 7];
+        *out = h;
+        return;
+    }
+    memset(&h, 0, sizeof h);
+    h.failure = OP_OTHER; h.subcode = 9001;
+    ++stats[9];
+    *out = h;
+}
+
+// The encounter's trial counters are thread-local and merged atomically once, as the
+// reference's conditional_particle_interaction_accumulate does (:4540-4549).
+template <class S>
+__device__ __noinline__ void conditional_interaction(
+    S* s, Hist* out, int pidx, double qs, double qe, float nm, float nr, float ki, float wl, float rough,
+    float radius, float aspect, int orientation, float kappa, int max_bounces, float coherent, const float* cdf,
+    const float* theta, int nt, float x, float y, float z, float vx, float vy, float vz, float rin, float zmin,
+    float zmean, int surface, float delta, float core, int max_trials, unsigned long long* gstats) {
+    unsigned long long stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    conditional_body(s, out, pidx, qs, qe, nm, nr, ki, wl, rough, radius, aspect, orientation, kappa, max_bounces,
+                     coherent, cdf, theta, nt, x, y, z, vx, vy, vz, rin, zmin, zmean, surface, delta, core, max_trials,
+                     stats);
+#pragma unroll
+    for (int i = 0; i < 10; ++i)
+        if (stats[i]) atomicAdd(gstats + i, stats[i]);
+}
+
+// Mie two-moment post-outcome angular map (:4459-4476)
+__device__ __noinline__ void moment_constraint(float vinx, float viny, float vinz, float* vx, float* vy, float* vz,
+                                               float A, float B) {
+    float c = fminf(fmaxf(o_dot(vinx, viny, vinz, *vx, *vy, *vz), -1.0f), 1.0f);
+    float d = fminf(fmaxf(1.0f - c, 0.0f), 2.0f);
+    float dm = fminf(fmaxf(A * d + B * d * d, 0.0f), 2.0f);
+    float cp = 1.0f - dm;
+    float px = *vx - c * vinx, py = *vy - c * viny, pz = *vz - c * vinz;
+    float pn = sqrtf(fmaxf(px * px + py * py + pz * pz, 0.0f));
+    if (pn > 1.0e-8f) { px /= pn; py /= pn; pz /= pn; }
+    else {
+        float e1x, e1y, e1z, e2x, e2y, e2z;
+        o_perp_basis(vinx, viny, vinz, &e1x, &e1y, &e1z, &e2x, &e2y, &e2z);
+        px = e1x; py = e1y; pz = e1z;
+    }
+    float sp = sqrtf(fmaxf(1.0f - cp * cp, 0.0f));
+    *vx = cp * vinx + sp * px; *vy = cp * viny + sp * py; *vz = cp * vinz + sp * pz;
+    o_normalize(vx, vy, vz);
+}
+
+__device__ __forceinline__ o_cell make_cell(const clr_scene_params& P) {
+    o_cell C = {P.n_water, P.n_acrylic, P.n_air, P.bottom_external_n, P.rin, P.rout, P.zmin,
+                P.zmin - P.bottom_disc_thickness, P.zmean, P.zwall_top, P.free_surface_model, P.vortex_delta_h,
+                P.vortex_core_radius};
+    return C;
+}
+__device__ __forceinline__ o_field make_field(const DevScene& D) {
+    o_field F = {D.P.sediment_model, D.P.free_surface_model, D.n_bins, D.n_radial, D.grid_nr, D.grid_nz,
+                 D.sedA, D.sedB, D.sed_norm, D.sed_radial_log, D.sed_grid, D.grid_zmax, D.P.rin, D.P.zmin,
+                 D.P.vortex_core_radius};
+    return F;
+}
+
+// Add the acrylic/headspace bounce counters of a sub-path to the ray.
+__device__ __forceinline__ void add_bounces(Ray& r, const o_bcount& b) {
+    r.cir += b.cir; r.cor += b.cor; r.ctir += b.ctir; r.tr += b.tr; r.ttir += b.ttir;
+    r.bir += b.bir; r.bor += b.bor; r.btir += b.btir;
+}
+
+// ---------------- launch segment: source, collimator, acrylic entry (:4650-4732) ----------------
+// Returns true when the history ended (r.st set), false when the ray entered the water.
+template <class S>
+__device__ __forceinline__ bool launch_segment(const DevScene& D, Ray& r, S* st, S* src) {
+    const clr_scene_params& P = D.P;
+    float x, y, z, vx = 0.0f, vy = 1.0f, vz = 0.0f;
+    if (P.source_kind == CLR_SOURCE_COLLIMATED_DISC) {
+        // New source (no reference counterpart): a uniform disc of radius disc_radius centred on the
+        // 180-degree axis at height disc_height, travelling along +y from just inside the sensor-ring radius.
+        float u1 = uniform(src), u2 = uniform(src);
+        float rr = P.disc_radius * sqrtf(u1);
+        float ph = 2.0f * CLR_PI_F * u2;
+        x = rr * cosf(ph);
+        z = P.disc_height + rr * sinf(ph);
+        y = -P.ring_in;
+    } else {
+        float u1 = fmaxf(uniform(src), 1e-12f), u2 = uniform(src);
+        float mag = sqrtf(-2.0f * logf(u1));
+        x = P.beam_sigma * mag * cosf(2.0f * CLR_PI_F * u2);
+        z = P.beam_sigma * mag * sinf(2.0f * CLR_PI_F * u2);
+        y = -P.source_r;
+        float polar, az;
+        if (P.source_angular_model == 0) {
+            polar = o_beta(src, P.alpha1, P.alpha2) * (CLR_PI_F / 2.0f);
+            az = 2.0f * CLR_PI_F * uniform(src);
+            float sp = sinf(polar);
+            vx = sp * cosf(az); vy = cosf(polar); vz = sp * sinf(az);
+        } else if (P.source_angular_model == 1) {
+            polar = o_beta_radiance_polar(src, P.alpha1, P.alpha2);
+            az = 2.0f * CLR_PI_F * uniform(src);
+            float sp = sinf(polar);
+            vx = sp * cosf(az); vy = cosf(polar); vz = sp * sinf(az);
+        } else {
+            float h = o_beta(src, P.alpha1, P.alpha2) * (CLR_PI_F / 2.0f);
+            if (uniform(src) < 0.5f) h = -h;
+            vx = sinf(h); vy = cosf(h); vz = 0.0f;
+        }
+        o_normalize(&vx, &vy, &vz);
+        if (vy <= 1e-12f) { r.st = 3; return true; }
+        if (P.source_bore_model == 0) {
+            if (x * x + z * z > P.counterbore_r * P.counterbore_r) { r.st = 3; return true; }
+            float t = (-P.throat_out - y) / vy;
+            if (t < -CLR_EPS_F) { r.st = 3; return true; }
+            if (t < 0.0f) t = 0.0f;
+            float xt = x + t * vx, zt = z + t * vz;
+            if (xt * xt + zt * zt > P.throat_r * P.throat_r) { r.st = 3; return true; }
+            t = (-P.ring_in - y) / vy;
+            if (t <= 0.0f) { r.st = 3; return true; }
+            x += t * vx; y += t * vy; z += t * vz;
+            if (x * x + z * z > P.throat_r * P.throat_r) { r.st = 3; return true; }
+        } else {
+            if (!o_source_collimator(src, P.source_bore_model, P.n_air, P.bore_n, P.max_bore_bounces, P.ring_in,
+                                     P.throat_out, P.source_r, P.throat_r, P.counterbore_r, &x, &y, &z, &vx, &vy, &vz,
+                                     &r.sbi, &r.sbr)) { r.st = 3; return true; }
+        }
+    }
+    const o_cell C = make_cell(P);
+    double tdw = o_cyl_hit_finite(x, y, z, vx, vy, vz, P.rout, P.zmin - P.bottom_disc_thickness, P.zwall_top);
+    float t = (tdw < 0.5 * (double)CLR_INF_F) ? (float)tdw : CLR_INF_F;
+    if (t >= CLR_INF_F * 0.5f) { r.st = 3; return true; }
+    x += t * vx; y += t * vy; z += t * vz;
+    float nx, ny;
+    o_radial_normal(x, y, &nx, &ny);
+    float ci = fminf(fmaxf(-o_dot(vx, vy, vz, nx, ny, 0.0f), 0.0f), 1.0f);
+    int tir = 0;
+    float R = o_fresnel(ci, P.n_air, P.n_acrylic, &tir);
+    float a, b, c;
+    if (tir || uniform(st) < R || !o_refract(vx, vy, vz, nx, ny, 0.0f, P.n_air, P.n_acrylic, &a, &b, &c)) {
+        o_reflect(vx, vy, vz, nx, ny, 0.0f, &a, &b, &c);
+        vx = a; vy = b; vz = c; r.cor++; if (tir) r.ctir++;
+        x += CLR_EPS_F * nx; y += CLR_EPS_F * ny;
+        r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
+        r.st = 1;
+        return true;
+    }
+    vx = a; vy = b; vz = c; x -= CLR_EPS_F * nx; y -= CLR_EPS_F * ny;
+    o_bcount bc = {0, 0, 0, 0, 0, 0, 0, 0};
+    int sub = 0, nb = 0;
+    int where = o_acrylic_solid(st, &C, C.n_air, C.n_bottom_ext, P.zmin, C.Zlow, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc,
+                                &sub, &nb);
+    bool ended = false;
+    if (where == 2) { r.st = 1; ended = true; }
+    else if (where == 3) { r.st = 7; ended = true; }
+    else if (where == 5) { r.st = 8; ended = true; }
+    else if (where == 4) {
+        int hs = 0, hb = 0;
+        int hw = o_headspace(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
+        if (hw == 1) r.entered = 1;
+        else if (hw == 2) { r.st = 1; ended = true; }
+        else if (hw == 3) { r.st = 7; ended = true; }
+        else if (hw == 4) { r.st = 6; ended = true; }
+        else if (hw == 5) { r.st = 8; ended = true; }
+        else { r.pf = OP_HEADSPACE_NO_BOUNDARY; r.pfs = hs; r.st = 4; ended = true; }
+    } else if (where != 1) {
+        r.pf = (sub == OS_ACRYLIC_BOUNCE_LIMIT) ? OP_ACRYLIC_BOUNCE_LIMIT : OP_ACRYLIC_NO_INTERSECTION;
+        r.pfs = sub; r.st = 4; ended = true;
+    }
+    add_bounces(r, bc);
+    r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
+    if (ended) return true;
+    r.entered = 1;
+    r.phase = PHASE_WATER;
+    r.step = 0;
+    return false;
+}
+
+// ---------------- one water free-flight step (one iteration of :4734-5066) ----------------
+// Returns true when the history ended.
+template <class S, bool kWeighted>
+__device__ __forceinline__ bool water_step(const DevScene& D, Ray& r, S* st, S* opt, unsigned long long* cstats) {
+    const clr_scene_params& P = D.P;
+    if (r.step >= (int)P.max_iterations) { r.pf = OP_ITERATION_LIMIT; r.pfs = OS_ITERATION_LIMIT; r.st = 4; return true; }
+    r.step++;
+    r.steps++;
+    const int TM = P.sediment_model, FSM = P.free_surface_model;
+    const float RIN = P.rin, ZMIN = P.zmin, ZMEAN = P.zmean, ZTOP = P.zwall_top, DH = P.vortex_delta_h,
+                CORE = P.vortex_core_radius;
+    float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
+    bool ended = false;
+    o_bcount bc = {0, 0, 0, 0, 0, 0, 0, 0};
+    do {
+        if (!isfinite(x) || !isfinite(y) || !isfinite(z)) { r.pf = OP_NONFINITE_POSITION; r.pfs = OS_NONFINITE_POSITION; r.st = 4; ended = true; break; }
+        if (!isfinite(vx) || !isfinite(vy) || !isfinite(vz)) { r.pf = OP_NONFINITE_DIRECTION; r.pfs = OS_NONFINITE_DIRECTION; r.st = 4; ended = true; break; }
+        float zsurf_here = o_surface_z(x, y, ZMEAN, RIN, FSM, DH, CORE);
+        if (z <= ZMIN || z >= zsurf_here) { r.st = 2; ended = true; break; }
+        double rr2w = (double)x * (double)x + (double)y * (double)y, ri2w = (double)RIN * (double)RIN;
+        double water_tol = 8.0 * 1.1920928955078125e-7 * ri2w;
+        if (rr2w > ri2w + water_tol) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; ended = true; break; }
+        double tsided = o_bore_wall_hit(x, y, z, vx, vy, vz, RIN, ZMIN, ZTOP);
+        if (tsided < 0.0) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; ended = true; break; }
+        float tside = (tsided < 0.5 * (double)CLR_INF_F) ? (float)tsided : CLR_INF_F;
+        float ttop = o_surface_hit(x, y, z, vx, vy, vz, ZMEAN, RIN, FSM, DH, CORE), tbottom = CLR_INF_F;
+        if (vz < -1e-14f) tbottom = (ZMIN - z) / vz;
+        if (!(ttop > 0.0f)) ttop = CLR_INF_F;
+        if (!(tbottom > 0.0f)) tbottom = CLR_INF_F;
+        int axial_top = (ttop <= tbottom && ttop < tside);
+        int axial_bottom = (tbottom < ttop && tbottom < tside);
+        int axial = axial_top || axial_bottom;
+        float tbound = axial_top ? ttop : (axial_bottom ? tbottom : tside);
+        if (tbound >= CLR_INF_F * 0.5f) { r.pf = OP_WATER_NO_BOUNDARY; r.pfs = OS_WATER_NO_BOUNDARY; r.st = 4; ended = true; break; }
+        const float MU_GEOM = (float)D.mu_channels[0], MU_WAVE = (float)D.mu_channels[1];
+        float freep = CLR_INF_F;
+        float MU_TOTAL = MU_GEOM + MU_WAVE;
+        float MU_TRACK = (TM == 0) ? MU_TOTAL : ((float)D.sed_major[0] + (float)D.sed_major[1]);
+        if (tbound > 0.0f && MU_TRACK > 0.0f) { float u = fmaxf(uniform(st), 1e-12f); freep = -logf(u) / MU_TRACK; }
+        int do_particle = freep < tbound;
+        float travel = do_particle ? freep : tbound;
+        x += travel * vx; y += travel * vy; z += travel * vz;
+        r.wp += travel;
+        double endpoint_r2 = (double)x * x + (double)y * y;
+        if (do_particle && (endpoint_r2 > ri2w + water_tol || z < ZMIN - CLR_EPS_F ||
+                            z > o_surface_z(x, y, ZMEAN, RIN, FSM, DH, CORE) + CLR_EPS_F)) {
+            r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; ended = true; break;
+        }
+        if (do_particle) {
+            const o_field F = make_field(D);
+            float LOCAL_GEOM = MU_GEOM, LOCAL_WAVE = MU_WAVE, LOCAL_TOTAL = MU_TOTAL;
+            if (TM != 0) {
+                double lg = 0.0, lw = 0.0;
+                for (int i = 0; i < D.n_bins; ++i) {
+                    double sc = o_local_scale(&F, i, x, y, z);
+                    lg += D.trace_geom[i] * sc;
+                    lw += D.trace_wave[i] * sc;
+                }
+                LOCAL_GEOM = (float)lg; LOCAL_WAVE = (float)lw; LOCAL_TOTAL = LOCAL_GEOM + LOCAL_WAVE;
+                if (!(LOCAL_TOTAL > 0.0f)) { r.nulls++; break; }
+                float slack = 64.0f * 1.1920928955078125e-7f * fmaxf(fabsf(MU_TRACK), 1.0f);
+                if (LOCAL_TOTAL > MU_TRACK + slack) { r.pf = OP_MAJORANT_VIOLATION; r.pfs = OS_MAJORANT; r.st = 4; ended = true; break; }
+                float pacc = LOCAL_TOTAL / fmaxf(MU_TRACK, 1e-30f);
+                if (pacc > 1.0f) pacc = 1.0f;
+                if (uniform(st) >= pacc) { r.nulls++; break; }
+            }
+            r.ic++;
+            const float vinx = vx, viny = vy, vinz = vz;
+            int event_pidx = -1;
+            float ipath = 0.0f;
+            const int COND = (P.event_model == 4 || P.event_model == 5);
+            const float COHERENT = fminf(fmaxf((float)D.mu_channels[7], 0.0f), 1.0f);
+            int use_wave = (LOCAL_WAVE > 0.0f && uniform(st) * LOCAL_TOTAL >= LOCAL_GEOM);
+            int sel = -1;
+            if (COND) {
+                if (TM == 0) sel = o_sample_cdf(st, use_wave ? D.wcdf : D.gcdf, D.n_bins);
+                else sel = o_sample_local_bin(st, &F, use_wave ? D.trace_wave : D.trace_geom, x, y, z,
+                                              (double)(use_wave ? LOCAL_WAVE : LOCAL_GEOM));
+            }
+            if (COND && D.k[sel] > 0.0) {
+                if (D.pk[sel] == 0.0f) { r.pf = OP_OTHER; r.pfs = 9003; r.st = 4; atomicAdd(&cstats[8], 1ull); ended = true; break; }
+                Hist h;
+                conditional_interaction(opt, &h, sel, D.qsca[sel], D.qext[sel], P.n_water, D.pn[sel], D.pk[sel],
+                                        P.wavelength, P.rough_alpha, D.prad[sel], P.spheroid_aspect,
+                                        P.orientation_model, P.orientation_kappa, P.max_particle_bounces, COHERENT,
+                                        D.phase_cdf, D.theta, D.nt, x, y, z, vx, vy, vz, RIN, ZMIN, ZMEAN, FSM, DH,
+                                        CORE, P.conditional_retries, cstats);
+                event_pidx = sel;
+                if (h.status != 1 && h.status != 2) { r.pf = h.failure ? h.failure : OP_OTHER; r.pfs = h.subcode; r.st = 4; ended = true; break; }
+                x = h.x; y = h.y; z = h.z; vx = h.vx; vy = h.vy; vz = h.vz;
+                r.pc.reflections += h.pc.reflections; r.pc.entry_reflections += h.pc.entry_reflections;
+                r.pc.internal_reflections += h.pc.internal_reflections; r.pc.absorptions += h.pc.absorptions;
+                if (h.channel == 0) r.gic++;
+                else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
+                if (h.status == 2) { r.st = 5; ended = true; break; }
+            } else if (use_wave) {
+                if (COND) atomicAdd(&cstats[0], 1ull);
+                r.wic++;
+                int pidx = sel >= 0 ? sel
+                                    : (TM == 0) ? o_sample_cdf(st, D.wcdf, D.n_bins)
+                                                : o_sample_local_bin(st, &F, D.trace_wave, x, y, z, (double)LOCAL_WAVE);
+                event_pidx = pidx;
+                int coherent = (COHERENT >= 1.0f) || (uniform(opt) < COHERENT);
+                if (coherent) {
+                    r.wcoh++;
+                    o_mie_direction(opt, D.phase_cdf, D.theta, D.nt, pidx, &vx, &vy, &vz);
+                    if (COND) { atomicAdd(&cstats[4], 1ull); atomicAdd(&cstats[7], 1ull); }
+                } else {
+                    r.wmorph++;
+                    float fr = sqrtf(x * x + y * y);
+                    float ffx = 1.0f, ffy = 0.0f, ffz = 0.0f;
+                    if (fr > 1e-12f) { ffx = -y / fr; ffy = x / fr; }
+                    int ppc = 0, pps = 0, pmb = 0, pmo = 0;
+                    int ps = o_spheroid_event(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha,
+                                              D.prad[pidx], P.spheroid_aspect, P.orientation_model,
+                                              P.orientation_kappa, ffx, ffy, ffz, P.max_particle_bounces, &vx, &vy,
+                                              &vz, &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
+                    if (ps == 2) { r.st = 5; ended = true; break; }
+                    if (ps != 1) { if (COND) atomicAdd(&cstats[8], 1ull); r.pf = ppc ? ppc : OP_OTHER; r.pfs = pps; r.st = 4; ended = true; break; }
+                    if (COND) { atomicAdd(&cstats[5], 1ull); atomicAdd(&cstats[7], 1ull); }
+                }
+            } else {
+                if (COND) atomicAdd(&cstats[0], 1ull);
+                r.gic++;
+                int pidx = sel >= 0 ? sel
+                                    : (TM == 0) ? o_sample_cdf(st, D.gcdf, D.n_bins)
+                                                : o_sample_local_bin(st, &F, D.trace_geom, x, y, z, (double)LOCAL_GEOM);
+                event_pidx = pidx;
+                float prad = D.prad[pidx];
+                float srho, sphi, sgx, sgy, sgz;
+                o_sphere_geometry(opt, prad, x, y, z, vx, vy, vz, &srho, &sphi, &sgx, &sgy, &sgz);
+                double dscx = (double)x - (double)prad * (double)sgx;
+                double dscy = (double)y - (double)prad * (double)sgy;
+                double dscz = (double)z - (double)prad * (double)sgz;
+                int accessible = o_sphere_accessible(dscx, dscy, dscz, (double)prad, RIN, ZMIN, ZMEAN, FSM, DH, CORE);
+                if (!accessible && COND) {
+                    atomicAdd(&cstats[2], 1ull);
+                    Hist h;
+                    conditional_interaction(opt, &h, pidx, D.qsca[pidx], D.qext[pidx], P.n_water, D.pn[pidx],
+                                            D.pk[pidx], P.wavelength, P.rough_alpha, prad, P.spheroid_aspect,
+                                            P.orientation_model, P.orientation_kappa, P.max_particle_bounces,
+                                            COHERENT, D.phase_cdf, D.theta, D.nt, x, y, z, vx, vy, vz, RIN, ZMIN,
+                                            ZMEAN, FSM, DH, CORE, P.conditional_retries - 1, cstats);
+                    if (h.status != 1) { r.pf = h.failure ? h.failure : OP_OTHER; r.pfs = h.subcode; r.st = 4; ended = true; break; }
+                    x = h.x; y = h.y; z = h.z; vx = h.vx; vy = h.vy; vz = h.vz;
+                    r.pc.reflections += h.pc.reflections; r.pc.entry_reflections += h.pc.entry_reflections;
+                    r.pc.internal_reflections += h.pc.internal_reflections; r.pc.absorptions += h.pc.absorptions;
+                    r.gic--;
+                    if (h.channel == 0) r.gic++;
+                    else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
+                } else {
+                    if (!accessible) { r.ic--; r.gic--; r.nulls++; break; }
+                    int ppc = 0, pps = 0, pmb = 0, pmo = 0;
+                    int ps = o_sphere_sampled(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, prad,
+                                              P.max_particle_bounces, sgx, sgy, sgz, dscx, dscy, dscz, &x, &y, &z, &vx,
+                                              &vy, &vz, &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
+                    if (ps == 2) { r.st = 5; ended = true; break; }
+                    if (ps != 1) { if (COND) atomicAdd(&cstats[8], 1ull); r.pf = ppc ? ppc : OP_OTHER; r.pfs = pps; r.st = 4; ended = true; break; }
+                    if (COND) { atomicAdd(&cstats[3], 1ull); atomicAdd(&cstats[7], 1ull); }
+                }
+            }
+            if (D.any_moment && event_pidx >= 0 && D.moment_mode[event_pidx])
+                moment_constraint(vinx, viny, vinz, &vx, &vy, &vz, (float)D.moment_a[event_pidx],
+                                  (float)D.moment_b[event_pidx]);
+            break;
+        }
+        const o_cell C = make_cell(P);
+        if (axial) {
+            float a, b, c;
+            int tir = 0;
+            if (axial_top) {
+                float snx = 0.0f, sny = 0.0f, snz = -1.0f;
+                o_surface_normal(x, y, RIN, FSM, DH, CORE, &snx, &sny, &snz);
+                float ci = fminf(fmaxf(-o_dot(vx, vy, vz, snx, sny, snz), 0.0f), 1.0f);
+                float R = o_fresnel(ci, P.n_water, P.n_air, &tir);
+                if (tir || uniform(st) < R || !o_refract(vx, vy, vz, snx, sny, snz, P.n_water, P.n_air, &a, &b, &c)) {
+                    o_reflect(vx, vy, vz, snx, sny, snz, &a, &b, &c);
+                    vx = a; vy = b; vz = c; r.tr++; if (tir) r.ttir++;
+                    if (!o_surface_offset(&x, &y, &z, snx, sny, snz, RIN, ZMIN, ZMEAN, FSM, DH, CORE)) {
+                        r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; ended = true;
+                    }
+                    break;
+                }
+                vx = a; vy = b; vz = c;
+                x -= CLR_EPS_F * snx; y -= CLR_EPS_F * sny; z -= CLR_EPS_F * snz;
+                int hs = 0, hb = 0;
+                int hw = o_headspace(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
+                if (hw == 1) break;
+                ended = true;
+                if (hw == 2) r.st = 1;
+                else if (hw == 3) r.st = 7;
+                else if (hw == 4) r.st = 6;
+                else { r.pf = OP_HEADSPACE_NO_BOUNDARY; r.pfs = hs; r.st = 4; }
+                break;
+            } else {
+                int bs = 0, bb = 0;
+                int where = o_bottom_disc(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &bs, &bb);
+                if (where == 1) break;
+                ended = true;
+                if (where == 2) { r.st = 1; break; }
+                if (where == 3) { r.st = 7; break; }
+                if (where == 5) { r.st = 8; break; }
+                if (where == 4) {
+                    int hs = 0, hb = 0;
+                    int hw = o_headspace(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
+                    if (hw == 1) { ended = false; break; }
+                    if (hw == 2) r.st = 1;
+                    else if (hw == 3) r.st = 7;
+                    else if (hw == 4) r.st = 6;
+                    else { r.pf = OP_HEADSPACE_NO_BOUNDARY; r.pfs = hs; r.st = 4; }
+                    break;
+                }
+                r.pf = (bs == OS_ACRYLIC_BOUNCE_LIMIT) ? OP_ACRYLIC_BOUNCE_LIMIT : OP_BOTTOM_GEOMETRY;
+                r.pfs = bs; r.st = 4;
+                break;
+            }
+        }
+        // water -> acrylic at the cylinder wall (:5038-5065)
+        {
+            float nx, ny;
+            o_radial_normal(x, y, &nx, &ny);
+            float ci = fminf(fmaxf(o_dot(vx, vy, vz, nx, ny, 0.0f), 0.0f), 1.0f);
+            int tir = 0;
+            float R = o_fresnel(ci, P.n_water, P.n_acrylic, &tir);
+            float a, b, c;
+            if (tir || uniform(st) < R || !o_refract(vx, vy, vz, -nx, -ny, 0.0f, P.n_water, P.n_acrylic, &a, &b, &c)) {
+                o_reflect(vx, vy, vz, nx, ny, 0.0f, &a, &b, &c);
+                vx = a; vy = b; vz = c; r.cir++; if (tir) r.ctir++;
+                x -= CLR_EPS_F * nx; y -= CLR_EPS_F * ny;
+                break;
+            }
+            vx = a; vy = b; vz = c; x += CLR_EPS_F * nx; y += CLR_EPS_F * ny;
+            int sub = 0, nb = 0;
+            int where = o_acrylic_solid(st, &C, C.n_air, C.n_bottom_ext, ZMIN, C.Zlow, &x, &y, &z, &vx, &vy, &vz, &r.ap,
+                                        &bc, &sub, &nb);
+            if (where == 1) break;
+            ended = true;
+            if (where == 2) { r.st = 1; break; }
+            if (where == 3) { r.st = 7; break; }
+            if (where == 5) { r.st = 8; break; }
+            if (where == 4) {
+                int hs = 0, hb = 0;
+                int hw = o_headspace(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
+                if (hw == 1) { ended = false; break; }
+                if (hw == 2) r.st = 1;
+                else if (hw == 3) r.st = 7;
+                else if (hw == 4) r.st = 6;
+                else if (hw == 5) r.st = 8;
+                else { r.pf = OP_HEADSPACE_NO_BOUNDARY; r.pfs = hs; r.st = 4; }
+                break;
+            }
+            r.pf = (sub == OS_ACRYLIC_BOUNCE_LIMIT) ? OP_ACRYLIC_BOUNCE_LIMIT : OP_ACRYLIC_NO_INTERSECTION;
+            r.pfs = sub; r.st = 4;
+        }
+    } while (false);
+    add_bounces(r, bc);
+    r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
+    (void)kWeighted;
+    return ended;
+}
+
+}  // namespace
+}  // namespace clr

@@ -1,0 +1,525 @@
+// Particle-physics precompute on the device (FP64).
+//
+// Replaces the precompute launched by ClaritasForwardModel._prepare_gpu_particle_physics
+// (CLARITAS/CLARITAS.py:6036-6965). The per-bin and per-angle arithmetic is the
+// reference's (kernels :3488-3592, :3845-3921, :3925-4038), so the tables the
+// photon kernel reads are identical to the reference's on the same GPU; only
+// the parallel decomposition changes:
+//  * Mie coefficients: one warp per size bin, the downward log-derivative
+//    recurrence kept in shared memory instead of a global scratch array;
+//  * phase pdf: one thread per (angle, group of 4 bins) sharing the angular
+//    pi_n/tau_n recurrence across the group (the recurrence depends only on the
+//    angle), instead of one thread per (bin, angle) recomputing it;
+//  * Schiller-Naumann radial slip: one thread per (bin, radius) instead of one
+//    thread for everything; the serial prefix sums and quadrature stay serial
+//    per bin so their rounding is unchanged.
+#include <cstdint>
+#include <cstring>
+#include "kernels.h"
+
+namespace clr {
+
+#define PD_PI 3.141592653589793238462643383279502884
+
+struct cdx { double re, im; };
+__device__ __forceinline__ cdx CD(double re, double im) { cdx z; z.re = re; z.im = im; return z; }
+__device__ __forceinline__ cdx cd_add(cdx a, cdx b) { return CD(a.re + b.re, a.im + b.im); }
+__device__ __forceinline__ cdx cd_sub(cdx a, cdx b) { return CD(a.re - b.re, a.im - b.im); }
+__device__ __forceinline__ cdx cd_mul(cdx a, cdx b) { return CD(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re); }
+__device__ __forceinline__ cdx cd_scale(cdx a, double s) { return CD(a.re * s, a.im * s); }
+__device__ __forceinline__ cdx cd_div(cdx a, cdx b) {
+    double d = b.re * b.re + b.im * b.im;
+    if (d < 1e-300) d = 1e-300;
+    return CD((a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d);
+}
+__device__ __forceinline__ double cd_abs2(cdx a) { return a.re * a.re + a.im * a.im; }
+__device__ __forceinline__ double cd_rmc(cdx a, cdx b) { return a.re * b.re + a.im * b.im; }
+
+// One warp per bin; lane 0 runs the recurrences (they are inherently serial). (:3495-3559)
+__global__ void __launch_bounds__(32) mie_coefficients_kernel(const double* __restrict__ diameter,
+                                                              const double* __restrict__ n_real,
+                                                              const double* __restrict__ k_imag, double n_medium,
+                                                              double wavelength, int n_particles,
+                                                              double* __restrict__ ab, int* __restrict__ nstop_out,
+                                                              double* size_parameter, double* qext, double* qsca,
+                                                              double* qabs, double* qback, double* asym_g,
+                                                              double* albedo, int* error_flag) {
+    extern __shared__ cdx Dsh[];
+    const int p = blockIdx.x;
+    if (p >= n_particles || threadIdx.x != 0) return;
+    double x = PD_PI * n_medium * diameter[p] / wavelength;
+    size_parameter[p] = x;
+    if (!(x > 0.0) || !(n_real[p] > 0.0) || !(n_medium > 0.0) || !(wavelength > 0.0)) {
+        nstop_out[p] = 0; qext[p] = qsca[p] = qabs[p] = qback[p] = asym_g[p] = 0.0; albedo[p] = 1.0;
+        atomicExch(error_flag, 2);
+        return;
+    }
+    double mr = n_real[p] / n_medium, mi = k_imag[p] / n_medium;
+    int nstop = (int)(x + 4.0 * cbrt(x) + 2.0);
+    if (nstop < 1) nstop = 1;
+    double mz = hypot(mr * x, mi * x);
+    int nmx = (int)fmax((double)nstop, mz) + 128;
+    if (nmx < nstop + 1) nmx = nstop + 1;
+    if (nmx >= CLR_MIE_MAX_ORDER || nstop >= CLR_MIE_MAX_ORDER) { nstop_out[p] = 0; atomicExch(error_flag, 1); return; }
+    nstop_out[p] = nstop;
+    Dsh[nmx] = CD(0.0, 0.0);
+    cdx z = CD(mr * x, mi * x);
+    for (int n = nmx; n >= 1; --n) {
+        cdx nz = cd_div(CD((double)n, 0.0), z);
+        cdx dn = Dsh[n];
+        Dsh[n - 1] = cd_sub(nz, cd_div(CD(1.0, 0.0), cd_add(dn, nz)));
+    }
+    double psi_nm1 = sin(x), psi_n = sin(x) / x - cos(x);
+    double chi_nm1 = cos(x), chi_n = cos(x) / x + sin(x);
+    cdx m = CD(mr, mi);
+    double4* abp = reinterpret_cast<double4*>(ab) + (size_t)p * CLR_MIE_MAX_ORDER;
+    for (int j = 0; j < nstop; ++j) {
+        int n = j + 1;
+        cdx xi_nm1 = CD(psi_nm1, -chi_nm1), xi_n = CD(psi_n, -chi_n);
+        cdx dn = Dsh[n];
+        cdx ca = cd_add(cd_div(dn, m), CD((double)n / x, 0.0));
+        cdx cb = cd_add(cd_mul(m, dn), CD((double)n / x, 0.0));
+        cdx aa = cd_div(cd_sub(cd_scale(ca, psi_n), CD(psi_nm1, 0.0)), cd_sub(cd_mul(ca, xi_n), xi_nm1));
+        cdx bb = cd_div(cd_sub(cd_scale(cb, psi_n), CD(psi_nm1, 0.0)), cd_sub(cd_mul(cb, xi_n), xi_nm1));
+        abp[j] = make_double4(aa.re, aa.im, bb.re, bb.im);
+        double psi_np1 = ((2.0 * n + 1.0) / x) * psi_n - psi_nm1;
+        double chi_np1 = ((2.0 * n + 1.0) / x) * chi_n - chi_nm1;
+        psi_nm1 = psi_n; psi_n = psi_np1; chi_nm1 = chi_n; chi_n = chi_np1;
+    }
+    double se = 0.0, ss = 0.0, sbr = 0.0, sbi = 0.0, t1 = 0.0, t2 = 0.0;
+    for (int j = 0; j < nstop; ++j) {
+        int n = j + 1;
+        double cn = 2.0 * n + 1.0;
+        double4 q = abp[j];
+        cdx aa = CD(q.x, q.y), bb = CD(q.z, q.w);
+        se += cn * (aa.re + bb.re);
+        ss += cn * (cd_abs2(aa) + cd_abs2(bb));
+        double sign = (n & 1) ? -1.0 : 1.0;
+        sbr += cn * sign * (aa.re - bb.re);
+        sbi += cn * sign * (aa.im - bb.im);
+        t2 += (cn / ((double)n * (n + 1.0))) * cd_rmc(aa, bb);
+        if (j + 1 < nstop) {
+            double4 q2 = abp[j + 1];
+            cdx an = CD(q2.x, q2.y), bn = CD(q2.z, q2.w);
+            t1 += ((double)n * (n + 2.0) / (n + 1.0)) * (cd_rmc(aa, an) + cd_rmc(bb, bn));
+        }
+    }
+    double x2 = x * x;
+    double qe = 2.0 * se / x2, qs = 2.0 * ss / x2, qb = (sbr * sbr + sbi * sbi) / x2;
+    if (qe < 0.0 && qe > -1e-12) qe = 0.0;
+    if (qs < 0.0 && qs > -1e-12) qs = 0.0;
+    double qa = qe - qs;
+    if (qa < 0.0 && qa > -1e-10) qa = 0.0;
+    double gg = qs > 0.0 ? 4.0 * (t1 + t2) / (x2 * qs) : 0.0;
+    if (gg > 1.0) gg = 1.0;
+    if (gg < -1.0) gg = -1.0;
+    qext[p] = qe; qsca[p] = qs; qabs[p] = qa; qback[p] = qb; asym_g[p] = gg; albedo[p] = qe > 0.0 ? qs / qe : 1.0;
+}
+
+// theta_j = pi/2 (1 - cos(pi j/(nt-1))) (:3488-3493), plus the float copy the sampler reads
+__global__ void theta_grid_kernel(double* theta, float* theta_f, int nt) {
+    int j = blockDim.x * blockIdx.x + threadIdx.x;
+    if (j >= nt) return;
+    double v;
+    if (j == 0) v = 0.0;
+    else if (j == nt - 1) v = PD_PI;
+    else { double u = (double)j / (double)(nt - 1); v = 0.5 * PD_PI * (1.0 - cos(PD_PI * u)); }
+    theta[j] = v;
+    theta_f[j] = (float)v;
+}
+
+#define PDF_GROUP 4
+// S1/S2 -> 0.5(|S1|^2+|S2|^2) sin(theta) for PDF_GROUP bins at one angle (:3561-3581)
+__global__ void __launch_bounds__(128) phase_pdf_kernel(const double* __restrict__ theta, int nt, int n_particles,
+                                                        const int* __restrict__ nstop, const double* __restrict__ ab,
+                                                        double* __restrict__ pdf) {
+    const int j = blockDim.x * blockIdx.x + threadIdx.x;
+    const int g0 = blockIdx.y * PDF_GROUP;
+    if (j >= nt) return;
+    double th = theta[j], mu = cos(th);
+    double s1r[PDF_GROUP], s1i[PDF_GROUP], s2r[PDF_GROUP], s2i[PDF_GROUP];
+    int ns[PDF_GROUP];
+    int kmax = 0;
+#pragma unroll
+    for (int g = 0; g < PDF_GROUP; ++g) {
+        s1r[g] = s1i[g] = s2r[g] = s2i[g] = 0.0;
+        ns[g] = (g0 + g < n_particles) ? nstop[g0 + g] : 0;
+        kmax = ns[g] > kmax ? ns[g] : kmax;
+    }
+    const double4* abp = reinterpret_cast<const double4*>(ab);
+    double pi_nm1 = 0.0, pi_n = 1.0;
+    for (int k = 0; k < kmax; ++k) {
+        int n = k + 1;
+        double nf = (double)n;
+        double tau = nf * mu * pi_n - (nf + 1.0) * pi_nm1;
+        double c = (2.0 * nf + 1.0) / (nf * (nf + 1.0));
+#pragma unroll
+        for (int g = 0; g < PDF_GROUP; ++g) {
+            if (k < ns[g]) {
+                double4 q = abp[(size_t)(g0 + g) * CLR_MIE_MAX_ORDER + k];
+                double ar = q.x, ai = q.y, br = q.z, bi = q.w;
+                s1r[g] += c * (ar * pi_n + br * tau);
+                s1i[g] += c * (ai * pi_n + bi * tau);
+                s2r[g] += c * (ar * tau + br * pi_n);
+                s2i[g] += c * (ai * tau + bi * pi_n);
+            }
+        }
+        double pi_np1 = ((2.0 * nf + 1.0) / nf) * mu * pi_n - ((nf + 1.0) / nf) * pi_nm1;
+        pi_nm1 = pi_n; pi_n = pi_np1;
+    }
+#pragma unroll
+    for (int g = 0; g < PDF_GROUP; ++g) {
+        if (g0 + g < n_particles) {
+            double intensity = 0.5 * (s1r[g] * s1r[g] + s1i[g] * s1i[g] + s2r[g] * s2r[g] + s2i[g] * s2i[g]);
+            pdf[(size_t)(g0 + g) * nt + j] = intensity * sin(th);
+        }
+    }
+}
+
+// Serial trapezoid CDF per bin, normalised and forced monotone (:3583-3592); also the float copy.
+__global__ void phase_cdf_kernel(const double* __restrict__ theta, const double* __restrict__ pdf, int nt,
+                                 int n_particles, double* __restrict__ cdf, float* __restrict__ cdf_f, int* error_flag) {
+    int p = blockDim.x * blockIdx.x + threadIdx.x;
+    if (p >= n_particles) return;
+    long long base = (long long)p * nt;
+    cdf[base] = 0.0;
+    double s = 0.0;
+    for (int j = 1; j < nt; ++j) {
+        double area = 0.5 * (pdf[base + j] + pdf[base + j - 1]) * (theta[j] - theta[j - 1]);
+        if (area < 0.0 && area > -1e-18) area = 0.0;
+        s += area;
+        cdf[base + j] = s;
+    }
+    if (!(s > 0.0) || !isfinite(s)) {
+        atomicExch(error_flag, 3);
+        for (int j = 0; j < nt; ++j) { cdf[base + j] = (double)j / (double)(nt - 1); cdf_f[base + j] = (float)cdf[base + j]; }
+        return;
+    }
+    double prev = 0.0;
+    for (int j = 0; j < nt; ++j) {
+        double v = cdf[base + j] / s;
+        if (v < prev) v = prev;
+        if (v > 1.0) v = 1.0;
+        cdf[base + j] = v;
+        prev = v;
+    }
+    cdf[base + nt - 1] = 1.0;
+    for (int j = 0; j < nt; ++j) cdf_f[base + j] = (float)cdf[base + j];
+}
+
+__global__ void dummy_phase_kernel(double* theta, float* theta_f, double* cdf, float* cdf_f, int n_particles) {
+    int p = blockDim.x * blockIdx.x + threadIdx.x;
+    if (p == 0) { theta[0] = 0.0; theta[1] = PD_PI; theta_f[0] = 0.0f; theta_f[1] = (float)PD_PI; }
+    if (p < n_particles) { cdf[2 * p] = 0.0; cdf[2 * p + 1] = 1.0; cdf_f[2 * p] = 0.0f; cdf_f[2 * p + 1] = 1.0f; }
+}
+
+// PSD normalisation (:3615-3635), rates and channel CDFs (:3845-3921), channel rate arrays
+// (:6362-6375) and the float copies the photon kernel reads. n <= 64: one thread.
+__global__ void transport_kernel(int n, const double* __restrict__ d, const double* __restrict__ w_in,
+                                 const double* __restrict__ qext, const double* __restrict__ qsca,
+                                 const double* __restrict__ k_imag, const double* __restrict__ n_real,
+                                 double concentration, double density, int weight_mode, int em, double wave_scale,
+                                 double n_medium, double wavelength, double wave_rms, double* w, double* radius,
+                                 double* nden, double* mug, double* mus, double* mue, double* muw, double* muev,
+                                 double* gcdf, double* wcdf, double* pcdf, double* muscal, double* trace_geom,
+                                 double* trace_wave, float* gcdf_f, float* wcdf_f, float* pn_f, float* pk_f,
+                                 float* prad_f, int* error_flag) {
+    if (blockIdx.x || threadIdx.x) return;
+    if (n < 1 || n > CLR_MAX_BINS) { atomicExch(error_flag, 20); return; }
+    if (!(density > 0.0) || concentration < 0.0) { atomicExch(error_flag, 21); return; }
+    double sw0 = 0.0;
+    for (int i = 0; i < n; ++i) sw0 += w_in[i];
+    if (!(sw0 > 0.0)) { atomicExch(error_flag, 22); return; }
+    for (int i = 0; i < n; ++i) w[i] = w_in[i] / sw0;
+    double sw = 0.0;
+    for (int i = 0; i < n; ++i) sw += w[i];
+    if (!(sw > 0.0)) { atomicExch(error_flag, 4); return; }
+    double pmass[CLR_MAX_BINS], srcw[CLR_MAX_BINS];
+    double avg_mass = 0.0;
+    for (int i = 0; i < n; ++i) {
+        double r = 0.5 * d[i];
+        radius[i] = r;
+        srcw[i] = w[i] / sw;
+        double m = density * (4.0 / 3.0) * PD_PI * r * r * r;
+        pmass[i] = m;
+        avg_mass += srcw[i] * m;
+    }
+    for (int i = 0; i < n; ++i) {
+        double nd = 0.0;
+        if (weight_mode == 0) nd = concentration * srcw[i] / pmass[i];
+        else nd = (avg_mass > 0.0 ? concentration / avg_mass : 0.0) * srcw[i];
+        nden[i] = nd;
+        double sg = PD_PI * radius[i] * radius[i], sa = fmax(qsca[i], 0.0) * sg, se = fmax(qext[i], 0.0) * sg;
+        double tol = 1e-10 * fmax(1.0, fmax(fabs(qext[i]), fabs(qsca[i])));
+        const double ki = k_imag[i];
+        if (!isfinite(ki) || ki < 0.0 || !isfinite(qext[i]) || !isfinite(qsca[i]) || qext[i] < -tol || qsca[i] < -tol ||
+            qsca[i] > qext[i] + tol || (ki == 0.0 && fabs(qext[i] - qsca[i]) > tol)) {
+            atomicExch(error_flag, 5);
+            return;
+        }
+        double swv = 0.0;
+        if (em == 3) swv = wave_scale * fmax(qsca[i] - 1.0, 0.0) * sg;
+        else if (em == 4 || em == 5) {
+            double rate = (ki > 0.0) ? se : sa;
+            swv = (ki > 0.0) ? ((sa > 0.0) ? rate * fmax(sa - sg, 0.0) / sa : 0.0) : fmax(sa - sg, 0.0);
+        }
+        mug[i] = nd * sg; mus[i] = nd * sa; mue[i] = nd * se; muw[i] = nd * swv;
+    }
+    double mg = 0.0, ms = 0.0, me = 0.0, mw = 0.0;
+    for (int i = 0; i < n; ++i) { mg += mug[i]; ms += mus[i]; me += mue[i]; mw += muw[i]; }
+    double mt = 0.0;
+    for (int i = 0; i < n; ++i) {
+        double mb;
+        if (em == 0) mb = mug[i];
+        else if (em == 1) mb = mus[i];
+        else if (em == 2) mb = mue[i];
+        else if (em == 3) mb = mug[i] + muw[i];
+        else mb = (k_imag[i] > 0.0) ? mue[i] : mus[i];
+        muev[i] = mb;
+        mt += mb;
+    }
+    const bool hyb = (em == 3) || (em == 4) || (em == 5);
+    double mtrace_geom = ((em == 4) || (em == 5)) ? fmax(mt - mw, 0.0) : ((em == 3) ? mg : mt);
+    double mtrace_wave = hyb ? mw : 0.0;
+    double cg = 0.0, cw = 0.0, ct = 0.0;
+    for (int i = 0; i < n; ++i) {
+        double mgi = ((em == 4) || (em == 5)) ? fmax(muev[i] - muw[i], 0.0) : mug[i];
+        double pg = hyb ? (mtrace_geom > 0.0 ? mgi / mtrace_geom : 0.0) : (mt > 0.0 ? muev[i] / mt : 0.0);
+        double pw = (hyb && mtrace_wave > 0.0 ? muw[i] / mtrace_wave : 0.0), pt = (mt > 0.0 ? muev[i] / mt : 0.0);
+        cg += pg; cw += pw; ct += pt;
+        gcdf[i] = cg; wcdf[i] = cw; pcdf[i] = ct;
+    }
+    if (cg > 0.0) gcdf[n - 1] = 1.0;
+    if (cw > 0.0) wcdf[n - 1] = 1.0;
+    if (ct > 0.0) pcdf[n - 1] = 1.0;
+    muscal[0] = mtrace_geom; muscal[1] = mtrace_wave; muscal[2] = mg; muscal[3] = ms;
+    muscal[4] = me; muscal[5] = mtrace_wave; muscal[6] = mt;
+    double cwave = 1.0;
+    if (hyb && wave_rms > 0.0 && wavelength > 0.0 && n_medium > 0.0) {
+        double a = 4.0 * PD_PI * n_medium * wave_rms / wavelength;
+        cwave = exp(-a * a);
+        if (cwave < 0.0) cwave = 0.0;
+        if (cwave > 1.0) cwave = 1.0;
+    }
+    muscal[7] = cwave;
+    for (int i = 0; i < n; ++i) {
+        if (em == 3) { trace_geom[i] = mug[i]; trace_wave[i] = muw[i]; }
+        else if (em == 4 || em == 5) { trace_geom[i] = fmax(muev[i] - muw[i], 0.0); trace_wave[i] = muw[i]; }
+        else { trace_geom[i] = muev[i]; trace_wave[i] = 0.0; }
+        gcdf_f[i] = (float)gcdf[i];
+        wcdf_f[i] = (float)wcdf[i];
+        pn_f[i] = (float)n_real[i];
+        pk_f[i] = (float)k_imag[i];
+        prad_f[i] = (float)radius[i];
+    }
+}
+
+// Schiller-Naumann terminal velocity by damped Newton (:3925-3937)
+__device__ double sn_velocity(double v0, double d, double rho_w, double mu, double* out_Re, double* out_drag) {
+    if (!(v0 > 0.0)) { *out_Re = 0.0; *out_drag = 1.0; return 0.0; }
+    double v = v0, K = rho_w * d / mu;
+    for (int it = 0; it < 24; ++it) {
+        double Re = fmax(K * v, 0.0);
+        double corr = 0.15 * pow(Re, 0.687);
+        double f = v * (1.0 + corr) - v0;
+        double df = 1.0 + 1.687 * corr;
+        double vn = fmax(v - f / df, 0.0);
+        if (fabs(vn - v) <= 2e-14 * fmax(1.0, fabs(v))) { v = vn; break; }
+        v = vn;
+    }
+    double Re = fmax(K * v, 0.0), drag = 1.0 + 0.15 * pow(Re, 0.687);
+    *out_Re = Re; *out_drag = drag;
+    return v;
+}
+
+struct SedArgs {
+    int n, TM, FSM, NQ, NRAD;
+    double rho_p, rho_w, mu, grav, Dt, R, ZMIN, ZMEAN, DH, CORE;
+};
+
+__device__ __forceinline__ void sed_geometry(const SedArgs& a, double* R2, double* a2, double* Hinf, double* hbar,
+                                             double* omega2, double* fR) {
+    *R2 = a.R * a.R; *a2 = a.CORE * a.CORE; *Hinf = 0.0; *hbar = 0.0; *omega2 = 0.0;
+    if (a.DH > 0.0 && a.FSM == 1) { *Hinf = a.DH; *hbar = 0.5 * a.DH; *omega2 = 2.0 * a.grav * a.DH / *R2; }
+    else if (a.DH > 0.0 && a.FSM == 2) {
+        *Hinf = a.DH * (*a2 + *R2) / *R2;
+        *hbar = *Hinf * (1.0 - (*a2 / *R2) * log1p(*R2 / *a2));
+        *omega2 = 2.0 * a.grav * *Hinf / *a2;
+    }
+    *fR = (a.FSM == 2) ? *R2 / (*a2 + *R2) : *R2;
+}
+
+// Per-bin radial slip table: one thread per (bin, radius) for the finite-Re models (:3975-3986).
+__global__ void sediment_slip_kernel(SedArgs a, const double* __restrict__ diameter, double* __restrict__ wr_out) {
+    const int i = blockIdx.y;
+    const int j = blockDim.x * blockIdx.x + threadIdx.x;
+    if (i >= a.n || j >= a.NRAD || a.TM == 0 || a.TM == 1) return;
+    double R2, a2, Hinf, hbar, omega2, fR;
+    sed_geometry(a, &R2, &a2, &Hinf, &hbar, &omega2, &fR);
+    double d = diameter[i];
+    double tau = a.rho_p * d * d / (18.0 * a.mu);
+    double drad = a.R / (double)(a.NRAD - 1);
+    double r = (double)j * drad, acc = 0.0;
+    if (r > 0.0) acc = (a.FSM == 1) ? omega2 * r : ((a.FSM == 2) ? omega2 * r / pow(1.0 + r * r / a2, 2.0) : 0.0);
+    double w0 = tau * acc, re = 0.0, drag = 1.0;
+    wr_out[(size_t)i * a.NRAD + j] = sn_velocity(w0, d, a.rho_w, a.mu, &re, &drag);
+}
+
+// Per-bin coefficients, radial potential and normalisation (:3958-4035); one thread per bin.
+__global__ void sediment_bin_kernel(SedArgs a, const double* __restrict__ diameter, const double* __restrict__ wr,
+                                    double* sedA, double* sedB, double* sed_norm, double* sed_max, double* radial_log,
+                                    int* error_flag) {
+    const int i = blockDim.x * blockIdx.x + threadIdx.x;
+    if (i >= a.n) return;
+    if (a.TM == 0) { sedA[i] = 0.0; sedB[i] = 0.0; sed_norm[i] = 1.0; sed_max[i] = 1.0; return; }
+    double R2, a2, Hinf, hbar, omega2, fR;
+    sed_geometry(a, &R2, &a2, &Hinf, &hbar, &omega2, &fR);
+    const double R = a.R, ZMIN = a.ZMIN, ZMEAN = a.ZMEAN, DH = a.DH;
+    const int NRAD = a.NRAD, NQ = a.NQ, FSM = a.FSM, TM = a.TM;
+    double Hmean = ZMEAN - ZMIN, dr = R / (double)NQ, drad = R / (double)(NRAD - 1);
+    double d = diameter[i];
+    double tau = a.rho_p * d * d / (18.0 * a.mu);
+    double ws0 = (a.rho_p - a.rho_w) * a.grav * d * d / (18.0 * a.mu);
+    double sre = 0.0, sdrag = 1.0;
+    double ws = (TM == 2 || TM == 3) ? sn_velocity(ws0, d, a.rho_w, a.mu, &sre, &sdrag) : ws0;
+    double Bc = ws / a.Dt;
+    sedB[i] = Bc;
+    double* RL = radial_log + (size_t)i * NRAD;
+    if (TM == 1) {
+        double Ac = tau * omega2 * ((FSM == 2) ? a2 : 1.0) / (2.0 * a.Dt);
+        sedA[i] = Ac;
+        for (int j = 0; j < NRAD; ++j) {
+            double r = (double)j * drad, rr2 = r * r, f = (FSM == 2) ? rr2 / (a2 + rr2) : rr2;
+            RL[j] = Ac * (f - fR);
+        }
+    } else {
+        const double* W = wr + (size_t)i * NRAD;
+        double total = 0.0, prev = 0.0;
+        for (int j = 0; j < NRAD; ++j) {
+            double w = W[j];
+            if (j > 0) total += 0.5 * (prev + w) * drad;
+            prev = w;
+        }
+        double cum = 0.0;
+        prev = 0.0;
+        for (int j = 0; j < NRAD; ++j) {
+            double w = W[j];
+            if (j > 0) cum += 0.5 * (prev + w) * drad;
+            prev = w;
+            double psi = (cum - total) / a.Dt;
+            if (psi > 0.0) psi = 0.0;
+            RL[j] = psi;
+        }
+        RL[NRAD - 1] = 0.0;
+        sedA[i] = (fR > 0.0) ? -RL[0] / fR : 0.0;
+    }
+    double integ = 0.0;
+    for (int j = 0; j < NQ; ++j) {
+        double r = ((double)j + 0.5) * dr, rr2 = r * r;
+        double zsurf = ZMEAN;
+        if (FSM == 1 && DH > 0.0) zsurf = ZMEAN + DH * (rr2 / R2 - 0.5);
+        else if (FSM == 2 && DH > 0.0) zsurf = ZMEAN - hbar + Hinf * rr2 / (a2 + rr2);
+        double Hh = fmax(zsurf - ZMIN, 0.0);
+        double rl;
+        if (TM == 1) {
+            double f = (FSM == 2) ? rr2 / (a2 + rr2) : rr2;
+            rl = sedA[i] * (f - fR);
+        } else {
+            double u = r / R * (double)(NRAD - 1);
+            int k = (int)floor(u);
+            if (k < 0) k = 0;
+            if (k > NRAD - 2) k = NRAD - 2;
+            double t = u - (double)k;
+            rl = (1.0 - t) * RL[k] + t * RL[k + 1];
+            if (rl > 0.0) rl = 0.0;
+        }
+        double radial = exp(rl);
+        double iz = (fabs(Bc) < 1e-14) ? radial * Hh : radial * (-expm1(-Bc * Hh)) / Bc;
+        integ += r * iz;
+    }
+    double norm = (2.0 / (R2 * Hmean)) * integ * dr;
+    if (!(norm > 0.0) || !isfinite(norm)) { atomicExch(error_flag, 34); return; }
+    sed_norm[i] = norm;
+    sed_max[i] = 1.0 / norm;
+}
+
+// Majorants in bin order (:4029-4036; grid model :4203-4220 on an all-active supplied grid).
+__global__ void sediment_majorant_kernel(SedArgs a, const double* trace_geom, const double* trace_wave, double* sed_A,
+                                         double* sed_norm, double* sed_max, const double* grid, int nr, int nz,
+                                         double* major, int* error_flag) {
+    if (blockIdx.x || threadIdx.x) return;
+    const int n = a.n;
+    double mg = 0.0, mw = 0.0;
+    if (a.TM == 0) {
+        for (int i = 0; i < n; ++i) { mg += trace_geom[i]; mw += trace_wave[i]; }
+        major[0] = mg; major[1] = mw; major[2] = mg + mw; major[3] = 0.0;
+        return;
+    }
+    double maxAeq = 0.0;
+    for (int i = 0; i < n; ++i) {
+        if (sed_A[i] > maxAeq) maxAeq = sed_A[i];
+        mg += trace_geom[i] * sed_max[i];
+        mw += trace_wave[i] * sed_max[i];
+    }
+    major[0] = mg; major[1] = mw; major[2] = mg + mw; major[3] = maxAeq;
+    if (!(major[2] >= 0.0) || !isfinite(major[2])) atomicExch(error_flag, 35);
+    if (a.TM == 3 && grid) {
+        const long long plane = (long long)nr * nz;
+        for (int p = 0; p < n; ++p) {
+            double mx = 0.0;
+            for (long long c = 0; c < plane; ++c) { double q = grid[p * plane + c]; if (q > mx) mx = q; }
+            if (!(mx > 0.0)) mx = 1.0;
+            sed_norm[p] = 1.0;
+            sed_max[p] = mx;
+        }
+        mg = 0.0; mw = 0.0;
+        for (int i = 0; i < n; ++i) { mg += trace_geom[i] * sed_max[i]; mw += trace_wave[i] * sed_max[i]; }
+        major[0] = mg; major[1] = mw; major[2] = mg + mw;
+    }
+}
+
+cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,
+                                        const clr_sediment_spec& ss, double* ab_scratch, cudaStream_t st) {
+    const int n = pb.n;
+    cudaError_t e;
+    double* ab = ab_scratch ? ab_scratch : pb.ab;
+    e = cudaMemsetAsync(pb.err, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    const size_t smem = (size_t)(CLR_MIE_MAX_ORDER + 1) * sizeof(cdx);
+    e = cudaFuncSetAttribute(mie_coefficients_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    mie_coefficients_kernel<<<n, 32, smem, st>>>(pb.d, pb.nidx, pb.kidx, ps.n_medium, ps.wavelength_m, n, ab, pb.nstop,
+                                                 pb.x, pb.qext, pb.qsca, pb.qabs, pb.qback, pb.g, pb.albedo, pb.err);
+    const int em = sp.event_model;
+    if (em == 3 || em == 4 || em == 5) {
+        const int nt = pb.nt;
+        theta_grid_kernel<<<(nt + 127) / 128, 128, 0, st>>>(pb.theta, pb.theta_f, nt);
+        dim3 grid((nt + 127) / 128, (n + PDF_GROUP - 1) / PDF_GROUP);
+        phase_pdf_kernel<<<grid, 128, 0, st>>>(pb.theta, nt, n, pb.nstop, ab, pb.pdf);
+        phase_cdf_kernel<<<(n + 63) / 64, 64, 0, st>>>(pb.theta, pb.pdf, nt, n, pb.phase_cdf, pb.phase_cdf_f, pb.err);
+    } else {
+        dummy_phase_kernel<<<(n + 127) / 128, 128, 0, st>>>(pb.theta, pb.theta_f, pb.phase_cdf, pb.phase_cdf_f, n);
+    }
+    transport_kernel<<<1, 1, 0, st>>>(n, pb.d, pb.w, pb.qext, pb.qsca, pb.kidx, pb.nidx, ps.concentration_kg_m3,
+                                      ps.density_kg_m3, ps.weight_mode, em, ps.hybrid_wave_scale, ps.n_medium,
+                                      ps.wavelength_m, ps.wave_rms_height_m, pb.w, pb.radius, pb.nden, pb.mug, pb.mus,
+                                      pb.mue, pb.muw, pb.muev, pb.gcdf, pb.wcdf, pb.pcdf, pb.muscal, pb.trace_geom,
+                                      pb.trace_wave, pb.gcdf_f, pb.wcdf_f, pb.pn_f, pb.pk_f, pb.prad_f, pb.err);
+    SedArgs a;
+    a.n = n; a.TM = sp.sediment_model; a.FSM = sp.free_surface_model; a.NQ = ss.n_quad; a.NRAD = ss.n_radial;
+    a.rho_p = ss.particle_density; a.rho_w = ss.water_density; a.mu = ss.water_viscosity; a.grav = ss.gravity;
+    a.Dt = ss.eddy_diffusivity; a.R = (double)sp.rin; a.ZMIN = (double)sp.zmin; a.ZMEAN = (double)sp.zmean;
+    a.DH = (double)sp.vortex_delta_h; a.CORE = (double)sp.vortex_core_radius;
+    if (a.TM == 2 || a.TM == 3) {
+        dim3 g((a.NRAD + 127) / 128, n);
+        sediment_slip_kernel<<<g, 128, 0, st>>>(a, pb.d, pb.sed_wr);
+    }
+    sediment_bin_kernel<<<(n + 63) / 64, 64, 0, st>>>(a, pb.d, pb.sed_wr, pb.sedA, pb.sedB, pb.sed_norm, pb.sed_max,
+                                                     pb.sed_radial_log, pb.err);
+    sediment_majorant_kernel<<<1, 1, 0, st>>>(a, pb.trace_geom, pb.trace_wave, pb.sedA, pb.sed_norm, pb.sed_max,
+                                              a.TM == 3 ? pb.sed_grid : nullptr, pb.grid_nr, pb.grid_nz, pb.sed_major,
+                                              pb.err);
+    return cudaGetLastError();
+}
+
+}  // namespace clr

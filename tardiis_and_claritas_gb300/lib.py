@@ -1,0 +1,121 @@
+"""ctypes binding of libclaritas_gb.so.
+
+The library is loaded from the package's in-tree build (tardiis_and_claritas_gb300/_lib).
+There is no fallback path: if the library is missing or fails to load, every
+call raises, so a run can never silently fall back to CPU code.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import abi
+from .build_ext import LIB_PATH
+
+_lock = threading.Lock()
+_lib = None
+
+
+class ClaritasLibraryError(RuntimeError):
+    pass
+
+
+def load(build_if_missing: bool = False):
+    """Load (and optionally build) libclaritas_gb.so."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            if not build_if_missing:
+                raise ClaritasLibraryError(
+                    f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+            from .build_ext import build
+            build()
+        lib = C.CDLL(LIB_PATH)
+        P = C.POINTER
+        sig = {
+            "clr_create": ([P(C.c_void_p), C.c_int], C.c_int),
+            "clr_destroy": ([C.c_void_p], C.c_int),
+            "clr_last_error": ([C.c_void_p], C.c_char_p),
+            "clr_version": ([], C.c_char_p),
+            "clr_set_scene": ([C.c_void_p, P(abi.SceneParams)], C.c_int),
+            "clr_build_particles": ([C.c_void_p, P(abi.ParticleSpec), P(abi.SedimentSpec)], C.c_int),
+            "clr_read_particle_physics": ([C.c_void_p, P(abi.ParticlePhysics)], C.c_int),
+            "clr_trace": ([C.c_void_p, P(abi.RunParams), P(abi.Tallies), C.c_void_p], C.c_int),
+            "clr_trace_host_records": ([C.c_void_p, P(abi.RunParams), P(abi.Tallies), C.c_void_p], C.c_int),
+            "clr_abi_sizeof": ([C.c_int], C.c_int64),
+        }
+        for name, (argt, rest) in sig.items():
+            f = getattr(lib, name)
+            f.argtypes = argt
+            f.restype = rest
+        _lib = lib
+        return lib
+
+
+def exported_symbols() -> list[str]:
+    return ["clr_create", "clr_destroy", "clr_last_error", "clr_version", "clr_set_scene", "clr_build_particles",
+            "clr_read_particle_physics", "clr_trace", "clr_trace_host_records", "clr_abi_sizeof"]
+
+
+class Context:
+    """One library context (one CUDA stream, the resident tables of one scene)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        self.h = C.c_void_p()
+        rc = self.lib.clr_create(C.byref(self.h), int(device))
+        if rc != 0:
+            raise ClaritasLibraryError(f"clr_create failed ({rc}): no usable CUDA device {device}")
+        self.n_bins = 0
+        self.n_theta = 0
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.lib.clr_last_error(self.h).decode(errors="replace")
+            raise RuntimeError(f"{what} failed ({rc}): {msg}")
+
+    def set_scene(self, sp: abi.SceneParams):
+        self._check(self.lib.clr_set_scene(self.h, C.byref(sp)), "clr_set_scene")
+
+    def build_particles(self, ps: abi.ParticleSpec, ss: abi.SedimentSpec):
+        self._check(self.lib.clr_build_particles(self.h, C.byref(ps), C.byref(ss)), "clr_build_particles")
+        self.n_bins = int(ps.n_bins)
+        self.n_theta = int(ps.n_theta)
+
+    def physics(self) -> dict:
+        pp, arrays = abi.alloc_physics(self.n_bins, self.n_theta)
+        self._check(self.lib.clr_read_particle_physics(self.h, C.byref(pp)), "clr_read_particle_physics")
+        arrays["phase_cdf"] = arrays["phase_cdf"].reshape(self.n_bins, self.n_theta)
+        return arrays
+
+    def trace(self, run: abi.RunParams, records: bool = False):
+        import numpy as np
+        T = abi.Tallies()
+        rec = None
+        if records:
+            rec = np.zeros(int(run.n_rays), dtype=abi.record_dtype())
+            rc = self.lib.clr_trace_host_records(self.h, C.byref(run), C.byref(T), rec.ctypes.data_as(C.c_void_p))
+        else:
+            rc = self.lib.clr_trace(self.h, C.byref(run), C.byref(T), None)
+        self._check(rc, "clr_trace")
+        return T.as_dict(), rec
+
+    def trace_device(self, run: abi.RunParams, records_ptr: int | None = None):
+        T = abi.Tallies()
+        self._check(self.lib.clr_trace(self.h, C.byref(run), C.byref(T), C.c_void_p(records_ptr) if records_ptr else None),
+                    "clr_trace")
+        return T
+
+    def close(self):
+        if self.h:
+            self.lib.clr_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -96,6 +96,7 @@ class OracleRun:
         if rc != 0:
             msg = getattr(self.lib, self.p + "last_error")(self.h).decode()
             getattr(self.lib, self.p + "free")(self.h)
+            self.h = C.c_void_p()
             raise RuntimeError(f"{kind} oracle prepare failed ({rc}): {msg}")
         self.n_bins = particles.diameter_m.size
         self.n_theta = getattr(self.lib, self.p + "n_theta")(self.h)

@@ -1,0 +1,161 @@
+"""GPU parity: the library's CUDA path against the reference's own kernels and the CPU oracle.
+
+1. Bit-exact: in the reference xorshift mode every per-ray record (status, all
+   event counters, failure codes, detector ids, air-exit position/direction,
+   path lengths) and every physics table must equal the reference's
+   trace_kernel/score_detectors_kernel output on the same GPU
+   (tests/golden/gpu_ref_fixtures.npz, made by tests/golden/make_gpu_fixtures.py).
+2. Statistical: detector tallies agree with the CPU oracle within 3 combined
+   standard errors at fixed photon counts (CPU and GPU libm differ, so histories
+   are not identical ray by ray), and the Philox production stream agrees with
+   the xorshift stream the same way.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+import parity_scenes as PS
+from tardiis_and_claritas_gb300 import abi, scene as S
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "gpu_ref_fixtures.npz")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from tardiis_and_claritas_gb300 import lib as L
+    from tardiis_and_claritas_gb300.build_ext import build
+    build()
+    c = L.Context(0)
+    yield c
+    c.close()
+
+
+def prepare(ctx, name):
+    cfg, parts, grid = PS.build(name)
+    ctx.set_scene(cfg.to_scene_params())
+    ps, ss = parts.spec(cfg), cfg.sediment_spec(grid)
+    ctx.build_particles(ps, ss)
+    return cfg, parts
+
+
+@pytest.fixture(scope="module")
+def gold():
+    if not os.path.exists(GOLD):
+        pytest.skip("tests/golden/gpu_ref_fixtures.npz not generated yet")
+    z = np.load(GOLD)
+    return z, json.loads(bytes(z["meta"]).decode())
+
+
+def first_mismatch(rec, compact_ref):
+    mine = PS.compact(rec, compact_ref.shape[0]).astype(np.int16)
+    bad = np.nonzero(np.any(mine != compact_ref, axis=1))[0]
+    if bad.size == 0:
+        return "first compact records agree; mismatch is later or in float fields"
+    i = int(bad[0])
+    return f"ray {i}: mine {dict(zip(PS.COMPACT_FIELDS, mine[i].tolist()))} ref {dict(zip(PS.COMPACT_FIELDS, compact_ref[i].tolist()))}"
+
+
+@pytest.mark.parametrize("name", list(PS.SCENES))
+def test_bit_exact_against_reference_kernels(ctx, gold, name):
+    z, meta = gold
+    m = meta["scenes"][name]
+    prepare(ctx, name)
+    ph = ctx.physics()
+    mism = [k for k, v in PS.physics_digests(ph).items() if v != m["physics_sha256"][k]]
+    assert not mism, f"{name}: physics tables differ from the reference kernels: {mism}"
+    tal, rec = ctx.trace(S.run_params(meta["n_rays"], seed=m["seed"]), records=True)
+    for k in PS.TALLY_KEYS:
+        np.testing.assert_array_equal(tal[k], z[f"{name}/{k}"], err_msg=f"{name}: {k}")
+    assert tal["event_counts"][:PS.EVENT_KEYS].tolist() == m["event_counts"]
+    assert [int(v) for v in tal["conditional_stats"]] == m["conditional_stats"]
+    assert PS.records_digest(rec) == m["records_sha256"], first_mismatch(rec, z[f"{name}/compact"])
+
+
+def _se_compare(a_counts, a_n, b_counts, b_n, k=3.0, floor=0):
+    """Per-channel binomial proportions agree within k combined standard errors."""
+    pa, pb = a_counts / a_n, b_counts / b_n
+    se = np.sqrt(pa * (1 - pa) / a_n + pb * (1 - pb) / b_n)
+    se = np.maximum(se, 1.0 / max(a_n, b_n))
+    z = np.abs(pa - pb) / se
+    keep = (a_counts + b_counts) > floor
+    return z[keep], keep
+
+
+@pytest.mark.parametrize("name", ["c1_smooth_coherent", "rough_spheroid", "absorbing_conditional", "schiller_sediment"])
+def test_tallies_agree_with_cpu_oracle(ctx, name):
+    import oracle_harness as H
+    cfg, parts, grid = PS.build(name)
+    prepare(ctx, name)
+    n = 400_000
+    gpu, _ = ctx.trace(S.run_params(n, seed=11))
+    orc = H.OracleRun("port", cfg, parts, grid=grid)
+    cpu, _ = orc.trace(S.run_params(n, seed=12))
+    for key in ("hw_native", "hw_mirror", "status_counts"):
+        z, _ = _se_compare(gpu[key].astype(float), n, cpu[key].astype(float), n)
+        # 3 SE per channel; with ~25 channels allow at most one 3-4 SE excursion and none beyond 4.5
+        assert np.max(z) < 4.5 and np.sum(z > 3.0) <= 1, f"{name} {key}: z={np.round(z, 2)}"
+
+
+def test_philox_stream_agrees_with_xorshift(ctx):
+    prepare(ctx, "rough_spheroid")
+    n = 400_000
+    a, _ = ctx.trace(S.run_params(n, seed=3, rng_mode=abi.RNG_REFERENCE_XORSHIFT))
+    b, _ = ctx.trace(S.run_params(n, seed=3, rng_mode=abi.RNG_PHILOX))
+    for key in ("hw_native", "status_counts"):
+        z, _ = _se_compare(a[key].astype(float), n, b[key].astype(float), n)
+        assert np.max(z) < 4.5 and np.sum(z > 3.0) <= 1, f"{key}: z={np.round(z, 2)}"
+
+
+def test_philox_is_partition_independent(ctx):
+    """Counter-based streams: tallies of [0,N) equal the sum of [0,N/2) and [N/2,N)."""
+    prepare(ctx, "rough_spheroid")
+    n = 100_000
+    full, _ = ctx.trace(S.run_params(n, seed=5, rng_mode=abi.RNG_PHILOX))
+    h1, _ = ctx.trace(S.run_params(n // 2, seed=5, rng_mode=abi.RNG_PHILOX))
+    h2, _ = ctx.trace(S.run_params(n - n // 2, seed=5, rng_mode=abi.RNG_PHILOX, ray_offset=n // 2))
+    for k in PS.TALLY_KEYS:
+        np.testing.assert_array_equal(full[k], h1[k] + h2[k], err_msg=k)
+
+
+def test_chunking_does_not_change_results(ctx):
+    """Work-queue granularity and grid size change scheduling only, never outcomes."""
+    prepare(ctx, "absorbing_conditional")
+    n = 50_000
+    a, ra = ctx.trace(S.run_params(n, seed=9, rays_per_item=64), records=True)
+    b, rb = ctx.trace(S.run_params(n, seed=9, rays_per_item=1024, max_blocks=3), records=True)
+    assert PS.records_digest(ra) == PS.records_digest(rb)
+    for k in PS.TALLY_KEYS:
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_record_and_tally_paths_agree(ctx):
+    prepare(ctx, "rough_spheroid")
+    run = S.run_params(30_000, seed=21)
+    a, rec = ctx.trace(run, records=True)
+    b, _ = ctx.trace(run, records=False)
+    for k in PS.TALLY_KEYS:
+        np.testing.assert_array_equal(a[k], b[k])
+    st = np.bincount(rec["status"], minlength=abi.N_STATUS)
+    np.testing.assert_array_equal(st, a["status_counts"])
+    nat = np.bincount(rec["native_id"][rec["native_id"] >= 0], minlength=18)
+    np.testing.assert_array_equal(nat, a["hw_native"])
+
+
+def test_empty_run(ctx):
+    prepare(ctx, "c1_smooth_coherent")
+    t, rec = ctx.trace(S.run_params(0), records=True)
+    assert t["n_rays"] == 0 and t["status_counts"].sum() == 0 and rec.size == 0
+
+
+def test_precompute_error_is_reported(ctx):
+    cfg = S.small_cell_config()
+    ctx.set_scene(cfg.to_scene_params())
+    big = S.Particles([5e-3], [1.0], [1.5], [0.0], 1.0)  # size parameter beyond MIE_MAX_ORDER
+    with pytest.raises(RuntimeError, match="error code 1"):
+        ctx.build_particles(big.spec(cfg), cfg.sediment_spec())

@@ -1,0 +1,112 @@
+"""CPU tests of the oracle (our C restatement) against the reference's own code.
+
+The golden file tests/golden/cpu_ref_fixtures.npz was produced by the
+reference's CUDA_SRC compiled for the host (tests/golden/make_cpu_fixtures.py).
+The restatement must reproduce it bit for bit on the platform it was made on:
+every per-ray record (digest), every physics table (digest) and every tally.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import platform
+
+import numpy as np
+import pytest
+
+import oracle_harness as H
+import parity_scenes as PS
+from tardiis_and_claritas_gb300 import scene as S
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "cpu_ref_fixtures.npz")
+
+
+@pytest.fixture(scope="module")
+def gold():
+    z = np.load(GOLD)
+    meta = json.loads(bytes(z["meta"]).decode())
+    return z, meta
+
+
+def test_erfinv_matches_scipy():
+    special = pytest.importorskip("scipy.special")
+    lib, _ = H.load("port")
+    ys = np.concatenate([np.linspace(-0.999999, 0.999999, 2001), [1e-300, -1e-12, 0.5, 0.9999999999, -0.9999999999]])
+    got = np.array([lib.clo_erfinv(float(y)) for y in ys])
+    want = special.erfinv(ys)
+    assert np.allclose(got, want, rtol=4e-15, atol=1e-300)
+
+
+def test_philox_known_answers():
+    """Published Philox4x32-10 test vectors (Random123 distribution, kat_vectors)."""
+    lib, _ = H.load("port")
+
+    def kat(key, ctr):
+        k = (C.c_uint32 * 2)(*key)
+        c = (C.c_uint32 * 4)(*ctr)
+        o = (C.c_uint32 * 4)()
+        lib.clo_philox4x32_10(k, c, o)
+        return list(o)
+
+    assert kat([0, 0], [0, 0, 0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert kat([0xFFFFFFFF] * 2, [0xFFFFFFFF] * 4) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+    assert kat([0xA4093822, 0x299F31D0], [0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344]) == [
+        0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+@pytest.mark.parametrize("name", list(PS.SCENES))
+def test_oracle_matches_reference_fixture(gold, name):
+    z, meta = gold
+    m = meta["scenes"][name]
+    cfg, parts, grid = PS.build(name)
+    orc = H.OracleRun("port", cfg, parts, grid=grid)
+    ph = orc.physics()
+    tal, rec = orc.trace(S.run_params(meta["n_rays"], seed=PS.seed_of(name)), records=True)
+    orc.close()
+    # integer outcomes: exact on any platform
+    for k in PS.TALLY_KEYS:
+        np.testing.assert_array_equal(tal[k], z[f"{name}/{k}"], err_msg=f"{name}: tally {k}")
+    assert tal["event_counts"][:PS.EVENT_KEYS].tolist() == m["event_counts"]
+    assert [int(v) for v in tal["conditional_stats"]] == m["conditional_stats"]
+    np.testing.assert_array_equal(PS.compact(rec, meta["n_compact"]).astype(np.int16), z[f"{name}/compact"])
+    # full bitwise record and table identity on the platform the fixture was generated on
+    if platform.machine() == meta["machine"]:
+        assert PS.records_digest(rec) == m["records_sha256"], f"{name}: per-ray records differ"
+        assert PS.physics_digests(ph) == m["physics_sha256"], f"{name}: physics tables differ"
+
+
+@pytest.mark.skipif(not H.reference_available(), reason="host build of the reference not present (no checkout)")
+@pytest.mark.parametrize("name", ["rough_spheroid", "absorbing_conditional", "scully_surface", "grid_sediment"])
+def test_oracle_matches_live_reference(name):
+    """Larger run against the live host build of the reference, when it could be built here."""
+    cfg, parts, grid = PS.build(name)
+    a = H.OracleRun("port", cfg, parts, grid=grid)
+    b = H.OracleRun("reference", cfg, parts, grid=grid)
+    pa, pb = a.physics(), b.physics()
+    for k in pa:
+        np.testing.assert_array_equal(pa[k], pb[k], err_msg=k)
+    run = S.run_params(50000, seed=7, ray_offset=123456)
+    ta, ra = a.trace(run, records=True)
+    tb, rb = b.trace(run, records=True)
+    assert PS.records_digest(ra) == PS.records_digest(rb)
+    for k in PS.TALLY_KEYS:
+        np.testing.assert_array_equal(ta[k], tb[k])
+
+
+def test_oracle_rejects_unsupported_modes():
+    cfg, parts, grid = PS.build("c1_smooth_coherent")
+    orc = H.OracleRun("port", cfg, parts)
+    with pytest.raises(RuntimeError):
+        orc.trace(S.run_params(10, rng_mode=1))
+
+
+def test_oracle_empty_run_and_precompute_errors():
+    cfg, parts, _ = PS.build("c1_smooth_coherent")
+    orc = H.OracleRun("port", cfg, parts)
+    tal, rec = orc.trace(S.run_params(0), records=True)
+    assert tal["n_rays"] == 0 and tal["status_counts"].sum() == 0 and rec.size == 0
+    # a size parameter beyond the Mie order limit is a precompute error (reference error code 1, :3510)
+    big = S.Particles([5e-3], [1.0], [1.5], [0.0], 1.0)
+    with pytest.raises(RuntimeError, match="Mie"):
+        H.OracleRun("port", cfg, big)
