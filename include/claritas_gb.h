@@ -185,6 +185,34 @@ enum {
     CLR_EV_RESERVED
 };
 
+#define CLR_N_SUBCODES 96
+#define CLR_IC_HIST 1024
+
+/* indices into clr_tallies.entered_sums (over rays with entered_water > 0) */
+enum {
+    CLR_ES_IC = 0, CLR_ES_GIC, CLR_ES_WIC, CLR_ES_WCOH, CLR_ES_WMORPH, CLR_ES_PR, CLR_ES_CIR, CLR_ES_COR,
+    CLR_ES_TOP, CLR_ES_BIR, CLR_ES_BOR, CLR_ES_CTIR, CLR_ES_TTIR, CLR_ES_BTIR, CLR_ES_PER, CLR_ES_PIR
+};
+/* indices into clr_tallies.ray_flags */
+enum {
+    CLR_RF_ENTERED = 0, CLR_RF_BALLISTIC, CLR_RF_ENTRY_REFLECTED, CLR_RF_INTERNAL_REFLECTED, CLR_RF_ABSORBED,
+    CLR_RF_CELL_TIR, CLR_RF_TOP_TIR, CLR_RF_BOTTOM_TIR, CLR_RF_SOURCE_ACCEPTED, CLR_RF_SOURCE_DIRECT,
+    CLR_RF_SOURCE_REFLECTED, CLR_RF_VALID_AIR, CLR_RF_TRAPPED
+};
+
+/* Compact index of a production failure subcode (CLARITAS/CLARITAS.py:1808-1895):
+ * 0..47 themselves; 1001..1007 -> 48..54; 1101..1107 -> 55..61; 2001..2002 -> 62..63;
+ * 2101..2104 -> 64..67; 3001..3006 -> 68..73; 4001 -> 74; 9001..9003 -> 75..77; other -> 95. */
+#define CLR_SUBCODE_INDEX(s)                                                              \
+    (((s) >= 0 && (s) < 48) ? (s)                                                         \
+     : ((s) >= 1001 && (s) <= 1007) ? 48 + (s) - 1001                                     \
+     : ((s) >= 1101 && (s) <= 1107) ? 55 + (s) - 1101                                     \
+     : ((s) >= 2001 && (s) <= 2002) ? 62 + (s) - 2001                                     \
+     : ((s) >= 2101 && (s) <= 2104) ? 64 + (s) - 2101                                     \
+     : ((s) >= 3001 && (s) <= 3006) ? 68 + (s) - 3001                                     \
+     : ((s) == 4001) ? 74                                                                 \
+     : ((s) >= 9001 && (s) <= 9003) ? 75 + (s) - 9001 : 95)
+
 /* Detector tallies of one run. Integer counts are exact; float sums are FP64. */
 typedef struct clr_tallies {
     int64_t n_rays;
@@ -201,8 +229,14 @@ typedef struct clr_tallies {
     int64_t failure_code_counts[CLR_N_FAILURE_CODES];
     int64_t event_counts[CLR_N_EVENT_COUNTERS];
     uint64_t conditional_stats[CLR_N_CONDITIONAL_STATS];
-    int32_t device_error;           /* nonzero if a bounded device wait gave up */
+    int32_t device_error;           /* nonzero if the kernel did not account for every ray */
     int32_t reserved[7];
+    /* per-ray statistics the reference's host derives from its per-ray arrays (simulate,
+     * CLARITAS/CLARITAS.py:8659-8735); see CLR_ES_* and CLR_RF_* for the indices */
+    int64_t entered_sums[16];       /* sums over rays that entered the water */
+    int64_t ray_flags[16];          /* counts of rays satisfying a predicate */
+    int64_t failure_subcode_counts[CLR_N_SUBCODES];  /* indexed by clr_subcode_index() */
+    int64_t ic_hist[CLR_IC_HIST];   /* interaction count of entered rays; last bin = overflow */
 } clr_tallies;
 
 /* Host copies of the particle-physics tables (diagnostics and parity checks).

@@ -14,6 +14,7 @@
 #define _GNU_SOURCE
 #include "claritas_oracle.h"
 #include "oracle_transport_b.h"
+#include "tally_extras.h"
 
 #include <stdio.h>
 #include <stdlib.h>
@@ -1149,6 +1150,7 @@ static void tally_merge(clr_tallies* dst, const clr_tallies* src) {
     for (int k = 0; k < CLR_N_STATUS; ++k) dst->status_counts[k] += src->status_counts[k];
     for (int k = 0; k < CLR_N_FAILURE_CODES; ++k) dst->failure_code_counts[k] += src->failure_code_counts[k];
     for (int k = 0; k < CLR_N_EVENT_COUNTERS; ++k) dst->event_counts[k] += src->event_counts[k];
+    clr_tally_merge_extras(dst, src);
     (void)d; (void)s;
 }
 
@@ -1166,15 +1168,19 @@ int clo_trace(clo_state* S, const clr_run_params* run, clr_tallies* T, clr_ray_r
     const int64_t n = run->n_rays;
 #pragma omp parallel
     {
-        clr_tallies L;
-        memset(&L, 0, sizeof L);
+        clr_tallies* Lp = (clr_tallies*)calloc(1, sizeof(clr_tallies));
+        clr_tallies L_dummy;
+        (void)L_dummy;
+#define L (*Lp)
         unsigned long long cs[10] = {0};
 #pragma omp for schedule(dynamic, 1024)
         for (int64_t i = 0; i < n; ++i) {
             uint32_t gid = run->ray_offset + (uint32_t)i;
             o_ray r;
             o_trace_ray(S, gid, run->seed0, run->seed1, run->seed2, cs, &r);
-            clr_ray_record* rec = records ? &records[i] : NULL;
+            clr_ray_record tmp;
+            memset(&tmp, 0, sizeof tmp);
+            clr_ray_record* rec = &tmp;
             o_score(&S->sp, run->detector_seed, gid, &r, &L, rec);
             if (r.st >= 0 && r.st < CLR_N_STATUS) L.status_counts[r.st]++;
             if (r.pf >= 0 && r.pf < CLR_N_FAILURE_CODES) L.failure_code_counts[r.pf]++;
@@ -1184,21 +1190,23 @@ int clo_trace(clo_state* S, const clr_run_params* run, clr_tallies* T, clr_ray_r
             for (int k = 0; k < 20; ++k) L.event_counts[k] += ev[k];
             L.event_counts[CLR_EV_WATER_STEPS] += r.steps;
             L.event_counts[CLR_EV_NULL_COLLISIONS] += r.nulls;
-            if (rec) {
-                rec->status = r.st;
-                int32_t* ri = &rec->interaction_count;
-                for (int k = 0; k < 20; ++k) ri[k] = ev[k];
-                rec->failure_code = r.pf; rec->failure_subcode = r.pfs;
-                rec->air_x = r.ax; rec->air_y = r.ay; rec->air_z = r.az;
-                rec->air_vx = r.avx; rec->air_vy = r.avy; rec->air_vz = r.avz;
-                rec->water_path = r.wp; rec->acrylic_path = r.ap;
-            }
+            rec->status = r.st;
+            int32_t* ri = &rec->interaction_count;
+            for (int k = 0; k < 20; ++k) ri[k] = ev[k];
+            rec->failure_code = r.pf; rec->failure_subcode = r.pfs;
+            rec->air_x = r.ax; rec->air_y = r.ay; rec->air_z = r.az;
+            rec->air_vx = r.avx; rec->air_vy = r.avy; rec->air_vz = r.avz;
+            rec->water_path = r.wp; rec->acrylic_path = r.ap;
+            clr_tally_add_ray_stats(&L, rec);
+            if (records) records[i] = tmp;
         }
 #pragma omp critical
         {
             tally_merge(T, &L);
             for (int k = 0; k < 10; ++k) cstats[k] += cs[k];
         }
+#undef L
+        free(Lp);
     }
     T->n_rays = n;
     for (int k = 0; k < 10; ++k) T->conditional_stats[k] = cstats[k];

@@ -14,6 +14,7 @@
 #include <string>
 #include <cuda_runtime.h>
 #include "claritas_gb.h"
+#include "tally_extras.h"
 
 #include "_ref/claritas_cuda_src.inc"
 
@@ -306,8 +307,10 @@ int clrefgpu_trace(void* h, const clr_run_params* run, clr_tallies* T, clr_ray_r
             int pf = hi[21][i];
             if (pf >= 0 && pf < CLR_N_FAILURE_CODES) T->failure_code_counts[pf]++;
             for (int k = 0; k < 20; ++k) T->event_counts[k] += hi[k][i];
-            if (records) {
-                clr_ray_record& r = records[start + i];
+            {
+                clr_ray_record tmp;
+                memset(&tmp, 0, sizeof tmp);
+                clr_ray_record& r = tmp;
                 int32_t* ri = &r.status;
                 ri[0] = st;
                 for (int k = 0; k < 20; ++k) ri[1 + k] = hi[k][i];
@@ -316,6 +319,8 @@ int clrefgpu_trace(void* h, const clr_run_params* run, clr_tallies* T, clr_ray_r
                 r.air_x = hf[0][i]; r.air_y = hf[1][i]; r.air_z = hf[2][i];
                 r.air_vx = hf[3][i]; r.air_vy = hf[4][i]; r.air_vz = hf[5][i];
                 r.water_path = hf[6][i]; r.acrylic_path = hf[7][i];
+                clr_tally_add_ray_stats(T, &r);
+                if (records) records[start + i] = tmp;
             }
         }
     }

@@ -29,6 +29,7 @@
 #endif
 
 #include "claritas_gb.h"
+#include "tally_extras.h"
 
 thread_local ref_dim3 threadIdx = {0, 0, 0};
 thread_local ref_dim3 blockIdx = {0, 0, 0};
@@ -328,9 +329,11 @@ int clref_trace(clref_state* h, const clr_run_params* run, clr_tallies* T, clr_r
             if (pf >= 0 && pf < CLR_N_FAILURE_CODES) T->failure_code_counts[pf]++;
             for (int k = 0; k < 20; ++k) T->event_counts[k] += I[k][i];
         }
-        if (records) {
+        {
             for (int i = 0; i < n; ++i) {
-                clr_ray_record& r = records[start + i];
+                clr_ray_record tmp;
+                memset(&tmp, 0, sizeof tmp);
+                clr_ray_record& r = tmp;
                 int32_t* ri = &r.status;
                 /* record order: status, then outi[0..19], then failure code/subcode */
                 ri[0] = I[20][i];
@@ -340,6 +343,8 @@ int clref_trace(clref_state* h, const clr_run_params* run, clr_tallies* T, clr_r
                 r.air_x = F[0][i]; r.air_y = F[1][i]; r.air_z = F[2][i];
                 r.air_vx = F[3][i]; r.air_vy = F[4][i]; r.air_vz = F[5][i];
                 r.water_path = F[6][i]; r.acrylic_path = F[7][i];
+                clr_tally_add_ray_stats(T, &r);
+                if (records) records[start + i] = tmp;
             }
         }
     }

@@ -15,6 +15,34 @@ N_STATUS = 16
 N_FAILURE_CODES = 32
 N_EVENT_COUNTERS = 24
 N_CONDITIONAL_STATS = 10
+N_SUBCODES = 96
+IC_HIST = 1024
+ES_NAMES = ["ic", "gic", "wic", "wcoh", "wmorph", "pr", "cir", "cor", "top", "bir", "bor", "ctir", "ttir", "btir",
+            "per", "pir"]
+RF_NAMES = ["entered", "ballistic", "entry_reflected", "internal_reflected", "absorbed", "cell_tir", "top_tir",
+            "bottom_tir", "source_accepted", "source_direct", "source_reflected", "valid_air", "trapped"]
+
+
+def subcode_index(s: int) -> int:
+    """Compact index of a production failure subcode (CLR_SUBCODE_INDEX in include/claritas_gb.h)."""
+    if 0 <= s < 48:
+        return s
+    for lo, hi, base in ((1001, 1007, 48), (1101, 1107, 55), (2001, 2002, 62), (2101, 2104, 64), (3001, 3006, 68),
+                         (4001, 4001, 74), (9001, 9003, 75)):
+        if lo <= s <= hi:
+            return base + s - lo
+    return 95
+
+
+def subcode_of_index(i: int) -> int:
+    """Inverse of subcode_index for the named ranges (95 maps to -1: 'other')."""
+    if i < 48:
+        return i
+    for lo, hi, base in ((1001, 1007, 48), (1101, 1107, 55), (2001, 2002, 62), (2101, 2104, 64), (3001, 3006, 68),
+                         (4001, 4001, 74), (9001, 9003, 75)):
+        if base <= i <= base + hi - lo:
+            return lo + i - base
+    return -1
 
 CLR_OK = 0
 CLR_ERR_INVALID_ARGUMENT = -1
@@ -130,6 +158,8 @@ class Tallies(C.Structure):
         ("event_counts", i64 * N_EVENT_COUNTERS),
         ("conditional_stats", u64 * N_CONDITIONAL_STATS),
         ("device_error", i32), ("reserved", i32 * 7),
+        ("entered_sums", i64 * 16), ("ray_flags", i64 * 16),
+        ("failure_subcode_counts", i64 * N_SUBCODES), ("ic_hist", i64 * IC_HIST),
     ]
 
     def as_dict(self) -> dict:

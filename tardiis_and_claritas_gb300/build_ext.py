@@ -24,6 +24,14 @@ LIB_PATH = os.path.join(LIB_DIR, "libclaritas_gb.so")
 SOURCES = ["clr_api.cu", "precompute.cu", "trace_xor.cu", "trace_philox.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"] + ARCH
+# Per-unit flags. The FP64 precompute and the xorshift parity kernels are compiled without
+# multiply-add contraction: their results are then fixed by the source's operation order alone,
+# which is the reference's, instead of by where the compiler happens to fuse a*b+c (that depends
+# on inlining and common-subexpression context, which necessarily differ between two programs).
+# The Philox production kernels keep contraction.
+UNIT_FLAGS: dict = {"precompute.cu": ["-fmad=false"], "trace_xor.cu": ["-fmad=false"]}
+if os.environ.get("CLR_ALL_NOFMA"):
+    UNIT_FLAGS = {s: ["-fmad=false"] for s in SOURCES}
 
 
 def nvcc() -> str:
@@ -36,6 +44,7 @@ def nvcc() -> str:
 def _digest() -> str:
     h = hashlib.sha256()
     h.update(" ".join(NVCC_FLAGS).encode())
+    h.update(repr(sorted(UNIT_FLAGS.items())).encode())
     for d in (CSRC, INCLUDE):
         for name in sorted(os.listdir(d)):
             if name.endswith((".cu", ".cuh", ".h")):
@@ -58,7 +67,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
 
     def compile_one(src: str):
         obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
-        cmd = [cc] + NVCC_FLAGS + ["-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [cc] + NVCC_FLAGS + UNIT_FLAGS.get(src, []) + ["-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         with open(os.path.join(BUILD_DIR, src + ".log"), "w") as f:
             f.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)

@@ -255,7 +255,8 @@ static void fill_scene(const clr_ctx* ctx, const clr_run_params* run, DevScene* 
     s->roulette_threshold = run->roulette_threshold; s->roulette_survival = run->roulette_survival;
 }
 
-static void tally_to_host(const DevTally& t, clr_tallies* out, int64_t n_rays) {
+static void tally_to_host(const DevTally& d, clr_tallies* out, int64_t n_rays) {
+    const TallyCore& t = d.c;
     memset(out, 0, sizeof *out);
     out->n_rays = n_rays;
     for (int j = 0; j < CLR_N_DETECTORS; ++j) {
@@ -273,6 +274,9 @@ static void tally_to_host(const DevTally& t, clr_tallies* out, int64_t n_rays) {
     for (int k = 0; k < CLR_N_FAILURE_CODES; ++k) out->failure_code_counts[k] = (int64_t)t.failure[k];
     for (int k = 0; k < CLR_N_EVENT_COUNTERS; ++k) out->event_counts[k] = (int64_t)t.events[k];
     for (int k = 0; k < CLR_N_CONDITIONAL_STATS; ++k) out->conditional_stats[k] = t.cstats[k];
+    for (int k = 0; k < 16; ++k) { out->entered_sums[k] = (int64_t)t.entered_sums[k]; out->ray_flags[k] = (int64_t)t.ray_flags[k]; }
+    for (int k = 0; k < CLR_N_SUBCODES; ++k) out->failure_subcode_counts[k] = (int64_t)t.subcodes[k];
+    for (int k = 0; k < CLR_IC_HIST; ++k) out->ic_hist[k] = (int64_t)d.ic_hi[k] + (k < 64 ? (int64_t)t.ic_lo[k] : 0);
     out->device_error = (t.n_done == (unsigned long long)n_rays) ? 0 : 1;
 }
 

@@ -44,8 +44,9 @@ struct DevScene {
     int32_t pad;
 };
 
-// Per-scenario tallies in device memory (64-bit counters, FP64 sums).
-struct DevTally {
+// Tally counters shared by the per-warp shared-memory tally and the per-scenario device tally.
+// Layout: hw block, FP64 sums, then a contiguous tail of 64-bit counters.
+struct TallyCore {
     unsigned long long hw[10][CLR_N_DETECTORS];   // native, mirror, nat direct, mir direct, nat stray, mir stray,
                                                   // nat face, mir face, legacy native, legacy mirror
     double sums[8][CLR_N_DETECTORS];              // photodiode nat/mir, incidence nat/mir, weight nat/mir, w^2 nat/mir
@@ -54,6 +55,18 @@ struct DevTally {
     unsigned long long events[CLR_N_EVENT_COUNTERS];
     unsigned long long cstats[CLR_N_CONDITIONAL_STATS];
     unsigned long long n_done;
+    unsigned long long entered_sums[16];
+    unsigned long long ray_flags[16];
+    unsigned long long subcodes[CLR_N_SUBCODES];
+    unsigned long long ic_lo[64];                 // interaction-count histogram, counts 0..63
+};
+#define CLR_TALLY_TAIL (CLR_N_STATUS + CLR_N_FAILURE_CODES + CLR_N_EVENT_COUNTERS + CLR_N_CONDITIONAL_STATS + 1 + 16 + 16 + CLR_N_SUBCODES + 64)
+
+// Per-scenario tallies in device memory: the core plus the high part of the histogram
+// (interaction counts >= 64, clamped to the last bin), updated with global atomics.
+struct DevTally {
+    TallyCore c;
+    unsigned long long ic_hi[CLR_IC_HIST];
 };
 
 }  // namespace clr

@@ -37,16 +37,7 @@ __device__ __forceinline__ void ray_reset(Ray& r) {
 }
 
 // per-warp shared tally region (64-bit counters; flushed to the owning scenario's DevTally)
-struct WarpTally {
-    unsigned long long hw[10][CLR_N_DETECTORS];
-    double sums[8][CLR_N_DETECTORS];
-    unsigned long long status[CLR_N_STATUS];
-    unsigned long long failure[CLR_N_FAILURE_CODES];
-    unsigned long long events[CLR_N_EVENT_COUNTERS];
-    unsigned long long cstats[CLR_N_CONDITIONAL_STATS];
-    unsigned long long n_done;
-};
-static_assert(sizeof(WarpTally) == sizeof(DevTally), "tally layouts must match");
+typedef TallyCore WarpTally;
 
 // offsets inside WarpTally/DevTally counter space (in units of unsigned long long after hw)
 #define CLR_OFF_HW(k, j) ((k) * CLR_N_DETECTORS + (j))
@@ -55,6 +46,10 @@ static_assert(sizeof(WarpTally) == sizeof(DevTally), "tally layouts must match")
 #define CLR_OFF_EV (CLR_OFF_FAIL + CLR_N_FAILURE_CODES)
 #define CLR_OFF_CS (CLR_OFF_EV + CLR_N_EVENT_COUNTERS)
 #define CLR_OFF_DONE (CLR_OFF_CS + CLR_N_CONDITIONAL_STATS)
+#define CLR_OFF_ES (CLR_OFF_DONE + 1)
+#define CLR_OFF_RF (CLR_OFF_ES + 16)
+#define CLR_OFF_SUB (CLR_OFF_RF + 16)
+#define CLR_OFF_ICLO (CLR_OFF_SUB + CLR_N_SUBCODES)
 
 // ---------------- conditional closure (:4479-4536) ----------------
 struct Hist {

@@ -163,11 +163,12 @@ __device__ __forceinline__ TallySink tally_sink(T* t) {
     s.tail = &t->status[0];
     return s;
 }
+__device__ __forceinline__ TallySink tally_sink_dev(DevTally* t) { return tally_sink(&t->c); }
 
 // Score a finished history and add it to `sink` (:4390-4436, tallies :7849-7862).
 template <class Mode>
 __device__ __forceinline__ void finish_ray(const DevScene& D, const Ray& r, uint32_t gid, const TallySink& sink,
-                                           clr_ray_record* rec) {
+                                           unsigned long long* ic_hi, clr_ray_record* rec) {
     const clr_scene_params& P = D.P;
     int ni = -1, mi = -1, nb = 0, mb = 0, nfb = 0, mfb = 0;
     if (r.st == 1 && isfinite(r.x) && isfinite(r.y) && isfinite(r.z) && isfinite(r.vx) && isfinite(r.vy) &&
@@ -243,6 +244,32 @@ __device__ __forceinline__ void finish_ray(const DevScene& D, const Ray& r, uint
     for (int k = 0; k < 22; ++k)
         if (ev[k]) sink.add_u(CLR_OFF_EV + k, (unsigned long long)(unsigned)ev[k]);
     sink.add_u(CLR_OFF_DONE, 1ull);
+    // per-ray statistics of the reference host (:8483-8508, :8665-8735)
+    if (r.pf != 0) sink.add_u(CLR_OFF_SUB + CLR_SUBCODE_INDEX(r.pfs), 1ull);
+    if (st != 3) {
+        sink.add_u(CLR_OFF_RF + CLR_RF_SOURCE_ACCEPTED, 1ull);
+        sink.add_u(CLR_OFF_RF + (r.sbr == 0 ? CLR_RF_SOURCE_DIRECT : CLR_RF_SOURCE_REFLECTED), 1ull);
+    }
+    if (st == 1 && isfinite(r.x) && isfinite(r.vx)) sink.add_u(CLR_OFF_RF + CLR_RF_VALID_AIR, 1ull);
+    if (st == 8) sink.add_u(CLR_OFF_RF + CLR_RF_TRAPPED, 1ull);
+    if (r.entered) {
+        sink.add_u(CLR_OFF_RF + CLR_RF_ENTERED, 1ull);
+        if (r.ic == 0) sink.add_u(CLR_OFF_RF + CLR_RF_BALLISTIC, 1ull);
+        if (r.pc.entry_reflections > 0) sink.add_u(CLR_OFF_RF + CLR_RF_ENTRY_REFLECTED, 1ull);
+        if (r.pc.internal_reflections > 0) sink.add_u(CLR_OFF_RF + CLR_RF_INTERNAL_REFLECTED, 1ull);
+        if (r.pc.absorptions > 0) sink.add_u(CLR_OFF_RF + CLR_RF_ABSORBED, 1ull);
+        if (r.ctir > 0) sink.add_u(CLR_OFF_RF + CLR_RF_CELL_TIR, 1ull);
+        if (r.ttir > 0) sink.add_u(CLR_OFF_RF + CLR_RF_TOP_TIR, 1ull);
+        if (r.btir > 0) sink.add_u(CLR_OFF_RF + CLR_RF_BOTTOM_TIR, 1ull);
+        const int es[16] = {r.ic, r.gic, r.wic, r.wcoh, r.wmorph, r.pc.reflections, r.cir, r.cor, r.tr, r.bir, r.bor,
+                            r.ctir, r.ttir, r.btir, r.pc.entry_reflections, r.pc.internal_reflections};
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+            if (es[k]) sink.add_u(CLR_OFF_ES + k, (unsigned long long)(unsigned)es[k]);
+        const int ic = r.ic < 0 ? 0 : r.ic;
+        if (ic < 64) sink.add_u(CLR_OFF_ICLO + ic, 1ull);
+        else atomicAdd(ic_hi + (ic < CLR_IC_HIST - 1 ? ic : CLR_IC_HIST - 1), 1ull);
+    }
     if (rec) {
         clr_ray_record o;
         o.status = st;
@@ -304,22 +331,20 @@ struct PhiloxMode {
 
 __device__ __forceinline__ void flush_warp_tally(WarpTally* t, DevTally* dst, int lane) {
     unsigned long long* su = &t->hw[0][0];
-    unsigned long long* du = &dst->hw[0][0];
-    const int n_u_before = 10 * CLR_N_DETECTORS;
-    for (int i = lane; i < n_u_before; i += 32) {
+    unsigned long long* du = &dst->c.hw[0][0];
+    for (int i = lane; i < 10 * CLR_N_DETECTORS; i += 32) {
         unsigned long long v = su[i];
         if (v) { atomicAdd(du + i, v); su[i] = 0ull; }
     }
     double* sd = &t->sums[0][0];
-    double* dd = &dst->sums[0][0];
+    double* dd = &dst->c.sums[0][0];
     for (int i = lane; i < 8 * CLR_N_DETECTORS; i += 32) {
         double v = sd[i];
         if (v != 0.0) { atomicAdd(dd + i, v); sd[i] = 0.0; }
     }
     unsigned long long* su2 = &t->status[0];
-    unsigned long long* du2 = &dst->status[0];
-    const int n_tail = CLR_N_STATUS + CLR_N_FAILURE_CODES + CLR_N_EVENT_COUNTERS + CLR_N_CONDITIONAL_STATS + 1;
-    for (int i = lane; i < n_tail; i += 32) {
+    unsigned long long* du2 = &dst->c.status[0];
+    for (int i = lane; i < CLR_TALLY_TAIL; i += 32) {
         unsigned long long v = su2[i];
         if (v) { atomicAdd(du2 + i, v); su2[i] = 0ull; }
     }
@@ -398,13 +423,13 @@ __global__ void __launch_bounds__(CLR_TRACE_THREADS) photon_kernel(const DevScen
         if (!__any_sync(FULL, have)) break;
         if (have) {
             const DevScene& D = scenes[sid];
-            const TallySink sink = (sid == home) ? home_sink : tally_sink(tallies + sid);
+            const TallySink sink = (sid == home) ? home_sink : tally_sink_dev(tallies + sid);
             bool done;
             if (r.phase == PHASE_LAUNCH) done = launch_segment(D, r, L.transport(), L.source());
             else done = water_step<typename Mode::Stream, kWeighted>(D, r, L.transport(), L.optics(),
-                                                                      (sid == home) ? &wt->cstats[0] : &tallies[sid].cstats[0]);
+                                                                      (sid == home) ? &wt->cstats[0] : &tallies[sid].c.cstats[0]);
             if (done) {
-                finish_ray<Mode>(D, r, gid, sink, kRecord ? records + rid : nullptr);
+                finish_ray<Mode>(D, r, gid, sink, tallies[sid].ic_hi, kRecord ? records + rid : nullptr);
                 have = false;
             }
         }

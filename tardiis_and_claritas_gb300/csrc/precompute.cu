@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(32) mie_coefficients_kernel(const double* __re
     size_parameter[p] = x;
     if (!(x > 0.0) || !(n_real[p] > 0.0) || !(n_medium > 0.0) || !(wavelength > 0.0)) {
         nstop_out[p] = 0; qext[p] = qsca[p] = qabs[p] = qback[p] = asym_g[p] = 0.0; albedo[p] = 1.0;
-        atomicExch(error_flag, 2);
+        atomicCAS(error_flag, 0, 2);
         return;
     }
     double mr = n_real[p] / n_medium, mi = k_imag[p] / n_medium;
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(32) mie_coefficients_kernel(const double* __re
     double mz = hypot(mr * x, mi * x);
     int nmx = (int)fmax((double)nstop, mz) + 128;
     if (nmx < nstop + 1) nmx = nstop + 1;
-    if (nmx >= CLR_MIE_MAX_ORDER || nstop >= CLR_MIE_MAX_ORDER) { nstop_out[p] = 0; atomicExch(error_flag, 1); return; }
+    if (nmx >= CLR_MIE_MAX_ORDER || nstop >= CLR_MIE_MAX_ORDER) { nstop_out[p] = 0; atomicCAS(error_flag, 0, 1); return; }
     nstop_out[p] = nstop;
     Dsh[nmx] = CD(0.0, 0.0);
     cdx z = CD(mr * x, mi * x);
@@ -191,7 +191,7 @@ __global__ void phase_cdf_kernel(const double* __restrict__ theta, const double*
         cdf[base + j] = s;
     }
     if (!(s > 0.0) || !isfinite(s)) {
-        atomicExch(error_flag, 3);
+        atomicCAS(error_flag, 0, 3);
         for (int j = 0; j < nt; ++j) { cdf[base + j] = (double)j / (double)(nt - 1); cdf_f[base + j] = (float)cdf[base + j]; }
         return;
     }
@@ -225,15 +225,15 @@ __global__ void transport_kernel(int n, const double* __restrict__ d, const doub
                                  double* trace_wave, float* gcdf_f, float* wcdf_f, float* pn_f, float* pk_f,
                                  float* prad_f, int* error_flag) {
     if (blockIdx.x || threadIdx.x) return;
-    if (n < 1 || n > CLR_MAX_BINS) { atomicExch(error_flag, 20); return; }
-    if (!(density > 0.0) || concentration < 0.0) { atomicExch(error_flag, 21); return; }
+    if (n < 1 || n > CLR_MAX_BINS) { atomicCAS(error_flag, 0, 20); return; }
+    if (!(density > 0.0) || concentration < 0.0) { atomicCAS(error_flag, 0, 21); return; }
     double sw0 = 0.0;
     for (int i = 0; i < n; ++i) sw0 += w_in[i];
-    if (!(sw0 > 0.0)) { atomicExch(error_flag, 22); return; }
+    if (!(sw0 > 0.0)) { atomicCAS(error_flag, 0, 22); return; }
     for (int i = 0; i < n; ++i) w[i] = w_in[i] / sw0;
     double sw = 0.0;
     for (int i = 0; i < n; ++i) sw += w[i];
-    if (!(sw > 0.0)) { atomicExch(error_flag, 4); return; }
+    if (!(sw > 0.0)) { atomicCAS(error_flag, 0, 4); return; }
     double pmass[CLR_MAX_BINS], srcw[CLR_MAX_BINS];
     double avg_mass = 0.0;
     for (int i = 0; i < n; ++i) {
@@ -254,7 +254,7 @@ __global__ void transport_kernel(int n, const double* __restrict__ d, const doub
         const double ki = k_imag[i];
         if (!isfinite(ki) || ki < 0.0 || !isfinite(qext[i]) || !isfinite(qsca[i]) || qext[i] < -tol || qsca[i] < -tol ||
             qsca[i] > qext[i] + tol || (ki == 0.0 && fabs(qext[i] - qsca[i]) > tol)) {
-            atomicExch(error_flag, 5);
+            atomicCAS(error_flag, 0, 5);
             return;
         }
         double swv = 0.0;
@@ -438,7 +438,7 @@ __global__ void sediment_bin_kernel(SedArgs a, const double* __restrict__ diamet
         integ += r * iz;
     }
     double norm = (2.0 / (R2 * Hmean)) * integ * dr;
-    if (!(norm > 0.0) || !isfinite(norm)) { atomicExch(error_flag, 34); return; }
+    if (!(norm > 0.0) || !isfinite(norm)) { atomicCAS(error_flag, 0, 34); return; }
     sed_norm[i] = norm;
     sed_max[i] = 1.0 / norm;
 }
@@ -462,7 +462,7 @@ __global__ void sediment_majorant_kernel(SedArgs a, const double* trace_geom, co
         mw += trace_wave[i] * sed_max[i];
     }
     major[0] = mg; major[1] = mw; major[2] = mg + mw; major[3] = maxAeq;
-    if (!(major[2] >= 0.0) || !isfinite(major[2])) atomicExch(error_flag, 35);
+    if (!(major[2] >= 0.0) || !isfinite(major[2])) atomicCAS(error_flag, 0, 35);
     if (a.TM == 3 && grid) {
         const long long plane = (long long)nr * nz;
         for (int p = 0; p < n; ++p) {

@@ -35,7 +35,11 @@ import parity_scenes as PS  # noqa: E402
 
 ORACLE = os.path.join(ROOT, "oracle")
 SRC = os.path.join(ORACLE, "_ref", "claritas_cuda_src.inc")
-SO = os.path.join(ORACLE, "_ref", "libclaritas_ref_gpu.so")
+# The bit-exact target is the reference source compiled without multiply-add contraction, as the
+# library's parity kernels are; CLR_REF_FMAD=true builds the reference as CuPy/NVRTC deploy it
+# (contraction on) for the agreement-rate fixture.
+FMAD = os.environ.get("CLR_REF_FMAD", "false")
+SO = os.path.join(ORACLE, "_ref", "libclaritas_ref_gpu.so" if FMAD == "true" else "libclaritas_ref_gpu_nofma.so")
 N_RAYS = 131072
 N_COMPACT = 4096
 
@@ -46,7 +50,7 @@ def build():
     if os.path.exists(SO) and os.path.getmtime(SO) > max(os.path.getmtime(SRC),
                                                          os.path.getmtime(os.path.join(ORACLE, "ref_gpu_driver.cu"))):
         return SO
-    cmd = ["nvcc", "-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-Xcompiler", "-fPIC",
+    cmd = ["nvcc", "-std=c++17", "-O3", f"-fmad={FMAD}", "-gencode", "arch=compute_103a,code=sm_103a", "-Xcompiler", "-fPIC",
            "-shared", "-w", "-I", os.path.join(ROOT, "include"), "-I", ORACLE,
            os.path.join(ORACLE, "ref_gpu_driver.cu"), "-o", SO]
     t = time.time()

@@ -83,7 +83,8 @@ def compact(rec: np.ndarray, n: int) -> np.ndarray:
 
 TALLY_KEYS = ("hw_native", "hw_mirror", "hw_native_direct", "hw_mirror_direct", "hw_native_stray",
               "hw_mirror_stray", "hw_native_face", "hw_mirror_face", "legacy_native", "legacy_mirror",
-              "status_counts", "failure_code_counts")
+              "status_counts", "failure_code_counts", "entered_sums", "ray_flags", "failure_subcode_counts",
+              "ic_hist")
 EVENT_KEYS = 20  # event_counts[0:20] are the reference's per-ray counter sums
 
 

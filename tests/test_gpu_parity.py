@@ -24,6 +24,7 @@ from tardiis_and_claritas_gb300 import abi, scene as S
 pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "gpu_ref_fixtures.npz")
+GOLD_FMA = os.path.join(os.path.dirname(__file__), "golden", "gpu_ref_fma_fixtures.npz")
 
 
 @pytest.fixture(scope="module")
@@ -75,6 +76,26 @@ def test_bit_exact_against_reference_kernels(ctx, gold, name):
     assert tal["event_counts"][:PS.EVENT_KEYS].tolist() == m["event_counts"]
     assert [int(v) for v in tal["conditional_stats"]] == m["conditional_stats"]
     assert PS.records_digest(rec) == m["records_sha256"], first_mismatch(rec, z[f"{name}/compact"])
+
+
+@pytest.mark.parametrize("name", list(PS.SCENES))
+def test_agreement_with_as_deployed_reference(ctx, name):
+    """The reference as CuPy/NVRTC deploy it fuses multiply-adds where its compiler chooses; the
+    resulting last-bit differences flip an integer outcome in only a handful of rays per 1e5."""
+    if not os.path.exists(GOLD_FMA):
+        pytest.skip("tests/golden/gpu_ref_fma_fixtures.npz not generated yet")
+    z = np.load(GOLD_FMA)
+    meta = json.loads(bytes(z["meta"]).decode())
+    m = meta["scenes"][name]
+    prepare(ctx, name)
+    n = meta["n_rays"]
+    tal, rec = ctx.trace(S.run_params(n, seed=m["seed"]), records=True)
+    mine = PS.compact(rec, meta["n_compact"]).astype(np.int16)
+    agree = np.mean(np.all(mine == z[f"{name}/compact"], axis=1))
+    assert agree >= 0.999, f"{name}: only {agree:.5f} of the first {meta['n_compact']} rays agree"
+    for k in ("hw_native", "hw_mirror", "status_counts"):
+        diff = np.abs(tal[k].astype(np.int64) - z[f"{name}/{k}"].astype(np.int64)).sum()
+        assert diff <= max(10, 1e-4 * n), f"{name} {k}: {diff} counts differ"
 
 
 def _se_compare(a_counts, a_n, b_counts, b_n, k=3.0, floor=0):
