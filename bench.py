@@ -1,0 +1,299 @@
+#!/usr/bin/env python3
+"""Benchmark of the photon-transport hot path (photons/s at fixed tally error).
+
+One "step" traces one batch of photons of the full-scene workload through the
+library's persistent photon kernel (transport + detector scoring + tallies in
+one launch). Photon counts are the same for GPU and CPU arms and both run the
+same estimator, so equal photon counts mean equal tally error.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload full|small]
+  python bench.py --impl reference ...   # the reference's own CPU implementation
+
+Multi-GPU (torchrun, one rank per GPU): replicas over disjoint photon ranges
+(counter-based Philox streams), no data-path collective; value = all photons /
+max-over-ranks time ("weak" scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Per-photon FP64 work of the full-scene workload, measured with ncu thread-level instruction
+# counters (DFMA counted as 2, DADD/DMUL as 1) on 1e6 photons of this workload; profiles/
+# photon_kernel_full_scene.md holds the capture. Used for the roofline's achieved FP64 rate.
+FP64_OPS_PER_PHOTON = {"full": None, "small": None}
+
+
+def workload(name: str):
+    from tardiis_and_claritas_gb300 import scene as S
+    if name == "full":
+        cfg, parts, grid, zmax = S.full_scene_workload()
+        return cfg, parts, grid, zmax, 100_000_000
+    cfg, parts, grid, zmax = S.small_plain_workload()
+    return cfg, parts, grid, zmax, 1_000_000
+
+
+def workload_config(name: str, n: int, rng: str) -> dict:
+    if name == "full":
+        return {"workload": "full scene: 63-bin clay/silt/sand mixture (2/20/100 um, sigma_g 1.4, 0.3/0.5/0.2) at "
+                            "500 mg/L in a 64x64 (r,z) Rouse(P=0.3) x radial-depletion field, stirred free surface "
+                            "(600 rpm, 5 mm core; localized-vortex surface), r=12.5 mm cell, smooth spheres with "
+                            "FP64 Mie phase tables (1801 angles), 860 nm",
+                "photons_per_step": n, "rng": rng, "l2": "flushed between steps (256 MiB write)"}
+    return {"workload": "small plain MC: 64 lognormal quartz bins (median 20 um, sigma_g 1.6) at 100 mg/L, uniform, "
+                        "flat surface, r=12.5 mm cell, Mie tables 1801 angles, 860 nm",
+            "photons_per_step": n, "rng": rng, "l2": "flushed between steps (256 MiB write)"}
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index, self.samples, self.proc, self.thread = index, [], None, None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE, text=True)
+        except (FileNotFoundError, OSError):
+            return
+
+        def read():
+            for line in self.proc.stdout:
+                self.samples.append([c.strip() for c in line.split(",")])
+
+        self.thread = threading.Thread(target=read, daemon=True)
+        self.thread.start()
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                mx.append(float(s[2]))
+                for nm, v in zip(names, s[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+class CpuReference:
+    """The reference's own CPU implementation of the path (its kernel source compiled for the host) or, where
+    that build is absent, the CPU restatement; prepared once, then timed on bounded samples of the workload."""
+
+    def __init__(self, name: str, threads: int):
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_harness as H
+        cfg, parts, grid, zmax, _ = workload(name)
+        self.kind = "reference" if H.reference_available() else "port"
+        self.o = H.OracleRun(self.kind, cfg, parts, grid=grid, grid_zmax=zmax)
+        self.threads = threads
+        self.probe = 20_000 if name == "full" else 200_000
+
+    def sample_size(self, seconds: float) -> int:
+        from tardiis_and_claritas_gb300 import scene as S
+        t = time.perf_counter()
+        self.o.trace(S.run_params(self.probe, seed=7), threads=self.threads)
+        dt = time.perf_counter() - t
+        return max(self.probe, int(self.probe * seconds / max(dt, 1e-3)))
+
+    def time(self, n: int, seed: int) -> float:
+        from tardiis_and_claritas_gb300 import scene as S
+        t = time.perf_counter()
+        self.o.trace(S.run_params(n, seed=seed), threads=self.threads)
+        return time.perf_counter() - t
+
+    def close(self):
+        self.o.close()
+
+
+def run_reference_arm(args, rank: int, world: int):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    name = args.workload
+    _, _, _, _, n_gpu = workload(name)
+    ref = CpuReference(name, threads)
+    n = ref.sample_size(args.cpu_seconds)
+    for i in range(args.warmup):
+        ref.time(max(n // 10, ref.probe), seed=100 + i)
+    total_t = sum(ref.time(n, seed=200 + k) for k in range(args.steps))
+    ref.close()
+    total_n = n * args.steps
+    value = total_n / total_t
+    line = {"impl": "reference", "metric": "photons/s (at fixed tally error)", "value": value, "unit": "photons/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64",
+            "data": "synthetic (seeded)", "config": workload_config(name, n_gpu, "reference xorshift"),
+            "cpu_baseline": {"value": value, "unit": "photons/s", "cores": threads, "kind": ref.kind,
+                             "sample": f"{n} photons of the same workload per step, {args.steps} steps"},
+            "e2e": {"value": value, "unit": "photons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["full", "small"], default="full")
+    ap.add_argument("--rng", choices=["philox", "xorshift"], default="philox")
+    ap.add_argument("--photons", type=int, default=0, help="override photons per step")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="gloo" if args.impl == "reference" else "nccl")
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import numpy as np
+    import torch
+    from tardiis_and_claritas_gb300 import abi, lib as L, scene as S
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    if dist:
+        dist.barrier(device_ids=[local_rank])
+    ctx = L.Context(local_rank)
+    cfg, parts, grid, zmax, n = workload(args.workload)
+    if args.photons:
+        n = args.photons
+    rng_mode = abi.RNG_PHILOX if args.rng == "philox" else abi.RNG_REFERENCE_XORSHIFT
+    sp = cfg.to_scene_params()
+    ss = cfg.sediment_spec(grid, zmax)
+    ps = parts.spec(cfg)
+    ctx.set_scene(sp)
+    ctx.build_particles(ps, ss)
+    fp64_peak = ctx.calibrate(1)
+    fp32_peak = ctx.calibrate(0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def run(step: int):
+        # disjoint photon ranges per rank and step (counter-based streams: partition independent)
+        off = ((rank * (args.warmup + args.steps) + step) * n) % (1 << 31)
+        return S.run_params(n, seed=20261203, ray_offset=off, rng_mode=rng_mode)
+
+    for w in range(args.warmup):
+        ctx.trace(run(w))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier(device_ids=[local_rank])
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    kernel_ms = []
+    tallies = []
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        T, _ = ctx.trace(run(args.warmup + k))
+        kernel_ms.append(ctx.last_kernel_ms())
+        tallies.append(T)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    total_ms = float(sum(kernel_ms))
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n * args.steps / (total_ms * 1e-3)
+
+    # end to end through the public API: host PSD/grid inputs (pinned) -> precompute -> trace -> tallies to host
+    e2e_steps = min(args.steps, 3)
+    pinned = {k: torch.from_numpy(getattr(parts, k)).pin_memory() for k in ("diameter_m", "weight", "n_real", "k_imag")}
+    grid_pin = torch.from_numpy(np.ascontiguousarray(grid)).pin_memory() if grid is not None else None
+    ps_e = abi.ParticleSpec.from_buffer_copy(ps)
+    for k, tsr in pinned.items():
+        setattr(ps_e, k, abi.C.cast(tsr.data_ptr(), abi.PD))
+    ss_e = abi.SedimentSpec.from_buffer_copy(ss)
+    if grid_pin is not None:
+        ss_e.grid = abi.C.cast(grid_pin.data_ptr(), abi.PD)
+    h2d = sum(t.numel() * 8 for t in pinned.values()) + (grid_pin.numel() * 8 if grid_pin is not None else 0) \
+        + abi.C.sizeof(abi.SceneParams) + abi.C.sizeof(abi.RunParams)
+    d2h = abi.C.sizeof(abi.Tallies)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        ctx.set_scene(sp)
+        ctx.build_particles(ps_e, ss_e)
+        ctx.trace(run(args.warmup + args.steps + k))
+    e2e_t = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_t], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e = world * n * e2e_steps / e2e_t
+
+    sched = np.sum([t["sched_stats"] for t in tallies], axis=0)
+    ev = np.sum([t["event_counts"] for t in tallies], axis=0)
+    fp64_per_photon = FP64_OPS_PER_PHOTON.get(args.workload)
+    launch_s = total_ms * 1e-3 / args.steps
+    roofline = {"bound": "fp64", "unit": "TFLOP/s", "peak": fp64_peak / 1e12,
+                "peak_source": "measured FP64 DFMA throughput (library calibration kernel, this GPU)",
+                "achieved": None, "frac": None, "traffic": None,
+                "fp32_peak_tflops": fp32_peak / 1e12}
+    if fp64_per_photon:
+        ach = fp64_per_photon * n / launch_s
+        roofline["achieved"] = ach / 1e12
+        roofline["frac"] = ach / fp64_peak
+    line = {"metric": "photons/s (at fixed tally error)", "value": value, "unit": "photons/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64",
+            "data": "synthetic (seeded)", "config": workload_config(args.workload, n, args.rng),
+            "e2e": {"value": e2e, "unit": "photons/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "steps": e2e_steps, "includes": "scene upload, Mie/table/rate/field precompute, trace, tally readback"},
+            "gpu_launches": args.steps, "clocks": clocks, "roofline": roofline,
+            "kernel": {"mean_ms": float(np.mean(kernel_ms)), "wall_s": wall,
+                       "water_steps_per_photon": float(ev[20] / (n * args.steps)),
+                       "lanes_per_iteration": [float(sched[4 + k] / max(sched[k], 1)) for k in range(3)],
+                       "cycle_share": [float(sched[8 + k] / max(sched[8:11].sum(), 1)) for k in range(3)]}}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        ref = CpuReference(args.workload, os.cpu_count() or 1)
+        ns = ref.sample_size(args.cpu_seconds)
+        dt = ref.time(ns, seed=8)
+        line["cpu_baseline"] = {"value": ns / dt, "unit": "photons/s", "cores": ref.threads, "kind": ref.kind,
+                                "sample": f"{ns} photons of the same workload, {dt:.1f} s"}
+        ref.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.barrier(device_ids=[local_rank])
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -237,6 +237,10 @@ typedef struct clr_tallies {
     int64_t ray_flags[16];          /* counts of rays satisfying a predicate */
     int64_t failure_subcode_counts[CLR_N_SUBCODES];  /* indexed by clr_subcode_index() */
     int64_t ic_hist[CLR_IC_HIST];   /* interaction count of entered rays; last bin = overflow */
+    /* scheduler profile of the photon kernel (no reference counterpart): per phase
+     * (0 source, 1 entry, 2 water) the warp iterations [k], the lanes that ran [4+k] and the
+     * SM clock cycles spent [8+k]; [11] cycles spent scoring finished histories */
+    int64_t sched_stats[16];
 } clr_tallies;
 
 /* Host copies of the particle-physics tables (diagnostics and parity checks).
@@ -281,6 +285,15 @@ int clr_trace(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray
 
 /* Same as clr_trace with HOST-resident record memory (copied back inside the call). */
 int clr_trace_host_records(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* host_records);
+
+/* Device time of the photon kernel in the last clr_trace call, measured with CUDA events recorded
+ * on the context's stream around the launch (milliseconds). No reference counterpart. */
+int clr_last_kernel_ms(const clr_ctx* ctx, float* ms);
+
+/* Calibration kernels for roofline denominators (no reference counterpart): sustained
+ * arithmetic throughput of this device in operations per second, counting a fused
+ * multiply-add as two operations. which = 0: FP32 FFMA; which = 1: FP64 DFMA. */
+int clr_calibrate(clr_ctx* ctx, int which, double* ops_per_second);
 
 /* Sizes of the ABI structs as compiled into the library (0 scene, 1 particle spec, 2 sediment spec,
  * 3 run params, 4 ray record, 5 tallies, 6 particle physics); -1 for an unknown index.

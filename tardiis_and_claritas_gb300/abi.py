@@ -160,6 +160,7 @@ class Tallies(C.Structure):
         ("device_error", i32), ("reserved", i32 * 7),
         ("entered_sums", i64 * 16), ("ray_flags", i64 * 16),
         ("failure_subcode_counts", i64 * N_SUBCODES), ("ic_hist", i64 * IC_HIST),
+        ("sched_stats", i64 * 16),
     ]
 
     def as_dict(self) -> dict:

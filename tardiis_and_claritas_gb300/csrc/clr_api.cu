@@ -32,6 +32,8 @@ struct clr_ctx {
     DevTally* d_tally = nullptr;
     unsigned long long* d_work = nullptr;
     int num_sms = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float last_kernel_ms = 0.0f;
 };
 
 static int fail(clr_ctx* c, int code, const char* fmt, ...) {
@@ -82,6 +84,8 @@ int clr_create(clr_ctx** out, int device) {
     CU(cudaMalloc(&ctx->d_chunk_begin, 2 * sizeof(long long)));
     CU(cudaMalloc(&ctx->d_tally, sizeof(DevTally)));
     CU(cudaMalloc(&ctx->d_work, sizeof(unsigned long long)));
+    CU(cudaEventCreate(&ctx->ev0));
+    CU(cudaEventCreate(&ctx->ev1));
     *out = ctx;
     return CLR_OK;
 }
@@ -95,6 +99,8 @@ int clr_destroy(clr_ctx* ctx) {
     cudaFree(ctx->d_chunk_begin);
     cudaFree(ctx->d_tally);
     cudaFree(ctx->d_work);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return CLR_OK;
@@ -277,6 +283,7 @@ static void tally_to_host(const DevTally& d, clr_tallies* out, int64_t n_rays) {
     for (int k = 0; k < 16; ++k) { out->entered_sums[k] = (int64_t)t.entered_sums[k]; out->ray_flags[k] = (int64_t)t.ray_flags[k]; }
     for (int k = 0; k < CLR_N_SUBCODES; ++k) out->failure_subcode_counts[k] = (int64_t)t.subcodes[k];
     for (int k = 0; k < CLR_IC_HIST; ++k) out->ic_hist[k] = (int64_t)d.ic_hi[k] + (k < 64 ? (int64_t)t.ic_lo[k] : 0);
+    for (int k = 0; k < 16; ++k) out->sched_stats[k] = (int64_t)d.sched[k];
     out->device_error = (t.n_done == (unsigned long long)n_rays) ? 0 : 1;
 }
 
@@ -310,10 +317,13 @@ static int trace_impl(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out,
     long long blocks_needed = (warps_needed * 32 + CLR_TRACE_THREADS - 1) / CLR_TRACE_THREADS;
     a.grid = (int)std::max(1LL, std::min(want, blocks_needed));
     if (run->max_blocks > 0) a.grid = std::max(1, std::min(a.grid, run->max_blocks));
+    CU(cudaEventRecord(ctx->ev0, st));
     if (cb[1] > 0) CU(launch_photon_kernel(a));
+    CU(cudaEventRecord(ctx->ev1, st));
     DevTally ht;
     CU(cudaMemcpyAsync(&ht, ctx->d_tally, sizeof ht, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
+    CU(cudaEventElapsedTime(&ctx->last_kernel_ms, ctx->ev0, ctx->ev1));
     tally_to_host(ht, out, run->n_rays);
     return CLR_OK;
 }
@@ -338,6 +348,30 @@ int clr_trace_host_records(clr_ctx* ctx, const clr_run_params* run, clr_tallies*
     }
     cudaFree(d);
     return rc;
+}
+
+int clr_last_kernel_ms(const clr_ctx* ctx, float* ms) {
+    if (!ctx || !ms) return CLR_ERR_INVALID_ARGUMENT;
+    *ms = ctx->last_kernel_ms;
+    return CLR_OK;
+}
+
+int clr_calibrate(clr_ctx* ctx, int which, double* ops_per_second) {
+    if (!ctx || !ops_per_second || which < 0 || which > 1) return CLR_ERR_INVALID_ARGUMENT;
+    CU(cudaSetDevice(ctx->device));
+    double best = 0.0;
+    for (int rep = 0; rep < 4; ++rep) {
+        double ops = 0.0;
+        CU(cudaEventRecord(ctx->ev0, ctx->stream));
+        CU(launch_calibration(which, ctx->num_sms, ctx->stream, &ops));
+        CU(cudaEventRecord(ctx->ev1, ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
+        float ms = 0.0f;
+        CU(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        if (rep > 0 && ms > 0.0f) best = std::max(best, ops / (ms * 1e-3));
+    }
+    *ops_per_second = best;
+    return CLR_OK;
 }
 
 /* sizes of the ABI structs as compiled, for the Python mirror's self-check */

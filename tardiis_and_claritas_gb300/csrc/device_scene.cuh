@@ -67,6 +67,7 @@ struct TallyCore {
 struct DevTally {
     TallyCore c;
     unsigned long long ic_hi[CLR_IC_HIST];
+    unsigned long long sched[16];
 };
 
 }  // namespace clr

@@ -34,6 +34,10 @@ inline int photon_kernel_occupancy(int rng_mode, bool records, bool /*weighted*/
     return rng_mode == CLR_RNG_PHILOX ? occupancy_philox(records) : occupancy_xor(records);
 }
 
+// Calibration kernels (calibrate.cu): FP32 FFMA (which=0) or FP64 DFMA (which=1) throughput loops.
+// Sets *ops to the number of operations the launch performs (an FMA counts 2).
+cudaError_t launch_calibration(int which, int num_sms, cudaStream_t stream, double* ops);
+
 // Device buffers of one scenario's particle physics (all FP64 unless named _f).
 struct ParticleBuffers {
     int n = 0, nt = 0, n_radial = 0, grid_nr = 2, grid_nz = 2;

@@ -16,7 +16,9 @@
 namespace clr {
 namespace {  // header-only device code: internal linkage in every translation unit
 
-enum : int { PHASE_LAUNCH = 0, PHASE_WATER = 1 };
+// Phases of a history. SOURCE (FP32 sampling up to collimator acceptance) rejects most photons;
+// ENTRY (outer-wall Fresnel, acrylic solid, headspace) and WATER are the FP64-heavy phases.
+enum : int { PHASE_SOURCE = 0, PHASE_ENTRY = 1, PHASE_WATER = 2 };
 
 struct Ray {
     float x, y, z, vx, vy, vz, wp, ap, w;
@@ -29,7 +31,7 @@ struct Ray {
 // Small per-history counters that the reference keeps in registers; summed into tallies at the end.
 __device__ __forceinline__ void ray_reset(Ray& r) {
     r.x = r.y = r.z = 0.f; r.vx = 0.f; r.vy = 1.f; r.vz = 0.f; r.wp = 0.f; r.ap = 0.f; r.w = 1.f;
-    r.phase = PHASE_LAUNCH; r.step = 0; r.st = 0; r.pf = 0; r.pfs = 0;
+    r.phase = PHASE_SOURCE; r.step = 0; r.st = 0; r.pf = 0; r.pfs = 0;
     r.ic = r.gic = r.wic = r.wcoh = r.wmorph = 0;
     r.cir = r.cor = r.ctir = r.tr = r.ttir = r.bir = r.bor = r.btir = r.sbi = r.sbr = r.entered = 0;
     r.pc.reflections = r.pc.entry_reflections = r.pc.internal_reflections = r.pc.absorptions = 0;
@@ -171,10 +173,10 @@ __device__ __forceinline__ void add_bounces(Ray& r, const o_bcount& b) {
     r.bir += b.bir; r.bor += b.bor; r.btir += b.btir;
 }
 
-// ---------------- launch segment: source, collimator, acrylic entry (:4650-4732) ----------------
-// Returns true when the history ended (r.st set), false when the ray entered the water.
+// ---------------- source segment: emission and collimator (:4650-4711) ----------------
+// Returns true when the history ended (rejected, r.st = 3); otherwise the ray waits in PHASE_ENTRY.
 template <class S>
-__device__ __forceinline__ bool launch_segment(const DevScene& D, Ray& r, S* st, S* src) {
+__device__ __forceinline__ bool source_segment(const DevScene& D, Ray& r, S* src) {
     const clr_scene_params& P = D.P;
     float x, y, z, vx = 0.0f, vy = 1.0f, vz = 0.0f;
     if (P.source_kind == CLR_SOURCE_COLLIMATED_DISC) {
@@ -227,6 +229,17 @@ __device__ __forceinline__ bool launch_segment(const DevScene& D, Ray& r, S* st,
                                      &r.sbi, &r.sbr)) { r.st = 3; return true; }
         }
     }
+    r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
+    r.phase = PHASE_ENTRY;
+    return false;
+}
+
+// ---------------- entry segment: air gap, outer wall, acrylic solid, headspace (:4699-4732) ----------------
+// Returns true when the history ended (r.st set), false when the ray entered the water.
+template <class S>
+__device__ __forceinline__ bool entry_segment(const DevScene& D, Ray& r, S* st) {
+    const clr_scene_params& P = D.P;
+    float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
     const o_cell C = make_cell(P);
     double tdw = o_cyl_hit_finite(x, y, z, vx, vy, vz, P.rout, P.zmin - P.bottom_disc_thickness, P.zwall_top);
     float t = (tdw < 0.5 * (double)CLR_INF_F) ? (float)tdw : CLR_INF_F;

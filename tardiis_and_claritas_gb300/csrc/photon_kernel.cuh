@@ -25,15 +25,27 @@ namespace clr {
 namespace {  // header-only device code: internal linkage in every translation unit
 
 // ---------------- detectors (:4237-4376) ----------------
-__device__ __forceinline__ int hardware_detector(float x, float y, float z, float vx, float vy, float vz, int mirror,
-                                                 float ring_in, float throat_out, float ring_out, float throat_r,
-                                                 float counterbore_r) {
+// Bore direction table (per block, shared memory): sin/cos of (10 j)(pi/180) for j = 0..18.
+struct DetTable {
+    float s[20], c[20];
+};
+__device__ __forceinline__ void det_table_init(DetTable* t) {
+    if (threadIdx.x < 19) {
+        const float th = o_det_theta((int)threadIdx.x);
+        t->s[threadIdx.x] = sinf(th);
+        t->c[threadIdx.x] = cosf(th);
+    }
+}
+
+__device__ __forceinline__ int hardware_detector(const DetTable& T, float x, float y, float z, float vx, float vy,
+                                                 float vz, int mirror, float ring_in, float throat_out, float ring_out,
+                                                 float throat_r, float counterbore_r) {
     if (mirror) { x = -x; vx = -vx; }
     float best_t = CLR_INF_F;
     int best = -1;
     float rth2 = throat_r * throat_r, rcb2 = counterbore_r * counterbore_r;
     for (int j = 0; j < 18; ++j) {
-        float th = o_det_theta(j), ux = sinf(th), uy = cosf(th);
+        float ux = T.s[j], uy = T.c[j];
         float den = vx * ux + vy * uy;
         if (den <= 1e-10f) continue;
         float pdot = x * ux + y * uy;
@@ -56,22 +68,21 @@ __device__ __forceinline__ float sfh213(float phi_deg) {
     float u = a / HALF_DEG;
     return 1.0f / (1.0f + powf(u, PW));
 }
-__device__ __forceinline__ float incidence_deg(float vx, float vy, int id, int mirror) {
+__device__ __forceinline__ float incidence_deg(const DetTable& T, float vx, float vy, int id, int mirror) {
     if (id < 0 || id >= 18) return -1.0f;
     if (mirror) vx = -vx;
-    float th = o_det_theta(id);
-    float ux = sinf(th), uy = cosf(th);
+    float ux = T.s[id], uy = T.c[id];
     float c = vx * ux + vy * uy;
     c = fminf(fmaxf(c, -1.0f), 1.0f);
     return acosf(c) * (180.0f / CLR_PI_F);
 }
-__device__ __forceinline__ int throat_opening(float x, float y, float z, float vx, float vy, float vz, float ring_in,
-                                              float throat_r) {
+__device__ __forceinline__ int throat_opening(const DetTable& T, float x, float y, float z, float vx, float vy,
+                                              float vz, float ring_in, float throat_r) {
     float best_t = CLR_INF_F;
     int best = -1;
     float r2 = throat_r * throat_r;
     for (int j = 0; j < 19; ++j) {
-        float th = o_det_theta(j), ux = sinf(th), uy = cosf(th);
+        float ux = T.s[j], uy = T.c[j];
         float den = vx * ux + vy * uy;
         if (den <= 1.0e-10f) continue;
         float pdot = x * ux + y * uy;
@@ -97,13 +108,14 @@ __device__ __forceinline__ float cylinder_hit(float x, float y, float vx, float 
     return t;
 }
 template <class S>
-__device__ __noinline__ int ring_face_path(S* s, float x, float y, float z, float vx, float vy, float vz, int mirror,
-                                           const clr_scene_params* P, int* bore_bounces, int* face_reflections) {
+__device__ __noinline__ int ring_face_path(S* s, const DetTable* T, float x, float y, float z, float vx, float vy,
+                                           float vz, int mirror, const clr_scene_params* P, int* bore_bounces,
+                                           int* face_reflections) {
     if (mirror) { x = -x; vx = -vx; }
     *bore_bounces = 0;
     *face_reflections = 0;
     if (P->ring_face_model == 0) return -1;
-    if (throat_opening(x, y, z, vx, vy, vz, P->ring_in, P->throat_r) >= 0) return -1;
+    if (throat_opening(*T, x, y, z, vx, vy, vz, P->ring_in, P->throat_r) >= 0) return -1;
     for (int b = 0; b < P->max_ring_face_bounces; ++b) {
         float tr = cylinder_hit(x, y, vx, vy, P->ring_in);
         if (tr >= CLR_INF_F * 0.5f) return -1;
@@ -131,14 +143,14 @@ __device__ __noinline__ int ring_face_path(S* s, float x, float y, float z, floa
         x += CLR_EPS_F * nx; y += CLR_EPS_F * ny;
         int db = 0, det;
         if (P->detector_bore_model == 0)
-            det = hardware_detector(x, y, z, vx, vy, vz, 0, P->ring_in, P->throat_out, P->ring_out, P->throat_r,
+            det = hardware_detector(*T, x, y, z, vx, vy, vz, 0, P->ring_in, P->throat_out, P->ring_out, P->throat_r,
                                     P->counterbore_r);
         else
             det = o_detector_collimator_path(s, x, y, z, vx, vy, vz, 0, P->ring_in, P->throat_out, P->ring_out,
                                              P->throat_r, P->counterbore_r, P->detector_bore_model, P->n_air, P->bore_n,
-                                             P->max_bore_bounces, &db);
+                                             P->max_bore_bounces, &db, T->s, T->c);
         if (det >= 0) { *bore_bounces = db; return det; }
-        if (throat_opening(x, y, z, vx, vy, vz, P->ring_in, P->throat_r) >= 0) return -1;
+        if (throat_opening(*T, x, y, z, vx, vy, vz, P->ring_in, P->throat_r) >= 0) return -1;
     }
     return -1;
 }
@@ -147,7 +159,7 @@ __device__ __noinline__ int ring_face_path(S* s, float x, float y, float z, floa
 struct TallySink {
     unsigned long long* hw;    // 10*18
     double* sums;              // 8*18
-    unsigned long long* tail;  // status..n_done
+    unsigned long long* tail;  // status..ic_lo
     __device__ __forceinline__ void add_u(int idx, unsigned long long v) const {
         if (idx < 10 * CLR_N_DETECTORS) atomicAdd(hw + idx, v);
         else atomicAdd(tail + (idx - CLR_OFF_STATUS), v);
@@ -165,41 +177,74 @@ __device__ __forceinline__ TallySink tally_sink(T* t) {
 }
 __device__ __forceinline__ TallySink tally_sink_dev(DevTally* t) { return tally_sink(&t->c); }
 
-// Score a finished history and add it to `sink` (:4390-4436, tallies :7849-7862).
+// Sum `v` over the lanes of `grp` and let the group's leader add it (one atomic per group, not per lane).
+__device__ __forceinline__ void group_add(const TallySink& sink, unsigned grp, bool leader, int idx, int v) {
+    const unsigned sum = __reduce_add_sync(grp, (unsigned)v);
+    if (leader && sum) sink.add_u(idx, (unsigned long long)sum);
+}
+// Count lanes of `grp` with `pred` and let the leader add the count.
+__device__ __forceinline__ void group_count(const TallySink& sink, unsigned grp, bool leader, int idx, bool pred) {
+    const unsigned n = __popc(__ballot_sync(grp, pred));
+    if (leader && n) sink.add_u(idx, (unsigned long long)n);
+}
+// Histogram update: lanes with equal keys are merged before one atomic per distinct key.
+__device__ __forceinline__ void group_hist(const TallySink& sink, unsigned grp, int base, int key, bool active) {
+    const unsigned part = __ballot_sync(grp, active);
+    if (active) {
+        const unsigned same = __match_any_sync(part, key);
+        if ((int)(threadIdx.x & 31) == __ffs(same) - 1) sink.add_u(base + key, (unsigned long long)__popc(same));
+    }
+}
+
+// Score finished histories and add them to the scenario tallies (:4390-4436, tallies :7849-7862,
+// per-ray statistics :8483-8508 and :8665-8735). Called by every lane whose photon finished in this
+// iteration; lanes are grouped by scenario so the frequent counters are reduced across the group first.
 template <class Mode>
-__device__ __forceinline__ void finish_ray(const DevScene& D, const Ray& r, uint32_t gid, const TallySink& sink,
-                                           unsigned long long* ic_hi, clr_ray_record* rec) {
+__device__ __forceinline__ void finish_ray(const DevScene& D, const DetTable& T, const Ray& r, uint32_t gid,
+                                           int sid, int home, WarpTally* wt, DevTally* tallies,
+                                           clr_ray_record* rec) {
     const clr_scene_params& P = D.P;
+    const int lane = threadIdx.x & 31;
+    const unsigned act = __activemask();
+    const unsigned grp = __match_any_sync(act, sid);
+    const bool leader = lane == __ffs(grp) - 1;
+    const TallySink sink = (sid == home) ? tally_sink(wt) : tally_sink_dev(tallies + sid);
     int ni = -1, mi = -1, nb = 0, mb = 0, nfb = 0, mfb = 0;
-    if (r.st == 1 && isfinite(r.x) && isfinite(r.y) && isfinite(r.z) && isfinite(r.vx) && isfinite(r.vy) &&
+    const int st = r.st;
+    if (st == 1 && isfinite(r.x) && isfinite(r.y) && isfinite(r.z) && isfinite(r.vx) && isfinite(r.vy) &&
         isfinite(r.vz)) {
         const float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
         if (P.detector_bore_model == 0 && P.ring_face_model == 0) {
-            ni = hardware_detector(x, y, z, vx, vy, vz, 0, P.ring_in, P.throat_out, P.ring_out, P.throat_r, P.counterbore_r);
-            mi = hardware_detector(x, y, z, vx, vy, vz, 1, P.ring_in, P.throat_out, P.ring_out, P.throat_r, P.counterbore_r);
+            ni = hardware_detector(T, x, y, z, vx, vy, vz, 0, P.ring_in, P.throat_out, P.ring_out, P.throat_r,
+                                   P.counterbore_r);
+            mi = hardware_detector(T, x, y, z, vx, vy, vz, 1, P.ring_in, P.throat_out, P.ring_out, P.throat_r,
+                                   P.counterbore_r);
         } else {
             typename Mode::Stream sN, sM;
             Mode::detector_streams(D, gid, &sN, &sM);
             if (P.detector_bore_model == 0) {
-                ni = hardware_detector(x, y, z, vx, vy, vz, 0, P.ring_in, P.throat_out, P.ring_out, P.throat_r, P.counterbore_r);
-                mi = hardware_detector(x, y, z, vx, vy, vz, 1, P.ring_in, P.throat_out, P.ring_out, P.throat_r, P.counterbore_r);
+                ni = hardware_detector(T, x, y, z, vx, vy, vz, 0, P.ring_in, P.throat_out, P.ring_out, P.throat_r,
+                                       P.counterbore_r);
+                mi = hardware_detector(T, x, y, z, vx, vy, vz, 1, P.ring_in, P.throat_out, P.ring_out, P.throat_r,
+                                       P.counterbore_r);
             } else {
                 ni = o_detector_collimator_path(&sN, x, y, z, vx, vy, vz, 0, P.ring_in, P.throat_out, P.ring_out,
                                                 P.throat_r, P.counterbore_r, P.detector_bore_model, P.n_air, P.bore_n,
-                                                P.max_bore_bounces, &nb);
+                                                P.max_bore_bounces, &nb, T.s, T.c);
                 mi = o_detector_collimator_path(&sM, x, y, z, vx, vy, vz, 1, P.ring_in, P.throat_out, P.ring_out,
                                                 P.throat_r, P.counterbore_r, P.detector_bore_model, P.n_air, P.bore_n,
-                                                P.max_bore_bounces, &mb);
+                                                P.max_bore_bounces, &mb, T.s, T.c);
             }
-            if (ni < 0 && P.ring_face_model != 0) ni = ring_face_path(&sN, x, y, z, vx, vy, vz, 0, &P, &nb, &nfb);
-            if (mi < 0 && P.ring_face_model != 0) mi = ring_face_path(&sM, x, y, z, vx, vy, vz, 1, &P, &mb, &mfb);
+            if (ni < 0 && P.ring_face_model != 0) ni = ring_face_path(&sN, &T, x, y, z, vx, vy, vz, 0, &P, &nb, &nfb);
+            if (mi < 0 && P.ring_face_model != 0) mi = ring_face_path(&sM, &T, x, y, z, vx, vy, vz, 1, &P, &mb, &mfb);
         }
+        // detector hits are rare and spread over 18 channels: per-lane atomics
         const double w = (double)r.w;
         if (ni >= 0) {
             sink.add_u(CLR_OFF_HW(0, ni), 1ull);
             sink.add_u(CLR_OFF_HW((nb > 0 || nfb > 0) ? 4 : 2, ni), 1ull);
             if (nfb > 0) sink.add_u(CLR_OFF_HW(6, ni), 1ull);
-            float phi = incidence_deg(vx, vy, ni, 0);
+            float phi = incidence_deg(T, vx, vy, ni, 0);
             if (phi >= 0.0f && isfinite(phi)) {
                 float resp = (P.photodiode_model == 0) ? 1.0f : sfh213(phi);
                 sink.add_d(0 * CLR_N_DETECTORS + ni, (double)resp * w);
@@ -212,7 +257,7 @@ __device__ __forceinline__ void finish_ray(const DevScene& D, const Ray& r, uint
             sink.add_u(CLR_OFF_HW(1, mi), 1ull);
             sink.add_u(CLR_OFF_HW((mb > 0 || mfb > 0) ? 5 : 3, mi), 1ull);
             if (mfb > 0) sink.add_u(CLR_OFF_HW(7, mi), 1ull);
-            float phi = incidence_deg(vx, vy, mi, 1);
+            float phi = incidence_deg(T, vx, vy, mi, 1);
             if (phi >= 0.0f && isfinite(phi)) {
                 float resp = (P.photodiode_model == 0) ? 1.0f : sfh213(phi);
                 sink.add_d(1 * CLR_N_DETECTORS + mi, (double)resp * w);
@@ -234,41 +279,42 @@ __device__ __forceinline__ void finish_ray(const DevScene& D, const Ray& r, uint
             }
         }
     }
-    const int st = r.st;
-    if (st >= 0 && st < CLR_N_STATUS) sink.add_u(CLR_OFF_STATUS + st, 1ull);
-    if (r.pf >= 0 && r.pf < CLR_N_FAILURE_CODES) sink.add_u(CLR_OFF_FAIL + r.pf, 1ull);
+    // frequent counters: reduced over the scenario group, one atomic per group
+    group_hist(sink, grp, CLR_OFF_STATUS, (st >= 0 && st < CLR_N_STATUS) ? st : 0, st >= 0 && st < CLR_N_STATUS);
+    group_hist(sink, grp, CLR_OFF_FAIL, r.pf, r.pf >= 0 && r.pf < CLR_N_FAILURE_CODES);
     const int ev[22] = {r.ic, r.gic, r.wic, r.wcoh, r.wmorph, r.pc.reflections, r.pc.entry_reflections,
                         r.pc.internal_reflections, r.pc.absorptions, r.cir, r.cor, r.ctir, r.tr, r.ttir, r.bir,
                         r.bor, r.btir, r.sbi, r.sbr, r.entered, r.steps, r.nulls};
+    const bool any_ev = __any_sync(grp, r.ic | r.cir | r.cor | r.ctir | r.tr | r.bir | r.bor | r.sbi | r.entered |
+                                            r.steps | r.nulls | r.pc.reflections | r.pc.absorptions);
+    if (any_ev) {
 #pragma unroll
-    for (int k = 0; k < 22; ++k)
-        if (ev[k]) sink.add_u(CLR_OFF_EV + k, (unsigned long long)(unsigned)ev[k]);
-    sink.add_u(CLR_OFF_DONE, 1ull);
-    // per-ray statistics of the reference host (:8483-8508, :8665-8735)
-    if (r.pf != 0) sink.add_u(CLR_OFF_SUB + CLR_SUBCODE_INDEX(r.pfs), 1ull);
-    if (st != 3) {
-        sink.add_u(CLR_OFF_RF + CLR_RF_SOURCE_ACCEPTED, 1ull);
-        sink.add_u(CLR_OFF_RF + (r.sbr == 0 ? CLR_RF_SOURCE_DIRECT : CLR_RF_SOURCE_REFLECTED), 1ull);
+        for (int k = 0; k < 22; ++k) group_add(sink, grp, leader, CLR_OFF_EV + k, ev[k]);
     }
-    if (st == 1 && isfinite(r.x) && isfinite(r.vx)) sink.add_u(CLR_OFF_RF + CLR_RF_VALID_AIR, 1ull);
-    if (st == 8) sink.add_u(CLR_OFF_RF + CLR_RF_TRAPPED, 1ull);
-    if (r.entered) {
-        sink.add_u(CLR_OFF_RF + CLR_RF_ENTERED, 1ull);
-        if (r.ic == 0) sink.add_u(CLR_OFF_RF + CLR_RF_BALLISTIC, 1ull);
-        if (r.pc.entry_reflections > 0) sink.add_u(CLR_OFF_RF + CLR_RF_ENTRY_REFLECTED, 1ull);
-        if (r.pc.internal_reflections > 0) sink.add_u(CLR_OFF_RF + CLR_RF_INTERNAL_REFLECTED, 1ull);
-        if (r.pc.absorptions > 0) sink.add_u(CLR_OFF_RF + CLR_RF_ABSORBED, 1ull);
-        if (r.ctir > 0) sink.add_u(CLR_OFF_RF + CLR_RF_CELL_TIR, 1ull);
-        if (r.ttir > 0) sink.add_u(CLR_OFF_RF + CLR_RF_TOP_TIR, 1ull);
-        if (r.btir > 0) sink.add_u(CLR_OFF_RF + CLR_RF_BOTTOM_TIR, 1ull);
+    if (leader) sink.add_u(CLR_OFF_DONE, (unsigned long long)__popc(grp));
+    if (r.pf != 0) sink.add_u(CLR_OFF_SUB + CLR_SUBCODE_INDEX(r.pfs), 1ull);
+    group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_SOURCE_ACCEPTED, st != 3);
+    group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_SOURCE_DIRECT, st != 3 && r.sbr == 0);
+    group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_SOURCE_REFLECTED, st != 3 && r.sbr != 0);
+    group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_VALID_AIR, st == 1 && isfinite(r.x) && isfinite(r.vx));
+    group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_TRAPPED, st == 8);
+    const bool ent = r.entered != 0;
+    if (__any_sync(grp, ent)) {
+        group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_ENTERED, ent);
+        group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_BALLISTIC, ent && r.ic == 0);
+        group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_ENTRY_REFLECTED, ent && r.pc.entry_reflections > 0);
+        group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_INTERNAL_REFLECTED, ent && r.pc.internal_reflections > 0);
+        group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_ABSORBED, ent && r.pc.absorptions > 0);
+        group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_CELL_TIR, ent && r.ctir > 0);
+        group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_TOP_TIR, ent && r.ttir > 0);
+        group_count(sink, grp, leader, CLR_OFF_RF + CLR_RF_BOTTOM_TIR, ent && r.btir > 0);
         const int es[16] = {r.ic, r.gic, r.wic, r.wcoh, r.wmorph, r.pc.reflections, r.cir, r.cor, r.tr, r.bir, r.bor,
                             r.ctir, r.ttir, r.btir, r.pc.entry_reflections, r.pc.internal_reflections};
 #pragma unroll
-        for (int k = 0; k < 16; ++k)
-            if (es[k]) sink.add_u(CLR_OFF_ES + k, (unsigned long long)(unsigned)es[k]);
+        for (int k = 0; k < 16; ++k) group_add(sink, grp, leader, CLR_OFF_ES + k, ent ? es[k] : 0);
         const int ic = r.ic < 0 ? 0 : r.ic;
-        if (ic < 64) sink.add_u(CLR_OFF_ICLO + ic, 1ull);
-        else atomicAdd(ic_hi + (ic < CLR_IC_HIST - 1 ? ic : CLR_IC_HIST - 1), 1ull);
+        group_hist(sink, grp, CLR_OFF_ICLO, ic < 64 ? ic : 0, ent && ic < 64);
+        if (ent && ic >= 64) atomicAdd(tallies[sid].ic_hi + (ic < CLR_IC_HIST - 1 ? ic : CLR_IC_HIST - 1), 1ull);
     }
     if (rec) {
         clr_ray_record o;
@@ -351,6 +397,9 @@ __device__ __forceinline__ void flush_warp_tally(WarpTally* t, DevTally* dst, in
     __syncwarp();
 }
 
+// lanes that must wait in ENTRY/WATER before the warp stops drawing new photons
+constexpr int kDeepThreshold = 24;
+
 template <class Mode, bool kRecord, bool kWeighted>
 __global__ void __launch_bounds__(CLR_TRACE_THREADS) photon_kernel(const DevScene* __restrict__ scenes,
                                                                    const long long* __restrict__ chunk_begin,
@@ -360,13 +409,15 @@ __global__ void __launch_bounds__(CLR_TRACE_THREADS) photon_kernel(const DevScen
                                                                    clr_ray_record* __restrict__ records) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WarpTally* wt = reinterpret_cast<WarpTally*>(smem_raw) + (threadIdx.x >> 5);
+    __shared__ DetTable det;
+    det_table_init(&det);
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     {
         unsigned long long* p = reinterpret_cast<unsigned long long*>(wt);
         for (int i = lane; i < (int)(sizeof(WarpTally) / 8); i += 32) p[i] = 0ull;
         __syncwarp();
     }
-    const TallySink home_sink = tally_sink(wt);
     int home = -1;
     long long cur_pos = 0, cur_end = 0;  // ray range of the warp's current chunk (within scenario cur_sid)
     int cur_sid = 0;
@@ -380,6 +431,7 @@ __global__ void __launch_bounds__(CLR_TRACE_THREADS) photon_kernel(const DevScen
     ray_reset(r);
     const unsigned FULL = 0xffffffffu;
     const unsigned lt_mask = (1u << lane) - 1u;
+    unsigned long long sched_it[3] = {0, 0, 0}, sched_lanes[3] = {0, 0, 0}, sched_cyc[4] = {0, 0, 0, 0};
     while (true) {
         // refill idle lanes from the warp's chunk, fetching new chunks as needed
         unsigned need = __ballot_sync(FULL, !have);
@@ -420,19 +472,45 @@ __global__ void __launch_bounds__(CLR_TRACE_THREADS) photon_kernel(const DevScen
             cur_pos += taken;
             need = __ballot_sync(FULL, !have);
         }
-        if (!__any_sync(FULL, have)) break;
-        if (have) {
+        // Phase-coherent scheduling: the warp runs one phase per iteration so the FP64-heavy phases
+        // execute with many lanes converged. SOURCE keeps refilling lanes until most lanes wait in a
+        // deeper phase (or the work queue is empty); then the deeper phase with the most lanes runs.
+        const unsigned m_src = __ballot_sync(FULL, have && r.phase == PHASE_SOURCE);
+        const unsigned m_ent = __ballot_sync(FULL, have && r.phase == PHASE_ENTRY);
+        const unsigned m_wat = __ballot_sync(FULL, have && r.phase == PHASE_WATER);
+        if (!(m_src | m_ent | m_wat)) break;
+        const int n_src = __popc(m_src), n_ent = __popc(m_ent), n_wat = __popc(m_wat);
+        int pick;
+        if (n_src && !exhausted && n_ent + n_wat < kDeepThreshold) pick = PHASE_SOURCE;
+        else if (n_ent >= n_wat && n_ent >= n_src) pick = PHASE_ENTRY;
+        else if (n_wat >= n_src) pick = PHASE_WATER;
+        else pick = PHASE_SOURCE;
+        const long long t0 = clock64();
+        if (lane == 0) { sched_it[pick]++; sched_lanes[pick] += (unsigned)__popc(pick == PHASE_SOURCE ? m_src : (pick == PHASE_ENTRY ? m_ent : m_wat)); }
+        if (have && r.phase == pick) {
             const DevScene& D = scenes[sid];
-            const TallySink sink = (sid == home) ? home_sink : tally_sink_dev(tallies + sid);
             bool done;
-            if (r.phase == PHASE_LAUNCH) done = launch_segment(D, r, L.transport(), L.source());
+            if (pick == PHASE_SOURCE) done = source_segment(D, r, L.source());
+            else if (pick == PHASE_ENTRY) done = entry_segment(D, r, L.transport());
             else done = water_step<typename Mode::Stream, kWeighted>(D, r, L.transport(), L.optics(),
                                                                       (sid == home) ? &wt->cstats[0] : &tallies[sid].c.cstats[0]);
             if (done) {
-                finish_ray<Mode>(D, r, gid, sink, tallies[sid].ic_hi, kRecord ? records + rid : nullptr);
+                const long long tf = clock64();
+                finish_ray<Mode>(D, det, r, gid, sid, home, wt, tallies, kRecord ? records + rid : nullptr);
                 have = false;
+                if (lane == __ffs(__activemask()) - 1) sched_cyc[3] += (unsigned long long)(clock64() - tf);
             }
         }
+        __syncwarp();
+        if (lane == 0) sched_cyc[pick] += (unsigned long long)(clock64() - t0);
+    }
+    if (lane == 0) {
+        for (int k = 0; k < 3; ++k) {
+            atomicAdd(&tallies[0].sched[k], sched_it[k]);
+            atomicAdd(&tallies[0].sched[4 + k], sched_lanes[k]);
+            atomicAdd(&tallies[0].sched[8 + k], sched_cyc[k]);
+        }
+        atomicAdd(&tallies[0].sched[11], sched_cyc[3]);
     }
     __syncwarp();
     if (home >= 0) flush_warp_tally(wt, tallies + home, lane);

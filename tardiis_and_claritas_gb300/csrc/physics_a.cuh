@@ -204,31 +204,33 @@ __device__ int o_source_collimator(S* st, int model, float n_air, float n_bore, 
     *x = q; *y = s; *z = w; *vx = vq; *vy = vs; *vz = vw;
     return 1;
 }
-/* detector direction tables: identical float arithmetic to (10*j)*(pi/180) then sinf/cosf */
+/* bore directions: sin/cos of (10 j)(pi/180), j = 0..18 (the 18 detectors and the source bore). The kernel
+ * evaluates them once per block with the same device sinf/cosf the reference calls per use (:4241-4244),
+ * so the table holds exactly the values the reference recomputes. */
 __device__ __forceinline__ float o_det_theta(int j) { return (10.0f * (float)j) * (CLR_PI_F / 180.0f); }
 
 template <class S>
 __device__ __noinline__ int o_detector_collimator_path(S* st, float x, float y, float z, float vx, float vy, float vz,
                                       int mirror, float ring_in, float throat_out, float ring_out, float throat_r,
                                       float counterbore_r, int model, float n_air, float n_bore, int max_bounces,
-                                      int* bounce_count) {
+                                      int* bounce_count, const float* dsin, const float* dcos) {
     if (mirror) { x = -x; vx = -vx; }
     float best_t = CLR_INF_F;
     int best = -1;
     for (int j = 0; j < 18; ++j) {
-        float th = o_det_theta(j), ux = sinf(th), uy = cosf(th);
+        float ux = dsin[j], uy = dcos[j];
         float den = vx * ux + vy * uy;
         if (den <= 1.0e-10f) continue;
         float pdot = x * ux + y * uy;
         float t = (ring_in - pdot) / den;
         if (t <= 0.0f) continue;
-        float etx = cosf(th), ety = -sinf(th);
+        float etx = dcos[j], ety = -dsin[j];
         float hx = x + t * vx, hy = y + t * vy, hz = z + t * vz;
         float q = hx * etx + hy * ety, w = hz;
         if (q * q + w * w <= throat_r * throat_r && t < best_t) { best_t = t; best = j; }
     }
     if (best < 0) return -1;
-    float th = o_det_theta(best), ux = sinf(th), uy = cosf(th), etx = cosf(th), ety = -sinf(th);
+    float ux = dsin[best], uy = dcos[best], etx = dcos[best], ety = -dsin[best];
     float hx = x + best_t * vx, hy = y + best_t * vy;
     float s = ring_in, q = hx * etx + hy * ety, w = z + best_t * vz;
     float vs = vx * ux + vy * uy, vq = vx * etx + vy * ety, vw = vz;

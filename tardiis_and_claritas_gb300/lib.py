@@ -46,6 +46,8 @@ def load(build_if_missing: bool = False):
             "clr_trace": ([C.c_void_p, P(abi.RunParams), P(abi.Tallies), C.c_void_p], C.c_int),
             "clr_trace_host_records": ([C.c_void_p, P(abi.RunParams), P(abi.Tallies), C.c_void_p], C.c_int),
             "clr_abi_sizeof": ([C.c_int], C.c_int64),
+            "clr_last_kernel_ms": ([C.c_void_p, P(C.c_float)], C.c_int),
+            "clr_calibrate": ([C.c_void_p, C.c_int, P(C.c_double)], C.c_int),
         }
         for name, (argt, rest) in sig.items():
             f = getattr(lib, name)
@@ -57,7 +59,8 @@ def load(build_if_missing: bool = False):
 
 def exported_symbols() -> list[str]:
     return ["clr_create", "clr_destroy", "clr_last_error", "clr_version", "clr_set_scene", "clr_build_particles",
-            "clr_read_particle_physics", "clr_trace", "clr_trace_host_records", "clr_abi_sizeof"]
+            "clr_read_particle_physics", "clr_trace", "clr_trace_host_records", "clr_abi_sizeof",
+            "clr_last_kernel_ms", "clr_calibrate"]
 
 
 class Context:
@@ -108,6 +111,16 @@ class Context:
         self._check(self.lib.clr_trace(self.h, C.byref(run), C.byref(T), C.c_void_p(records_ptr) if records_ptr else None),
                     "clr_trace")
         return T
+
+    def last_kernel_ms(self) -> float:
+        v = C.c_float()
+        self._check(self.lib.clr_last_kernel_ms(self.h, C.byref(v)), "clr_last_kernel_ms")
+        return float(v.value)
+
+    def calibrate(self, which: int) -> float:
+        v = C.c_double()
+        self._check(self.lib.clr_calibrate(self.h, int(which), C.byref(v)), "clr_calibrate")
+        return float(v.value)
 
     def close(self):
         if self.h:

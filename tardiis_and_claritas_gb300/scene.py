@@ -478,3 +478,83 @@ def three_component_particles(concentration_mg_l: float = 500.0, bins_per_compon
     d, w = d[order], w[order]
     m = d.size
     return Particles(d, w / w.sum(), np.full(m, n), np.full(m, k), concentration_mg_l * 1e-3, density)
+
+
+def stirrer_scully_delta_h(rpm: float, core_radius_m: float, R: float, gravity: float = 9.81) -> float:
+    """Wall-minus-centre height of the localized Scully surface whose core turns at `rpm`.
+
+    Inverts the reference's relation omega_c = sqrt(2 g H_inf)/a with H_inf = dH (a^2+R^2)/R^2
+    (vortex_surface_geometry, CLARITAS/CLARITAS.py:772-779) for dH.
+    """
+    omega = float(rpm) * 2.0 * math.pi / 60.0
+    a, R2 = float(core_radius_m), float(R) * float(R)
+    h_inf = (omega * a) ** 2 / (2.0 * gravity)
+    return h_inf * R2 / (a * a + R2)
+
+
+def rouse_radial_grid(cfg: ModelConfig, n_bins: int, nr: int = 64, nz: int = 64, rouse: float = 0.3,
+                      ref_height_frac: float = 0.05, radial_kappa: float = 0.5) -> tuple[np.ndarray, float]:
+    """Concentration-scale field on the reference's cell-centred (r, z) grid, volume mean 1 over the water.
+
+    Vertical: Rouse profile c/c_a = [((h - s)/s) (a/(h - a))]^P, s the height above the bottom, h the local
+    water depth, a = ref_height_frac*h (clamped below a). Radial: centrifugal depletion exp(kappa (r^2/R^2 - 1)).
+    Cells above the local free surface take the value of the highest liquid cell in their column, as the
+    reference's grid extension does (CLARITAS/CLARITAS.py:4195-4201), so bilinear lookups near the surface
+    stay inside the field. Returns (grid [bins][nr][nz], grid_zmax).
+    """
+    R, zmin = float(cfg.tube_inner_radius_m), cfg.zmin
+    vg = vortex_surface_geometry(cfg.free_surface_model, cfg.zmean, R, cfg.vortex_wall_center_height_difference_m,
+                                 cfg.vortex_core_radius_m, cfg.gravity_m_s2)
+    zmax = float(vg["wall_z"])
+    dr, dz = R / nr, (zmax - zmin) / nz
+    rc = (np.arange(nr) + 0.5) * dr
+    zc = zmin + (np.arange(nz) + 0.5) * dz
+
+    def surface(r):
+        if cfg.free_surface_model == "flat" or cfg.vortex_wall_center_height_difference_m <= 0:
+            return np.full_like(r, cfg.zmean)
+        dh = cfg.vortex_wall_center_height_difference_m
+        if cfg.free_surface_model == "parabolic_vortex":
+            return cfg.zmean + dh * (r * r / (R * R) - 0.5)
+        a2, R2 = cfg.vortex_core_radius_m ** 2, R * R
+        return cfg.zmean - vg["h_bar"] + vg["h_inf"] * r * r / (a2 + r * r)
+
+    zs = surface(rc)
+    g = np.zeros((nr, nz))
+    active = np.zeros((nr, nz), bool)
+    for i in range(nr):
+        h = zs[i] - zmin
+        a = ref_height_frac * h
+        s = np.clip(zc - zmin, 1e-9, None)
+        live = zc < zs[i]
+        prof = np.where(s > a, (((h - s) / s) * (a / (h - a))).clip(min=0.0) ** rouse, 1.0)
+        g[i] = prof * math.exp(radial_kappa * (rc[i] ** 2 / (R * R) - 1.0))
+        active[i] = live
+        top = np.nonzero(live)[0]
+        if top.size:
+            g[i, top[-1] + 1:] = g[i, top[-1]]
+    w = (rc[:, None] * dr * dz) * active
+    g /= (g * w).sum() / w.sum()
+    return np.ascontiguousarray(np.broadcast_to(g, (n_bins, nr, nz))), zmax
+
+
+def full_scene_workload(n_photons: int = 100_000_000):
+    """The full scene: three-component mixture at 500 mg/L in a (r, z) Rouse x radial-depletion field with a
+    stirred (600 rpm, 5 mm core) free surface, small cell. Returns (config, particles, grid)."""
+    base = small_cell_config(particle_surface_rms_slope_deg=0.0, wave_surface_rms_height_m=0.0)
+    dh = stirrer_scully_delta_h(600.0, 0.005, base.tube_inner_radius_m)
+    cfg = small_cell_config(particle_surface_rms_slope_deg=0.0, wave_surface_rms_height_m=0.0,
+                            free_surface_model="localized_scully_vortex", vortex_wall_center_height_difference_m=dh,
+                            vortex_core_radius_m=0.005,
+                            sediment_transport_model="schiller_naumann_meridional_advection_diffusion")
+    cfg.validate()
+    parts = three_component_particles(500.0)
+    grid, zmax = rouse_radial_grid(cfg, parts.diameter_m.size)
+    return cfg, parts, grid, zmax
+
+
+def small_plain_workload():
+    """The small plain-MC case: 64 lognormal bins (median 20 um, sigma_g 1.6) of quartz at 100 mg/L, uniform."""
+    cfg = small_cell_config(particle_surface_rms_slope_deg=0.0, wave_surface_rms_height_m=0.0)
+    cfg.validate()
+    return cfg, quartz_particles(100.0), None, None

@@ -84,12 +84,12 @@ def load(kind: str = "port"):
 class OracleRun:
     """Prepared scene in one of the CPU oracles."""
 
-    def __init__(self, kind, cfg, particles, grid=None, moments=None):
+    def __init__(self, kind, cfg, particles, grid=None, moments=None, grid_zmax=None):
         self.lib, self.p = load(kind)
         self.cfg = cfg
         self.sp = cfg.to_scene_params()
         self.ps = particles.spec(cfg, moments)
-        self.ss = cfg.sediment_spec(grid)
+        self.ss = cfg.sediment_spec(grid, grid_zmax)
         self.h = C.c_void_p()
         rc = getattr(self.lib, self.p + "prepare")(C.byref(self.sp), C.byref(self.ps), C.byref(self.ss),
                                                    C.byref(self.h))
