@@ -55,6 +55,16 @@ enum {
     CLR_RNG_PHILOX = 1              /* counter-based Philox4x32-10 keyed by (seed, scenario, photon) */
 };
 
+/* run flags */
+enum {
+    /* the counter-based stream uses the reference's own samplers everywhere, with no
+       equivalent-distribution replacement (validates those replacements) */
+    CLR_RUN_EXACT_SAMPLERS = 1,
+    /* run the single persistent photon kernel instead of the wavefront engine (same per-ray results
+       in the xorshift parity mode; kept for comparison and as the record-run fallback) */
+    CLR_RUN_PERSISTENT_KERNEL = 2
+};
+
 /* photon weighting */
 enum {
     CLR_WEIGHT_ANALOG = 0,   /* reference semantics: absorption is terminal, every weight is 1 */
@@ -153,7 +163,8 @@ typedef struct clr_run_params {
     float roulette_survival;        /* weight given to survivors; probability = w / survival */
     int32_t max_blocks;             /* 0 = occupancy-derived grid; >0 caps the resident blocks (tuning, tests) */
     int32_t rays_per_item;          /* work-queue granularity; 0 = default */
-    int32_t reserved[4];
+    int32_t flags;                  /* CLR_RUN_* bits */
+    int32_t reserved[3];
 } clr_run_params;
 
 /* Per-ray record, written only when a record buffer is passed to clr_trace

@@ -54,6 +54,8 @@ CLR_ERR_DEVICE_TIMEOUT = -6
 
 RNG_REFERENCE_XORSHIFT = 0
 RNG_PHILOX = 1
+RUN_EXACT_SAMPLERS = 1
+RUN_PERSISTENT_KERNEL = 2
 WEIGHT_ANALOG = 0
 WEIGHT_IMPLICIT = 1
 SOURCE_REFERENCE_LED = 0
@@ -121,7 +123,7 @@ class RunParams(C.Structure):
         ("n_rays", i64), ("ray_offset", u32), ("seed0", u32), ("seed1", u32), ("seed2", u32),
         ("detector_seed", u32), ("rng_mode", i32), ("philox_key", u64), ("scenario_id", u32),
         ("weight_mode", i32), ("roulette_threshold", f32), ("roulette_survival", f32),
-        ("max_blocks", i32), ("rays_per_item", i32), ("reserved", i32 * 4),
+        ("max_blocks", i32), ("rays_per_item", i32), ("flags", i32), ("reserved", i32 * 3),
     ]
 
 

@@ -34,6 +34,16 @@ struct clr_ctx {
     int num_sms = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_kernel_ms = 0.0f;
+    // wavefront engine pool (allocated on first use)
+    unsigned wave_cap = 0;
+    void *wave_ray = nullptr, *wave_lane = nullptr;
+    SlotMeta* wave_meta = nullptr;
+    uint32_t* wave_q = nullptr;
+    WaveCtl* wave_ctl = nullptr;
+    long long* wave_begin = nullptr;
+    unsigned* wave_live = nullptr;  // pinned
+    cudaEvent_t wave_ev = nullptr;
+    int last_passes = 0;
 };
 
 static int fail(clr_ctx* c, int code, const char* fmt, ...) {
@@ -99,6 +109,14 @@ int clr_destroy(clr_ctx* ctx) {
     cudaFree(ctx->d_chunk_begin);
     cudaFree(ctx->d_tally);
     cudaFree(ctx->d_work);
+    cudaFree(ctx->wave_ray);
+    cudaFree(ctx->wave_lane);
+    cudaFree(ctx->wave_meta);
+    cudaFree(ctx->wave_q);
+    cudaFree(ctx->wave_ctl);
+    cudaFree(ctx->wave_begin);
+    if (ctx->wave_live) cudaFreeHost(ctx->wave_live);
+    if (ctx->wave_ev) cudaEventDestroy(ctx->wave_ev);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -162,7 +180,7 @@ int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sed
     double** darr[] = {&pb.d, &pb.w, &pb.nidx, &pb.kidx, &pb.x, &pb.qext, &pb.qsca, &pb.qabs, &pb.qback, &pb.g,
                        &pb.albedo, &pb.radius, &pb.nden, &pb.mug, &pb.mus, &pb.mue, &pb.muw, &pb.muev, &pb.gcdf,
                        &pb.wcdf, &pb.pcdf, &pb.moment_a, &pb.moment_b, &pb.trace_geom, &pb.trace_wave, &pb.sedA,
-                       &pb.sedB, &pb.sed_norm, &pb.sed_max};
+                       &pb.sedB, &pb.sed_norm, &pb.sed_max, &pb.grid_max};
     for (double** p : darr) CU(D(p, n));
     float** farr[] = {&pb.gcdf_f, &pb.wcdf_f, &pb.pn_f, &pb.pk_f, &pb.prad_f};
     for (float** p : farr) CU(F(p, n));
@@ -199,6 +217,15 @@ int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sed
     CU(cudaMemcpyAsync(pb.moment_b, mb.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(pb.moment_mode, mm.data(), n, cudaMemcpyHostToDevice, st));
     if (sp.sediment_model == 3) {
+        bool nonneg = ss->grid_zmax > (double)sp.zmin;
+        for (size_t c = 0; c < grid_cells && nonneg; ++c) nonneg = ss->grid[c] >= 0.0;
+        const size_t plane = (size_t)pb.grid_nr * pb.grid_nz;
+        if (nonneg && 2 * plane * n * sizeof(int2) <= (size_t(1) << 30)) {
+            pb.node_tables = 1;
+            CU(dalloc(ctx, (void**)&pb.node_mu, plane * sizeof(float2)));
+            CU(dalloc(ctx, (void**)&pb.node_alias, 2 * plane * n * sizeof(int2)));
+            CU(dalloc(ctx, (void**)&pb.node_major, sizeof(float)));
+        }
         CU(cudaMemcpyAsync(pb.sed_grid, ss->grid, grid_cells * sizeof(double), cudaMemcpyHostToDevice, st));
     } else {
         const double one[4] = {1.0, 1.0, 1.0, 1.0};
@@ -207,6 +234,8 @@ int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sed
     CU(enqueue_particle_precompute(pb, sp, *ps, *ss, nullptr, st));
     int herr = 0;
     CU(cudaMemcpyAsync(&herr, pb.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (pb.node_tables)
+        CU(cudaMemcpyAsync(&pb.node_major_host, pb.node_major, sizeof(float), cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     if (herr) return fail(ctx, CLR_ERR_PRECOMPUTE, "particle precompute failed with error code %d", herr);
     ctx->built = true;
@@ -255,6 +284,10 @@ static void fill_scene(const clr_ctx* ctx, const clr_run_params* run, DevScene* 
     s->sed_grid = pb.sed_grid; s->mu_channels = pb.muscal; s->sed_major = pb.sed_major;
     s->n_bins = pb.n; s->nt = pb.nt; s->n_radial = pb.n_radial; s->grid_nr = pb.grid_nr; s->grid_nz = pb.grid_nz;
     s->any_moment = pb.any_moment; s->grid_zmax = (float)pb.grid_zmax;
+    const bool node = pb.node_tables && !(run->flags & CLR_RUN_EXACT_SAMPLERS);
+    s->node_mu = node ? pb.node_mu : nullptr;
+    s->node_alias = node ? pb.node_alias : nullptr;
+    s->node_major = pb.node_major_host;
     s->seed0 = run->seed0; s->seed1 = run->seed1; s->seed2 = run->seed2; s->det_seed = run->detector_seed;
     s->ray_offset = run->ray_offset; s->scenario_id = run->scenario_id; s->philox_key = run->philox_key;
     s->n_rays = run->n_rays; s->weight_mode = run->weight_mode;
@@ -287,6 +320,23 @@ static void tally_to_host(const DevTally& d, clr_tallies* out, int64_t n_rays) {
     out->device_error = (t.n_done == (unsigned long long)n_rays) ? 0 : 1;
 }
 
+// Photon pool of the wavefront engine: 2^20 slots (about 230 MB), allocated once per context.
+static int wave_pool_ready(clr_ctx* ctx) {
+    if (ctx->wave_cap) return CLR_OK;
+    const unsigned cap = 1u << 20;
+    const size_t lane = std::max(wave_lane_bytes(CLR_RNG_PHILOX), wave_lane_bytes(CLR_RNG_REFERENCE_XORSHIFT));
+    CU(cudaMalloc(&ctx->wave_ray, (size_t)cap * wave_ray_bytes()));
+    CU(cudaMalloc(&ctx->wave_lane, (size_t)cap * lane));
+    CU(cudaMalloc(&ctx->wave_meta, (size_t)cap * sizeof(SlotMeta)));
+    CU(cudaMalloc(&ctx->wave_q, (size_t)CLR_WQ_COUNT * cap * sizeof(uint32_t)));
+    CU(cudaMalloc(&ctx->wave_ctl, sizeof(WaveCtl)));
+    CU(cudaMalloc(&ctx->wave_begin, 2 * sizeof(long long)));
+    CU(cudaHostAlloc((void**)&ctx->wave_live, sizeof(unsigned), cudaHostAllocDefault));
+    CU(cudaEventCreateWithFlags(&ctx->wave_ev, cudaEventDisableTiming));
+    ctx->wave_cap = cap;
+    return CLR_OK;
+}
+
 static int trace_impl(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* d_records) {
     if (!ctx || !run || !out) return CLR_ERR_INVALID_ARGUMENT;
     if (!ctx->built) return fail(ctx, CLR_ERR_NOT_READY, "clr_build_particles must succeed before clr_trace");
@@ -317,8 +367,29 @@ static int trace_impl(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out,
     long long blocks_needed = (warps_needed * 32 + CLR_TRACE_THREADS - 1) / CLR_TRACE_THREADS;
     a.grid = (int)std::max(1LL, std::min(want, blocks_needed));
     if (run->max_blocks > 0) a.grid = std::max(1, std::min(a.grid, run->max_blocks));
+    const bool persistent = (run->flags & CLR_RUN_PERSISTENT_KERNEL) != 0;
+    WaveLaunch w{};
+    if (!persistent) {
+        int rc = wave_pool_ready(ctx);
+        if (rc != CLR_OK) return rc;
+        const long long rb[2] = {0, run->n_rays};
+        CU(cudaMemcpyAsync(ctx->wave_begin, rb, sizeof rb, cudaMemcpyHostToDevice, st));
+        w.scenes = ctx->d_scene; w.n_scen = 1; w.ray_begin = ctx->wave_begin; w.total = (unsigned long long)run->n_rays;
+        w.tallies = ctx->d_tally; w.records = d_records;
+        w.ray = ctx->wave_ray; w.lane = ctx->wave_lane; w.meta = ctx->wave_meta; w.qbuf = ctx->wave_q;
+        w.ctl = ctx->wave_ctl; w.cap = ctx->wave_cap; w.host_live = ctx->wave_live; w.flag_event = ctx->wave_ev;
+    }
     CU(cudaEventRecord(ctx->ev0, st));
-    if (cb[1] > 0) CU(launch_photon_kernel(a));
+    if (persistent) {
+        if (cb[1] > 0) CU(launch_photon_kernel(a));
+    } else if (run->n_rays > 0) {
+        const long long max_passes = 100000 + 8LL * (long long)ctx->sp.max_iterations;
+        cudaError_t e = a.rng_mode == CLR_RNG_PHILOX ? wave_run_philox(w, ctx->num_sms, st, max_passes, &ctx->last_passes)
+                                                     : wave_run_xor(w, ctx->num_sms, st, max_passes, &ctx->last_passes);
+        if (e == cudaErrorLaunchTimeout)
+            return fail(ctx, CLR_ERR_DEVICE_TIMEOUT, "wavefront engine did not drain within %lld passes", max_passes);
+        CU(e);
+    }
     CU(cudaEventRecord(ctx->ev1, st));
     DevTally ht;
     CU(cudaMemcpyAsync(&ht, ctx->d_tally, sizeof ht, cudaMemcpyDeviceToHost, st));

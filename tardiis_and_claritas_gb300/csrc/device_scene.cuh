@@ -33,6 +33,11 @@ struct DevScene {
     const double* sed_grid;
     const double* mu_channels;  // [8] transport_precompute_kernel output
     const double* sed_major;    // [4]
+    // Node tables of the (r, z) field for the counter-based stream (sediment model 3 only): per node the
+    // channel rates summed over bins, and per channel and node an alias table over bins. Null when absent.
+    const float2* node_mu;      // [nr*nz] (geometric, wave)
+    const int2* node_alias;     // [2][nr*nz][n_bins] (probability bits, alias bin)
+    float node_major;           // max over nodes of the summed rate: a majorant of the interpolated field
     int32_t n_bins, nt, n_radial, grid_nr, grid_nz, any_moment;
     float grid_zmax;
     // run description of this scenario

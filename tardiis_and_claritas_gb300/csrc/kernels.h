@@ -34,6 +34,45 @@ inline int photon_kernel_occupancy(int rng_mode, bool records, bool /*weighted*/
     return rng_mode == CLR_RNG_PHILOX ? occupancy_philox(records) : occupancy_xor(records);
 }
 
+// ---------------- wavefront engine (wavefront.cuh) ----------------
+#define CLR_WQ_COUNT 10  // stage queues: free, entry, flight, cond, geom, morph, top, bottom, side, fin
+
+struct SlotMeta {
+    uint32_t gid;   // global ray id (ray_offset + rid): the random-stream key
+    int32_t sid;    // scenario
+    long long rid;  // ray index within the scenario
+    int32_t pidx;   // size bin of a pending particle event
+    int32_t pad;
+};
+
+struct WaveCtl {
+    unsigned long long next_photon, total_photons;
+    unsigned head[CLR_WQ_COUNT], tail[CLR_WQ_COUNT], snap[CLR_WQ_COUNT], finished[CLR_WQ_COUNT];
+    unsigned live, passes;
+};
+
+struct WaveLaunch {
+    const DevScene* scenes;
+    int n_scen;
+    const long long* ray_begin;    // [n_scen + 1] first photon of each scenario in the run's photon order
+    unsigned long long total;
+    DevTally* tallies;
+    clr_ray_record* records;       // nullable
+    void* ray;                     // [cap] Ray
+    void* lane;                    // [cap] random-stream state
+    SlotMeta* meta;                // [cap]
+    uint32_t* qbuf;                // [CLR_WQ_COUNT][cap]
+    WaveCtl* ctl;
+    unsigned cap;                  // slots, a power of two
+    unsigned* host_live;           // pinned host word
+    cudaEvent_t flag_event;
+};
+
+cudaError_t wave_run_xor(const WaveLaunch& w, int num_sms, cudaStream_t st, long long max_passes, int* passes);
+cudaError_t wave_run_philox(const WaveLaunch& w, int num_sms, cudaStream_t st, long long max_passes, int* passes);
+size_t wave_ray_bytes();
+size_t wave_lane_bytes(int rng_mode);
+
 // Calibration kernels (calibrate.cu): FP32 FFMA (which=0) or FP64 DFMA (which=1) throughput loops.
 // Sets *ops to the number of operations the launch performs (an FMA counts 2).
 cudaError_t launch_calibration(int which, int num_sms, cudaStream_t stream, double* ops);
@@ -57,8 +96,14 @@ struct ParticleBuffers {
     int any_moment = 0;
     double *trace_geom = nullptr, *trace_wave = nullptr;
     double *sedA = nullptr, *sedB = nullptr, *sed_norm = nullptr, *sed_max = nullptr, *sed_radial_log = nullptr,
-           *sed_wr = nullptr, *sed_major = nullptr, *sed_grid = nullptr;
+           *sed_wr = nullptr, *sed_major = nullptr, *sed_grid = nullptr, *grid_max = nullptr;
     int* err = nullptr;
+    // node tables of the (r, z) field for the counter-based stream (sediment model 3, non-negative grid)
+    int node_tables = 0;
+    float2* node_mu = nullptr;     // [nr*nz]
+    int2* node_alias = nullptr;    // [2][nr*nz][n]
+    float* node_major = nullptr;   // [1]
+    float node_major_host = 0.0f;
 };
 
 // Enqueue the whole precompute on `stream`. Host inputs are copied in; error codes land in pb.err.

@@ -290,30 +290,109 @@ __device__ __forceinline__ bool entry_segment(const DevScene& D, Ray& r, S* st) 
     return false;
 }
 
+// ---------------- field lookup for the counter-based stream (sediment model 3) ----------------
+// The interpolated field sum_i mu_i g_i(r, z) is linear in the node values, so it equals the bilinear
+// interpolation of the node sums G_c = sum_i mu_i g_i[c]. A bin drawn with probability proportional to
+// mu_i g_i(r, z) is drawn by composition: a corner c with probability w_c G_c / sum_c' w_c' G_c', then a
+// bin from node c's alias table (probability mu_i g_i[c] / G_c). The distribution is the reference's
+// (o_sample_local_bin); the work is four node reads and one alias read instead of a pass over all bins.
+struct NodeLookup {
+    int node[4];
+    float wg[2][4];
+    float local[2];
+};
+
+__device__ __forceinline__ void node_lookup(const DevScene& D, float x, float y, float z, NodeLookup& L) {
+    const int NR = D.grid_nr, NZ = D.grid_nz;
+    const float R = D.P.rin, zmin = D.P.zmin;
+    const float rr = fminf(sqrtf(fmaxf(x * x + y * y, 0.0f)), R);
+    float ur = rr * ((float)NR / R) - 0.5f;
+    float uz = (z - zmin) * ((float)NZ / (D.grid_zmax - zmin)) - 0.5f;
+    ur = fminf(fmaxf(ur, 0.0f), (float)(NR - 1));
+    uz = fminf(fmaxf(uz, 0.0f), (float)(NZ - 1));
+    int i = (int)ur, k = (int)uz;
+    float tr = ur - (float)i, tz = uz - (float)k;
+    if (i >= NR - 1) { i = NR - 2; tr = 1.0f; }
+    if (k >= NZ - 1) { k = NZ - 2; tz = 1.0f; }
+    const int b = i * NZ + k;
+    L.node[0] = b; L.node[1] = b + NZ; L.node[2] = b + 1; L.node[3] = b + NZ + 1;
+    const float w[4] = {(1.0f - tr) * (1.0f - tz), tr * (1.0f - tz), (1.0f - tr) * tz, tr * tz};
+    float lg = 0.0f, lw = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const float2 g = __ldg(&D.node_mu[L.node[c]]);
+        L.wg[0][c] = w[c] * g.x;
+        L.wg[1][c] = w[c] * g.y;
+        lg += L.wg[0][c];
+        lw += L.wg[1][c];
+    }
+    L.local[0] = lg;
+    L.local[1] = lw;
+}
+
+template <class S>
+__device__ __forceinline__ int node_sample_bin(const DevScene& D, S* st, const NodeLookup& L, int ch) {
+    if (!(L.local[ch] > 0.0f)) return 0;
+    const float target = uniform(st) * L.local[ch];
+    int c = -1, last = 0;
+    float cum = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float wq = L.wg[ch][q];
+        if (wq > 0.0f) last = q;
+        cum += wq;
+        if (c < 0 && wq > 0.0f && target < cum) c = q;
+    }
+    if (c < 0) c = last;
+    const int n = D.n_bins;
+    const int2* A = D.node_alias + ((size_t)ch * (size_t)(D.grid_nr * D.grid_nz) + (size_t)L.node[c]) * (size_t)n;
+    const int j = (int)__umulhi(st->next(), (uint32_t)n);
+    const int2 e = __ldg(&A[j]);
+    return (uniform(st) < __int_as_float(e.x)) ? j : e.y;
+}
+
 // ---------------- one water free-flight step (one iteration of :4734-5066) ----------------
-// Returns true when the history ended.
-template <class S, bool kWeighted>
-__device__ __forceinline__ bool water_step(const DevScene& D, Ray& r, S* st, S* opt, unsigned long long* cstats) {
+// An iteration is split into its flight part (boundary distances, free path, move, delta-tracking
+// acceptance, channel and bin choice, and the cheap outcomes: null collisions, coherent Mie
+// scattering, Fresnel reflections at the free surface and the cell wall) and one handler per
+// expensive outcome (conditional closure, geometric sphere, spheroid morphology, transmission into
+// the headspace or the acrylic wall, bottom disc). The persistent kernel runs both back to back
+// (water_step); the wavefront engine runs each handler as its own kernel over a queue of photons.
+// Split or not, the arithmetic and the per-ray draw order are those of the reference iteration.
+enum : int { WE_NONE = 0, WE_ENDED = 1, WE_COND = 2, WE_GEOM = 3, WE_MORPH = 4, WE_TOP = 5, WE_BOTTOM = 6,
+             WE_SIDE = 7 };
+
+__device__ __forceinline__ void apply_moment(const DevScene& D, int pidx, float vinx, float viny, float vinz, float* vx,
+                                             float* vy, float* vz) {
+    if (D.any_moment && pidx >= 0 && D.moment_mode[pidx])
+        moment_constraint(vinx, viny, vinz, vx, vy, vz, (float)D.moment_a[pidx], (float)D.moment_b[pidx]);
+}
+
+// Flight part. Returns WE_NONE when the iteration completed (the photon stays in the water),
+// WE_ENDED when the history ended, else the handler that completes the iteration (*ev_pidx is the
+// bin of a particle event). Position and direction are stored in r in every case.
+template <class S>
+__device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S* opt, unsigned long long* cstats,
+                                            int* ev_pidx) {
     const clr_scene_params& P = D.P;
-    if (r.step >= (int)P.max_iterations) { r.pf = OP_ITERATION_LIMIT; r.pfs = OS_ITERATION_LIMIT; r.st = 4; return true; }
+    if (r.step >= (int)P.max_iterations) { r.pf = OP_ITERATION_LIMIT; r.pfs = OS_ITERATION_LIMIT; r.st = 4; return WE_ENDED; }
     r.step++;
     r.steps++;
     const int TM = P.sediment_model, FSM = P.free_surface_model;
     const float RIN = P.rin, ZMIN = P.zmin, ZMEAN = P.zmean, ZTOP = P.zwall_top, DH = P.vortex_delta_h,
                 CORE = P.vortex_core_radius;
     float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
-    bool ended = false;
-    o_bcount bc = {0, 0, 0, 0, 0, 0, 0, 0};
+    int res = WE_NONE;
     do {
-        if (!isfinite(x) || !isfinite(y) || !isfinite(z)) { r.pf = OP_NONFINITE_POSITION; r.pfs = OS_NONFINITE_POSITION; r.st = 4; ended = true; break; }
-        if (!isfinite(vx) || !isfinite(vy) || !isfinite(vz)) { r.pf = OP_NONFINITE_DIRECTION; r.pfs = OS_NONFINITE_DIRECTION; r.st = 4; ended = true; break; }
+        if (!isfinite(x) || !isfinite(y) || !isfinite(z)) { r.pf = OP_NONFINITE_POSITION; r.pfs = OS_NONFINITE_POSITION; r.st = 4; res = WE_ENDED; break; }
+        if (!isfinite(vx) || !isfinite(vy) || !isfinite(vz)) { r.pf = OP_NONFINITE_DIRECTION; r.pfs = OS_NONFINITE_DIRECTION; r.st = 4; res = WE_ENDED; break; }
         float zsurf_here = o_surface_z(x, y, ZMEAN, RIN, FSM, DH, CORE);
-        if (z <= ZMIN || z >= zsurf_here) { r.st = 2; ended = true; break; }
+        if (z <= ZMIN || z >= zsurf_here) { r.st = 2; res = WE_ENDED; break; }
         double rr2w = (double)x * (double)x + (double)y * (double)y, ri2w = (double)RIN * (double)RIN;
         double water_tol = 8.0 * 1.1920928955078125e-7 * ri2w;
-        if (rr2w > ri2w + water_tol) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; ended = true; break; }
+        if (rr2w > ri2w + water_tol) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break; }
         double tsided = o_bore_wall_hit(x, y, z, vx, vy, vz, RIN, ZMIN, ZTOP);
-        if (tsided < 0.0) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; ended = true; break; }
+        if (tsided < 0.0) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break; }
         float tside = (tsided < 0.5 * (double)CLR_INF_F) ? (float)tsided : CLR_INF_F;
         float ttop = o_surface_hit(x, y, z, vx, vy, vz, ZMEAN, RIN, FSM, DH, CORE), tbottom = CLR_INF_F;
         if (vz < -1e-14f) tbottom = (ZMIN - z) / vz;
@@ -323,11 +402,14 @@ __device__ __forceinline__ bool water_step(const DevScene& D, Ray& r, S* st, S* 
         int axial_bottom = (tbottom < ttop && tbottom < tside);
         int axial = axial_top || axial_bottom;
         float tbound = axial_top ? ttop : (axial_bottom ? tbottom : tside);
-        if (tbound >= CLR_INF_F * 0.5f) { r.pf = OP_WATER_NO_BOUNDARY; r.pfs = OS_WATER_NO_BOUNDARY; r.st = 4; ended = true; break; }
+        if (tbound >= CLR_INF_F * 0.5f) { r.pf = OP_WATER_NO_BOUNDARY; r.pfs = OS_WATER_NO_BOUNDARY; r.st = 4; res = WE_ENDED; break; }
         const float MU_GEOM = (float)D.mu_channels[0], MU_WAVE = (float)D.mu_channels[1];
         float freep = CLR_INF_F;
         float MU_TOTAL = MU_GEOM + MU_WAVE;
-        float MU_TRACK = (TM == 0) ? MU_TOTAL : ((float)D.sed_major[0] + (float)D.sed_major[1]);
+        // counter-based streams with node tables use the node-sum majorant (never above the reference's)
+        const bool node_fast = kCounterStream<S> && TM == 3 && D.node_alias != nullptr;
+        float MU_TRACK = (TM == 0) ? MU_TOTAL : node_fast ? D.node_major
+                                                          : ((float)D.sed_major[0] + (float)D.sed_major[1]);
         if (tbound > 0.0f && MU_TRACK > 0.0f) { float u = fmaxf(uniform(st), 1e-12f); freep = -logf(u) / MU_TRACK; }
         int do_particle = freep < tbound;
         float travel = do_particle ? freep : tbound;
@@ -336,176 +418,109 @@ __device__ __forceinline__ bool water_step(const DevScene& D, Ray& r, S* st, S* 
         double endpoint_r2 = (double)x * x + (double)y * y;
         if (do_particle && (endpoint_r2 > ri2w + water_tol || z < ZMIN - CLR_EPS_F ||
                             z > o_surface_z(x, y, ZMEAN, RIN, FSM, DH, CORE) + CLR_EPS_F)) {
-            r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; ended = true; break;
+            r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break;
         }
         if (do_particle) {
             const o_field F = make_field(D);
             float LOCAL_GEOM = MU_GEOM, LOCAL_WAVE = MU_WAVE, LOCAL_TOTAL = MU_TOTAL;
+            NodeLookup NL;
             if (TM != 0) {
-                double lg = 0.0, lw = 0.0;
-                for (int i = 0; i < D.n_bins; ++i) {
-                    double sc = o_local_scale(&F, i, x, y, z);
-                    lg += D.trace_geom[i] * sc;
-                    lw += D.trace_wave[i] * sc;
+                if (node_fast) {
+                    node_lookup(D, x, y, z, NL);
+                    LOCAL_GEOM = NL.local[0]; LOCAL_WAVE = NL.local[1];
+                } else if (TM == 3) {
+                    const o_grid_w gw = o_grid_weights(&F, x, y, z);
+                    double lg = 0.0, lw = 0.0;
+                    for (int i = 0; i < D.n_bins; ++i) {
+                        double sc = o_grid_sample_w(&F, gw, i);
+                        lg += D.trace_geom[i] * sc;
+                        lw += D.trace_wave[i] * sc;
+                    }
+                    LOCAL_GEOM = (float)lg; LOCAL_WAVE = (float)lw;
+                } else {
+                    double lg = 0.0, lw = 0.0;
+                    for (int i = 0; i < D.n_bins; ++i) {
+                        double sc = o_local_scale(&F, i, x, y, z);
+                        lg += D.trace_geom[i] * sc;
+                        lw += D.trace_wave[i] * sc;
+                    }
+                    LOCAL_GEOM = (float)lg; LOCAL_WAVE = (float)lw;
                 }
-                LOCAL_GEOM = (float)lg; LOCAL_WAVE = (float)lw; LOCAL_TOTAL = LOCAL_GEOM + LOCAL_WAVE;
+                LOCAL_TOTAL = LOCAL_GEOM + LOCAL_WAVE;
                 if (!(LOCAL_TOTAL > 0.0f)) { r.nulls++; break; }
                 float slack = 64.0f * 1.1920928955078125e-7f * fmaxf(fabsf(MU_TRACK), 1.0f);
-                if (LOCAL_TOTAL > MU_TRACK + slack) { r.pf = OP_MAJORANT_VIOLATION; r.pfs = OS_MAJORANT; r.st = 4; ended = true; break; }
+                if (LOCAL_TOTAL > MU_TRACK + slack) { r.pf = OP_MAJORANT_VIOLATION; r.pfs = OS_MAJORANT; r.st = 4; res = WE_ENDED; break; }
                 float pacc = LOCAL_TOTAL / fmaxf(MU_TRACK, 1e-30f);
                 if (pacc > 1.0f) pacc = 1.0f;
                 if (uniform(st) >= pacc) { r.nulls++; break; }
             }
             r.ic++;
             const float vinx = vx, viny = vy, vinz = vz;
-            int event_pidx = -1;
-            float ipath = 0.0f;
             const int COND = (P.event_model == 4 || P.event_model == 5);
             const float COHERENT = fminf(fmaxf((float)D.mu_channels[7], 0.0f), 1.0f);
             int use_wave = (LOCAL_WAVE > 0.0f && uniform(st) * LOCAL_TOTAL >= LOCAL_GEOM);
             int sel = -1;
             if (COND) {
                 if (TM == 0) sel = o_sample_cdf(st, use_wave ? D.wcdf : D.gcdf, D.n_bins);
+                else if (node_fast) sel = node_sample_bin(D, st, NL, use_wave);
                 else sel = o_sample_local_bin(st, &F, use_wave ? D.trace_wave : D.trace_geom, x, y, z,
                                               (double)(use_wave ? LOCAL_WAVE : LOCAL_GEOM));
             }
             if (COND && D.k[sel] > 0.0) {
-                if (D.pk[sel] == 0.0f) { r.pf = OP_OTHER; r.pfs = 9003; r.st = 4; atomicAdd(&cstats[8], 1ull); ended = true; break; }
-                Hist h;
-                conditional_interaction(opt, &h, sel, D.qsca[sel], D.qext[sel], P.n_water, D.pn[sel], D.pk[sel],
-                                        P.wavelength, P.rough_alpha, D.prad[sel], P.spheroid_aspect,
-                                        P.orientation_model, P.orientation_kappa, P.max_particle_bounces, COHERENT,
-                                        D.phase_cdf, D.theta, D.nt, x, y, z, vx, vy, vz, RIN, ZMIN, ZMEAN, FSM, DH,
-                                        CORE, P.conditional_retries, cstats);
-                event_pidx = sel;
-                if (h.status != 1 && h.status != 2) { r.pf = h.failure ? h.failure : OP_OTHER; r.pfs = h.subcode; r.st = 4; ended = true; break; }
-                x = h.x; y = h.y; z = h.z; vx = h.vx; vy = h.vy; vz = h.vz;
-                r.pc.reflections += h.pc.reflections; r.pc.entry_reflections += h.pc.entry_reflections;
-                r.pc.internal_reflections += h.pc.internal_reflections; r.pc.absorptions += h.pc.absorptions;
-                if (h.channel == 0) r.gic++;
-                else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
-                if (h.status == 2) { r.st = 5; ended = true; break; }
-            } else if (use_wave) {
+                if (D.pk[sel] == 0.0f) { r.pf = OP_OTHER; r.pfs = 9003; r.st = 4; atomicAdd(&cstats[8], 1ull); res = WE_ENDED; break; }
+                *ev_pidx = sel;
+                res = WE_COND;
+                break;
+            }
+            if (use_wave) {
                 if (COND) atomicAdd(&cstats[0], 1ull);
                 r.wic++;
                 int pidx = sel >= 0 ? sel
                                     : (TM == 0) ? o_sample_cdf(st, D.wcdf, D.n_bins)
+                                    : node_fast ? node_sample_bin(D, st, NL, 1)
                                                 : o_sample_local_bin(st, &F, D.trace_wave, x, y, z, (double)LOCAL_WAVE);
-                event_pidx = pidx;
                 int coherent = (COHERENT >= 1.0f) || (uniform(opt) < COHERENT);
                 if (coherent) {
                     r.wcoh++;
                     o_mie_direction(opt, D.phase_cdf, D.theta, D.nt, pidx, &vx, &vy, &vz);
                     if (COND) { atomicAdd(&cstats[4], 1ull); atomicAdd(&cstats[7], 1ull); }
-                } else {
-                    r.wmorph++;
-                    float fr = sqrtf(x * x + y * y);
-                    float ffx = 1.0f, ffy = 0.0f, ffz = 0.0f;
-                    if (fr > 1e-12f) { ffx = -y / fr; ffy = x / fr; }
-                    int ppc = 0, pps = 0, pmb = 0, pmo = 0;
-                    int ps = o_spheroid_event(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha,
-                                              D.prad[pidx], P.spheroid_aspect, P.orientation_model,
-                                              P.orientation_kappa, ffx, ffy, ffz, P.max_particle_bounces, &vx, &vy,
-                                              &vz, &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
-                    if (ps == 2) { r.st = 5; ended = true; break; }
-                    if (ps != 1) { if (COND) atomicAdd(&cstats[8], 1ull); r.pf = ppc ? ppc : OP_OTHER; r.pfs = pps; r.st = 4; ended = true; break; }
-                    if (COND) { atomicAdd(&cstats[5], 1ull); atomicAdd(&cstats[7], 1ull); }
+                    apply_moment(D, pidx, vinx, viny, vinz, &vx, &vy, &vz);
+                    break;
                 }
-            } else {
-                if (COND) atomicAdd(&cstats[0], 1ull);
-                r.gic++;
-                int pidx = sel >= 0 ? sel
-                                    : (TM == 0) ? o_sample_cdf(st, D.gcdf, D.n_bins)
-                                                : o_sample_local_bin(st, &F, D.trace_geom, x, y, z, (double)LOCAL_GEOM);
-                event_pidx = pidx;
-                float prad = D.prad[pidx];
-                float srho, sphi, sgx, sgy, sgz;
-                o_sphere_geometry(opt, prad, x, y, z, vx, vy, vz, &srho, &sphi, &sgx, &sgy, &sgz);
-                double dscx = (double)x - (double)prad * (double)sgx;
-                double dscy = (double)y - (double)prad * (double)sgy;
-                double dscz = (double)z - (double)prad * (double)sgz;
-                int accessible = o_sphere_accessible(dscx, dscy, dscz, (double)prad, RIN, ZMIN, ZMEAN, FSM, DH, CORE);
-                if (!accessible && COND) {
-                    atomicAdd(&cstats[2], 1ull);
-                    Hist h;
-                    conditional_interaction(opt, &h, pidx, D.qsca[pidx], D.qext[pidx], P.n_water, D.pn[pidx],
-                                            D.pk[pidx], P.wavelength, P.rough_alpha, prad, P.spheroid_aspect,
-                                            P.orientation_model, P.orientation_kappa, P.max_particle_bounces,
-                                            COHERENT, D.phase_cdf, D.theta, D.nt, x, y, z, vx, vy, vz, RIN, ZMIN,
-                                            ZMEAN, FSM, DH, CORE, P.conditional_retries - 1, cstats);
-                    if (h.status != 1) { r.pf = h.failure ? h.failure : OP_OTHER; r.pfs = h.subcode; r.st = 4; ended = true; break; }
-                    x = h.x; y = h.y; z = h.z; vx = h.vx; vy = h.vy; vz = h.vz;
-                    r.pc.reflections += h.pc.reflections; r.pc.entry_reflections += h.pc.entry_reflections;
-                    r.pc.internal_reflections += h.pc.internal_reflections; r.pc.absorptions += h.pc.absorptions;
-                    r.gic--;
-                    if (h.channel == 0) r.gic++;
-                    else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
-                } else {
-                    if (!accessible) { r.ic--; r.gic--; r.nulls++; break; }
-                    int ppc = 0, pps = 0, pmb = 0, pmo = 0;
-                    int ps = o_sphere_sampled(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, prad,
-                                              P.max_particle_bounces, sgx, sgy, sgz, dscx, dscy, dscz, &x, &y, &z, &vx,
-                                              &vy, &vz, &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
-                    if (ps == 2) { r.st = 5; ended = true; break; }
-                    if (ps != 1) { if (COND) atomicAdd(&cstats[8], 1ull); r.pf = ppc ? ppc : OP_OTHER; r.pfs = pps; r.st = 4; ended = true; break; }
-                    if (COND) { atomicAdd(&cstats[3], 1ull); atomicAdd(&cstats[7], 1ull); }
-                }
+                r.wmorph++;
+                *ev_pidx = pidx;
+                res = WE_MORPH;
+                break;
             }
-            if (D.any_moment && event_pidx >= 0 && D.moment_mode[event_pidx])
-                moment_constraint(vinx, viny, vinz, &vx, &vy, &vz, (float)D.moment_a[event_pidx],
-                                  (float)D.moment_b[event_pidx]);
+            if (COND) atomicAdd(&cstats[0], 1ull);
+            r.gic++;
+            *ev_pidx = sel >= 0 ? sel
+                                : (TM == 0) ? o_sample_cdf(st, D.gcdf, D.n_bins)
+                                : node_fast ? node_sample_bin(D, st, NL, 0)
+                                            : o_sample_local_bin(st, &F, D.trace_geom, x, y, z, (double)LOCAL_GEOM);
+            res = WE_GEOM;
             break;
         }
-        const o_cell C = make_cell(P);
-        if (axial) {
+        if (axial_bottom) { res = WE_BOTTOM; break; }
+        if (axial_top) {
             float a, b, c;
             int tir = 0;
-            if (axial_top) {
-                float snx = 0.0f, sny = 0.0f, snz = -1.0f;
-                o_surface_normal(x, y, RIN, FSM, DH, CORE, &snx, &sny, &snz);
-                float ci = fminf(fmaxf(-o_dot(vx, vy, vz, snx, sny, snz), 0.0f), 1.0f);
-                float R = o_fresnel(ci, P.n_water, P.n_air, &tir);
-                if (tir || uniform(st) < R || !o_refract(vx, vy, vz, snx, sny, snz, P.n_water, P.n_air, &a, &b, &c)) {
-                    o_reflect(vx, vy, vz, snx, sny, snz, &a, &b, &c);
-                    vx = a; vy = b; vz = c; r.tr++; if (tir) r.ttir++;
-                    if (!o_surface_offset(&x, &y, &z, snx, sny, snz, RIN, ZMIN, ZMEAN, FSM, DH, CORE)) {
-                        r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; ended = true;
-                    }
-                    break;
+            float snx = 0.0f, sny = 0.0f, snz = -1.0f;
+            o_surface_normal(x, y, RIN, FSM, DH, CORE, &snx, &sny, &snz);
+            float ci = fminf(fmaxf(-o_dot(vx, vy, vz, snx, sny, snz), 0.0f), 1.0f);
+            float R = o_fresnel(ci, P.n_water, P.n_air, &tir);
+            if (tir || uniform(st) < R || !o_refract(vx, vy, vz, snx, sny, snz, P.n_water, P.n_air, &a, &b, &c)) {
+                o_reflect(vx, vy, vz, snx, sny, snz, &a, &b, &c);
+                vx = a; vy = b; vz = c; r.tr++; if (tir) r.ttir++;
+                if (!o_surface_offset(&x, &y, &z, snx, sny, snz, RIN, ZMIN, ZMEAN, FSM, DH, CORE)) {
+                    r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED;
                 }
-                vx = a; vy = b; vz = c;
-                x -= CLR_EPS_F * snx; y -= CLR_EPS_F * sny; z -= CLR_EPS_F * snz;
-                int hs = 0, hb = 0;
-                int hw = o_headspace(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
-                if (hw == 1) break;
-                ended = true;
-                if (hw == 2) r.st = 1;
-                else if (hw == 3) r.st = 7;
-                else if (hw == 4) r.st = 6;
-                else { r.pf = OP_HEADSPACE_NO_BOUNDARY; r.pfs = hs; r.st = 4; }
-                break;
-            } else {
-                int bs = 0, bb = 0;
-                int where = o_bottom_disc(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &bs, &bb);
-                if (where == 1) break;
-                ended = true;
-                if (where == 2) { r.st = 1; break; }
-                if (where == 3) { r.st = 7; break; }
-                if (where == 5) { r.st = 8; break; }
-                if (where == 4) {
-                    int hs = 0, hb = 0;
-                    int hw = o_headspace(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
-                    if (hw == 1) { ended = false; break; }
-                    if (hw == 2) r.st = 1;
-                    else if (hw == 3) r.st = 7;
-                    else if (hw == 4) r.st = 6;
-                    else { r.pf = OP_HEADSPACE_NO_BOUNDARY; r.pfs = hs; r.st = 4; }
-                    break;
-                }
-                r.pf = (bs == OS_ACRYLIC_BOUNCE_LIMIT) ? OP_ACRYLIC_BOUNCE_LIMIT : OP_BOTTOM_GEOMETRY;
-                r.pfs = bs; r.st = 4;
                 break;
             }
+            vx = a; vy = b; vz = c;
+            x -= CLR_EPS_F * snx; y -= CLR_EPS_F * sny; z -= CLR_EPS_F * snz;
+            res = WE_TOP;
+            break;
         }
         // water -> acrylic at the cylinder wall (:5038-5065)
         {
@@ -522,33 +537,215 @@ __device__ __forceinline__ bool water_step(const DevScene& D, Ray& r, S* st, S* 
                 break;
             }
             vx = a; vy = b; vz = c; x += CLR_EPS_F * nx; y += CLR_EPS_F * ny;
-            int sub = 0, nb = 0;
-            int where = o_acrylic_solid(st, &C, C.n_air, C.n_bottom_ext, ZMIN, C.Zlow, &x, &y, &z, &vx, &vy, &vz, &r.ap,
-                                        &bc, &sub, &nb);
-            if (where == 1) break;
-            ended = true;
-            if (where == 2) { r.st = 1; break; }
-            if (where == 3) { r.st = 7; break; }
-            if (where == 5) { r.st = 8; break; }
-            if (where == 4) {
-                int hs = 0, hb = 0;
-                int hw = o_headspace(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
-                if (hw == 1) { ended = false; break; }
-                if (hw == 2) r.st = 1;
-                else if (hw == 3) r.st = 7;
-                else if (hw == 4) r.st = 6;
-                else if (hw == 5) r.st = 8;
-                else { r.pf = OP_HEADSPACE_NO_BOUNDARY; r.pfs = hs; r.st = 4; }
-                break;
-            }
-            r.pf = (sub == OS_ACRYLIC_BOUNCE_LIMIT) ? OP_ACRYLIC_BOUNCE_LIMIT : OP_ACRYLIC_NO_INTERSECTION;
-            r.pfs = sub; r.st = 4;
+            res = WE_SIDE;
         }
     } while (false);
+    r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
+    return res;
+}
+
+// ---- handlers: each completes the iteration its flight part started; true when the history ended ----
+
+template <class S>
+__device__ __forceinline__ bool water_cond(const DevScene& D, Ray& r, S* opt, unsigned long long* cstats, int sel) {
+    const clr_scene_params& P = D.P;
+    float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
+    const float vinx = vx, viny = vy, vinz = vz;
+    const float COHERENT = fminf(fmaxf((float)D.mu_channels[7], 0.0f), 1.0f);
+    bool ended = false;
+    Hist h;
+    conditional_interaction(opt, &h, sel, D.qsca[sel], D.qext[sel], P.n_water, D.pn[sel], D.pk[sel], P.wavelength,
+                            P.rough_alpha, D.prad[sel], P.spheroid_aspect, P.orientation_model, P.orientation_kappa,
+                            P.max_particle_bounces, COHERENT, D.phase_cdf, D.theta, D.nt, x, y, z, vx, vy, vz, P.rin,
+                            P.zmin, P.zmean, P.free_surface_model, P.vortex_delta_h, P.vortex_core_radius,
+                            P.conditional_retries, cstats);
+    do {
+        if (h.status != 1 && h.status != 2) { r.pf = h.failure ? h.failure : OP_OTHER; r.pfs = h.subcode; r.st = 4; ended = true; break; }
+        x = h.x; y = h.y; z = h.z; vx = h.vx; vy = h.vy; vz = h.vz;
+        r.pc.reflections += h.pc.reflections; r.pc.entry_reflections += h.pc.entry_reflections;
+        r.pc.internal_reflections += h.pc.internal_reflections; r.pc.absorptions += h.pc.absorptions;
+        if (h.channel == 0) r.gic++;
+        else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
+        if (h.status == 2) { r.st = 5; ended = true; break; }
+        apply_moment(D, sel, vinx, viny, vinz, &vx, &vy, &vz);
+    } while (false);
+    r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
+    return ended;
+}
+
+template <class S>
+__device__ __forceinline__ bool water_geom(const DevScene& D, Ray& r, S* opt, unsigned long long* cstats, int pidx) {
+    const clr_scene_params& P = D.P;
+    const float RIN = P.rin, ZMIN = P.zmin, ZMEAN = P.zmean, DH = P.vortex_delta_h, CORE = P.vortex_core_radius;
+    const int FSM = P.free_surface_model;
+    float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
+    const float vinx = vx, viny = vy, vinz = vz;
+    const int COND = (P.event_model == 4 || P.event_model == 5);
+    const float COHERENT = fminf(fmaxf((float)D.mu_channels[7], 0.0f), 1.0f);
+    bool ended = false;
+    do {
+        float prad = D.prad[pidx];
+        float srho, sphi, sgx, sgy, sgz;
+        o_sphere_geometry(opt, prad, x, y, z, vx, vy, vz, &srho, &sphi, &sgx, &sgy, &sgz);
+        double dscx = (double)x - (double)prad * (double)sgx;
+        double dscy = (double)y - (double)prad * (double)sgy;
+        double dscz = (double)z - (double)prad * (double)sgz;
+        int accessible = o_sphere_accessible(dscx, dscy, dscz, (double)prad, RIN, ZMIN, ZMEAN, FSM, DH, CORE);
+        if (!accessible && COND) {
+            atomicAdd(&cstats[2], 1ull);
+            Hist h;
+            conditional_interaction(opt, &h, pidx, D.qsca[pidx], D.qext[pidx], P.n_water, D.pn[pidx], D.pk[pidx],
+                                    P.wavelength, P.rough_alpha, prad, P.spheroid_aspect, P.orientation_model,
+                                    P.orientation_kappa, P.max_particle_bounces, COHERENT, D.phase_cdf, D.theta, D.nt,
+                                    x, y, z, vx, vy, vz, RIN, ZMIN, ZMEAN, FSM, DH, CORE, P.conditional_retries - 1,
+                                    cstats);
+            if (h.status != 1) { r.pf = h.failure ? h.failure : OP_OTHER; r.pfs = h.subcode; r.st = 4; ended = true; break; }
+            x = h.x; y = h.y; z = h.z; vx = h.vx; vy = h.vy; vz = h.vz;
+            r.pc.reflections += h.pc.reflections; r.pc.entry_reflections += h.pc.entry_reflections;
+            r.pc.internal_reflections += h.pc.internal_reflections; r.pc.absorptions += h.pc.absorptions;
+            r.gic--;
+            if (h.channel == 0) r.gic++;
+            else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
+        } else {
+            if (!accessible) { r.ic--; r.gic--; r.nulls++; break; }
+            float ipath = 0.0f;
+            int ppc = 0, pps = 0, pmb = 0, pmo = 0;
+            int ps = o_sphere_sampled(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, prad,
+                                      P.max_particle_bounces, sgx, sgy, sgz, dscx, dscy, dscz, &x, &y, &z, &vx, &vy,
+                                      &vz, &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
+            if (ps == 2) { r.st = 5; ended = true; break; }
+            if (ps != 1) { if (COND) atomicAdd(&cstats[8], 1ull); r.pf = ppc ? ppc : OP_OTHER; r.pfs = pps; r.st = 4; ended = true; break; }
+            if (COND) { atomicAdd(&cstats[3], 1ull); atomicAdd(&cstats[7], 1ull); }
+        }
+        apply_moment(D, pidx, vinx, viny, vinz, &vx, &vy, &vz);
+    } while (false);
+    r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
+    return ended;
+}
+
+template <class S>
+__device__ __forceinline__ bool water_morph(const DevScene& D, Ray& r, S* opt, unsigned long long* cstats, int pidx) {
+    const clr_scene_params& P = D.P;
+    float x = r.x, y = r.y, vx = r.vx, vy = r.vy, vz = r.vz;
+    const float vinx = vx, viny = vy, vinz = vz;
+    const int COND = (P.event_model == 4 || P.event_model == 5);
+    bool ended = false;
+    do {
+        float fr = sqrtf(x * x + y * y);
+        float ffx = 1.0f, ffy = 0.0f, ffz = 0.0f;
+        if (fr > 1e-12f) { ffx = -y / fr; ffy = x / fr; }
+        float ipath = 0.0f;
+        int ppc = 0, pps = 0, pmb = 0, pmo = 0;
+        int ps = o_spheroid_event(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, D.prad[pidx],
+                                  P.spheroid_aspect, P.orientation_model, P.orientation_kappa, ffx, ffy, ffz,
+                                  P.max_particle_bounces, &vx, &vy, &vz, &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
+        if (ps == 2) { r.st = 5; ended = true; break; }
+        if (ps != 1) { if (COND) atomicAdd(&cstats[8], 1ull); r.pf = ppc ? ppc : OP_OTHER; r.pfs = pps; r.st = 4; ended = true; break; }
+        if (COND) { atomicAdd(&cstats[5], 1ull); atomicAdd(&cstats[7], 1ull); }
+        apply_moment(D, pidx, vinx, viny, vinz, &vx, &vy, &vz);
+    } while (false);
+    r.vx = vx; r.vy = vy; r.vz = vz;
+    return ended;
+}
+
+// transmitted through the free surface into the headspace
+template <class S>
+__device__ __forceinline__ bool water_top(const DevScene& D, Ray& r, S* st) {
+    const o_cell C = make_cell(D.P);
+    float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
+    o_bcount bc = {0, 0, 0, 0, 0, 0, 0, 0};
+    int hs = 0, hb = 0;
+    const int hw = o_headspace(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
+    bool ended = hw != 1;
+    if (hw == 1) {}
+    else if (hw == 2) r.st = 1;
+    else if (hw == 3) r.st = 7;
+    else if (hw == 4) r.st = 6;
+    else { r.pf = OP_HEADSPACE_NO_BOUNDARY; r.pfs = hs; r.st = 4; }
     add_bounces(r, bc);
     r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
-    (void)kWeighted;
     return ended;
+}
+
+// reached the bottom disc
+template <class S>
+__device__ __forceinline__ bool water_bottom(const DevScene& D, Ray& r, S* st) {
+    const o_cell C = make_cell(D.P);
+    float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
+    o_bcount bc = {0, 0, 0, 0, 0, 0, 0, 0};
+    int bs = 0, bb = 0;
+    const int where = o_bottom_disc(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &bs, &bb);
+    bool ended = true;
+    if (where == 1) ended = false;
+    else if (where == 2) r.st = 1;
+    else if (where == 3) r.st = 7;
+    else if (where == 5) r.st = 8;
+    else if (where == 4) {
+        int hs = 0, hb = 0;
+        const int hw = o_headspace(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
+        if (hw == 1) ended = false;
+        else if (hw == 2) r.st = 1;
+        else if (hw == 3) r.st = 7;
+        else if (hw == 4) r.st = 6;
+        else { r.pf = OP_HEADSPACE_NO_BOUNDARY; r.pfs = hs; r.st = 4; }
+    } else {
+        r.pf = (bs == OS_ACRYLIC_BOUNCE_LIMIT) ? OP_ACRYLIC_BOUNCE_LIMIT : OP_BOTTOM_GEOMETRY;
+        r.pfs = bs; r.st = 4;
+    }
+    add_bounces(r, bc);
+    r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
+    return ended;
+}
+
+// transmitted into the acrylic wall
+template <class S>
+__device__ __forceinline__ bool water_side(const DevScene& D, Ray& r, S* st) {
+    const clr_scene_params& P = D.P;
+    const o_cell C = make_cell(P);
+    float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
+    o_bcount bc = {0, 0, 0, 0, 0, 0, 0, 0};
+    int sub = 0, nb = 0;
+    const int where = o_acrylic_solid(st, &C, C.n_air, C.n_bottom_ext, P.zmin, C.Zlow, &x, &y, &z, &vx, &vy, &vz,
+                                      &r.ap, &bc, &sub, &nb);
+    bool ended = true;
+    if (where == 1) ended = false;
+    else if (where == 2) r.st = 1;
+    else if (where == 3) r.st = 7;
+    else if (where == 5) r.st = 8;
+    else if (where == 4) {
+        int hs = 0, hb = 0;
+        const int hw = o_headspace(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
+        if (hw == 1) ended = false;
+        else if (hw == 2) r.st = 1;
+        else if (hw == 3) r.st = 7;
+        else if (hw == 4) r.st = 6;
+        else if (hw == 5) r.st = 8;
+        else { r.pf = OP_HEADSPACE_NO_BOUNDARY; r.pfs = hs; r.st = 4; }
+    } else {
+        r.pf = (sub == OS_ACRYLIC_BOUNCE_LIMIT) ? OP_ACRYLIC_BOUNCE_LIMIT : OP_ACRYLIC_NO_INTERSECTION;
+        r.pfs = sub; r.st = 4;
+    }
+    add_bounces(r, bc);
+    r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
+    return ended;
+}
+
+// One whole water iteration (flight part and its handler).
+template <class S, bool kWeighted>
+__device__ __forceinline__ bool water_step(const DevScene& D, Ray& r, S* st, S* opt, unsigned long long* cstats) {
+    int pidx = -1;
+    const int e = water_flight(D, r, st, opt, cstats, &pidx);
+    (void)kWeighted;
+    switch (e) {
+        case WE_NONE: return false;
+        case WE_ENDED: return true;
+        case WE_COND: return water_cond(D, r, opt, cstats, pidx);
+        case WE_GEOM: return water_geom(D, r, opt, cstats, pidx);
+        case WE_MORPH: return water_morph(D, r, opt, cstats, pidx);
+        case WE_TOP: return water_top(D, r, st);
+        case WE_BOTTOM: return water_bottom(D, r, st);
+        default: return water_side(D, r, st);
+    }
 }
 
 }  // namespace

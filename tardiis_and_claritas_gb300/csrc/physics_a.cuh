@@ -514,9 +514,18 @@ typedef struct {
     float grid_zmax, R, zmin, core;
 } o_field;
 
-__device__ double o_grid_sample(const o_field* f, int pidx, float x, float y, float z) {
+// Cell and weights of the bilinear lookup at (x, y, z): the same for every size bin, so a loop over
+// bins computes them once (the arithmetic is the reference's, so the values are bit-identical).
+struct o_grid_w {
+    long long i, k;
+    double tr, tz;
+    int ok;
+};
+__device__ __forceinline__ o_grid_w o_grid_weights(const o_field* f, float x, float y, float z) {
+    o_grid_w w;
     const int NR = f->grid_nr, NZ = f->grid_nz;
-    if (NR < 2 || NZ < 2 || !(f->grid_zmax > f->zmin)) return 1.0;
+    w.ok = !(NR < 2 || NZ < 2 || !(f->grid_zmax > f->zmin));
+    if (!w.ok) { w.i = w.k = 0; w.tr = w.tz = 0.0; return w; }
     double rr = sqrt(fmax((double)x * (double)x + (double)y * (double)y, 0.0));
     if (rr < 0.0) rr = 0.0;
     if (rr > (double)f->R) rr = (double)f->R;
@@ -530,15 +539,20 @@ __device__ double o_grid_sample(const o_field* f, int pidx, float x, float y, fl
     double tr = ur - (double)i, tz = uz - (double)k;
     if (i >= NR - 1) { i = NR - 2; tr = 1.0; }
     if (k >= NZ - 1) { k = NZ - 2; tz = 1.0; }
-    long long plane = (long long)NR * (long long)NZ;
-    long long b = (long long)pidx * plane;
-    const double* G = f->grid;
-    double q00 = G[b + (long long)i * NZ + k];
-    double q10 = G[b + (long long)(i + 1) * NZ + k];
-    double q01 = G[b + (long long)i * NZ + k + 1];
-    double q11 = G[b + (long long)(i + 1) * NZ + k + 1];
-    double q0 = (1.0 - tr) * q00 + tr * q10, q1 = (1.0 - tr) * q01 + tr * q11;
-    return fmax((1.0 - tz) * q0 + tz * q1, 0.0);
+    w.i = i; w.k = k; w.tr = tr; w.tz = tz;
+    return w;
+}
+__device__ __forceinline__ double o_grid_sample_w(const o_field* f, const o_grid_w& w, int pidx) {
+    if (!w.ok) return 1.0;
+    const long long NZ = f->grid_nz;
+    const double* G = f->grid + (long long)pidx * ((long long)f->grid_nr * NZ) + w.i * NZ + w.k;
+    double q00 = G[0], q10 = G[NZ], q01 = G[1], q11 = G[NZ + 1];
+    double q0 = (1.0 - w.tr) * q00 + w.tr * q10, q1 = (1.0 - w.tr) * q01 + w.tr * q11;
+    return fmax((1.0 - w.tz) * q0 + w.tz * q1, 0.0);
+}
+__device__ double o_grid_sample(const o_field* f, int pidx, float x, float y, float z) {
+    const o_grid_w w = o_grid_weights(f, x, y, z);
+    return o_grid_sample_w(f, w, pidx);
 }
 __device__ double o_local_scale(const o_field* f, int pidx, float x, float y, float z) {
     if (f->model == 0) return 1.0;
@@ -578,6 +592,14 @@ __device__ int o_sample_local_bin(S* s, const o_field* f, const double* mu_bin, 
                               double local_total) {
     if (!(local_total > 0.0)) return 0;
     double target = (double)uniform(s) * local_total, cum = 0.0;
+    if (f->model == 3) {
+        const o_grid_w w = o_grid_weights(f, x, y, z);
+        for (int i = 0; i < f->n_bins; ++i) {
+            cum += mu_bin[i] * o_grid_sample_w(f, w, i);
+            if (target <= cum) return i;
+        }
+        return f->n_bins > 0 ? f->n_bins - 1 : 0;
+    }
     for (int i = 0; i < f->n_bins; ++i) {
         double sc = o_local_scale(f, i, x, y, z);
         cum += mu_bin[i] * sc;

@@ -444,8 +444,27 @@ __global__ void sediment_bin_kernel(SedArgs a, const double* __restrict__ diamet
 }
 
 // Majorants in bin order (:4029-4036; grid model :4203-4220 on an all-active supplied grid).
+// Per-bin maximum of the (r, z) grid (the max of non-negative terms starting at 0, as the reference's
+// serial scan, so the order of the reduction does not change the value). One block per bin.
+__global__ void sediment_grid_max_kernel(const double* __restrict__ grid, long long plane, double* grid_max) {
+    const int p = blockIdx.x;
+    double mx = 0.0;
+    for (long long c = threadIdx.x; c < plane; c += blockDim.x) {
+        const double q = grid[p * plane + c];
+        if (q > mx) mx = q;
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h && red[threadIdx.x + h] > red[threadIdx.x]) red[threadIdx.x] = red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) grid_max[p] = red[0];
+}
+
 __global__ void sediment_majorant_kernel(SedArgs a, const double* trace_geom, const double* trace_wave, double* sed_A,
-                                         double* sed_norm, double* sed_max, const double* grid, int nr, int nz,
+                                         double* sed_norm, double* sed_max, const double* grid_max,
                                          double* major, int* error_flag) {
     if (blockIdx.x || threadIdx.x) return;
     const int n = a.n;
@@ -463,11 +482,9 @@ __global__ void sediment_majorant_kernel(SedArgs a, const double* trace_geom, co
     }
     major[0] = mg; major[1] = mw; major[2] = mg + mw; major[3] = maxAeq;
     if (!(major[2] >= 0.0) || !isfinite(major[2])) atomicCAS(error_flag, 0, 35);
-    if (a.TM == 3 && grid) {
-        const long long plane = (long long)nr * nz;
+    if (a.TM == 3 && grid_max) {
         for (int p = 0; p < n; ++p) {
-            double mx = 0.0;
-            for (long long c = 0; c < plane; ++c) { double q = grid[p * plane + c]; if (q > mx) mx = q; }
+            double mx = grid_max[p];
             if (!(mx > 0.0)) mx = 1.0;
             sed_norm[p] = 1.0;
             sed_max[p] = mx;
@@ -475,6 +492,55 @@ __global__ void sediment_majorant_kernel(SedArgs a, const double* trace_geom, co
         mg = 0.0; mw = 0.0;
         for (int i = 0; i < n; ++i) { mg += trace_geom[i] * sed_max[i]; mw += trace_wave[i] * sed_max[i]; }
         major[0] = mg; major[1] = mw; major[2] = mg + mw;
+    }
+}
+
+// Node tables of the (r, z) field for the counter-based stream: for channel ch (0 geometric, 1 wave) and
+// node c, G = sum_i mu_ch[i] grid[i][c] (FP64, bin order) and a Walker/Vose alias table over the bins with
+// probabilities mu_ch[i] grid[i][c] / G. One thread per (channel, node); reads of grid[i][c] coalesce over c.
+// The host enables these tables only for grids with no negative value, where the reference's clamp of the
+// interpolated value at zero never acts, so the interpolated sum equals the interpolation of the sums.
+__global__ void sediment_node_kernel(const double* __restrict__ grid, const double* __restrict__ trace_geom,
+                                     const double* __restrict__ trace_wave, int n, int plane, float2* node_mu,
+                                     int2* node_alias, unsigned int* node_major_bits) {
+    const int t = blockDim.x * blockIdx.x + threadIdx.x;
+    if (t >= 2 * plane) return;
+    const int ch = t / plane, c = t - ch * plane;
+    const double* mu = ch ? trace_wave : trace_geom;
+    double p[CLR_MAX_BINS];
+    double G = 0.0;
+    for (int i = 0; i < n; ++i) {
+        p[i] = mu[i] * grid[(size_t)i * plane + c];
+        G += p[i];
+    }
+    float* dst = reinterpret_cast<float*>(&node_mu[c]) + ch;
+    *dst = (float)G;
+    int2* A = node_alias + ((size_t)ch * plane + c) * n;
+    if (!(G > 0.0)) {
+        for (int i = 0; i < n; ++i) A[i] = make_int2(__float_as_int(1.0f), i);
+    } else {
+        unsigned char small[CLR_MAX_BINS], large[CLR_MAX_BINS];
+        int ns = 0, nl = 0;
+        for (int i = 0; i < n; ++i) {
+            p[i] = p[i] * (double)n / G;
+            if (p[i] < 1.0) small[ns++] = (unsigned char)i; else large[nl++] = (unsigned char)i;
+        }
+        while (ns > 0 && nl > 0) {
+            const int sm = small[--ns], lg = large[--nl];
+            A[sm] = make_int2(__float_as_int((float)p[sm]), lg);
+            p[lg] = (p[lg] + p[sm]) - 1.0;
+            if (p[lg] < 1.0) small[ns++] = (unsigned char)lg; else large[nl++] = (unsigned char)lg;
+        }
+        while (nl > 0) { const int i = large[--nl]; A[i] = make_int2(__float_as_int(1.0f), i); }
+        while (ns > 0) { const int i = small[--ns]; A[i] = make_int2(__float_as_int(1.0f), i); }
+    }
+    if (ch == 0) {
+        // majorant of the summed field: max over nodes of G_geom + G_wave (non-negative, so the
+        // float bit patterns order like the values)
+        double Gw = 0.0;
+        for (int i = 0; i < n; ++i) Gw += trace_wave[i] * grid[(size_t)i * plane + c];
+        const float tot = (float)(G + Gw) * (1.0f + 4.0f * 1.1920928955078125e-7f);
+        atomicMax(node_major_bits, __float_as_uint(tot));
     }
 }
 
@@ -516,9 +582,18 @@ cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_par
     }
     sediment_bin_kernel<<<(n + 63) / 64, 64, 0, st>>>(a, pb.d, pb.sed_wr, pb.sedA, pb.sedB, pb.sed_norm, pb.sed_max,
                                                      pb.sed_radial_log, pb.err);
+    if (a.TM == 3)
+        sediment_grid_max_kernel<<<n, 256, 0, st>>>(pb.sed_grid, (long long)pb.grid_nr * pb.grid_nz, pb.grid_max);
     sediment_majorant_kernel<<<1, 1, 0, st>>>(a, pb.trace_geom, pb.trace_wave, pb.sedA, pb.sed_norm, pb.sed_max,
-                                              a.TM == 3 ? pb.sed_grid : nullptr, pb.grid_nr, pb.grid_nz, pb.sed_major,
-                                              pb.err);
+                                              a.TM == 3 ? pb.grid_max : nullptr, pb.sed_major, pb.err);
+    if (pb.node_tables) {
+        const int plane = pb.grid_nr * pb.grid_nz;
+        e = cudaMemsetAsync(pb.node_major, 0, sizeof(float), st);
+        if (e != cudaSuccess) return e;
+        sediment_node_kernel<<<(2 * plane + 127) / 128, 128, 0, st>>>(
+            pb.sed_grid, pb.trace_geom, pb.trace_wave, n, plane, pb.node_mu, pb.node_alias,
+            reinterpret_cast<unsigned int*>(pb.node_major));
+    }
     return cudaGetLastError();
 }
 

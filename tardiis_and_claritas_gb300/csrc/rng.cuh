@@ -59,6 +59,11 @@ struct PhiloxStream {
     }
 };
 
+// True for the counter-based stream: paths that only need the reference's distributions (not its
+// draw sequence) may then use cheaper but equivalent samplers.
+template <class S> constexpr bool kCounterStream = false;
+template <> constexpr bool kCounterStream<PhiloxStream> = true;
+
 template <class S>
 __device__ __forceinline__ float uniform(S* s) { return (float)s->next() * 2.3283064e-10f; }
 

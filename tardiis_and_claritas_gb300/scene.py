@@ -409,7 +409,7 @@ def reference_seeds(seed: int) -> tuple[int, int, int, int]:
 
 def run_params(n_rays: int, seed: int = 0, ray_offset: int = 0, rng_mode: int = abi.RNG_REFERENCE_XORSHIFT,
                weight_mode: int = abi.WEIGHT_ANALOG, roulette_threshold: float = 1e-4, roulette_survival: float = 1e-3,
-               scenario_id: int = 0, max_blocks: int = 0, rays_per_item: int = 0) -> abi.RunParams:
+               scenario_id: int = 0, max_blocks: int = 0, rays_per_item: int = 0, flags: int = 0) -> abi.RunParams:
     r = abi.RunParams()
     r.n_rays = int(n_rays)
     r.ray_offset = int(ray_offset) & 0xFFFFFFFF
@@ -422,6 +422,7 @@ def run_params(n_rays: int, seed: int = 0, ray_offset: int = 0, rng_mode: int = 
     r.roulette_survival = float(roulette_survival)
     r.max_blocks = int(max_blocks)
     r.rays_per_item = int(rays_per_item)
+    r.flags = int(flags)
     return r
 
 

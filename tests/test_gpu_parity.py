@@ -62,15 +62,19 @@ def first_mismatch(rec, compact_ref):
     return f"ray {i}: mine {dict(zip(PS.COMPACT_FIELDS, mine[i].tolist()))} ref {dict(zip(PS.COMPACT_FIELDS, compact_ref[i].tolist()))}"
 
 
+ENGINES = {"wavefront": 0, "persistent": abi.RUN_PERSISTENT_KERNEL}
+
+
+@pytest.mark.parametrize("engine", list(ENGINES))
 @pytest.mark.parametrize("name", list(PS.SCENES))
-def test_bit_exact_against_reference_kernels(ctx, gold, name):
+def test_bit_exact_against_reference_kernels(ctx, gold, name, engine):
     z, meta = gold
     m = meta["scenes"][name]
     prepare(ctx, name)
     ph = ctx.physics()
     mism = [k for k, v in PS.physics_digests(ph).items() if v != m["physics_sha256"][k]]
     assert not mism, f"{name}: physics tables differ from the reference kernels: {mism}"
-    tal, rec = ctx.trace(S.run_params(meta["n_rays"], seed=m["seed"]), records=True)
+    tal, rec = ctx.trace(S.run_params(meta["n_rays"], seed=m["seed"], flags=ENGINES[engine]), records=True)
     for k in PS.TALLY_KEYS:
         np.testing.assert_array_equal(tal[k], z[f"{name}/{k}"], err_msg=f"{name}: {k}")
     assert tal["event_counts"][:PS.EVENT_KEYS].tolist() == m["event_counts"]
@@ -143,6 +147,18 @@ def test_philox_is_partition_independent(ctx):
     h2, _ = ctx.trace(S.run_params(n - n // 2, seed=5, rng_mode=abi.RNG_PHILOX, ray_offset=n // 2))
     for k in PS.TALLY_KEYS:
         np.testing.assert_array_equal(full[k], h1[k] + h2[k], err_msg=k)
+
+
+@pytest.mark.parametrize("name", ["grid_sediment", "absorbing_conditional", "reflective_bores"])
+def test_engines_agree_without_records(ctx, name):
+    """Tally-only runs (no record buffer) of the two engines give identical integer tallies."""
+    prepare(ctx, name)
+    n = 200_000
+    a, _ = ctx.trace(S.run_params(n, seed=77))
+    b, _ = ctx.trace(S.run_params(n, seed=77, flags=abi.RUN_PERSISTENT_KERNEL))
+    for k in PS.TALLY_KEYS:
+        np.testing.assert_array_equal(a[k], b[k], err_msg=f"{name}: {k}")
+    assert a["device_error"] == 0 and b["device_error"] == 0
 
 
 def test_chunking_does_not_change_results(ctx):

@@ -1,0 +1,84 @@
+"""GPU: the production (counter-based Philox) path against the reference-exact path and the CPU oracle.
+
+The Philox path may replace a sampler with an equivalent one (same distribution, different draws):
+for sediment model 3 it samples the (r, z) field through per-node sums and alias tables instead of a
+pass over all size bins. These tests check that the tallies, failure accounting and interaction-count
+distribution of that path agree with the reference-exact xorshift path and with the CPU oracle within
+binomial / normal standard errors at fixed photon counts.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import parity_scenes as PS
+from tardiis_and_claritas_gb300 import abi, scene as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from tardiis_and_claritas_gb300 import lib as L
+    from tardiis_and_claritas_gb300.build_ext import build
+    build()
+    c = L.Context(0)
+    yield c
+    c.close()
+
+
+def _z_binomial(a, na, b, nb):
+    pa, pb = a / na, b / nb
+    se = np.maximum(np.sqrt(pa * (1 - pa) / na + pb * (1 - pb) / nb), 1.0 / max(na, nb))
+    return np.abs(pa - pb) / se
+
+
+def _assert_agree(a, na, b, nb, what):
+    for key in ("hw_native", "hw_mirror", "status_counts", "failure_code_counts"):
+        z = _z_binomial(a[key].astype(float), na, b[key].astype(float), nb)
+        assert np.max(z) < 4.5 and np.sum(z > 3.0) <= 1, f"{what} {key}: z={np.round(z, 2)}"
+    # interaction-count distribution: P(ic = k) for k < 16 and P(ic >= 16) as binomial proportions
+    # (the count has a heavy tail, so its sample mean and variance are not a usable statistic)
+    ha, hb = a["ic_hist"].astype(float), b["ic_hist"].astype(float)
+    ca = np.append(ha[:16], ha[16:].sum())
+    cb = np.append(hb[:16], hb[16:].sum())
+    z = _z_binomial(ca, na, cb, nb)
+    assert np.max(z) < 4.5 and np.sum(z > 3.0) <= 1, f"{what} interaction counts: z={np.round(z, 2)}"
+
+
+def _load(ctx, cfg, parts, grid, zmax=None):
+    ctx.set_scene(cfg.to_scene_params())
+    ctx.build_particles(parts.spec(cfg), cfg.sediment_spec(grid, zmax))
+
+
+def test_node_tables_match_exact_field_on_per_bin_grid(ctx):
+    """Per-bin random grid: the composition sampler must reproduce bin choices that differ by node."""
+    cfg, parts, grid = PS.build("grid_sediment")
+    _load(ctx, cfg, parts, grid)
+    n = 400_000
+    a, _ = ctx.trace(S.run_params(n, seed=21, rng_mode=abi.RNG_REFERENCE_XORSHIFT))
+    b, _ = ctx.trace(S.run_params(n, seed=21, rng_mode=abi.RNG_PHILOX))
+    _assert_agree(a, n, b, n, "grid_sediment")
+
+
+def test_full_scene_philox_matches_cpu_oracle(ctx):
+    import oracle_harness as H
+    cfg, parts, grid, zmax = S.full_scene_workload()
+    _load(ctx, cfg, parts, grid, zmax)
+    n_gpu = 2_000_000
+    g, _ = ctx.trace(S.run_params(n_gpu, seed=31, rng_mode=abi.RNG_PHILOX))
+    assert g["device_error"] == 0
+    orc = H.OracleRun("port", cfg, parts, grid=grid, grid_zmax=zmax)
+    n_cpu = 300_000
+    c, _ = orc.trace(S.run_params(n_cpu, seed=32))
+    orc.close()
+    _assert_agree(g, n_gpu, c, n_cpu, "full scene")
+
+
+def test_full_scene_philox_matches_xorshift(ctx):
+    cfg, parts, grid, zmax = S.full_scene_workload()
+    _load(ctx, cfg, parts, grid, zmax)
+    n = 1_000_000
+    a, _ = ctx.trace(S.run_params(n, seed=41, rng_mode=abi.RNG_REFERENCE_XORSHIFT))
+    b, _ = ctx.trace(S.run_params(n, seed=41, rng_mode=abi.RNG_PHILOX))
+    _assert_agree(a, n, b, n, "full scene xorshift/philox")
