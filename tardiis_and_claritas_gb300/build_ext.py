@@ -90,6 +90,17 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     return LIB_PATH
 
 
+def _short_name(mangled: str) -> str:
+    """Demangled kernel name without namespaces (falls back to the mangled name)."""
+    try:
+        name = subprocess.run(["c++filt", mangled], capture_output=True, text=True, check=True).stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return mangled[:100]
+    for junk in ("clr::", "(anonymous namespace)::", "void "):
+        name = name.replace(junk, "")
+    return name.split("(")[0][:100]
+
+
 def resource_report() -> str:
     """ptxas register/stack summary of the last build (from the per-unit logs)."""
     out = []
@@ -102,7 +113,7 @@ def resource_report() -> str:
             if "Compiling entry function" in line:
                 entry = line.split("'")[1]
             elif "Used" in line and "registers" in line and entry:
-                out.append(f"{src}: {entry[:80]} :: {line.strip()}")
+                out.append(f"{src}: {_short_name(entry)} :: {line.strip().replace('ptxas info    : ', '')}")
                 entry = None
     return "\n".join(out)
 

@@ -320,15 +320,15 @@ static void tally_to_host(const DevTally& d, clr_tallies* out, int64_t n_rays) {
     out->device_error = (t.n_done == (unsigned long long)n_rays) ? 0 : 1;
 }
 
-// Photon pool of the wavefront engine: 2^20 slots (about 230 MB), allocated once per context.
+// Photon pool of the wavefront engine: 2^21 slots (about 640 MB with the queue rings), allocated once per context.
 static int wave_pool_ready(clr_ctx* ctx) {
     if (ctx->wave_cap) return CLR_OK;
-    const unsigned cap = 1u << 20;
+    const unsigned cap = 1u << 21;
     const size_t lane = std::max(wave_lane_bytes(CLR_RNG_PHILOX), wave_lane_bytes(CLR_RNG_REFERENCE_XORSHIFT));
     CU(cudaMalloc(&ctx->wave_ray, (size_t)cap * wave_ray_bytes()));
     CU(cudaMalloc(&ctx->wave_lane, (size_t)cap * lane));
     CU(cudaMalloc(&ctx->wave_meta, (size_t)cap * sizeof(SlotMeta)));
-    CU(cudaMalloc(&ctx->wave_q, (size_t)CLR_WQ_COUNT * cap * sizeof(uint32_t)));
+    CU(cudaMalloc(&ctx->wave_q, (size_t)CLR_WQ_COUNT * 2 * cap * sizeof(uint32_t)));  // rings of 2 * cap
     CU(cudaMalloc(&ctx->wave_ctl, sizeof(WaveCtl)));
     CU(cudaMalloc(&ctx->wave_begin, 2 * sizeof(long long)));
     CU(cudaHostAlloc((void**)&ctx->wave_live, sizeof(unsigned), cudaHostAllocDefault));

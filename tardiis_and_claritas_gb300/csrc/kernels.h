@@ -35,19 +35,21 @@ inline int photon_kernel_occupancy(int rng_mode, bool records, bool /*weighted*/
 }
 
 // ---------------- wavefront engine (wavefront.cuh) ----------------
-#define CLR_WQ_COUNT 10  // stage queues: free, entry, flight, cond, geom, morph, top, bottom, side, fin
+#define CLR_WQ_COUNT 11  // stage queues: free, entry, flight, cond, geom, morph, top, bottom, side, acrylic, fin
 
 struct SlotMeta {
     uint32_t gid;   // global ray id (ray_offset + rid): the random-stream key
     int32_t sid;    // scenario
     long long rid;  // ray index within the scenario
     int32_t pidx;   // size bin of a pending particle event
+    int32_t acr_caller;                       // pending acrylic traversal: which handler started it
+    int32_t acr_it, acr_stuck, acr_last;      // and its loop state
     int32_t pad;
 };
 
 struct WaveCtl {
     unsigned long long next_photon, total_photons;
-    unsigned head[CLR_WQ_COUNT], tail[CLR_WQ_COUNT], snap[CLR_WQ_COUNT], finished[CLR_WQ_COUNT];
+    unsigned head[CLR_WQ_COUNT], tail[CLR_WQ_COUNT], snap[CLR_WQ_COUNT], finished[CLR_WQ_COUNT], skips[CLR_WQ_COUNT];
     unsigned live, passes;
 };
 
@@ -61,7 +63,7 @@ struct WaveLaunch {
     void* ray;                     // [cap] Ray
     void* lane;                    // [cap] random-stream state
     SlotMeta* meta;                // [cap]
-    uint32_t* qbuf;                // [CLR_WQ_COUNT][cap]
+    uint32_t* qbuf;                // [CLR_WQ_COUNT][2 * cap] queue rings
     WaveCtl* ctl;
     unsigned cap;                  // slots, a power of two
     unsigned* host_live;           // pinned host word

@@ -368,6 +368,32 @@ __device__ __forceinline__ void apply_moment(const DevScene& D, int pidx, float 
         moment_constraint(vinx, viny, vinz, vx, vy, vz, (float)D.moment_a[pidx], (float)D.moment_b[pidx]);
 }
 
+// True when the straight segment of length t from (x, y, z) along v stays inside the water: the
+// cylinder and the half-space above the bottom are convex, so their test is the endpoint's; the free
+// surface height grows with the radius in every surface model, so the segment stays below it when its
+// highest point lies below the surface height at its smallest radius. Margins (tens of nm) absorb FP32
+// rounding; a segment that fails the test takes the exact boundary computation.
+__device__ __forceinline__ bool flight_clear(const clr_scene_params& P, float x, float y, float z, float vx, float vy,
+                                             float vz, float t) {
+    if (!(t < 1.0f)) return false;
+    const float x1 = x + t * vx, y1 = y + t * vy, z1 = z + t * vz;
+    const float R = P.rin;
+    if (!(x1 * x1 + y1 * y1 < R * R * 0.99999f)) return false;
+    if (!(z1 > P.zmin + 1e-6f)) return false;
+    float rmin2 = fminf(x * x + y * y, x1 * x1 + y1 * y1);
+    const float a = vx * vx + vy * vy;
+    if (a > 1e-20f) {
+        const float ts = -(x * vx + y * vy) / a;
+        if (ts > 0.0f && ts < t) {
+            const float xs = x + ts * vx, ys = y + ts * vy;
+            rmin2 = fminf(rmin2, xs * xs + ys * ys);
+        }
+    }
+    const float zs = o_surface_z(sqrtf(rmin2), 0.0f, P.zmean, R, P.free_surface_model, P.vortex_delta_h,
+                                 P.vortex_core_radius);
+    return fmaxf(z, z1) < zs - 1e-6f;
+}
+
 // Flight part. Returns WE_NONE when the iteration completed (the photon stays in the water),
 // WE_ENDED when the history ended, else the handler that completes the iteration (*ev_pidx is the
 // bin of a particle event). Position and direction are stored in r in every case.
@@ -391,28 +417,49 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
         double rr2w = (double)x * (double)x + (double)y * (double)y, ri2w = (double)RIN * (double)RIN;
         double water_tol = 8.0 * 1.1920928955078125e-7 * ri2w;
         if (rr2w > ri2w + water_tol) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break; }
-        double tsided = o_bore_wall_hit(x, y, z, vx, vy, vz, RIN, ZMIN, ZTOP);
-        if (tsided < 0.0) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break; }
-        float tside = (tsided < 0.5 * (double)CLR_INF_F) ? (float)tsided : CLR_INF_F;
-        float ttop = o_surface_hit(x, y, z, vx, vy, vz, ZMEAN, RIN, FSM, DH, CORE), tbottom = CLR_INF_F;
-        if (vz < -1e-14f) tbottom = (ZMIN - z) / vz;
-        if (!(ttop > 0.0f)) ttop = CLR_INF_F;
-        if (!(tbottom > 0.0f)) tbottom = CLR_INF_F;
-        int axial_top = (ttop <= tbottom && ttop < tside);
-        int axial_bottom = (tbottom < ttop && tbottom < tside);
-        int axial = axial_top || axial_bottom;
-        float tbound = axial_top ? ttop : (axial_bottom ? tbottom : tside);
-        if (tbound >= CLR_INF_F * 0.5f) { r.pf = OP_WATER_NO_BOUNDARY; r.pfs = OS_WATER_NO_BOUNDARY; r.st = 4; res = WE_ENDED; break; }
         const float MU_GEOM = (float)D.mu_channels[0], MU_WAVE = (float)D.mu_channels[1];
-        float freep = CLR_INF_F;
         float MU_TOTAL = MU_GEOM + MU_WAVE;
         // counter-based streams with node tables use the node-sum majorant (never above the reference's)
         const bool node_fast = kCounterStream<S> && TM == 3 && D.node_alias != nullptr;
         float MU_TRACK = (TM == 0) ? MU_TOTAL : node_fast ? D.node_major
                                                           : ((float)D.sed_major[0] + (float)D.sed_major[1]);
-        if (tbound > 0.0f && MU_TRACK > 0.0f) { float u = fmaxf(uniform(st), 1e-12f); freep = -logf(u) / MU_TRACK; }
-        int do_particle = freep < tbound;
-        float travel = do_particle ? freep : tbound;
+        int axial_top = 0, axial_bottom = 0, do_particle = 0;
+        float travel = 0.0f;
+        bool lazy = false;
+        float fp_pre = CLR_INF_F;
+        if constexpr (kCounterStream<S>) {
+            // Counter-based streams draw the free path first; when the whole segment provably stays in
+            // the water the boundary distances (FP64 wall and free-surface roots) are not needed.
+            if (MU_TRACK > 0.0f) {
+                const float u = fmaxf(uniform(st), 1e-12f);
+                fp_pre = -logf(u) / MU_TRACK;
+                if (flight_clear(P, x, y, z, vx, vy, vz, fp_pre)) { do_particle = 1; travel = fp_pre; lazy = true; }
+            }
+        }
+        if (!lazy) {
+            double tsided = o_bore_wall_hit(x, y, z, vx, vy, vz, RIN, ZMIN, ZTOP);
+            if (tsided < 0.0) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break; }
+            float tside = (tsided < 0.5 * (double)CLR_INF_F) ? (float)tsided : CLR_INF_F;
+            float ttop = o_surface_hit(x, y, z, vx, vy, vz, ZMEAN, RIN, FSM, DH, CORE), tbottom = CLR_INF_F;
+            if (vz < -1e-14f) tbottom = (ZMIN - z) / vz;
+            if (!(ttop > 0.0f)) ttop = CLR_INF_F;
+            if (!(tbottom > 0.0f)) tbottom = CLR_INF_F;
+            axial_top = (ttop <= tbottom && ttop < tside);
+            axial_bottom = (tbottom < ttop && tbottom < tside);
+            float tbound = axial_top ? ttop : (axial_bottom ? tbottom : tside);
+            if (tbound >= CLR_INF_F * 0.5f) { r.pf = OP_WATER_NO_BOUNDARY; r.pfs = OS_WATER_NO_BOUNDARY; r.st = 4; res = WE_ENDED; break; }
+            float freep = CLR_INF_F;
+            if (tbound > 0.0f && MU_TRACK > 0.0f) {
+                if constexpr (kCounterStream<S>) {
+                    freep = fp_pre;
+                } else {
+                    float u = fmaxf(uniform(st), 1e-12f);
+                    freep = -logf(u) / MU_TRACK;
+                }
+            }
+            do_particle = freep < tbound;
+            travel = do_particle ? freep : tbound;
+        }
         x += travel * vx; y += travel * vy; z += travel * vz;
         r.wp += travel;
         double endpoint_r2 = (double)x * x + (double)y * y;
@@ -667,67 +714,87 @@ __device__ __forceinline__ bool water_top(const DevScene& D, Ray& r, S* st) {
     return ended;
 }
 
-// reached the bottom disc
+// ---- water iterations that continue inside the acrylic (cell wall or bottom disc) ----
+// The traversal of the acrylic solid can take up to 16384 bounces (light trapped by total internal
+// reflection); the wavefront engine runs it in bounded pieces, so its loop state travels with the photon.
+enum : int { ACR_SIDE = 0, ACR_BOTTOM = 1 };
+
+// Outcome of an iteration once its acrylic traversal (or the bottom-disc entry) gave `where`;
+// true when the history ended. The two callers differ only as the reference's branches do.
 template <class S>
-__device__ __forceinline__ bool water_bottom(const DevScene& D, Ray& r, S* st) {
-    const o_cell C = make_cell(D.P);
-    float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
-    o_bcount bc = {0, 0, 0, 0, 0, 0, 0, 0};
-    int bs = 0, bb = 0;
-    const int where = o_bottom_disc(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &bs, &bb);
-    bool ended = true;
-    if (where == 1) ended = false;
-    else if (where == 2) r.st = 1;
-    else if (where == 3) r.st = 7;
-    else if (where == 5) r.st = 8;
-    else if (where == 4) {
+__device__ __forceinline__ bool acrylic_outcome(const DevScene& D, Ray& r, S* st, int caller, int where, int sub,
+                                                float* x, float* y, float* z, float* vx, float* vy, float* vz,
+                                                o_bcount* bc) {
+    if (where == 1) return false;
+    if (where == 2) { r.st = 1; return true; }
+    if (where == 3) { r.st = 7; return true; }
+    if (where == 5) { r.st = 8; return true; }
+    if (where == 4) {
+        const o_cell C = make_cell(D.P);
         int hs = 0, hb = 0;
-        const int hw = o_headspace(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
-        if (hw == 1) ended = false;
-        else if (hw == 2) r.st = 1;
+        const int hw = o_headspace(st, &C, x, y, z, vx, vy, vz, &r.ap, bc, &hs, &hb);
+        if (hw == 1) return false;
+        if (hw == 2) r.st = 1;
         else if (hw == 3) r.st = 7;
         else if (hw == 4) r.st = 6;
+        else if (hw == 5 && caller == ACR_SIDE) r.st = 8;
         else { r.pf = OP_HEADSPACE_NO_BOUNDARY; r.pfs = hs; r.st = 4; }
-    } else {
-        r.pf = (bs == OS_ACRYLIC_BOUNCE_LIMIT) ? OP_ACRYLIC_BOUNCE_LIMIT : OP_BOTTOM_GEOMETRY;
-        r.pfs = bs; r.st = 4;
+        return true;
     }
-    add_bounces(r, bc);
-    r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
-    return ended;
+    if (caller == ACR_SIDE) r.pf = (sub == OS_ACRYLIC_BOUNCE_LIMIT) ? OP_ACRYLIC_BOUNCE_LIMIT : OP_ACRYLIC_NO_INTERSECTION;
+    else r.pf = (sub == OS_ACRYLIC_BOUNCE_LIMIT) ? OP_ACRYLIC_BOUNCE_LIMIT : OP_BOTTOM_GEOMETRY;
+    r.pfs = sub;
+    r.st = 4;
+    return true;
 }
 
-// transmitted into the acrylic wall
+// Runs up to `budget` bounces of the traversal (0: to its end). Returns 0 when the iteration ended with
+// the photon in the water, 1 when the history ended, 2 when the traversal continues (state in *as).
 template <class S>
-__device__ __forceinline__ bool water_side(const DevScene& D, Ray& r, S* st) {
+__device__ __forceinline__ int acrylic_visit(const DevScene& D, Ray& r, S* st, int caller, o_acr_state* as,
+                                             int budget) {
     const clr_scene_params& P = D.P;
     const o_cell C = make_cell(P);
     float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
     o_bcount bc = {0, 0, 0, 0, 0, 0, 0, 0};
     int sub = 0, nb = 0;
-    const int where = o_acrylic_solid(st, &C, C.n_air, C.n_bottom_ext, P.zmin, C.Zlow, &x, &y, &z, &vx, &vy, &vz,
-                                      &r.ap, &bc, &sub, &nb);
-    bool ended = true;
-    if (where == 1) ended = false;
-    else if (where == 2) r.st = 1;
-    else if (where == 3) r.st = 7;
-    else if (where == 5) r.st = 8;
-    else if (where == 4) {
-        int hs = 0, hb = 0;
-        const int hw = o_headspace(st, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
-        if (hw == 1) ended = false;
-        else if (hw == 2) r.st = 1;
-        else if (hw == 3) r.st = 7;
-        else if (hw == 4) r.st = 6;
-        else if (hw == 5) r.st = 8;
-        else { r.pf = OP_HEADSPACE_NO_BOUNDARY; r.pfs = hs; r.st = 4; }
-    } else {
-        r.pf = (sub == OS_ACRYLIC_BOUNCE_LIMIT) ? OP_ACRYLIC_BOUNCE_LIMIT : OP_ACRYLIC_NO_INTERSECTION;
-        r.pfs = sub; r.st = 4;
-    }
+    const int where = o_acrylic_run(st, &C, C.n_air, C.n_bottom_ext, P.zmin, C.Zlow, &x, &y, &z, &vx, &vy, &vz, &r.ap,
+                                    &bc, &sub, &nb, as, budget);
+    int res = 2;
+    if (where >= 0) res = acrylic_outcome(D, r, st, caller, where, sub, &x, &y, &z, &vx, &vy, &vz, &bc) ? 1 : 0;
     add_bounces(r, bc);
     r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
-    return ended;
+    return res;
+}
+
+// reached the bottom disc: same return codes as acrylic_visit
+template <class S>
+__device__ __forceinline__ int water_bottom_visit(const DevScene& D, Ray& r, S* st, o_acr_state* as, int budget) {
+    const o_cell C = make_cell(D.P);
+    float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
+    o_bcount bc = {0, 0, 0, 0, 0, 0, 0, 0};
+    int bs = 0, bb = 0;
+    const int e = o_bottom_entry(st, &C, &x, &y, &z, &vx, &vy, &vz, &bc, &bs, &bb);
+    int res = 2;
+    if (e != 6) res = acrylic_outcome(D, r, st, ACR_BOTTOM, e, bs, &x, &y, &z, &vx, &vy, &vz, &bc) ? 1 : 0;
+    add_bounces(r, bc);
+    r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
+    if (e != 6) return res;
+    *as = o_acr_start();
+    return acrylic_visit(D, r, st, ACR_BOTTOM, as, budget);
+}
+
+template <class S>
+__device__ __forceinline__ bool water_bottom(const DevScene& D, Ray& r, S* st) {
+    o_acr_state as;
+    return water_bottom_visit(D, r, st, &as, 0) == 1;
+}
+
+// transmitted into the acrylic wall
+template <class S>
+__device__ __forceinline__ bool water_side(const DevScene& D, Ray& r, S* st) {
+    o_acr_state as = o_acr_start();
+    return acrylic_visit(D, r, st, ACR_SIDE, &as, 0) == 1;
 }
 
 // One whole water iteration (flight part and its handler).

@@ -933,19 +933,30 @@ typedef struct {
     int model; float dh, core;
 } o_cell;
 
+/* Loop state of a traversal of the acrylic solid, so that a traversal can run in bounded pieces. */
+typedef struct {
+    int it, stuck, last_surf;
+} o_acr_state;
+__device__ __forceinline__ o_acr_state o_acr_start() {
+    o_acr_state a = {0, 0, -1};
+    return a;
+}
+
 /* inside the connected acrylic solid; 1 water, 2 external air, 3 bottom external, 4 headspace,
- * 5 trapped, 0 failure (:3143-3198) */
+ * 5 trapped, 0 failure (:3143-3198). Runs bounces from as->it on; with budget > 0 at most `budget`
+ * of them, returning -1 (and the loop state in *as) when the traversal has not ended by then. */
 template <class S>
-__device__ __noinline__ int o_acrylic_solid(S* s, const o_cell* C, float n_side_air, float n_bottom_ext, float Zmin,
-                           float Zlow, float* x, float* y, float* z, float* vx, float* vy, float* vz,
-                           float* acrylic_path, o_bcount* bc, int* sub, int* out_bounces) {
-    *sub = OS_NONE;
-    *out_bounces = 0;
+__device__ __noinline__ int o_acrylic_run(S* s, const o_cell* C, float n_side_air, float n_bottom_ext, float Zmin,
+                                          float Zlow, float* x, float* y, float* z, float* vx, float* vy, float* vz,
+                                          float* acrylic_path, o_bcount* bc, int* sub, int* out_bounces,
+                                          o_acr_state* as, int budget) {
     const int cap = 16384;
-    int stuck = 0, last_surf = -1;
+    int stuck = as->stuck, last_surf = as->last_surf;
     const float n_water = C->n_water, n_acrylic = C->n_acrylic, n_air = n_side_air;
     const float Rin = C->Rin, Rout = C->Rout, Ztop = C->Ztop;
-    for (int it = 0; it < cap; ++it) {
+    const int it0 = as->it;
+    const int end = (budget > 0 && cap - it0 > budget) ? it0 + budget : cap;
+    for (int it = it0; it < end; ++it) {
         *out_bounces = it;
         double td = 1.0e300;
         int surf = o_acrylic_next(*x, *y, *z, *vx, *vy, *vz, Rin, Rout, Zmin, Zlow, Ztop, &td);
@@ -1026,6 +1037,10 @@ __device__ __noinline__ int o_acrylic_solid(S* s, const o_cell* C, float n_side_
         if (stuck >= 8) { *sub = OS_ACRYLIC_BOUNCE_LIMIT; return 0; }
         last_surf = surf;
     }
+    if (end < cap) {
+        as->it = end; as->stuck = stuck; as->last_surf = last_surf;
+        return -1;
+    }
     if (o_trapped(*x, *y, *z, *vx, *vy, *vz, n_water, n_acrylic, n_air, n_bottom_ext, Rin, Rout)) {
         *sub = OS_NONE; *out_bounces = 16384;
         return 5;
@@ -1034,10 +1049,22 @@ __device__ __noinline__ int o_acrylic_solid(S* s, const o_cell* C, float n_side_
     *out_bounces = 16384;
     return 0;
 }
-/* water -> bottom disc (:3211-3224) */
 template <class S>
-__device__ __noinline__ int o_bottom_disc(S* s, const o_cell* C, float* x, float* y, float* z, float* vx, float* vy, float* vz,
-                         float* acrylic_path, o_bcount* bc, int* sub, int* out_bounces) {
+__device__ __forceinline__ int o_acrylic_solid(S* s, const o_cell* C, float n_side_air, float n_bottom_ext, float Zmin,
+                                               float Zlow, float* x, float* y, float* z, float* vx, float* vy,
+                                               float* vz, float* acrylic_path, o_bcount* bc, int* sub,
+                                               int* out_bounces) {
+    *sub = OS_NONE;
+    *out_bounces = 0;
+    o_acr_state as = o_acr_start();
+    return o_acrylic_run(s, C, n_side_air, n_bottom_ext, Zmin, Zlow, x, y, z, vx, vy, vz, acrylic_path, bc, sub,
+                         out_bounces, &as, 0);
+}
+/* water -> bottom disc (:3211-3224), first part: 1 reflected back into the water, 0 failure,
+ * 6 transmitted into the disc (the traversal of the acrylic solid follows) */
+template <class S>
+__device__ __forceinline__ int o_bottom_entry(S* s, const o_cell* C, float* x, float* y, float* z, float* vx,
+                                              float* vy, float* vz, o_bcount* bc, int* sub, int* out_bounces) {
     *sub = OS_NONE;
     *out_bounces = 0;
     {
@@ -1057,6 +1084,13 @@ __device__ __noinline__ int o_bottom_disc(S* s, const o_cell* C, float* x, float
     }
     *vx = a; *vy = b; *vz = c;
     *z = C->Zmin - CLR_EPS_F;
+    return 6;
+}
+template <class S>
+__device__ __noinline__ int o_bottom_disc(S* s, const o_cell* C, float* x, float* y, float* z, float* vx, float* vy, float* vz,
+                         float* acrylic_path, o_bcount* bc, int* sub, int* out_bounces) {
+    const int e = o_bottom_entry(s, C, x, y, z, vx, vy, vz, bc, sub, out_bounces);
+    if (e != 6) return e;
     return o_acrylic_solid(s, C, C->n_air, C->n_bottom_ext, C->Zmin, C->Zlow, x, y, z, vx, vy, vz, acrylic_path, bc,
                            sub, out_bounces);
 }

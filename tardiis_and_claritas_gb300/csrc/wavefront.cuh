@@ -12,15 +12,19 @@
 //          Fresnel reflections at the surface and the wall)     -> an event queue, FIN, or FLIGHT
 //   COND, GEOM, MORPH   particle events (conditional closure, geometric sphere, spheroid)
 //   TOP, BOTTOM, SIDE   transmission into the headspace, the bottom disc, the acrylic wall
-//                                                                -> FLIGHT or FIN
+//                                                                -> FLIGHT, FIN or ACRYL
+//   ACRYL  the next bounded piece of a long traversal of the acrylic solid
 //   FIN    detector scoring and tallies; the slot returns to the free queue
 //
-// One pass launches the ten stage kernels in that order. Queues are ring buffers of slot ids with
-// monotonically increasing 32-bit head/tail counters (capacity a power of two, so wrap-around is
-// exact). A stage consumes the window [head, snap) of its queue, where snap is the tail that the
-// previous stage kernel's last block recorded after all of its pushes, so a stage never consumes
-// slots pushed while it runs (FLIGHT may push to itself). Pushes are aggregated per warp and queue.
-// The last block of FIN sets a live flag that the host reads every few passes.
+// A pass is one CUDA graph: a begin kernel, then the eleven stage kernels as independent branches, so
+// the latency-bound stages (long FP64 chains in the acrylic, rare events) overlap with the
+// throughput-bound ones instead of idling the GPU behind them. Queues are ring buffers of slot ids
+// with monotonically increasing 32-bit head/tail counters; the ring holds twice the pool, so a window
+// being consumed and the pushes that land behind it never collide (wrap-around is exact because the
+// ring size is a power of two). The begin kernel retires the previous pass's windows and snapshots
+// every queue: during the pass each stage consumes [head, snap) of its queue while all pushes land at
+// or after the tail, so no slot is handled twice in a pass and no stage reads an entry still being
+// written. Pushes are aggregated per warp and queue. Rare stages skip passes until a batch is queued.
 //
 // Within each stage the device functions, arithmetic and per-ray draw order are the persistent
 // kernel's (they are the same functions), so per-ray results in the xorshift parity mode are
@@ -31,12 +35,25 @@
 namespace clr {
 namespace {
 
-enum : int { WQ_FREE = 0, WQ_ENTRY, WQ_FLIGHT, WQ_COND, WQ_GEOM, WQ_MORPH, WQ_TOP, WQ_BOTTOM, WQ_SIDE, WQ_FIN };
+enum : int { WQ_FREE = 0, WQ_ENTRY, WQ_FLIGHT, WQ_COND, WQ_GEOM, WQ_MORPH, WQ_TOP, WQ_BOTTOM, WQ_SIDE, WQ_ACRYL,
+             WQ_FIN };
 static_assert(WQ_FIN + 1 == CLR_WQ_COUNT, "queue count");
 
 constexpr int kWaveThreads = 256;
 // water flights per FLIGHT visit before the photon is re-queued (bounds lane imbalance in a warp)
 constexpr int kFlightSteps = 8;
+// Rare stages (few photons per pass, long serial work per photon) run only when their queue holds a
+// full batch, after kMaxSkips passes, or while the pool drains.
+constexpr unsigned kRareBatch = 8192;
+constexpr unsigned kMaxSkips = 8;
+__host__ __device__ constexpr bool stage_is_rare(int q) {
+    return q == WQ_COND || q == WQ_MORPH || q == WQ_TOP || q == WQ_BOTTOM;
+}
+// minimum resident blocks per SM (register budget) per stage
+__host__ __device__ constexpr int stage_min_blocks(int q) { return q == WQ_COND ? 1 : 2; }
+// acrylic bounces per visit of SIDE, BOTTOM and ACRYL (a traversal can take 16384), all of them
+// once every photon has been drawn
+constexpr int kAcrBudget = 256;
 
 template <class Mode>
 struct WavePool {
@@ -54,6 +71,10 @@ __device__ __forceinline__ WavePool<Mode> wave_pool(const WaveLaunch& w) {
     return p;
 }
 
+// ring of queue q (2 * cap entries)
+__device__ __forceinline__ uint32_t* wave_ring(const WaveLaunch& w, int q) { return w.qbuf + (size_t)q * 2u * w.cap; }
+__device__ __forceinline__ unsigned wave_mask(const WaveLaunch& w) { return 2u * w.cap - 1u; }
+
 // Warp-aggregated push of `slot` to queue `q` (q < 0: no push). Called by all 32 lanes.
 __device__ __forceinline__ void wave_push(const WaveLaunch& w, int q, uint32_t slot) {
     const unsigned FULL = 0xffffffffu;
@@ -65,34 +86,29 @@ __device__ __forceinline__ void wave_push(const WaveLaunch& w, int q, uint32_t s
     base = __shfl_sync(FULL, base, leader);
     if (q >= 0) {
         const unsigned pos = base + (unsigned)__popc(grp & ((1u << lane) - 1u));
-        w.qbuf[(size_t)q * w.cap + (pos & (w.cap - 1u))] = slot;
+        wave_ring(w, q)[pos & wave_mask(w)] = slot;
     }
 }
 
-// End of a stage kernel: the last block to finish retires the consumed window and records the
-// snapshot of the next stage's queue; the last block of FIN also computes the live flag.
-__device__ __forceinline__ void wave_commit(const WaveLaunch& w, int q) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned done = atomicAdd(&w.ctl->finished[q], 1u);
-        if (done == gridDim.x - 1) {
-            __threadfence();
-            WaveCtl* c = w.ctl;
-            c->head[q] = c->snap[q];
-            const int nq = (q + 1) % CLR_WQ_COUNT;
-            c->snap[nq] = atomicAdd(&c->tail[nq], 0u);
-            c->finished[q] = 0u;
-            if (q == WQ_FIN) {
-                unsigned pending = 0;
-                for (int k = 1; k < CLR_WQ_COUNT; ++k) pending |= atomicAdd(&c->tail[k], 0u) - c->head[k];
-                const unsigned long long np = atomicAdd(&c->next_photon, 0ull);
-                c->live = (pending != 0u || np < c->total_photons) ? 1u : 0u;
-                c->passes++;
-            }
-            __threadfence();
-        }
+// Begin of a pass (one thread): retire the windows of the previous pass, decide which stages run, take
+// the windows of this pass, and publish whether any photon is still in flight or undrawn.
+__global__ void wave_begin_kernel(WaveLaunch w) {
+    if (threadIdx.x | blockIdx.x) return;
+    WaveCtl* c = w.ctl;
+    const bool drawing = c->next_photon < c->total_photons;
+    unsigned pending = 0;
+    for (int q = 0; q < CLR_WQ_COUNT; ++q) {
+        c->head[q] = c->snap[q];
+        const unsigned n = c->tail[q] - c->head[q];
+        if (q != WQ_FREE) pending |= n;
+        bool run = n > 0;
+        if (q == WQ_FREE) run = run && drawing;
+        else if (stage_is_rare(q) && n < kRareBatch && c->skips[q] < kMaxSkips && drawing) run = false;
+        c->snap[q] = run ? c->tail[q] : c->head[q];
+        c->skips[q] = run ? 0u : c->skips[q] + (n > 0 ? 1u : 0u);
     }
+    c->live = (pending != 0u || drawing) ? 1u : 0u;
+    c->passes++;
 }
 
 // Per-block conditional-closure statistics for scenario 0 (others go straight to the device tally).
@@ -112,18 +128,25 @@ __device__ __forceinline__ void block_stats_flush(BlockStats* b, DevTally* t, in
     if (threadIdx.x == 0 && b->items) atomicAdd(&t[0].sched[q], b->items);
 }
 
-// Window of the stage's queue, iterated in warp-uniform chunks of 32 entries.
+// Chunk order of a stage: warp k of block b takes chunks (k * gridDim.x + b) + j * (all warps), so a
+// window smaller than the grid is spread over every block (and SM) rather than the first blocks.
+__device__ __forceinline__ unsigned wave_first_chunk() { return (threadIdx.x >> 5) * gridDim.x + blockIdx.x; }
+
+// This pass's window of queue q, iterated in warp-uniform chunks of 32 entries.
 struct WaveWindow {
     unsigned head, n;
 };
 __device__ __forceinline__ WaveWindow wave_window(const WaveLaunch& w, int q) {
     WaveWindow win;
-    win.head = *(volatile unsigned*)&w.ctl->head[q];
-    win.n = *(volatile unsigned*)&w.ctl->snap[q] - win.head;
+    win.head = w.ctl->head[q];
+    win.n = w.ctl->snap[q] - win.head;
     return win;
 }
 
-template <class Mode>
+__device__ __forceinline__ bool wave_drawing(const WaveLaunch& w) {
+    return *(volatile unsigned long long*)&w.ctl->next_photon < w.ctl->total_photons;
+}
+
 __device__ __forceinline__ void photon_of(const WaveLaunch& w, unsigned long long p, int* sid, long long* rid) {
     int lo = 0, hi = w.n_scen - 1;
     while (lo < hi) {  // last scenario whose first photon is <= p
@@ -134,31 +157,35 @@ __device__ __forceinline__ void photon_of(const WaveLaunch& w, unsigned long lon
     *rid = (long long)(p - (unsigned long long)w.ray_begin[lo]);
 }
 
+__device__ __forceinline__ void warp_tally_zero(WarpTally* wt, int lane) {
+    unsigned long long* p = reinterpret_cast<unsigned long long*>(wt);
+    for (int i = lane; i < (int)(sizeof(WarpTally) / 8); i += 32) p[i] = 0ull;
+}
+
 // ---------------- GEN: fill free slots with photons that pass the source collimator ----------------
 template <class Mode>
 __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
+    const WaveWindow win = wave_window(w, WQ_FREE);
+    if (win.n == 0) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WarpTally* wt = reinterpret_cast<WarpTally*>(smem_raw) + (threadIdx.x >> 5);
     __shared__ DetTable det;
     __shared__ unsigned long long items;
     det_table_init(&det);
     const int lane = threadIdx.x & 31;
-    {
-        unsigned long long* p = reinterpret_cast<unsigned long long*>(wt);
-        for (int i = lane; i < (int)(sizeof(WarpTally) / 8); i += 32) p[i] = 0ull;
-    }
+    warp_tally_zero(wt, lane);
     if (threadIdx.x == 0) items = 0ull;
     __syncthreads();
     const WavePool<Mode> pool = wave_pool<Mode>(w);
-    const WaveWindow win = wave_window(w, WQ_FREE);
+    const uint32_t* ring = wave_ring(w, WQ_FREE);
     const unsigned FULL = 0xffffffffu;
-    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, n_warps = (gridDim.x * blockDim.x) >> 5;
-    bool out = *(volatile unsigned long long*)&w.ctl->next_photon >= w.ctl->total_photons;
+    const unsigned warp = wave_first_chunk(), n_warps = (gridDim.x * blockDim.x) >> 5;
+    bool out = !wave_drawing(w);
     unsigned long long drawn = 0;
     for (unsigned base = warp * 32u; base < win.n && !__all_sync(FULL, out); base += n_warps * 32u) {
         const unsigned i = base + lane;
         const bool valid = i < win.n;
-        const uint32_t slot = valid ? w.qbuf[(size_t)WQ_FREE * w.cap + ((win.head + i) & (w.cap - 1u))] : 0u;
+        const uint32_t slot = valid ? ring[(win.head + i) & wave_mask(w)] : 0u;
         bool filled = false;
         while (true) {
             const unsigned need = __ballot_sync(FULL, valid && !filled && !out);
@@ -173,7 +200,7 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
                 } else {
                     int sid;
                     long long rid;
-                    photon_of<Mode>(w, p, &sid, &rid);
+                    photon_of(w, p, &sid, &rid);
                     const DevScene& D = w.scenes[sid];
                     const uint32_t gid = D.ray_offset + (uint32_t)rid;
                     typename Mode::Lane L;
@@ -187,20 +214,21 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
                         pool.ray[slot] = r;
                         pool.lane[slot] = L;
                         SlotMeta m;
-                        m.gid = gid; m.sid = sid; m.rid = rid; m.pidx = -1; m.pad = 0;
+                        m.gid = gid; m.sid = sid; m.rid = rid; m.pidx = -1;
+                        m.acr_caller = 0; m.acr_it = 0; m.acr_stuck = 0; m.acr_last = -1; m.pad = 0;
                         pool.meta[slot] = m;
                         filled = true;
                     }
                 }
             }
         }
+        // slots left unfilled once every photon is drawn are not needed again
         wave_push(w, filled ? WQ_ENTRY : -1, slot);
     }
     atomicAdd(&items, drawn);
     __syncthreads();
     flush_warp_tally(wt, w.tallies, lane);
     if (threadIdx.x == 0 && items) atomicAdd(&w.tallies[0].sched[WQ_FREE], items);
-    wave_commit(w, WQ_FREE);
 }
 
 // ---------------- generic stage kernel (ENTRY, FLIGHT and the event handlers) ----------------
@@ -235,26 +263,46 @@ __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevSce
         return water_morph(D, r, L.optics(), cstats, m.pidx) ? WQ_FIN : WQ_FLIGHT;
     } else if constexpr (Q == WQ_TOP) {
         return water_top(D, r, L.transport()) ? WQ_FIN : WQ_FLIGHT;
-    } else if constexpr (Q == WQ_BOTTOM) {
-        return water_bottom(D, r, L.transport()) ? WQ_FIN : WQ_FLIGHT;
     } else {
-        return water_side(D, r, L.transport()) ? WQ_FIN : WQ_FLIGHT;
+        // SIDE, BOTTOM and ACRYL: a bounded piece of the acrylic traversal
+        const int budget = wave_drawing(w) ? kAcrBudget : 0;
+        o_acr_state as;
+        int caller, v;
+        if constexpr (Q == WQ_BOTTOM) {
+            caller = ACR_BOTTOM;
+            v = water_bottom_visit(D, r, L.transport(), &as, budget);
+        } else if constexpr (Q == WQ_SIDE) {
+            caller = ACR_SIDE;
+            as = o_acr_start();
+            v = acrylic_visit(D, r, L.transport(), ACR_SIDE, &as, budget);
+        } else {
+            caller = m.acr_caller;
+            as.it = m.acr_it; as.stuck = m.acr_stuck; as.last_surf = m.acr_last;
+            v = acrylic_visit(D, r, L.transport(), caller, &as, budget);
+        }
+        if (v == 2) {
+            m.acr_caller = caller; m.acr_it = as.it; m.acr_stuck = as.stuck; m.acr_last = as.last_surf;
+            return WQ_ACRYL;
+        }
+        return v ? WQ_FIN : WQ_FLIGHT;
     }
 }
 
 template <class Mode, int Q>
-__global__ void __launch_bounds__(kWaveThreads) wave_stage_kernel(WaveLaunch w) {
+__global__ void __launch_bounds__(kWaveThreads, stage_min_blocks(Q)) wave_stage_kernel(WaveLaunch w) {
+    const WaveWindow win = wave_window(w, Q);
+    if (win.n == 0) return;
     __shared__ BlockStats bs;
     block_stats_init(&bs);
     const WavePool<Mode> pool = wave_pool<Mode>(w);
-    const WaveWindow win = wave_window(w, Q);
+    const uint32_t* ring = wave_ring(w, Q);
     const int lane = threadIdx.x & 31;
-    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, n_warps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned warp = wave_first_chunk(), n_warps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long done = 0;
     for (unsigned base = warp * 32u; base < win.n; base += n_warps * 32u) {
         const unsigned i = base + lane;
         const bool valid = i < win.n;
-        const uint32_t slot = valid ? w.qbuf[(size_t)Q * w.cap + ((win.head + i) & (w.cap - 1u))] : 0u;
+        const uint32_t slot = valid ? ring[(win.head + i) & wave_mask(w)] : 0u;
         int dest = -1;
         if (valid) {
             Ray r = pool.ray[slot];
@@ -266,38 +314,37 @@ __global__ void __launch_bounds__(kWaveThreads) wave_stage_kernel(WaveLaunch w) 
             pool.ray[slot] = r;
             pool.lane[slot] = L;
             if (Q == WQ_FLIGHT) pool.meta[slot].pidx = m.pidx;
+            if ((Q == WQ_SIDE || Q == WQ_BOTTOM || Q == WQ_ACRYL) && dest == WQ_ACRYL) pool.meta[slot] = m;
             done++;
         }
         wave_push(w, dest, slot);
     }
     atomicAdd(&bs.items, done);
     block_stats_flush(&bs, w.tallies, Q);
-    wave_commit(w, Q);
 }
 
 // ---------------- FIN: detector scoring and tallies; the slot becomes free ----------------
 template <class Mode, bool kRecord>
 __global__ void __launch_bounds__(kWaveThreads) wave_fin_kernel(WaveLaunch w) {
+    const WaveWindow win = wave_window(w, WQ_FIN);
+    if (win.n == 0) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WarpTally* wt = reinterpret_cast<WarpTally*>(smem_raw) + (threadIdx.x >> 5);
     __shared__ DetTable det;
     __shared__ unsigned long long items;
     det_table_init(&det);
     const int lane = threadIdx.x & 31;
-    {
-        unsigned long long* p = reinterpret_cast<unsigned long long*>(wt);
-        for (int i = lane; i < (int)(sizeof(WarpTally) / 8); i += 32) p[i] = 0ull;
-    }
+    warp_tally_zero(wt, lane);
     if (threadIdx.x == 0) items = 0ull;
     __syncthreads();
     const WavePool<Mode> pool = wave_pool<Mode>(w);
-    const WaveWindow win = wave_window(w, WQ_FIN);
-    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, n_warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t* ring = wave_ring(w, WQ_FIN);
+    const unsigned warp = wave_first_chunk(), n_warps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long done = 0;
     for (unsigned base = warp * 32u; base < win.n; base += n_warps * 32u) {
         const unsigned i = base + lane;
         const bool valid = i < win.n;
-        const uint32_t slot = valid ? w.qbuf[(size_t)WQ_FIN * w.cap + ((win.head + i) & (w.cap - 1u))] : 0u;
+        const uint32_t slot = valid ? ring[(win.head + i) & wave_mask(w)] : 0u;
         if (valid) {
             const Ray r = pool.ray[slot];
             const SlotMeta m = pool.meta[slot];
@@ -311,17 +358,17 @@ __global__ void __launch_bounds__(kWaveThreads) wave_fin_kernel(WaveLaunch w) {
     __syncthreads();
     flush_warp_tally(wt, w.tallies, lane);
     if (threadIdx.x == 0 && items) atomicAdd(&w.tallies[0].sched[WQ_FIN], items);
-    wave_commit(w, WQ_FIN);
 }
 
 __global__ void wave_init_kernel(WaveLaunch w) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.cap) w.qbuf[(size_t)WQ_FREE * w.cap + i] = i;
+    if (i < w.cap) wave_ring(w, WQ_FREE)[i] = i;
     if (i == 0) {
         WaveCtl* c = w.ctl;
-        for (int k = 0; k < CLR_WQ_COUNT; ++k) { c->head[k] = 0u; c->tail[k] = 0u; c->snap[k] = 0u; c->finished[k] = 0u; }
+        for (int k = 0; k < CLR_WQ_COUNT; ++k) {
+            c->head[k] = 0u; c->tail[k] = 0u; c->snap[k] = 0u; c->finished[k] = 0u; c->skips[k] = 0u;
+        }
         c->tail[WQ_FREE] = w.cap;
-        c->snap[WQ_FREE] = w.cap;
         c->next_photon = 0ull;
         c->total_photons = w.total;
         c->live = w.total > 0 ? 1u : 0u;
@@ -330,44 +377,76 @@ __global__ void wave_init_kernel(WaveLaunch w) {
 }
 
 // ---------------- host driver ----------------
+// One pass as a graph: the begin kernel, then every stage kernel depending only on it.
 template <class Mode, bool kRecord>
-struct WaveKernels {
+struct WavePass {
     static constexpr int kSmemTally = (kWaveThreads / 32) * (int)sizeof(WarpTally);
-    int grid[CLR_WQ_COUNT] = {0};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
 
-    cudaError_t setup(int num_sms) {
-        cudaError_t e;
-        e = cudaFuncSetAttribute(wave_gen_kernel<Mode>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTally);
-        if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(wave_fin_kernel<Mode, kRecord>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 kSmemTally);
-        if (e != cudaSuccess) return e;
-        int occ[CLR_WQ_COUNT] = {0};
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[WQ_FREE], wave_gen_kernel<Mode>, kWaveThreads, kSmemTally);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[WQ_ENTRY], wave_stage_kernel<Mode, WQ_ENTRY>, kWaveThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[WQ_FLIGHT], wave_stage_kernel<Mode, WQ_FLIGHT>, kWaveThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[WQ_COND], wave_stage_kernel<Mode, WQ_COND>, kWaveThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[WQ_GEOM], wave_stage_kernel<Mode, WQ_GEOM>, kWaveThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[WQ_MORPH], wave_stage_kernel<Mode, WQ_MORPH>, kWaveThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[WQ_TOP], wave_stage_kernel<Mode, WQ_TOP>, kWaveThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[WQ_BOTTOM], wave_stage_kernel<Mode, WQ_BOTTOM>, kWaveThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[WQ_SIDE], wave_stage_kernel<Mode, WQ_SIDE>, kWaveThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[WQ_FIN], wave_fin_kernel<Mode, kRecord>, kWaveThreads, kSmemTally);
-        for (int k = 0; k < CLR_WQ_COUNT; ++k) grid[k] = num_sms * (occ[k] > 0 ? occ[k] : 1);
-        return cudaGetLastError();
+    ~WavePass() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
     }
 
-    void pass(const WaveLaunch& w, cudaStream_t st) const {
-        wave_gen_kernel<Mode><<<grid[WQ_FREE], kWaveThreads, kSmemTally, st>>>(w);
-        wave_stage_kernel<Mode, WQ_ENTRY><<<grid[WQ_ENTRY], kWaveThreads, 0, st>>>(w);
-        wave_stage_kernel<Mode, WQ_FLIGHT><<<grid[WQ_FLIGHT], kWaveThreads, 0, st>>>(w);
-        wave_stage_kernel<Mode, WQ_COND><<<grid[WQ_COND], kWaveThreads, 0, st>>>(w);
-        wave_stage_kernel<Mode, WQ_GEOM><<<grid[WQ_GEOM], kWaveThreads, 0, st>>>(w);
-        wave_stage_kernel<Mode, WQ_MORPH><<<grid[WQ_MORPH], kWaveThreads, 0, st>>>(w);
-        wave_stage_kernel<Mode, WQ_TOP><<<grid[WQ_TOP], kWaveThreads, 0, st>>>(w);
-        wave_stage_kernel<Mode, WQ_BOTTOM><<<grid[WQ_BOTTOM], kWaveThreads, 0, st>>>(w);
-        wave_stage_kernel<Mode, WQ_SIDE><<<grid[WQ_SIDE], kWaveThreads, 0, st>>>(w);
-        wave_fin_kernel<Mode, kRecord><<<grid[WQ_FIN], kWaveThreads, kSmemTally, st>>>(w);
+    static cudaError_t grid_of(const void* kernel, int smem, int num_sms, int per_sm_cap, dim3* g) {
+        int occ = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kWaveThreads, smem);
+        if (e != cudaSuccess) return e;
+        if (occ < 1) occ = 1;
+        if (per_sm_cap > 0 && occ > per_sm_cap) occ = per_sm_cap;
+        *g = dim3((unsigned)(num_sms * occ));
+        return cudaSuccess;
+    }
+
+    cudaError_t build(const WaveLaunch& w, int num_sms) {
+        cudaError_t e;
+        if ((e = cudaFuncSetAttribute(wave_gen_kernel<Mode>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      kSmemTally)) != cudaSuccess)
+            return e;
+        if ((e = cudaFuncSetAttribute(wave_fin_kernel<Mode, kRecord>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      kSmemTally)) != cudaSuccess)
+            return e;
+        if ((e = cudaGraphCreate(&graph, 0)) != cudaSuccess) return e;
+        void* args[] = {const_cast<WaveLaunch*>(&w)};
+        cudaKernelNodeParams p = {};
+        p.kernelParams = args;
+        p.func = (void*)wave_begin_kernel;
+        p.gridDim = dim3(1);
+        p.blockDim = dim3(32);
+        p.sharedMemBytes = 0;
+        cudaGraphNode_t begin;
+        if ((e = cudaGraphAddKernelNode(&begin, graph, nullptr, 0, &p)) != cudaSuccess) return e;
+        struct StageK {
+            const void* fn;
+            int smem;
+            int per_sm_cap;
+        };
+        // rare stages get one block per SM: their windows are small and their warps long-lived
+        const StageK ks[CLR_WQ_COUNT] = {
+            {(const void*)wave_gen_kernel<Mode>, kSmemTally, 0},
+            {(const void*)wave_stage_kernel<Mode, WQ_ENTRY>, 0, 0},
+            {(const void*)wave_stage_kernel<Mode, WQ_FLIGHT>, 0, 0},
+            {(const void*)wave_stage_kernel<Mode, WQ_COND>, 0, 1},
+            {(const void*)wave_stage_kernel<Mode, WQ_GEOM>, 0, 0},
+            {(const void*)wave_stage_kernel<Mode, WQ_MORPH>, 0, 1},
+            {(const void*)wave_stage_kernel<Mode, WQ_TOP>, 0, 1},
+            {(const void*)wave_stage_kernel<Mode, WQ_BOTTOM>, 0, 1},
+            {(const void*)wave_stage_kernel<Mode, WQ_SIDE>, 0, 0},
+            {(const void*)wave_stage_kernel<Mode, WQ_ACRYL>, 0, 1},
+            {(const void*)wave_fin_kernel<Mode, kRecord>, kSmemTally, 0},
+        };
+        p.blockDim = dim3(kWaveThreads);
+        for (int q = 0; q < CLR_WQ_COUNT; ++q) {
+            dim3 g;
+            if ((e = grid_of(ks[q].fn, ks[q].smem, num_sms, ks[q].per_sm_cap, &g)) != cudaSuccess) return e;
+            p.func = const_cast<void*>(ks[q].fn);
+            p.gridDim = g;
+            p.sharedMemBytes = (unsigned)ks[q].smem;
+            cudaGraphNode_t node;
+            if ((e = cudaGraphAddKernelNode(&node, graph, &begin, 1, &p)) != cudaSuccess) return e;
+        }
+        return cudaGraphInstantiate(&exec, graph, 0);
     }
 };
 
@@ -376,28 +455,34 @@ struct WaveKernels {
 // find empty windows and return at once.
 template <class Mode, bool kRecord>
 cudaError_t wave_run_t(const WaveLaunch& w, int num_sms, cudaStream_t st, long long max_passes, int* passes_out) {
-    WaveKernels<Mode, kRecord> K;
-    cudaError_t e = K.setup(num_sms);
+    WavePass<Mode, kRecord> P;
+    cudaError_t e = P.build(w, num_sms);
     if (e != cudaSuccess) return e;
     wave_init_kernel<<<(w.cap + 255) / 256, 256, 0, st>>>(w);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int batch = 8;
     long long launched = 0;
     volatile unsigned* live = w.host_live;
-    for (int k = 0; k < batch; ++k) K.pass(w, st);
+    for (int k = 0; k < batch; ++k)
+        if ((e = cudaGraphLaunch(P.exec, st)) != cudaSuccess) return e;
     launched += batch;
     while (true) {
         if ((e = cudaMemcpyAsync((void*)w.host_live, &w.ctl->live, sizeof(unsigned), cudaMemcpyDeviceToHost, st)) !=
             cudaSuccess)
             return e;
         if ((e = cudaEventRecord(w.flag_event, st)) != cudaSuccess) return e;
-        for (int k = 0; k < batch; ++k) K.pass(w, st);
+        for (int k = 0; k < batch; ++k)
+            if ((e = cudaGraphLaunch(P.exec, st)) != cudaSuccess) return e;
         launched += batch;
         if ((e = cudaEventSynchronize(w.flag_event)) != cudaSuccess) return e;
         if (*live == 0u) break;
-        if (launched > max_passes) return cudaErrorLaunchTimeout;
+        if (launched > max_passes) {
+            cudaStreamSynchronize(st);
+            return cudaErrorLaunchTimeout;
+        }
     }
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // wait for the passes queued after the flag read before the graph is destroyed
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     if (passes_out) *passes_out = (int)launched;
     return cudaSuccess;
 }
