@@ -236,6 +236,8 @@ int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sed
     CU(cudaMemcpyAsync(&herr, pb.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     if (pb.node_tables)
         CU(cudaMemcpyAsync(&pb.node_major_host, pb.node_major, sizeof(float), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(pb.muscal_host, pb.muscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(pb.sed_major_host, pb.sed_major, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     if (herr) return fail(ctx, CLR_ERR_PRECOMPUTE, "particle precompute failed with error code %d", herr);
     ctx->built = true;
@@ -288,6 +290,9 @@ static void fill_scene(const clr_ctx* ctx, const clr_run_params* run, DevScene* 
     s->node_mu = node ? pb.node_mu : nullptr;
     s->node_alias = node ? pb.node_alias : nullptr;
     s->node_major = pb.node_major_host;
+    s->mu_geom_f = (float)pb.muscal_host[0]; s->mu_wave_f = (float)pb.muscal_host[1];
+    s->coherent_f = (float)pb.muscal_host[7];
+    s->sed_major_f[0] = (float)pb.sed_major_host[0]; s->sed_major_f[1] = (float)pb.sed_major_host[1];
     s->seed0 = run->seed0; s->seed1 = run->seed1; s->seed2 = run->seed2; s->det_seed = run->detector_seed;
     s->ray_offset = run->ray_offset; s->scenario_id = run->scenario_id; s->philox_key = run->philox_key;
     s->n_rays = run->n_rays; s->weight_mode = run->weight_mode;

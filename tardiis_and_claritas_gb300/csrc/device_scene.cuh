@@ -38,6 +38,9 @@ struct DevScene {
     const float2* node_mu;      // [nr*nz] (geometric, wave)
     const int2* node_alias;     // [2][nr*nz][n_bins] (probability bits, alias bin)
     float node_major;           // max over nodes of the summed rate: a majorant of the interpolated field
+    // FP32 casts of transport scalars the water step reads every flight (round-to-nearest casts of the
+    // FP64 values, identical to casting on the device): mu_channels[0], [1], [7] and sed_major[0], [1]
+    float mu_geom_f, mu_wave_f, coherent_f, sed_major_f[2];
     int32_t n_bins, nt, n_radial, grid_nr, grid_nz, any_moment;
     float grid_zmax;
     // run description of this scenario

@@ -106,6 +106,7 @@ struct ParticleBuffers {
     int2* node_alias = nullptr;    // [2][nr*nz][n]
     float* node_major = nullptr;   // [1]
     float node_major_host = 0.0f;
+    double muscal_host[8] = {0}, sed_major_host[4] = {0};  // host copies of muscal and sed_major
 };
 
 // Enqueue the whole precompute on `stream`. Host inputs are copied in; error codes land in pb.err.

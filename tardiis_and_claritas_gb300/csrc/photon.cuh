@@ -414,15 +414,20 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
         if (!isfinite(vx) || !isfinite(vy) || !isfinite(vz)) { r.pf = OP_NONFINITE_DIRECTION; r.pfs = OS_NONFINITE_DIRECTION; r.st = 4; res = WE_ENDED; break; }
         float zsurf_here = o_surface_z(x, y, ZMEAN, RIN, FSM, DH, CORE);
         if (z <= ZMIN || z >= zsurf_here) { r.st = 2; res = WE_ENDED; break; }
-        double rr2w = (double)x * (double)x + (double)y * (double)y, ri2w = (double)RIN * (double)RIN;
-        double water_tol = 8.0 * 1.1920928955078125e-7 * ri2w;
-        if (rr2w > ri2w + water_tol) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break; }
-        const float MU_GEOM = (float)D.mu_channels[0], MU_WAVE = (float)D.mu_channels[1];
+        bool outside;
+        if constexpr (kCounterStream<S>) {
+            outside = x * x + y * y > RIN * RIN * (1.0f + 8.0f * 1.1920928955078125e-7f);
+        } else {
+            double rr2w = (double)x * (double)x + (double)y * (double)y, ri2w = (double)RIN * (double)RIN;
+            double water_tol = 8.0 * 1.1920928955078125e-7 * ri2w;
+            outside = rr2w > ri2w + water_tol;
+        }
+        if (outside) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break; }
+        const float MU_GEOM = D.mu_geom_f, MU_WAVE = D.mu_wave_f;
         float MU_TOTAL = MU_GEOM + MU_WAVE;
         // counter-based streams with node tables use the node-sum majorant (never above the reference's)
         const bool node_fast = kCounterStream<S> && TM == 3 && D.node_alias != nullptr;
-        float MU_TRACK = (TM == 0) ? MU_TOTAL : node_fast ? D.node_major
-                                                          : ((float)D.sed_major[0] + (float)D.sed_major[1]);
+        float MU_TRACK = (TM == 0) ? MU_TOTAL : node_fast ? D.node_major : (D.sed_major_f[0] + D.sed_major_f[1]);
         int axial_top = 0, axial_bottom = 0, do_particle = 0;
         float travel = 0.0f;
         bool lazy = false;
@@ -462,10 +467,17 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
         }
         x += travel * vx; y += travel * vy; z += travel * vz;
         r.wp += travel;
-        double endpoint_r2 = (double)x * x + (double)y * y;
-        if (do_particle && (endpoint_r2 > ri2w + water_tol || z < ZMIN - CLR_EPS_F ||
-                            z > o_surface_z(x, y, ZMEAN, RIN, FSM, DH, CORE) + CLR_EPS_F)) {
-            r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break;
+        if (do_particle && !lazy) {
+            bool end_out;
+            if constexpr (kCounterStream<S>) {
+                end_out = x * x + y * y > RIN * RIN * (1.0f + 8.0f * 1.1920928955078125e-7f);
+            } else {
+                double endpoint_r2 = (double)x * x + (double)y * y, ri2w = (double)RIN * (double)RIN;
+                end_out = endpoint_r2 > ri2w + 8.0 * 1.1920928955078125e-7 * ri2w;
+            }
+            if (end_out || z < ZMIN - CLR_EPS_F || z > o_surface_z(x, y, ZMEAN, RIN, FSM, DH, CORE) + CLR_EPS_F) {
+                r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break;
+            }
         }
         if (do_particle) {
             const o_field F = make_field(D);
@@ -504,7 +516,7 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
             r.ic++;
             const float vinx = vx, viny = vy, vinz = vz;
             const int COND = (P.event_model == 4 || P.event_model == 5);
-            const float COHERENT = fminf(fmaxf((float)D.mu_channels[7], 0.0f), 1.0f);
+            const float COHERENT = fminf(fmaxf(D.coherent_f, 0.0f), 1.0f);
             int use_wave = (LOCAL_WAVE > 0.0f && uniform(st) * LOCAL_TOTAL >= LOCAL_GEOM);
             int sel = -1;
             if (COND) {
@@ -598,7 +610,7 @@ __device__ __forceinline__ bool water_cond(const DevScene& D, Ray& r, S* opt, un
     const clr_scene_params& P = D.P;
     float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
     const float vinx = vx, viny = vy, vinz = vz;
-    const float COHERENT = fminf(fmaxf((float)D.mu_channels[7], 0.0f), 1.0f);
+    const float COHERENT = fminf(fmaxf(D.coherent_f, 0.0f), 1.0f);
     bool ended = false;
     Hist h;
     conditional_interaction(opt, &h, sel, D.qsca[sel], D.qext[sel], P.n_water, D.pn[sel], D.pk[sel], P.wavelength,
@@ -628,16 +640,24 @@ __device__ __forceinline__ bool water_geom(const DevScene& D, Ray& r, S* opt, un
     float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
     const float vinx = vx, viny = vy, vinz = vz;
     const int COND = (P.event_model == 4 || P.event_model == 5);
-    const float COHERENT = fminf(fmaxf((float)D.mu_channels[7], 0.0f), 1.0f);
+    const float COHERENT = fminf(fmaxf(D.coherent_f, 0.0f), 1.0f);
     bool ended = false;
     do {
         float prad = D.prad[pidx];
         float srho, sphi, sgx, sgy, sgz;
         o_sphere_geometry(opt, prad, x, y, z, vx, vy, vz, &srho, &sphi, &sgx, &sgy, &sgz);
-        double dscx = (double)x - (double)prad * (double)sgx;
-        double dscy = (double)y - (double)prad * (double)sgy;
-        double dscz = (double)z - (double)prad * (double)sgz;
-        int accessible = o_sphere_accessible(dscx, dscy, dscz, (double)prad, RIN, ZMIN, ZMEAN, FSM, DH, CORE);
+        double dscx = 0.0, dscy = 0.0, dscz = 0.0;
+        float fcx = 0.0f, fcy = 0.0f, fcz = 0.0f;
+        int accessible;
+        if constexpr (kCounterStream<S>) {
+            fcx = x - prad * sgx; fcy = y - prad * sgy; fcz = z - prad * sgz;
+            accessible = f_sphere_accessible(fcx, fcy, fcz, prad, RIN, ZMIN, ZMEAN, FSM, DH, CORE);
+        } else {
+            dscx = (double)x - (double)prad * (double)sgx;
+            dscy = (double)y - (double)prad * (double)sgy;
+            dscz = (double)z - (double)prad * (double)sgz;
+            accessible = o_sphere_accessible(dscx, dscy, dscz, (double)prad, RIN, ZMIN, ZMEAN, FSM, DH, CORE);
+        }
         if (!accessible && COND) {
             atomicAdd(&cstats[2], 1ull);
             Hist h;
@@ -657,7 +677,13 @@ __device__ __forceinline__ bool water_geom(const DevScene& D, Ray& r, S* opt, un
             if (!accessible) { r.ic--; r.gic--; r.nulls++; break; }
             float ipath = 0.0f;
             int ppc = 0, pps = 0, pmb = 0, pmo = 0;
-            int ps = o_sphere_sampled(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, prad,
+            int ps;
+            if constexpr (kCounterStream<S>)
+                ps = f_sphere_sampled(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, prad,
+                                      P.max_particle_bounces, sgx, sgy, sgz, fcx, fcy, fcz, &x, &y, &z, &vx, &vy,
+                                      &vz, &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
+            else
+                ps = o_sphere_sampled(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, prad,
                                       P.max_particle_bounces, sgx, sgy, sgz, dscx, dscy, dscz, &x, &y, &z, &vx, &vy,
                                       &vz, &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
             if (ps == 2) { r.st = 5; ended = true; break; }

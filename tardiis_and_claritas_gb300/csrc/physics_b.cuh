@@ -539,6 +539,119 @@ __device__ int o_sphere_sampled(S* s, float n_medium, float n_particle, float k_
     *pf = OP_OTHER; *pfs = OS_NONE;
     return 0;
 }
+/* FP32 versions of the sphere accessibility test and chord walk for the counter-based stream: the
+ * same tests in the same order; the chord tolerance is scaled from DBL_EPS to FLT_EPS (chords are
+ * relative to the sphere centre, so their relative accuracy is FP32's whatever the cell size) and
+ * the accessibility test asks for a clearance of a few FP32 ulps instead of allowing an overlap. */
+__device__ __forceinline__ int f_sphere_accessible(float cx, float cy, float cz, float radius, float Rin, float Zmin,
+                                                   float Zmean, int model, float dh, float core) {
+    const float rc = hypotf(cx, cy), rr = radius;
+    const float wall = (Rin - rc) - rr;
+    const float bottom = cz - rr - Zmin;
+    const float rmin = fmaxf(0.0f, rc - rr);
+    float zsurf = Zmean;
+    if (model != 0 && dh > 0.0f) {
+        const float q = rmin * rmin, R2 = Rin * Rin;
+        if (model == 1) {
+            zsurf = Zmean + dh * (q / R2 - 0.5f);
+        } else {
+            const float a2 = core * core;
+            const float H = dh * (a2 + R2) / R2;
+            const float hbar = H * (1.0f - (a2 / R2) * log1pf(R2 / a2));
+            zsurf = Zmean - hbar + H * q / (a2 + q);
+        }
+    }
+    const float top = zsurf - (cz + rr);
+    // The FP64 test accepts spheres within ~1e-15 m of the boundary. In FP32 the clearances carry
+    // errors of a few ulps of the cell coordinates, so a sphere must clear every boundary by four of
+    // them: a borderline sphere is rejected rather than allowed to intrude, and exit points on it
+    // stay inside the water.
+    const float scale = fmaxf(fmaxf(fabsf(Rin), fabsf(cz)), fmaxf(rr, 1.0e-6f));
+    const float tol = 4.0f * 1.1920928955078125e-7f * scale;
+    return (wall >= tol && bottom >= tol && top >= tol) ? 1 : 0;
+}
+template <class S>
+__device__ int f_sphere_sampled(S* s, float n_medium, float n_particle, float k_particle, float wavelength,
+                                float rough_alpha, float radius, int max_bounces, float gnx, float gny, float gnz,
+                                float cx, float cy, float cz, float* x, float* y, float* z, float* vx, float* vy,
+                                float* vz, float* internal_path, o_pcount* pc, int* pf, int* pfs, int* macro,
+                                int* micro) {
+    const float FEPS = 1.1920928955078125e-7f;
+    *pf = OP_OK; *pfs = OS_NONE; *macro = 0; *micro = 0;
+    if (radius <= 0.0f) return 1;
+    const int WD = 4096;
+    int top = 1, order = 0, mfc = OF_NONE;
+    int ms = o_micro_walk(s, rough_alpha, WD, gnx, gny, gnz, n_medium, 0.0f, n_particle, k_particle, vx, vy, vz, &top,
+                          &order, &mfc);
+    *micro = order;
+    if (ms != OM_ESCAPE) { *pf = (ms == OM_WATCHDOG) ? OP_MICRO_WATCHDOG : OP_MICRO_NUMERICAL; *pfs = mfc; return 0; }
+    if (top) { pc->reflections++; pc->entry_reflections++; return 1; }
+    if (o_dot(*vx, *vy, *vz, gnx, gny, gnz) >= 0.0f) { *pf = OP_MACRO_GEOMETRY; *pfs = OS_SPHERE_ENTRY_SIDE; return 0; }
+    const float rr = radius, rr2 = rr * rr;
+    float qx = rr * gnx, qy = rr * gny, qz = rr * gnz;
+    const float qn0 = sqrtf(qx * qx + qy * qy + qz * qz);
+    if (!(qn0 > 0.0f) || !isfinite(qn0)) { *pf = OP_MACRO_GEOMETRY; *pfs = OS_SPHERE_CHORD; return 0; }
+    qx *= rr / qn0; qy *= rr / qn0; qz *= rr / qn0;
+    const float alpha_abs = (wavelength > 0.0f && k_particle > 0.0f) ? (4.0f * CLR_PI_F * k_particle / wavelength) : 0.0f;
+    for (int bounce = 0; bounce <= max_bounces; ++bounce) {
+        *macro = bounce;
+        const float dvx = *vx, dvy = *vy, dvz = *vz;
+        const float A = dvx * dvx + dvy * dvy + dvz * dvz;
+        const float q2 = qx * qx + qy * qy + qz * qz;
+        if (!(A > 0.0f) || !isfinite(A) || !isfinite(q2)) { *pf = OP_MACRO_GEOMETRY; *pfs = OS_SPHERE_CHORD; return 0; }
+        const float qnorm = sqrtf(q2);
+        if (!(qnorm > 0.0f) || !isfinite(qnorm)) { *pf = OP_MACRO_GEOMETRY; *pfs = OS_SPHERE_CHORD; return 0; }
+        const float qproj = rr / qnorm;
+        qx *= qproj; qy *= qproj; qz *= qproj;
+        const float B = qx * dvx + qy * dvy + qz * dvz;
+        if (!(B < 0.0f) || !isfinite(B)) { *pf = OP_MACRO_GEOMETRY; *pfs = OS_SPHERE_INTERNAL_SIDE; return 0; }
+        const float chord = -2.0f * B / A;
+        if (!(chord > 0.0f) || !isfinite(chord)) { *pf = OP_MACRO_GEOMETRY; *pfs = OS_SPHERE_CHORD; return 0; }
+        const float tqx = qx + chord * dvx, tqy = qy + chord * dvy, tqz = qz + chord * dvz;
+        const float arrival = tqx * dvx + tqy * dvy + tqz * dvz;
+        const float tq2 = tqx * tqx + tqy * tqy + tqz * tqz;
+        const float err = fabsf(tq2 - rr2);
+        const float tol = 512.0f * FEPS * fmaxf(rr2, 1.0e-30f);
+        if (!(arrival > 0.0f) || !isfinite(arrival) || !isfinite(tq2) || err > tol) {
+            *pf = OP_MACRO_GEOMETRY; *pfs = OS_SPHERE_CHORD; return 0;
+        }
+        if (alpha_abs > 0.0f) {
+            const float dist = -logf((float)open_uniform(s)) / alpha_abs;
+            if (dist < chord) {
+                qx += dist * dvx; qy += dist * dvy; qz += dist * dvz;
+                *x = cx + qx; *y = cy + qy; *z = cz + qz;
+                *internal_path += dist;
+                pc->absorptions++;
+                return 2;
+            }
+        }
+        qx = tqx; qy = tqy; qz = tqz;
+        *internal_path += chord;
+        const float qn = sqrtf(qx * qx + qy * qy + qz * qz);
+        if (!(qn > 0.0f) || !isfinite(qn)) { *pf = OP_MACRO_GEOMETRY; *pfs = OS_SPHERE_CHORD; return 0; }
+        const float proj = rr / qn;
+        qx *= proj; qy *= proj; qz *= proj;
+        *x = cx + qx; *y = cy + qy; *z = cz + qz;
+        float nox = qx / rr, noy = qy / rr, noz = qz / rr;
+        o_normalize(&nox, &noy, &noz);
+        const float bx = -nox, by = -noy, bz = -noz;
+        top = 1; order = 0; mfc = OF_NONE;
+        ms = o_micro_walk(s, rough_alpha, WD, bx, by, bz, n_particle, k_particle, n_medium, 0.0f, vx, vy, vz, &top,
+                          &order, &mfc);
+        *micro = order;
+        if (ms != OM_ESCAPE) { *pf = (ms == OM_WATCHDOG) ? OP_MICRO_WATCHDOG : OP_MICRO_NUMERICAL; *pfs = mfc; return 0; }
+        if (!top) {
+            if (o_dot(*vx, *vy, *vz, nox, noy, noz) <= 0.0f) { *pf = OP_MACRO_GEOMETRY; *pfs = OS_SPHERE_EXIT_SIDE; return 0; }
+            return 1;
+        }
+        if (o_dot(*vx, *vy, *vz, nox, noy, noz) >= 0.0f) { *pf = OP_MACRO_GEOMETRY; *pfs = OS_SPHERE_INTERNAL_SIDE; return 0; }
+        pc->reflections++;
+        pc->internal_reflections++;
+        if (bounce == max_bounces) { *pf = OP_MACRO_BOUNCE_LIMIT; *pfs = OS_SPHERE_BOUNCE_LIMIT; return 0; }
+    }
+    *pf = OP_OTHER; *pfs = OS_NONE;
+    return 0;
+}
 /* sphere interaction from a fresh placement at the origin (:2601-2612) */
 template <class S>
 __device__ int o_sphere_fresh(S* s, float n_medium, float n_particle, float k_particle, float wavelength,
@@ -879,6 +992,65 @@ __device__ __forceinline__ int o_tir_ci(double ci, double n1, double n2) {
     double st = (n1 / n2) * sqrt(fmax(0.0, 1.0 - ci * ci));
     return st >= 1.0;
 }
+/* ---- FP32 versions for the counter-based (production) stream ----
+ * Same surfaces, same order of tests and the same support tolerance (already stated in FP32
+ * epsilons); roots by the cancellation-free quadratic formula in FP32. Positions are FP32 in the
+ * reference as well; the FP64 roots above are what the parity mode runs. */
+__device__ __forceinline__ int f_cyl_roots(float x, float y, float vx, float vy, float R, float* t0, float* t1) {
+    *t0 = CLR_INF_F; *t1 = CLR_INF_F;
+    const float a = vx * vx + vy * vy;
+    if (!(a > 1e-30f) || !isfinite(a)) return 0;
+    const float b = x * vx + y * vy, c = (x * x + y * y) - R * R;
+    float d = b * b - a * c;
+    const float dtol = 16.0f * 1.1920928955078125e-7f * (fabsf(b * b) + fabsf(a * c) + 1e-30f);
+    if (d < 0.0f) { if (d >= -dtol) d = 0.0f; else return 0; }
+    const float sd = sqrtf(fmaxf(d, 0.0f)), q = -b - copysignf(sd, b);
+    const float r0 = (fabsf(q) > 1e-30f) ? q / a : (-b - sd) / a;
+    const float r1 = (fabsf(q) > 1e-30f) ? c / q : (-b + sd) / a;
+    float a0 = CLR_INF_F, a1 = CLR_INF_F;
+    if (r0 > 0.0f && isfinite(r0)) a0 = r0;
+    if (r1 > 0.0f && isfinite(r1)) { if (r1 < a0) { a1 = a0; a0 = r1; } else a1 = r1; }
+    *t0 = a0; *t1 = a1;
+    return (a0 < CLR_INF_F) + (a1 < CLR_INF_F);
+}
+__device__ __forceinline__ void f_consider(float t, int surf, float* best, int* best_surf) {
+    if (t > 0.0f && isfinite(t) && t < *best) { *best = t; *best_surf = surf; }
+}
+__device__ __forceinline__ int f_acrylic_next(float x, float y, float z, float vx, float vy, float vz, float Rin,
+                                              float Rout, float Zmin, float Zlow, float Ztop, float* t_out) {
+    float best = CLR_INF_F;
+    int surf = 0;
+    const float tol = (float)o_support_tol(Rin, Rout, Zmin, Zlow, Ztop);
+    float r0, r1;
+    f_cyl_roots(x, y, vx, vy, Rin, &r0, &r1);
+    if (r0 < CLR_INF_F) { const float zh = z + r0 * vz; if (zh >= Zmin - tol && zh <= Ztop + tol) f_consider(r0, 1, &best, &surf); }
+    if (r1 < CLR_INF_F) { const float zh = z + r1 * vz; if (zh >= Zmin - tol && zh <= Ztop + tol) f_consider(r1, 1, &best, &surf); }
+    f_cyl_roots(x, y, vx, vy, Rout, &r0, &r1);
+    if (r0 < CLR_INF_F) { const float zh = z + r0 * vz; if (zh >= Zlow - tol && zh <= Ztop + tol) f_consider(r0, 2, &best, &surf); }
+    if (r1 < CLR_INF_F) { const float zh = z + r1 * vz; if (zh >= Zlow - tol && zh <= Ztop + tol) f_consider(r1, 2, &best, &surf); }
+    if (vz < 0.0f) {
+        const float t = (Zlow - z) / vz;
+        if (t > 0.0f && isfinite(t)) {
+            const float rr = hypotf(x + t * vx, y + t * vy);
+            if (rr <= Rout + tol) f_consider(t, 3, &best, &surf);
+        }
+    }
+    if (vz > 0.0f) {
+        const float t = (Ztop - z) / vz;
+        if (t > 0.0f && isfinite(t)) {
+            const float rr = hypotf(x + t * vx, y + t * vy);
+            if (rr >= Rin - tol && rr <= Rout + tol) f_consider(t, 4, &best, &surf);
+        }
+        const float ta = (Zmin - z) / vz;
+        if (ta > 0.0f && isfinite(ta)) {
+            const float rr = hypotf(x + ta * vx, y + ta * vy);
+            if (rr < Rin - tol) f_consider(ta, 5, &best, &surf);
+        }
+    }
+    *t_out = best;
+    return surf;
+}
+
 /* conserved-orbit trapped-TIR classifier (:3089-3138) */
 __device__ __noinline__ int o_trapped(float x, float y, float z, float vx, float vy, float vz, float n_water, float n_acrylic,
                      float n_air, float n_bottom_ext, float Rin, float Rout) {
@@ -956,12 +1128,22 @@ __device__ __noinline__ int o_acrylic_run(S* s, const o_cell* C, float n_side_ai
     const float Rin = C->Rin, Rout = C->Rout, Ztop = C->Ztop;
     const int it0 = as->it;
     const int end = (budget > 0 && cap - it0 > budget) ? it0 + budget : cap;
+    int surf_next = 0;
     for (int it = it0; it < end; ++it) {
         *out_bounces = it;
-        double td = 1.0e300;
-        int surf = o_acrylic_next(*x, *y, *z, *vx, *vy, *vz, Rin, Rout, Zmin, Zlow, Ztop, &td);
-        if (!surf || !(td > 0.0) || !isfinite(td) || td >= 1.0e299) { *sub = OS_ACRYLIC_NO_INTERSECTION; return 0; }
-        float t = (float)td;
+        float t;
+        if constexpr (kCounterStream<S>) {
+            int surf_f = f_acrylic_next(*x, *y, *z, *vx, *vy, *vz, Rin, Rout, Zmin, Zlow, Ztop, &t);
+            if (!surf_f || !(t > 0.0f) || !isfinite(t) || t >= CLR_INF_F) { *sub = OS_ACRYLIC_NO_INTERSECTION; return 0; }
+            surf_next = surf_f;
+        } else {
+            double td = 1.0e300;
+            int surf_d = o_acrylic_next(*x, *y, *z, *vx, *vy, *vz, Rin, Rout, Zmin, Zlow, Ztop, &td);
+            if (!surf_d || !(td > 0.0) || !isfinite(td) || td >= 1.0e299) { *sub = OS_ACRYLIC_NO_INTERSECTION; return 0; }
+            t = (float)td;
+            surf_next = surf_d;
+        }
+        const int surf = surf_next;
         float px = *x, py = *y, pz = *z, pvx = *vx, pvy = *vy, pvz = *vz;
         *x += t * (*vx); *y += t * (*vy); *z += t * (*vz);
         *acrylic_path += t;
