@@ -44,7 +44,9 @@ struct SlotMeta {
     int32_t pidx;   // size bin of a pending particle event
     int32_t acr_caller;                       // pending acrylic traversal: which handler started it
     int32_t acr_it, acr_stuck, acr_last;      // and its loop state
-    int32_t pad;
+    int32_t cond_kind;                        // pending conditional closure: which event it completes
+    int32_t cond_started, cond_trial, cond_target;  // and its loop state
+    int32_t pad[2];
 };
 
 struct WaveCtl {

@@ -60,27 +60,47 @@ struct Hist {
     int status, channel, macro, micro, failure, subcode;
 };
 
+// Loop state of a closure, so that its trials can run in bounded pieces (a closure can take 16384).
+struct CondState {
+    int started;  // setup (argument checks, the absorbed/scattered target draw) done
+    int trial;    // next trial
+    int target;   // pre-drawn target outcome: 1 absorbed, 0 scattered
+};
+__device__ __forceinline__ CondState cond_start() {
+    CondState c = {0, 0, 0};
+    return c;
+}
+
+// Runs the closure from *cs for at most `budget` trials (0: to its end). Returns 1 with *out set when
+// the closure finished, 0 when the budget ran out first (state in *cs).
 template <class S>
-__device__ __forceinline__ void conditional_body(
+__device__ __forceinline__ int conditional_body(
     S* s, Hist* out, int pidx, double qs, double qe, float nm, float nr, float ki, float wl, float rough,
     float radius, float aspect, int orientation, float kappa, int max_bounces, float coherent, const float* cdf,
     const float* theta, int nt, float x, float y, float z, float vx, float vy, float vz, float rin, float zmin,
-    float zmean, int surface, float delta, float core, int max_trials, unsigned long long* stats) {
+    float zmean, int surface, float delta, float core, int max_trials, unsigned long long* stats, CondState* cs,
+    int budget) {
     Hist h;
     memset(&h, 0, sizeof h);
     h.failure = OP_OTHER; h.subcode = 9002;
     double tol = 1e-10 * fmax(1.0, fmax(fabs(qs), fabs(qe)));
-    if (max_trials == 0) { h.subcode = 9001; ++stats[9]; *out = h; return; }
-    if (!isfinite(qs) || !isfinite(qe) || qe <= 0.0 || qs < -tol || qs > qe + tol || max_trials < 1) { ++stats[8]; *out = h; return; }
     double albedo = (ki == 0.0f && fabs(qe - qs) <= tol) ? 1.0 : fmin(fmax(qs / qe, 0.0), 1.0);
-    double pabs = (ki == 0.0f && fabs(qe - qs) <= tol) ? 0.0 : fmin(fmax((qe - qs) / qe, 0.0), 1.0);
-    const double MINP = 2.3283064365386962890625e-10;
-    if ((ki > 0.0f && (pabs <= 0.0 || albedo >= 1.0)) || (albedo > 0.0 && albedo < MINP) || (pabs > 0.0 && pabs < MINP)) {
-        h.subcode = 9003; ++stats[8]; *out = h; return;
+    if (!cs->started) {
+        if (max_trials == 0) { h.subcode = 9001; ++stats[9]; *out = h; return 1; }
+        if (!isfinite(qs) || !isfinite(qe) || qe <= 0.0 || qs < -tol || qs > qe + tol || max_trials < 1) { ++stats[8]; *out = h; return 1; }
+        double pabs = (ki == 0.0f && fabs(qe - qs) <= tol) ? 0.0 : fmin(fmax((qe - qs) / qe, 0.0), 1.0);
+        const double MINP = 2.3283064365386962890625e-10;
+        if ((ki > 0.0f && (pabs <= 0.0 || albedo >= 1.0)) || (albedo > 0.0 && albedo < MINP) || (pabs > 0.0 && pabs < MINP)) {
+            h.subcode = 9003; ++stats[8]; *out = h; return 1;
+        }
+        cs->target = (albedo < 1.0 && uniform53(s) >= albedo);
+        cs->started = 1;
+        cs->trial = 0;
     }
-    int target_absorbed = (albedo < 1.0 && uniform53(s) >= albedo);
+    const int target_absorbed = cs->target;
     double wave = qs > 0.0 ? fmax(qs - 1.0, 0.0) / qs : 0.0;
-    for (int trial = 0; trial < max_trials; ++trial) {
+    const int end = (budget > 0 && max_trials - cs->trial > budget) ? cs->trial + budget : max_trials;
+    for (int trial = cs->trial; trial < end; ++trial) {
         ++stats[0];
         memset(&h, 0, sizeof h);
         h.x = x; h.y = y; h.z = z; h.vx = vx; h.vy = vy; h.vz = vz;
@@ -97,41 +117,54 @@ __device__ __forceinline__ void conditional_body(
         } else {
             float rho, phi, gx, gy, gz;
             o_sphere_geometry(s, radius, x, y, z, vx, vy, vz, &rho, &phi, &gx, &gy, &gz);
-            double dcx = (double)x - (double)radius * gx, dcy = (double)y - (double)radius * gy,
-                   dcz = (double)z - (double)radius * gz;
-            if (!o_sphere_accessible(dcx, dcy, dcz, radius, rin, zmin, zmean, surface, delta, core)) { ++stats[2]; continue; }
-            h.status = o_sphere_sampled(s, nm, nr, ki, wl, rough, radius, max_bounces, gx, gy, gz, dcx, dcy, dcz, &h.x,
-                                        &h.y, &h.z, &h.vx, &h.vy, &h.vz, &h.path, &h.pc, &h.failure, &h.subcode,
-                                        &h.macro, &h.micro);
+            if constexpr (kCounterStream<S>) {
+                const float fcx = x - radius * gx, fcy = y - radius * gy, fcz = z - radius * gz;
+                if (!f_sphere_accessible(fcx, fcy, fcz, radius, rin, zmin, zmean, surface, delta, core)) { ++stats[2]; continue; }
+                h.status = f_sphere_sampled(s, nm, nr, ki, wl, rough, radius, max_bounces, gx, gy, gz, fcx, fcy, fcz,
+                                            &h.x, &h.y, &h.z, &h.vx, &h.vy, &h.vz, &h.path, &h.pc, &h.failure,
+                                            &h.subcode, &h.macro, &h.micro);
+            } else {
+                double dcx = (double)x - (double)radius * gx, dcy = (double)y - (double)radius * gy,
+                       dcz = (double)z - (double)radius * gz;
+                if (!o_sphere_accessible(dcx, dcy, dcz, radius, rin, zmin, zmean, surface, delta, core)) { ++stats[2]; continue; }
+                h.status = o_sphere_sampled(s, nm, nr, ki, wl, rough, radius, max_bounces, gx, gy, gz, dcx, dcy, dcz,
+                                            &h.x, &h.y, &h.z, &h.vx, &h.vy, &h.vz, &h.path, &h.pc, &h.failure,
+                                            &h.subcode, &h.macro, &h.micro);
+            }
         }
-        if (h.status != 1 && h.status != 2) { ++stats[8]; *out = h; return; }
+        if (h.status != 1 && h.status != 2) { ++stats[8]; *out = h; return 1; }
         if ((h.status == 2) != target_absorbed) { ++stats[1]; continue; }
         ++stats[3 + h.channel];
         ++stats[h.status == 2 ? 6 : 7];
         *out = h;
-        return;
+        return 1;
     }
+    if (end < max_trials) { cs->trial = end; return 0; }
     memset(&h, 0, sizeof h);
     h.failure = OP_OTHER; h.subcode = 9001;
     ++stats[9];
     *out = h;
+    return 1;
 }
 
-// The encounter's trial counters are thread-local and merged atomically once, as the
-// reference's conditional_particle_interaction_accumulate does (:4540-4549).
+// The encounter's trial counters are thread-local and merged atomically once per call, as the
+// reference's conditional_particle_interaction_accumulate does once per encounter (:4540-4549);
+// the sums are the same.
 template <class S>
-__device__ __noinline__ void conditional_interaction(
+__device__ __noinline__ int conditional_interaction(
     S* s, Hist* out, int pidx, double qs, double qe, float nm, float nr, float ki, float wl, float rough,
     float radius, float aspect, int orientation, float kappa, int max_bounces, float coherent, const float* cdf,
     const float* theta, int nt, float x, float y, float z, float vx, float vy, float vz, float rin, float zmin,
-    float zmean, int surface, float delta, float core, int max_trials, unsigned long long* gstats) {
+    float zmean, int surface, float delta, float core, int max_trials, unsigned long long* gstats,
+    CondState* cs, int budget) {
     unsigned long long stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    conditional_body(s, out, pidx, qs, qe, nm, nr, ki, wl, rough, radius, aspect, orientation, kappa, max_bounces,
-                     coherent, cdf, theta, nt, x, y, z, vx, vy, vz, rin, zmin, zmean, surface, delta, core, max_trials,
-                     stats);
+    const int done = conditional_body(s, out, pidx, qs, qe, nm, nr, ki, wl, rough, radius, aspect, orientation, kappa,
+                                      max_bounces, coherent, cdf, theta, nt, x, y, z, vx, vy, vz, rin, zmin, zmean,
+                                      surface, delta, core, max_trials, stats, cs, budget);
 #pragma unroll
     for (int i = 0; i < 10; ++i)
         if (stats[i]) atomicAdd(gstats + i, stats[i]);
+    return done;
 }
 
 // Mie two-moment post-outcome angular map (:4459-4476)
@@ -605,43 +638,65 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
 
 // ---- handlers: each completes the iteration its flight part started; true when the history ended ----
 
+// Conditional closures complete either a flight whose bin is absorbing (CK_FLIGHT, :4818-4830) or a
+// geometric event whose sampled sphere does not fit in the water (CK_GEOM, :4890-4905).
+enum : int { CK_FLIGHT = 0, CK_GEOM = 1 };
+
+// Runs (part of) a closure. Returns 0 when the iteration ended with the photon in the water, 1 when the
+// history ended, 2 when the closure continues (state in *cs; with budget 0 it always finishes).
 template <class S>
-__device__ __forceinline__ bool water_cond(const DevScene& D, Ray& r, S* opt, unsigned long long* cstats, int sel) {
+__device__ __forceinline__ int closure_visit(const DevScene& D, Ray& r, S* opt, unsigned long long* cstats, int pidx,
+                                             int kind, CondState* cs, int budget) {
     const clr_scene_params& P = D.P;
     float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
     const float vinx = vx, viny = vy, vinz = vz;
     const float COHERENT = fminf(fmaxf(D.coherent_f, 0.0f), 1.0f);
-    bool ended = false;
     Hist h;
-    conditional_interaction(opt, &h, sel, D.qsca[sel], D.qext[sel], P.n_water, D.pn[sel], D.pk[sel], P.wavelength,
-                            P.rough_alpha, D.prad[sel], P.spheroid_aspect, P.orientation_model, P.orientation_kappa,
-                            P.max_particle_bounces, COHERENT, D.phase_cdf, D.theta, D.nt, x, y, z, vx, vy, vz, P.rin,
-                            P.zmin, P.zmean, P.free_surface_model, P.vortex_delta_h, P.vortex_core_radius,
-                            P.conditional_retries, cstats);
+    const int done = conditional_interaction(
+        opt, &h, pidx, D.qsca[pidx], D.qext[pidx], P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha,
+        D.prad[pidx], P.spheroid_aspect, P.orientation_model, P.orientation_kappa, P.max_particle_bounces, COHERENT,
+        D.phase_cdf, D.theta, D.nt, x, y, z, vx, vy, vz, P.rin, P.zmin, P.zmean, P.free_surface_model,
+        P.vortex_delta_h, P.vortex_core_radius, kind == CK_GEOM ? P.conditional_retries - 1 : P.conditional_retries,
+        cstats, cs, budget);
+    if (!done) return 2;
+    bool ended = false;
     do {
-        if (h.status != 1 && h.status != 2) { r.pf = h.failure ? h.failure : OP_OTHER; r.pfs = h.subcode; r.st = 4; ended = true; break; }
+        if (kind == CK_FLIGHT) {
+            if (h.status != 1 && h.status != 2) { r.pf = h.failure ? h.failure : OP_OTHER; r.pfs = h.subcode; r.st = 4; ended = true; break; }
+        } else {
+            if (h.status != 1) { r.pf = h.failure ? h.failure : OP_OTHER; r.pfs = h.subcode; r.st = 4; ended = true; break; }
+        }
         x = h.x; y = h.y; z = h.z; vx = h.vx; vy = h.vy; vz = h.vz;
         r.pc.reflections += h.pc.reflections; r.pc.entry_reflections += h.pc.entry_reflections;
         r.pc.internal_reflections += h.pc.internal_reflections; r.pc.absorptions += h.pc.absorptions;
+        if (kind == CK_GEOM) r.gic--;
         if (h.channel == 0) r.gic++;
         else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
-        if (h.status == 2) { r.st = 5; ended = true; break; }
-        apply_moment(D, sel, vinx, viny, vinz, &vx, &vy, &vz);
+        if (kind == CK_FLIGHT && h.status == 2) { r.st = 5; ended = true; break; }
+        apply_moment(D, pidx, vinx, viny, vinz, &vx, &vy, &vz);
     } while (false);
     r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
-    return ended;
+    return ended ? 1 : 0;
 }
 
 template <class S>
-__device__ __forceinline__ bool water_geom(const DevScene& D, Ray& r, S* opt, unsigned long long* cstats, int pidx) {
+__device__ __forceinline__ bool water_cond(const DevScene& D, Ray& r, S* opt, unsigned long long* cstats, int sel) {
+    CondState cs = cond_start();
+    return closure_visit(D, r, opt, cstats, sel, CK_FLIGHT, &cs, 0) == 1;
+}
+
+// Geometric event up to the closure: returns 0 (iteration done, photon in water), 1 (history ended) or
+// 3 (the sampled sphere does not fit and the closure completes the event).
+template <class S>
+__device__ __forceinline__ int water_geom_visit(const DevScene& D, Ray& r, S* opt, unsigned long long* cstats,
+                                                int pidx) {
     const clr_scene_params& P = D.P;
     const float RIN = P.rin, ZMIN = P.zmin, ZMEAN = P.zmean, DH = P.vortex_delta_h, CORE = P.vortex_core_radius;
     const int FSM = P.free_surface_model;
     float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
     const float vinx = vx, viny = vy, vinz = vz;
     const int COND = (P.event_model == 4 || P.event_model == 5);
-    const float COHERENT = fminf(fmaxf(D.coherent_f, 0.0f), 1.0f);
-    bool ended = false;
+    int res = 0;
     do {
         float prad = D.prad[pidx];
         float srho, sphi, sgx, sgy, sgz;
@@ -660,40 +715,36 @@ __device__ __forceinline__ bool water_geom(const DevScene& D, Ray& r, S* opt, un
         }
         if (!accessible && COND) {
             atomicAdd(&cstats[2], 1ull);
-            Hist h;
-            conditional_interaction(opt, &h, pidx, D.qsca[pidx], D.qext[pidx], P.n_water, D.pn[pidx], D.pk[pidx],
-                                    P.wavelength, P.rough_alpha, prad, P.spheroid_aspect, P.orientation_model,
-                                    P.orientation_kappa, P.max_particle_bounces, COHERENT, D.phase_cdf, D.theta, D.nt,
-                                    x, y, z, vx, vy, vz, RIN, ZMIN, ZMEAN, FSM, DH, CORE, P.conditional_retries - 1,
-                                    cstats);
-            if (h.status != 1) { r.pf = h.failure ? h.failure : OP_OTHER; r.pfs = h.subcode; r.st = 4; ended = true; break; }
-            x = h.x; y = h.y; z = h.z; vx = h.vx; vy = h.vy; vz = h.vz;
-            r.pc.reflections += h.pc.reflections; r.pc.entry_reflections += h.pc.entry_reflections;
-            r.pc.internal_reflections += h.pc.internal_reflections; r.pc.absorptions += h.pc.absorptions;
-            r.gic--;
-            if (h.channel == 0) r.gic++;
-            else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
-        } else {
-            if (!accessible) { r.ic--; r.gic--; r.nulls++; break; }
-            float ipath = 0.0f;
-            int ppc = 0, pps = 0, pmb = 0, pmo = 0;
-            int ps;
-            if constexpr (kCounterStream<S>)
-                ps = f_sphere_sampled(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, prad,
-                                      P.max_particle_bounces, sgx, sgy, sgz, fcx, fcy, fcz, &x, &y, &z, &vx, &vy,
-                                      &vz, &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
-            else
-                ps = o_sphere_sampled(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, prad,
-                                      P.max_particle_bounces, sgx, sgy, sgz, dscx, dscy, dscz, &x, &y, &z, &vx, &vy,
-                                      &vz, &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
-            if (ps == 2) { r.st = 5; ended = true; break; }
-            if (ps != 1) { if (COND) atomicAdd(&cstats[8], 1ull); r.pf = ppc ? ppc : OP_OTHER; r.pfs = pps; r.st = 4; ended = true; break; }
-            if (COND) { atomicAdd(&cstats[3], 1ull); atomicAdd(&cstats[7], 1ull); }
+            res = 3;
+            break;
         }
+        if (!accessible) { r.ic--; r.gic--; r.nulls++; break; }
+        float ipath = 0.0f;
+        int ppc = 0, pps = 0, pmb = 0, pmo = 0;
+        int ps;
+        if constexpr (kCounterStream<S>)
+            ps = f_sphere_sampled(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, prad,
+                                  P.max_particle_bounces, sgx, sgy, sgz, fcx, fcy, fcz, &x, &y, &z, &vx, &vy, &vz,
+                                  &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
+        else
+            ps = o_sphere_sampled(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, prad,
+                                  P.max_particle_bounces, sgx, sgy, sgz, dscx, dscy, dscz, &x, &y, &z, &vx, &vy, &vz,
+                                  &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
+        if (ps == 2) { r.st = 5; res = 1; break; }
+        if (ps != 1) { if (COND) atomicAdd(&cstats[8], 1ull); r.pf = ppc ? ppc : OP_OTHER; r.pfs = pps; r.st = 4; res = 1; break; }
+        if (COND) { atomicAdd(&cstats[3], 1ull); atomicAdd(&cstats[7], 1ull); }
         apply_moment(D, pidx, vinx, viny, vinz, &vx, &vy, &vz);
     } while (false);
     r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
-    return ended;
+    return res;
+}
+
+template <class S>
+__device__ __forceinline__ bool water_geom(const DevScene& D, Ray& r, S* opt, unsigned long long* cstats, int pidx) {
+    const int g = water_geom_visit(D, r, opt, cstats, pidx);
+    if (g != 3) return g == 1;
+    CondState cs = cond_start();
+    return closure_visit(D, r, opt, cstats, pidx, CK_GEOM, &cs, 0) == 1;
 }
 
 template <class S>

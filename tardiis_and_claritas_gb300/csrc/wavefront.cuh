@@ -10,7 +10,8 @@
 //   ENTRY  air gap, outer wall, acrylic, headspace               -> FLIGHT or FIN
 //   FLIGHT water flights with the cheap outcomes inline (null collisions, coherent Mie scattering,
 //          Fresnel reflections at the surface and the wall)     -> an event queue, FIN, or FLIGHT
-//   COND, GEOM, MORPH   particle events (conditional closure, geometric sphere, spheroid)
+//   COND, GEOM, MORPH   particle events (conditional closure, geometric sphere, spheroid); a long
+//          closure runs in bounded pieces through the COND queue
 //   TOP, BOTTOM, SIDE   transmission into the headspace, the bottom disc, the acrylic wall
 //                                                                -> FLIGHT, FIN or ACRYL
 //   ACRYL  the next bounded piece of a long traversal of the acrylic solid
@@ -54,6 +55,10 @@ __host__ __device__ constexpr int stage_min_blocks(int q) { return q == WQ_COND 
 // acrylic bounces per visit of SIDE, BOTTOM and ACRYL (a traversal can take 16384), all of them
 // once every photon has been drawn
 constexpr int kAcrBudget = 256;
+// closure trials per visit: a few inline in GEOM (most closures end in one or two), more per COND visit
+// (a closure can take 16384 trials, e.g. when no sampled sphere fits)
+constexpr int kCondInline = 8;
+constexpr int kCondBudget = 1024;
 
 template <class Mode>
 struct WavePool {
@@ -215,7 +220,9 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
                         pool.lane[slot] = L;
                         SlotMeta m;
                         m.gid = gid; m.sid = sid; m.rid = rid; m.pidx = -1;
-                        m.acr_caller = 0; m.acr_it = 0; m.acr_stuck = 0; m.acr_last = -1; m.pad = 0;
+                        m.acr_caller = 0; m.acr_it = 0; m.acr_stuck = 0; m.acr_last = -1;
+                        m.cond_kind = 0; m.cond_started = 0; m.cond_trial = 0; m.cond_target = 0;
+                        m.pad[0] = m.pad[1] = 0;
                         pool.meta[slot] = m;
                         filled = true;
                     }
@@ -246,7 +253,9 @@ __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevSce
             m.pidx = pidx;
             switch (e) {
                 case WE_ENDED: return WQ_FIN;
-                case WE_COND: return WQ_COND;
+                case WE_COND:
+                    m.cond_kind = CK_FLIGHT; m.cond_started = 0; m.cond_trial = 0; m.cond_target = 0;
+                    return WQ_COND;
                 case WE_GEOM: return WQ_GEOM;
                 case WE_MORPH: return WQ_MORPH;
                 case WE_TOP: return WQ_TOP;
@@ -255,10 +264,24 @@ __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevSce
             }
         }
         return WQ_FLIGHT;
-    } else if constexpr (Q == WQ_COND) {
-        return water_cond(D, r, L.optics(), cstats, m.pidx) ? WQ_FIN : WQ_FLIGHT;
-    } else if constexpr (Q == WQ_GEOM) {
-        return water_geom(D, r, L.optics(), cstats, m.pidx) ? WQ_FIN : WQ_FLIGHT;
+    } else if constexpr (Q == WQ_COND || Q == WQ_GEOM) {
+        CondState cs;
+        int v;
+        if constexpr (Q == WQ_GEOM) {
+            v = water_geom_visit(D, r, L.optics(), cstats, m.pidx);
+            if (v != 3) return v ? WQ_FIN : WQ_FLIGHT;
+            m.cond_kind = CK_GEOM;
+            cs = cond_start();
+            v = closure_visit(D, r, L.optics(), cstats, m.pidx, CK_GEOM, &cs, kCondInline);
+        } else {
+            cs.started = m.cond_started; cs.trial = m.cond_trial; cs.target = m.cond_target;
+            v = closure_visit(D, r, L.optics(), cstats, m.pidx, m.cond_kind, &cs, kCondBudget);
+        }
+        if (v == 2) {
+            m.cond_started = cs.started; m.cond_trial = cs.trial; m.cond_target = cs.target;
+            return WQ_COND;
+        }
+        return v ? WQ_FIN : WQ_FLIGHT;
     } else if constexpr (Q == WQ_MORPH) {
         return water_morph(D, r, L.optics(), cstats, m.pidx) ? WQ_FIN : WQ_FLIGHT;
     } else if constexpr (Q == WQ_TOP) {
@@ -313,8 +336,7 @@ __global__ void __launch_bounds__(kWaveThreads, stage_min_blocks(Q)) wave_stage_
             dest = wave_stage_body<Mode, Q>(w, D, r, L, m, cstats);
             pool.ray[slot] = r;
             pool.lane[slot] = L;
-            if (Q == WQ_FLIGHT) pool.meta[slot].pidx = m.pidx;
-            if ((Q == WQ_SIDE || Q == WQ_BOTTOM || Q == WQ_ACRYL) && dest == WQ_ACRYL) pool.meta[slot] = m;
+            if (Q == WQ_FLIGHT || dest == WQ_ACRYL || dest == WQ_COND) pool.meta[slot] = m;
             done++;
         }
         wave_push(w, dest, slot);
