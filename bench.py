@@ -28,10 +28,11 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# Per-photon FP64 work of the full-scene workload, measured with ncu thread-level instruction
-# counters (DFMA counted as 2, DADD/DMUL as 1) on 1e6 photons of this workload; profiles/
-# photon_kernel_full_scene.md holds the capture. Used for the roofline's achieved FP64 rate.
-FP64_OPS_PER_PHOTON = {"full": None, "small": None}
+# Work per photon of the wavefront engine on each workload (counter-based stream), summed over every
+# stage kernel of one ncu capture of a 4e6-photon trace (see profiles/wavefront_stages_full_scene.md):
+# warp instructions issued, FP64 flops executed (DFMA counted as 2) and DRAM bytes read + written.
+# The issue-slot roofline divides warp instructions issued per second by 4 schedulers x SMs x clock.
+PER_PHOTON = {"full": None, "small": None}
 
 
 def workload(name: str):
@@ -53,6 +54,14 @@ def workload_config(name: str, n: int, rng: str) -> dict:
     return {"workload": "small plain MC: 64 lognormal quartz bins (median 20 um, sigma_g 1.6) at 100 mg/L, uniform, "
                         "flat surface, r=12.5 mm cell, Mie tables 1801 angles, 860 nm",
             "photons_per_step": n, "rng": rng, "l2": "flushed between steps (256 MiB write)"}
+
+
+def measured_peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 class ClockSampler:
@@ -215,11 +224,15 @@ def main():
     kernel_ms = []
     tallies = []
     wall0 = time.perf_counter()
+    launches = passes = 0
     for k in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         T, _ = ctx.trace(run(args.warmup + k))
         kernel_ms.append(ctx.last_kernel_ms())
+        nl, npass = ctx.last_launches()
+        launches += nl
+        passes += npass
         tallies.append(T)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
@@ -258,28 +271,37 @@ def main():
     e2e = world * n * e2e_steps / e2e_t
 
     sched = np.sum([t["sched_stats"] for t in tallies], axis=0)
-    ev = np.sum([t["event_counts"] for t in tallies], axis=0)
-    fp64_per_photon = FP64_OPS_PER_PHOTON.get(args.workload)
     launch_s = total_ms * 1e-3 / args.steps
-    roofline = {"bound": "fp64", "unit": "TFLOP/s", "peak": fp64_peak / 1e12,
-                "peak_source": "measured FP64 DFMA throughput (library calibration kernel, this GPU)",
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    sm_mhz = measured_peaks().get("sm_max_mhz") or 2070.0
+    issue_peak = 4.0 * sms * sm_mhz * 1e6  # warp instructions per second
+    per = PER_PHOTON.get(args.workload) if rng_mode == abi.RNG_PHILOX else None
+    roofline = {"bound": "issue", "unit": "Twarp-inst/s", "peak": issue_peak / 1e12,
+                "peak_source": f"4 warp schedulers x {sms} SMs x {sm_mhz:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json)",
                 "achieved": None, "frac": None, "traffic": None,
-                "fp32_peak_tflops": fp32_peak / 1e12}
-    if fp64_per_photon:
-        ach = fp64_per_photon * n / launch_s
-        roofline["achieved"] = ach / 1e12
-        roofline["frac"] = ach / fp64_peak
+                "dominant": "one trace: all wavefront stage kernels (they run concurrently inside each pass graph)"}
+    if per:
+        ach = per["warp_inst"] * n / launch_s
+        roofline.update({"achieved": ach / 1e12, "frac": ach / issue_peak, "traffic": per["dram_bytes"] * n,
+                         "traffic_unit": "bytes per trace (ncu dram__bytes_read+write, scaled by photons)"})
+        roofline["fp64"] = {"achieved_tflops": per["fp64_flops"] * n / launch_s / 1e12,
+                            "peak_tflops": fp64_peak / 1e12,
+                            "frac": per["fp64_flops"] * n / launch_s / fp64_peak,
+                            "peak_source": "measured DFMA loop (library calibration kernel, same GPU)"}
+        roofline["hbm"] = {"achieved_gbs": per["dram_bytes"] * n / launch_s / 1e9,
+                           "peak_gbs": measured_peaks().get("hbm_gbs")}
+    stage_names = ["gen", "entry", "flight", "cond", "geom", "morph", "top", "bottom", "side", "acryl", "fin"]
     line = {"metric": "photons/s (at fixed tally error)", "value": value, "unit": "photons/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 transport, f64 Mie",
             "data": "synthetic (seeded)", "config": workload_config(args.workload, n, args.rng),
             "e2e": {"value": e2e, "unit": "photons/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "steps": e2e_steps, "includes": "scene upload, Mie/table/rate/field precompute, trace, tally readback"},
-            "gpu_launches": args.steps, "clocks": clocks, "roofline": roofline,
-            "kernel": {"mean_ms": float(np.mean(kernel_ms)), "wall_s": wall,
-                       "water_steps_per_photon": float(ev[20] / (n * args.steps)),
-                       "lanes_per_iteration": [float(sched[4 + k] / max(sched[k], 1)) for k in range(3)],
-                       "cycle_share": [float(sched[8 + k] / max(sched[8:11].sum(), 1)) for k in range(3)]}}
+            "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline,
+            "engine": {"passes_per_trace": passes / args.steps, "wall_s": wall,
+                       "stage_visits_per_photon": {stage_names[i]: float(sched[i] / (n * args.steps))
+                                                   for i in range(len(stage_names))},
+                       "fp32_peak_tflops": fp32_peak / 1e12}}
     if rank == 0 and world == 1 and not args.no_cpu:
         ref = CpuReference(args.workload, os.cpu_count() or 1)
         ns = ref.sample_size(args.cpu_seconds)

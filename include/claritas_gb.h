@@ -297,9 +297,14 @@ int clr_trace(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray
 /* Same as clr_trace with HOST-resident record memory (copied back inside the call). */
 int clr_trace_host_records(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* host_records);
 
-/* Device time of the photon kernel in the last clr_trace call, measured with CUDA events recorded
- * on the context's stream around the launch (milliseconds). No reference counterpart. */
+/* Device time of the photon transport in the last clr_trace call, measured with CUDA events
+ * recorded on the context's stream around its launches (milliseconds). No reference counterpart. */
 int clr_last_kernel_ms(const clr_ctx* ctx, float* ms);
+
+/* Kernel launches of the last clr_trace call (the wavefront engine launches one graph of 12 kernel
+ * nodes per pass plus one initialisation kernel; the persistent kernel is one launch) and the number
+ * of wavefront passes (0 for the persistent kernel). No reference counterpart. */
+int clr_last_launches(const clr_ctx* ctx, int64_t* launches, int64_t* passes);
 
 /* Calibration kernels for roofline denominators (no reference counterpart): sustained
  * arithmetic throughput of this device in operations per second, counting a fused

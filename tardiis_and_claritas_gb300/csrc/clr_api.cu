@@ -44,6 +44,7 @@ struct clr_ctx {
     unsigned* wave_live = nullptr;  // pinned
     cudaEvent_t wave_ev = nullptr;
     int last_passes = 0;
+    long long last_launches = 0;
 };
 
 static int fail(clr_ctx* c, int code, const char* fmt, ...) {
@@ -385,8 +386,11 @@ static int trace_impl(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out,
         w.ctl = ctx->wave_ctl; w.cap = ctx->wave_cap; w.host_live = ctx->wave_live; w.flag_event = ctx->wave_ev;
     }
     CU(cudaEventRecord(ctx->ev0, st));
+    ctx->last_passes = 0;
+    ctx->last_launches = 0;
     if (persistent) {
         if (cb[1] > 0) CU(launch_photon_kernel(a));
+        ctx->last_launches = cb[1] > 0 ? 1 : 0;
     } else if (run->n_rays > 0) {
         const long long max_passes = 100000 + 8LL * (long long)ctx->sp.max_iterations;
         cudaError_t e = a.rng_mode == CLR_RNG_PHILOX ? wave_run_philox(w, ctx->num_sms, st, max_passes, &ctx->last_passes)
@@ -394,6 +398,7 @@ static int trace_impl(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out,
         if (e == cudaErrorLaunchTimeout)
             return fail(ctx, CLR_ERR_DEVICE_TIMEOUT, "wavefront engine did not drain within %lld passes", max_passes);
         CU(e);
+        ctx->last_launches = 1 + (long long)ctx->last_passes * (1 + CLR_WQ_COUNT);
     }
     CU(cudaEventRecord(ctx->ev1, st));
     DevTally ht;
@@ -424,6 +429,13 @@ int clr_trace_host_records(clr_ctx* ctx, const clr_run_params* run, clr_tallies*
     }
     cudaFree(d);
     return rc;
+}
+
+int clr_last_launches(const clr_ctx* ctx, int64_t* launches, int64_t* passes) {
+    if (!ctx || !launches || !passes) return CLR_ERR_INVALID_ARGUMENT;
+    *passes = ctx->last_passes;
+    *launches = ctx->last_launches;
+    return CLR_OK;
 }
 
 int clr_last_kernel_ms(const clr_ctx* ctx, float* ms) {

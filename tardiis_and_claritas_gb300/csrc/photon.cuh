@@ -475,10 +475,17 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
             }
         }
         if (!lazy) {
-            double tsided = o_bore_wall_hit(x, y, z, vx, vy, vz, RIN, ZMIN, ZTOP);
-            if (tsided < 0.0) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break; }
-            float tside = (tsided < 0.5 * (double)CLR_INF_F) ? (float)tsided : CLR_INF_F;
-            float ttop = o_surface_hit(x, y, z, vx, vy, vz, ZMEAN, RIN, FSM, DH, CORE), tbottom = CLR_INF_F;
+            float tside, ttop, tbottom = CLR_INF_F;
+            if constexpr (kCounterStream<S>) {
+                tside = f_bore_wall_hit(x, y, z, vx, vy, vz, RIN, ZMIN, ZTOP);
+                if (tside < 0.0f) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break; }
+                ttop = f_surface_hit(x, y, z, vx, vy, vz, ZMEAN, RIN, FSM, DH, CORE);
+            } else {
+                double tsided = o_bore_wall_hit(x, y, z, vx, vy, vz, RIN, ZMIN, ZTOP);
+                if (tsided < 0.0) { r.pf = OP_INVALID_MEDIUM; r.pfs = OS_WATER_OUTSIDE; r.st = 4; res = WE_ENDED; break; }
+                tside = (tsided < 0.5 * (double)CLR_INF_F) ? (float)tsided : CLR_INF_F;
+                ttop = o_surface_hit(x, y, z, vx, vy, vz, ZMEAN, RIN, FSM, DH, CORE);
+            }
             if (vz < -1e-14f) tbottom = (ZMIN - z) / vz;
             if (!(ttop > 0.0f)) ttop = CLR_INF_F;
             if (!(tbottom > 0.0f)) tbottom = CLR_INF_F;

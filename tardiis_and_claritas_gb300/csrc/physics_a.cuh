@@ -480,6 +480,110 @@ __device__ __forceinline__ float o_surface_hit(float x, float y, float z, float 
     }
     return o_surface_hit_curved(x, y, z, vx, vy, vz, zmean, R, model, dh, core);
 }
+/* FP32 first positive crossing of the free surface, for the counter-based stream. Parabolic: the
+ * quadratic by the cancellation-free formula. Scully: with q(t) = r(t)^2 the crossing solves
+ * P(t) = (a^2 + q) (z(t) - zs(r(t))) = c3 t^3 + c2 t^2 + c1 t + c0 = 0 (P < 0 below the surface),
+ * restricted to the chord of the ray inside the tube, where the surface formula holds: the chord is
+ * split at the cubic's turning points and the first sign change is bisected to FP32 resolution. This
+ * is the reference's bounded-root search (o_scully_bounded_root), which it uses whenever its Cardano
+ * root fails validation; the roots agree to FP32 rounding. */
+__device__ __forceinline__ float f_quadratic_min_positive(float A, float B, float Cc) {
+    if (fabsf(A) < 1e-24f) {
+        if (fabsf(B) < 1e-24f) return CLR_INF_F;
+        const float t = -Cc / B;
+        return t > 0.0f ? t : CLR_INF_F;
+    }
+    const float D = B * B - 4.0f * A * Cc;
+    if (D < 0.0f) return CLR_INF_F;
+    const float sd = sqrtf(fmaxf(D, 0.0f));
+    const float q = -0.5f * (B + copysignf(sd, B));
+    const float t1 = (fabsf(q) > 1e-30f) ? q / A : (-B - sd) / (2.0f * A);
+    const float t2 = (fabsf(q) > 1e-30f) ? Cc / q : (-B + sd) / (2.0f * A);
+    float best = CLR_INF_F;
+    if (t1 > 0.0f && t1 < best) best = t1;
+    if (t2 > 0.0f && t2 < best) best = t2;
+    return best;
+}
+__device__ __forceinline__ float f_cubic(float c3, float c2, float c1, float c0, float t) {
+    return ((c3 * t + c2) * t + c1) * t + c0;
+}
+__device__ __noinline__ float f_surface_hit_curved(float x, float y, float z, float vx, float vy, float vz,
+                                                   float zmean, float R, int model, float dh, float core) {
+    if (model == 1) {
+        const float aa = dh / (R * R);
+        const float A = -aa * (vx * vx + vy * vy);
+        const float B = vz - 2.0f * aa * (x * vx + y * vy);
+        const float Cc = z - (zmean - 0.5f * dh) - aa * (x * x + y * y);
+        return f_quadratic_min_positive(A, B, Cc);
+    }
+    const float RR = R * R, aa = core * core;
+    const float H = dh * (aa + RR) / RR;
+    const float Csurf = zmean - H * (1.0f - (aa / RR) * log1pf(RR / aa));
+    const float Q2 = vx * vx + vy * vy, Q1 = 2.0f * (x * vx + y * vy), Q0 = x * x + y * y;
+    const float L0 = z - Csurf;
+    if (!(Q2 > 0.0f)) {  // vertical ray: the surface height is constant along it
+        const float t = (vz != 0.0f) ? ((Csurf + H * Q0 / (aa + Q0)) - z) / vz : CLR_INF_F;
+        return (t > 0.0f && Q0 <= RR * (1.0f + 2e-6f)) ? t : CLR_INF_F;
+    }
+    const float c3 = vz * Q2, c2 = (L0 - H) * Q2 + vz * Q1, c1 = (L0 - H) * Q1 + vz * (aa + Q0);
+    const float c0 = L0 * aa + (L0 - H) * Q0;
+    // chord of the ray inside the tube: q(t) <= R^2
+    const float dc = Q1 * Q1 - 4.0f * Q2 * (Q0 - RR);
+    if (dc < 0.0f) return CLR_INF_F;
+    const float qq = -0.5f * (Q1 + copysignf(sqrtf(dc), Q1));
+    const float ta = (qq != 0.0f) ? qq / Q2 : -Q1 / (2.0f * Q2);
+    const float tb = (qq != 0.0f) ? (Q0 - RR) / qq : ta;
+    const float lo = fmaxf(0.0f, fminf(ta, tb)), hi = fmaxf(ta, tb);
+    if (!(hi > lo) || !isfinite(hi)) return CLR_INF_F;
+    float cuts[4];
+    int n = 0;
+    cuts[n++] = lo;
+    const float A = 3.0f * c3, B = 2.0f * c2, Cd = c1;
+    if (A != 0.0f) {
+        const float disc = B * B - 4.0f * A * Cd;
+        if (disc >= 0.0f) {
+            const float q = -0.5f * (B + copysignf(sqrtf(disc), B));
+            const float r1 = (q != 0.0f) ? q / A : -B / (2.0f * A);
+            const float r2 = (q != 0.0f) ? Cd / q : r1;
+            const float s1 = fminf(r1, r2), s2 = fmaxf(r1, r2);
+            if (s1 > lo && s1 < hi) cuts[n++] = s1;
+            if (s2 > lo && s2 < hi && s2 != s1) cuts[n++] = s2;
+        }
+    } else if (B != 0.0f) {
+        const float r = -Cd / B;
+        if (r > lo && r < hi) cuts[n++] = r;
+    }
+    cuts[n++] = hi;
+    for (int i = 0; i < n - 1; ++i) {
+        float l = cuts[i], r = cuts[i + 1];
+        float fl = f_cubic(c3, c2, c1, c0, l);
+        const float fr = f_cubic(c3, c2, c1, c0, r);
+        if (l > 0.0f && fl == 0.0f) return l;
+        if ((fl < 0.0f && fr > 0.0f) || (fl > 0.0f && fr < 0.0f)) {
+            for (int j = 0; j < 40; ++j) {
+                const float m = l + 0.5f * (r - l);
+                if (m == l || m == r) break;
+                const float fm = f_cubic(c3, c2, c1, c0, m);
+                if (fm == 0.0f) { l = r = m; break; }
+                if ((fl < 0.0f) == (fm < 0.0f)) { l = m; fl = fm; } else r = m;
+            }
+            const float t = l + 0.5f * (r - l);
+            return t > 0.0f ? t : CLR_INF_F;
+        }
+        if (r > 0.0f && fr == 0.0f) return r;
+    }
+    return CLR_INF_F;
+}
+__device__ __forceinline__ float f_surface_hit(float x, float y, float z, float vx, float vy, float vz, float zmean,
+                                               float R, int model, float dh, float core) {
+    if (model == 0 || dh <= 0.0f) {
+        if (fabsf(vz) <= 1e-14f) return CLR_INF_F;
+        const float t = (zmean - z) / vz;
+        return (t > 0.0f) ? t : CLR_INF_F;
+    }
+    return f_surface_hit_curved(x, y, z, vx, vy, vz, zmean, R, model, dh, core);
+}
+
 /* unit normal into the water (:1768-1779) */
 __device__ __forceinline__ void o_surface_normal(float x, float y, float R, int model, float dh, float core, float* nx, float* ny,
                                     float* nz) {

@@ -919,6 +919,31 @@ __device__ double o_bore_wall_hit(float x, float y, float z, float vx, float vy,
     double zh = (double)z + t * (double)vz;
     return (zh >= zlo - ztol && zh <= zhi + ztol) ? t : 1.0e300;
 }
+/* FP32 distance to the tube wall from inside, for the counter-based stream: the same cases and
+ * tolerances as o_bore_wall_hit (its tolerances are stated in FP32 epsilons already). */
+__device__ __forceinline__ float f_bore_wall_hit(float x, float y, float z, float vx, float vy, float vz, float R,
+                                                 float zlo, float zhi) {
+    const float RR = R * R;
+    const float rr2 = x * x + y * y;
+    float c = rr2 - RR, b = x * vx + y * vy;
+    const float a = vx * vx + vy * vy;
+    const float radial_tol = 8.0f * 1.1920928955078125e-7f * RR;
+    const float ztol = (float)o_support_tol(R, R, zlo, zlo, zhi);
+    if (c > radial_tol || !isfinite(c) || !isfinite(b) || !isfinite(a)) return -1.0f;
+    if (c >= 0.0f) {
+        if (b >= 0.0f && a > 0.0f && z >= zlo - ztol && z <= zhi + ztol) return 0.0f;
+        b *= sqrtf(RR / rr2);
+        c = 0.0f;
+    }
+    if (!(a > 1e-30f)) return CLR_INF_F;
+    const float d = b * b - a * c;
+    if (d < 0.0f) return CLR_INF_F;
+    const float sd = sqrtf(d), q = -b - copysignf(sd, b);
+    const float t = (b < 0.0f) ? q / a : ((q != 0.0f) ? c / q : 0.0f);
+    if (!(t >= 0.0f) || !isfinite(t)) return CLR_INF_F;
+    const float zh = z + t * vz;
+    return (zh >= zlo - ztol && zh <= zhi + ztol) ? t : CLR_INF_F;
+}
 /* water-side offset after a free-surface event (:2962-2977) */
 __device__ int o_surface_offset(float* x, float* y, float* z, float nx, float ny, float nz, float R, float ZMIN,
                             float ZMEAN, int model, float dh, float core) {

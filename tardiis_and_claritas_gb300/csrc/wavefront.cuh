@@ -48,7 +48,7 @@ constexpr int kFlightSteps = 8;
 constexpr unsigned kRareBatch = 8192;
 constexpr unsigned kMaxSkips = 8;
 __host__ __device__ constexpr bool stage_is_rare(int q) {
-    return q == WQ_COND || q == WQ_MORPH || q == WQ_TOP || q == WQ_BOTTOM;
+    return q == WQ_MORPH || q == WQ_TOP || q == WQ_BOTTOM;
 }
 // minimum resident blocks per SM (register budget) per stage
 __host__ __device__ constexpr int stage_min_blocks(int q) { return q == WQ_COND ? 1 : 2; }
@@ -58,7 +58,7 @@ constexpr int kAcrBudget = 256;
 // closure trials per visit: a few inline in GEOM (most closures end in one or two), more per COND visit
 // (a closure can take 16384 trials, e.g. when no sampled sphere fits)
 constexpr int kCondInline = 8;
-constexpr int kCondBudget = 1024;
+constexpr int kCondBudget = 512;
 
 template <class Mode>
 struct WavePool {

@@ -47,6 +47,7 @@ def load(build_if_missing: bool = False):
             "clr_trace_host_records": ([C.c_void_p, P(abi.RunParams), P(abi.Tallies), C.c_void_p], C.c_int),
             "clr_abi_sizeof": ([C.c_int], C.c_int64),
             "clr_last_kernel_ms": ([C.c_void_p, P(C.c_float)], C.c_int),
+            "clr_last_launches": ([C.c_void_p, P(C.c_int64), P(C.c_int64)], C.c_int),
             "clr_calibrate": ([C.c_void_p, C.c_int, P(C.c_double)], C.c_int),
         }
         for name, (argt, rest) in sig.items():
@@ -60,7 +61,7 @@ def load(build_if_missing: bool = False):
 def exported_symbols() -> list[str]:
     return ["clr_create", "clr_destroy", "clr_last_error", "clr_version", "clr_set_scene", "clr_build_particles",
             "clr_read_particle_physics", "clr_trace", "clr_trace_host_records", "clr_abi_sizeof",
-            "clr_last_kernel_ms", "clr_calibrate"]
+            "clr_last_kernel_ms", "clr_last_launches", "clr_calibrate"]
 
 
 class Context:
@@ -116,6 +117,12 @@ class Context:
         v = C.c_float()
         self._check(self.lib.clr_last_kernel_ms(self.h, C.byref(v)), "clr_last_kernel_ms")
         return float(v.value)
+
+    def last_launches(self) -> tuple[int, int]:
+        """(kernel launches, wavefront passes) of the last trace."""
+        n, p = C.c_int64(), C.c_int64()
+        self._check(self.lib.clr_last_launches(self.h, C.byref(n), C.byref(p)), "clr_last_launches")
+        return int(n.value), int(p.value)
 
     def calibrate(self, which: int) -> float:
         v = C.c_double()
