@@ -52,6 +52,7 @@ struct SlotMeta {
 struct WaveCtl {
     unsigned long long next_photon, total_photons;
     unsigned head[CLR_WQ_COUNT], tail[CLR_WQ_COUNT], snap[CLR_WQ_COUNT], finished[CLR_WQ_COUNT], skips[CLR_WQ_COUNT];
+    unsigned claim[CLR_WQ_COUNT];  // next unclaimed entry of this pass's window (chunks of 32)
     unsigned live, passes;
 };
 

@@ -111,31 +111,47 @@ __global__ void wave_begin_kernel(WaveLaunch w) {
         else if (stage_is_rare(q) && n < kRareBatch && c->skips[q] < kMaxSkips && drawing) run = false;
         c->snap[q] = run ? c->tail[q] : c->head[q];
         c->skips[q] = run ? 0u : c->skips[q] + (n > 0 ? 1u : 0u);
+        c->claim[q] = 0u;
     }
     c->live = (pending != 0u || drawing) ? 1u : 0u;
     c->passes++;
 }
 
 // Per-block conditional-closure statistics for scenario 0 (others go straight to the device tally).
+// The last warp of the block to finish flushes them, so warps leave without waiting at a barrier.
 struct BlockStats {
     unsigned long long cs[CLR_N_CONDITIONAL_STATS];
-    unsigned long long items;
+    unsigned warps_done;
 };
 __device__ __forceinline__ void block_stats_init(BlockStats* b) {
     if (threadIdx.x < CLR_N_CONDITIONAL_STATS) b->cs[threadIdx.x] = 0ull;
-    if (threadIdx.x == 0) b->items = 0ull;
+    if (threadIdx.x == 0) b->warps_done = 0u;
     __syncthreads();
 }
-__device__ __forceinline__ void block_stats_flush(BlockStats* b, DevTally* t, int q) {
-    __syncthreads();
-    if (threadIdx.x < CLR_N_CONDITIONAL_STATS && b->cs[threadIdx.x])
-        atomicAdd(&t[0].c.cstats[threadIdx.x], b->cs[threadIdx.x]);
-    if (threadIdx.x == 0 && b->items) atomicAdd(&t[0].sched[q], b->items);
+__device__ __forceinline__ void warp_done(BlockStats* b, DevTally* t, int q, unsigned long long items) {
+    const int lane = threadIdx.x & 31;
+    const unsigned long long sum = __reduce_add_sync(0xffffffffu, (unsigned)items);
+    if (lane == 0 && sum) atomicAdd(&t[0].sched[q], sum);
+    __threadfence_block();
+    unsigned done = 0;
+    if (lane == 0) done = atomicAdd(&b->warps_done, 1u);
+    done = __shfl_sync(0xffffffffu, done, 0);
+    if (done == (blockDim.x >> 5) - 1) {
+        __threadfence_block();
+        if (lane < CLR_N_CONDITIONAL_STATS) {
+            const unsigned long long v = atomicAdd(&b->cs[lane], 0ull);
+            if (v) atomicAdd(&t[0].c.cstats[lane], v);
+        }
+    }
 }
 
-// Chunk order of a stage: warp k of block b takes chunks (k * gridDim.x + b) + j * (all warps), so a
-// window smaller than the grid is spread over every block (and SM) rather than the first blocks.
-__device__ __forceinline__ unsigned wave_first_chunk() { return (threadIdx.x >> 5) * gridDim.x + blockIdx.x; }
+// Next chunk of 32 entries of this pass's window for the calling warp (all lanes call). Warps claim
+// chunks dynamically, so a warp that drew short histories takes more chunks than one that drew long ones.
+__device__ __forceinline__ unsigned wave_claim(const WaveLaunch& w, int q) {
+    unsigned b = 0;
+    if ((threadIdx.x & 31) == 0) b = atomicAdd(&w.ctl->claim[q], 32u);
+    return __shfl_sync(0xffffffffu, b, 0);
+}
 
 // This pass's window of queue q, iterated in warp-uniform chunks of 32 entries.
 struct WaveWindow {
@@ -175,19 +191,16 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WarpTally* wt = reinterpret_cast<WarpTally*>(smem_raw) + (threadIdx.x >> 5);
     __shared__ DetTable det;
-    __shared__ unsigned long long items;
     det_table_init(&det);
     const int lane = threadIdx.x & 31;
     warp_tally_zero(wt, lane);
-    if (threadIdx.x == 0) items = 0ull;
     __syncthreads();
     const WavePool<Mode> pool = wave_pool<Mode>(w);
     const uint32_t* ring = wave_ring(w, WQ_FREE);
     const unsigned FULL = 0xffffffffu;
-    const unsigned warp = wave_first_chunk(), n_warps = (gridDim.x * blockDim.x) >> 5;
     bool out = !wave_drawing(w);
     unsigned long long drawn = 0;
-    for (unsigned base = warp * 32u; base < win.n && !__all_sync(FULL, out); base += n_warps * 32u) {
+    for (unsigned base = wave_claim(w, WQ_FREE); base < win.n && !__all_sync(FULL, out); base = wave_claim(w, WQ_FREE)) {
         const unsigned i = base + lane;
         const bool valid = i < win.n;
         const uint32_t slot = valid ? ring[(win.head + i) & wave_mask(w)] : 0u;
@@ -232,10 +245,9 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
         // slots left unfilled once every photon is drawn are not needed again
         wave_push(w, filled ? WQ_ENTRY : -1, slot);
     }
-    atomicAdd(&items, drawn);
-    __syncthreads();
+    const unsigned long long sum = __reduce_add_sync(FULL, (unsigned)drawn);
+    if (lane == 0 && sum) atomicAdd(&w.tallies[0].sched[WQ_FREE], sum);
     flush_warp_tally(wt, w.tallies, lane);
-    if (threadIdx.x == 0 && items) atomicAdd(&w.tallies[0].sched[WQ_FREE], items);
 }
 
 // ---------------- generic stage kernel (ENTRY, FLIGHT and the event handlers) ----------------
@@ -320,9 +332,8 @@ __global__ void __launch_bounds__(kWaveThreads, stage_min_blocks(Q)) wave_stage_
     const WavePool<Mode> pool = wave_pool<Mode>(w);
     const uint32_t* ring = wave_ring(w, Q);
     const int lane = threadIdx.x & 31;
-    const unsigned warp = wave_first_chunk(), n_warps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long done = 0;
-    for (unsigned base = warp * 32u; base < win.n; base += n_warps * 32u) {
+    for (unsigned base = wave_claim(w, Q); base < win.n; base = wave_claim(w, Q)) {
         const unsigned i = base + lane;
         const bool valid = i < win.n;
         const uint32_t slot = valid ? ring[(win.head + i) & wave_mask(w)] : 0u;
@@ -341,8 +352,7 @@ __global__ void __launch_bounds__(kWaveThreads, stage_min_blocks(Q)) wave_stage_
         }
         wave_push(w, dest, slot);
     }
-    atomicAdd(&bs.items, done);
-    block_stats_flush(&bs, w.tallies, Q);
+    warp_done(&bs, w.tallies, Q, done);
 }
 
 // ---------------- FIN: detector scoring and tallies; the slot becomes free ----------------
@@ -353,17 +363,14 @@ __global__ void __launch_bounds__(kWaveThreads) wave_fin_kernel(WaveLaunch w) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WarpTally* wt = reinterpret_cast<WarpTally*>(smem_raw) + (threadIdx.x >> 5);
     __shared__ DetTable det;
-    __shared__ unsigned long long items;
     det_table_init(&det);
     const int lane = threadIdx.x & 31;
     warp_tally_zero(wt, lane);
-    if (threadIdx.x == 0) items = 0ull;
     __syncthreads();
     const WavePool<Mode> pool = wave_pool<Mode>(w);
     const uint32_t* ring = wave_ring(w, WQ_FIN);
-    const unsigned warp = wave_first_chunk(), n_warps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long done = 0;
-    for (unsigned base = warp * 32u; base < win.n; base += n_warps * 32u) {
+    for (unsigned base = wave_claim(w, WQ_FIN); base < win.n; base = wave_claim(w, WQ_FIN)) {
         const unsigned i = base + lane;
         const bool valid = i < win.n;
         const uint32_t slot = valid ? ring[(win.head + i) & wave_mask(w)] : 0u;
@@ -376,10 +383,9 @@ __global__ void __launch_bounds__(kWaveThreads) wave_fin_kernel(WaveLaunch w) {
         }
         wave_push(w, valid ? WQ_FREE : -1, slot);
     }
-    atomicAdd(&items, done);
-    __syncthreads();
+    const unsigned long long sum = __reduce_add_sync(0xffffffffu, (unsigned)done);
+    if (lane == 0 && sum) atomicAdd(&w.tallies[0].sched[WQ_FIN], sum);
     flush_warp_tally(wt, w.tallies, lane);
-    if (threadIdx.x == 0 && items) atomicAdd(&w.tallies[0].sched[WQ_FIN], items);
 }
 
 __global__ void wave_init_kernel(WaveLaunch w) {
@@ -389,6 +395,7 @@ __global__ void wave_init_kernel(WaveLaunch w) {
         WaveCtl* c = w.ctl;
         for (int k = 0; k < CLR_WQ_COUNT; ++k) {
             c->head[k] = 0u; c->tail[k] = 0u; c->snap[k] = 0u; c->finished[k] = 0u; c->skips[k] = 0u;
+            c->claim[k] = 0u;
         }
         c->tail[WQ_FREE] = w.cap;
         c->next_photon = 0ull;
