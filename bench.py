@@ -32,7 +32,7 @@ sys.path.insert(0, ROOT)
 # stage kernel of one ncu capture of a 4e6-photon trace (see profiles/wavefront_stages_full_scene.md):
 # warp instructions issued, FP64 flops executed (DFMA counted as 2) and DRAM bytes read + written.
 # The issue-slot roofline divides warp instructions issued per second by 4 schedulers x SMs x clock.
-PER_PHOTON = {"full": None, "small": None}
+PER_PHOTON = {"full": {"warp_inst": 499.7, "fp64_flops": 17.1, "dram_bytes": 852.8}, "small": None}
 
 
 def workload(name: str):
@@ -172,6 +172,7 @@ def main():
     ap.add_argument("--photons", type=int, default=0, help="override photons per step")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--e2e-steps", type=int, default=3, help="steps of the end-to-end leg (0: skip it)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -211,7 +212,7 @@ def main():
 
     def run(step: int):
         # disjoint photon ranges per rank and step (counter-based streams: partition independent)
-        off = ((rank * (args.warmup + args.steps) + step) * n) % (1 << 31)
+        off = S.replica_ray_offset(rank, step, args.warmup + args.steps + max(args.e2e_steps, 0), n)
         return S.run_params(n, seed=20261203, ray_offset=off, rng_mode=rng_mode)
 
     for w in range(args.warmup):
@@ -245,7 +246,7 @@ def main():
     value = world * n * args.steps / (total_ms * 1e-3)
 
     # end to end through the public API: host PSD/grid inputs (pinned) -> precompute -> trace -> tallies to host
-    e2e_steps = min(args.steps, 3)
+    e2e_steps = max(0, min(args.steps, args.e2e_steps))
     pinned = {k: torch.from_numpy(getattr(parts, k)).pin_memory() for k in ("diameter_m", "weight", "n_real", "k_imag")}
     grid_pin = torch.from_numpy(np.ascontiguousarray(grid)).pin_memory() if grid is not None else None
     ps_e = abi.ParticleSpec.from_buffer_copy(ps)
@@ -263,12 +264,12 @@ def main():
         ctx.set_scene(sp)
         ctx.build_particles(ps_e, ss_e)
         ctx.trace(run(args.warmup + args.steps + k))
-    e2e_t = time.perf_counter() - t0
+    e2e_t = max(time.perf_counter() - t0, 1e-9)
     if dist:
         t = torch.tensor([e2e_t], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_t = float(t.item())
-    e2e = world * n * e2e_steps / e2e_t
+    e2e = world * n * e2e_steps / e2e_t if e2e_steps else None
 
     sched = np.sum([t["sched_stats"] for t in tallies], axis=0)
     launch_s = total_ms * 1e-3 / args.steps

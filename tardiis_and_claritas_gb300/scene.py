@@ -429,6 +429,13 @@ def run_params(n_rays: int, seed: int = 0, ray_offset: int = 0, rng_mode: int = 
 # ----------------------------------------------------------------------------------------------
 # Synthetic workloads (seeded; shapes and value ranges of the benchmark descriptions)
 # ----------------------------------------------------------------------------------------------
+def replica_ray_offset(rank: int, step: int, steps_per_rank: int, n_rays: int) -> int:
+    """First global photon id of one replica step. Replicas (one per GPU) and their steps take
+    disjoint, contiguous photon ranges; with per-ray random streams keyed by the global photon id the
+    summed integer tallies of the shards equal those of one run over the union."""
+    return ((int(rank) * int(steps_per_rank) + int(step)) * int(n_rays)) % (1 << 31)
+
+
 def lognormal_mass_psd(n_bins: int, d_min: float, d_max: float, median: float, sigma_g: float):
     """Log-spaced diameters with lognormal mass weights (bin-centre density x log-width)."""
     d = np.geomspace(d_min, d_max, n_bins)
