@@ -32,7 +32,7 @@ sys.path.insert(0, ROOT)
 # stage kernel of one ncu capture of a 4e6-photon trace (see profiles/wavefront_stages_full_scene.md):
 # warp instructions issued, FP64 flops executed (DFMA counted as 2) and DRAM bytes read + written.
 # The issue-slot roofline divides warp instructions issued per second by 4 schedulers x SMs x clock.
-PER_PHOTON = {"full": {"warp_inst": 499.7, "fp64_flops": 17.1, "dram_bytes": 852.8}, "small": None}
+PER_PHOTON = {"full": {"warp_inst": 495.5, "fp64_flops": 17.1, "dram_bytes": 850.1}, "small": None}
 
 
 def workload(name: str):
@@ -173,6 +173,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--e2e-steps", type=int, default=3, help="steps of the end-to-end leg (0: skip it)")
+    ap.add_argument("--engine", choices=["wavefront", "persistent"], default="wavefront",
+                    help="photon engine (the persistent kernel is kept for comparison)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -213,7 +215,8 @@ def main():
     def run(step: int):
         # disjoint photon ranges per rank and step (counter-based streams: partition independent)
         off = S.replica_ray_offset(rank, step, args.warmup + args.steps + max(args.e2e_steps, 0), n)
-        return S.run_params(n, seed=20261203, ray_offset=off, rng_mode=rng_mode)
+        return S.run_params(n, seed=20261203, ray_offset=off, rng_mode=rng_mode,
+                            flags=abi.RUN_PERSISTENT_KERNEL if args.engine == "persistent" else 0)
 
     for w in range(args.warmup):
         ctx.trace(run(w))
@@ -276,7 +279,7 @@ def main():
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     sm_mhz = measured_peaks().get("sm_max_mhz") or 2070.0
     issue_peak = 4.0 * sms * sm_mhz * 1e6  # warp instructions per second
-    per = PER_PHOTON.get(args.workload) if rng_mode == abi.RNG_PHILOX else None
+    per = PER_PHOTON.get(args.workload) if (rng_mode == abi.RNG_PHILOX and args.engine == "wavefront") else None
     roofline = {"bound": "issue", "unit": "Twarp-inst/s", "peak": issue_peak / 1e12,
                 "peak_source": f"4 warp schedulers x {sms} SMs x {sm_mhz:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json)",
                 "achieved": None, "frac": None, "traffic": None,
@@ -292,10 +295,12 @@ def main():
         roofline["hbm"] = {"achieved_gbs": per["dram_bytes"] * n / launch_s / 1e9,
                            "peak_gbs": measured_peaks().get("hbm_gbs")}
     stage_names = ["gen", "entry", "flight", "cond", "geom", "morph", "top", "bottom", "side", "acryl", "fin"]
+    cfg_line = workload_config(args.workload, n, args.rng)
+    cfg_line["engine"] = args.engine
     line = {"metric": "photons/s (at fixed tally error)", "value": value, "unit": "photons/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 transport, f64 Mie",
-            "data": "synthetic (seeded)", "config": workload_config(args.workload, n, args.rng),
+            "data": "synthetic (seeded)", "config": cfg_line,
             "e2e": {"value": e2e, "unit": "photons/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "steps": e2e_steps, "includes": "scene upload, Mie/table/rate/field precompute, trace, tally readback"},
             "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline,

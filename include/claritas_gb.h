@@ -294,6 +294,12 @@ int clr_read_particle_physics(clr_ctx* ctx, clr_particle_physics* out);
  * clr_ray_record entries, or NULL for the tally-only hot path. */
 int clr_trace(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* records);
 
+/* Trace n_runs runs of the current scene in one engine execution (one persistent-kernel launch or
+ * one sequence of wavefront passes): each run has its own photon range, seeds and tallies
+ * (outs[n_runs]). The runs share rng_mode, weight_mode and flags. Replaces the reference's chunk loop
+ * when the caller wants per-batch tallies (batch jackknife, CLARITAS/CLARITAS.py:5244, :7638-7862). */
+int clr_trace_batch(clr_ctx* ctx, const clr_run_params* runs, int n_runs, clr_tallies* outs);
+
 /* Same as clr_trace with HOST-resident record memory (copied back inside the call). */
 int clr_trace_host_records(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* host_records);
 

@@ -45,6 +45,7 @@ struct clr_ctx {
     cudaEvent_t wave_ev = nullptr;
     int last_passes = 0;
     long long last_launches = 0;
+    int run_cap = 0;  // runs the per-run buffers hold
 };
 
 static int fail(clr_ctx* c, int code, const char* fmt, ...) {
@@ -61,6 +62,8 @@ static int fail(clr_ctx* c, int code, const char* fmt, ...) {
         cudaError_t e_ = (call);                                                                  \
         if (e_ != cudaSuccess) return fail(ctx, CLR_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
+
+static int run_buffers_ready(clr_ctx* ctx, int n);
 
 static cudaError_t dalloc(clr_ctx* ctx, void** p, size_t bytes) {
     cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
@@ -91,10 +94,11 @@ int clr_create(clr_ctx** out, int device) {
     CU(cudaSetDevice(device));
     CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     CU(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
-    CU(cudaMalloc(&ctx->d_scene, sizeof(DevScene)));
-    CU(cudaMalloc(&ctx->d_chunk_begin, 2 * sizeof(long long)));
-    CU(cudaMalloc(&ctx->d_tally, sizeof(DevTally)));
     CU(cudaMalloc(&ctx->d_work, sizeof(unsigned long long)));
+    {
+        const int rc = run_buffers_ready(ctx, 1);
+        if (rc != CLR_OK) return rc;
+    }
     CU(cudaEventCreate(&ctx->ev0));
     CU(cudaEventCreate(&ctx->ev1));
     *out = ctx;
@@ -336,51 +340,80 @@ static int wave_pool_ready(clr_ctx* ctx) {
     CU(cudaMalloc(&ctx->wave_meta, (size_t)cap * sizeof(SlotMeta)));
     CU(cudaMalloc(&ctx->wave_q, (size_t)CLR_WQ_COUNT * 2 * cap * sizeof(uint32_t)));  // rings of 2 * cap
     CU(cudaMalloc(&ctx->wave_ctl, sizeof(WaveCtl)));
-    CU(cudaMalloc(&ctx->wave_begin, 2 * sizeof(long long)));
     CU(cudaHostAlloc((void**)&ctx->wave_live, sizeof(unsigned), cudaHostAllocDefault));
     CU(cudaEventCreateWithFlags(&ctx->wave_ev, cudaEventDisableTiming));
     ctx->wave_cap = cap;
     return CLR_OK;
 }
 
-static int trace_impl(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* d_records) {
-    if (!ctx || !run || !out) return CLR_ERR_INVALID_ARGUMENT;
+// Per-run buffers (scene descriptions, work-chunk and photon prefixes, tallies) for up to n runs.
+static int run_buffers_ready(clr_ctx* ctx, int n) {
+    if (n <= ctx->run_cap) return CLR_OK;
+    int cap = std::max(n, 2 * ctx->run_cap);
+    cudaFree(ctx->d_scene); cudaFree(ctx->d_chunk_begin); cudaFree(ctx->d_tally); cudaFree(ctx->wave_begin);
+    ctx->d_scene = nullptr; ctx->d_chunk_begin = nullptr; ctx->d_tally = nullptr; ctx->wave_begin = nullptr;
+    ctx->run_cap = 0;
+    CU(cudaMalloc(&ctx->d_scene, (size_t)cap * sizeof(DevScene)));
+    CU(cudaMalloc(&ctx->d_chunk_begin, (size_t)(cap + 1) * sizeof(long long)));
+    CU(cudaMalloc(&ctx->d_tally, (size_t)cap * sizeof(DevTally)));
+    CU(cudaMalloc(&ctx->wave_begin, (size_t)(cap + 1) * sizeof(long long)));
+    ctx->run_cap = cap;
+    return CLR_OK;
+}
+
+// Traces n runs of the current scene in one engine execution (one launch of the persistent kernel or
+// one sequence of wavefront passes), each run with its own photon range, seeds and tallies.
+static int trace_runs(clr_ctx* ctx, const clr_run_params* runs, int n, clr_tallies* outs, clr_ray_record* d_records) {
+    if (!ctx || !runs || !outs || n < 1) return CLR_ERR_INVALID_ARGUMENT;
     if (!ctx->built) return fail(ctx, CLR_ERR_NOT_READY, "clr_build_particles must succeed before clr_trace");
-    if (run->n_rays < 0 || (uint64_t)run->ray_offset + (uint64_t)run->n_rays > (1ull << 32))
-        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "ray range exceeds uint32 global ids");
-    if (run->rng_mode != CLR_RNG_REFERENCE_XORSHIFT && run->rng_mode != CLR_RNG_PHILOX)
-        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "unknown rng_mode %d", run->rng_mode);
-    if (run->weight_mode == CLR_WEIGHT_IMPLICIT && run->rng_mode != CLR_RNG_PHILOX)
-        return fail(ctx, CLR_ERR_UNSUPPORTED, "implicit-capture weighting runs on the Philox stream only");
+    if (d_records && n != 1) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "per-ray records need a single run");
+    const clr_run_params& r0 = runs[0];
+    for (int i = 0; i < n; ++i) {
+        const clr_run_params* run = runs + i;
+        if (run->n_rays < 0 || (uint64_t)run->ray_offset + (uint64_t)run->n_rays > (1ull << 32))
+            return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "run %d: ray range exceeds uint32 global ids", i);
+        if (run->rng_mode != CLR_RNG_REFERENCE_XORSHIFT && run->rng_mode != CLR_RNG_PHILOX)
+            return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "run %d: unknown rng_mode %d", i, run->rng_mode);
+        if (run->weight_mode == CLR_WEIGHT_IMPLICIT && run->rng_mode != CLR_RNG_PHILOX)
+            return fail(ctx, CLR_ERR_UNSUPPORTED, "implicit-capture weighting runs on the Philox stream only");
+        if (run->rng_mode != r0.rng_mode || run->weight_mode != r0.weight_mode || run->flags != r0.flags)
+            return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "runs of one call must share rng_mode, weight_mode and flags");
+    }
     CU(cudaSetDevice(ctx->device));
+    int rc = run_buffers_ready(ctx, n);
+    if (rc != CLR_OK) return rc;
     cudaStream_t st = ctx->stream;
-    DevScene hs;
-    fill_scene(ctx, run, &hs);
-    const int chunk = run->rays_per_item > 0 ? run->rays_per_item : 256;
-    long long cb[2] = {0, (run->n_rays + chunk - 1) / chunk};
-    CU(cudaMemcpyAsync(ctx->d_scene, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(ctx->d_chunk_begin, cb, sizeof cb, cudaMemcpyHostToDevice, st));
-    CU(cudaMemsetAsync(ctx->d_tally, 0, sizeof(DevTally), st));
+    std::vector<DevScene> hs(n);
+    std::vector<long long> cb(n + 1), rb(n + 1);
+    const int chunk = r0.rays_per_item > 0 ? r0.rays_per_item : 256;
+    cb[0] = 0; rb[0] = 0;
+    for (int i = 0; i < n; ++i) {
+        fill_scene(ctx, runs + i, &hs[i]);
+        cb[i + 1] = cb[i] + (runs[i].n_rays + chunk - 1) / chunk;
+        rb[i + 1] = rb[i] + runs[i].n_rays;
+    }
+    const long long total = rb[n];
+    CU(cudaMemcpyAsync(ctx->d_scene, hs.data(), n * sizeof(DevScene), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->d_chunk_begin, cb.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(ctx->d_tally, 0, n * sizeof(DevTally), st));
     CU(cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long), st));
     LaunchArgs a;
-    a.scenes = ctx->d_scene; a.chunk_begin = ctx->d_chunk_begin; a.n_scen = 1; a.n_chunks = cb[1];
+    a.scenes = ctx->d_scene; a.chunk_begin = ctx->d_chunk_begin; a.n_scen = n; a.n_chunks = cb[n];
     a.chunk_rays = chunk; a.work = ctx->d_work; a.tallies = ctx->d_tally; a.records = d_records;
-    a.stream = st; a.rng_mode = run->rng_mode; a.weighted = run->weight_mode == CLR_WEIGHT_IMPLICIT;
+    a.stream = st; a.rng_mode = r0.rng_mode; a.weighted = r0.weight_mode == CLR_WEIGHT_IMPLICIT;
     int occ = photon_kernel_occupancy(a.rng_mode, d_records != nullptr, a.weighted);
     if (occ < 1) occ = 1;
     long long want = (long long)ctx->num_sms * occ;
-    long long warps_needed = (cb[1] + 0);  // one chunk per warp is the finest useful split
-    long long blocks_needed = (warps_needed * 32 + CLR_TRACE_THREADS - 1) / CLR_TRACE_THREADS;
+    long long blocks_needed = (cb[n] * 32 + CLR_TRACE_THREADS - 1) / CLR_TRACE_THREADS;  // a chunk per warp at most
     a.grid = (int)std::max(1LL, std::min(want, blocks_needed));
-    if (run->max_blocks > 0) a.grid = std::max(1, std::min(a.grid, run->max_blocks));
-    const bool persistent = (run->flags & CLR_RUN_PERSISTENT_KERNEL) != 0;
+    if (r0.max_blocks > 0) a.grid = std::max(1, std::min(a.grid, r0.max_blocks));
+    const bool persistent = (r0.flags & CLR_RUN_PERSISTENT_KERNEL) != 0;
     WaveLaunch w{};
     if (!persistent) {
-        int rc = wave_pool_ready(ctx);
+        rc = wave_pool_ready(ctx);
         if (rc != CLR_OK) return rc;
-        const long long rb[2] = {0, run->n_rays};
-        CU(cudaMemcpyAsync(ctx->wave_begin, rb, sizeof rb, cudaMemcpyHostToDevice, st));
-        w.scenes = ctx->d_scene; w.n_scen = 1; w.ray_begin = ctx->wave_begin; w.total = (unsigned long long)run->n_rays;
+        CU(cudaMemcpyAsync(ctx->wave_begin, rb.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, st));
+        w.scenes = ctx->d_scene; w.n_scen = n; w.ray_begin = ctx->wave_begin; w.total = (unsigned long long)total;
         w.tallies = ctx->d_tally; w.records = d_records;
         w.ray = ctx->wave_ray; w.lane = ctx->wave_lane; w.meta = ctx->wave_meta; w.qbuf = ctx->wave_q;
         w.ctl = ctx->wave_ctl; w.cap = ctx->wave_cap; w.host_live = ctx->wave_live; w.flag_event = ctx->wave_ev;
@@ -389,9 +422,9 @@ static int trace_impl(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out,
     ctx->last_passes = 0;
     ctx->last_launches = 0;
     if (persistent) {
-        if (cb[1] > 0) CU(launch_photon_kernel(a));
-        ctx->last_launches = cb[1] > 0 ? 1 : 0;
-    } else if (run->n_rays > 0) {
+        if (cb[n] > 0) CU(launch_photon_kernel(a));
+        ctx->last_launches = cb[n] > 0 ? 1 : 0;
+    } else if (total > 0) {
         const long long max_passes = 100000 + 8LL * (long long)ctx->sp.max_iterations;
         cudaError_t e = a.rng_mode == CLR_RNG_PHILOX ? wave_run_philox(w, ctx->num_sms, st, max_passes, &ctx->last_passes)
                                                      : wave_run_xor(w, ctx->num_sms, st, max_passes, &ctx->last_passes);
@@ -401,18 +434,26 @@ static int trace_impl(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out,
         ctx->last_launches = 1 + (long long)ctx->last_passes * (1 + CLR_WQ_COUNT);
     }
     CU(cudaEventRecord(ctx->ev1, st));
-    DevTally ht;
-    CU(cudaMemcpyAsync(&ht, ctx->d_tally, sizeof ht, cudaMemcpyDeviceToHost, st));
+    std::vector<DevTally> ht(n);
+    CU(cudaMemcpyAsync(ht.data(), ctx->d_tally, n * sizeof(DevTally), cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     CU(cudaEventElapsedTime(&ctx->last_kernel_ms, ctx->ev0, ctx->ev1));
-    tally_to_host(ht, out, run->n_rays);
+    for (int i = 0; i < n; ++i) tally_to_host(ht[i], outs + i, runs[i].n_rays);
     return CLR_OK;
+}
+
+static int trace_impl(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* d_records) {
+    return trace_runs(ctx, run, 1, out, d_records);
 }
 
 extern "C" {
 
 int clr_trace(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* records) {
     return trace_impl(ctx, run, out, records);
+}
+
+int clr_trace_batch(clr_ctx* ctx, const clr_run_params* runs, int n_runs, clr_tallies* outs) {
+    return trace_runs(ctx, runs, n_runs, outs, nullptr);
 }
 
 int clr_trace_host_records(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* host_records) {

@@ -200,6 +200,7 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
     const unsigned FULL = 0xffffffffu;
     bool out = !wave_drawing(w);
     unsigned long long drawn = 0;
+    int home = -1;  // scenario whose counts this warp keeps in shared memory (that of its first photon)
     for (unsigned base = wave_claim(w, WQ_FREE); base < win.n && !__all_sync(FULL, out); base = wave_claim(w, WQ_FREE)) {
         const unsigned i = base + lane;
         const bool valid = i < win.n;
@@ -211,6 +212,12 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
             unsigned long long b0 = 0;
             if (lane == __ffs(need) - 1) b0 = atomicAdd(&w.ctl->next_photon, (unsigned long long)__popc(need));
             b0 = __shfl_sync(FULL, b0, __ffs(need) - 1);
+            if (home < 0 && b0 < w.ctl->total_photons) {
+                int hs;
+                long long hr;
+                photon_of(w, b0, &hs, &hr);
+                home = hs;
+            }
             if ((need >> lane) & 1u) {
                 const unsigned long long p = b0 + (unsigned long long)__popc(need & ((1u << lane) - 1u));
                 if (p >= w.ctl->total_photons) {
@@ -227,7 +234,7 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
                     ray_reset(r);
                     drawn++;
                     if (source_segment(D, r, L.source())) {
-                        finish_ray<Mode>(D, det, r, gid, sid, 0, wt, w.tallies, w.records ? w.records + rid : nullptr);
+                        finish_ray<Mode>(D, det, r, gid, sid, home, wt, w.tallies, w.records ? w.records + rid : nullptr);
                     } else {
                         pool.ray[slot] = r;
                         pool.lane[slot] = L;
@@ -247,7 +254,7 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
     }
     const unsigned long long sum = __reduce_add_sync(FULL, (unsigned)drawn);
     if (lane == 0 && sum) atomicAdd(&w.tallies[0].sched[WQ_FREE], sum);
-    flush_warp_tally(wt, w.tallies, lane);
+    if (home >= 0) flush_warp_tally(wt, w.tallies + home, lane);
 }
 
 // ---------------- generic stage kernel (ENTRY, FLIGHT and the event handlers) ----------------
@@ -370,22 +377,26 @@ __global__ void __launch_bounds__(kWaveThreads) wave_fin_kernel(WaveLaunch w) {
     const WavePool<Mode> pool = wave_pool<Mode>(w);
     const uint32_t* ring = wave_ring(w, WQ_FIN);
     unsigned long long done = 0;
+    int home = -1;  // scenario whose counts this warp keeps in shared memory (that of its first photon)
     for (unsigned base = wave_claim(w, WQ_FIN); base < win.n; base = wave_claim(w, WQ_FIN)) {
         const unsigned i = base + lane;
         const bool valid = i < win.n;
         const uint32_t slot = valid ? ring[(win.head + i) & wave_mask(w)] : 0u;
+        SlotMeta m;
+        m.sid = 0;
+        if (valid) m = pool.meta[slot];
+        if (home < 0) home = __shfl_sync(0xffffffffu, m.sid, 0);  // lane 0 is valid in every claimed chunk
         if (valid) {
             const Ray r = pool.ray[slot];
-            const SlotMeta m = pool.meta[slot];
             const DevScene& D = w.scenes[m.sid];
-            finish_ray<Mode>(D, det, r, m.gid, m.sid, 0, wt, w.tallies, kRecord ? w.records + m.rid : nullptr);
+            finish_ray<Mode>(D, det, r, m.gid, m.sid, home, wt, w.tallies, kRecord ? w.records + m.rid : nullptr);
             done++;
         }
         wave_push(w, valid ? WQ_FREE : -1, slot);
     }
     const unsigned long long sum = __reduce_add_sync(0xffffffffu, (unsigned)done);
     if (lane == 0 && sum) atomicAdd(&w.tallies[0].sched[WQ_FIN], sum);
-    flush_warp_tally(wt, w.tallies, lane);
+    if (home >= 0) flush_warp_tally(wt, w.tallies + home, lane);
 }
 
 __global__ void wave_init_kernel(WaveLaunch w) {

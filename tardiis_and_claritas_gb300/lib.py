@@ -45,6 +45,7 @@ def load(build_if_missing: bool = False):
             "clr_read_particle_physics": ([C.c_void_p, P(abi.ParticlePhysics)], C.c_int),
             "clr_trace": ([C.c_void_p, P(abi.RunParams), P(abi.Tallies), C.c_void_p], C.c_int),
             "clr_trace_host_records": ([C.c_void_p, P(abi.RunParams), P(abi.Tallies), C.c_void_p], C.c_int),
+            "clr_trace_batch": ([C.c_void_p, P(abi.RunParams), C.c_int, P(abi.Tallies)], C.c_int),
             "clr_abi_sizeof": ([C.c_int], C.c_int64),
             "clr_last_kernel_ms": ([C.c_void_p, P(C.c_float)], C.c_int),
             "clr_last_launches": ([C.c_void_p, P(C.c_int64), P(C.c_int64)], C.c_int),
@@ -60,7 +61,7 @@ def load(build_if_missing: bool = False):
 
 def exported_symbols() -> list[str]:
     return ["clr_create", "clr_destroy", "clr_last_error", "clr_version", "clr_set_scene", "clr_build_particles",
-            "clr_read_particle_physics", "clr_trace", "clr_trace_host_records", "clr_abi_sizeof",
+            "clr_read_particle_physics", "clr_trace", "clr_trace_host_records", "clr_trace_batch", "clr_abi_sizeof",
             "clr_last_kernel_ms", "clr_last_launches", "clr_calibrate"]
 
 
@@ -106,6 +107,14 @@ class Context:
             rc = self.lib.clr_trace(self.h, C.byref(run), C.byref(T), None)
         self._check(rc, "clr_trace")
         return T.as_dict(), rec
+
+    def trace_batch(self, runs: list) -> list:
+        """Trace several runs of the current scene together; one tally dict per run."""
+        n = len(runs)
+        arr = (abi.RunParams * n)(*runs)
+        outs = (abi.Tallies * n)()
+        self._check(self.lib.clr_trace_batch(self.h, arr, n, outs), "clr_trace_batch")
+        return [outs[i].as_dict() for i in range(n)]
 
     def trace_device(self, run: abi.RunParams, records_ptr: int | None = None):
         T = abi.Tallies()

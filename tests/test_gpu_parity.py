@@ -197,3 +197,17 @@ def test_precompute_error_is_reported(ctx):
     big = S.Particles([5e-3], [1.0], [1.5], [0.0], 1.0)  # size parameter beyond MIE_MAX_ORDER
     with pytest.raises(RuntimeError, match="error code 1"):
         ctx.build_particles(big.spec(cfg), cfg.sediment_spec())
+
+
+@pytest.mark.parametrize("engine", list(ENGINES))
+def test_trace_batch_equals_single_runs(ctx, engine):
+    """Runs traced together (clr_trace_batch) give each run exactly its single-run integer tallies."""
+    prepare(ctx, "schiller_sediment")
+    runs = [S.run_params(n, seed=sd, ray_offset=off, flags=ENGINES[engine])
+            for n, sd, off in ((30_000, 1, 0), (5_000, 2, 30_000), (0, 3, 0), (47_000, 4, 123_456))]
+    batch = ctx.trace_batch(runs)
+    for run, got in zip(runs, batch):
+        want, _ = ctx.trace(run)
+        for k in PS.TALLY_KEYS:
+            np.testing.assert_array_equal(got[k], want[k], err_msg=f"{engine} n={run.n_rays}: {k}")
+        assert got["n_rays"] == run.n_rays and got["device_error"] == 0
