@@ -317,6 +317,25 @@ int clr_last_launches(const clr_ctx* ctx, int64_t* launches, int64_t* passes);
  * multiply-add as two operations. which = 0: FP32 FFMA; which = 1: FP64 DFMA. */
 int clr_calibrate(clr_ctx* ctx, int which, double* ops_per_second);
 
+/* Allocation-free Mie tables (no reference counterpart; the reference always allocates through
+ * CuPy). Computes, for n_bins <= CLR_NOALLOC_MAX_BINS (16) particle bins and
+ * 2 <= n_theta <= CLR_NOALLOC_MAX_THETA (4097) angles, the extinction and scattering efficiencies,
+ * the asymmetry parameter, the theta grid and the per-bin phase CDF -- the same kernels and values as
+ * clr_build_particles -- into caller-owned DEVICE buffers (d_qext, d_qsca, d_asym_g: [n_bins];
+ * d_theta: [n_theta]; d_phase_cdf: [n_bins][n_theta]) on `stream` (a cudaStream_t, or NULL for the
+ * context's stream). The inputs d_diameter_m, d_n_real, d_k_imag are device arrays of n_bins doubles.
+ * No memory is allocated or freed: the scratch is a fixed set of file-scope device arrays (about 3 MB
+ * per device) whose addresses are resolved on the first call for each device -- make that first call
+ * before any stream capture. The scratch is shared by every context on a device, so calls must not
+ * overlap on one device (serialise them). Only the error word is reset per call; the call synchronises
+ * `stream` to read it and returns CLR_ERR_PRECOMPUTE with "error code k" on a Mie failure, and
+ * CLR_ERR_INVALID_ARGUMENT (with the limits in the message) for sizes beyond the scratch. */
+#define CLR_NOALLOC_MAX_BINS 16
+#define CLR_NOALLOC_MAX_THETA 4097
+int clr_mie_phase_noalloc(clr_ctx* ctx, const double* d_diameter_m, const double* d_n_real, const double* d_k_imag,
+                          int n_bins, double n_medium, double wavelength_m, int n_theta, double* d_qext,
+                          double* d_qsca, double* d_asym_g, double* d_theta, double* d_phase_cdf, void* stream);
+
 /* Sizes of the ABI structs as compiled into the library (0 scene, 1 particle spec, 2 sediment spec,
  * 3 run params, 4 ray record, 5 tallies, 6 particle physics); -1 for an unknown index.
  * No reference counterpart: lets a binding check its struct mirror against the library. */

@@ -472,6 +472,34 @@ int clr_trace_host_records(clr_ctx* ctx, const clr_run_params* run, clr_tallies*
     return rc;
 }
 
+int clr_mie_phase_noalloc(clr_ctx* ctx, const double* d_diameter_m, const double* d_n_real, const double* d_k_imag,
+                          int n_bins, double n_medium, double wavelength_m, int n_theta, double* d_qext,
+                          double* d_qsca, double* d_asym_g, double* d_theta, double* d_phase_cdf, void* stream) {
+    if (!ctx) return CLR_ERR_INVALID_ARGUMENT;
+    if (n_bins < 1 || n_bins > CLR_NOALLOC_MAX_BINS || n_theta < 2 || n_theta > CLR_NOALLOC_MAX_THETA)
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT,
+                    "clr_mie_phase_noalloc: n_bins must be 1..%d and n_theta 2..%d (its fixed scratch), got %d and %d",
+                    CLR_NOALLOC_MAX_BINS, CLR_NOALLOC_MAX_THETA, n_bins, n_theta);
+    if (!d_diameter_m || !d_n_real || !d_k_imag || !d_qext || !d_qsca || !d_asym_g || !d_theta || !d_phase_cdf)
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "clr_mie_phase_noalloc: null buffer");
+    if (!(wavelength_m > 0.0) || !(n_medium > 0.0))
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "clr_mie_phase_noalloc: wavelength and medium index must be positive");
+    CU(cudaSetDevice(ctx->device));
+    NoallocScratch sc;
+    CU(noalloc_scratch(ctx->device, &sc));
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    MiePhaseBuffers b;
+    b.ab = sc.ab; b.nstop = sc.nstop; b.x = sc.x; b.qext = d_qext; b.qsca = d_qsca; b.qabs = sc.qabs;
+    b.qback = sc.qback; b.g = d_asym_g; b.albedo = sc.albedo; b.theta = d_theta; b.theta_f = sc.theta_f;
+    b.pdf = sc.pdf; b.cdf = d_phase_cdf; b.cdf_f = sc.cdf_f; b.err = sc.err;
+    CU(enqueue_mie_phase(d_diameter_m, d_n_real, d_k_imag, n_bins, n_medium, wavelength_m, n_theta, b, st));
+    int herr = 0;
+    CU(cudaMemcpyAsync(&herr, sc.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (herr) return fail(ctx, CLR_ERR_PRECOMPUTE, "clr_mie_phase_noalloc failed with error code %d", herr);
+    return CLR_OK;
+}
+
 int clr_last_launches(const clr_ctx* ctx, int64_t* launches, int64_t* passes) {
     if (!ctx || !launches || !passes) return CLR_ERR_INVALID_ARGUMENT;
     *passes = ctx->last_passes;

@@ -112,6 +112,31 @@ struct ParticleBuffers {
     double muscal_host[8] = {0}, sed_major_host[4] = {0};  // host copies of muscal and sed_major
 };
 
+// Buffers of enqueue_mie_phase (every one supplied by the caller).
+struct MiePhaseBuffers {
+    double* ab;       // [n][CLR_MIE_MAX_ORDER][4] a_n, b_n scratch
+    int* nstop;       // [n]
+    double *x, *qext, *qsca, *qabs, *qback, *g, *albedo;  // [n]
+    double* theta;    // [nt]
+    float* theta_f;   // [nt]
+    double* pdf;      // [n][nt] scratch
+    double* cdf;      // [n][nt]
+    float* cdf_f;     // [n][nt]
+    int* err;         // error word, cleared by the call
+};
+cudaError_t enqueue_mie_phase(const double* d, const double* nr, const double* k, int n, double n_medium,
+                              double wavelength, int nt, const MiePhaseBuffers& b, cudaStream_t stream);
+
+// Scratch of the allocation-free Mie/phase entry point: file-scope __device__ arrays (noalloc.cu) of
+// CLR_NOALLOC_MAX_BINS bins and CLR_NOALLOC_MAX_THETA angles, their addresses resolved once per device.
+struct NoallocScratch {
+    double *ab, *pdf, *x, *qabs, *qback, *albedo;
+    float *theta_f, *cdf_f;
+    int *nstop, *err;
+};
+// Resolves (once per device, with that device current) and returns the scratch addresses.
+cudaError_t noalloc_scratch(int device, NoallocScratch* out);
+
 // Enqueue the whole precompute on `stream`. Host inputs are copied in; error codes land in pb.err.
 // `ab_scratch` may supply the Mie a_n/b_n scratch (n*CLR_MIE_MAX_ORDER*4 doubles); when null, pb.ab is used.
 cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,

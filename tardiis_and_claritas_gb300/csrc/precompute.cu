@@ -544,6 +544,25 @@ __global__ void sediment_node_kernel(const double* __restrict__ grid, const doub
     }
 }
 
+// Mie efficiencies, asymmetry, theta grid and phase CDF of n bins into buffers the caller supplies
+// (the first steps of enqueue_particle_precompute, with no buffer of its own). Used by the
+// allocation-free entry point.
+cudaError_t enqueue_mie_phase(const double* d, const double* nr, const double* k, int n, double n_medium,
+                              double wavelength, int nt, const MiePhaseBuffers& b, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(b.err, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    const size_t smem = (size_t)(CLR_MIE_MAX_ORDER + 1) * sizeof(cdx);
+    e = cudaFuncSetAttribute(mie_coefficients_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    mie_coefficients_kernel<<<n, 32, smem, st>>>(d, nr, k, n_medium, wavelength, n, b.ab, b.nstop, b.x, b.qext,
+                                                 b.qsca, b.qabs, b.qback, b.g, b.albedo, b.err);
+    theta_grid_kernel<<<(nt + 127) / 128, 128, 0, st>>>(b.theta, b.theta_f, nt);
+    dim3 grid((nt + 127) / 128, (n + PDF_GROUP - 1) / PDF_GROUP);
+    phase_pdf_kernel<<<grid, 128, 0, st>>>(b.theta, nt, n, b.nstop, b.ab, b.pdf);
+    phase_cdf_kernel<<<(n + 63) / 64, 64, 0, st>>>(b.theta, b.pdf, nt, n, b.cdf, b.cdf_f, b.err);
+    return cudaGetLastError();
+}
+
 cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,
                                         const clr_sediment_spec& ss, double* ab_scratch, cudaStream_t st) {
     const int n = pb.n;

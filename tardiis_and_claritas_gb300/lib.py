@@ -49,6 +49,9 @@ def load(build_if_missing: bool = False):
             "clr_abi_sizeof": ([C.c_int], C.c_int64),
             "clr_last_kernel_ms": ([C.c_void_p, P(C.c_float)], C.c_int),
             "clr_last_launches": ([C.c_void_p, P(C.c_int64), P(C.c_int64)], C.c_int),
+            "clr_mie_phase_noalloc": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
+                                       C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p], C.c_int),
             "clr_calibrate": ([C.c_void_p, C.c_int, P(C.c_double)], C.c_int),
         }
         for name, (argt, rest) in sig.items():
@@ -62,7 +65,7 @@ def load(build_if_missing: bool = False):
 def exported_symbols() -> list[str]:
     return ["clr_create", "clr_destroy", "clr_last_error", "clr_version", "clr_set_scene", "clr_build_particles",
             "clr_read_particle_physics", "clr_trace", "clr_trace_host_records", "clr_trace_batch", "clr_abi_sizeof",
-            "clr_last_kernel_ms", "clr_last_launches", "clr_calibrate"]
+            "clr_last_kernel_ms", "clr_last_launches", "clr_calibrate", "clr_mie_phase_noalloc"]
 
 
 class Context:
@@ -132,6 +135,16 @@ class Context:
         n, p = C.c_int64(), C.c_int64()
         self._check(self.lib.clr_last_launches(self.h, C.byref(n), C.byref(p)), "clr_last_launches")
         return int(n.value), int(p.value)
+
+    def mie_phase_noalloc(self, diameter_ptr: int, n_real_ptr: int, k_imag_ptr: int, n_bins: int, n_medium: float,
+                          wavelength_m: float, n_theta: int, qext_ptr: int, qsca_ptr: int, asym_g_ptr: int,
+                          theta_ptr: int, phase_cdf_ptr: int, stream_ptr: int = 0):
+        """clr_mie_phase_noalloc on caller-owned device buffers (pointers as integers)."""
+        self._check(self.lib.clr_mie_phase_noalloc(
+            self.h, C.c_void_p(diameter_ptr), C.c_void_p(n_real_ptr), C.c_void_p(k_imag_ptr), int(n_bins),
+            float(n_medium), float(wavelength_m), int(n_theta), C.c_void_p(qext_ptr), C.c_void_p(qsca_ptr),
+            C.c_void_p(asym_g_ptr), C.c_void_p(theta_ptr), C.c_void_p(phase_cdf_ptr),
+            C.c_void_p(stream_ptr) if stream_ptr else None), "clr_mie_phase_noalloc")
 
     def calibrate(self, which: int) -> float:
         v = C.c_double()
