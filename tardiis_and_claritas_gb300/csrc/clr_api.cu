@@ -202,6 +202,7 @@ int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sed
     CU(D(&pb.sed_major, 4));
     CU(D(&pb.sed_radial_log, (size_t)n * ss->n_radial));
     CU(D(&pb.sed_wr, (size_t)n * ss->n_radial));
+    CU(D(&pb.sed_terms, (size_t)n * ss->n_quad));
     const size_t grid_cells = (size_t)pb.grid_nr * pb.grid_nz * (sp.sediment_model == 3 ? n : 1);
     CU(D(&pb.sed_grid, grid_cells));
     cudaStream_t st = ctx->stream;

@@ -102,6 +102,7 @@ struct ParticleBuffers {
     double *trace_geom = nullptr, *trace_wave = nullptr;
     double *sedA = nullptr, *sedB = nullptr, *sed_norm = nullptr, *sed_max = nullptr, *sed_radial_log = nullptr,
            *sed_wr = nullptr, *sed_major = nullptr, *sed_grid = nullptr, *grid_max = nullptr;
+    double* sed_terms = nullptr;  // [n][n_quad] quadrature terms of the sediment normalisation
     int* err = nullptr;
     // node tables of the (r, z) field for the counter-based stream (sediment model 3, non-negative grid)
     int node_tables = 0;

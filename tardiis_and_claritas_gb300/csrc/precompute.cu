@@ -35,7 +35,14 @@ __device__ __forceinline__ cdx cd_div(cdx a, cdx b) {
 __device__ __forceinline__ double cd_abs2(cdx a) { return a.re * a.re + a.im * a.im; }
 __device__ __forceinline__ double cd_rmc(cdx a, cdx b) { return a.re * b.re + a.im * b.im; }
 
-// One warp per bin; lane 0 runs the recurrences (they are inherently serial). (:3495-3559)
+// One warp per bin (:3495-3559). The recurrences are serial and stay on lane 0: the downward
+// log-derivative recurrence D_{n-1} = n/z - 1/(D_n + n/z) and the upward Riccati-Bessel psi/chi
+// recurrences. Everything independent across orders is spread over the 32 lanes: the n/z quotients
+// before the downward recurrence, and the a_n, b_n quotients after it. The efficiency sums stay
+// serial on lane 0. Every value has the one-thread expression, and every sum its order.
+// Shared memory: D[0..nmx], n/z[0..nmx] (complex) and psi[0..nstop+1], chi[0..nstop+1] (real).
+constexpr size_t kMieSmem = (size_t)2 * (CLR_MIE_MAX_ORDER + 1) * sizeof(cdx) + (size_t)2 * (CLR_MIE_MAX_ORDER + 2) * sizeof(double);
+
 __global__ void __launch_bounds__(32) mie_coefficients_kernel(const double* __restrict__ diameter,
                                                               const double* __restrict__ n_real,
                                                               const double* __restrict__ k_imag, double n_medium,
@@ -45,13 +52,19 @@ __global__ void __launch_bounds__(32) mie_coefficients_kernel(const double* __re
                                                               double* qabs, double* qback, double* asym_g,
                                                               double* albedo, int* error_flag) {
     extern __shared__ cdx Dsh[];
+    cdx* NZ = Dsh + (CLR_MIE_MAX_ORDER + 1);
+    double* PSI = reinterpret_cast<double*>(NZ + (CLR_MIE_MAX_ORDER + 1));
+    double* CHI = PSI + (CLR_MIE_MAX_ORDER + 2);
     const int p = blockIdx.x;
-    if (p >= n_particles || threadIdx.x != 0) return;
+    const int lane = threadIdx.x;
+    if (p >= n_particles) return;
     double x = PD_PI * n_medium * diameter[p] / wavelength;
-    size_parameter[p] = x;
     if (!(x > 0.0) || !(n_real[p] > 0.0) || !(n_medium > 0.0) || !(wavelength > 0.0)) {
-        nstop_out[p] = 0; qext[p] = qsca[p] = qabs[p] = qback[p] = asym_g[p] = 0.0; albedo[p] = 1.0;
-        atomicCAS(error_flag, 0, 2);
+        if (lane == 0) {
+            size_parameter[p] = x;
+            nstop_out[p] = 0; qext[p] = qsca[p] = qabs[p] = qback[p] = asym_g[p] = 0.0; albedo[p] = 1.0;
+            atomicCAS(error_flag, 0, 2);
+        }
         return;
     }
     double mr = n_real[p] / n_medium, mi = k_imag[p] / n_medium;
@@ -60,21 +73,45 @@ __global__ void __launch_bounds__(32) mie_coefficients_kernel(const double* __re
     double mz = hypot(mr * x, mi * x);
     int nmx = (int)fmax((double)nstop, mz) + 128;
     if (nmx < nstop + 1) nmx = nstop + 1;
-    if (nmx >= CLR_MIE_MAX_ORDER || nstop >= CLR_MIE_MAX_ORDER) { nstop_out[p] = 0; atomicCAS(error_flag, 0, 1); return; }
-    nstop_out[p] = nstop;
-    Dsh[nmx] = CD(0.0, 0.0);
-    cdx z = CD(mr * x, mi * x);
-    for (int n = nmx; n >= 1; --n) {
-        cdx nz = cd_div(CD((double)n, 0.0), z);
-        cdx dn = Dsh[n];
-        Dsh[n - 1] = cd_sub(nz, cd_div(CD(1.0, 0.0), cd_add(dn, nz)));
+    if (nmx >= CLR_MIE_MAX_ORDER || nstop >= CLR_MIE_MAX_ORDER) {
+        if (lane == 0) { size_parameter[p] = x; nstop_out[p] = 0; atomicCAS(error_flag, 0, 1); }
+        return;
     }
-    double psi_nm1 = sin(x), psi_n = sin(x) / x - cos(x);
-    double chi_nm1 = cos(x), chi_n = cos(x) / x + sin(x);
-    cdx m = CD(mr, mi);
+    const cdx z = CD(mr * x, mi * x);
+    for (int n = 1 + lane; n <= nmx; n += 32) NZ[n] = cd_div(CD((double)n, 0.0), z);
+    __syncwarp();
+    if (lane == 0) {
+        size_parameter[p] = x;
+        nstop_out[p] = nstop;
+        Dsh[nmx] = CD(0.0, 0.0);
+        for (int n = nmx; n >= 1; --n) {
+            cdx nz = NZ[n];
+            cdx dn = Dsh[n];
+            Dsh[n - 1] = cd_sub(nz, cd_div(CD(1.0, 0.0), cd_add(dn, nz)));
+        }
+    }
+    __syncwarp();
+    // (2n+1)/x of every order, in the n/z space (no longer needed), for the upward recurrences
+    double* Q2X = reinterpret_cast<double*>(NZ);
+    for (int n = 1 + lane; n <= nstop; n += 32) Q2X[n] = (2.0 * n + 1.0) / x;
+    __syncwarp();
+    if (lane == 0) {
+        double psi_nm1 = sin(x), psi_n = sin(x) / x - cos(x);
+        double chi_nm1 = cos(x), chi_n = cos(x) / x + sin(x);
+        PSI[0] = psi_nm1; PSI[1] = psi_n; CHI[0] = chi_nm1; CHI[1] = chi_n;
+        for (int n = 1; n <= nstop; ++n) {
+            double psi_np1 = Q2X[n] * psi_n - psi_nm1;
+            double chi_np1 = Q2X[n] * chi_n - chi_nm1;
+            psi_nm1 = psi_n; psi_n = psi_np1; chi_nm1 = chi_n; chi_n = chi_np1;
+            PSI[n + 1] = psi_n; CHI[n + 1] = chi_n;
+        }
+    }
+    __syncwarp();
+    const cdx m = CD(mr, mi);
     double4* abp = reinterpret_cast<double4*>(ab) + (size_t)p * CLR_MIE_MAX_ORDER;
-    for (int j = 0; j < nstop; ++j) {
+    for (int j = lane; j < nstop; j += 32) {
         int n = j + 1;
+        const double psi_nm1 = PSI[n - 1], psi_n = PSI[n], chi_nm1 = CHI[n - 1], chi_n = CHI[n];
         cdx xi_nm1 = CD(psi_nm1, -chi_nm1), xi_n = CD(psi_n, -chi_n);
         cdx dn = Dsh[n];
         cdx ca = cd_add(cd_div(dn, m), CD((double)n / x, 0.0));
@@ -82,10 +119,18 @@ __global__ void __launch_bounds__(32) mie_coefficients_kernel(const double* __re
         cdx aa = cd_div(cd_sub(cd_scale(ca, psi_n), CD(psi_nm1, 0.0)), cd_sub(cd_mul(ca, xi_n), xi_nm1));
         cdx bb = cd_div(cd_sub(cd_scale(cb, psi_n), CD(psi_nm1, 0.0)), cd_sub(cd_mul(cb, xi_n), xi_nm1));
         abp[j] = make_double4(aa.re, aa.im, bb.re, bb.im);
-        double psi_np1 = ((2.0 * n + 1.0) / x) * psi_n - psi_nm1;
-        double chi_np1 = ((2.0 * n + 1.0) / x) * chi_n - chi_nm1;
-        psi_nm1 = psi_n; psi_n = psi_np1; chi_nm1 = chi_n; chi_n = chi_np1;
     }
+    // quotients of the efficiency sums, in the same space (Q2X is no longer needed):
+    // C1[n] = (2n+1)/(n(n+1)), C2[n] = n(n+2)/(n+1)
+    double* C1 = Q2X;
+    double* C2 = Q2X + (CLR_MIE_MAX_ORDER + 1);
+    for (int n = 1 + lane; n <= nstop; n += 32) {
+        const double cn = 2.0 * n + 1.0;
+        C1[n] = cn / ((double)n * (n + 1.0));
+        C2[n] = (double)n * (n + 2.0) / (n + 1.0);
+    }
+    __syncwarp();
+    if (lane != 0) return;
     double se = 0.0, ss = 0.0, sbr = 0.0, sbi = 0.0, t1 = 0.0, t2 = 0.0;
     for (int j = 0; j < nstop; ++j) {
         int n = j + 1;
@@ -97,11 +142,11 @@ __global__ void __launch_bounds__(32) mie_coefficients_kernel(const double* __re
         double sign = (n & 1) ? -1.0 : 1.0;
         sbr += cn * sign * (aa.re - bb.re);
         sbi += cn * sign * (aa.im - bb.im);
-        t2 += (cn / ((double)n * (n + 1.0))) * cd_rmc(aa, bb);
+        t2 += C1[n] * cd_rmc(aa, bb);
         if (j + 1 < nstop) {
             double4 q2 = abp[j + 1];
             cdx an = CD(q2.x, q2.y), bn = CD(q2.z, q2.w);
-            t1 += ((double)n * (n + 2.0) / (n + 1.0)) * (cd_rmc(aa, an) + cd_rmc(bb, bn));
+            t1 += C2[n] * (cd_rmc(aa, an) + cd_rmc(bb, bn));
         }
     }
     double x2 = x * x;
@@ -129,12 +174,24 @@ __global__ void theta_grid_kernel(double* theta, float* theta_f, int nt) {
 }
 
 #define PDF_GROUP 4
+constexpr size_t kPdfSmem = (size_t)CLR_MIE_MAX_ORDER * sizeof(double3);
 // S1/S2 -> 0.5(|S1|^2+|S2|^2) sin(theta) for PDF_GROUP bins at one angle (:3561-3581)
 __global__ void __launch_bounds__(128) phase_pdf_kernel(const double* __restrict__ theta, int nt, int n_particles,
                                                         const int* __restrict__ nstop, const double* __restrict__ ab,
                                                         double* __restrict__ pdf) {
+    // quotients of each order n = k + 1 (identical to evaluating them inline):
+    // (2n+1)/(n(n+1)), (2n+1)/n, (n+1)/n
+    extern __shared__ double3 QN[];  // [CLR_MIE_MAX_ORDER], dynamic (kPdfSmem bytes)
     const int j = blockDim.x * blockIdx.x + threadIdx.x;
     const int g0 = blockIdx.y * PDF_GROUP;
+    int kmax_blk = 0;
+    for (int g = 0; g < PDF_GROUP; ++g)
+        if (g0 + g < n_particles && nstop[g0 + g] > kmax_blk) kmax_blk = nstop[g0 + g];
+    for (int k = threadIdx.x; k < kmax_blk; k += blockDim.x) {
+        const double nf = (double)(k + 1);
+        QN[k] = make_double3((2.0 * nf + 1.0) / (nf * (nf + 1.0)), (2.0 * nf + 1.0) / nf, (nf + 1.0) / nf);
+    }
+    __syncthreads();
     if (j >= nt) return;
     double th = theta[j], mu = cos(th);
     double s1r[PDF_GROUP], s1i[PDF_GROUP], s2r[PDF_GROUP], s2i[PDF_GROUP];
@@ -152,7 +209,8 @@ __global__ void __launch_bounds__(128) phase_pdf_kernel(const double* __restrict
         int n = k + 1;
         double nf = (double)n;
         double tau = nf * mu * pi_n - (nf + 1.0) * pi_nm1;
-        double c = (2.0 * nf + 1.0) / (nf * (nf + 1.0));
+        const double3 qn = QN[k];  // the three quotients of order n, computed once per block above
+        double c = qn.x;
 #pragma unroll
         for (int g = 0; g < PDF_GROUP; ++g) {
             if (k < ns[g]) {
@@ -164,7 +222,7 @@ __global__ void __launch_bounds__(128) phase_pdf_kernel(const double* __restrict
                 s2i[g] += c * (ai * tau + bi * pi_n);
             }
         }
-        double pi_np1 = ((2.0 * nf + 1.0) / nf) * mu * pi_n - ((nf + 1.0) / nf) * pi_nm1;
+        double pi_np1 = qn.y * mu * pi_n - qn.z * pi_nm1;
         pi_nm1 = pi_n; pi_n = pi_np1;
     }
 #pragma unroll
@@ -176,35 +234,52 @@ __global__ void __launch_bounds__(128) phase_pdf_kernel(const double* __restrict
     }
 }
 
-// Serial trapezoid CDF per bin, normalised and forced monotone (:3583-3592); also the float copy.
-__global__ void phase_cdf_kernel(const double* __restrict__ theta, const double* __restrict__ pdf, int nt,
-                                 int n_particles, double* __restrict__ cdf, float* __restrict__ cdf_f, int* error_flag) {
-    int p = blockDim.x * blockIdx.x + threadIdx.x;
+// Trapezoid CDF per bin, normalised and forced monotone (:3583-3592); also the float copy. One warp per
+// bin: the trapezoid areas and the normalised values are independent per angle and spread over the
+// lanes; the prefix sum and the monotone clamp stay serial on lane 0, so every value is the serial one.
+__global__ void __launch_bounds__(32) phase_cdf_kernel(const double* __restrict__ theta, const double* __restrict__ pdf,
+                                                       int nt, int n_particles, double* __restrict__ cdf,
+                                                       float* __restrict__ cdf_f, int* error_flag) {
+    const int p = blockIdx.x;
+    const int lane = threadIdx.x;
     if (p >= n_particles) return;
-    long long base = (long long)p * nt;
-    cdf[base] = 0.0;
-    double s = 0.0;
-    for (int j = 1; j < nt; ++j) {
+    const long long base = (long long)p * nt;
+    for (int j = 1 + lane; j < nt; j += 32) {
         double area = 0.5 * (pdf[base + j] + pdf[base + j - 1]) * (theta[j] - theta[j - 1]);
         if (area < 0.0 && area > -1e-18) area = 0.0;
-        s += area;
-        cdf[base + j] = s;
+        cdf[base + j] = area;
     }
+    __syncwarp();
+    double s = 0.0;
+    if (lane == 0) {
+        cdf[base] = 0.0;
+        for (int j = 1; j < nt; ++j) {
+            s += cdf[base + j];
+            cdf[base + j] = s;
+        }
+    }
+    s = __shfl_sync(0xffffffffu, s, 0);
+    __syncwarp();
     if (!(s > 0.0) || !isfinite(s)) {
-        atomicCAS(error_flag, 0, 3);
-        for (int j = 0; j < nt; ++j) { cdf[base + j] = (double)j / (double)(nt - 1); cdf_f[base + j] = (float)cdf[base + j]; }
+        if (lane == 0) atomicCAS(error_flag, 0, 3);
+        for (int j = lane; j < nt; j += 32) { cdf[base + j] = (double)j / (double)(nt - 1); cdf_f[base + j] = (float)cdf[base + j]; }
         return;
     }
-    double prev = 0.0;
-    for (int j = 0; j < nt; ++j) {
-        double v = cdf[base + j] / s;
-        if (v < prev) v = prev;
-        if (v > 1.0) v = 1.0;
-        cdf[base + j] = v;
-        prev = v;
+    for (int j = lane; j < nt; j += 32) cdf[base + j] = cdf[base + j] / s;
+    __syncwarp();
+    if (lane == 0) {
+        double prev = 0.0;
+        for (int j = 0; j < nt; ++j) {
+            double v = cdf[base + j];
+            if (v < prev) v = prev;
+            if (v > 1.0) v = 1.0;
+            cdf[base + j] = v;
+            prev = v;
+        }
+        cdf[base + nt - 1] = 1.0;
     }
-    cdf[base + nt - 1] = 1.0;
-    for (int j = 0; j < nt; ++j) cdf_f[base + j] = (float)cdf[base + j];
+    __syncwarp();
+    for (int j = lane; j < nt; j += 32) cdf_f[base + j] = (float)cdf[base + j];
 }
 
 __global__ void dummy_phase_kernel(double* theta, float* theta_f, double* cdf, float* cdf_f, int n_particles) {
@@ -365,13 +440,21 @@ __global__ void sediment_slip_kernel(SedArgs a, const double* __restrict__ diame
     wr_out[(size_t)i * a.NRAD + j] = sn_velocity(w0, d, a.rho_w, a.mu, &re, &drag);
 }
 
-// Per-bin coefficients, radial potential and normalisation (:3958-4035); one thread per bin.
-__global__ void sediment_bin_kernel(SedArgs a, const double* __restrict__ diameter, const double* __restrict__ wr,
-                                    double* sedA, double* sedB, double* sed_norm, double* sed_max, double* radial_log,
-                                    int* error_flag) {
-    const int i = blockDim.x * blockIdx.x + threadIdx.x;
+// Per-bin coefficients, radial potential and normalisation (:3958-4035); one warp per bin. Lane 0 runs
+// the serial parts (slip velocity, prefix sums of the radial potential, the quadrature sum); the
+// quadrature terms, each an independent exp/expm1 evaluation, are computed by all lanes into `terms`
+// first, so every value and the order of every sum are those of the one-thread version.
+__global__ void __launch_bounds__(32) sediment_bin_kernel(SedArgs a, const double* __restrict__ diameter,
+                                                          const double* __restrict__ wr, double* sedA, double* sedB,
+                                                          double* sed_norm, double* sed_max, double* radial_log,
+                                                          double* __restrict__ terms, int* error_flag) {
+    const int i = blockIdx.x;
+    const int lane = threadIdx.x;
     if (i >= a.n) return;
-    if (a.TM == 0) { sedA[i] = 0.0; sedB[i] = 0.0; sed_norm[i] = 1.0; sed_max[i] = 1.0; return; }
+    if (a.TM == 0) {
+        if (lane == 0) { sedA[i] = 0.0; sedB[i] = 0.0; sed_norm[i] = 1.0; sed_max[i] = 1.0; }
+        return;
+    }
     double R2, a2, Hinf, hbar, omega2, fR;
     sed_geometry(a, &R2, &a2, &Hinf, &hbar, &omega2, &fR);
     const double R = a.R, ZMIN = a.ZMIN, ZMEAN = a.ZMEAN, DH = a.DH;
@@ -383,38 +466,42 @@ __global__ void sediment_bin_kernel(SedArgs a, const double* __restrict__ diamet
     double sre = 0.0, sdrag = 1.0;
     double ws = (TM == 2 || TM == 3) ? sn_velocity(ws0, d, a.rho_w, a.mu, &sre, &sdrag) : ws0;
     double Bc = ws / a.Dt;
-    sedB[i] = Bc;
     double* RL = radial_log + (size_t)i * NRAD;
-    if (TM == 1) {
-        double Ac = tau * omega2 * ((FSM == 2) ? a2 : 1.0) / (2.0 * a.Dt);
-        sedA[i] = Ac;
-        for (int j = 0; j < NRAD; ++j) {
-            double r = (double)j * drad, rr2 = r * r, f = (FSM == 2) ? rr2 / (a2 + rr2) : rr2;
-            RL[j] = Ac * (f - fR);
+    const double Ac = tau * omega2 * ((FSM == 2) ? a2 : 1.0) / (2.0 * a.Dt);
+    if (lane == 0) {
+        sedB[i] = Bc;
+        if (TM == 1) {
+            sedA[i] = Ac;
+            for (int j = 0; j < NRAD; ++j) {
+                double r = (double)j * drad, rr2 = r * r, f = (FSM == 2) ? rr2 / (a2 + rr2) : rr2;
+                RL[j] = Ac * (f - fR);
+            }
+        } else {
+            const double* W = wr + (size_t)i * NRAD;
+            double total = 0.0, prev = 0.0;
+            for (int j = 0; j < NRAD; ++j) {
+                double w = W[j];
+                if (j > 0) total += 0.5 * (prev + w) * drad;
+                prev = w;
+            }
+            double cum = 0.0;
+            prev = 0.0;
+            for (int j = 0; j < NRAD; ++j) {
+                double w = W[j];
+                if (j > 0) cum += 0.5 * (prev + w) * drad;
+                prev = w;
+                double psi = (cum - total) / a.Dt;
+                if (psi > 0.0) psi = 0.0;
+                RL[j] = psi;
+            }
+            RL[NRAD - 1] = 0.0;
+            sedA[i] = (fR > 0.0) ? -RL[0] / fR : 0.0;
         }
-    } else {
-        const double* W = wr + (size_t)i * NRAD;
-        double total = 0.0, prev = 0.0;
-        for (int j = 0; j < NRAD; ++j) {
-            double w = W[j];
-            if (j > 0) total += 0.5 * (prev + w) * drad;
-            prev = w;
-        }
-        double cum = 0.0;
-        prev = 0.0;
-        for (int j = 0; j < NRAD; ++j) {
-            double w = W[j];
-            if (j > 0) cum += 0.5 * (prev + w) * drad;
-            prev = w;
-            double psi = (cum - total) / a.Dt;
-            if (psi > 0.0) psi = 0.0;
-            RL[j] = psi;
-        }
-        RL[NRAD - 1] = 0.0;
-        sedA[i] = (fR > 0.0) ? -RL[0] / fR : 0.0;
     }
-    double integ = 0.0;
-    for (int j = 0; j < NQ; ++j) {
+    __syncwarp();
+    const double A_i = (TM == 1) ? Ac : ((fR > 0.0) ? -RL[0] / fR : 0.0);
+    double* T = terms + (size_t)i * NQ;
+    for (int j = lane; j < NQ; j += 32) {
         double r = ((double)j + 0.5) * dr, rr2 = r * r;
         double zsurf = ZMEAN;
         if (FSM == 1 && DH > 0.0) zsurf = ZMEAN + DH * (rr2 / R2 - 0.5);
@@ -423,7 +510,7 @@ __global__ void sediment_bin_kernel(SedArgs a, const double* __restrict__ diamet
         double rl;
         if (TM == 1) {
             double f = (FSM == 2) ? rr2 / (a2 + rr2) : rr2;
-            rl = sedA[i] * (f - fR);
+            rl = A_i * (f - fR);
         } else {
             double u = r / R * (double)(NRAD - 1);
             int k = (int)floor(u);
@@ -435,15 +522,18 @@ __global__ void sediment_bin_kernel(SedArgs a, const double* __restrict__ diamet
         }
         double radial = exp(rl);
         double iz = (fabs(Bc) < 1e-14) ? radial * Hh : radial * (-expm1(-Bc * Hh)) / Bc;
-        integ += r * iz;
+        T[j] = r * iz;
     }
+    __syncwarp();
+    if (lane != 0) return;
+    double integ = 0.0;
+    for (int j = 0; j < NQ; ++j) integ += T[j];
     double norm = (2.0 / (R2 * Hmean)) * integ * dr;
     if (!(norm > 0.0) || !isfinite(norm)) { atomicCAS(error_flag, 0, 34); return; }
     sed_norm[i] = norm;
     sed_max[i] = 1.0 / norm;
 }
 
-// Majorants in bin order (:4029-4036; grid model :4203-4220 on an all-active supplied grid).
 // Per-bin maximum of the (r, z) grid (the max of non-negative terms starting at 0, as the reference's
 // serial scan, so the order of the reduction does not change the value). One block per bin.
 __global__ void sediment_grid_max_kernel(const double* __restrict__ grid, long long plane, double* grid_max) {
@@ -551,15 +641,17 @@ cudaError_t enqueue_mie_phase(const double* d, const double* nr, const double* k
                               double wavelength, int nt, const MiePhaseBuffers& b, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(b.err, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
-    const size_t smem = (size_t)(CLR_MIE_MAX_ORDER + 1) * sizeof(cdx);
+    const size_t smem = kMieSmem;
     e = cudaFuncSetAttribute(mie_coefficients_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(phase_pdf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPdfSmem);
     if (e != cudaSuccess) return e;
     mie_coefficients_kernel<<<n, 32, smem, st>>>(d, nr, k, n_medium, wavelength, n, b.ab, b.nstop, b.x, b.qext,
                                                  b.qsca, b.qabs, b.qback, b.g, b.albedo, b.err);
     theta_grid_kernel<<<(nt + 127) / 128, 128, 0, st>>>(b.theta, b.theta_f, nt);
     dim3 grid((nt + 127) / 128, (n + PDF_GROUP - 1) / PDF_GROUP);
-    phase_pdf_kernel<<<grid, 128, 0, st>>>(b.theta, nt, n, b.nstop, b.ab, b.pdf);
-    phase_cdf_kernel<<<(n + 63) / 64, 64, 0, st>>>(b.theta, b.pdf, nt, n, b.cdf, b.cdf_f, b.err);
+    phase_pdf_kernel<<<grid, 128, kPdfSmem, st>>>(b.theta, nt, n, b.nstop, b.ab, b.pdf);
+    phase_cdf_kernel<<<n, 32, 0, st>>>(b.theta, b.pdf, nt, n, b.cdf, b.cdf_f, b.err);
     return cudaGetLastError();
 }
 
@@ -570,8 +662,10 @@ cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_par
     double* ab = ab_scratch ? ab_scratch : pb.ab;
     e = cudaMemsetAsync(pb.err, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
-    const size_t smem = (size_t)(CLR_MIE_MAX_ORDER + 1) * sizeof(cdx);
+    const size_t smem = kMieSmem;
     e = cudaFuncSetAttribute(mie_coefficients_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(phase_pdf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPdfSmem);
     if (e != cudaSuccess) return e;
     mie_coefficients_kernel<<<n, 32, smem, st>>>(pb.d, pb.nidx, pb.kidx, ps.n_medium, ps.wavelength_m, n, ab, pb.nstop,
                                                  pb.x, pb.qext, pb.qsca, pb.qabs, pb.qback, pb.g, pb.albedo, pb.err);
@@ -580,8 +674,8 @@ cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_par
         const int nt = pb.nt;
         theta_grid_kernel<<<(nt + 127) / 128, 128, 0, st>>>(pb.theta, pb.theta_f, nt);
         dim3 grid((nt + 127) / 128, (n + PDF_GROUP - 1) / PDF_GROUP);
-        phase_pdf_kernel<<<grid, 128, 0, st>>>(pb.theta, nt, n, pb.nstop, ab, pb.pdf);
-        phase_cdf_kernel<<<(n + 63) / 64, 64, 0, st>>>(pb.theta, pb.pdf, nt, n, pb.phase_cdf, pb.phase_cdf_f, pb.err);
+        phase_pdf_kernel<<<grid, 128, kPdfSmem, st>>>(pb.theta, nt, n, pb.nstop, ab, pb.pdf);
+        phase_cdf_kernel<<<n, 32, 0, st>>>(pb.theta, pb.pdf, nt, n, pb.phase_cdf, pb.phase_cdf_f, pb.err);
     } else {
         dummy_phase_kernel<<<(n + 127) / 128, 128, 0, st>>>(pb.theta, pb.theta_f, pb.phase_cdf, pb.phase_cdf_f, n);
     }
@@ -599,8 +693,8 @@ cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_par
         dim3 g((a.NRAD + 127) / 128, n);
         sediment_slip_kernel<<<g, 128, 0, st>>>(a, pb.d, pb.sed_wr);
     }
-    sediment_bin_kernel<<<(n + 63) / 64, 64, 0, st>>>(a, pb.d, pb.sed_wr, pb.sedA, pb.sedB, pb.sed_norm, pb.sed_max,
-                                                     pb.sed_radial_log, pb.err);
+    sediment_bin_kernel<<<n, 32, 0, st>>>(a, pb.d, pb.sed_wr, pb.sedA, pb.sedB, pb.sed_norm, pb.sed_max,
+                                          pb.sed_radial_log, pb.sed_terms, pb.err);
     if (a.TM == 3)
         sediment_grid_max_kernel<<<n, 256, 0, st>>>(pb.sed_grid, (long long)pb.grid_nr * pb.grid_nz, pb.grid_max);
     sediment_majorant_kernel<<<1, 1, 0, st>>>(a, pb.trace_geom, pb.trace_wave, pb.sedA, pb.sed_norm, pb.sed_max,
