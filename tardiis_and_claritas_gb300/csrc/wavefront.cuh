@@ -42,7 +42,7 @@ static_assert(WQ_FIN + 1 == CLR_WQ_COUNT, "queue count");
 
 constexpr int kWaveThreads = 256;
 // water flights per FLIGHT visit before the photon is re-queued (bounds lane imbalance in a warp)
-constexpr int kFlightSteps = 8;
+constexpr int kFlightSteps = 4;
 // Rare stages (few photons per pass, long serial work per photon) run only when their queue holds a
 // full batch, after kMaxSkips passes, or while the pool drains.
 constexpr unsigned kRareBatch = 8192;
