@@ -6,8 +6,11 @@ library's persistent photon kernel (transport + detector scoring + tallies in
 one launch). Photon counts are the same for GPU and CPU arms and both run the
 same estimator, so equal photon counts mean equal tally error.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload full|small]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload full|small|sweep]
   python bench.py --impl reference ...   # the reference's own CPU implementation
+
+With --workload sweep a step builds and traces the 512-scenario batched sweep (per-scenario Mie
+tables, rates and photon counts log-uniform over 1e5-1e7) and the metric is scenarios/s.
 
 Multi-GPU (torchrun, one rank per GPU): replicas over disjoint photon ranges
 (counter-based Philox streams), no data-path collective; value = all photons /
@@ -32,7 +35,7 @@ sys.path.insert(0, ROOT)
 # stage kernel of one ncu capture of a 4e6-photon trace (see profiles/wavefront_stages_full_scene.md):
 # warp instructions issued, FP64 flops executed (DFMA counted as 2) and DRAM bytes read + written.
 # The issue-slot roofline divides warp instructions issued per second by 4 schedulers x SMs x clock.
-PER_PHOTON = {"full": {"warp_inst": 495.5, "fp64_flops": 17.1, "dram_bytes": 850.1}, "small": None}
+PER_PHOTON = {"full": {"warp_inst": 495.5, "fp64_flops": 17.1, "dram_bytes": 850.1}, "small": None, "sweep": None}
 
 
 def workload(name: str):
@@ -54,6 +57,148 @@ def workload_config(name: str, n: int, rng: str) -> dict:
     return {"workload": "small plain MC: 64 lognormal quartz bins (median 20 um, sigma_g 1.6) at 100 mg/L, uniform, "
                         "flat surface, r=12.5 mm cell, Mie tables 1801 angles, 860 nm",
             "photons_per_step": n, "rng": rng, "l2": "flushed between steps (256 MiB write)"}
+
+
+SWEEP_SCENARIOS = 512
+SWEEP_WORKLOAD = ("batched sweep: 512 scenarios in the r=12.5 mm cell (40 mm water), seeds 0..511, sampled with "
+                  "numpy PCG64(0): photons log-uniform 1e5-1e7, concentration log-uniform 1-1e4 mg/L, median "
+                  "diameter log-uniform 2-200 um, sigma_g U(1.2,2.0), stirrer rpm U(0,1200) (localized-vortex "
+                  "surface, 5 mm core), particle index U(1.50,1.60); 64 lognormal bins over 1-200 um, FP64 Mie "
+                  "phase tables (1801 angles) per scenario, 860 nm, uniform sediment")
+
+
+def optical_depth_proxy(sc) -> float:
+    """Radius x extinction of the scenario's particles with Q_ext = 2 (a ranking key for CPU cost)."""
+    p = sc.particles
+    w = p.weight / p.weight.sum()
+    return 1.5 * 2.0 * p.concentration_kg_m3 / p.density_kg_m3 * float((w / p.diameter_m).sum()) * \
+        sc.cfg.tube_inner_radius_m
+
+
+def sweep_cpu_estimate(scs: list, threads: int, seconds: float, n_sample: int = 16):
+    """Scenarios/s of the reference's CPU path on a bounded sample of the sweep. The scenarios are ranked
+    by optical depth and n_sample of them, evenly spaced in that ranking (the densest included), are
+    prepared (particle precompute, timed) and traced on a photon sample (timed). Every scenario of the
+    sweep is then charged the precompute time and per-photon time of the sampled scenario nearest to it
+    in the ranking, times its own photon count; the rate is scenarios over the summed time."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_harness as H
+    from tardiis_and_claritas_gb300 import scene as S
+    kind = "reference" if H.reference_available() else "port"
+    order = sorted(range(len(scs)), key=lambda i: optical_depth_proxy(scs[i]))
+    m_s = min(n_sample, len(scs))
+    ranks = sorted({round(k * (len(scs) - 1) / max(m_s - 1, 1)) for k in range(m_s)})
+    idx = [order[r] for r in ranks]
+    budget = seconds / len(idx)
+    traced, cost = 0, {}
+    for i in idx:
+        sc = scs[i]
+        t0 = time.perf_counter()
+        o = H.OracleRun(kind, sc.cfg, sc.particles)
+        t_prep = time.perf_counter() - t0
+        # grow the photon sample until it takes about its share of the time budget (or is the whole run)
+        m = min(sc.n_photons, 2000)
+        while True:
+            t1 = time.perf_counter()
+            o.trace(S.run_params(m, seed=sc.seed + 7), threads=threads)
+            dt = time.perf_counter() - t1
+            if m >= sc.n_photons or dt >= 0.5 * budget:
+                break
+            m = int(min(sc.n_photons, m * min(8.0, max(2.0, budget / max(dt, 1e-4)))))
+        o.close()
+        traced += m
+        cost[i] = (t_prep, dt / m)
+    total = 0.0
+    for r, i in enumerate(order):
+        near = idx[min(range(len(ranks)), key=lambda k: abs(ranks[k] - r))]
+        t_prep, t_photon = cost[near]
+        total += t_prep + scs[i].n_photons * t_photon
+    return {"value": len(scs) / total, "unit": "scenarios/s", "cores": threads, "kind": kind,
+            "sample": f"{len(idx)} of {len(scs)} scenarios spread over the optical-depth ranking: precompute "
+                      f"timed, {traced} photons traced; each scenario charged the nearest sampled scenario's "
+                      f"precompute and per-photon time times its own photon count"}
+
+
+def run_sweep(args, ctx, rank: int, world: int, local_rank: int, dist, dev) -> dict:
+    """The batched sweep: one step = clr_sweep_build + clr_sweep_trace of every scenario."""
+    import numpy as np
+    import torch
+    from tardiis_and_claritas_gb300 import abi, scene as S
+    scs = S.sweep_workload(SWEEP_SCENARIOS, sampler_seed=rank)
+    scenes, parts, seds = S.sweep_specs(scs)
+    n_photons = sum(sc.n_photons for sc in scs)
+    rng_mode = abi.RNG_PHILOX if args.rng == "philox" else abi.RNG_REFERENCE_XORSHIFT
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def runs(step: int):
+        return [S.run_params(sc.n_photons, seed=sc.seed + 1000 * step, rng_mode=rng_mode, scenario_id=i)
+                for i, sc in enumerate(scs)]
+
+    for w in range(args.warmup):
+        ctx.sweep_build(scenes, parts, seds)
+        ctx.sweep_trace(runs(w))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier(device_ids=[local_rank])
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    build_ms, trace_ms, walls = [], [], []
+    launches = passes = 0
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.sweep_build(scenes, parts, seds)
+        build_ms.append(ctx.last_kernel_ms())
+        T = ctx.sweep_trace(runs(args.warmup + k))
+        trace_ms.append(ctx.last_kernel_ms())
+        walls.append(time.perf_counter() - t0)
+        nl, npass = ctx.last_launches()
+        launches += nl
+        passes += npass
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    dev_ms = float(sum(build_ms) + sum(trace_ms))
+    wall_s = float(sum(walls))
+    if dist:
+        t = torch.tensor([dev_ms, wall_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms, wall_s = float(t[0].item()), float(t[1].item())
+    value = world * SWEEP_SCENARIOS * args.steps / (dev_ms * 1e-3)
+    e2e = world * SWEEP_SCENARIOS * args.steps / wall_s
+    h2d = sum(int(p.n_bins) * (4 * 8 + 2 * 8 + 1) for p in parts) + SWEEP_SCENARIOS * (
+        abi.C.sizeof(abi.SceneParams) + abi.C.sizeof(abi.RunParams) + 8)
+    d2h = SWEEP_SCENARIOS * (abi.C.sizeof(abi.Tallies) + 8 * 8 + 4 * 8 + 4) + 4
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    sm_mhz = measured_peaks().get("sm_max_mhz") or 2070.0
+    issue_peak = 4.0 * sms * sm_mhz * 1e6
+    per = PER_PHOTON.get("sweep") if rng_mode == abi.RNG_PHILOX else None
+    trace_s = float(sum(trace_ms)) * 1e-3 / args.steps
+    roofline = {"bound": "issue", "unit": "Twarp-inst/s", "peak": issue_peak / 1e12,
+                "peak_source": f"4 warp schedulers x {sms} SMs x {sm_mhz:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json)",
+                "achieved": None, "frac": None, "traffic": None,
+                "dominant": "the sweep's trace: all wavefront stage kernels over every scenario's photons"}
+    if per:
+        ach = per["warp_inst"] * n_photons / trace_s
+        roofline.update({"achieved": ach / 1e12, "frac": ach / issue_peak, "traffic": per["dram_bytes"] * n_photons,
+                         "traffic_unit": "bytes per sweep trace (ncu dram__bytes_read+write, scaled by photons)"})
+    line = {"metric": "scenarios/s (at fixed tally error)", "value": value, "unit": "scenarios/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 transport, f64 Mie",
+            "data": "synthetic (seeded)",
+            "config": {"workload": SWEEP_WORKLOAD, "scenarios": SWEEP_SCENARIOS, "photons_per_step": n_photons,
+                       "rng": args.rng, "l2": "flushed between steps (256 MiB write); tables exceed L2"},
+            "e2e": {"value": e2e, "unit": "scenarios/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "steps": args.steps,
+                    "includes": "host wall time of clr_sweep_build (scenario upload, batched Mie/phase tables, rates) "
+                                "+ clr_sweep_trace (all scenarios, tallies to host)"},
+            "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline,
+            "sweep": {"build_ms": float(np.mean(build_ms)), "trace_ms": float(np.mean(trace_ms)),
+                      "photons_per_s": n_photons / trace_s, "passes_per_trace": passes / args.steps,
+                      "detected_native_total": int(sum(int(t["hw_native"].sum()) for t in T))}}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = sweep_cpu_estimate(scs, os.cpu_count() or 1, args.cpu_seconds)
+    return line
 
 
 def measured_peaks() -> dict:
@@ -142,6 +287,23 @@ def run_reference_arm(args, rank: int, world: int):
         return
     threads = os.cpu_count() or 1
     name = args.workload
+    if name == "sweep":
+        from tardiis_and_claritas_gb300 import scene as S
+        scs = S.sweep_workload(SWEEP_SCENARIOS)
+        for _ in range(args.warmup):
+            sweep_cpu_estimate(scs[:1], threads, 1.0)
+        vals = [sweep_cpu_estimate(scs, threads, args.cpu_seconds) for _ in range(args.steps)]
+        value = sum(v["value"] for v in vals) / len(vals)
+        cpu = dict(vals[-1], value=value)
+        line = {"impl": "reference", "metric": "scenarios/s (at fixed tally error)", "value": value,
+                "unit": "scenarios/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32/f64", "data": "synthetic (seeded)",
+                "config": {"workload": SWEEP_WORKLOAD, "scenarios": SWEEP_SCENARIOS, "rng": "reference xorshift"},
+                "cpu_baseline": cpu,
+                "e2e": {"value": value, "unit": "scenarios/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     _, _, _, _, n_gpu = workload(name)
     ref = CpuReference(name, threads)
     n = ref.sample_size(args.cpu_seconds)
@@ -167,7 +329,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["full", "small"], default="full")
+    ap.add_argument("--workload", choices=["full", "small", "sweep"], default="full")
     ap.add_argument("--rng", choices=["philox", "xorshift"], default="philox")
     ap.add_argument("--photons", type=int, default=0, help="override photons per step")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
@@ -199,6 +361,15 @@ def main():
     if dist:
         dist.barrier(device_ids=[local_rank])
     ctx = L.Context(local_rank)
+    if args.workload == "sweep":
+        line = run_sweep(args, ctx, rank, world, local_rank, dist, dev)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        ctx.close()
+        if dist:
+            dist.barrier(device_ids=[local_rank])
+            dist.destroy_process_group()
+        return
     cfg, parts, grid, zmax, n = workload(args.workload)
     if args.photons:
         n = args.photons

@@ -300,11 +300,30 @@ int clr_trace(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray
  * when the caller wants per-batch tallies (batch jackknife, CLARITAS/CLARITAS.py:5244, :7638-7862). */
 int clr_trace_batch(clr_ctx* ctx, const clr_run_params* runs, int n_runs, clr_tallies* outs);
 
+/* Scenario sweep (the batched-sweep caller of the reference, run_one_case over many scenarios,
+ * CLARITAS/CLARITAS.py:13020): builds the particle tables of n_scenarios scenes, each with its own
+ * scene parameters, particles and sediment (scenes[i], particles[i], sediments[i]), with the
+ * arithmetic of clr_set_scene + clr_build_particles, so every scenario's tables equal those of a
+ * single build. The Mie coefficient and phase-table kernels run over the bins of many scenarios per
+ * launch. Replaces the previous sweep of the context (the current single scene is not touched).
+ * Errors name the first failing scenario; a precompute error code applies to the whole sweep. */
+int clr_sweep_build(clr_ctx* ctx, int n_scenarios, const clr_scene_params* scenes, const clr_particle_spec* particles,
+                    const clr_sediment_spec* sediments);
+
+/* Trace every scenario of the built sweep in one engine execution: runs[i] (photon count, seeds,
+ * ray offset) traces scenario i, tallies into outs[i]; n_runs must equal the sweep's scenario count
+ * and the runs share rng_mode, weight_mode and flags. */
+int clr_sweep_trace(clr_ctx* ctx, const clr_run_params* runs, int n_runs, clr_tallies* outs);
+
+/* clr_read_particle_physics for scenario `scenario` of the built sweep. */
+int clr_sweep_read_particle_physics(clr_ctx* ctx, int scenario, clr_particle_physics* out);
+
 /* Same as clr_trace with HOST-resident record memory (copied back inside the call). */
 int clr_trace_host_records(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* host_records);
 
-/* Device time of the photon transport in the last clr_trace call, measured with CUDA events
- * recorded on the context's stream around its launches (milliseconds). No reference counterpart. */
+/* Device time of the photon transport in the last clr_trace* / clr_sweep_trace call, or of the
+ * precompute in the last clr_sweep_build, measured with CUDA events recorded on the context's stream
+ * around its launches and copies (milliseconds). No reference counterpart. */
 int clr_last_kernel_ms(const clr_ctx* ctx, float* ms);
 
 /* Kernel launches of the last clr_trace call (the wavefront engine launches one graph of 12 kernel

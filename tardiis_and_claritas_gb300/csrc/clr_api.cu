@@ -46,6 +46,14 @@ struct clr_ctx {
     int last_passes = 0;
     long long last_launches = 0;
     int run_cap = 0;  // runs the per-run buffers hold
+    // scenario sweep (clr_sweep_build): scene parameters and tables of every scenario, carved from one
+    // arena; the Mie scratch (a_n/b_n rows and phase pdf of one chunk of bins) is kept between builds
+    std::vector<clr_scene_params> sw_sp;
+    std::vector<ParticleBuffers> sw_pb;
+    void* sw_arena = nullptr;
+    size_t sw_arena_bytes = 0;
+    void* sw_scratch = nullptr;
+    size_t sw_scratch_bytes = 0;
 };
 
 static int fail(clr_ctx* c, int code, const char* fmt, ...) {
@@ -120,6 +128,8 @@ int clr_destroy(clr_ctx* ctx) {
     cudaFree(ctx->wave_q);
     cudaFree(ctx->wave_ctl);
     cudaFree(ctx->wave_begin);
+    cudaFree(ctx->sw_arena);
+    cudaFree(ctx->sw_scratch);
     if (ctx->wave_live) cudaFreeHost(ctx->wave_live);
     if (ctx->wave_ev) cudaEventDestroy(ctx->wave_ev);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -129,9 +139,9 @@ int clr_destroy(clr_ctx* ctx) {
     return CLR_OK;
 }
 
-int clr_set_scene(clr_ctx* ctx, const clr_scene_params* scene) {
-    if (!ctx || !scene) return CLR_ERR_INVALID_ARGUMENT;
-    const clr_scene_params& s = *scene;
+}  // extern "C"
+
+static int check_scene(clr_ctx* ctx, const clr_scene_params& s) {
     if (!(0 < s.rin && s.rin < s.rout && s.rout < s.ring_in && s.ring_in < s.throat_out &&
           s.throat_out <= s.source_r && s.source_r <= s.ring_out))
         return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "TARDIIS radial/source geometry is inconsistent");
@@ -142,25 +152,23 @@ int clr_set_scene(clr_ctx* ctx, const clr_scene_params* scene) {
         return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "model code out of range");
     if (s.source_kind != CLR_SOURCE_REFERENCE_LED && s.source_kind != CLR_SOURCE_COLLIMATED_DISC)
         return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "unknown source_kind %d", s.source_kind);
-    ctx->sp = s;
-    ctx->scene_set = true;
-    ctx->built = false;
     return CLR_OK;
 }
 
-int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sediment_spec* ss) {
-    if (!ctx || !ps || !ss) return CLR_ERR_INVALID_ARGUMENT;
-    if (!ctx->scene_set) return fail(ctx, CLR_ERR_NOT_READY, "clr_set_scene must be called first");
+static bool hybrid_model(const clr_scene_params& sp) {
+    return sp.event_model == 3 || sp.event_model == 4 || sp.event_model == 5;
+}
+
+// Argument checks of a particle build for scene sp (including the reference's sediment precompute
+// error codes 31-33, :3958-3967).
+static int check_particles(clr_ctx* ctx, const clr_scene_params& sp, const clr_particle_spec* ps,
+                           const clr_sediment_spec* ss) {
     const int n = ps->n_bins;
     if (n < 1 || n > CLR_MAX_BINS) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "n_bins must be 1..%d", CLR_MAX_BINS);
-    const clr_scene_params& sp = ctx->sp;
-    const bool hybrid = sp.event_model == 3 || sp.event_model == 4 || sp.event_model == 5;
-    const int nt = hybrid ? ps->n_theta : 2;
-    if (hybrid && nt < 257) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "n_theta must be >= 257");
+    if (hybrid_model(sp) && ps->n_theta < 257) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "n_theta must be >= 257");
     if (!ps->diameter_m || !ps->weight || !ps->n_real || !ps->k_imag)
         return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "particle arrays must not be null");
     if (ss->n_radial < 65 || ss->n_quad < 64) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "sediment lookup sizes too small");
-    // sediment precompute argument checks (error codes 31-33 of the reference kernel, :3958-3967)
     if (sp.sediment_model != 0) {
         if (!(ss->particle_density > ss->water_density) || !(ss->water_density > 0.0) || !(ss->water_viscosity > 0.0) ||
             !(ss->gravity > 0.0) || !(ss->eddy_diffusivity > 0.0) || !(sp.rin > 0.0f))
@@ -173,6 +181,41 @@ int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sed
         if (sp.sediment_model == 3 && (!ss->grid || ss->grid_nr < 2 || ss->grid_nz < 2))
             return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "sediment model 3 needs a [bins][nr][nz] grid");
     }
+    return CLR_OK;
+}
+
+// Node tables pay off (and are exact) for a model-3 grid with no negative value and a moderate size.
+static bool wants_node_tables(const clr_scene_params& sp, const clr_sediment_spec& ss, int n, size_t grid_cells) {
+    if (sp.sediment_model != 3) return false;
+    bool nonneg = ss.grid_zmax > (double)sp.zmin;
+    for (size_t c = 0; c < grid_cells && nonneg; ++c) nonneg = ss.grid[c] >= 0.0;
+    const size_t plane = (size_t)ss.grid_nr * ss.grid_nz;
+    return nonneg && 2 * plane * n * sizeof(int2) <= (size_t(1) << 30);
+}
+
+extern "C" {
+
+int clr_set_scene(clr_ctx* ctx, const clr_scene_params* scene) {
+    if (!ctx || !scene) return CLR_ERR_INVALID_ARGUMENT;
+    const clr_scene_params& s = *scene;
+    const int rc = check_scene(ctx, s);
+    if (rc != CLR_OK) return rc;
+    ctx->sp = s;
+    ctx->scene_set = true;
+    ctx->built = false;
+    return CLR_OK;
+}
+
+int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sediment_spec* ss) {
+    if (!ctx || !ps || !ss) return CLR_ERR_INVALID_ARGUMENT;
+    if (!ctx->scene_set) return fail(ctx, CLR_ERR_NOT_READY, "clr_set_scene must be called first");
+    const clr_scene_params& sp = ctx->sp;
+    {
+        const int rc = check_particles(ctx, sp, ps, ss);
+        if (rc != CLR_OK) return rc;
+    }
+    const int n = ps->n_bins;
+    const int nt = hybrid_model(sp) ? ps->n_theta : 2;
     CU(cudaSetDevice(ctx->device));
     free_particles(ctx);
     ParticleBuffers& pb = ctx->pb;
@@ -223,10 +266,8 @@ int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sed
     CU(cudaMemcpyAsync(pb.moment_b, mb.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(pb.moment_mode, mm.data(), n, cudaMemcpyHostToDevice, st));
     if (sp.sediment_model == 3) {
-        bool nonneg = ss->grid_zmax > (double)sp.zmin;
-        for (size_t c = 0; c < grid_cells && nonneg; ++c) nonneg = ss->grid[c] >= 0.0;
         const size_t plane = (size_t)pb.grid_nr * pb.grid_nz;
-        if (nonneg && 2 * plane * n * sizeof(int2) <= (size_t(1) << 30)) {
+        if (wants_node_tables(sp, *ss, n, grid_cells)) {
             pb.node_tables = 1;
             CU(dalloc(ctx, (void**)&pb.node_mu, plane * sizeof(float2)));
             CU(dalloc(ctx, (void**)&pb.node_alias, 2 * plane * n * sizeof(int2)));
@@ -250,10 +291,9 @@ int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sed
     return CLR_OK;
 }
 
-int clr_read_particle_physics(clr_ctx* ctx, clr_particle_physics* o) {
-    if (!ctx || !o) return CLR_ERR_INVALID_ARGUMENT;
-    if (!ctx->built) return fail(ctx, CLR_ERR_NOT_READY, "particles not built");
-    const ParticleBuffers& pb = ctx->pb;
+}  // extern "C"
+
+static int read_physics(clr_ctx* ctx, const ParticleBuffers& pb, clr_particle_physics* o) {
     const int n = pb.n;
     CU(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
@@ -276,13 +316,16 @@ int clr_read_particle_physics(clr_ctx* ctx, clr_particle_physics* o) {
     return CLR_OK;
 }
 
-}  // extern "C"
+extern "C" int clr_read_particle_physics(clr_ctx* ctx, clr_particle_physics* o) {
+    if (!ctx || !o) return CLR_ERR_INVALID_ARGUMENT;
+    if (!ctx->built) return fail(ctx, CLR_ERR_NOT_READY, "particles not built");
+    return read_physics(ctx, ctx->pb, o);
+}
 
 // Fill the device scene description for the current tables and a run.
-static void fill_scene(const clr_ctx* ctx, const clr_run_params* run, DevScene* s) {
-    const ParticleBuffers& pb = ctx->pb;
+static void fill_scene(const clr_scene_params& sp, const ParticleBuffers& pb, const clr_run_params* run, DevScene* s) {
     memset(s, 0, sizeof *s);
-    s->P = ctx->sp;
+    s->P = sp;
     s->gcdf = pb.gcdf_f; s->wcdf = pb.wcdf_f; s->phase_cdf = pb.phase_cdf_f; s->theta = pb.theta_f;
     s->pn = pb.pn_f; s->pk = pb.pk_f; s->prad = pb.prad_f;
     s->k = pb.kidx; s->qsca = pb.qsca; s->qext = pb.qext;
@@ -341,7 +384,7 @@ static int wave_pool_ready(clr_ctx* ctx) {
     CU(cudaMalloc(&ctx->wave_meta, (size_t)cap * sizeof(SlotMeta)));
     CU(cudaMalloc(&ctx->wave_q, (size_t)CLR_WQ_COUNT * 2 * cap * sizeof(uint32_t)));  // rings of 2 * cap
     CU(cudaMalloc(&ctx->wave_ctl, sizeof(WaveCtl)));
-    CU(cudaHostAlloc((void**)&ctx->wave_live, sizeof(unsigned), cudaHostAllocDefault));
+    CU(cudaHostAlloc((void**)&ctx->wave_live, 4 * sizeof(unsigned), cudaHostAllocDefault));
     CU(cudaEventCreateWithFlags(&ctx->wave_ev, cudaEventDisableTiming));
     ctx->wave_cap = cap;
     return CLR_OK;
@@ -362,11 +405,17 @@ static int run_buffers_ready(clr_ctx* ctx, int n) {
     return CLR_OK;
 }
 
-// Traces n runs of the current scene in one engine execution (one launch of the persistent kernel or
-// one sequence of wavefront passes), each run with its own photon range, seeds and tallies.
-static int trace_runs(clr_ctx* ctx, const clr_run_params* runs, int n, clr_tallies* outs, clr_ray_record* d_records) {
+// The scene and tables a run traces.
+struct SceneRef {
+    const clr_scene_params* sp;
+    const ParticleBuffers* pb;
+};
+
+// Traces n runs in one engine execution (one launch of the persistent kernel or one sequence of
+// wavefront passes), each run with its own scene, photon range, seeds and tallies.
+static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* runs, int n, clr_tallies* outs,
+                      clr_ray_record* d_records) {
     if (!ctx || !runs || !outs || n < 1) return CLR_ERR_INVALID_ARGUMENT;
-    if (!ctx->built) return fail(ctx, CLR_ERR_NOT_READY, "clr_build_particles must succeed before clr_trace");
     if (d_records && n != 1) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "per-ray records need a single run");
     const clr_run_params& r0 = runs[0];
     for (int i = 0; i < n; ++i) {
@@ -388,8 +437,10 @@ static int trace_runs(clr_ctx* ctx, const clr_run_params* runs, int n, clr_talli
     std::vector<long long> cb(n + 1), rb(n + 1);
     const int chunk = r0.rays_per_item > 0 ? r0.rays_per_item : 256;
     cb[0] = 0; rb[0] = 0;
+    long long max_iter = 0;
     for (int i = 0; i < n; ++i) {
-        fill_scene(ctx, runs + i, &hs[i]);
+        fill_scene(*refs[i].sp, *refs[i].pb, runs + i, &hs[i]);
+        max_iter = std::max(max_iter, (long long)refs[i].sp->max_iterations);
         cb[i + 1] = cb[i] + (runs[i].n_rays + chunk - 1) / chunk;
         rb[i + 1] = rb[i] + runs[i].n_rays;
     }
@@ -426,7 +477,7 @@ static int trace_runs(clr_ctx* ctx, const clr_run_params* runs, int n, clr_talli
         if (cb[n] > 0) CU(launch_photon_kernel(a));
         ctx->last_launches = cb[n] > 0 ? 1 : 0;
     } else if (total > 0) {
-        const long long max_passes = 100000 + 8LL * (long long)ctx->sp.max_iterations;
+        const long long max_passes = 100000 + 8LL * max_iter;
         cudaError_t e = a.rng_mode == CLR_RNG_PHILOX ? wave_run_philox(w, ctx->num_sms, st, max_passes, &ctx->last_passes)
                                                      : wave_run_xor(w, ctx->num_sms, st, max_passes, &ctx->last_passes);
         if (e == cudaErrorLaunchTimeout)
@@ -443,8 +494,266 @@ static int trace_runs(clr_ctx* ctx, const clr_run_params* runs, int n, clr_talli
     return CLR_OK;
 }
 
+// Runs of the current scene (clr_set_scene + clr_build_particles).
+static int trace_current(clr_ctx* ctx, const clr_run_params* runs, int n, clr_tallies* outs, clr_ray_record* d_records) {
+    if (!ctx) return CLR_ERR_INVALID_ARGUMENT;
+    if (!ctx->built) return fail(ctx, CLR_ERR_NOT_READY, "clr_build_particles must succeed before clr_trace");
+    if (n < 1) return CLR_ERR_INVALID_ARGUMENT;
+    std::vector<SceneRef> refs(n, SceneRef{&ctx->sp, &ctx->pb});
+    return trace_runs(ctx, refs.data(), runs, n, outs, d_records);
+}
+
 static int trace_impl(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* d_records) {
-    return trace_runs(ctx, run, 1, out, d_records);
+    return trace_current(ctx, run, 1, out, d_records);
+}
+
+// ---------------- scenario sweep: many scenes built and traced together ----------------
+// Every scenario keeps its own ParticleBuffers, but each per-bin array is one slice of a sweep-wide
+// array (scenario i's bins start at bin_off[i]), so the Mie coefficient, phase pdf and phase CDF
+// kernels run over the bins of many scenarios per launch. The scene-dependent rest of the precompute
+// (rates, sediment coefficients, majorants) stays per scenario.
+
+// Bump allocator over one device arena; with base 0 it only measures.
+struct Arena {
+    uintptr_t base = 0;
+    size_t off = 0;
+    template <class T>
+    T* take(size_t count) {
+        off = (off + 255) & ~(size_t)255;
+        T* p = reinterpret_cast<T*>(base + off);
+        off += std::max<size_t>(count * sizeof(T), 16);
+        return p;
+    }
+};
+
+static double* ParticleBuffers::* const kBinF64[] = {
+    &ParticleBuffers::d, &ParticleBuffers::w, &ParticleBuffers::nidx, &ParticleBuffers::kidx, &ParticleBuffers::x,
+    &ParticleBuffers::qext, &ParticleBuffers::qsca, &ParticleBuffers::qabs, &ParticleBuffers::qback,
+    &ParticleBuffers::g, &ParticleBuffers::albedo, &ParticleBuffers::radius, &ParticleBuffers::nden,
+    &ParticleBuffers::mug, &ParticleBuffers::mus, &ParticleBuffers::mue, &ParticleBuffers::muw,
+    &ParticleBuffers::muev, &ParticleBuffers::gcdf, &ParticleBuffers::wcdf, &ParticleBuffers::pcdf,
+    &ParticleBuffers::moment_a, &ParticleBuffers::moment_b, &ParticleBuffers::trace_geom,
+    &ParticleBuffers::trace_wave, &ParticleBuffers::sedA, &ParticleBuffers::sedB, &ParticleBuffers::sed_norm,
+    &ParticleBuffers::sed_max, &ParticleBuffers::grid_max};
+static float* ParticleBuffers::* const kBinF32[] = {&ParticleBuffers::gcdf_f, &ParticleBuffers::wcdf_f,
+                                                   &ParticleBuffers::pn_f, &ParticleBuffers::pk_f,
+                                                   &ParticleBuffers::prad_f};
+
+struct SweepLayout {
+    std::vector<long long> bin_off, tab_off, rad_off, quad_off, cell_off;
+    long long bins = 0, tabs = 0, rads = 0, quads = 0, cells = 0;
+    std::vector<int> group_first;  // first scenario of each run of scenarios with one Mie key, + sentinel
+};
+
+// Two scenarios whose Mie inputs other than the particles agree (their bins can share one launch).
+static bool same_mie_key(const ParticleBuffers& a, const clr_particle_spec& pa, const ParticleBuffers& b,
+                         const clr_particle_spec& pb) {
+    return a.nt == b.nt && pa.n_medium == pb.n_medium && pa.wavelength_m == pb.wavelength_m;
+}
+
+static void sweep_carve(Arena& A, const SweepLayout& L, std::vector<ParticleBuffers>& pbs) {
+    const int ns = (int)pbs.size();
+    for (auto mp : kBinF64) {
+        double* b = A.take<double>(L.bins);
+        for (int i = 0; i < ns; ++i) pbs[i].*mp = b + L.bin_off[i];
+    }
+    for (auto mp : kBinF32) {
+        float* b = A.take<float>(L.bins);
+        for (int i = 0; i < ns; ++i) pbs[i].*mp = b + L.bin_off[i];
+    }
+    int* nstop = A.take<int>(L.bins);
+    uint8_t* mm = A.take<uint8_t>(L.bins);
+    double* cdf = A.take<double>(L.tabs);
+    float* cdf_f = A.take<float>(L.tabs);
+    double* muscal = A.take<double>(8 * (size_t)ns);
+    double* smaj = A.take<double>(4 * (size_t)ns);
+    float* nmaj = A.take<float>(ns);
+    double* srl = A.take<double>(L.rads);
+    double* swr = A.take<double>(L.rads);
+    double* sterm = A.take<double>(L.quads);
+    double* grid = A.take<double>(L.cells);
+    int* err = A.take<int>(1);
+    for (int i = 0; i < ns; ++i) {
+        ParticleBuffers& pb = pbs[i];
+        pb.nstop = nstop + L.bin_off[i];
+        pb.moment_mode = mm + L.bin_off[i];
+        pb.phase_cdf = cdf + L.tab_off[i];
+        pb.phase_cdf_f = cdf_f + L.tab_off[i];
+        pb.muscal = muscal + 8 * (size_t)i;
+        pb.sed_major = smaj + 4 * (size_t)i;
+        pb.node_major = nmaj + i;
+        pb.sed_radial_log = srl + L.rad_off[i];
+        pb.sed_wr = swr + L.rad_off[i];
+        pb.sed_terms = sterm + L.quad_off[i];
+        pb.sed_grid = grid + L.cell_off[i];
+        pb.err = err;
+        pb.ab = nullptr;
+        pb.pdf = nullptr;
+        if (pb.node_tables) {
+            const size_t plane = (size_t)pb.grid_nr * pb.grid_nz;
+            pb.node_mu = A.take<float2>(plane);
+            pb.node_alias = A.take<int2>(2 * plane * pb.n);
+        }
+    }
+    for (size_t g = 0; g + 1 < L.group_first.size(); ++g) {
+        const int nt = pbs[L.group_first[g]].nt;
+        double* th = A.take<double>(nt);
+        float* th_f = A.take<float>(nt);
+        for (int i = L.group_first[g]; i < L.group_first[g + 1]; ++i) { pbs[i].theta = th; pbs[i].theta_f = th_f; }
+    }
+}
+
+// Bins per Mie launch of a sweep: bounds the a_n/b_n and pdf scratch (at most ~0.5 GB of a_n/b_n rows).
+constexpr int kSweepChunkBins = 4096;
+
+static int sweep_build(clr_ctx* ctx, int ns, const clr_scene_params* sps, const clr_particle_spec* pss,
+                       const clr_sediment_spec* sss) {
+    ctx->sw_sp.clear();
+    ctx->sw_pb.clear();
+    if (ns < 1 || !sps || !pss || !sss) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "clr_sweep_build: no scenarios");
+    std::vector<ParticleBuffers> pbs(ns);
+    SweepLayout L;
+    L.bin_off.resize(ns + 1); L.tab_off.resize(ns + 1); L.rad_off.resize(ns + 1); L.quad_off.resize(ns + 1);
+    L.cell_off.resize(ns + 1);
+    for (int i = 0; i < ns; ++i) {
+        const clr_scene_params& sp = sps[i];
+        int rc = check_scene(ctx, sp);
+        if (rc == CLR_OK) rc = check_particles(ctx, sp, pss + i, sss + i);
+        if (rc != CLR_OK) {
+            ctx->err = "scenario " + std::to_string(i) + ": " + ctx->err;
+            return rc;
+        }
+        ParticleBuffers& pb = pbs[i];
+        const int n = pss[i].n_bins;
+        pb.n = n;
+        pb.nt = hybrid_model(sp) ? pss[i].n_theta : 2;
+        pb.n_radial = sss[i].n_radial;
+        pb.grid_nr = sp.sediment_model == 3 ? sss[i].grid_nr : 2;
+        pb.grid_nz = sp.sediment_model == 3 ? sss[i].grid_nz : 2;
+        pb.grid_zmax = sss[i].grid_zmax;
+        const long long cells = sp.sediment_model == 3 ? (long long)pb.grid_nr * pb.grid_nz * n : 1;
+        pb.node_tables = wants_node_tables(sp, sss[i], n, (size_t)cells) ? 1 : 0;
+        L.bin_off[i] = L.bins; L.bins += n;
+        L.tab_off[i] = L.tabs; L.tabs += (long long)n * pb.nt;
+        L.rad_off[i] = L.rads; L.rads += (long long)n * pb.n_radial;
+        L.quad_off[i] = L.quads; L.quads += (long long)n * sss[i].n_quad;
+        L.cell_off[i] = L.cells; L.cells += cells;
+        if (i == 0 || !same_mie_key(pbs[i - 1], pss[i - 1], pb, pss[i])) L.group_first.push_back(i);
+    }
+    L.group_first.push_back(ns);
+    L.bin_off[ns] = L.bins; L.tab_off[ns] = L.tabs; L.rad_off[ns] = L.rads; L.quad_off[ns] = L.quads;
+    L.cell_off[ns] = L.cells;
+    CU(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    {
+        Arena probe;
+        std::vector<ParticleBuffers> tmp = pbs;
+        sweep_carve(probe, L, tmp);
+        if (probe.off > ctx->sw_arena_bytes) {
+            CU(cudaStreamSynchronize(st));
+            cudaFree(ctx->sw_arena);
+            ctx->sw_arena = nullptr;
+            ctx->sw_arena_bytes = 0;
+            CU(cudaMalloc(&ctx->sw_arena, probe.off));
+            ctx->sw_arena_bytes = probe.off;
+        }
+    }
+    Arena A;
+    A.base = reinterpret_cast<uintptr_t>(ctx->sw_arena);
+    sweep_carve(A, L, pbs);
+    // host staging of the inputs, in the sweep's bin order
+    std::vector<double> hd(L.bins), hw(L.bins), hn(L.bins), hk(L.bins), ma(L.bins, 1.0), mb(L.bins, 0.0);
+    std::vector<uint8_t> mm(L.bins, 0);
+    std::vector<double> cells(L.cells, 1.0);
+    for (int i = 0; i < ns; ++i) {
+        const clr_particle_spec& ps = pss[i];
+        const long long o = L.bin_off[i];
+        std::copy(ps.diameter_m, ps.diameter_m + ps.n_bins, hd.begin() + o);
+        std::copy(ps.weight, ps.weight + ps.n_bins, hw.begin() + o);
+        std::copy(ps.n_real, ps.n_real + ps.n_bins, hn.begin() + o);
+        std::copy(ps.k_imag, ps.k_imag + ps.n_bins, hk.begin() + o);
+        if (ps.moment_enabled && ps.moment_a && ps.moment_b && ps.moment_mode) {
+            for (int b = 0; b < ps.n_bins; ++b) {
+                ma[o + b] = ps.moment_a[b]; mb[o + b] = ps.moment_b[b]; mm[o + b] = ps.moment_mode[b];
+                pbs[i].any_moment |= ps.moment_mode[b] ? 1 : 0;
+            }
+        }
+        if (sps[i].sediment_model == 3)
+            std::copy(sss[i].grid, sss[i].grid + (L.cell_off[i + 1] - L.cell_off[i]), cells.begin() + L.cell_off[i]);
+    }
+    const ParticleBuffers& P0 = pbs[0];  // per-bin arrays start at scenario 0's slices
+    CU(cudaEventRecord(ctx->ev0, st));
+    CU(cudaMemcpyAsync(P0.d, hd.data(), L.bins * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P0.w, hw.data(), L.bins * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P0.nidx, hn.data(), L.bins * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P0.kidx, hk.data(), L.bins * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P0.moment_a, ma.data(), L.bins * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P0.moment_b, mb.data(), L.bins * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P0.moment_mode, mm.data(), L.bins, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P0.sed_grid, cells.data(), L.cells * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(P0.err, 0, sizeof(int), st));
+    // Mie tables: chunks of at most kSweepChunkBins bins within each run of scenarios sharing the key
+    struct Chunk { int s0; long long b0, b1; int cap; };
+    std::vector<Chunk> chunks;
+    size_t scratch = 0;
+    for (size_t g = 0; g + 1 < L.group_first.size(); ++g) {
+        const int s0 = L.group_first[g], s1 = L.group_first[g + 1];
+        const clr_particle_spec& ps = pss[s0];
+        for (long long b0 = L.bin_off[s0]; b0 < L.bin_off[s1]; b0 += kSweepChunkBins) {
+            const long long b1 = std::min(b0 + kSweepChunkBins, L.bin_off[s1]);
+            const int cap = mie_order_bound(hd.data() + b0, hn.data() + b0, hk.data() + b0, (int)(b1 - b0),
+                                            ps.n_medium, ps.wavelength_m);
+            chunks.push_back({s0, b0, b1, cap});
+            const size_t ab = (size_t)(b1 - b0) * cap * 4 * sizeof(double);
+            const size_t pdf = hybrid_model(sps[s0]) ? (size_t)(b1 - b0) * pbs[s0].nt * sizeof(double) : 0;
+            scratch = std::max(scratch, ((ab + 255) & ~(size_t)255) + pdf);
+        }
+    }
+    if (scratch > ctx->sw_scratch_bytes) {
+        CU(cudaStreamSynchronize(st));
+        cudaFree(ctx->sw_scratch);
+        ctx->sw_scratch = nullptr;
+        ctx->sw_scratch_bytes = 0;
+        CU(cudaMalloc(&ctx->sw_scratch, scratch));
+        ctx->sw_scratch_bytes = scratch;
+    }
+    for (const Chunk& c : chunks) {
+        const ParticleBuffers& G = pbs[c.s0];
+        const long long nb = c.b1 - c.b0;
+        const long long tab = L.tab_off[c.s0] + (c.b0 - L.bin_off[c.s0]) * G.nt;
+        MiePhaseBuffers b;
+        b.ab = static_cast<double*>(ctx->sw_scratch);
+        b.pdf = reinterpret_cast<double*>(static_cast<char*>(ctx->sw_scratch) +
+                                          (((size_t)nb * c.cap * 4 * sizeof(double) + 255) & ~(size_t)255));
+        b.nstop = P0.nstop + c.b0; b.x = P0.x + c.b0; b.qext = P0.qext + c.b0; b.qsca = P0.qsca + c.b0;
+        b.qabs = P0.qabs + c.b0; b.qback = P0.qback + c.b0; b.g = P0.g + c.b0; b.albedo = P0.albedo + c.b0;
+        b.theta = G.theta; b.theta_f = G.theta_f;
+        b.cdf = P0.phase_cdf + tab; b.cdf_f = P0.phase_cdf_f + tab; b.err = P0.err;
+        CU(enqueue_mie_tables(P0.d + c.b0, P0.nidx + c.b0, P0.kidx + c.b0, (int)nb, pss[c.s0].n_medium,
+                              pss[c.s0].wavelength_m, G.nt, hybrid_model(sps[c.s0]), c.cap, b, st));
+    }
+    for (int i = 0; i < ns; ++i) CU(enqueue_scene_rates(pbs[i], sps[i], pss[i], sss[i], st));
+    int herr = 0;
+    std::vector<double> hmu(8 * (size_t)ns), hsm(4 * (size_t)ns);
+    std::vector<float> hnm(ns);
+    CU(cudaMemcpyAsync(&herr, P0.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(hmu.data(), P0.muscal, hmu.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(hsm.data(), P0.sed_major, hsm.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(hnm.data(), P0.node_major, hnm.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CU(cudaEventRecord(ctx->ev1, st));
+    CU(cudaStreamSynchronize(st));
+    CU(cudaEventElapsedTime(&ctx->last_kernel_ms, ctx->ev0, ctx->ev1));
+    if (herr) return fail(ctx, CLR_ERR_PRECOMPUTE, "sweep particle precompute failed with error code %d", herr);
+    for (int i = 0; i < ns; ++i) {
+        std::copy(hmu.begin() + 8 * i, hmu.begin() + 8 * i + 8, pbs[i].muscal_host);
+        std::copy(hsm.begin() + 4 * i, hsm.begin() + 4 * i + 4, pbs[i].sed_major_host);
+        pbs[i].node_major_host = hnm[i];
+    }
+    ctx->sw_sp.assign(sps, sps + ns);
+    ctx->sw_pb = std::move(pbs);
+    ctx->last_passes = 0;
+    ctx->last_launches = 0;
+    return CLR_OK;
 }
 
 extern "C" {
@@ -454,7 +763,31 @@ int clr_trace(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray
 }
 
 int clr_trace_batch(clr_ctx* ctx, const clr_run_params* runs, int n_runs, clr_tallies* outs) {
-    return trace_runs(ctx, runs, n_runs, outs, nullptr);
+    return trace_current(ctx, runs, n_runs, outs, nullptr);
+}
+
+int clr_sweep_build(clr_ctx* ctx, int n_scenarios, const clr_scene_params* scenes, const clr_particle_spec* particles,
+                    const clr_sediment_spec* sediments) {
+    if (!ctx) return CLR_ERR_INVALID_ARGUMENT;
+    return sweep_build(ctx, n_scenarios, scenes, particles, sediments);
+}
+
+int clr_sweep_trace(clr_ctx* ctx, const clr_run_params* runs, int n_runs, clr_tallies* outs) {
+    if (!ctx) return CLR_ERR_INVALID_ARGUMENT;
+    if (ctx->sw_pb.empty()) return fail(ctx, CLR_ERR_NOT_READY, "clr_sweep_build must succeed before clr_sweep_trace");
+    if (n_runs != (int)ctx->sw_pb.size())
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "clr_sweep_trace: %d runs for %d scenarios", n_runs,
+                    (int)ctx->sw_pb.size());
+    std::vector<SceneRef> refs(n_runs);
+    for (int i = 0; i < n_runs; ++i) refs[i] = SceneRef{&ctx->sw_sp[i], &ctx->sw_pb[i]};
+    return trace_runs(ctx, refs.data(), runs, n_runs, outs, nullptr);
+}
+
+int clr_sweep_read_particle_physics(clr_ctx* ctx, int scenario, clr_particle_physics* out) {
+    if (!ctx || !out) return CLR_ERR_INVALID_ARGUMENT;
+    if (scenario < 0 || scenario >= (int)ctx->sw_pb.size())
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "scenario %d outside the built sweep", scenario);
+    return read_physics(ctx, ctx->sw_pb[scenario], out);
 }
 
 int clr_trace_host_records(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* host_records) {

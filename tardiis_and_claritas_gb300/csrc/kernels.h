@@ -53,7 +53,10 @@ struct WaveCtl {
     unsigned long long next_photon, total_photons;
     unsigned head[CLR_WQ_COUNT], tail[CLR_WQ_COUNT], snap[CLR_WQ_COUNT], finished[CLR_WQ_COUNT], skips[CLR_WQ_COUNT];
     unsigned claim[CLR_WQ_COUNT];  // next unclaimed entry of this pass's window (chunks of 32)
-    unsigned live, passes;
+    unsigned live;        // a photon is undrawn or in flight (read by the host)
+    unsigned tail_ready;  // every photon is drawn and few remain in flight: the tail kernel may finish them
+    unsigned in_flight;   // photons in flight at the last pass's begin
+    unsigned passes;
 };
 
 struct WaveLaunch {
@@ -127,6 +130,15 @@ struct MiePhaseBuffers {
 };
 cudaError_t enqueue_mie_phase(const double* d, const double* nr, const double* k, int n, double n_medium,
                               double wavelength, int nt, const MiePhaseBuffers& b, cudaStream_t stream);
+// The same for a launch whose a_n/b_n rows are `order_cap` orders apart (mie_order_bound of its bins),
+// placeholder tables instead of the phase tables when `hybrid` is false, and no reset of the error word.
+cudaError_t enqueue_mie_tables(const double* d, const double* nr, const double* k, int n, double n_medium,
+                               double wavelength, int nt, bool hybrid, int order_cap, const MiePhaseBuffers& b,
+                               cudaStream_t stream);
+// Orders the Mie kernel needs for these bins (host arithmetic, with slack), at most CLR_MIE_MAX_ORDER.
+int mie_order_bound(const double* d, const double* nr, const double* k, int n, double n_medium, double wavelength);
+// Precompute error code of a Mie launch whose order bound was too small (not a reference code).
+#define CLR_ERR_CODE_ORDER_CAP 90
 
 // Scratch of the allocation-free Mie/phase entry point: file-scope __device__ arrays (noalloc.cu) of
 // CLR_NOALLOC_MAX_BINS bins and CLR_NOALLOC_MAX_THETA angles, their addresses resolved once per device.
@@ -142,5 +154,8 @@ cudaError_t noalloc_scratch(int device, NoallocScratch* out);
 // `ab_scratch` may supply the Mie a_n/b_n scratch (n*CLR_MIE_MAX_ORDER*4 doubles); when null, pb.ab is used.
 cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,
                                         const clr_sediment_spec& ss, double* ab_scratch, cudaStream_t stream);
+// The part of it after the Mie tables (rates, sediment, node tables); pb's Mie outputs must be ready.
+cudaError_t enqueue_scene_rates(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,
+                                const clr_sediment_spec& ss, cudaStream_t stream);
 
 }  // namespace clr

@@ -13,6 +13,8 @@
 //  * Schiller-Naumann radial slip: one thread per (bin, radius) instead of one
 //    thread for everything; the serial prefix sums and quadrature stay serial
 //    per bin so their rounding is unchanged.
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include "kernels.h"
@@ -40,21 +42,26 @@ __device__ __forceinline__ double cd_rmc(cdx a, cdx b) { return a.re * b.re + a.
 // recurrences. Everything independent across orders is spread over the 32 lanes: the n/z quotients
 // before the downward recurrence, and the a_n, b_n quotients after it. The efficiency sums stay
 // serial on lane 0. Every value has the one-thread expression, and every sum its order.
-// Shared memory: D[0..nmx], n/z[0..nmx] (complex) and psi[0..nstop+1], chi[0..nstop+1] (real).
-constexpr size_t kMieSmem = (size_t)2 * (CLR_MIE_MAX_ORDER + 1) * sizeof(cdx) + (size_t)2 * (CLR_MIE_MAX_ORDER + 2) * sizeof(double);
+// Shared memory: D[0..nmx], n/z[0..nmx] (complex) and psi[0..nstop+1], chi[0..nstop+1] (real), laid out
+// for `order_cap` orders (at most CLR_MIE_MAX_ORDER; a launch over small particles asks for less, so more
+// blocks share an SM). The a_n, b_n rows of `ab` are `order_cap` orders apart.
+__host__ __device__ constexpr size_t mie_smem_bytes(int order_cap) {
+    return (size_t)2 * (order_cap + 1) * sizeof(cdx) + (size_t)2 * (order_cap + 2) * sizeof(double);
+}
+constexpr size_t kMieSmem = mie_smem_bytes(CLR_MIE_MAX_ORDER);
 
 __global__ void __launch_bounds__(32) mie_coefficients_kernel(const double* __restrict__ diameter,
                                                               const double* __restrict__ n_real,
                                                               const double* __restrict__ k_imag, double n_medium,
-                                                              double wavelength, int n_particles,
+                                                              double wavelength, int n_particles, int order_cap,
                                                               double* __restrict__ ab, int* __restrict__ nstop_out,
                                                               double* size_parameter, double* qext, double* qsca,
                                                               double* qabs, double* qback, double* asym_g,
                                                               double* albedo, int* error_flag) {
     extern __shared__ cdx Dsh[];
-    cdx* NZ = Dsh + (CLR_MIE_MAX_ORDER + 1);
-    double* PSI = reinterpret_cast<double*>(NZ + (CLR_MIE_MAX_ORDER + 1));
-    double* CHI = PSI + (CLR_MIE_MAX_ORDER + 2);
+    cdx* NZ = Dsh + (order_cap + 1);
+    double* PSI = reinterpret_cast<double*>(NZ + (order_cap + 1));
+    double* CHI = PSI + (order_cap + 2);
     const int p = blockIdx.x;
     const int lane = threadIdx.x;
     if (p >= n_particles) return;
@@ -75,6 +82,10 @@ __global__ void __launch_bounds__(32) mie_coefficients_kernel(const double* __re
     if (nmx < nstop + 1) nmx = nstop + 1;
     if (nmx >= CLR_MIE_MAX_ORDER || nstop >= CLR_MIE_MAX_ORDER) {
         if (lane == 0) { size_parameter[p] = x; nstop_out[p] = 0; atomicCAS(error_flag, 0, 1); }
+        return;
+    }
+    if (nmx > order_cap) {  // the host's bound on the orders of this launch was too small (never expected)
+        if (lane == 0) { size_parameter[p] = x; nstop_out[p] = 0; atomicCAS(error_flag, 0, CLR_ERR_CODE_ORDER_CAP); }
         return;
     }
     const cdx z = CD(mr * x, mi * x);
@@ -108,7 +119,7 @@ __global__ void __launch_bounds__(32) mie_coefficients_kernel(const double* __re
     }
     __syncwarp();
     const cdx m = CD(mr, mi);
-    double4* abp = reinterpret_cast<double4*>(ab) + (size_t)p * CLR_MIE_MAX_ORDER;
+    double4* abp = reinterpret_cast<double4*>(ab) + (size_t)p * order_cap;
     for (int j = lane; j < nstop; j += 32) {
         int n = j + 1;
         const double psi_nm1 = PSI[n - 1], psi_n = PSI[n], chi_nm1 = CHI[n - 1], chi_n = CHI[n];
@@ -123,7 +134,7 @@ __global__ void __launch_bounds__(32) mie_coefficients_kernel(const double* __re
     // quotients of the efficiency sums, in the same space (Q2X is no longer needed):
     // C1[n] = (2n+1)/(n(n+1)), C2[n] = n(n+2)/(n+1)
     double* C1 = Q2X;
-    double* C2 = Q2X + (CLR_MIE_MAX_ORDER + 1);
+    double* C2 = Q2X + (order_cap + 1);
     for (int n = 1 + lane; n <= nstop; n += 32) {
         const double cn = 2.0 * n + 1.0;
         C1[n] = cn / ((double)n * (n + 1.0));
@@ -174,14 +185,15 @@ __global__ void theta_grid_kernel(double* theta, float* theta_f, int nt) {
 }
 
 #define PDF_GROUP 4
-constexpr size_t kPdfSmem = (size_t)CLR_MIE_MAX_ORDER * sizeof(double3);
+__host__ __device__ constexpr size_t pdf_smem_bytes(int order_cap) { return (size_t)order_cap * sizeof(double3); }
+constexpr size_t kPdfSmem = pdf_smem_bytes(CLR_MIE_MAX_ORDER);
 // S1/S2 -> 0.5(|S1|^2+|S2|^2) sin(theta) for PDF_GROUP bins at one angle (:3561-3581)
 __global__ void __launch_bounds__(128) phase_pdf_kernel(const double* __restrict__ theta, int nt, int n_particles,
-                                                        const int* __restrict__ nstop, const double* __restrict__ ab,
-                                                        double* __restrict__ pdf) {
+                                                        int order_cap, const int* __restrict__ nstop,
+                                                        const double* __restrict__ ab, double* __restrict__ pdf) {
     // quotients of each order n = k + 1 (identical to evaluating them inline):
     // (2n+1)/(n(n+1)), (2n+1)/n, (n+1)/n
-    extern __shared__ double3 QN[];  // [CLR_MIE_MAX_ORDER], dynamic (kPdfSmem bytes)
+    extern __shared__ double3 QN[];  // [order_cap], dynamic (pdf_smem_bytes(order_cap))
     const int j = blockDim.x * blockIdx.x + threadIdx.x;
     const int g0 = blockIdx.y * PDF_GROUP;
     int kmax_blk = 0;
@@ -214,7 +226,7 @@ __global__ void __launch_bounds__(128) phase_pdf_kernel(const double* __restrict
 #pragma unroll
         for (int g = 0; g < PDF_GROUP; ++g) {
             if (k < ns[g]) {
-                double4 q = abp[(size_t)(g0 + g) * CLR_MIE_MAX_ORDER + k];
+                double4 q = abp[(size_t)(g0 + g) * order_cap + k];
                 double ar = q.x, ai = q.y, br = q.z, bi = q.w;
                 s1r[g] += c * (ar * pi_n + br * tau);
                 s1i[g] += c * (ai * pi_n + bi * tau);
@@ -634,6 +646,53 @@ __global__ void sediment_node_kernel(const double* __restrict__ grid, const doub
     }
 }
 
+// Upper bound of the orders the Mie kernel needs for n bins: the largest nmx = max(nstop, |m x|) + 128 of
+// the bins (:3506-3512), recomputed on the host from the same inputs with a few orders of slack for
+// libm differences in cbrt and hypot, and never above CLR_MIE_MAX_ORDER (bins past that limit fail in
+// the kernel with the reference's error code 1 before using shared memory).
+int mie_order_bound(const double* d, const double* nr, const double* k, int n, double n_medium, double wavelength) {
+    int cap = 1;
+    for (int i = 0; i < n; ++i) {
+        const double x = PD_PI * n_medium * d[i] / wavelength;
+        if (!(x > 0.0) || !(n_medium > 0.0)) continue;
+        const double mz = std::hypot(nr[i] / n_medium * x, k[i] / n_medium * x);
+        const double nstop = x + 4.0 * std::cbrt(x) + 2.0;
+        const double nmx = std::fmax(nstop, mz) + 128.0 + 8.0;
+        cap = nmx >= (double)CLR_MIE_MAX_ORDER ? CLR_MIE_MAX_ORDER : std::max(cap, (int)nmx + 1);
+    }
+    return std::min(cap, (int)CLR_MIE_MAX_ORDER);
+}
+
+static cudaError_t set_table_attributes() {
+    cudaError_t e = cudaFuncSetAttribute(mie_coefficients_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kMieSmem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(phase_pdf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPdfSmem);
+}
+
+// Mie coefficients and efficiencies of n bins, then (hybrid event models) the theta grid and the phase
+// pdf and CDF, else the two-point placeholder tables. `b.ab` holds n * order_cap a_n/b_n pairs and
+// `b.pdf` n * nt values. The error word is not reset here.
+cudaError_t enqueue_mie_tables(const double* d, const double* nr, const double* k, int n, double n_medium,
+                               double wavelength, int nt, bool hybrid, int order_cap, const MiePhaseBuffers& b,
+                               cudaStream_t st) {
+    cudaError_t e = set_table_attributes();
+    if (e != cudaSuccess) return e;
+    mie_coefficients_kernel<<<n, 32, mie_smem_bytes(order_cap), st>>>(d, nr, k, n_medium, wavelength, n, order_cap,
+                                                                      b.ab, b.nstop, b.x, b.qext, b.qsca, b.qabs,
+                                                                      b.qback, b.g, b.albedo, b.err);
+    if (hybrid) {
+        theta_grid_kernel<<<(nt + 127) / 128, 128, 0, st>>>(b.theta, b.theta_f, nt);
+        dim3 grid((nt + 127) / 128, (n + PDF_GROUP - 1) / PDF_GROUP);
+        phase_pdf_kernel<<<grid, 128, pdf_smem_bytes(order_cap), st>>>(b.theta, nt, n, order_cap, b.nstop, b.ab,
+                                                                        b.pdf);
+        phase_cdf_kernel<<<n, 32, 0, st>>>(b.theta, b.pdf, nt, n, b.cdf, b.cdf_f, b.err);
+    } else {
+        dummy_phase_kernel<<<(n + 127) / 128, 128, 0, st>>>(b.theta, b.theta_f, b.cdf, b.cdf_f, n);
+    }
+    return cudaGetLastError();
+}
+
 // Mie efficiencies, asymmetry, theta grid and phase CDF of n bins into buffers the caller supplies
 // (the first steps of enqueue_particle_precompute, with no buffer of its own). Used by the
 // allocation-free entry point.
@@ -641,44 +700,15 @@ cudaError_t enqueue_mie_phase(const double* d, const double* nr, const double* k
                               double wavelength, int nt, const MiePhaseBuffers& b, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(b.err, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
-    const size_t smem = kMieSmem;
-    e = cudaFuncSetAttribute(mie_coefficients_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(phase_pdf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPdfSmem);
-    if (e != cudaSuccess) return e;
-    mie_coefficients_kernel<<<n, 32, smem, st>>>(d, nr, k, n_medium, wavelength, n, b.ab, b.nstop, b.x, b.qext,
-                                                 b.qsca, b.qabs, b.qback, b.g, b.albedo, b.err);
-    theta_grid_kernel<<<(nt + 127) / 128, 128, 0, st>>>(b.theta, b.theta_f, nt);
-    dim3 grid((nt + 127) / 128, (n + PDF_GROUP - 1) / PDF_GROUP);
-    phase_pdf_kernel<<<grid, 128, kPdfSmem, st>>>(b.theta, nt, n, b.nstop, b.ab, b.pdf);
-    phase_cdf_kernel<<<n, 32, 0, st>>>(b.theta, b.pdf, nt, n, b.cdf, b.cdf_f, b.err);
-    return cudaGetLastError();
+    return enqueue_mie_tables(d, nr, k, n, n_medium, wavelength, nt, true, CLR_MIE_MAX_ORDER, b, st);
 }
 
-cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,
-                                        const clr_sediment_spec& ss, double* ab_scratch, cudaStream_t st) {
+// The scene-dependent rest of the precompute of one scenario, after its Mie tables: PSD normalisation
+// and rates, sediment coefficients, majorants and node tables.
+cudaError_t enqueue_scene_rates(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,
+                                const clr_sediment_spec& ss, cudaStream_t st) {
     const int n = pb.n;
-    cudaError_t e;
-    double* ab = ab_scratch ? ab_scratch : pb.ab;
-    e = cudaMemsetAsync(pb.err, 0, sizeof(int), st);
-    if (e != cudaSuccess) return e;
-    const size_t smem = kMieSmem;
-    e = cudaFuncSetAttribute(mie_coefficients_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(phase_pdf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPdfSmem);
-    if (e != cudaSuccess) return e;
-    mie_coefficients_kernel<<<n, 32, smem, st>>>(pb.d, pb.nidx, pb.kidx, ps.n_medium, ps.wavelength_m, n, ab, pb.nstop,
-                                                 pb.x, pb.qext, pb.qsca, pb.qabs, pb.qback, pb.g, pb.albedo, pb.err);
     const int em = sp.event_model;
-    if (em == 3 || em == 4 || em == 5) {
-        const int nt = pb.nt;
-        theta_grid_kernel<<<(nt + 127) / 128, 128, 0, st>>>(pb.theta, pb.theta_f, nt);
-        dim3 grid((nt + 127) / 128, (n + PDF_GROUP - 1) / PDF_GROUP);
-        phase_pdf_kernel<<<grid, 128, kPdfSmem, st>>>(pb.theta, nt, n, pb.nstop, ab, pb.pdf);
-        phase_cdf_kernel<<<n, 32, 0, st>>>(pb.theta, pb.pdf, nt, n, pb.phase_cdf, pb.phase_cdf_f, pb.err);
-    } else {
-        dummy_phase_kernel<<<(n + 127) / 128, 128, 0, st>>>(pb.theta, pb.theta_f, pb.phase_cdf, pb.phase_cdf_f, n);
-    }
     transport_kernel<<<1, 1, 0, st>>>(n, pb.d, pb.w, pb.qext, pb.qsca, pb.kidx, pb.nidx, ps.concentration_kg_m3,
                                       ps.density_kg_m3, ps.weight_mode, em, ps.hybrid_wave_scale, ps.n_medium,
                                       ps.wavelength_m, ps.wave_rms_height_m, pb.w, pb.radius, pb.nden, pb.mug, pb.mus,
@@ -701,13 +731,29 @@ cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_par
                                               a.TM == 3 ? pb.grid_max : nullptr, pb.sed_major, pb.err);
     if (pb.node_tables) {
         const int plane = pb.grid_nr * pb.grid_nz;
-        e = cudaMemsetAsync(pb.node_major, 0, sizeof(float), st);
+        cudaError_t e = cudaMemsetAsync(pb.node_major, 0, sizeof(float), st);
         if (e != cudaSuccess) return e;
         sediment_node_kernel<<<(2 * plane + 127) / 128, 128, 0, st>>>(
             pb.sed_grid, pb.trace_geom, pb.trace_wave, n, plane, pb.node_mu, pb.node_alias,
             reinterpret_cast<unsigned int*>(pb.node_major));
     }
     return cudaGetLastError();
+}
+
+cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,
+                                        const clr_sediment_spec& ss, double* ab_scratch, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(pb.err, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    MiePhaseBuffers b;
+    b.ab = ab_scratch ? ab_scratch : pb.ab;
+    b.nstop = pb.nstop; b.x = pb.x; b.qext = pb.qext; b.qsca = pb.qsca; b.qabs = pb.qabs; b.qback = pb.qback;
+    b.g = pb.g; b.albedo = pb.albedo; b.theta = pb.theta; b.theta_f = pb.theta_f; b.pdf = pb.pdf;
+    b.cdf = pb.phase_cdf; b.cdf_f = pb.phase_cdf_f; b.err = pb.err;
+    const int em = sp.event_model;
+    e = enqueue_mie_tables(pb.d, pb.nidx, pb.kidx, pb.n, ps.n_medium, ps.wavelength_m, pb.nt,
+                           em == 3 || em == 4 || em == 5, CLR_MIE_MAX_ORDER, b, st);
+    if (e != cudaSuccess) return e;
+    return enqueue_scene_rates(pb, sp, ps, ss, st);
 }
 
 }  // namespace clr

@@ -31,6 +31,8 @@
 // kernel's (they are the same functions), so per-ray results in the xorshift parity mode are
 // identical to the reference's whichever engine runs.
 #pragma once
+#include <algorithm>
+#include <cstddef>
 #include "photon_kernel.cuh"
 
 namespace clr {
@@ -43,6 +45,11 @@ static_assert(WQ_FIN + 1 == CLR_WQ_COUNT, "queue count");
 constexpr int kWaveThreads = 256;
 // water flights per FLIGHT visit before the photon is re-queued (bounds lane imbalance in a warp)
 constexpr int kFlightSteps = 4;
+// Once every photon is drawn and at most kTailPhotons remain in flight, the passes stop and one tail
+// kernel runs each remaining photon to its end in a single thread: the longest histories (thousands of
+// flights in optically dense scenes) then cost one step each instead of a pass each.
+constexpr unsigned kTailPhotons = 65536;
+constexpr int kTailThreads = 128;
 // Rare stages (few photons per pass, long serial work per photon) run only when their queue holds a
 // full batch, after kMaxSkips passes, or while the pool drains.
 constexpr unsigned kRareBatch = 8192;
@@ -115,6 +122,11 @@ __global__ void wave_begin_kernel(WaveLaunch w) {
     }
     c->live = (pending != 0u || drawing) ? 1u : 0u;
     c->passes++;
+    // photons still in flight after this pass at the most (every queue but FREE), once all are drawn
+    unsigned in_flight = 0;
+    for (int q = 1; q < CLR_WQ_COUNT; ++q) in_flight += c->tail[q] - c->head[q];
+    c->tail_ready = (!drawing && in_flight <= kTailPhotons) ? 1u : 0u;
+    c->in_flight = in_flight;
 }
 
 // Per-block conditional-closure statistics for scenario 0 (others go straight to the device tally).
@@ -399,6 +411,58 @@ __global__ void __launch_bounds__(kWaveThreads) wave_fin_kernel(WaveLaunch w) {
     if (home >= 0) flush_warp_tally(wt, w.tallies + home, lane);
 }
 
+// ---------------- TAIL: the last photons, each run to its end by one thread ----------------
+template <class Mode>
+__device__ __forceinline__ int tail_visit(const WaveLaunch& w, int q, const DevScene& D, Ray& r,
+                                          typename Mode::Lane& L, SlotMeta& m, unsigned long long* cstats) {
+    switch (q) {
+        case WQ_ENTRY: return wave_stage_body<Mode, WQ_ENTRY>(w, D, r, L, m, cstats);
+        case WQ_FLIGHT: return wave_stage_body<Mode, WQ_FLIGHT>(w, D, r, L, m, cstats);
+        case WQ_COND: return wave_stage_body<Mode, WQ_COND>(w, D, r, L, m, cstats);
+        case WQ_GEOM: return wave_stage_body<Mode, WQ_GEOM>(w, D, r, L, m, cstats);
+        case WQ_MORPH: return wave_stage_body<Mode, WQ_MORPH>(w, D, r, L, m, cstats);
+        case WQ_TOP: return wave_stage_body<Mode, WQ_TOP>(w, D, r, L, m, cstats);
+        case WQ_BOTTOM: return wave_stage_body<Mode, WQ_BOTTOM>(w, D, r, L, m, cstats);
+        case WQ_SIDE: return wave_stage_body<Mode, WQ_SIDE>(w, D, r, L, m, cstats);
+        default: return wave_stage_body<Mode, WQ_ACRYL>(w, D, r, L, m, cstats);
+    }
+}
+
+// Runs after the last pass, when every photon is drawn: the photons still queued (entries [snap, tail)
+// of every queue but FREE) are taken one per thread and carried through the same stage bodies, in the
+// same order, as the passes would carry them, then scored. Per-ray results are those of the passes.
+template <class Mode, bool kRecord>
+__global__ void __launch_bounds__(kTailThreads) wave_tail_kernel(WaveLaunch w) {
+    __shared__ DetTable det;
+    det_table_init(&det);
+    __syncthreads();
+    const WaveCtl* c = w.ctl;
+    unsigned first[CLR_WQ_COUNT + 1];
+    first[0] = first[1] = 0;
+    for (int q = 1; q < CLR_WQ_COUNT; ++q) first[q + 1] = first[q] + (c->tail[q] - c->snap[q]);
+    const unsigned total = first[CLR_WQ_COUNT];
+    const WavePool<Mode> pool = wave_pool<Mode>(w);
+    unsigned long long visits[CLR_WQ_COUNT] = {};
+    for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        int q = 1;
+        while (idx >= first[q + 1]) ++q;
+        const uint32_t slot = wave_ring(w, q)[(c->snap[q] + (idx - first[q])) & wave_mask(w)];
+        Ray r = pool.ray[slot];
+        typename Mode::Lane L = pool.lane[slot];
+        SlotMeta m = pool.meta[slot];
+        const DevScene& D = w.scenes[m.sid];
+        unsigned long long* cstats = w.tallies[m.sid].c.cstats;
+        while (q != WQ_FIN) {
+            ++visits[q];
+            q = tail_visit<Mode>(w, q, D, r, L, m, cstats);
+        }
+        ++visits[WQ_FIN];
+        finish_ray<Mode>(D, det, r, m.gid, m.sid, -1, nullptr, w.tallies, kRecord ? w.records + m.rid : nullptr);
+    }
+    for (int q = 1; q < CLR_WQ_COUNT; ++q)
+        if (visits[q]) atomicAdd(&w.tallies[0].sched[q], visits[q]);
+}
+
 __global__ void wave_init_kernel(WaveLaunch w) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < w.cap) wave_ring(w, WQ_FREE)[i] = i;
@@ -413,6 +477,8 @@ __global__ void wave_init_kernel(WaveLaunch w) {
         c->total_photons = w.total;
         c->live = w.total > 0 ? 1u : 0u;
         c->passes = 0u;
+        c->tail_ready = 0u;
+        c->in_flight = 0u;
     }
 }
 
@@ -502,20 +568,32 @@ cudaError_t wave_run_t(const WaveLaunch& w, int num_sms, cudaStream_t st, long l
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int batch = 8;
     long long launched = 0;
-    volatile unsigned* live = w.host_live;
+    volatile unsigned* live = w.host_live;  // [live, tail_ready, in_flight] of the pass before the read
+    static_assert(offsetof(WaveCtl, tail_ready) == offsetof(WaveCtl, live) + sizeof(unsigned) &&
+                      offsetof(WaveCtl, in_flight) == offsetof(WaveCtl, live) + 2 * sizeof(unsigned),
+                  "flag words are read together");
     for (int k = 0; k < batch; ++k)
         if ((e = cudaGraphLaunch(P.exec, st)) != cudaSuccess) return e;
     launched += batch;
     while (true) {
-        if ((e = cudaMemcpyAsync((void*)w.host_live, &w.ctl->live, sizeof(unsigned), cudaMemcpyDeviceToHost, st)) !=
-            cudaSuccess)
+        if ((e = cudaMemcpyAsync((void*)w.host_live, &w.ctl->live, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                 st)) != cudaSuccess)
             return e;
         if ((e = cudaEventRecord(w.flag_event, st)) != cudaSuccess) return e;
         for (int k = 0; k < batch; ++k)
             if ((e = cudaGraphLaunch(P.exec, st)) != cudaSuccess) return e;
         launched += batch;
         if ((e = cudaEventSynchronize(w.flag_event)) != cudaSuccess) return e;
-        if (*live == 0u) break;
+        if (live[0] == 0u) break;
+        if (live[1] != 0u) {
+            // at most live[2] photons remain after the passes already queued: finish them in one launch
+            const unsigned n = live[2];
+            const int blocks = (int)std::max(1u, std::min(n, 65536u * kTailThreads) / kTailThreads + 1);
+            wave_tail_kernel<Mode, kRecord><<<blocks, kTailThreads, 0, st>>>(w);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            launched += 1;
+            break;
+        }
         if (launched > max_passes) {
             cudaStreamSynchronize(st);
             return cudaErrorLaunchTimeout;

@@ -53,6 +53,10 @@ def load(build_if_missing: bool = False):
                                        C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p], C.c_int),
             "clr_calibrate": ([C.c_void_p, C.c_int, P(C.c_double)], C.c_int),
+            "clr_sweep_build": ([C.c_void_p, C.c_int, P(abi.SceneParams), P(abi.ParticleSpec), P(abi.SedimentSpec)],
+                                C.c_int),
+            "clr_sweep_trace": ([C.c_void_p, P(abi.RunParams), C.c_int, P(abi.Tallies)], C.c_int),
+            "clr_sweep_read_particle_physics": ([C.c_void_p, C.c_int, P(abi.ParticlePhysics)], C.c_int),
         }
         for name, (argt, rest) in sig.items():
             f = getattr(lib, name)
@@ -65,7 +69,8 @@ def load(build_if_missing: bool = False):
 def exported_symbols() -> list[str]:
     return ["clr_create", "clr_destroy", "clr_last_error", "clr_version", "clr_set_scene", "clr_build_particles",
             "clr_read_particle_physics", "clr_trace", "clr_trace_host_records", "clr_trace_batch", "clr_abi_sizeof",
-            "clr_last_kernel_ms", "clr_last_launches", "clr_calibrate", "clr_mie_phase_noalloc"]
+            "clr_last_kernel_ms", "clr_last_launches", "clr_calibrate", "clr_mie_phase_noalloc", "clr_sweep_build",
+            "clr_sweep_trace", "clr_sweep_read_particle_physics"]
 
 
 class Context:
@@ -118,6 +123,33 @@ class Context:
         outs = (abi.Tallies * n)()
         self._check(self.lib.clr_trace_batch(self.h, arr, n, outs), "clr_trace_batch")
         return [outs[i].as_dict() for i in range(n)]
+
+    def sweep_build(self, scenes: list, particles: list, sediments: list):
+        """Build the tables of many scenarios (scene params, particle specs and sediment specs, one each)."""
+        n = len(scenes)
+        if not (len(particles) == len(sediments) == n):
+            raise ValueError("one scene, particle spec and sediment spec per scenario")
+        sa = (abi.SceneParams * n)(*scenes)
+        pa = (abi.ParticleSpec * n)(*particles)
+        qa = (abi.SedimentSpec * n)(*sediments)
+        self._check(self.lib.clr_sweep_build(self.h, n, sa, pa, qa), "clr_sweep_build")
+        self.sweep_shape = [(int(p.n_bins), int(p.n_theta)) for p in particles]
+
+    def sweep_trace(self, runs: list) -> list:
+        """Trace every scenario of the built sweep together (runs[i] traces scenario i)."""
+        n = len(runs)
+        arr = (abi.RunParams * n)(*runs)
+        outs = (abi.Tallies * n)()
+        self._check(self.lib.clr_sweep_trace(self.h, arr, n, outs), "clr_sweep_trace")
+        return [outs[i].as_dict() for i in range(n)]
+
+    def sweep_physics(self, scenario: int, n_bins: int, n_theta: int) -> dict:
+        """The resident tables of one scenario of the built sweep (as physics())."""
+        pp, arrays = abi.alloc_physics(n_bins, n_theta)
+        self._check(self.lib.clr_sweep_read_particle_physics(self.h, int(scenario), C.byref(pp)),
+                    "clr_sweep_read_particle_physics")
+        arrays["phase_cdf"] = arrays["phase_cdf"].reshape(n_bins, n_theta)
+        return arrays
 
     def trace_device(self, run: abi.RunParams, records_ptr: int | None = None):
         T = abi.Tallies()

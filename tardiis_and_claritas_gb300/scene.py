@@ -566,3 +566,58 @@ def small_plain_workload():
     cfg = small_cell_config(particle_surface_rms_slope_deg=0.0, wave_surface_rms_height_m=0.0)
     cfg.validate()
     return cfg, quartz_particles(100.0), None, None
+
+
+@dataclass
+class SweepScenario:
+    """One scenario of a batched sweep: its configuration, particles, photon count and seed."""
+    cfg: ModelConfig
+    particles: Particles
+    n_photons: int
+    seed: int
+    params: dict
+
+
+def sweep_workload(n_scenarios: int = 512, sampler_seed: int = 0, n_bins: int = 64,
+                   photons: tuple = (1e5, 1e7), scale_photons: float = 1.0) -> list:
+    """The batched sweep: n_scenarios scenarios in the small cell, drawn with numpy's PCG64 from
+    `sampler_seed`. Per scenario: photon count log-uniform over `photons` (times scale_photons),
+    concentration log-uniform 1-1e4 mg/L, median diameter log-uniform 2-200 um, sigma_g uniform 1.2-2.0,
+    stirrer rpm uniform 0-1200 (localized-vortex surface with a 5 mm core), particle index uniform
+    1.50-1.60 (k = 0); 860 nm; 64 lognormal mass bins over 1-200 um; uniform sediment; scenario i uses
+    seed i."""
+    rng = np.random.Generator(np.random.PCG64(int(sampler_seed)))
+    n = int(n_scenarios)
+    lo, hi = math.log(photons[0]), math.log(photons[1])
+    n_ph = np.exp(rng.uniform(lo, hi, n))
+    conc = np.exp(rng.uniform(math.log(1.0), math.log(1e4), n))
+    d50 = np.exp(rng.uniform(math.log(2.0), math.log(200.0), n))
+    sig = rng.uniform(1.2, 2.0, n)
+    rpm = rng.uniform(0.0, 1200.0, n)
+    nidx = rng.uniform(1.50, 1.60, n)
+    base = small_cell_config(particle_surface_rms_slope_deg=0.0, wave_surface_rms_height_m=0.0)
+    out = []
+    for i in range(n):
+        dh = stirrer_scully_delta_h(float(rpm[i]), 0.005, base.tube_inner_radius_m)
+        if dh > 0.0:
+            cfg = small_cell_config(particle_surface_rms_slope_deg=0.0, wave_surface_rms_height_m=0.0,
+                                    free_surface_model="localized_scully_vortex",
+                                    vortex_wall_center_height_difference_m=dh, vortex_core_radius_m=0.005)
+        else:
+            cfg = small_cell_config(particle_surface_rms_slope_deg=0.0, wave_surface_rms_height_m=0.0)
+        cfg.validate()
+        parts = quartz_particles(float(conc[i]), n_bins=n_bins, median_um=float(d50[i]), sigma_g=float(sig[i]),
+                                 n=float(nidx[i]))
+        out.append(SweepScenario(cfg, parts, max(1, int(round(float(n_ph[i]) * scale_photons))), i,
+                                 dict(concentration_mg_l=float(conc[i]), median_um=float(d50[i]),
+                                      sigma_g=float(sig[i]), rpm=float(rpm[i]), n_particle=float(nidx[i]))))
+    return out
+
+
+def sweep_specs(scenarios: list) -> tuple[list, list, list]:
+    """ABI inputs of a sweep: (scene params, particle specs, sediment specs), one each per scenario."""
+    scenes = [sc.cfg.to_scene_params() for sc in scenarios]
+    parts = [sc.particles.spec(sc.cfg) for sc in scenarios]
+    seds = [sc.cfg.sediment_spec() for sc in scenarios]
+    return scenes, parts, seds
+
