@@ -360,6 +360,49 @@ int clr_mie_phase_noalloc(clr_ctx* ctx, const double* d_diameter_m, const double
  * No reference counterpart: lets a binding check its struct mirror against the library. */
 int64_t clr_abi_sizeof(int which);
 
+/* ---------------------------------------------------------------------------------------------
+ * Surrogate network of the detector signals (no reference counterpart: the reference runs a full
+ * Monte Carlo for every scenario query). A multilayer perceptron
+ *   CLR_MLP_INPUTS -> CLR_MLP_WIDTH (x4 hidden layers, SiLU) -> CLR_MLP_OUTPUTS
+ * with BF16 weights and activations and FP32 accumulation; its 256x256 layers (forward,
+ * backward-data and weight-gradient products) run on the tensor cores (tcgen05), the rest on CUDA
+ * cores. FP32 master weights, Adam (beta1 0.9, beta2 0.999, eps 1e-8), mean-squared-error loss over
+ * the outputs. Inputs and targets are device FP32 arrays [n][CLR_MLP_INPUTS] / [n][CLR_MLP_OUTPUTS]
+ * in whatever normalisation the caller trains with. Parameters are one flat FP32 vector: W1 [256][6],
+ * b1, W2 [256][256], b2, W3, b3, W4, b4, W5 [3][256], b5.
+ * ------------------------------------------------------------------------------------------- */
+#define CLR_MLP_INPUTS 6
+#define CLR_MLP_WIDTH 256
+#define CLR_MLP_OUTPUTS 3
+#define CLR_MLP_PARAMS 199939
+typedef struct clr_mlp clr_mlp;
+
+/* max_batch: rows of the work buffers (a multiple of 128); weights drawn uniform in
+ * +-1/sqrt(fan_in) from `seed`. */
+int clr_mlp_create(clr_mlp** out, int device, int max_batch, uint64_t seed);
+int clr_mlp_destroy(clr_mlp* net);
+const char* clr_mlp_last_error(const clr_mlp* net);
+int clr_mlp_set_params(clr_mlp* net, const float* host_params, int64_t count);  /* resets Adam */
+int clr_mlp_get_params(clr_mlp* net, float* host_params, int64_t count);
+/* d_y[n][3] = network(d_x[n][6]) for any n (processed in max_batch chunks) on `stream` (NULL: the
+ * network's own), synchronous. */
+int clr_mlp_forward(clr_mlp* net, const float* d_x, int64_t n, float* d_y, void* stream);
+/* Loss and gradient of one batch of n rows (a multiple of 128, at most max_batch) without an update:
+ * grads_host[CLR_MLP_PARAMS] (nullable) and the mean squared error. */
+int clr_mlp_gradients(clr_mlp* net, const float* d_x, const float* d_t, int64_t n, float* grads_host, float* loss);
+/* Adam steps over d_index[0 .. n_index) in batches of `batch` rows (a multiple of 128): each step
+ * gathers its rows of d_x/d_t by index, runs forward and backward and updates; the step is one CUDA
+ * graph launch. mean_loss: the mean batch loss of the call. */
+int clr_mlp_train(clr_mlp* net, const float* d_x, const float* d_t, const int32_t* d_index, int64_t n_index,
+                  int batch, float lr, float* mean_loss);
+/* Device time of the last clr_mlp_forward / clr_mlp_train call (CUDA events on its stream), ms. */
+int clr_mlp_last_ms(const clr_mlp* net, float* ms);
+/* C[M][256] = A[M][K] . B[256][K]^T on the tensor cores: BF16 row-major operands (K a multiple of
+ * 64, leading dimensions multiples of 8 elements, 16-byte aligned), FP32 result (ldc >= 256),
+ * synchronous on `stream`. */
+int clr_bf16_gemm_n256(const void* d_a, int64_t lda, const void* d_b, int64_t ldb, int64_t M, int64_t K, float* d_c,
+                       int64_t ldc, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,7 +21,8 @@ BUILD_DIR = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libclaritas_gb.so")
 
-SOURCES = ["clr_api.cu", "precompute.cu", "trace_xor.cu", "trace_philox.cu", "calibrate.cu", "noalloc.cu"]
+SOURCES = ["clr_api.cu", "precompute.cu", "trace_xor.cu", "trace_philox.cu", "calibrate.cu", "noalloc.cu",
+           "surrogate.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"] + ARCH
 # Per-unit flags. The FP64 precompute and the xorshift parity kernels are compiled without

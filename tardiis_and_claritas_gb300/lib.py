@@ -57,6 +57,19 @@ def load(build_if_missing: bool = False):
                                 C.c_int),
             "clr_sweep_trace": ([C.c_void_p, P(abi.RunParams), C.c_int, P(abi.Tallies)], C.c_int),
             "clr_sweep_read_particle_physics": ([C.c_void_p, C.c_int, P(abi.ParticlePhysics)], C.c_int),
+            "clr_mlp_create": ([P(C.c_void_p), C.c_int, C.c_int, C.c_uint64], C.c_int),
+            "clr_mlp_destroy": ([C.c_void_p], C.c_int),
+            "clr_mlp_last_error": ([C.c_void_p], C.c_char_p),
+            "clr_mlp_set_params": ([C.c_void_p, P(C.c_float), C.c_int64], C.c_int),
+            "clr_mlp_get_params": ([C.c_void_p, P(C.c_float), C.c_int64], C.c_int),
+            "clr_mlp_forward": ([C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p], C.c_int),
+            "clr_mlp_gradients": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, P(C.c_float), P(C.c_float)],
+                                  C.c_int),
+            "clr_mlp_train": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_float,
+                               P(C.c_float)], C.c_int),
+            "clr_mlp_last_ms": ([C.c_void_p, P(C.c_float)], C.c_int),
+            "clr_bf16_gemm_n256": ([C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p,
+                                    C.c_int64, C.c_void_p], C.c_int),
         }
         for name, (argt, rest) in sig.items():
             f = getattr(lib, name)
@@ -70,7 +83,9 @@ def exported_symbols() -> list[str]:
     return ["clr_create", "clr_destroy", "clr_last_error", "clr_version", "clr_set_scene", "clr_build_particles",
             "clr_read_particle_physics", "clr_trace", "clr_trace_host_records", "clr_trace_batch", "clr_abi_sizeof",
             "clr_last_kernel_ms", "clr_last_launches", "clr_calibrate", "clr_mie_phase_noalloc", "clr_sweep_build",
-            "clr_sweep_trace", "clr_sweep_read_particle_physics"]
+            "clr_sweep_trace", "clr_sweep_read_particle_physics", "clr_mlp_create", "clr_mlp_destroy",
+            "clr_mlp_last_error", "clr_mlp_set_params", "clr_mlp_get_params", "clr_mlp_forward", "clr_mlp_gradients",
+            "clr_mlp_train", "clr_mlp_last_ms", "clr_bf16_gemm_n256"]
 
 
 class Context:
@@ -193,3 +208,80 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+class Network:
+    """The surrogate network (clr_mlp): device pointers are passed as integers (e.g. tensor.data_ptr())."""
+
+    N_PARAMS = 199939
+
+    def __init__(self, device: int = 0, max_batch: int = 65536, seed: int = 0):
+        self.lib = load()
+        self.h = C.c_void_p()
+        rc = self.lib.clr_mlp_create(C.byref(self.h), int(device), int(max_batch), int(seed))
+        if rc != 0:
+            raise ClaritasLibraryError(f"clr_mlp_create failed ({rc})")
+        self.max_batch = int(max_batch)
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.lib.clr_mlp_last_error(self.h).decode(errors="replace")
+            raise RuntimeError(f"{what} failed ({rc}): {msg}")
+
+    def set_params(self, p):
+        import numpy as np
+        a = np.ascontiguousarray(p, dtype=np.float32)
+        self._check(self.lib.clr_mlp_set_params(self.h, a.ctypes.data_as(C.POINTER(C.c_float)), a.size),
+                    "clr_mlp_set_params")
+
+    def get_params(self):
+        import numpy as np
+        a = np.zeros(self.N_PARAMS, dtype=np.float32)
+        self._check(self.lib.clr_mlp_get_params(self.h, a.ctypes.data_as(C.POINTER(C.c_float)), a.size),
+                    "clr_mlp_get_params")
+        return a
+
+    def forward(self, x_ptr: int, n: int, y_ptr: int, stream: int = 0):
+        self._check(self.lib.clr_mlp_forward(self.h, C.c_void_p(x_ptr), int(n), C.c_void_p(y_ptr),
+                                             C.c_void_p(stream) if stream else None), "clr_mlp_forward")
+
+    def gradients(self, x_ptr: int, t_ptr: int, n: int):
+        import numpy as np
+        g = np.zeros(self.N_PARAMS, dtype=np.float32)
+        loss = C.c_float()
+        self._check(self.lib.clr_mlp_gradients(self.h, C.c_void_p(x_ptr), C.c_void_p(t_ptr), int(n),
+                                               g.ctypes.data_as(C.POINTER(C.c_float)), C.byref(loss)),
+                    "clr_mlp_gradients")
+        return float(loss.value), g
+
+    def train(self, x_ptr: int, t_ptr: int, idx_ptr: int, n_index: int, batch: int, lr: float) -> float:
+        loss = C.c_float()
+        self._check(self.lib.clr_mlp_train(self.h, C.c_void_p(x_ptr), C.c_void_p(t_ptr), C.c_void_p(idx_ptr),
+                                           int(n_index), int(batch), float(lr), C.byref(loss)), "clr_mlp_train")
+        return float(loss.value)
+
+    def last_ms(self) -> float:
+        v = C.c_float()
+        self._check(self.lib.clr_mlp_last_ms(self.h, C.byref(v)), "clr_mlp_last_ms")
+        return float(v.value)
+
+    def close(self):
+        if self.h:
+            self.lib.clr_mlp_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def bf16_gemm_n256(a_ptr: int, lda: int, b_ptr: int, ldb: int, M: int, K: int, c_ptr: int, ldc: int,
+                   stream: int = 0):
+    """C[M][256] = A[M][K] . B[256][K]^T on the tensor cores (BF16 in, FP32 out)."""
+    rc = load().clr_bf16_gemm_n256(C.c_void_p(a_ptr), int(lda), C.c_void_p(b_ptr), int(ldb), int(M), int(K),
+                                   C.c_void_p(c_ptr), int(ldc), C.c_void_p(stream) if stream else None)
+    if rc != 0:
+        raise RuntimeError(f"clr_bf16_gemm_n256 failed ({rc})")
+
