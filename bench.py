@@ -201,6 +201,79 @@ def run_sweep(args, ctx, rank: int, world: int, local_rank: int, dist, dev) -> d
     return line
 
 
+def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> dict:
+    """Surrogate workload: Monte Carlo training data from the batched sweep, training of the tensor-core
+    network, judgement against Monte Carlo with 100x the photons, then timed inference (a step = one
+    batch of 65536 queries)."""
+    import numpy as np
+    import torch
+    from tardiis_and_claritas_gb300 import lib as L, surrogate as G
+    ctx = L.Context(local_rank)
+    t0 = time.perf_counter()
+    train = G.make_dataset(ctx, args.sur_train, args.sur_photons, sampler_seed=1000 + rank, seed_base=0)
+    test = G.make_dataset(ctx, args.sur_test, 100 * args.sur_photons, sampler_seed=2000 + rank, seed_base=10 ** 6)
+    data_s = time.perf_counter() - t0
+    ctx.close()
+    model = G.Surrogate(local_rank, max_batch=65536, seed=rank)
+    hist = model.fit(train, epochs=args.sur_epochs, batch=2048)
+    err = G.judge(model, test)
+    base = G.linear_baseline(train, test)
+    batch = 65536
+    x = torch.randn(batch, 6, generator=torch.Generator().manual_seed(1)).to(dev)
+    for _ in range(args.warmup):
+        model.predict_device(x)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier(device_ids=[local_rank])
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    ms = []
+    for _ in range(args.steps):
+        model.predict_device(x)
+        ms.append(model.net.last_ms())
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    dev_s = float(sum(ms)) * 1e-3
+    if dist:
+        t = torch.tensor([dev_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s = float(t.item())
+    value = world * batch * args.steps / dev_s
+    speed = G.query_speed(model, batch=batch, reps=max(3, args.steps))
+    flop_q = 2.0 * (6 * 256 + 3 * 256 * 256 + 256 * 3)
+    peaks = measured_peaks()
+    peak = peaks.get("bf16_tflops") or 1900.0
+    ach = flop_q * value / world / 1e12
+    mc_s_per_scen = train.mc_seconds / len(train.x)
+    mc_s_judge = test.mc_seconds / len(test.x)
+    line = {"metric": "surrogate queries/s (error vs Monte Carlo judge stated)", "value": value,
+            "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 weights/activations, f32 accumulation", "data": "synthetic (seeded); labels from this MC",
+            "config": {"workload": "surrogate MLP 6-256x4(SiLU)-3 of the sweep's detector signals (channels 9, 0, 17); "
+                                   f"trained on {args.sur_train} sweep scenarios at {args.sur_photons:.0e} photons, "
+                                   f"judged on {args.sur_test} held-out scenarios at {100 * args.sur_photons:.0e} "
+                                   "photons; inference batch 65536",
+                       "inference_batch": batch, "l2": "inputs resident (3 MB); weights L2-resident by design"},
+            "e2e": {"value": speed["e2e_queries_per_s"] * world, "unit": "queries/s",
+                    "h2d_bytes_per_step": batch * 6 * 4, "d2h_bytes_per_step": batch * 3 * 4},
+            "gpu_launches": args.steps * 5, "clocks": clocks,
+            "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                         "peak_source": "bf16_tflops of MEASURED_PEAKS.json" if peaks.get("bf16_tflops") else "fallback",
+                         "traffic": None, "flop_per_query": flop_q},
+            "surrogate": {"judge": err, "linear_baseline": base,
+                          "train": {"scenarios": len(train.x), "photons_each": args.sur_photons,
+                                    "epochs": args.sur_epochs, "final_loss": hist[-1][2],
+                                    "train_seconds": model.train_seconds,
+                                    "ms_per_epoch": float(np.median([h[3] for h in hist]))},
+                          "mc": {"data_seconds_wall": data_s, "train_labels_device_s_per_scenario": mc_s_per_scen,
+                                 "judge_device_s_per_scenario": mc_s_judge},
+                          "speedup_vs_mc_at_training_photons": (value / world) * mc_s_per_scen,
+                          "speedup_vs_mc_at_judge_photons": (value / world) * mc_s_judge}}
+    model.close()
+    return line
+
+
 def measured_peaks() -> dict:
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -287,6 +360,23 @@ def run_reference_arm(args, rank: int, world: int):
         return
     threads = os.cpu_count() or 1
     name = args.workload
+    if name == "surrogate":
+        # the reference has no surrogate: it answers each query with its Monte Carlo (CPU here), at the
+        # surrogate's training photon count
+        from tardiis_and_claritas_gb300 import scene as S
+        p = args.sur_photons
+        scs = S.sweep_workload(SWEEP_SCENARIOS, sampler_seed=2000, photons=(p, p))
+        vals = [sweep_cpu_estimate(scs, threads, args.cpu_seconds) for _ in range(max(1, args.steps))]
+        value = sum(v["value"] for v in vals) / len(vals)
+        line = {"impl": "reference", "metric": "surrogate queries/s (error vs Monte Carlo judge stated)",
+                "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32/f64", "data": "synthetic (seeded)",
+                "config": {"workload": f"one Monte Carlo run of {p:.0e} photons per query (sweep scenarios)"},
+                "cpu_baseline": dict(vals[-1], value=value, unit="queries/s"),
+                "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     if name == "sweep":
         from tardiis_and_claritas_gb300 import scene as S
         scs = S.sweep_workload(SWEEP_SCENARIOS)
@@ -329,7 +419,11 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["full", "small", "sweep"], default="full")
+    ap.add_argument("--workload", choices=["full", "small", "sweep", "surrogate"], default="full")
+    ap.add_argument("--sur-train", type=int, default=16384, help="surrogate: training scenarios")
+    ap.add_argument("--sur-test", type=int, default=256, help="surrogate: judged held-out scenarios")
+    ap.add_argument("--sur-photons", type=int, default=1_000_000, help="surrogate: photons per training scenario")
+    ap.add_argument("--sur-epochs", type=int, default=400, help="surrogate: training epochs")
     ap.add_argument("--rng", choices=["philox", "xorshift"], default="philox")
     ap.add_argument("--photons", type=int, default=0, help="override photons per step")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
@@ -360,6 +454,14 @@ def main():
     dev = torch.device("cuda", local_rank)
     if dist:
         dist.barrier(device_ids=[local_rank])
+    if args.workload == "surrogate":
+        line = run_surrogate(args, rank, world, local_rank, dist, dev)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        if dist:
+            dist.barrier(device_ids=[local_rank])
+            dist.destroy_process_group()
+        return
     ctx = L.Context(local_rank)
     if args.workload == "sweep":
         line = run_sweep(args, ctx, rank, world, local_rank, dist, dev)

@@ -1,0 +1,208 @@
+"""Surrogate of the detector signals, trained on batched Monte Carlo and judged by it.
+
+The reference answers every scenario query with a full Monte Carlo run (ClaritasForwardModel.simulate,
+CLARITAS/CLARITAS.py:7160). Here a small network (libclaritas_gb.so's clr_mlp: 6 -> 256 x4 SiLU -> 3, BF16
+tensor-core training and inference) maps the scenario parameters of the batched sweep to three detector
+signals, and the Monte Carlo stays both its training-data source and the judge of its error:
+
+  inputs  (6): log10 concentration [mg/L], log10 median diameter [um], sigma_g, stirrer rpm / 1000,
+               particle refractive index, log10 geometric optical depth (radius x 3 C Q / (2 rho d_32),
+               Q = 2: a closed form of the inputs, no Mie evaluation needed at query time)
+  outputs (3): log10 of the detected fraction (symmetric score (native + mirror) / 2 per launched photon,
+               plus half a count) at the 90-degree aperture (channel 9), the transmitted one (channel 0)
+               and the rearmost, 170-degree one (channel 17, the backscatter signal).
+
+Scenarios come from the sweep sampler (scene.sweep_workload); Monte Carlo labels from clr_sweep_build +
+clr_sweep_trace, 512 scenarios per engine execution.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+from . import abi, lib as L, scene as S
+
+CHANNELS = (9, 0, 17)
+SIGNAL_NAMES = ("signal_90deg", "signal_transmitted", "signal_backscatter_170deg")
+FEATURE_NAMES = ("log10_concentration_mg_l", "log10_median_um", "sigma_g", "rpm_per_1000", "particle_index",
+                 "log10_optical_depth")
+
+
+def optical_depth(sc: S.SweepScenario) -> float:
+    """Radius x extinction for Q_ext = 2 (geometric optics) of the scenario's size distribution."""
+    p = sc.particles
+    w = p.weight / p.weight.sum()
+    return 1.5 * 2.0 * p.concentration_kg_m3 / p.density_kg_m3 * float((w / p.diameter_m).sum()) * \
+        sc.cfg.tube_inner_radius_m
+
+
+def features(scs: list) -> np.ndarray:
+    out = np.zeros((len(scs), 6))
+    for i, sc in enumerate(scs):
+        q = sc.params
+        out[i] = (math.log10(q["concentration_mg_l"]), math.log10(q["median_um"]), q["sigma_g"], q["rpm"] / 1000.0,
+                  q["n_particle"], math.log10(max(optical_depth(sc), 1e-12)))
+    return out
+
+
+def signals(tallies: dict, n_photons: int) -> np.ndarray:
+    sym = 0.5 * (tallies["hw_native"] + tallies["hw_mirror"]).astype(np.float64)
+    return np.log10((sym[list(CHANNELS)] + 0.5) / float(n_photons))
+
+
+@dataclass
+class Dataset:
+    x: np.ndarray          # [n][6] features
+    y: np.ndarray          # [n][3] log10 signals
+    hits: np.ndarray       # [n][3] symmetric scores (counts) behind y
+    photons: np.ndarray    # [n]
+    mc_seconds: float      # device time of the Monte Carlo that made the labels (builds + traces)
+    scenarios: list = field(default_factory=list)
+
+
+def monte_carlo(ctx: L.Context, scs: list, chunk: int = 512, rng: str = "philox", seed_base: int = 0) -> Dataset:
+    """Monte Carlo labels of the scenarios, `chunk` scenarios per sweep build + trace."""
+    mode = abi.RNG_PHILOX if rng == "philox" else abi.RNG_REFERENCE_XORSHIFT
+    ys, hs, secs = [], [], 0.0
+    for c0 in range(0, len(scs), chunk):
+        part = scs[c0:c0 + chunk]
+        scenes, parts, seds = S.sweep_specs(part)
+        ctx.sweep_build(scenes, parts, seds)
+        secs += ctx.last_kernel_ms() * 1e-3
+        runs = [S.run_params(sc.n_photons, seed=seed_base + sc.seed, rng_mode=mode, scenario_id=i)
+                for i, sc in enumerate(part)]
+        T = ctx.sweep_trace(runs)
+        secs += ctx.last_kernel_ms() * 1e-3
+        for sc, t in zip(part, T):
+            ys.append(signals(t, sc.n_photons))
+            sym = 0.5 * (t["hw_native"] + t["hw_mirror"]).astype(np.float64)
+            hs.append(sym[list(CHANNELS)])
+    return Dataset(features(scs), np.array(ys), np.array(hs), np.array([sc.n_photons for sc in scs]), secs, scs)
+
+
+def make_dataset(ctx: L.Context, n_scenarios: int, photons: int, sampler_seed: int, seed_base: int = 0) -> Dataset:
+    """n_scenarios scenarios of the sweep sampler, each traced with `photons` photons."""
+    scs = S.sweep_workload(n_scenarios, sampler_seed=sampler_seed, photons=(photons, photons))
+    return monte_carlo(ctx, scs, seed_base=seed_base)
+
+
+class Surrogate:
+    """The trained network plus its input/output standardisation."""
+
+    def __init__(self, device: int = 0, max_batch: int = 65536, seed: int = 0):
+        import torch
+        self.torch = torch
+        self.dev = torch.device("cuda", device)
+        self.net = L.Network(device, max_batch=max_batch, seed=seed)
+        self.x_mean = np.zeros(6)
+        self.x_std = np.ones(6)
+        self.y_mean = np.zeros(3)
+        self.y_std = np.ones(3)
+        self.history: list = []
+
+    def fit(self, data: Dataset, epochs: int = 400, batch: int = 2048, lr: float = 2e-3, lr_min: float = 5e-5,
+            seed: int = 0) -> list:
+        torch = self.torch
+        self.x_mean, self.x_std = data.x.mean(0), data.x.std(0) + 1e-12
+        self.y_mean, self.y_std = data.y.mean(0), data.y.std(0) + 1e-12
+        x = torch.from_numpy(((data.x - self.x_mean) / self.x_std).astype(np.float32)).to(self.dev)
+        t = torch.from_numpy(((data.y - self.y_mean) / self.y_std).astype(np.float32)).to(self.dev)
+        n = x.shape[0]
+        use = (n // batch) * batch
+        g = torch.Generator().manual_seed(seed)
+        hist = []
+        t0 = time.perf_counter()
+        for e in range(epochs):
+            lr_e = lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * e / max(epochs - 1, 1)))
+            idx = torch.randperm(n, generator=g)[:use].to(torch.int32).to(self.dev)
+            loss = self.net.train(x.data_ptr(), t.data_ptr(), idx.data_ptr(), use, batch, lr_e)
+            hist.append((e, lr_e, loss, self.net.last_ms()))
+        self.train_seconds = time.perf_counter() - t0
+        self.history = hist
+        return hist
+
+    def predict_device(self, x_std):
+        """Standardised inputs (device tensor [n][6]) -> standardised outputs (device tensor [n][3])."""
+        torch = self.torch
+        y = torch.empty((x_std.shape[0], 3), dtype=torch.float32, device=self.dev)
+        self.net.forward(x_std.data_ptr(), x_std.shape[0], y.data_ptr())
+        return y
+
+    def predict(self, x: np.ndarray) -> np.ndarray:
+        torch = self.torch
+        xs = torch.from_numpy(((x - self.x_mean) / self.x_std).astype(np.float32)).to(self.dev)
+        y = self.predict_device(xs).cpu().numpy().astype(np.float64)
+        return y * self.y_std + self.y_mean
+
+    def state(self) -> dict:
+        return {"params": self.net.get_params(), "x_mean": self.x_mean, "x_std": self.x_std, "y_mean": self.y_mean,
+                "y_std": self.y_std}
+
+    def load_state(self, st: dict):
+        self.net.set_params(np.asarray(st["params"], dtype=np.float32))
+        for k in ("x_mean", "x_std", "y_mean", "y_std"):
+            setattr(self, k, np.asarray(st[k], dtype=np.float64))
+
+    def close(self):
+        self.net.close()
+
+
+def judge(model: Surrogate, data: Dataset, min_hits: float = 2500.0) -> dict:
+    """Relative error of the surrogate's signals against Monte Carlo labels (the judge), per channel, over
+    scenarios whose judge count is at least `min_hits` (relative standard error <= 1/sqrt(min_hits): 2 % at
+    the default; the 90-degree aperture sees ~5e-5 of the photons, so 1e8 judge photons give ~5e3 counts)."""
+    pred = model.predict(data.x)
+    out = {}
+    for k, name in enumerate(SIGNAL_NAMES):
+        ok = data.hits[:, k] >= min_hits
+        rel = np.abs(10.0 ** (pred[ok, k] - data.y[ok, k]) - 1.0)
+        judge_se = 1.0 / np.sqrt(np.maximum(data.hits[ok, k], 1.0))
+        out[name] = {"scenarios": int(ok.sum()), "median_rel_error": float(np.median(rel)) if ok.any() else None,
+                     "p90_rel_error": float(np.quantile(rel, 0.9)) if ok.any() else None,
+                     "within_1pct": float(np.mean(rel <= 0.01)) if ok.any() else None,
+                     "judge_median_rel_se": float(np.median(judge_se)) if ok.any() else None}
+    return out
+
+
+def linear_baseline(train: Dataset, test: Dataset, min_hits: float = 2500.0) -> dict:
+    """The method without the network: least squares on the same six features (plus their squares and a
+    constant), same judge and error measure."""
+    def design(x):
+        return np.hstack([np.ones((x.shape[0], 1)), x, x * x])
+    coef, *_ = np.linalg.lstsq(design(train.x), train.y, rcond=None)
+    pred = design(test.x) @ coef
+    out = {}
+    for k, name in enumerate(SIGNAL_NAMES):
+        ok = test.hits[:, k] >= min_hits
+        rel = np.abs(10.0 ** (pred[ok, k] - test.y[ok, k]) - 1.0)
+        out[name] = {"median_rel_error": float(np.median(rel)) if ok.any() else None,
+                     "p90_rel_error": float(np.quantile(rel, 0.9)) if ok.any() else None}
+    return out
+
+
+def query_speed(model: Surrogate, batch: int = 65536, reps: int = 20) -> dict:
+    """Inference throughput on `batch`-query batches resident on the device (CUDA events around each call,
+    inside the library), and end to end from host memory."""
+    torch = model.torch
+    x = torch.randn(batch, 6, generator=torch.Generator().manual_seed(1)).to(model.dev)
+    for _ in range(3):
+        model.predict_device(x)
+    ms = []
+    for _ in range(reps):
+        model.predict_device(x)
+        ms.append(model.net.last_ms())
+    xh = torch.randn(batch, 6).pin_memory()
+    yh = torch.empty(batch, 3).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        y = model.predict_device(xh.to(model.dev, non_blocking=True))
+        yh.copy_(y)
+    torch.cuda.synchronize()
+    e2e = (time.perf_counter() - t0) / reps
+    dev = float(np.median(ms)) * 1e-3
+    return {"batch": batch, "device_s_per_batch": dev, "queries_per_s": batch / dev, "e2e_queries_per_s": batch / e2e}

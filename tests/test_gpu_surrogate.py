@@ -101,3 +101,29 @@ def test_training_reduces_the_loss(torch_cuda):
     mse = float(((y.cpu().numpy() - t[:1024]) ** 2).mean())
     assert abs(mse - loss_or) < 0.05 * loss_or + 1e-5
     net.close()
+
+
+def test_surrogate_of_monte_carlo_beats_the_method_without_it(torch_cuda):
+    """Trained on batched Monte Carlo of sweep scenarios, the network predicts held-out scenarios' signals
+    (judged by Monte Carlo with 100x the photons) better than a least-squares fit on the same features,
+    and answers queries far faster than the Monte Carlo."""
+    from tardiis_and_claritas_gb300 import lib as L, surrogate as G
+    ctx = L.Context(0)
+    train = G.make_dataset(ctx, 2048, 1_000_000, sampler_seed=31)
+    test = G.make_dataset(ctx, 128, 20_000_000, sampler_seed=32, seed_base=10 ** 6)
+    ctx.close()
+    model = G.Surrogate(0, max_batch=4096, seed=0)
+    hist = model.fit(train, epochs=300, batch=1024)
+    assert hist[-1][2] < 0.2 * hist[0][2]
+    # the 90-degree aperture sees ~5e-5 of the photons: judge scenarios with >= 400 counts there (5 % error)
+    err = G.judge(model, test, min_hits=400.0)
+    base = G.linear_baseline(train, test, min_hits=400.0)
+    assert err["signal_transmitted"]["scenarios"] >= 100, err
+    assert err["signal_transmitted"]["median_rel_error"] < 0.5 * base["signal_transmitted"]["median_rel_error"], \
+        (err, base)
+    for name in G.SIGNAL_NAMES:
+        if err[name]["scenarios"] >= 10:
+            assert err[name]["median_rel_error"] < base[name]["median_rel_error"], (name, err[name], base[name])
+    speed = G.query_speed(model, batch=4096, reps=5)
+    assert speed["queries_per_s"] > 1e3 * len(test.x) / test.mc_seconds
+    model.close()
