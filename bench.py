@@ -257,7 +257,7 @@ def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> di
                        "inference_batch": batch, "l2": "inputs resident (3 MB); weights L2-resident by design"},
             "e2e": {"value": speed["e2e_queries_per_s"] * world, "unit": "queries/s",
                     "h2d_bytes_per_step": batch * 6 * 4, "d2h_bytes_per_step": batch * 3 * 4},
-            "gpu_launches": args.steps * 5, "clocks": clocks,
+            "gpu_launches": args.steps, "clocks": clocks,
             "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                          "peak_source": "bf16_tflops of MEASURED_PEAKS.json" if peaks.get("bf16_tflops") else "fallback",
                          "traffic": None, "flop_per_query": flop_q},

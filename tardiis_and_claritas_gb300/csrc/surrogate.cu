@@ -427,7 +427,13 @@ __global__ void small_grads_kernel(const bf16* const* __restrict__ dzt, long lon
 struct PackArgs {
     bf16* w[6];
     bf16* wt[6];
+    bf16* wp[6];  // l = 2..4: the shared-memory image of W_l as a B operand (256 x 256 core-matrix layout)
 };
+// element (r, k) of a K = 256 operand image in the core-matrix layout (8 x 16-byte core matrices, K-adjacent
+// core matrices 128 bytes apart, 8-row groups 4096 bytes apart), in BF16 elements
+__host__ __device__ __forceinline__ int img_idx(int r, int k) {
+    return ((r >> 3) * 4096 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2) >> 1;
+}
 __device__ __forceinline__ void pack_one(const PackArgs& pa, long long p, float v) {
     const bf16 b = __float2bfloat16(v);
     for (int l = 1; l <= 5; ++l) {
@@ -436,9 +442,13 @@ __device__ __forceinline__ void pack_one(const PackArgs& pa, long long p, float 
         const long long o = p - off_w(l);
         if (o >= 0 && o < (long long)nin * nout) {
             pa.w[l][o] = b;
-            if (pa.wt[l]) {
-                const long long out = o / nin, in = o % nin;
-                pa.wt[l][in * nout + out] = b;
+            const int out = (int)(o / nin), in = (int)(o % nin);
+            if (pa.wt[l]) pa.wt[l][(long long)in * nout + out] = b;
+            if (pa.wp[l]) {
+                if (l == 1)  // 256 x 16 image (K = 16): 8-row groups 256 bytes apart
+                    pa.wp[1][((out >> 3) * 256 + (in >> 3) * 128 + (out & 7) * 16 + (in & 7) * 2) >> 1] = b;
+                else
+                    pa.wp[l][img_idx(out, in)] = b;  // 256 x 256, or 16 x 256 for W5 (rows 3..15 stay zero)
             }
         }
     }
@@ -464,13 +474,229 @@ __global__ void adam_kernel(float* params, float* grads, float* m1, float* m2, f
     pack_one(pa, p, v);
 }
 
+// ---------------- fused inference: every layer of a 128-row tile on one SM ----------------
+// A persistent CTA per SM walks 128-row tiles, with every product on the tensor cores: layer 1 as one
+// tcgen05.mma with K padded from 6 to 16, the three 256x256 layers as 16 MMAs each, and the 256 -> 3
+// output layer as 16 MMAs with N padded to 16. The small padded weight images (W1, W5) stay in shared
+// memory; each 256x256 weight image (128 KB) comes in by one cp.async.bulk copy that starts as soon as
+// the previous layer's MMAs have completed, so it overlaps that layer's epilogue. Each epilogue reads the
+// accumulator with tcgen05.ld, adds the bias, applies SiLU (one tanh.approx per element) and writes the
+// next layer's A image. Activations never leave the SM.
+constexpr int kInferThreads = 512;               // warp w reads TMEM lane quarter w % 4, columns 64 (w / 4) ..
+constexpr int kABytes = kM * kHid * 2;           // 64 KB: the tile's activations, K = 256
+constexpr int kWBytes = kHid * kHid * 2;         // 128 KB: one 256x256 weight image
+constexpr int kXBytes = kM * 16 * 2;             // 4 KB: the tile's inputs, K padded to 16
+constexpr int kW1Bytes = kHid * 16 * 2;          // 8 KB: W1 image, 256 x 16
+constexpr int kW5Bytes = 16 * kHid * 2;          // 8 KB: W5 image, 16 (3 used) x 256
+constexpr int kOffSmW = kABytes;
+constexpr int kOffSmX = kOffSmW + kWBytes;
+constexpr int kOffSmW1 = kOffSmX + kXBytes;
+constexpr int kOffSmW5 = kOffSmW1 + kW1Bytes;
+constexpr int kOffSmBias = kOffSmW5 + kW5Bytes;              // f32 [4][256]: b1..b4
+constexpr int kOffSmB5 = kOffSmBias + 4 * kHid * 4;          // f32 [4]
+constexpr int kOffSmBar = kOffSmB5 + 16;                     // 2 mbarriers
+constexpr int kOffSmSlot = kOffSmBar + 16;                   // TMEM address
+constexpr int kInferSmem = kOffSmSlot + 16;
+static_assert(kOffSmBar % 8 == 0 && kInferSmem <= 227 * 1024, "shared-memory plan");
+// instruction descriptors: N = 256 (hidden layers) and N = 16 (output layer)
+constexpr uint32_t kIdescN16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(16 >> 3) << 17) |
+                               ((uint32_t)(kM >> 4) << 24);
+
+struct InferArgs {
+    const float* x;      // [n][6]
+    float* y;            // [n][3]
+    long long n;
+    int tiles;
+    const bf16* wp[3];   // images of W2, W3, W4 (256 x 256)
+    const bf16* w1p;     // image of W1 padded to 256 x 16
+    const bf16* w5p;     // image of W5 padded to 16 x 256
+    const float* params;
+    int* err;
+};
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// silu(z) = z/2 (1 + tanh(z/2)): one multi-function-unit operation per element (hardware tanh approximation,
+// relative error far below the BF16 rounding that follows)
+__device__ __forceinline__ float silu_tanh(float z) {
+    const float h = 0.5f * z;
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
+    return fmaf(h, t, h);
+}
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v) {
+    uint32_t r0, r1, r2, r3;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    v[0] = __uint_as_float(r0); v[1] = __uint_as_float(r1); v[2] = __uint_as_float(r2); v[3] = __uint_as_float(r3);
+}
+
+__global__ void __launch_bounds__(kInferThreads, 1) mlp_infer_kernel(InferArgs a) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    bf16* A = reinterpret_cast<bf16*>(sm);
+    bf16* W = reinterpret_cast<bf16*>(sm + kOffSmW);
+    unsigned char* X = sm + kOffSmX;
+    float* bs = reinterpret_cast<float*>(sm + kOffSmBias);
+    float* b5s = reinterpret_cast<float*>(sm + kOffSmB5);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kOffSmBar);  // [0] weights arrived, [1] MMAs done
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + kOffSmSlot);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int quarter = warp & 3, cgroup = warp >> 2;  // TMEM lane quarter, group of 64 columns
+    const int r = quarter * 32 + lane;  // this thread's row of the tile (and TMEM lane)
+    {
+        const uint4* s1 = reinterpret_cast<const uint4*>(a.w1p);
+        const uint4* s5 = reinterpret_cast<const uint4*>(a.w5p);
+        uint4* d1 = reinterpret_cast<uint4*>(sm + kOffSmW1);
+        uint4* d5 = reinterpret_cast<uint4*>(sm + kOffSmW5);
+        for (int i = tid; i < kW1Bytes / 16; i += kInferThreads) d1[i] = s1[i];
+        for (int i = tid; i < kW5Bytes / 16; i += kInferThreads) d5[i] = s5[i];
+    }
+    for (int i = tid; i < 4 * kHid; i += kInferThreads) bs[i] = a.params[off_b(1 + i / kHid) + i % kHid];
+    if (tid < kOut) b5s[tid] = a.params[kOffB5 + tid];
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tmem_alloc(tslot, 256);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t tlane = tmem + ((uint32_t)(quarter * 32) << 16);
+    const uint32_t sA = smem_u32(A), sW = smem_u32(W), sX = smem_u32(X);
+    const uint32_t sW1 = smem_u32(sm + kOffSmW1), sW5 = smem_u32(sm + kOffSmW5);
+    unsigned wphase = 0, mphase = 0;
+    bool w_pending = false;  // thread 0: a weight copy was issued and not yet waited for
+    if (tid == 0 && (int)blockIdx.x < a.tiles) {
+        bulk_load(W, a.wp[0], kWBytes, &bar[0]);
+        w_pending = true;
+    }
+    // MMAs of one layer by thread 0, then every thread waits for their completion (bounded)
+    auto run_mma = [&](int kind) -> bool {
+        bool issued = true;
+        if (tid == 0) {
+            if (kind == 1) {  // 256x256 layer: needs its weight image
+                issued = mbar_wait(&bar[0], wphase & 1u, a.err, 3);
+                w_pending = !issued;
+            }
+            if (issued) {
+                tc_fence_after();
+                if (kind == 0) {
+                    mma_bf16(tmem, smem_desc(sX, 128, 256), smem_desc(sW1, 128, 256), kIdesc, 0u);
+                } else {
+                    const uint32_t b0 = kind == 1 ? sW : sW5;
+                    const uint32_t idesc = kind == 1 ? kIdesc : kIdescN16;
+#pragma unroll
+                    for (int kk = 0; kk < kHid / 16; ++kk)
+                        mma_bf16(tmem, smem_desc(sA + kk * 256, 128, 4096), smem_desc(b0 + kk * 256, 128, 4096),
+                                 idesc, kk > 0 ? 1u : 0u);
+                }
+                mma_commit(&bar[1]);
+            }
+        }
+        if (kind == 1) wphase++;
+        if (!__syncthreads_and(issued)) return false;
+        const bool done = mbar_wait(&bar[1], mphase & 1u, a.err, 4);
+        mphase++;
+        return __syncthreads_and(done);
+    };
+    // bias + SiLU of this thread's 64 columns of the accumulator row into the next A image
+    auto hidden_epilogue = [&](const float* bias) {
+        tc_fence_after();
+#pragma unroll 1
+        for (int c = 0; c < 2; ++c) {
+            const int j0 = cgroup * 64 + c * 32;
+            float v[32];
+            tmem_ld32(tlane + (uint32_t)j0, v);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float4 b0 = *reinterpret_cast<const float4*>(bias + j0 + 8 * q);
+                const float4 b1 = *reinterpret_cast<const float4*>(bias + j0 + 8 * q + 4);
+                const float* e = v + 8 * q;
+                uint4 o;
+                o.x = pack_bf16x2(silu_tanh(e[0] + b0.x), silu_tanh(e[1] + b0.y));
+                o.y = pack_bf16x2(silu_tanh(e[2] + b0.z), silu_tanh(e[3] + b0.w));
+                o.z = pack_bf16x2(silu_tanh(e[4] + b1.x), silu_tanh(e[5] + b1.y));
+                o.w = pack_bf16x2(silu_tanh(e[6] + b1.z), silu_tanh(e[7] + b1.w));
+                *reinterpret_cast<uint4*>(A + img_idx(r, j0 + 8 * q)) = o;
+            }
+        }
+        fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+    };
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < a.tiles && ok; tile += gridDim.x) {
+        const long long row = (long long)tile * kM + r;
+        const bool valid = row < a.n;
+        if (cgroup == 0) {  // the tile's inputs as a 128 x 16 A image (K 6..15 zero)
+            float xv[kIn];
+#pragma unroll
+            for (int i = 0; i < kIn; ++i) xv[i] = valid ? a.x[row * kIn + i] : 0.0f;
+            uint4 lo;
+            lo.x = pack_bf16x2(xv[0], xv[1]);
+            lo.y = pack_bf16x2(xv[2], xv[3]);
+            lo.z = pack_bf16x2(xv[4], xv[5]);
+            lo.w = 0u;
+            *reinterpret_cast<uint4*>(X + (r >> 3) * 256 + (r & 7) * 16) = lo;
+            *reinterpret_cast<uint4*>(X + (r >> 3) * 256 + 128 + (r & 7) * 16) = make_uint4(0u, 0u, 0u, 0u);
+        }
+        fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+        if (!(ok = run_mma(0))) break;
+        hidden_epilogue(bs);
+        for (int l = 0; l < 3 && ok; ++l) {
+            if (!(ok = run_mma(1))) break;
+            // the weight buffer is free: bring in the next layer's weights (or the first layer's for the next tile)
+            if (tid == 0) {
+                if (l < 2) { bulk_load(W, a.wp[l + 1], kWBytes, &bar[0]); w_pending = true; }
+                else if (tile + (int)gridDim.x < a.tiles) { bulk_load(W, a.wp[0], kWBytes, &bar[0]); w_pending = true; }
+            }
+            hidden_epilogue(bs + (l + 1) * kHid);
+        }
+        if (!ok) break;
+        if (!(ok = run_mma(2))) break;
+        tc_fence_after();
+        float v[4];
+        if (cgroup == 0) {
+            tmem_ld4(tlane, v);
+            if (valid)
+#pragma unroll
+                for (int k = 0; k < kOut; ++k) a.y[row * kOut + k] = v[k] + b5s[k];
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    // a weight copy still in flight (only after a failed wait) must land before the CTA leaves
+    if (tid == 0 && w_pending) (void)mbar_wait(&bar[0], wphase & 1u, a.err, 5);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 256);
+    }
+}
+
 }  // namespace mlpk
 
 using namespace mlpk;
 
 // ---------------- the network object behind the C ABI ----------------
 struct clr_mlp {
-    int device = 0;
+    int device = 0, num_sms = 0;
     cudaStream_t stream = nullptr;
     int cap = 0;  // batch rows of the work buffers (multiple of 128)
     std::string err;
@@ -590,6 +816,8 @@ int clr_mlp_create(clr_mlp** out, int device, int max_batch, uint64_t seed) {
     MCU(cudaSetDevice(device));
     MCU(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
     MCU(set_gemm_attributes());
+    MCU(cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem));
+    MCU(cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, device));
     MCU(cudaEventCreate(&m->ev0));
     MCU(cudaEventCreate(&m->ev1));
     auto F = [&](float** p, size_t cnt) { return malloc_tracked(m, (void**)p, cnt * sizeof(float)); };
@@ -598,7 +826,14 @@ int clr_mlp_create(clr_mlp** out, int device, int max_batch, uint64_t seed) {
     for (int l = 1; l <= 5; ++l) {
         const int nin = l == 1 ? kIn : kHid, nout = l == 5 ? kOut : kHid;
         MCU(H(&m->pa.w[l], (size_t)nin * nout));
-        if (l >= 2 && l <= 4) MCU(H(&m->pa.wt[l], (size_t)nin * nout));
+        if (l >= 2 && l <= 4) {
+            MCU(H(&m->pa.wt[l], (size_t)nin * nout));
+            MCU(H(&m->pa.wp[l], (size_t)nin * nout));
+        }
+        if (l == 1 || l == 5) {  // padded images: zero padding written once, weights by every pack
+            MCU(H(&m->pa.wp[l], (size_t)kHid * 16));
+            MCU(cudaMemset(m->pa.wp[l], 0, (size_t)kHid * 16 * sizeof(bf16)));
+        }
     }
     const size_t act = (size_t)m->cap * kHid;
     for (int l = 1; l <= 4; ++l) {
@@ -675,14 +910,16 @@ int clr_mlp_forward(clr_mlp* m, const float* d_x, int64_t n, float* d_y, void* s
     MCU(cudaSetDevice(m->device));
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : m->stream;
     MCU(cudaEventRecord(m->ev0, st));
-    for (long long r0 = 0; r0 < n; r0 += m->cap) {
-        const int rows = (int)std::min<long long>(m->cap, n - r0);
-        gather_kernel<<<(rows + 255) / 256, 256, 0, st>>>(d_x, nullptr, nullptr, r0, rows, m->xb, nullptr);
-        MCU(cudaGetLastError());
-        MCU(forward_rows(m, rows, false, st));
-        head_kernel<<<(rows * 32 + 255) / 256, 256, 0, st>>>(m->h[4], nullptr, rows, m->pa.w[5], m->params + kOffB5,
-                                                             nullptr, d_y + r0 * kOut, nullptr, nullptr, nullptr, 0,
-                                                             nullptr);
+    if (n > 0) {
+        InferArgs a{};
+        a.x = d_x; a.y = d_y; a.n = n;
+        const long long tiles = (n + kM - 1) / kM;
+        if (tiles > (1LL << 30)) return mfail(m, CLR_ERR_INVALID_ARGUMENT, "clr_mlp_forward: too many rows");
+        a.tiles = (int)tiles;
+        a.wp[0] = m->pa.wp[2]; a.wp[1] = m->pa.wp[3]; a.wp[2] = m->pa.wp[4];
+        a.w1p = m->pa.wp[1]; a.w5p = m->pa.wp[5]; a.params = m->params; a.err = m->d_err;
+        const int grid = (int)std::min<long long>(tiles, m->num_sms);
+        mlp_infer_kernel<<<grid, kInferThreads, kInferSmem, st>>>(a);
         MCU(cudaGetLastError());
     }
     MCU(cudaEventRecord(m->ev1, st));
