@@ -35,7 +35,7 @@ sys.path.insert(0, ROOT)
 # stage kernel of one ncu capture of a 4e6-photon trace (see profiles/wavefront_stages_full_scene.md):
 # warp instructions issued, FP64 flops executed (DFMA counted as 2) and DRAM bytes read + written.
 # The issue-slot roofline divides warp instructions issued per second by 4 schedulers x SMs x clock.
-PER_PHOTON = {"full": {"warp_inst": 495.5, "fp64_flops": 17.1, "dram_bytes": 850.1}, "small": None, "sweep": None}
+PER_PHOTON = {"full": {"warp_inst": 423.5, "fp64_flops": 17.1, "dram_bytes": 981.8}, "small": None, "sweep": None}
 
 
 def workload(name: str):

@@ -54,6 +54,8 @@ struct clr_ctx {
     size_t sw_arena_bytes = 0;
     void* sw_scratch = nullptr;
     size_t sw_scratch_bytes = 0;
+    void* sw_jobs = nullptr;  // job descriptions of the batched rate kernels
+    size_t sw_jobs_bytes = 0;
 };
 
 static int fail(clr_ctx* c, int code, const char* fmt, ...) {
@@ -130,6 +132,7 @@ int clr_destroy(clr_ctx* ctx) {
     cudaFree(ctx->wave_begin);
     cudaFree(ctx->sw_arena);
     cudaFree(ctx->sw_scratch);
+    cudaFree(ctx->sw_jobs);
     if (ctx->wave_live) cudaFreeHost(ctx->wave_live);
     if (ctx->wave_ev) cudaEventDestroy(ctx->wave_ev);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -732,7 +735,20 @@ static int sweep_build(clr_ctx* ctx, int ns, const clr_scene_params* sps, const 
         CU(enqueue_mie_tables(P0.d + c.b0, P0.nidx + c.b0, P0.kidx + c.b0, (int)nb, pss[c.s0].n_medium,
                               pss[c.s0].wavelength_m, G.nt, hybrid_model(sps[c.s0]), c.cap, b, st));
     }
-    for (int i = 0; i < ns; ++i) CU(enqueue_scene_rates(pbs[i], sps[i], pss[i], sss[i], st));
+    {
+        const size_t need = scene_rates_batch_scratch(ns);
+        if (need > ctx->sw_jobs_bytes) {
+            CU(cudaStreamSynchronize(st));
+            cudaFree(ctx->sw_jobs);
+            ctx->sw_jobs = nullptr;
+            ctx->sw_jobs_bytes = 0;
+            CU(cudaMalloc(&ctx->sw_jobs, need));
+            ctx->sw_jobs_bytes = need;
+        }
+        std::vector<ParticleBuffers*> pp(ns);
+        for (int i = 0; i < ns; ++i) pp[i] = &pbs[i];
+        CU(enqueue_scene_rates_batch(pp.data(), sps, pss, sss, ns, ctx->sw_jobs, st));
+    }
     int herr = 0;
     std::vector<double> hmu(8 * (size_t)ns), hsm(4 * (size_t)ns);
     std::vector<float> hnm(ns);

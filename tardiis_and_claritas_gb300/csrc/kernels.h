@@ -157,5 +157,11 @@ cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_par
 // The part of it after the Mie tables (rates, sediment, node tables); pb's Mie outputs must be ready.
 cudaError_t enqueue_scene_rates(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,
                                 const clr_sediment_spec& ss, cudaStream_t stream);
+// The same for n scenarios at once (one launch each for the one-thread rate and majorant kernels);
+// d_scratch: scene_rates_batch_scratch(n) bytes of device memory.
+size_t scene_rates_batch_scratch(int n);
+cudaError_t enqueue_scene_rates_batch(ParticleBuffers* const* pbs, const clr_scene_params* sps,
+                                      const clr_particle_spec* pss, const clr_sediment_spec* sss, int n,
+                                      void* d_scratch, cudaStream_t stream);
 
 }  // namespace clr

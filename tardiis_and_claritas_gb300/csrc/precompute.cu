@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <vector>
 #include "kernels.h"
 
 namespace clr {
@@ -302,16 +303,16 @@ __global__ void dummy_phase_kernel(double* theta, float* theta_f, double* cdf, f
 
 // PSD normalisation (:3615-3635), rates and channel CDFs (:3845-3921), channel rate arrays
 // (:6362-6375) and the float copies the photon kernel reads. n <= 64: one thread.
-__global__ void transport_kernel(int n, const double* __restrict__ d, const double* __restrict__ w_in,
-                                 const double* __restrict__ qext, const double* __restrict__ qsca,
-                                 const double* __restrict__ k_imag, const double* __restrict__ n_real,
-                                 double concentration, double density, int weight_mode, int em, double wave_scale,
-                                 double n_medium, double wavelength, double wave_rms, double* w, double* radius,
-                                 double* nden, double* mug, double* mus, double* mue, double* muw, double* muev,
-                                 double* gcdf, double* wcdf, double* pcdf, double* muscal, double* trace_geom,
-                                 double* trace_wave, float* gcdf_f, float* wcdf_f, float* pn_f, float* pk_f,
-                                 float* prad_f, int* error_flag) {
-    if (blockIdx.x || threadIdx.x) return;
+__device__ __noinline__ void transport_body(int n, const double* __restrict__ d, const double* __restrict__ w_in,
+                                            const double* __restrict__ qext, const double* __restrict__ qsca,
+                                            const double* __restrict__ k_imag, const double* __restrict__ n_real,
+                                            double concentration, double density, int weight_mode, int em,
+                                            double wave_scale, double n_medium, double wavelength, double wave_rms,
+                                            double* w, double* radius, double* nden, double* mug, double* mus,
+                                            double* mue, double* muw, double* muev, double* gcdf, double* wcdf,
+                                            double* pcdf, double* muscal, double* trace_geom, double* trace_wave,
+                                            float* gcdf_f, float* wcdf_f, float* pn_f, float* pk_f, float* prad_f,
+                                            int* error_flag) {
     if (n < 1 || n > CLR_MAX_BINS) { atomicCAS(error_flag, 0, 20); return; }
     if (!(density > 0.0) || concentration < 0.0) { atomicCAS(error_flag, 0, 21); return; }
     double sw0 = 0.0;
@@ -399,6 +400,31 @@ __global__ void transport_kernel(int n, const double* __restrict__ d, const doub
         pk_f[i] = (float)k_imag[i];
         prad_f[i] = (float)radius[i];
     }
+}
+
+// The rates of one scenario (a single thread) and of many scenarios in one launch (a thread per
+// scenario): both run transport_body, so every value is the same.
+struct TransportJob {
+    int n, weight_mode, em;
+    const double *d, *w_in, *qext, *qsca, *k_imag, *n_real;
+    double concentration, density, wave_scale, n_medium, wavelength, wave_rms;
+    double *w, *radius, *nden, *mug, *mus, *mue, *muw, *muev, *gcdf, *wcdf, *pcdf, *muscal, *trace_geom, *trace_wave;
+    float *gcdf_f, *wcdf_f, *pn_f, *pk_f, *prad_f;
+    int* error_flag;
+};
+__device__ __forceinline__ void transport_job(const TransportJob& j) {
+    transport_body(j.n, j.d, j.w_in, j.qext, j.qsca, j.k_imag, j.n_real, j.concentration, j.density, j.weight_mode,
+                   j.em, j.wave_scale, j.n_medium, j.wavelength, j.wave_rms, j.w, j.radius, j.nden, j.mug, j.mus,
+                   j.mue, j.muw, j.muev, j.gcdf, j.wcdf, j.pcdf, j.muscal, j.trace_geom, j.trace_wave, j.gcdf_f,
+                   j.wcdf_f, j.pn_f, j.pk_f, j.prad_f, j.error_flag);
+}
+__global__ void transport_kernel(TransportJob j) {
+    if (blockIdx.x || threadIdx.x) return;
+    transport_job(j);
+}
+__global__ void transport_batch_kernel(const TransportJob* __restrict__ jobs, int count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) transport_job(jobs[i]);
 }
 
 // Schiller-Naumann terminal velocity by damped Newton (:3925-3937)
@@ -565,10 +591,9 @@ __global__ void sediment_grid_max_kernel(const double* __restrict__ grid, long l
     if (threadIdx.x == 0) grid_max[p] = red[0];
 }
 
-__global__ void sediment_majorant_kernel(SedArgs a, const double* trace_geom, const double* trace_wave, double* sed_A,
-                                         double* sed_norm, double* sed_max, const double* grid_max,
-                                         double* major, int* error_flag) {
-    if (blockIdx.x || threadIdx.x) return;
+__device__ __noinline__ void majorant_body(const SedArgs& a, const double* trace_geom, const double* trace_wave,
+                                           double* sed_A, double* sed_norm, double* sed_max, const double* grid_max,
+                                           double* major, int* error_flag) {
     const int n = a.n;
     double mg = 0.0, mw = 0.0;
     if (a.TM == 0) {
@@ -594,6 +619,25 @@ __global__ void sediment_majorant_kernel(SedArgs a, const double* trace_geom, co
         mg = 0.0; mw = 0.0;
         for (int i = 0; i < n; ++i) { mg += trace_geom[i] * sed_max[i]; mw += trace_wave[i] * sed_max[i]; }
         major[0] = mg; major[1] = mw; major[2] = mg + mw;
+    }
+}
+
+struct MajorantJob {
+    SedArgs a;
+    const double *trace_geom, *trace_wave, *grid_max;
+    double *sed_A, *sed_norm, *sed_max, *major;
+    int* error_flag;
+};
+__global__ void sediment_majorant_kernel(MajorantJob j) {
+    if (blockIdx.x || threadIdx.x) return;
+    majorant_body(j.a, j.trace_geom, j.trace_wave, j.sed_A, j.sed_norm, j.sed_max, j.grid_max, j.major, j.error_flag);
+}
+__global__ void sediment_majorant_batch_kernel(const MajorantJob* __restrict__ jobs, int count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) {
+        const MajorantJob& j = jobs[i];
+        majorant_body(j.a, j.trace_geom, j.trace_wave, j.sed_A, j.sed_norm, j.sed_max, j.grid_max, j.major,
+                      j.error_flag);
     }
 }
 
@@ -703,40 +747,100 @@ cudaError_t enqueue_mie_phase(const double* d, const double* nr, const double* k
     return enqueue_mie_tables(d, nr, k, n, n_medium, wavelength, nt, true, CLR_MIE_MAX_ORDER, b, st);
 }
 
+static TransportJob transport_job_of(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps) {
+    TransportJob j;
+    j.n = pb.n; j.weight_mode = ps.weight_mode; j.em = sp.event_model;
+    j.d = pb.d; j.w_in = pb.w; j.qext = pb.qext; j.qsca = pb.qsca; j.k_imag = pb.kidx; j.n_real = pb.nidx;
+    j.concentration = ps.concentration_kg_m3; j.density = ps.density_kg_m3; j.wave_scale = ps.hybrid_wave_scale;
+    j.n_medium = ps.n_medium; j.wavelength = ps.wavelength_m; j.wave_rms = ps.wave_rms_height_m;
+    j.w = pb.w; j.radius = pb.radius; j.nden = pb.nden; j.mug = pb.mug; j.mus = pb.mus; j.mue = pb.mue;
+    j.muw = pb.muw; j.muev = pb.muev; j.gcdf = pb.gcdf; j.wcdf = pb.wcdf; j.pcdf = pb.pcdf; j.muscal = pb.muscal;
+    j.trace_geom = pb.trace_geom; j.trace_wave = pb.trace_wave; j.gcdf_f = pb.gcdf_f; j.wcdf_f = pb.wcdf_f;
+    j.pn_f = pb.pn_f; j.pk_f = pb.pk_f; j.prad_f = pb.prad_f; j.error_flag = pb.err;
+    return j;
+}
+
+static SedArgs sed_args_of(const ParticleBuffers& pb, const clr_scene_params& sp, const clr_sediment_spec& ss) {
+    SedArgs a;
+    a.n = pb.n; a.TM = sp.sediment_model; a.FSM = sp.free_surface_model; a.NQ = ss.n_quad; a.NRAD = ss.n_radial;
+    a.rho_p = ss.particle_density; a.rho_w = ss.water_density; a.mu = ss.water_viscosity; a.grav = ss.gravity;
+    a.Dt = ss.eddy_diffusivity; a.R = (double)sp.rin; a.ZMIN = (double)sp.zmin; a.ZMEAN = (double)sp.zmean;
+    a.DH = (double)sp.vortex_delta_h; a.CORE = (double)sp.vortex_core_radius;
+    return a;
+}
+
+static MajorantJob majorant_job_of(ParticleBuffers& pb, const SedArgs& a) {
+    MajorantJob j;
+    j.a = a; j.trace_geom = pb.trace_geom; j.trace_wave = pb.trace_wave; j.grid_max = a.TM == 3 ? pb.grid_max : nullptr;
+    j.sed_A = pb.sedA; j.sed_norm = pb.sed_norm; j.sed_max = pb.sed_max; j.major = pb.sed_major; j.error_flag = pb.err;
+    return j;
+}
+
+// Sediment bin coefficients (and the finite-Re slip table, the grid maxima) of one scenario.
+static void enqueue_sediment_bins(ParticleBuffers& pb, const SedArgs& a, cudaStream_t st) {
+    if (a.TM == 2 || a.TM == 3) {
+        dim3 g((a.NRAD + 127) / 128, a.n);
+        sediment_slip_kernel<<<g, 128, 0, st>>>(a, pb.d, pb.sed_wr);
+    }
+    sediment_bin_kernel<<<a.n, 32, 0, st>>>(a, pb.d, pb.sed_wr, pb.sedA, pb.sedB, pb.sed_norm, pb.sed_max,
+                                            pb.sed_radial_log, pb.sed_terms, pb.err);
+    if (a.TM == 3)
+        sediment_grid_max_kernel<<<a.n, 256, 0, st>>>(pb.sed_grid, (long long)pb.grid_nr * pb.grid_nz, pb.grid_max);
+}
+
+static cudaError_t enqueue_node_tables(ParticleBuffers& pb, cudaStream_t st) {
+    if (!pb.node_tables) return cudaSuccess;
+    const int plane = pb.grid_nr * pb.grid_nz;
+    cudaError_t e = cudaMemsetAsync(pb.node_major, 0, sizeof(float), st);
+    if (e != cudaSuccess) return e;
+    sediment_node_kernel<<<(2 * plane + 127) / 128, 128, 0, st>>>(pb.sed_grid, pb.trace_geom, pb.trace_wave, pb.n,
+                                                                  plane, pb.node_mu, pb.node_alias,
+                                                                  reinterpret_cast<unsigned int*>(pb.node_major));
+    return cudaSuccess;
+}
+
 // The scene-dependent rest of the precompute of one scenario, after its Mie tables: PSD normalisation
 // and rates, sediment coefficients, majorants and node tables.
 cudaError_t enqueue_scene_rates(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,
                                 const clr_sediment_spec& ss, cudaStream_t st) {
-    const int n = pb.n;
-    const int em = sp.event_model;
-    transport_kernel<<<1, 1, 0, st>>>(n, pb.d, pb.w, pb.qext, pb.qsca, pb.kidx, pb.nidx, ps.concentration_kg_m3,
-                                      ps.density_kg_m3, ps.weight_mode, em, ps.hybrid_wave_scale, ps.n_medium,
-                                      ps.wavelength_m, ps.wave_rms_height_m, pb.w, pb.radius, pb.nden, pb.mug, pb.mus,
-                                      pb.mue, pb.muw, pb.muev, pb.gcdf, pb.wcdf, pb.pcdf, pb.muscal, pb.trace_geom,
-                                      pb.trace_wave, pb.gcdf_f, pb.wcdf_f, pb.pn_f, pb.pk_f, pb.prad_f, pb.err);
-    SedArgs a;
-    a.n = n; a.TM = sp.sediment_model; a.FSM = sp.free_surface_model; a.NQ = ss.n_quad; a.NRAD = ss.n_radial;
-    a.rho_p = ss.particle_density; a.rho_w = ss.water_density; a.mu = ss.water_viscosity; a.grav = ss.gravity;
-    a.Dt = ss.eddy_diffusivity; a.R = (double)sp.rin; a.ZMIN = (double)sp.zmin; a.ZMEAN = (double)sp.zmean;
-    a.DH = (double)sp.vortex_delta_h; a.CORE = (double)sp.vortex_core_radius;
-    if (a.TM == 2 || a.TM == 3) {
-        dim3 g((a.NRAD + 127) / 128, n);
-        sediment_slip_kernel<<<g, 128, 0, st>>>(a, pb.d, pb.sed_wr);
+    transport_kernel<<<1, 1, 0, st>>>(transport_job_of(pb, sp, ps));
+    const SedArgs a = sed_args_of(pb, sp, ss);
+    enqueue_sediment_bins(pb, a, st);
+    sediment_majorant_kernel<<<1, 1, 0, st>>>(majorant_job_of(pb, a));
+    cudaError_t e = enqueue_node_tables(pb, st);
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+size_t scene_rates_batch_scratch(int n) { return (size_t)n * (sizeof(TransportJob) + sizeof(MajorantJob)) + 256; }
+
+// The same for n scenarios: the one-thread rate and majorant kernels of all scenarios run as one launch
+// each (a thread per scenario); the sediment bins and node tables stay per scenario. `d_scratch` holds
+// scene_rates_batch_scratch(n) bytes of device memory for the job descriptions.
+cudaError_t enqueue_scene_rates_batch(ParticleBuffers* const* pbs, const clr_scene_params* sps,
+                                      const clr_particle_spec* pss, const clr_sediment_spec* sss, int n,
+                                      void* d_scratch, cudaStream_t st) {
+    std::vector<TransportJob> tj(n);
+    std::vector<MajorantJob> mj(n);
+    std::vector<SedArgs> sa(n);
+    for (int i = 0; i < n; ++i) {
+        tj[i] = transport_job_of(*pbs[i], sps[i], pss[i]);
+        sa[i] = sed_args_of(*pbs[i], sps[i], sss[i]);
+        mj[i] = majorant_job_of(*pbs[i], sa[i]);
     }
-    sediment_bin_kernel<<<n, 32, 0, st>>>(a, pb.d, pb.sed_wr, pb.sedA, pb.sedB, pb.sed_norm, pb.sed_max,
-                                          pb.sed_radial_log, pb.sed_terms, pb.err);
-    if (a.TM == 3)
-        sediment_grid_max_kernel<<<n, 256, 0, st>>>(pb.sed_grid, (long long)pb.grid_nr * pb.grid_nz, pb.grid_max);
-    sediment_majorant_kernel<<<1, 1, 0, st>>>(a, pb.trace_geom, pb.trace_wave, pb.sedA, pb.sed_norm, pb.sed_max,
-                                              a.TM == 3 ? pb.grid_max : nullptr, pb.sed_major, pb.err);
-    if (pb.node_tables) {
-        const int plane = pb.grid_nr * pb.grid_nz;
-        cudaError_t e = cudaMemsetAsync(pb.node_major, 0, sizeof(float), st);
-        if (e != cudaSuccess) return e;
-        sediment_node_kernel<<<(2 * plane + 127) / 128, 128, 0, st>>>(
-            pb.sed_grid, pb.trace_geom, pb.trace_wave, n, plane, pb.node_mu, pb.node_alias,
-            reinterpret_cast<unsigned int*>(pb.node_major));
-    }
+    TransportJob* d_tj = static_cast<TransportJob*>(d_scratch);
+    MajorantJob* d_mj = reinterpret_cast<MajorantJob*>(
+        (reinterpret_cast<uintptr_t>(d_tj + n) + 255) & ~(uintptr_t)255);
+    // pageable sources: the copies are staged before the calls return
+    cudaError_t e = cudaMemcpyAsync(d_tj, tj.data(), n * sizeof(TransportJob), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(d_mj, mj.data(), n * sizeof(MajorantJob), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    transport_batch_kernel<<<(n + 63) / 64, 64, 0, st>>>(d_tj, n);
+    for (int i = 0; i < n; ++i) enqueue_sediment_bins(*pbs[i], sa[i], st);
+    sediment_majorant_batch_kernel<<<(n + 63) / 64, 64, 0, st>>>(d_mj, n);
+    for (int i = 0; i < n; ++i)
+        if ((e = enqueue_node_tables(*pbs[i], st)) != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
