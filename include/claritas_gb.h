@@ -144,8 +144,17 @@ typedef struct clr_sediment_spec {
     double particle_density, water_density, water_viscosity, gravity, eddy_diffusivity;
     int32_t n_quad, n_radial;
     int32_t grid_nr, grid_nz;
-    const double* grid;             /* nullable unless sediment_model == 3 */
-    double grid_zmax;
+    const double* grid;             /* sediment model 3: a supplied field, or NULL to solve it (below) */
+    double grid_zmax;               /* top of the (r,z) grid: the free surface at the wall */
+    /* FP64 cell geometry of the sediment precompute, as the reference passes it to those kernels
+     * (float64 arguments, CLARITAS/CLARITAS.py:6413-6418); rin = 0 widens the scene's FP32 values */
+    double rin, zmin, zmean, vortex_delta_h, vortex_core_radius;
+    /* sediment model 3 with grid == NULL: the field is solved on the device on meridional_nr x
+     * meridional_nz cells, the reference's meridional advection-diffusion solver
+     * (CLARITAS/CLARITAS.py:4040-4215 driven by :6451-6725; defaults 48 x 96, 8000 iterations, check
+     * every 250, tolerance 1e-6, SOR 1.75; peak speed = circulation ratio x peak azimuthal speed) */
+    int32_t meridional_nr, meridional_nz, solver_max_iterations, solver_check_interval;
+    double solver_tolerance, solver_sor, meridional_peak_speed;
 } clr_sediment_spec;
 
 /* One transport run over a contiguous range of global ray ids. The three
@@ -314,6 +323,13 @@ int clr_sweep_build(clr_ctx* ctx, int n_scenarios, const clr_scene_params* scene
  * ray offset) traces scenario i, tallies into outs[i]; n_runs must equal the sweep's scenario count
  * and the runs share rng_mode, weight_mode and flags. */
 int clr_sweep_trace(clr_ctx* ctx, const clr_run_params* runs, int n_runs, clr_tallies* outs);
+
+/* The resident (r,z) sediment field of the current scene (sediment model 3): grid_out (nullable)
+ * receives [bins][nr][nz] doubles (the solved field after the reference's column extension, or the
+ * supplied one); iterations and max_residual (nullable) the solver's iteration count and final largest
+ * residual (0 for a supplied grid), the reference's meridional_solver_iterations / _max_residual. */
+int clr_read_sediment_field(clr_ctx* ctx, double* grid_out, int32_t* nr, int32_t* nz, int32_t* iterations,
+                            double* max_residual);
 
 /* clr_read_particle_physics for scenario `scenario` of the built sweep. */
 int clr_sweep_read_particle_physics(clr_ctx* ctx, int scenario, clr_particle_physics* out);

@@ -367,8 +367,13 @@ int clo_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, const c
     S->sed_A = zalloc(n); S->sed_B = zalloc(n); S->sed_norm = zalloc(n); S->sed_max = zalloc(n);
     S->sed_radial_log = zalloc((size_t)n * NRAD); S->sed_major = zalloc(4);
     const int TM = sp->sediment_model, FSM = sp->free_surface_model;
-    const double R = (double)sp->rin, ZMIN = (double)sp->zmin, ZMEAN = (double)sp->zmean;
-    const double DH = (double)sp->vortex_delta_h, CORE = (double)sp->vortex_core_radius;
+    /* FP64 geometry as the reference passes it (float64 arguments, CLARITAS/CLARITAS.py:6413-6418);
+       a spec without it widens the scene's FP32 values */
+    const int g64 = ss->rin > 0.0;
+    const double R = g64 ? ss->rin : (double)sp->rin, ZMIN = g64 ? ss->zmin : (double)sp->zmin;
+    const double ZMEAN = g64 ? ss->zmean : (double)sp->zmean;
+    const double DH = g64 ? ss->vortex_delta_h : (double)sp->vortex_delta_h;
+    const double CORE = g64 ? ss->vortex_core_radius : (double)sp->vortex_core_radius;
     if (TM == 0) {
         double mg = 0.0, mw = 0.0;
         for (int i = 0; i < n; ++i) { S->sed_norm[i] = 1.0; S->sed_max[i] = 1.0; mg += S->trace_geom[i]; mw += S->trace_wave[i]; }

@@ -4,7 +4,7 @@
 // tests/golden/make_gpu_fixtures.py (nvcc, sm_103a) from the reference source
 // extracted by oracle/ref_extract.py. It replays the reference host's launch
 // sequence: the precompute of _prepare_gpu_particle_physics
-// (CLARITAS/CLARITAS.py:6147-6449, :6694-6725 for a supplied model-3 grid) and,
+// (CLARITAS/CLARITAS.py:6147-6449, the meridional solver :6451-6725 or a supplied model-3 grid) and,
 // per chunk, trace_kernel with its 234 arguments (:7638-7758) followed by
 // score_detectors_kernel (:7783-7847) on 256-thread blocks. Its per-ray
 // outputs are the bit-exact target for the library's xorshift parity mode.
@@ -33,6 +33,8 @@ struct RefGpu {
     double *sed_tau, *sed_ws, *sed_sre, *sed_sdrag, *sed_A, *sed_B, *sed_norm, *sed_max, *sed_min, *sed_rmax, *sed_rre,
         *sed_rcenter, *sed_radial_log, *sed_radial_wr, *sed_sc, *sed_sw, *sed_bc, *sed_bw, *sed_major, *sed_grid;
     int* err;
+    int solver_iterations = 0;
+    double solver_residual = 0.0;
     std::string msg;
 };
 
@@ -155,17 +157,79 @@ int clrefgpu_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, co
     A(sed_radial_wr, (size_t)n * NR) A(sed_sc, n) A(sed_sw, n) A(sed_bc, n) A(sed_bw, n) A(sed_major, 4)
     cudaMemset(S->sed_major, 0, 4 * 8);
     cudaMemset(S->err, 0, sizeof(int));
+    // FP64 geometry as the reference's host passes it (:6413-6418), else the scene's FP32 values widened
+    const bool g64 = ss->rin > 0.0;
+    const double GR = g64 ? ss->rin : (double)sp->rin, GZMIN = g64 ? ss->zmin : (double)sp->zmin;
+    const double GZMEAN = g64 ? ss->zmean : (double)sp->zmean;
+    const double GDH = g64 ? ss->vortex_delta_h : (double)sp->vortex_delta_h;
+    const double GCORE = g64 ? ss->vortex_core_radius : (double)sp->vortex_core_radius;
     sediment_transport_precompute_kernel<<<1, 1>>>(
         S->d, n, sp->sediment_model, ss->particle_density, ss->water_density, ss->water_viscosity, ss->gravity,
-        ss->eddy_diffusivity, (double)sp->rin, (double)sp->zmin, (double)sp->zmean, sp->free_surface_model,
-        (double)sp->vortex_delta_h, (double)sp->vortex_core_radius, ss->n_quad, NR, S->trace_geom, S->trace_wave,
+        ss->eddy_diffusivity, GR, GZMIN, GZMEAN, sp->free_surface_model,
+        GDH, GCORE, ss->n_quad, NR, S->trace_geom, S->trace_wave,
         S->sed_tau, S->sed_ws, S->sed_sre, S->sed_sdrag, S->sed_A, S->sed_B, S->sed_norm, S->sed_max, S->sed_rmax,
         S->sed_rre, S->sed_rcenter, S->sed_radial_log, S->sed_radial_wr, S->sed_sc, S->sed_sw, S->sed_bc, S->sed_bw,
         S->sed_major, S->err);
     rc = check(S, "sediment precompute");
     if (rc) return rc;
     S->grid_zmax = (float)ss->grid_zmax;
-    if (sp->sediment_model == 3) {
+    if (sp->sediment_model == 3 && !ss->grid) {
+        // the reference's meridional solver, launched as its host does (:6451-6725)
+        const int GNR = ss->meridional_nr, GNZ = ss->meridional_nz, FSM = sp->free_surface_model;
+        S->grid_nr = GNR; S->grid_nz = GNZ;
+        const size_t plane = (size_t)GNR * GNZ, total = plane * n;
+        A(sed_grid, total)
+        unsigned char* active;
+        double *ap, *ae, *aw, *an, *as, *residual;
+        dmalloc(S, &active, plane);
+        dmalloc(S, &ap, total); dmalloc(S, &ae, total); dmalloc(S, &aw, total); dmalloc(S, &an, total);
+        dmalloc(S, &as, total); dmalloc(S, &residual, n);
+        const int th = 256, bp = (int)((plane + th - 1) / th), bt = (int)((total + th - 1) / th);
+        const double ZG = ss->grid_zmax;
+        meridional_active_mask_kernel<<<bp, th>>>(GNR, GNZ, GR, GZMIN, ZG, GZMEAN, FSM, GDH, GCORE, active);
+        meridional_grid_initialize_kernel<<<bt, th>>>(n, GNR, GNZ, GR, GZMIN, ZG, FSM, GCORE, S->sed_A, S->sed_B,
+                                                      S->sed_norm, S->sed_radial_log, NR, active, S->sed_grid);
+        meridional_build_coefficients_kernel<<<bt, th>>>(n, GNR, GNZ, GR, GZMIN, ZG, GZMEAN, FSM, GDH, GCORE,
+                                                         ss->meridional_peak_speed, ss->eddy_diffusivity, S->sed_ws,
+                                                         S->sed_radial_wr, NR, active, ap, ae, aw, an, as);
+        cudaMemset(S->err, 0, sizeof(int));
+        meridional_normalize_kernel<<<n, 1>>>(n, GNR, GNZ, GR, GZMIN, ZG, GZMEAN, active, S->sed_grid, S->err);
+        rc = check(S, "meridional initial normalization");
+        if (rc) return rc;
+        const int max_it = ss->solver_max_iterations, every = ss->solver_check_interval;
+        const int min_it = max_it < 1000 ? max_it : 1000;
+        int iters = 0, last = 0;
+        std::vector<double> res(n, 0.0);
+        for (int it = 1; it <= max_it; ++it) {
+            meridional_relax_kernel<<<bt, th>>>(n, GNR, GNZ, 0, ss->solver_sor, active, ap, ae, aw, an, as, S->sed_grid);
+            meridional_relax_kernel<<<bt, th>>>(n, GNR, GNZ, 1, ss->solver_sor, active, ap, ae, aw, an, as, S->sed_grid);
+            if (it % 20 == 0)
+                meridional_normalize_kernel<<<n, 1>>>(n, GNR, GNZ, GR, GZMIN, ZG, GZMEAN, active, S->sed_grid, S->err);
+            if (it % every == 0 || it == max_it) {
+                meridional_normalize_kernel<<<n, 1>>>(n, GNR, GNZ, GR, GZMIN, ZG, GZMEAN, active, S->sed_grid, S->err);
+                meridional_residual_kernel<<<n, 1>>>(n, GNR, GNZ, active, ap, ae, aw, an, as, S->sed_grid, residual);
+                rc = check(S, "meridional normalization");
+                if (rc) return rc;
+                cudaMemcpy(res.data(), residual, n * 8, cudaMemcpyDeviceToHost);
+                last = it;
+                double mx = 0.0;
+                for (double v : res) mx = v > mx ? v : mx;
+                if (it >= min_it && mx <= ss->solver_tolerance) { iters = it; break; }
+            }
+        }
+        if (iters == 0) iters = last ? last : max_it;
+        double mx = 0.0;
+        for (double v : res) mx = v > mx ? v : mx;
+        S->solver_iterations = iters;
+        S->solver_residual = mx;
+        if (mx > ss->solver_tolerance) { S->msg = "meridional transport solver did not converge"; return -7; }
+        meridional_extend_grid_kernel<<<(n * GNR + th - 1) / th, th>>>(n, GNR, GNZ, active, S->sed_grid);
+        meridional_finalize_kernel<<<n, 1>>>(n, GNR, GNZ, GR, GZMIN, ZG, active, S->sed_grid, S->sed_norm, S->sed_max,
+                                             S->sed_min, S->sed_sc, S->sed_sw, S->sed_bc, S->sed_bw);
+        meridional_majorants_kernel<<<1, 1>>>(n, S->trace_geom, S->trace_wave, S->sed_max, S->sed_major);
+        rc = check(S, "meridional majorants");
+        if (rc) return rc;
+    } else if (sp->sediment_model == 3) {
         S->grid_nr = ss->grid_nr; S->grid_nz = ss->grid_nz;
         const size_t plane = (size_t)ss->grid_nr * ss->grid_nz;
         A(sed_grid, plane * n)
@@ -173,7 +237,7 @@ int clrefgpu_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, co
         unsigned char* active;
         dmalloc(S, &active, plane);
         cudaMemset(active, 1, plane);
-        meridional_finalize_kernel<<<n, 1>>>(n, ss->grid_nr, ss->grid_nz, (double)sp->rin, (double)sp->zmin,
+        meridional_finalize_kernel<<<n, 1>>>(n, ss->grid_nr, ss->grid_nz, GR, GZMIN,
                                              ss->grid_zmax, active, S->sed_grid, S->sed_norm, S->sed_max, S->sed_min,
                                              S->sed_sc, S->sed_sw, S->sed_bc, S->sed_bw);
         meridional_majorants_kernel<<<1, 1>>>(n, S->trace_geom, S->trace_wave, S->sed_max, S->sed_major);
@@ -186,6 +250,16 @@ int clrefgpu_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, co
     }
     return 0;
 #undef A
+}
+
+int clrefgpu_read_sediment_field(void* h, double* grid, int* nr, int* nz, int* iterations, double* max_residual) {
+    RefGpu* S = (RefGpu*)h;
+    if (nr) *nr = S->grid_nr;
+    if (nz) *nz = S->grid_nz;
+    if (iterations) *iterations = S->solver_iterations;
+    if (max_residual) *max_residual = S->solver_residual;
+    if (grid) cudaMemcpy(grid, S->sed_grid, (size_t)S->n * S->grid_nr * S->grid_nz * 8, cudaMemcpyDeviceToHost);
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
 }
 
 int clrefgpu_read_physics(void* h, clr_particle_physics* o) {

@@ -178,10 +178,16 @@ int clref_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, const
     S->sed_radial_wr.assign((size_t)n * NR, 0.0); S->sed_sc = arr(); S->sed_sw = arr(); S->sed_bc = arr();
     S->sed_bw = arr(); S->sed_major.assign(4, 0.0);
     set_index(1, 0);
+    // FP64 geometry as the reference's host passes it (:6413-6418), else the scene's FP32 values widened
+    const bool g64 = ss->rin > 0.0;
+    const double GR = g64 ? ss->rin : (double)sp->rin, GZMIN = g64 ? ss->zmin : (double)sp->zmin;
+    const double GZMEAN = g64 ? ss->zmean : (double)sp->zmean;
+    const double GDH = g64 ? ss->vortex_delta_h : (double)sp->vortex_delta_h;
+    const double GCORE = g64 ? ss->vortex_core_radius : (double)sp->vortex_core_radius;
     sediment_transport_precompute_kernel(
         S->d.data(), n, sp->sediment_model, ss->particle_density, ss->water_density, ss->water_viscosity,
-        ss->gravity, ss->eddy_diffusivity, (double)sp->rin, (double)sp->zmin, (double)sp->zmean,
-        sp->free_surface_model, (double)sp->vortex_delta_h, (double)sp->vortex_core_radius, ss->n_quad, NR,
+        ss->gravity, ss->eddy_diffusivity, GR, GZMIN, GZMEAN,
+        sp->free_surface_model, GDH, GCORE, ss->n_quad, NR,
         S->trace_geom.data(), S->trace_wave.data(), S->sed_tau.data(), S->sed_ws.data(), S->sed_sre.data(),
         S->sed_sdrag.data(), S->sed_A.data(), S->sed_B.data(), S->sed_norm.data(), S->sed_max.data(),
         S->sed_rmax.data(), S->sed_rre.data(), S->sed_rcenter.data(), S->sed_radial_log.data(),
@@ -198,7 +204,7 @@ int clref_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, const
         std::vector<unsigned char> active(plane, 1);
         for (int p = 0; p < n; ++p) {
             set_index(1, p);
-            meridional_finalize_kernel(n, ss->grid_nr, ss->grid_nz, (double)sp->rin, (double)sp->zmin,
+            meridional_finalize_kernel(n, ss->grid_nr, ss->grid_nz, GR, GZMIN,
                                        ss->grid_zmax, active.data(), S->sed_grid.data(), S->sed_norm.data(),
                                        S->sed_max.data(), S->sed_min.data(), S->sed_sc.data(), S->sed_sw.data(),
                                        S->sed_bc.data(), S->sed_bw.data());

@@ -115,6 +115,10 @@ class SedimentSpec(C.Structure):
         ("eddy_diffusivity", f64),
         ("n_quad", i32), ("n_radial", i32), ("grid_nr", i32), ("grid_nz", i32),
         ("grid", PD), ("grid_zmax", f64),
+        ("rin", f64), ("zmin", f64), ("zmean", f64), ("vortex_delta_h", f64), ("vortex_core_radius", f64),
+        ("meridional_nr", i32), ("meridional_nz", i32), ("solver_max_iterations", i32),
+        ("solver_check_interval", i32), ("solver_tolerance", f64), ("solver_sor", f64),
+        ("meridional_peak_speed", f64),
     ]
 
 

@@ -181,18 +181,58 @@ static int check_particles(clr_ctx* ctx, const clr_scene_params& sp, const clr_p
             return fail(ctx, CLR_ERR_PRECOMPUTE, "sediment transport precompute failed with error code 32");
         if (!((double)sp.zmean - (double)sp.zmin > 0.0))
             return fail(ctx, CLR_ERR_PRECOMPUTE, "sediment transport precompute failed with error code 33");
-        if (sp.sediment_model == 3 && (!ss->grid || ss->grid_nr < 2 || ss->grid_nz < 2))
-            return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "sediment model 3 needs a [bins][nr][nz] grid");
+        if (sp.sediment_model == 3 && ss->grid && (ss->grid_nr < 2 || ss->grid_nz < 2))
+            return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "a supplied model-3 grid needs at least 2 x 2 cells");
+        if (sp.sediment_model == 3 && !ss->grid) {
+            // the reference's constructor rules for the solver settings (:5867-5887)
+            if (ss->meridional_nr < 16 || ss->meridional_nz < 32)
+                return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "meridional grid must be at least 16 x 32 cells");
+            if (ss->solver_max_iterations < 250 || ss->solver_check_interval < 10)
+                return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "meridional solver needs >= 250 iterations, checks every >= 10");
+            if (!(ss->solver_tolerance > 0.0 && ss->solver_tolerance < 1e-2))
+                return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "meridional_solver_tolerance must be in (0,1e-2)");
+            if (!(ss->solver_sor >= 1.0 && ss->solver_sor < 1.95))
+                return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "meridional_solver_sor must be in [1,1.95)");
+            if (!(ss->meridional_peak_speed >= 0.0) || !(ss->grid_zmax > (double)sp.zmin))
+                return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "meridional peak speed and grid top must be valid");
+            if ((size_t)ss->meridional_nr * ss->meridional_nz * 9 > 200 * 1024)
+                return fail(ctx, CLR_ERR_UNSUPPORTED, "meridional grid of %d x %d cells exceeds one CTA's shared memory",
+                            ss->meridional_nr, ss->meridional_nz);
+            if (n > 152) return fail(ctx, CLR_ERR_UNSUPPORTED, "meridional solver runs one CTA per bin (<= 152)");
+        }
     }
     return CLR_OK;
 }
 
+// The sediment spec with its FP64 geometry filled from the scene where the caller left it zero.
+static clr_sediment_spec filled_sediment(const clr_scene_params& sp, const clr_sediment_spec& ss) {
+    clr_sediment_spec o = ss;
+    if (!(o.rin > 0.0)) {
+        o.rin = (double)sp.rin; o.zmin = (double)sp.zmin; o.zmean = (double)sp.zmean;
+        o.vortex_delta_h = (double)sp.vortex_delta_h; o.vortex_core_radius = (double)sp.vortex_core_radius;
+    }
+    return o;
+}
+
+// The (r, z) grid of a model-3 scene: the supplied one's shape or the solver's.
+static bool solves_grid(const clr_scene_params& sp, const clr_sediment_spec& ss) {
+    return sp.sediment_model == 3 && !ss.grid;
+}
+static int grid_nr_of(const clr_scene_params& sp, const clr_sediment_spec& ss) {
+    return sp.sediment_model != 3 ? 2 : (ss.grid ? ss.grid_nr : ss.meridional_nr);
+}
+static int grid_nz_of(const clr_scene_params& sp, const clr_sediment_spec& ss) {
+    return sp.sediment_model != 3 ? 2 : (ss.grid ? ss.grid_nz : ss.meridional_nz);
+}
+
 // Node tables pay off (and are exact) for a model-3 grid with no negative value and a moderate size.
+// (A solved field is positive everywhere: the solver clamps at 1e-14 and extends from liquid cells.)
 static bool wants_node_tables(const clr_scene_params& sp, const clr_sediment_spec& ss, int n, size_t grid_cells) {
     if (sp.sediment_model != 3) return false;
     bool nonneg = ss.grid_zmax > (double)sp.zmin;
-    for (size_t c = 0; c < grid_cells && nonneg; ++c) nonneg = ss.grid[c] >= 0.0;
-    const size_t plane = (size_t)ss.grid_nr * ss.grid_nz;
+    if (ss.grid)
+        for (size_t c = 0; c < grid_cells && nonneg; ++c) nonneg = ss.grid[c] >= 0.0;
+    const size_t plane = (size_t)grid_nr_of(sp, ss) * grid_nz_of(sp, ss);
     return nonneg && 2 * plane * n * sizeof(int2) <= (size_t(1) << 30);
 }
 
@@ -209,29 +249,31 @@ int clr_set_scene(clr_ctx* ctx, const clr_scene_params* scene) {
     return CLR_OK;
 }
 
-int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sediment_spec* ss) {
-    if (!ctx || !ps || !ss) return CLR_ERR_INVALID_ARGUMENT;
+int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sediment_spec* ss_in) {
+    if (!ctx || !ps || !ss_in) return CLR_ERR_INVALID_ARGUMENT;
     if (!ctx->scene_set) return fail(ctx, CLR_ERR_NOT_READY, "clr_set_scene must be called first");
     const clr_scene_params& sp = ctx->sp;
     {
-        const int rc = check_particles(ctx, sp, ps, ss);
+        const int rc = check_particles(ctx, sp, ps, ss_in);
         if (rc != CLR_OK) return rc;
     }
+    const clr_sediment_spec sse = filled_sediment(sp, *ss_in);
+    const clr_sediment_spec* ss = &sse;
     const int n = ps->n_bins;
     const int nt = hybrid_model(sp) ? ps->n_theta : 2;
     CU(cudaSetDevice(ctx->device));
     free_particles(ctx);
     ParticleBuffers& pb = ctx->pb;
     pb.n = n; pb.nt = nt; pb.n_radial = ss->n_radial;
-    pb.grid_nr = sp.sediment_model == 3 ? ss->grid_nr : 2;
-    pb.grid_nz = sp.sediment_model == 3 ? ss->grid_nz : 2;
+    pb.grid_nr = grid_nr_of(sp, *ss);
+    pb.grid_nz = grid_nz_of(sp, *ss);
     pb.grid_zmax = ss->grid_zmax;
     auto D = [&](double** p, size_t cnt) { return dalloc(ctx, (void**)p, cnt * sizeof(double)); };
     auto F = [&](float** p, size_t cnt) { return dalloc(ctx, (void**)p, cnt * sizeof(float)); };
     double** darr[] = {&pb.d, &pb.w, &pb.nidx, &pb.kidx, &pb.x, &pb.qext, &pb.qsca, &pb.qabs, &pb.qback, &pb.g,
                        &pb.albedo, &pb.radius, &pb.nden, &pb.mug, &pb.mus, &pb.mue, &pb.muw, &pb.muev, &pb.gcdf,
                        &pb.wcdf, &pb.pcdf, &pb.moment_a, &pb.moment_b, &pb.trace_geom, &pb.trace_wave, &pb.sedA,
-                       &pb.sedB, &pb.sed_norm, &pb.sed_max, &pb.grid_max};
+                       &pb.sedB, &pb.sed_norm, &pb.sed_max, &pb.grid_max, &pb.sed_ws};
     for (double** p : darr) CU(D(p, n));
     float** farr[] = {&pb.gcdf_f, &pb.wcdf_f, &pb.pn_f, &pb.pk_f, &pb.prad_f};
     for (float** p : farr) CU(F(p, n));
@@ -276,21 +318,56 @@ int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sed
             CU(dalloc(ctx, (void**)&pb.node_alias, 2 * plane * n * sizeof(int2)));
             CU(dalloc(ctx, (void**)&pb.node_major, sizeof(float)));
         }
-        CU(cudaMemcpyAsync(pb.sed_grid, ss->grid, grid_cells * sizeof(double), cudaMemcpyHostToDevice, st));
+        if (ss->grid) {
+            CU(cudaMemcpyAsync(pb.sed_grid, ss->grid, grid_cells * sizeof(double), cudaMemcpyHostToDevice, st));
+        } else {
+            CU(D(&pb.merid_coef, meridional_coef_doubles(n, pb.grid_nr, pb.grid_nz)));
+            CU(D(&pb.merid_residual, 2 * (size_t)n + 1));
+            CU(dalloc(ctx, (void**)&pb.merid_bar, 2 * sizeof(unsigned)));
+            CU(dalloc(ctx, (void**)&pb.merid_stats, sizeof(int)));
+        }
     } else {
         const double one[4] = {1.0, 1.0, 1.0, 1.0};
         CU(cudaMemcpyAsync(pb.sed_grid, one, sizeof(double), cudaMemcpyHostToDevice, st));
     }
-    CU(enqueue_particle_precompute(pb, sp, *ps, *ss, nullptr, st));
+    CU(enqueue_particle_precompute(pb, sp, *ps, *ss, nullptr, st));  // ss: FP64 geometry filled
     int herr = 0;
     CU(cudaMemcpyAsync(&herr, pb.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     if (pb.node_tables)
         CU(cudaMemcpyAsync(&pb.node_major_host, pb.node_major, sizeof(float), cudaMemcpyDeviceToHost, st));
     CU(cudaMemcpyAsync(pb.muscal_host, pb.muscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
     CU(cudaMemcpyAsync(pb.sed_major_host, pb.sed_major, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (pb.merid_coef) {
+        CU(cudaMemcpyAsync(&pb.solver_iterations, pb.merid_stats, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(&pb.solver_max_residual, pb.merid_residual + 2 * (size_t)n, sizeof(double),
+                           cudaMemcpyDeviceToHost, st));
+    }
     CU(cudaStreamSynchronize(st));
     if (herr) return fail(ctx, CLR_ERR_PRECOMPUTE, "particle precompute failed with error code %d", herr);
+    if (pb.merid_coef && pb.solver_max_residual > ss->solver_tolerance)
+        return fail(ctx, CLR_ERR_PRECOMPUTE,
+                    "meridional transport solver did not converge: max residual=%.6g after %d iterations",
+                    pb.solver_max_residual, pb.solver_iterations);
     ctx->built = true;
+    return CLR_OK;
+}
+
+int clr_read_sediment_field(clr_ctx* ctx, double* grid_out, int32_t* nr, int32_t* nz, int32_t* iterations,
+                            double* max_residual) {
+    if (!ctx) return CLR_ERR_INVALID_ARGUMENT;
+    if (!ctx->built) return fail(ctx, CLR_ERR_NOT_READY, "particles not built");
+    const ParticleBuffers& pb = ctx->pb;
+    if (ctx->sp.sediment_model != 3) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "the scene has no (r,z) field");
+    if (nr) *nr = pb.grid_nr;
+    if (nz) *nz = pb.grid_nz;
+    if (iterations) *iterations = pb.merid_coef ? pb.solver_iterations : 0;
+    if (max_residual) *max_residual = pb.merid_coef ? pb.solver_max_residual : 0.0;
+    if (grid_out) {
+        CU(cudaSetDevice(ctx->device));
+        CU(cudaMemcpyAsync(grid_out, pb.sed_grid, (size_t)pb.n * pb.grid_nr * pb.grid_nz * sizeof(double),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
+    }
     return CLR_OK;
 }
 
@@ -537,7 +614,7 @@ static double* ParticleBuffers::* const kBinF64[] = {
     &ParticleBuffers::muev, &ParticleBuffers::gcdf, &ParticleBuffers::wcdf, &ParticleBuffers::pcdf,
     &ParticleBuffers::moment_a, &ParticleBuffers::moment_b, &ParticleBuffers::trace_geom,
     &ParticleBuffers::trace_wave, &ParticleBuffers::sedA, &ParticleBuffers::sedB, &ParticleBuffers::sed_norm,
-    &ParticleBuffers::sed_max, &ParticleBuffers::grid_max};
+    &ParticleBuffers::sed_max, &ParticleBuffers::grid_max, &ParticleBuffers::sed_ws};
 static float* ParticleBuffers::* const kBinF32[] = {&ParticleBuffers::gcdf_f, &ParticleBuffers::wcdf_f,
                                                    &ParticleBuffers::pn_f, &ParticleBuffers::pk_f,
                                                    &ParticleBuffers::prad_f};
@@ -597,6 +674,12 @@ static void sweep_carve(Arena& A, const SweepLayout& L, std::vector<ParticleBuff
             pb.node_mu = A.take<float2>(plane);
             pb.node_alias = A.take<int2>(2 * plane * pb.n);
         }
+        if (pb.solver_iterations < 0) {  // marks a scenario whose model-3 field is solved
+            pb.merid_coef = A.take<double>(meridional_coef_doubles(pb.n, pb.grid_nr, pb.grid_nz));
+            pb.merid_residual = A.take<double>(2 * (size_t)pb.n + 1);
+            pb.merid_bar = A.take<unsigned>(2);
+            pb.merid_stats = A.take<int>(1);
+        }
     }
     for (size_t g = 0; g + 1 < L.group_first.size(); ++g) {
         const int nt = pbs[L.group_first[g]].nt;
@@ -610,10 +693,13 @@ static void sweep_carve(Arena& A, const SweepLayout& L, std::vector<ParticleBuff
 constexpr int kSweepChunkBins = 4096;
 
 static int sweep_build(clr_ctx* ctx, int ns, const clr_scene_params* sps, const clr_particle_spec* pss,
-                       const clr_sediment_spec* sss) {
+                       const clr_sediment_spec* sss_in) {
     ctx->sw_sp.clear();
     ctx->sw_pb.clear();
-    if (ns < 1 || !sps || !pss || !sss) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "clr_sweep_build: no scenarios");
+    if (ns < 1 || !sps || !pss || !sss_in) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "clr_sweep_build: no scenarios");
+    std::vector<clr_sediment_spec> fss(ns);
+    for (int i = 0; i < ns; ++i) fss[i] = filled_sediment(sps[i], sss_in[i]);
+    const clr_sediment_spec* sss = fss.data();
     std::vector<ParticleBuffers> pbs(ns);
     SweepLayout L;
     L.bin_off.resize(ns + 1); L.tab_off.resize(ns + 1); L.rad_off.resize(ns + 1); L.quad_off.resize(ns + 1);
@@ -631,9 +717,10 @@ static int sweep_build(clr_ctx* ctx, int ns, const clr_scene_params* sps, const 
         pb.n = n;
         pb.nt = hybrid_model(sp) ? pss[i].n_theta : 2;
         pb.n_radial = sss[i].n_radial;
-        pb.grid_nr = sp.sediment_model == 3 ? sss[i].grid_nr : 2;
-        pb.grid_nz = sp.sediment_model == 3 ? sss[i].grid_nz : 2;
+        pb.grid_nr = grid_nr_of(sp, sss[i]);
+        pb.grid_nz = grid_nz_of(sp, sss[i]);
         pb.grid_zmax = sss[i].grid_zmax;
+        if (solves_grid(sp, sss[i])) pb.solver_iterations = -1;
         const long long cells = sp.sediment_model == 3 ? (long long)pb.grid_nr * pb.grid_nz * n : 1;
         pb.node_tables = wants_node_tables(sp, sss[i], n, (size_t)cells) ? 1 : 0;
         L.bin_off[i] = L.bins; L.bins += n;
@@ -681,7 +768,7 @@ static int sweep_build(clr_ctx* ctx, int ns, const clr_scene_params* sps, const 
                 pbs[i].any_moment |= ps.moment_mode[b] ? 1 : 0;
             }
         }
-        if (sps[i].sediment_model == 3)
+        if (sps[i].sediment_model == 3 && sss[i].grid)
             std::copy(sss[i].grid, sss[i].grid + (L.cell_off[i + 1] - L.cell_off[i]), cells.begin() + L.cell_off[i]);
     }
     const ParticleBuffers& P0 = pbs[0];  // per-bin arrays start at scenario 0's slices
@@ -756,10 +843,21 @@ static int sweep_build(clr_ctx* ctx, int ns, const clr_scene_params* sps, const 
     CU(cudaMemcpyAsync(hmu.data(), P0.muscal, hmu.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     CU(cudaMemcpyAsync(hsm.data(), P0.sed_major, hsm.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     CU(cudaMemcpyAsync(hnm.data(), P0.node_major, hnm.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+    for (int i = 0; i < ns; ++i)
+        if (pbs[i].merid_coef) {
+            CU(cudaMemcpyAsync(&pbs[i].solver_iterations, pbs[i].merid_stats, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CU(cudaMemcpyAsync(&pbs[i].solver_max_residual, pbs[i].merid_residual + 2 * (size_t)pbs[i].n,
+                               sizeof(double), cudaMemcpyDeviceToHost, st));
+        }
     CU(cudaEventRecord(ctx->ev1, st));
     CU(cudaStreamSynchronize(st));
     CU(cudaEventElapsedTime(&ctx->last_kernel_ms, ctx->ev0, ctx->ev1));
     if (herr) return fail(ctx, CLR_ERR_PRECOMPUTE, "sweep particle precompute failed with error code %d", herr);
+    for (int i = 0; i < ns; ++i)
+        if (pbs[i].merid_coef && pbs[i].solver_max_residual > sss[i].solver_tolerance)
+            return fail(ctx, CLR_ERR_PRECOMPUTE,
+                        "scenario %d: meridional transport solver did not converge: max residual=%.6g after %d iterations",
+                        i, pbs[i].solver_max_residual, pbs[i].solver_iterations);
     for (int i = 0; i < ns; ++i) {
         std::copy(hmu.begin() + 8 * i, hmu.begin() + 8 * i + 8, pbs[i].muscal_host);
         std::copy(hsm.begin() + 4 * i, hsm.begin() + 4 * i + 4, pbs[i].sed_major_host);

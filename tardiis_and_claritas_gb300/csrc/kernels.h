@@ -106,6 +106,15 @@ struct ParticleBuffers {
     double *sedA = nullptr, *sedB = nullptr, *sed_norm = nullptr, *sed_max = nullptr, *sed_radial_log = nullptr,
            *sed_wr = nullptr, *sed_major = nullptr, *sed_grid = nullptr, *grid_max = nullptr;
     double* sed_terms = nullptr;  // [n][n_quad] quadrature terms of the sediment normalisation
+    double* sed_ws = nullptr;     // [n] settling velocity
+    // sediment model 3 without a supplied grid: the meridional solver's coefficient planes [n][5][nr*nz],
+    // residuals [2][n] + the final largest residual, grid-barrier words and iteration count (null otherwise)
+    double* merid_coef = nullptr;
+    double* merid_residual = nullptr;
+    unsigned* merid_bar = nullptr;
+    int* merid_stats = nullptr;
+    int solver_iterations = 0;
+    double solver_max_residual = 0.0;
     int* err = nullptr;
     // node tables of the (r, z) field for the counter-based stream (sediment model 3, non-negative grid)
     int node_tables = 0;
@@ -154,6 +163,11 @@ cudaError_t noalloc_scratch(int device, NoallocScratch* out);
 // `ab_scratch` may supply the Mie a_n/b_n scratch (n*CLR_MIE_MAX_ORDER*4 doubles); when null, pb.ab is used.
 cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,
                                         const clr_sediment_spec& ss, double* ab_scratch, cudaStream_t stream);
+// The meridional advection-diffusion field of sediment model 3 (one cooperative launch, a CTA per bin)
+// into pb.sed_grid and pb.grid_max; pb.merid_* must be allocated (meridional_coef_doubles coefficients).
+size_t meridional_coef_doubles(int n, int nr, int nz);
+cudaError_t enqueue_meridional_solve(ParticleBuffers& pb, const clr_scene_params& sp, const clr_sediment_spec& ss,
+                                     cudaStream_t stream);
 // The part of it after the Mie tables (rates, sediment, node tables); pb's Mie outputs must be ready.
 cudaError_t enqueue_scene_rates(ParticleBuffers& pb, const clr_scene_params& sp, const clr_particle_spec& ps,
                                 const clr_sediment_spec& ss, cudaStream_t stream);

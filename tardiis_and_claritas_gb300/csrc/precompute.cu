@@ -485,12 +485,13 @@ __global__ void sediment_slip_kernel(SedArgs a, const double* __restrict__ diame
 __global__ void __launch_bounds__(32) sediment_bin_kernel(SedArgs a, const double* __restrict__ diameter,
                                                           const double* __restrict__ wr, double* sedA, double* sedB,
                                                           double* sed_norm, double* sed_max, double* radial_log,
-                                                          double* __restrict__ terms, int* error_flag) {
+                                                          double* __restrict__ terms, double* ws_out,
+                                                          int* error_flag) {
     const int i = blockIdx.x;
     const int lane = threadIdx.x;
     if (i >= a.n) return;
     if (a.TM == 0) {
-        if (lane == 0) { sedA[i] = 0.0; sedB[i] = 0.0; sed_norm[i] = 1.0; sed_max[i] = 1.0; }
+        if (lane == 0) { sedA[i] = 0.0; sedB[i] = 0.0; sed_norm[i] = 1.0; sed_max[i] = 1.0; ws_out[i] = 0.0; }
         return;
     }
     double R2, a2, Hinf, hbar, omega2, fR;
@@ -508,6 +509,7 @@ __global__ void __launch_bounds__(32) sediment_bin_kernel(SedArgs a, const doubl
     const double Ac = tau * omega2 * ((FSM == 2) ? a2 : 1.0) / (2.0 * a.Dt);
     if (lane == 0) {
         sedB[i] = Bc;
+        ws_out[i] = ws;
         if (TM == 1) {
             sedA[i] = Ac;
             for (int j = 0; j < NRAD; ++j) {
@@ -690,6 +692,331 @@ __global__ void sediment_node_kernel(const double* __restrict__ grid, const doub
     }
 }
 
+// ---------------- meridional advection-diffusion field (sediment model 3 without a supplied grid) ----------------
+// The reference solves, per size bin, the stationary axisymmetric advection-diffusion of the sediment in
+// the secondary (meridional) circulation of the stirred cell on a cell-centred (r, z) grid: upwind finite
+// volumes with no-flux walls, red-black SOR, per-bin mass renormalisation every 20 iterations and at every
+// convergence check, stopping at the first check (after at least min(1000, max) iterations) where the
+// largest relative residual over all bins is within tolerance (CLARITAS/CLARITAS.py:4040-4215, driven by
+// :6451-6725, one launch per half-sweep). Here one cooperative launch does all of it: a CTA per bin keeps
+// its bin's plane in shared memory; the bins meet only at the checks (a bounded grid barrier) to agree on
+// the largest residual. Every cell value, sum order and stopping iteration is the reference's.
+
+// free-surface height and slope at radius r (:4046-4057)
+__device__ void merid_surface(int FSM, double r, double ZMEAN, double R, double DH, double CORE, double* zs, double* hp) {
+    double rr = fmin(fmax(r, 0.0), R), rr2 = rr * rr, R2 = R * R;
+    *zs = ZMEAN; *hp = 0.0;
+    if (!(DH > 0.0) || FSM == 0) return;
+    if (FSM == 1) { *zs = ZMEAN + DH * (rr2 / R2 - 0.5); *hp = 2.0 * DH * rr / R2; return; }
+    double a2 = CORE * CORE, Hinf = DH * (a2 + R2) / R2;
+    double hbar = Hinf * (1.0 - (a2 / R2) * log1p(R2 / a2));
+    *zs = ZMEAN - hbar + Hinf * rr2 / (a2 + rr2);
+    *hp = 2.0 * Hinf * a2 * rr / ((a2 + rr2) * (a2 + rr2));
+}
+// secondary-circulation velocity from the streamfunction psi = -2U r^2 (1-r^2/R^2)^2 eta(1-eta) (:4059-4073)
+__device__ void merid_velocity(double r, double z, double ZMIN, double ZMEAN, double R, int FSM, double DH, double CORE,
+                               double UPEAK, double* ur, double* uz) {
+    *ur = 0.0; *uz = 0.0;
+    if (!(UPEAK > 0.0) || !(R > 0.0) || !(DH > 0.0) || (FSM == 2 && !(CORE > 0.0))) return;
+    double rr = fmin(fmax(r, 0.0), R), R2 = R * R, rr2 = rr * rr, zs = ZMEAN, hp = 0.0;
+    merid_surface(FSM, rr, ZMEAN, R, DH, CORE, &zs, &hp);
+    double H = zs - ZMIN;
+    if (!(H > 0.0)) return;
+    double eta = (z - ZMIN) / H;
+    if (eta < 0.0) eta = 0.0;
+    if (eta > 1.0) eta = 1.0;
+    double sq = rr2 / R2, f = eta * (1.0 - eta), fp = 1.0 - 2.0 * eta;
+    double Apsi = 2.0 * UPEAK, om = 1.0 - sq;
+    *ur = Apsi * rr * om * om * fp / H;
+    *uz = -Apsi * (2.0 * om * (1.0 - 3.0 * sq) * f - rr * om * om * fp * eta * hp / H);
+}
+// radial slip interpolated from the per-bin table (:4075-4082)
+__device__ double merid_slip(int p, double r, double R, const double* WR, int NRAD) {
+    if (NRAD < 2 || !(R > 0.0)) return 0.0;
+    double q = fmin(fmax(r / R, 0.0), 1.0) * (double)(NRAD - 1);
+    int j = (int)floor(q);
+    double t = q - (double)j;
+    if (j >= NRAD - 1) { j = NRAD - 2; t = 1.0; }
+    long long b = (long long)p * (long long)NRAD;
+    return (1.0 - t) * WR[b + j] + t * WR[b + j + 1];
+}
+// a point inside the liquid (:4084-4089)
+__device__ int merid_fluid(double r, double z, double ZMIN, double ZMEAN, double R, int FSM, double DH, double CORE) {
+    if (z < ZMIN) return 0;
+    double zs = ZMEAN, hp = 0.0;
+    merid_surface(FSM, r, ZMEAN, R, DH, CORE, &zs, &hp);
+    return z < zs;
+}
+// the finite-Re drift-diffusion field at a cell centre (sediment_local_scale with model 2, :1560-1593),
+// which starts the iteration (:4100-4112)
+__device__ double merid_initial(int FSM, int p, const double* SA, const double* SB, const double* SN, const double* RL,
+                                int NRAD, float x, float z, float R, float ZMIN) {
+    (void)FSM; (void)SA;
+    double rr2 = (double)x * (double)x + 0.0 * 0.0;
+    double R2 = (double)R * (double)R;
+    if (rr2 > R2) rr2 = R2;
+    double rr = sqrt(fmax(rr2, 0.0));
+    double u = (R > 0.0) ? rr / (double)R * (double)(NRAD - 1) : 0.0;
+    int j = (int)floor(u);
+    if (j < 0) j = 0;
+    if (j > NRAD - 2) j = NRAD - 2;
+    double t = u - (double)j;
+    long long base = (long long)p * (long long)NRAD;
+    double radial_log = (1.0 - t) * RL[base + j] + t * RL[base + j + 1];
+    if (radial_log > 0.0) radial_log = 0.0;
+    double h = fmax((double)z - (double)ZMIN, 0.0);
+    double logrel = radial_log - SB[p] * h;
+    double ns = SN[p];
+    if (!(ns > 0.0)) return 0.0;
+    return exp(logrel) / ns;
+}
+
+__device__ __forceinline__ unsigned long long merid_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Barrier over the co-resident CTAs of a cooperative launch; gives up (error 91) after two seconds.
+__device__ bool merid_grid_barrier(unsigned* count, unsigned* gen, unsigned nblocks, int* err) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok_s = 1;
+        volatile unsigned* vgen = gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        if (atomicAdd(count, 1u) + 1u == nblocks) {
+            *count = 0u;
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            const unsigned long long t0 = merid_ns();
+            while (*vgen == g) {
+                if (merid_ns() - t0 > 2000000000ull) { ok_s = 0; atomicCAS(err, 0, 91); break; }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+struct MeridArgs {
+    int n, NR, NZ, NRAD, FSM, max_it, check_every;
+    double R, ZMIN, ZMEAN, ZGRIDMAX, DH, CORE, UPEAK, Dt, OMEGA, TOL;
+    const double *sedA, *sedB, *sed_norm, *radial_log, *wr, *ws;
+    double* grid;       // [n][NR][NZ]
+    double* coef;       // [n][5][NR*NZ]: AP, AE, AW, AN, AS
+    double* grid_max;   // [n] largest value over the liquid cells
+    double* residual;   // [2][n] residual of every bin at the last two checks
+    unsigned* bar;      // [2] barrier count and generation (zero before the launch)
+    int* err;           // first error code
+    int* iterations;    // [1] iterations done (the reference's solver_iterations)
+    double* max_residual;  // [1]
+};
+
+constexpr int kMeridThreads = 512;
+
+__global__ void __launch_bounds__(kMeridThreads) meridional_solve_kernel(MeridArgs a) {
+    extern __shared__ __align__(16) unsigned char msm[];
+    const int NR = a.NR, NZ = a.NZ, plane = NR * NZ, p = blockIdx.x, tid = threadIdx.x;
+    double* G = reinterpret_cast<double*>(msm);
+    unsigned char* act = msm + (size_t)plane * 8;
+    __shared__ double red[kMeridThreads / 32];
+    __shared__ double scale_s;
+    __shared__ int bad_s;
+    const double dr = a.R / (double)NR, dz = (a.ZGRIDMAX - a.ZMIN) / (double)NZ;
+    double* AP = a.coef + (size_t)p * 5 * plane;
+    double* AE = AP + plane;
+    double* AW = AE + plane;
+    double* AN = AW + plane;
+    double* AS = AN + plane;
+    // liquid cells (:4091-4098) and the starting field (:4100-4112)
+    for (int c = tid; c < plane; c += kMeridThreads) {
+        const int i = c / NZ, k = c - i * NZ;
+        const double r = ((double)i + 0.5) * dr, z = a.ZMIN + ((double)k + 0.5) * dz;
+        act[c] = (unsigned char)(merid_fluid(r, z, a.ZMIN, a.ZMEAN, a.R, a.FSM, a.DH, a.CORE) ? 1 : 0);
+    }
+    __syncthreads();
+    for (int c = tid; c < plane; c += kMeridThreads) {
+        const int i = c / NZ, k = c - i * NZ;
+        if (!act[c]) { G[c] = 0.0; continue; }
+        const float x = (float)(((double)i + 0.5) * dr), z = (float)(a.ZMIN + ((double)k + 0.5) * dz);
+        G[c] = merid_initial(a.FSM, p, a.sedA, a.sedB, a.sed_norm, a.radial_log, a.NRAD, x, z, (float)a.R,
+                             (float)a.ZMIN);
+    }
+    // upwind finite-volume coefficients (:4114-4159)
+    for (int c = tid; c < plane; c += kMeridThreads) {
+        const int i = c / NZ, k = c - i * NZ;
+        AP[c] = AE[c] = AW[c] = AN[c] = AS[c] = 0.0;
+        if (!act[c]) continue;
+        double rc = ((double)i + 0.5) * dr, zc = a.ZMIN + ((double)k + 0.5) * dz;
+        double rw = (double)i * dr, re = (double)(i + 1) * dr;
+        double Az = 0.5 * (re * re - rw * rw), ap = 0.0, ur = 0.0, uz = 0.0, V = 0.0, F = 0.0, diff = 0.0;
+        if (i + 1 < NR && act[(i + 1) * NZ + k] && merid_fluid(re, zc, a.ZMIN, a.ZMEAN, a.R, a.FSM, a.DH, a.CORE)) {
+            merid_velocity(re, zc, a.ZMIN, a.ZMEAN, a.R, a.FSM, a.DH, a.CORE, a.UPEAK, &ur, &uz);
+            V = ur + merid_slip(p, re, a.R, a.wr, a.NRAD); F = V * re * dz; diff = a.Dt * re * dz / dr;
+            AE[c] = diff + fmax(-F, 0.0); ap += diff + fmax(F, 0.0);
+        }
+        if (i > 0 && act[(i - 1) * NZ + k] && merid_fluid(rw, zc, a.ZMIN, a.ZMEAN, a.R, a.FSM, a.DH, a.CORE)) {
+            merid_velocity(rw, zc, a.ZMIN, a.ZMEAN, a.R, a.FSM, a.DH, a.CORE, a.UPEAK, &ur, &uz);
+            V = ur + merid_slip(p, rw, a.R, a.wr, a.NRAD); F = -V * rw * dz; diff = a.Dt * rw * dz / dr;
+            AW[c] = diff + fmax(-F, 0.0); ap += diff + fmax(F, 0.0);
+        }
+        double zf = zc + 0.5 * dz;
+        if (k + 1 < NZ && act[i * NZ + k + 1] && merid_fluid(rc, zf, a.ZMIN, a.ZMEAN, a.R, a.FSM, a.DH, a.CORE)) {
+            merid_velocity(rc, zf, a.ZMIN, a.ZMEAN, a.R, a.FSM, a.DH, a.CORE, a.UPEAK, &ur, &uz);
+            V = uz - a.ws[p]; F = V * Az; diff = a.Dt * Az / dz;
+            AN[c] = diff + fmax(-F, 0.0); ap += diff + fmax(F, 0.0);
+        }
+        zf = zc - 0.5 * dz;
+        if (k > 0 && act[i * NZ + k - 1] && merid_fluid(rc, zf, a.ZMIN, a.ZMEAN, a.R, a.FSM, a.DH, a.CORE)) {
+            merid_velocity(rc, zf, a.ZMIN, a.ZMEAN, a.R, a.FSM, a.DH, a.CORE, a.UPEAK, &ur, &uz);
+            V = uz - a.ws[p]; F = -V * Az; diff = a.Dt * Az / dz;
+            AS[c] = diff + fmax(-F, 0.0); ap += diff + fmax(F, 0.0);
+        }
+        AP[c] = ap;
+    }
+    __syncthreads();
+    // per-bin mass renormalisation (:4176-4187): the mass sum runs serially in the reference's order
+    auto normalize = [&]() {
+        if (tid == 0) {
+            double mass = 0.0;
+            for (int i = 0; i < NR; ++i) {
+                double rw = (double)i * dr, re = (double)(i + 1) * dr, vol = 0.5 * (re * re - rw * rw) * dz;
+                for (int k = 0; k < NZ; ++k) {
+                    const int c = i * NZ + k;
+                    if (act[c]) mass += G[c] * vol;
+                }
+            }
+            double target = 0.5 * a.R * a.R * (a.ZMEAN - a.ZMIN);
+            bad_s = (!(mass > 0.0) || !(target > 0.0) || !isfinite(mass)) ? 1 : 0;
+            if (bad_s) atomicCAS(a.err, 0, 41);
+            scale_s = bad_s ? 1.0 : target / mass;
+        }
+        __syncthreads();
+        if (!bad_s) {
+            const double sc = scale_s;
+            for (int c = tid; c < plane; c += kMeridThreads)
+                if (act[c]) G[c] *= sc;
+        }
+        __syncthreads();
+    };
+    // one colour of the red-black SOR sweep (:4161-4174)
+    auto relax = [&](int parity) {
+        for (int c = tid; c < plane; c += kMeridThreads) {
+            const int i = c / NZ, k = c - i * NZ;
+            if (!act[c] || ((i + k) & 1) != parity || !(AP[c] > 0.0)) continue;
+            double num = 0.0;
+            if (i + 1 < NR) num += AE[c] * G[(i + 1) * NZ + k];
+            if (i > 0) num += AW[c] * G[(i - 1) * NZ + k];
+            if (k + 1 < NZ) num += AN[c] * G[i * NZ + k + 1];
+            if (k > 0) num += AS[c] * G[i * NZ + k - 1];
+            double target = num / AP[c], old = G[c], nv = (1.0 - a.OMEGA) * old + a.OMEGA * target;
+            if (!isfinite(nv) || nv < 1e-14) nv = 1e-14;
+            G[c] = nv;
+        }
+        __syncthreads();
+    };
+    // largest relative residual of the bin (:4189-4197)
+    auto residual = [&]() -> double {
+        double mr = 0.0;
+        for (int c = tid; c < plane; c += kMeridThreads) {
+            const int i = c / NZ, k = c - i * NZ;
+            if (!act[c] || !(AP[c] > 0.0)) continue;
+            double num = 0.0;
+            if (i + 1 < NR) num += AE[c] * G[(i + 1) * NZ + k];
+            if (i > 0) num += AW[c] * G[(i - 1) * NZ + k];
+            if (k + 1 < NZ) num += AN[c] * G[i * NZ + k + 1];
+            if (k > 0) num += AS[c] * G[i * NZ + k - 1];
+            double den = fmax(fabs(AP[c] * G[c]), 1e-30), q = fabs(AP[c] * G[c] - num) / den;
+            if (q > mr) mr = q;
+        }
+        for (int o = 16; o > 0; o >>= 1) mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+        if ((tid & 31) == 0) red[tid >> 5] = mr;
+        __syncthreads();
+        double m = 0.0;
+        for (int w = 0; w < kMeridThreads / 32; ++w) m = fmax(m, red[w]);
+        __syncthreads();
+        return m;
+    };
+    normalize();
+    const int min_it = a.max_it < 1000 ? a.max_it : 1000;
+    int done = 0, last_checked = 0, checks = 0;
+    double worst = 0.0;
+    bool stop = false;
+    // the initial normalisation is checked before the first sweep (:6561-6575)
+    if (!merid_grid_barrier(a.bar, a.bar + 1, gridDim.x, a.err)) stop = true;
+    if (!stop && *(volatile int*)a.err) stop = true;
+    for (int it = 1; it <= a.max_it && !stop; ++it) {
+        relax(0);
+        relax(1);
+        if (it % 20 == 0) normalize();
+        if (it % a.check_every == 0 || it == a.max_it) {
+            normalize();
+            const double r = residual();
+            double* slot = a.residual + (size_t)(checks & 1) * a.n;
+            if (tid == 0) slot[p] = r;
+            if (!merid_grid_barrier(a.bar, a.bar + 1, gridDim.x, a.err)) break;
+            worst = 0.0;
+            for (int q = 0; q < a.n; ++q) worst = fmax(worst, ((volatile double*)slot)[q]);
+            last_checked = it;
+            ++checks;
+            if (*(volatile int*)a.err) break;
+            if (it >= min_it && worst <= a.TOL) { done = it; break; }
+        }
+    }
+    if (done == 0) done = last_checked ? last_checked : a.max_it;
+    if (p == 0 && tid == 0) { *a.iterations = done; *a.max_residual = worst; }
+    // extend each column above the free surface with its highest liquid value (:4199-4205)
+    for (int i = tid; i < NR; i += kMeridThreads) {
+        int top = -1;
+        for (int k = NZ - 1; k >= 0; --k)
+            if (act[i * NZ + k]) { top = k; break; }
+        if (top < 0) { for (int k = 0; k < NZ; ++k) G[i * NZ + k] = 1.0; continue; }
+        const double q = G[i * NZ + top];
+        for (int k = top + 1; k < NZ; ++k) G[i * NZ + k] = q;
+    }
+    __syncthreads();
+    double mx = 0.0;
+    for (int c = tid; c < plane; c += kMeridThreads) {
+        a.grid[(size_t)p * plane + c] = G[c];
+        if (act[c] && G[c] > mx) mx = G[c];
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((tid & 31) == 0) red[tid >> 5] = mx;
+    __syncthreads();
+    if (tid == 0) {
+        double m = 0.0;
+        for (int w = 0; w < kMeridThreads / 32; ++w) m = fmax(m, red[w]);
+        a.grid_max[p] = m;  // the majorant kernel takes 1 where this is not positive (:4207-4209)
+    }
+}
+
+size_t meridional_coef_doubles(int n, int nr, int nz) { return (size_t)n * 5 * nr * nz; }
+
+cudaError_t enqueue_meridional_solve(ParticleBuffers& pb, const clr_scene_params& sp, const clr_sediment_spec& ss,
+                                     cudaStream_t st) {
+    MeridArgs a;
+    a.n = pb.n; a.NR = pb.grid_nr; a.NZ = pb.grid_nz; a.NRAD = pb.n_radial; a.FSM = sp.free_surface_model;
+    a.max_it = ss.solver_max_iterations; a.check_every = ss.solver_check_interval;
+    a.R = ss.rin; a.ZMIN = ss.zmin; a.ZMEAN = ss.zmean; a.ZGRIDMAX = ss.grid_zmax; a.DH = ss.vortex_delta_h;
+    a.CORE = ss.vortex_core_radius; a.UPEAK = ss.meridional_peak_speed; a.Dt = ss.eddy_diffusivity;
+    a.OMEGA = ss.solver_sor; a.TOL = ss.solver_tolerance;
+    a.sedA = pb.sedA; a.sedB = pb.sedB; a.sed_norm = pb.sed_norm; a.radial_log = pb.sed_radial_log; a.wr = pb.sed_wr;
+    a.ws = pb.sed_ws; a.grid = pb.sed_grid; a.coef = pb.merid_coef; a.grid_max = pb.grid_max;
+    a.residual = pb.merid_residual; a.bar = pb.merid_bar; a.err = pb.err; a.iterations = pb.merid_stats;
+    a.max_residual = reinterpret_cast<double*>(pb.merid_residual + 2 * (size_t)pb.n);
+    const size_t smem = (size_t)a.NR * a.NZ * 9;
+    cudaError_t e = cudaFuncSetAttribute(meridional_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(pb.merid_bar, 0, 2 * sizeof(unsigned), st)) != cudaSuccess) return e;
+    void* args[] = {&a};
+    return cudaLaunchCooperativeKernel((const void*)meridional_solve_kernel, dim3(a.n), dim3(kMeridThreads), args,
+                                       smem, st);
+}
+
 // Upper bound of the orders the Mie kernel needs for n bins: the largest nmx = max(nstop, |m x|) + 128 of
 // the bins (:3506-3512), recomputed on the host from the same inputs with a few orders of slack for
 // libm differences in cbrt and hypot, and never above CLR_MIE_MAX_ORDER (bins past that limit fail in
@@ -764,8 +1091,11 @@ static SedArgs sed_args_of(const ParticleBuffers& pb, const clr_scene_params& sp
     SedArgs a;
     a.n = pb.n; a.TM = sp.sediment_model; a.FSM = sp.free_surface_model; a.NQ = ss.n_quad; a.NRAD = ss.n_radial;
     a.rho_p = ss.particle_density; a.rho_w = ss.water_density; a.mu = ss.water_viscosity; a.grav = ss.gravity;
-    a.Dt = ss.eddy_diffusivity; a.R = (double)sp.rin; a.ZMIN = (double)sp.zmin; a.ZMEAN = (double)sp.zmean;
-    a.DH = (double)sp.vortex_delta_h; a.CORE = (double)sp.vortex_core_radius;
+    // FP64 geometry as the reference passes it to its sediment kernels (the host fills it from the scene's
+    // FP32 values when the caller leaves it zero)
+    a.Dt = ss.eddy_diffusivity; a.R = ss.rin; a.ZMIN = ss.zmin; a.ZMEAN = ss.zmean;
+    a.DH = ss.vortex_delta_h; a.CORE = ss.vortex_core_radius;
+    (void)sp;
     return a;
 }
 
@@ -783,8 +1113,8 @@ static void enqueue_sediment_bins(ParticleBuffers& pb, const SedArgs& a, cudaStr
         sediment_slip_kernel<<<g, 128, 0, st>>>(a, pb.d, pb.sed_wr);
     }
     sediment_bin_kernel<<<a.n, 32, 0, st>>>(a, pb.d, pb.sed_wr, pb.sedA, pb.sedB, pb.sed_norm, pb.sed_max,
-                                            pb.sed_radial_log, pb.sed_terms, pb.err);
-    if (a.TM == 3)
+                                            pb.sed_radial_log, pb.sed_terms, pb.sed_ws, pb.err);
+    if (a.TM == 3 && !pb.merid_coef)  // a supplied grid: its largest value per bin (the solver gives its own)
         sediment_grid_max_kernel<<<a.n, 256, 0, st>>>(pb.sed_grid, (long long)pb.grid_nr * pb.grid_nz, pb.grid_max);
 }
 
@@ -806,6 +1136,10 @@ cudaError_t enqueue_scene_rates(ParticleBuffers& pb, const clr_scene_params& sp,
     transport_kernel<<<1, 1, 0, st>>>(transport_job_of(pb, sp, ps));
     const SedArgs a = sed_args_of(pb, sp, ss);
     enqueue_sediment_bins(pb, a, st);
+    if (pb.merid_coef) {
+        cudaError_t e = enqueue_meridional_solve(pb, sp, ss, st);
+        if (e != cudaSuccess) return e;
+    }
     sediment_majorant_kernel<<<1, 1, 0, st>>>(majorant_job_of(pb, a));
     cudaError_t e = enqueue_node_tables(pb, st);
     if (e != cudaSuccess) return e;
@@ -838,6 +1172,8 @@ cudaError_t enqueue_scene_rates_batch(ParticleBuffers* const* pbs, const clr_sce
     if (e != cudaSuccess) return e;
     transport_batch_kernel<<<(n + 63) / 64, 64, 0, st>>>(d_tj, n);
     for (int i = 0; i < n; ++i) enqueue_sediment_bins(*pbs[i], sa[i], st);
+    for (int i = 0; i < n; ++i)
+        if (pbs[i]->merid_coef && (e = enqueue_meridional_solve(*pbs[i], sps[i], sss[i], st)) != cudaSuccess) return e;
     sediment_majorant_batch_kernel<<<(n + 63) / 64, 64, 0, st>>>(d_mj, n);
     for (int i = 0; i < n; ++i)
         if ((e = enqueue_node_tables(*pbs[i], st)) != cudaSuccess) return e;

@@ -12,8 +12,8 @@ adaptive stopping rule (:8818-8880) exactly as the reference's batch loop does.
 Two random streams are offered: ``rng="philox"`` (default; the fast production path) and
 ``rng="reference"`` (the reference's per-ray xorshift streams and seeds: per-ray outcomes equal the
 reference kernels'). Features outside the photon-transport path raise ``NotImplementedError``:
-light-history diagnostics and heat maps (``light_transport_config``, ``heatmap_size``), population
-aggregation/fragmentation and the meridional solver. Named materials (the reference's loess/kaolin PSD
+light-history diagnostics and heat maps (``light_transport_config``, ``heatmap_size``) and population
+aggregation/fragmentation. Named materials (the reference's loess/kaolin PSD
 tables) are not bundled: pass a ``scene.Particles`` as ``material`` or register one under a name.
 """
 from __future__ import annotations
@@ -319,12 +319,17 @@ class ClaritasForwardModel:
                None if weights is None else tuple(np.asarray(weights, dtype=float)), weight_mode)
         ctx = self._context()
         if key != self._prepared_key:
-            if self.config.sediment_transport_model == "schiller_naumann_meridional_advection_diffusion":
-                raise NotImplementedError("the meridional advection-diffusion field solver is outside this "
-                                          "library; pass a precomputed (r, z) field through scene.sediment_spec")
-            ctx.build_particles(parts.spec(self.config), self.config.sediment_spec())
+            # sediment model 3 without a supplied field: the library solves the meridional field on the device
+            ss = self.config.sediment_spec()
+            ctx.build_particles(parts.spec(self.config), ss)
             self._prepared_key = key
             self._physics = ctx.physics()
+            self._meridional = {"peak_speed": float(ss.meridional_peak_speed), "nr": 2, "nz": 2, "iterations": 0,
+                                "max_residual": 0.0}
+            if self.config.sediment_transport_model == "schiller_naumann_meridional_advection_diffusion":
+                f = ctx.sediment_field()
+                self._meridional.update(nr=f["nr"], nz=f["nz"], iterations=f["iterations"],
+                                        max_residual=f["max_residual"])
         return parts
 
     def _prepare_gpu_particle_physics(self, material, concentration_g_per_L, weights=None,
@@ -570,8 +575,9 @@ class ClaritasForwardModel:
             sediment_majorant_geom_per_m=float(sed[0]), sediment_majorant_wave_per_m=float(sed[1]),
             sediment_majorant_total_per_m=float(sed[2]), sediment_max_bin_density_scale=float("nan"),
             meridional_circulation_ratio=cfg.meridional_circulation_ratio,
-            meridional_peak_speed_m_s=float("nan"), meridional_grid_nr=0, meridional_grid_nz=0,
-            meridional_solver_iterations=0, meridional_solver_max_residual=float("nan"),
+            meridional_peak_speed_m_s=self._meridional["peak_speed"], meridional_grid_nr=self._meridional["nr"],
+            meridional_grid_nz=self._meridional["nz"], meridional_solver_iterations=self._meridional["iterations"],
+            meridional_solver_max_residual=self._meridional["max_residual"],
             mean_bottom_inner_reflections=per_entered(es["bir"]), mean_bottom_outer_reflections=per_entered(es["bor"]),
             bottom_tir_fraction=per_entered(rf["bottom_tir"]),
             top_exit_fraction=float(st[ST_TOP]) / nrays, bottom_exit_fraction=float(st[ST_BOTTOM]) / nrays,

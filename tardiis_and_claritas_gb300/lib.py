@@ -70,6 +70,8 @@ def load(build_if_missing: bool = False):
             "clr_mlp_last_ms": ([C.c_void_p, P(C.c_float)], C.c_int),
             "clr_bf16_gemm_n256": ([C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p,
                                     C.c_int64, C.c_void_p], C.c_int),
+            "clr_read_sediment_field": ([C.c_void_p, C.c_void_p, P(C.c_int32), P(C.c_int32), P(C.c_int32),
+                                         P(C.c_double)], C.c_int),
         }
         for name, (argt, rest) in sig.items():
             f = getattr(lib, name)
@@ -85,7 +87,7 @@ def exported_symbols() -> list[str]:
             "clr_last_kernel_ms", "clr_last_launches", "clr_calibrate", "clr_mie_phase_noalloc", "clr_sweep_build",
             "clr_sweep_trace", "clr_sweep_read_particle_physics", "clr_mlp_create", "clr_mlp_destroy",
             "clr_mlp_last_error", "clr_mlp_set_params", "clr_mlp_get_params", "clr_mlp_forward", "clr_mlp_gradients",
-            "clr_mlp_train", "clr_mlp_last_ms", "clr_bf16_gemm_n256"]
+            "clr_mlp_train", "clr_mlp_last_ms", "clr_bf16_gemm_n256", "clr_read_sediment_field"]
 
 
 class Context:
@@ -118,6 +120,18 @@ class Context:
         self._check(self.lib.clr_read_particle_physics(self.h, C.byref(pp)), "clr_read_particle_physics")
         arrays["phase_cdf"] = arrays["phase_cdf"].reshape(self.n_bins, self.n_theta)
         return arrays
+
+    def sediment_field(self) -> dict:
+        """The (r, z) sediment field of the current model-3 scene and its solver statistics."""
+        import numpy as np
+        nr, nz, it, res = C.c_int32(), C.c_int32(), C.c_int32(), C.c_double()
+        self._check(self.lib.clr_read_sediment_field(self.h, None, C.byref(nr), C.byref(nz), C.byref(it),
+                                                     C.byref(res)), "clr_read_sediment_field")
+        g = np.zeros((self.n_bins, nr.value, nz.value), dtype=np.float64)
+        self._check(self.lib.clr_read_sediment_field(self.h, g.ctypes.data_as(C.c_void_p), None, None, None, None),
+                    "clr_read_sediment_field")
+        return {"grid": g, "nr": int(nr.value), "nz": int(nz.value), "iterations": int(it.value),
+                "max_residual": float(res.value)}
 
     def trace(self, run: abi.RunParams, records: bool = False):
         import numpy as np

@@ -285,6 +285,21 @@ class ModelConfig:
                                      self.vortex_wall_center_height_difference_m, self.vortex_core_radius_m,
                                      self.gravity_m_s2)
         sp.grid_zmax = float(vg["wall_z"]) if grid_zmax is None else float(grid_zmax)
+        # FP64 geometry as the reference passes it to its sediment kernels (CLARITAS/CLARITAS.py:6413-6418)
+        sp.rin, sp.zmin, sp.zmean = float(self.tube_inner_radius_m), self.zmin, self.zmean
+        sp.vortex_delta_h = float(self.vortex_wall_center_height_difference_m)
+        sp.vortex_core_radius = float(self.vortex_core_radius_m)
+        # meridional solver settings (used for sediment model 3 without a supplied grid, :6451-6725); the peak
+        # speed is chi x the vortex's peak azimuthal speed for a stirred surface, else 0 (:5901-5907)
+        sp.meridional_nr, sp.meridional_nz = int(self.meridional_grid_nr), int(self.meridional_grid_nz)
+        sp.solver_max_iterations = int(self.meridional_solver_max_iterations)
+        sp.solver_check_interval = int(self.meridional_solver_check_interval)
+        sp.solver_tolerance = float(self.meridional_solver_tolerance)
+        sp.solver_sor = float(self.meridional_solver_sor)
+        stirred = (self.free_surface_model in ("localized_scully_vortex", "parabolic_vortex")
+                   and self.vortex_wall_center_height_difference_m > 0.0)
+        sp.meridional_peak_speed = (float(self.meridional_circulation_ratio) * float(vg["vtheta_peak_m_s"])
+                                    if stirred else 0.0)
         keep = []
         if grid is not None:
             g = np.ascontiguousarray(grid, dtype=np.float64)

@@ -38,7 +38,7 @@ def main():
         raise SystemExit("host build of the reference unavailable: run oracle/ref_extract.py first")
     out = {}
     meta = {"n_rays": N_RAYS, "n_compact": N_COMPACT, "machine": platform.machine(), "scenes": {}}
-    for name in PS.SCENES:
+    for name in PS.CPU_SCENES:
         cfg, parts, grid = PS.build(name)
         ref = H.OracleRun("reference", cfg, parts, grid=grid)
         ph = ref.physics()

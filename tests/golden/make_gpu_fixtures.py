@@ -16,6 +16,7 @@ the library against this file bit for bit.
 from __future__ import annotations
 
 import argparse
+import hashlib
 import ctypes as C
 import json
 import os
@@ -69,7 +70,19 @@ def load():
     lib.clrefgpu_last_error.argtypes = [C.c_void_p]
     lib.clrefgpu_last_error.restype = C.c_char_p
     lib.clrefgpu_free.argtypes = [C.c_void_p]
+    lib.clrefgpu_read_sediment_field.argtypes = [C.c_void_p, C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int),
+                                                 P(C.c_double)]
     return lib
+
+
+def field_of(lib, h, n_bins: int) -> dict:
+    """The reference's (r, z) sediment field of a model-3 scene: digest, shape, solver statistics, bin 0."""
+    nr, nz, it, res = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+    lib.clrefgpu_read_sediment_field(h, None, C.byref(nr), C.byref(nz), C.byref(it), C.byref(res))
+    g = np.zeros((n_bins, nr.value, nz.value), dtype=np.float64)
+    lib.clrefgpu_read_sediment_field(h, g.ctypes.data_as(C.c_void_p), None, None, None, None)
+    return {"sha256": hashlib.sha256(g.tobytes()).hexdigest(), "nr": nr.value, "nz": nz.value,
+            "iterations": it.value, "max_residual": res.value, "bin0": g[0]}
 
 
 def run_scene(lib, name: str, n_rays: int = N_RAYS):
@@ -82,6 +95,7 @@ def run_scene(lib, name: str, n_rays: int = N_RAYS):
     nt = lib.clrefgpu_n_theta(h)
     pp, arrays = abi.alloc_physics(parts.diameter_m.size, nt)
     lib.clrefgpu_read_physics(h, C.byref(pp))
+    field = field_of(lib, h, parts.diameter_m.size) if sp.sediment_model == 3 else None
     run = S.run_params(n_rays, seed=PS.seed_of(name))
     T = abi.Tallies()
     rec = np.zeros(n_rays, dtype=abi.record_dtype())
@@ -89,7 +103,7 @@ def run_scene(lib, name: str, n_rays: int = N_RAYS):
     if rc != 0:
         raise RuntimeError(f"{name}: reference trace failed {rc}: {lib.clrefgpu_last_error(h).decode()}")
     lib.clrefgpu_free(h)
-    return arrays, T.as_dict(), rec
+    return arrays, T.as_dict(), rec, field
 
 
 def main():
@@ -102,10 +116,13 @@ def main():
     meta = {"n_rays": a.rays, "n_compact": N_COMPACT, "scenes": {}}
     for name in PS.SCENES:
         t = time.time()
-        ph, tal, rec = run_scene(lib, name, a.rays)
+        ph, tal, rec, field = run_scene(lib, name, a.rays)
         meta["scenes"][name] = {"records_sha256": PS.records_digest(rec), "physics_sha256": PS.physics_digests(ph),
                                 "seed": PS.seed_of(name), "event_counts": tal["event_counts"][:PS.EVENT_KEYS].tolist(),
                                 "conditional_stats": [int(v) for v in tal["conditional_stats"]]}
+        if field is not None:
+            out[f"{name}/field_bin0"] = field.pop("bin0")
+            meta["scenes"][name]["field"] = field
         out[f"{name}/compact"] = PS.compact(rec, N_COMPACT).astype(np.int16)
         for k in PS.TALLY_KEYS:
             out[f"{name}/{k}"] = tal[k]

@@ -5,7 +5,7 @@ on, so that together they exercise every branch of the transport path:
 rough/smooth particle surfaces, spheroid morphology, coherent Mie sampling,
 absorbing bins (conditional closure), the three free surfaces, the four
 sediment transport models, reflective bores and ring face, photodiode
-response and the source angular laws.
+response and the source angular laws, and the meridional field solver.
 """
 from __future__ import annotations
 
@@ -43,6 +43,9 @@ SCENES = {
                           dict(concentration_mg_l=2000.0), False),
     "grid_sediment": (dict(PARABOLIC, sediment_transport_model="schiller_naumann_meridional_advection_diffusion"),
                       dict(concentration_mg_l=2000.0), True),
+    # model 3 without a supplied field: the meridional advection-diffusion solver makes it
+    "meridional_solver": (dict(SCULLY, sediment_transport_model="schiller_naumann_meridional_advection_diffusion"),
+                          dict(concentration_mg_l=2000.0), False),
     "reflective_bores": (dict(source_bore_surface_model="smooth_fresnel_nylon",
                               detector_bore_surface_model="smooth_fresnel_nylon",
                               ring_inner_face_surface_model="smooth_fresnel_nylon"),
@@ -52,6 +55,12 @@ SCENES = {
     "vmf_orientation": (dict(wave_spheroid_orientation_model="local_tangential_axial_vmf",
                              wave_spheroid_orientation_kappa=3.0), dict(concentration_mg_l=2000.0), False),
 }
+
+
+# Scenes the CPU oracle does not cover: the meridional field solver is pinned against the reference's own
+# solver kernels on the GPU only.
+GPU_ONLY = {"meridional_solver"}
+CPU_SCENES = [k for k in SCENES if k not in GPU_ONLY]
 
 
 def build(name: str):

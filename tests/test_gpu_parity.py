@@ -82,6 +82,20 @@ def test_bit_exact_against_reference_kernels(ctx, gold, name, engine):
     assert PS.records_digest(rec) == m["records_sha256"], first_mismatch(rec, z[f"{name}/compact"])
 
 
+def test_meridional_field_equals_reference_solver(ctx, gold):
+    """Sediment model 3 without a supplied field: the library's one-launch solver gives the reference
+    solver's field bit for bit, with its iteration count and final residual."""
+    import hashlib
+    z, meta = gold
+    m = meta["scenes"]["meridional_solver"]["field"]
+    prepare(ctx, "meridional_solver")
+    f = ctx.sediment_field()
+    assert (f["nr"], f["nz"]) == (m["nr"], m["nz"])
+    assert f["iterations"] == m["iterations"] and f["max_residual"] == m["max_residual"], (f["iterations"], m)
+    np.testing.assert_array_equal(f["grid"][0], z["meridional_solver/field_bin0"])
+    assert hashlib.sha256(f["grid"].tobytes()).hexdigest() == m["sha256"]
+
+
 @pytest.mark.parametrize("name", list(PS.SCENES))
 def test_agreement_with_as_deployed_reference(ctx, name):
     """The reference as CuPy/NVRTC deploy it fuses multiply-adds where its compiler chooses; the

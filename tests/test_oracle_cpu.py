@@ -55,7 +55,7 @@ def test_philox_known_answers():
         0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
 
 
-@pytest.mark.parametrize("name", list(PS.SCENES))
+@pytest.mark.parametrize("name", PS.CPU_SCENES)
 def test_oracle_matches_reference_fixture(gold, name):
     z, meta = gold
     m = meta["scenes"][name]
