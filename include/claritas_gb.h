@@ -192,6 +192,13 @@ typedef struct clr_ray_record {
     float water_path, acrylic_path;
 } clr_ray_record;
 
+/* indices into clr_tallies.path_sums: per-channel sums over detected rays of their interaction,
+ * geometric, wave, coherent-wave, morphology-wave, particle entry-reflection and internal-reflection
+ * counts (the reference's path_*_sums, CLARITAS/CLARITAS.py:8033-8056) */
+#define CLR_N_PATH_SUMS 7
+enum { CLR_PS_INTERACTIONS = 0, CLR_PS_GEOMETRIC, CLR_PS_WAVE, CLR_PS_COHERENT, CLR_PS_MORPHOLOGY,
+       CLR_PS_ENTRY_REFLECTIONS, CLR_PS_INTERNAL_REFLECTIONS };
+
 /* indices into clr_tallies.event_counts (sums of per-ray counters over the run) */
 enum {
     CLR_EV_INTERACTIONS = 0, CLR_EV_GEOMETRIC, CLR_EV_WAVE, CLR_EV_COHERENT, CLR_EV_MORPHOLOGY,
@@ -261,6 +268,11 @@ typedef struct clr_tallies {
      * (0 source, 1 entry, 2 water) the warp iterations [k], the lanes that ran [4+k] and the
      * SM clock cycles spent [8+k]; [11] cycles spent scoring finished histories */
     int64_t sched_stats[16];
+    /* detected rays partitioned for the particle-path diagnostics (the reference's host partitions of its
+     * per-ray arrays, CLARITAS/CLARITAS.py:8019-8110): index 0 native, 1 mirror detector id */
+    int64_t order_hits[2][6][CLR_N_DETECTORS];            /* by particle-interaction count 0,1,2,3,4,5+ */
+    int64_t geometric_order_hits[2][6][CLR_N_DETECTORS];  /* by geometric-event count 0,1,2,3,4,5+ */
+    int64_t path_sums[CLR_N_PATH_SUMS][2][CLR_N_DETECTORS];  /* sums of per-ray counters (CLR_PS_*) */
 } clr_tallies;
 
 /* Host copies of the particle-physics tables (diagnostics and parity checks).

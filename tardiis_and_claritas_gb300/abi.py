@@ -17,6 +17,7 @@ N_EVENT_COUNTERS = 24
 N_CONDITIONAL_STATS = 10
 N_SUBCODES = 96
 IC_HIST = 1024
+N_PATH_SUMS = 7  # CLR_N_PATH_SUMS
 ES_NAMES = ["ic", "gic", "wic", "wcoh", "wmorph", "pr", "cir", "cor", "top", "bir", "bor", "ctir", "ttir", "btir",
             "per", "pir"]
 RF_NAMES = ["entered", "ballistic", "entry_reflected", "internal_reflected", "absorbed", "cell_tir", "top_tir",
@@ -167,6 +168,8 @@ class Tallies(C.Structure):
         ("entered_sums", i64 * 16), ("ray_flags", i64 * 16),
         ("failure_subcode_counts", i64 * N_SUBCODES), ("ic_hist", i64 * IC_HIST),
         ("sched_stats", i64 * 16),
+        ("order_hits", i64 * N_DETECTORS * 6 * 2), ("geometric_order_hits", i64 * N_DETECTORS * 6 * 2),
+        ("path_sums", i64 * N_DETECTORS * 2 * N_PATH_SUMS),
     ]
 
     def as_dict(self) -> dict:

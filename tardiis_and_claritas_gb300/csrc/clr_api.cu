@@ -451,6 +451,14 @@ static void tally_to_host(const DevTally& d, clr_tallies* out, int64_t n_rays) {
     for (int k = 0; k < CLR_N_SUBCODES; ++k) out->failure_subcode_counts[k] = (int64_t)t.subcodes[k];
     for (int k = 0; k < CLR_IC_HIST; ++k) out->ic_hist[k] = (int64_t)d.ic_hi[k] + (k < 64 ? (int64_t)t.ic_lo[k] : 0);
     for (int k = 0; k < 16; ++k) out->sched_stats[k] = (int64_t)d.sched[k];
+    for (int side = 0; side < 2; ++side)
+        for (int j = 0; j < CLR_N_DETECTORS; ++j) {
+            for (int o = 0; o < 6; ++o) {
+                out->order_hits[side][o][j] = (int64_t)d.pd.order[side][o][j];
+                out->geometric_order_hits[side][o][j] = (int64_t)d.pd.geom_order[side][o][j];
+            }
+            for (int k = 0; k < CLR_N_PATH_SUMS; ++k) out->path_sums[k][side][j] = (int64_t)d.pd.sums[k][side][j];
+        }
     out->device_error = (t.n_done == (unsigned long long)n_rays) ? 0 : 1;
 }
 

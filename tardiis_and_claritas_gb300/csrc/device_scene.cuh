@@ -70,12 +70,22 @@ struct TallyCore {
 };
 #define CLR_TALLY_TAIL (CLR_N_STATUS + CLR_N_FAILURE_CODES + CLR_N_EVENT_COUNTERS + CLR_N_CONDITIONAL_STATS + 1 + 16 + 16 + CLR_N_SUBCODES + 64)
 
+// Detector hits partitioned for the particle-path diagnostics of the reference's host
+// (CLARITAS/CLARITAS.py:8019-8110: native [0] and mirror [1] detector ids of every detected ray), counted
+// on the device instead of from per-ray arrays.
+struct PathDiag {
+    unsigned long long order[2][6][CLR_N_DETECTORS];       // by particle-interaction count 0,1,2,3,4,5+
+    unsigned long long geom_order[2][6][CLR_N_DETECTORS];  // by geometric-event count 0,1,2,3,4,5+
+    unsigned long long sums[CLR_N_PATH_SUMS][2][CLR_N_DETECTORS];  // per-ray counter sums (CLR_PS_*)
+};
+
 // Per-scenario tallies in device memory: the core plus the high part of the histogram
 // (interaction counts >= 64, clamped to the last bin), updated with global atomics.
 struct DevTally {
     TallyCore c;
     unsigned long long ic_hi[CLR_IC_HIST];
     unsigned long long sched[16];
+    PathDiag pd;
 };
 
 }  // namespace clr

@@ -266,6 +266,23 @@ __device__ __forceinline__ void finish_ray(const DevScene& D, const DetTable& T,
             sink.add_d(5 * CLR_N_DETECTORS + mi, w);
             sink.add_d(7 * CLR_N_DETECTORS + mi, w * w);
         }
+        // particle-path partitions of the detected ray (one set per detector id it reaches)
+        {
+            PathDiag& pd = tallies[sid].pd;
+            const int oi = r.ic < 5 ? r.ic : 5, gi = r.gic < 5 ? r.gic : 5;
+            const int pv[CLR_N_PATH_SUMS] = {r.ic, r.gic, r.wic, r.wcoh, r.wmorph, r.pc.entry_reflections,
+                                            r.pc.internal_reflections};
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                const int id = side ? mi : ni;
+                if (id < 0) continue;
+                atomicAdd(&pd.order[side][oi][id], 1ull);
+                atomicAdd(&pd.geom_order[side][gi][id], 1ull);
+#pragma unroll
+                for (int k = 0; k < CLR_N_PATH_SUMS; ++k)
+                    if (pv[k] > 0) atomicAdd(&pd.sums[k][side][id], (unsigned long long)pv[k]);
+            }
+        }
         // legacy angular windows (:4429-4434)
         for (int mirror = 0; mirror < 2; ++mirror) {
             float xx = mirror ? -x : x;

@@ -619,7 +619,42 @@ class ClaritasForwardModel:
             native_detector_detection_fraction=float(native.sum() if ideal else pd_nat.sum()) / nrays,
             mirror_detector_detection_fraction=float(mirror.sum() if ideal else pd_mir.sum()) / nrays,
             legacy_channel_score_per_ray=float(legacy_sym_total.sum()) / nrays,
-            symmetry_variance_reduction=bool(sym), batch_diagnostics=rows, particle_diagnostics=dict(ph))
+            symmetry_variance_reduction=bool(sym), batch_diagnostics=rows, particle_diagnostics=dict(ph),
+            detector_particle_path_diagnostics=self._path_diagnostics(tot, hw_sym, avg))
+
+    # The reference's detector particle-path diagnostics (simulate, CLARITAS.py:8019-8110 and :8972-9140) from
+    # the device partitions of the detected rays; partitions that need per-ray provenance the device does not
+    # keep (first/last bin, deflection angles, causal sequences) are not produced.
+    _ORDER_LABELS = ["0", "1", "2", "3", "4", "5+"]
+    _MEAN_KEYS = ["mean_particle_interactions_by_channel", "mean_geometric_interactions_by_channel",
+                  "mean_wave_interactions_by_channel", "mean_coherent_wave_interactions_by_channel",
+                  "mean_morphology_wave_interactions_by_channel", "mean_entry_reflections_by_channel",
+                  "mean_internal_reflections_by_channel"]
+    _CSTAT_NAMES = ["candidate_trials", "outcome_rejections", "inaccessible_trials", "accepted_geometric",
+                    "accepted_coherent", "accepted_morphology", "accepted_absorptions", "accepted_scatterings",
+                    "numerical_failures", "retry_exhaustions"]
+
+    def _path_diagnostics(self, tot: dict, denp: np.ndarray, avg: bool) -> dict:
+        def sym(native, mirror):
+            return 0.5 * (native + mirror) if avg else native.copy()
+        oh = np.asarray(tot["order_hits"], dtype=np.float64)            # [side][order][channel]
+        gh = np.asarray(tot["geometric_order_hits"], dtype=np.float64)  # [side][order][channel]
+        ps = np.asarray(tot["path_sums"], dtype=np.float64)             # [sum][side][channel]
+        order, gorder = sym(oh[0], oh[1]), sym(gh[0], gh[1])            # [6][18]
+        sums = sym(ps[:, 0, :], ps[:, 1, :])                            # [7][18]
+        denp = np.asarray(denp, dtype=np.float64)
+        out = {"exact_particle_order_labels": list(self._ORDER_LABELS), "exact_particle_order_scores": order,
+               "exact_geometric_order_labels": list(self._ORDER_LABELS), "exact_geometric_order_scores": gorder,
+               "exact_particle_order_partition_closure_error_scores": denp - order.sum(axis=0),
+               "exact_geometric_order_partition_closure_error_scores": denp - gorder.sum(axis=0)}
+        for k, key in enumerate(self._MEAN_KEYS):
+            out[key] = np.divide(sums[k], denp, out=np.full(denp.shape, np.nan), where=denp > 0)
+        cond = self.config.particle_event_model in ("hybrid_mie_exact_rate", "hybrid_mie_exact_rate_moment_constrained")
+        out["conditional_sampler_counts"] = dict(zip(self._CSTAT_NAMES, [int(v) for v in tot["conditional_stats"]]))
+        out["closure"] = ("Mie extinction and terminal outcomes; conditional finite-particle angular/path law"
+                          if cond else self.config.particle_event_model + "; configured unconditional event law")
+        out["conditional_max_trials"] = 16384
+        return out
 
     def close(self):
         if self._ctx is not None:

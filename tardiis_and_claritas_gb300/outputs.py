@@ -1,0 +1,190 @@
+"""The reference's per-case output files, written from a ForwardResult.
+
+* ``detector_response.csv`` — one row per detector angle with the reference's columns and integrity checks
+  (`_write_detector_outputs`, CLARITAS/CLARITAS.py:12653-12696): absolute and normalised symmetric scores,
+  native/mirror counts, the particle-uninteracted / interacted split from the exact interaction-order
+  partition, sqrt(N) and batch-jackknife standard errors.
+* ``run_summary.json`` — the case summary under the reference's key names (`_summary_dict`, :12849-12971),
+  filled from the result and the model configuration; keys that describe the reference's own script
+  environment (source digest, comparison baselines) carry this library's equivalents or None.
+
+JSON and CSV values go through the reference's sanitiser rules (`_json_safe`, :11362-11375): arrays become
+lists, NumPy scalars Python scalars, non-finite floats None; JSON is written sorted with indent 2.
+"""
+from __future__ import annotations
+
+import csv
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+
+from .scene import DETECTOR_ANGLES_DEG, vortex_surface_geometry
+
+
+class CaseIntegrityError(RuntimeError):
+    """A result field failed the reference's output integrity checks."""
+
+
+def json_safe(value):
+    if isinstance(value, np.ndarray):
+        return value.tolist()
+    if isinstance(value, np.generic):
+        return value.item()
+    if isinstance(value, Path):
+        return str(value)
+    if isinstance(value, dict):
+        return {str(k): json_safe(v) for k, v in value.items()}
+    if isinstance(value, (list, tuple)):
+        return [json_safe(v) for v in value]
+    if isinstance(value, float) and not np.isfinite(value):
+        return None
+    return value
+
+
+def write_json(path, data) -> None:
+    Path(path).write_text(json.dumps(json_safe(data), indent=2, sort_keys=True), encoding="utf-8")
+
+
+def save_csv(path, fieldnames, rows) -> None:
+    with Path(path).open("w", newline="", encoding="utf-8") as f:
+        w = csv.DictWriter(f, fieldnames=list(fieldnames))
+        w.writeheader()
+        for row in rows:
+            w.writerow({k: json_safe(row.get(k)) for k in fieldnames})
+
+
+def write_detector_outputs(out, material: str, concentration: float, wavelength_nm: float, seed: int, res) -> list:
+    """detector_response.csv of one case; returns its rows."""
+    out = Path(out)
+    score = np.asarray(res.hardware_symmetry_scores, dtype=float)
+    norm = np.asarray(res.normalized_hardware_symmetry_response, dtype=float)
+    jk = np.asarray(res.hardware_normalized_jackknife_se, dtype=float)
+    native = np.asarray(res.hardware_native_hits, dtype=np.int64)
+    mirror = np.asarray(res.hardware_mirror_hits, dtype=np.int64)
+    expected = (len(DETECTOR_ANGLES_DEG),)
+    if any(a.shape != expected for a in (score, norm, jk, native, mirror)):
+        raise ValueError("corrupted production detector array shape")
+    if any(not np.all(np.isfinite(a)) or np.any(a < 0) for a in (score, norm, native, mirror)):
+        raise CaseIntegrityError("nonfinite or negative production detector field")
+    order_scores = np.asarray(res.detector_particle_path_diagnostics["exact_particle_order_scores"])
+    if order_scores.shape != (6, len(score)) or not np.allclose(order_scores.sum(axis=0), score, rtol=1e-12,
+                                                                 atol=1e-8):
+        raise CaseIntegrityError("particle interaction-order detector partition does not close")
+    rows = []
+    for i, angle in enumerate(DETECTOR_ANGLES_DEG):
+        rows.append({
+            "material": material,
+            "concentration_g_L": concentration,
+            "wavelength_nm": wavelength_nm,
+            "seed": seed,
+            "n_rays": int(res.n_rays),
+            "angle_deg": float(angle),
+            "absolute_score": float(score[i]),
+            "particle_uninteracted_score": float(order_scores[0, i]),
+            "particle_interacted_score": float(np.sum(order_scores[1:, i])),
+            "absolute_score_per_launched_ray": float(score[i] / res.n_rays),
+            "normalized_score": float(norm[i]),
+            "native_hit_count": int(native[i]),
+            "mirror_hit_count": int(mirror[i]),
+            "absolute_score_sqrtN_se_approx": float(math.sqrt(max(score[i], 0.0))),
+            "normalized_score_jackknife_se": float(jk[i]) if np.isfinite(jk[i]) else None,
+        })
+    out.mkdir(parents=True, exist_ok=True)
+    save_csv(out / "detector_response.csv", rows[0].keys(), rows)
+    return rows
+
+
+def summary_dict(material: str, concentration: float, wavelength_nm: float, seed: int, gpu_name: str,
+                 runtime_s: float, res, cfg, out, wavelength_assumptions=None) -> dict:
+    """The case summary under the reference's keys (values from the result and the configuration)."""
+    from . import lib
+    ph = res.particle_diagnostics or {}
+    total_nd = float(np.sum(np.asarray(ph.get("number_density_by_bin", []), dtype=float)))
+    mu_sca, mu_ext = float(res.mu_sca_per_m), float(res.mu_ext_per_m)
+    vg = vortex_surface_geometry(cfg.free_surface_model, cfg.zmean, cfg.tube_inner_radius_m,
+                                 cfg.vortex_wall_center_height_difference_m, cfg.vortex_core_radius_m,
+                                 cfg.gravity_m_s2)
+    sensor_h = float(cfg.sensor_height_above_bottom_m)
+    pd = res.detector_particle_path_diagnostics or {}
+    return {
+        "claritas_source_sha256": None,
+        "library_version": lib.load().clr_version().decode(),
+        "configuration_valid": True,
+        "material": material,
+        "concentration_g_L": float(concentration),
+        "wavelength_nm": float(wavelength_nm),
+        "n_rays": int(res.n_rays),
+        "requested_n_rays": int(res.requested_n_rays),
+        "seed": int(seed),
+        "runtime_s": float(runtime_s),
+        "gpu_device_index": 0,
+        "gpu_name": gpu_name,
+        "output_directory": str(out),
+        "stop_reason": res.stop_reason,
+        "production_failure_count": int(res.production_failure_count),
+        "entered_water_fraction": float(res.entered_water_fraction),
+        "air_exit_fraction": float(res.air_exit_fraction),
+        "axial_loss_fraction": float(res.axial_loss_fraction),
+        "detector_detection_fraction": float(res.detector_detection_fraction),
+        "mean_particle_interactions": float(res.mean_interactions),
+        "mean_geometric_interactions": float(res.mean_geometric_interactions),
+        "mean_wave_interactions": float(res.mean_wave_interactions),
+        "total_particle_number_density_m3": total_nd,
+        "mu_geom_per_m": float(res.mu_geom_per_m),
+        "mu_wave_per_m": float(res.mu_wave_per_m),
+        "mu_event_per_m": float(res.mu_event_per_m),
+        "mu_sca_per_m": mu_sca,
+        "mu_ext_per_m": mu_ext,
+        "mu_abs_per_m": max(mu_ext - mu_sca, 0.0),
+        "single_scattering_albedo": mu_sca / mu_ext if mu_ext > 0 else None,
+        "optical_depth_diameter": float(res.optical_depth_diameter),
+        "geometric_optical_depth_diameter": float(res.geometric_optical_depth_diameter),
+        "sediment_transport_model": res.sediment_transport_model,
+        "steady_state_sediment_enabled": cfg.sediment_transport_model != "uniform",
+        "sediment_eddy_diffusivity_m2_s": float(res.sediment_eddy_diffusivity_m2_s),
+        "sediment_particle_density_kg_m3": float(cfg.density_kg_per_m3),
+        "water_density_kg_m3": float(cfg.water_density_kg_per_m3),
+        "water_dynamic_viscosity_pa_s": float(cfg.water_dynamic_viscosity_pa_s),
+        "gravity_m_s2": float(cfg.gravity_m_s2),
+        "vortex_enabled": cfg.free_surface_model != "flat" and cfg.vortex_wall_center_height_difference_m > 0,
+        "free_surface_model": cfg.free_surface_model,
+        "vortex_wall_center_height_difference_m": float(cfg.vortex_wall_center_height_difference_m),
+        "vortex_core_radius_m": (float(cfg.vortex_core_radius_m)
+                                 if cfg.free_surface_model == "localized_scully_vortex" else None),
+        "vortex_equivalent_core_rpm": (float(vg["equivalent_core_rpm"])
+                                       if np.isfinite(vg["equivalent_core_rpm"]) else None),
+        "vortex_equivalent_rigid_body_rpm": (float(vg["equivalent_rigid_body_rpm"])
+                                             if np.isfinite(vg["equivalent_rigid_body_rpm"]) else None),
+        "vortex_center_surface_height_above_bottom_m": float(vg["center_z"] + sensor_h),
+        "vortex_wall_surface_height_above_bottom_m": float(vg["wall_z"] + sensor_h),
+        "meridional_circulation_ratio": float(cfg.meridional_circulation_ratio),
+        "sample_cell_diameter_m": 2.0 * float(cfg.tube_inner_radius_m),
+        "sample_cell_height_m": float(cfg.tube_length_m),
+        "water_level_m": float(cfg.water_height_m),
+        "sensor_ring_height_m": sensor_h,
+        "validated_geometry_baseline": None,
+        "validated_sediment_baseline": None,
+        "comparison_configuration_match": None,
+        "parabolic_transport_validation_pass": (
+            bool(int(res.production_failure_count) == 0 and np.isfinite(float(res.sediment_majorant_total_per_m)))
+            if cfg.free_surface_model == "parabolic_vortex" else None),
+        "particle_event_model": res.particle_event_model,
+        "conditional_outcome_closure": pd.get("closure"),
+        "conditional_sampler_counts": pd.get("conditional_sampler_counts"),
+        "particle_surface_rms_slope_deg": float(res.particle_surface_rms_slope_deg),
+        "wave_surface_rms_height_nm": float(res.wave_surface_rms_height_nm),
+        "wavelength_assumptions": wavelength_assumptions,
+    }
+
+
+def write_run_summary(out, material: str, concentration: float, wavelength_nm: float, seed: int, gpu_name: str,
+                      runtime_s: float, res, cfg, wavelength_assumptions=None) -> dict:
+    """run_summary.json of one case; returns the dict written."""
+    out = Path(out)
+    out.mkdir(parents=True, exist_ok=True)
+    d = summary_dict(material, concentration, wavelength_nm, seed, gpu_name, runtime_s, res, cfg, out,
+                     wavelength_assumptions)
+    write_json(out / "run_summary.json", d)
+    return d
