@@ -315,6 +315,46 @@ int clr_read_particle_physics(clr_ctx* ctx, clr_particle_physics* out);
  * clr_ray_record entries, or NULL for the tally-only hot path. */
 int clr_trace(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* records);
 
+/* Light-history diagnostics of the following traces of the current scene (the reference's
+ * simulate(light_transport_config=..., heatmap_size=...), CLARITAS/CLARITAS.py:7229-7300): for rays with
+ * global id < max_rays every water segment's track length is deposited into an nx x ny x nz voxel grid
+ * over x, y in [-rin, rin] and z in [zmin, zmax] by an exact FP64 traversal (also into a second grid
+ * once the ray has had a particle event), accepted particle-event sites are counted per voxel, the
+ * first representative_rays rays keep up to max_segments_per_ray clipped segments, and (heatmap_size
+ * > 0, every ray) every 10 um of water path adds one count to x-y and z-y heat maps. Nothing here draws a random
+ * number or changes a history. The buffers are zeroed by this call and accumulate over the following
+ * traces of the context until it is called again. */
+typedef struct clr_light_config {
+    int32_t enabled;                /* voxel grids, events and trajectories; 0 with heatmap_size 0: all off */
+    int32_t nx, ny, nz;             /* voxels per axis, each >= 4 */
+    int32_t max_rays;               /* >= 1 */
+    int32_t representative_rays, max_segments_per_ray;
+    int32_t heatmap_size;           /* 0: no heat maps */
+    float zmax;                     /* voxel box top: the higher of the free surface's centre and wall heights */
+    float heat_zmax;                /* heat-map z range top: the free surface height at the wall */
+} clr_light_config;
+int clr_set_light_diagnostics(clr_ctx* ctx, const clr_light_config* config);
+
+/* Results of the last trace with light diagnostics on; every array pointer may be NULL. */
+typedef struct clr_light_result {
+    float* track_length;            /* [nz][ny][nx] */
+    float* post_scatter_track_length;
+    float* scatter_event_weight;
+    uint32_t* scatter_event_count;
+    float* heatmap_xy;              /* [heatmap_size][heatmap_size] */
+    float* heatmap_zy;
+    float *trajectory_x0, *trajectory_y0, *trajectory_z0, *trajectory_x1, *trajectory_y1, *trajectory_z1;
+    int32_t* trajectory_order;      /* [representative_rays][max_segments_per_ray]: particle events before */
+    int32_t* trajectory_count;      /* [representative_rays] */
+    int32_t* trajectory_overflow;   /* [representative_rays] */
+    double segment_length_total, deposited_length_total;
+    int64_t segment_count, scatter_event_total;
+    int64_t error_count, boundary_adjustment_count, event_outside_count;
+    float first_outside_xyz_tol[4]; /* first event outside the box: x, y, z, tolerance */
+    uint32_t first_outside_ray, first_outside_set;
+} clr_light_result;
+int clr_read_light_diagnostics(clr_ctx* ctx, clr_light_result* out);
+
 /* Trace n_runs runs of the current scene in one engine execution (one persistent-kernel launch or
  * one sequence of wavefront passes): each run has its own photon range, seeds and tallies
  * (outs[n_runs]). The runs share rng_mode, weight_mode and flags. Replaces the reference's chunk loop

@@ -226,3 +226,25 @@ def records_to_numpy(buf, n: int):
 def record_dtype():
     import numpy as np
     return np.dtype([(nm, np.int32) for nm in RECORD_INT_FIELDS] + [(nm, np.float32) for nm in RECORD_FLOAT_FIELDS])
+
+
+class LightConfig(C.Structure):
+    _fields_ = [("enabled", i32), ("nx", i32), ("ny", i32), ("nz", i32), ("max_rays", i32),
+                ("representative_rays", i32), ("max_segments_per_ray", i32), ("heatmap_size", i32),
+                ("zmax", f32), ("heat_zmax", f32)]
+
+
+PF32 = C.POINTER(C.c_float)
+
+
+class LightResult(C.Structure):
+    _fields_ = [("track_length", PF32), ("post_scatter_track_length", PF32), ("scatter_event_weight", PF32),
+                ("scatter_event_count", C.POINTER(C.c_uint32)), ("heatmap_xy", PF32), ("heatmap_zy", PF32),
+                ("trajectory_x0", PF32), ("trajectory_y0", PF32), ("trajectory_z0", PF32),
+                ("trajectory_x1", PF32), ("trajectory_y1", PF32), ("trajectory_z1", PF32),
+                ("trajectory_order", PI32), ("trajectory_count", PI32), ("trajectory_overflow", PI32),
+                ("segment_length_total", f64), ("deposited_length_total", f64),
+                ("segment_count", i64), ("scatter_event_total", i64),
+                ("error_count", i64), ("boundary_adjustment_count", i64), ("event_outside_count", i64),
+                ("first_outside_xyz_tol", f32 * 4), ("first_outside_ray", u32), ("first_outside_set", u32)]
+

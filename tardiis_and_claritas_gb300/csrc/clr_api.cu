@@ -56,6 +56,12 @@ struct clr_ctx {
     size_t sw_scratch_bytes = 0;
     void* sw_jobs = nullptr;  // job descriptions of the batched rate kernels
     size_t sw_jobs_bytes = 0;
+    // light-history diagnostics (clr_set_light_diagnostics): host description, its device copy, buffers
+    bool light_on = false;
+    clr_light_config light_cfg{};
+    LightDiag light{};
+    LightDiag* d_light = nullptr;
+    std::vector<void*> light_allocs;
 };
 
 static int fail(clr_ctx* c, int code, const char* fmt, ...) {
@@ -133,6 +139,7 @@ int clr_destroy(clr_ctx* ctx) {
     cudaFree(ctx->sw_arena);
     cudaFree(ctx->sw_scratch);
     cudaFree(ctx->sw_jobs);
+    for (void* p : ctx->light_allocs) cudaFree(p);
     if (ctx->wave_live) cudaFreeHost(ctx->wave_live);
     if (ctx->wave_ev) cudaEventDestroy(ctx->wave_ev);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -502,7 +509,7 @@ struct SceneRef {
 // Traces n runs in one engine execution (one launch of the persistent kernel or one sequence of
 // wavefront passes), each run with its own scene, photon range, seeds and tallies.
 static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* runs, int n, clr_tallies* outs,
-                      clr_ray_record* d_records) {
+                      clr_ray_record* d_records, const LightDiag* d_light = nullptr) {
     if (!ctx || !runs || !outs || n < 1) return CLR_ERR_INVALID_ARGUMENT;
     if (d_records && n != 1) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "per-ray records need a single run");
     const clr_run_params& r0 = runs[0];
@@ -528,6 +535,7 @@ static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* 
     long long max_iter = 0;
     for (int i = 0; i < n; ++i) {
         fill_scene(*refs[i].sp, *refs[i].pb, runs + i, &hs[i]);
+        hs[i].light = d_light;
         max_iter = std::max(max_iter, (long long)refs[i].sp->max_iterations);
         cb[i + 1] = cb[i] + (runs[i].n_rays + chunk - 1) / chunk;
         rb[i + 1] = rb[i] + runs[i].n_rays;
@@ -588,7 +596,29 @@ static int trace_current(clr_ctx* ctx, const clr_run_params* runs, int n, clr_ta
     if (!ctx->built) return fail(ctx, CLR_ERR_NOT_READY, "clr_build_particles must succeed before clr_trace");
     if (n < 1) return CLR_ERR_INVALID_ARGUMENT;
     std::vector<SceneRef> refs(n, SceneRef{&ctx->sp, &ctx->pb});
-    return trace_runs(ctx, refs.data(), runs, n, outs, d_records);
+    return trace_runs(ctx, refs.data(), runs, n, outs, d_records, ctx->light_on ? ctx->d_light : nullptr);
+}
+
+// Zero the light-diagnostic buffers (trajectory coordinates to NaN and orders to -1, as the reference).
+static int light_reset(clr_ctx* ctx) {
+    {
+        const LightDiag& L = ctx->light;
+        const size_t vox = (size_t)L.nx * L.ny * L.nz, traj = (size_t)std::max(L.rep_rays * L.max_segments, 1);
+        const size_t heat = (size_t)std::max(L.vis * L.vis, 1), reps = (size_t)std::max(L.rep_rays, 1);
+        cudaStream_t st = ctx->stream;
+        CU(cudaMemsetAsync(L.total, 0, vox * 4, st)); CU(cudaMemsetAsync(L.post, 0, vox * 4, st));
+        CU(cudaMemsetAsync(L.event_weight, 0, vox * 4, st)); CU(cudaMemsetAsync(L.event_count, 0, vox * 4, st));
+        CU(cudaMemsetAsync(L.seg_total, 0, 8, st)); CU(cudaMemsetAsync(L.dep_total, 0, 8, st));
+        CU(cudaMemsetAsync(L.seg_count, 0, 8, st)); CU(cudaMemsetAsync(L.event_total, 0, 8, st));
+        CU(cudaMemsetAsync(L.err_count, 0, 4, st)); CU(cudaMemsetAsync(L.adj_count, 0, 4, st));
+        CU(cudaMemsetAsync(L.outside, 0, 32, st));
+        for (float* p : {L.tx0, L.ty0, L.tz0, L.tx1, L.ty1, L.tz1}) CU(cudaMemsetAsync(p, 0xFF, traj * 4, st));
+        CU(cudaMemsetAsync(L.torder, 0xFF, traj * 4, st));
+        CU(cudaMemsetAsync(L.tcount, 0, reps * 4, st)); CU(cudaMemsetAsync(L.toverflow, 0, reps * 4, st));
+        CU(cudaMemsetAsync(L.heat_xy, 0, heat * 4, st)); CU(cudaMemsetAsync(L.heat_zy, 0, heat * 4, st));
+        CU(cudaStreamSynchronize(st));
+    }
+    return CLR_OK;
 }
 
 static int trace_impl(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray_record* d_records) {
@@ -886,6 +916,95 @@ int clr_trace(clr_ctx* ctx, const clr_run_params* run, clr_tallies* out, clr_ray
 
 int clr_trace_batch(clr_ctx* ctx, const clr_run_params* runs, int n_runs, clr_tallies* outs) {
     return trace_current(ctx, runs, n_runs, outs, nullptr);
+}
+
+int clr_set_light_diagnostics(clr_ctx* ctx, const clr_light_config* cfg) {
+    if (!ctx || !cfg) return CLR_ERR_INVALID_ARGUMENT;
+    CU(cudaSetDevice(ctx->device));
+    CU(cudaStreamSynchronize(ctx->stream));
+    for (void* p : ctx->light_allocs) cudaFree(p);
+    ctx->light_allocs.clear();
+    ctx->light_on = false;
+    ctx->light = LightDiag{};
+    if (cfg->heatmap_size < 0) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "heatmap_size must be >= 0");
+    if (!cfg->enabled && cfg->heatmap_size == 0) return CLR_OK;
+    // the reference's configuration rules (:7246-7252) and allocation cap (:7266-7275)
+    const bool vx = cfg->enabled != 0;
+    if (vx && cfg->max_rays < 1) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "light diagnostic max_rays must be >=1");
+    if (vx && std::min(cfg->nx, std::min(cfg->ny, cfg->nz)) < 4)
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "light diagnostic grid dimensions must each be >=4");
+    const int rep = vx ? std::min(cfg->representative_rays, cfg->max_rays) : 0;
+    if (vx && (rep < 0 || cfg->max_segments_per_ray < 1))
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "invalid representative-ray diagnostic configuration");
+    const size_t vox = vx ? (size_t)cfg->nx * cfg->ny * cfg->nz : 1;
+    const size_t traj = (size_t)std::max(rep * (vx ? cfg->max_segments_per_ray : 1), 1), reps = (size_t)std::max(rep, 1);
+    const size_t bytes = vox * 20 + traj * 32 + reps * 8 + 8;
+    if (bytes > 1000000000ull)
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "light diagnostic allocation is too large (%.3g GB)", bytes / 1e9);
+    const size_t heat = (size_t)std::max(cfg->heatmap_size * cfg->heatmap_size, 1);
+    LightDiag& L = ctx->light;
+    L.voxels = vx ? 1 : 0;
+    L.nx = vx ? cfg->nx : 1; L.ny = vx ? cfg->ny : 1; L.nz = vx ? cfg->nz : 1; L.max_rays = vx ? cfg->max_rays : 0;
+    L.rep_rays = rep; L.max_segments = vx ? cfg->max_segments_per_ray : 0; L.vis = cfg->heatmap_size;
+    L.zmax = cfg->zmax;
+    L.zvis = cfg->heat_zmax;
+    auto A = [&](void** p, size_t b) {
+        cudaError_t e = cudaMalloc(p, b);
+        if (e == cudaSuccess) ctx->light_allocs.push_back(*p);
+        return e;
+    };
+    CU(A((void**)&L.total, vox * 4)); CU(A((void**)&L.post, vox * 4)); CU(A((void**)&L.event_weight, vox * 4));
+    CU(A((void**)&L.event_count, vox * 4));
+    CU(A((void**)&L.seg_total, 8)); CU(A((void**)&L.dep_total, 8)); CU(A((void**)&L.seg_count, 8));
+    CU(A((void**)&L.event_total, 8)); CU(A((void**)&L.err_count, 4)); CU(A((void**)&L.adj_count, 4));
+    CU(A((void**)&L.outside, 32));
+    for (float** p : {&L.tx0, &L.ty0, &L.tz0, &L.tx1, &L.ty1, &L.tz1}) CU(A((void**)p, traj * 4));
+    CU(A((void**)&L.torder, traj * 4)); CU(A((void**)&L.tcount, reps * 4)); CU(A((void**)&L.toverflow, reps * 4));
+    CU(A((void**)&L.heat_xy, heat * 4)); CU(A((void**)&L.heat_zy, heat * 4));
+    CU(A((void**)&ctx->d_light, sizeof(LightDiag)));
+    CU(cudaMemcpy(ctx->d_light, &L, sizeof L, cudaMemcpyHostToDevice));
+    ctx->light_cfg = *cfg;
+    const int rc = light_reset(ctx);
+    if (rc != CLR_OK) return rc;
+    ctx->light_on = true;
+    return CLR_OK;
+}
+
+int clr_read_light_diagnostics(clr_ctx* ctx, clr_light_result* o) {
+    if (!ctx || !o) return CLR_ERR_INVALID_ARGUMENT;
+    if (!ctx->light_on) return fail(ctx, CLR_ERR_NOT_READY, "light diagnostics are off");
+    CU(cudaSetDevice(ctx->device));
+    const LightDiag& L = ctx->light;
+    cudaStream_t st = ctx->stream;
+    const size_t vox = (size_t)L.nx * L.ny * L.nz, traj = (size_t)L.rep_rays * L.max_segments;
+    const size_t heat = (size_t)L.vis * L.vis, reps = (size_t)L.rep_rays;
+    struct Cp { void* dst; const void* src; size_t bytes; };
+    const Cp cps[] = {{o->track_length, L.total, vox * 4}, {o->post_scatter_track_length, L.post, vox * 4},
+                      {o->scatter_event_weight, L.event_weight, vox * 4}, {o->scatter_event_count, L.event_count, vox * 4},
+                      {o->heatmap_xy, L.heat_xy, heat * 4}, {o->heatmap_zy, L.heat_zy, heat * 4},
+                      {o->trajectory_x0, L.tx0, traj * 4}, {o->trajectory_y0, L.ty0, traj * 4},
+                      {o->trajectory_z0, L.tz0, traj * 4}, {o->trajectory_x1, L.tx1, traj * 4},
+                      {o->trajectory_y1, L.ty1, traj * 4}, {o->trajectory_z1, L.tz1, traj * 4},
+                      {o->trajectory_order, L.torder, traj * 4}, {o->trajectory_count, L.tcount, reps * 4},
+                      {o->trajectory_overflow, L.toverflow, reps * 4}};
+    for (const Cp& c : cps)
+        if (c.dst && c.bytes) CU(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, st));
+    unsigned long long sc = 0, et = 0;
+    unsigned err = 0, adj = 0, outside[8] = {0};
+    CU(cudaMemcpyAsync(&o->segment_length_total, L.seg_total, 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&o->deposited_length_total, L.dep_total, 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&sc, L.seg_count, 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&et, L.event_total, 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&err, L.err_count, 4, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&adj, L.adj_count, 4, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(outside, L.outside, 32, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    o->segment_count = (int64_t)sc; o->scatter_event_total = (int64_t)et;
+    o->error_count = err; o->boundary_adjustment_count = adj; o->event_outside_count = outside[0];
+    for (int k = 0; k < 3; ++k) memcpy(&o->first_outside_xyz_tol[k], &outside[1 + k], 4);
+    memcpy(&o->first_outside_xyz_tol[3], &outside[5], 4);
+    o->first_outside_ray = outside[4]; o->first_outside_set = outside[6];
+    return CLR_OK;
 }
 
 int clr_sweep_build(clr_ctx* ctx, int n_scenarios, const clr_scene_params* scenes, const clr_particle_spec* particles,

@@ -7,6 +7,22 @@
 
 namespace clr {
 
+// Light-history diagnostics of a trace (no effect on any history: no random draw, diagnostic buffers only).
+// Voxel grids are [nz][ny][nx] over x, y in [-R, R] and z in [zmin, zmax]; heat maps [vis][vis].
+struct LightDiag {
+    int voxels;                             // voxel grids, events and trajectories on (heat maps are separate)
+    int nx, ny, nz, max_rays, rep_rays, max_segments, vis;
+    float zmax, zvis;                       // voxel box top; heat-map z range top (surface height at the wall)
+    float *total, *post, *event_weight;     // track length, after >= 1 particle event; scatter-event weight
+    unsigned *event_count;                  // scatter events per voxel
+    double *seg_total, *dep_total;          // [1] clipped segment length, deposited length
+    unsigned long long *seg_count, *event_total;
+    unsigned *err_count, *adj_count, *outside;  // [1], [1], [8]: count, first outside x, y, z, gid, tol, set
+    float *tx0, *ty0, *tz0, *tx1, *ty1, *tz1;   // [rep_rays][max_segments] representative trajectories
+    int *torder, *tcount, *toverflow;           // [rep_rays][max_segments], [rep_rays], [rep_rays]
+    float *heat_xy, *heat_zy;                   // [vis][vis] (vis 0: none)
+};
+
 struct DevScene {
     clr_scene_params P;
     // particle tables (float copies are exact casts of the FP64 tables, which is what the
@@ -50,6 +66,7 @@ struct DevScene {
     int32_t weight_mode;
     float roulette_threshold, roulette_survival;
     int32_t pad;
+    const LightDiag* light;     // null unless light-history diagnostics are on for this trace
 };
 
 // Tally counters shared by the per-warp shared-memory tally and the per-scenario device tally.

@@ -427,12 +427,159 @@ __device__ __forceinline__ bool flight_clear(const clr_scene_params& P, float x,
     return fmaxf(z, z1) < zs - 1e-6f;
 }
 
+// ---------------- light-history diagnostics (observational: no random draw, no state change) ----------------
+// Heat maps: every 10 um along a water segment one count in the x-y and z-y maps (:3296-3310).
+__device__ void light_heat_segment(const LightDiag& L, float x0, float y0, float z0, float vx, float vy, float vz,
+                                   float dist, float Rin, float zmin) {
+    const int vis = L.vis;
+    if (vis <= 0 || dist <= 0.0f) return;
+    const float spacing = 1.0e-5f;
+    int n = (int)ceilf(dist / spacing);
+    if (n < 1) n = 1;
+    if (n > 20000) n = 20000;
+    for (int k = 1; k <= n; ++k) {
+        float f = (float)k / (float)n;
+        float x = x0 + vx * dist * f, y = y0 + vy * dist * f, z = z0 + vz * dist * f;
+        int ix = (int)(((x + Rin) / (2.0f * Rin)) * vis);
+        int iy = vis - 1 - (int)(((y + Rin) / (2.0f * Rin)) * vis);
+        int iz = (int)(((z - zmin) / (L.zvis - zmin)) * vis);
+        if (ix >= 0 && ix < vis && iy >= 0 && iy < vis) atomicAdd(&L.heat_xy[iy * vis + ix], 1.0f);
+        if (iz >= 0 && iz < vis && iy >= 0 && iy < vis) atomicAdd(&L.heat_zy[iy * vis + iz], 1.0f);
+    }
+}
+
+__device__ __forceinline__ int light_clip_axis(double p, double d, double lo, double hi, double* t0, double* t1) {
+    if (fabs(d) < 1.0e-30f) return (p >= lo && p <= hi) ? 1 : 0;
+    double a = (lo - p) / d, b = (hi - p) / d;
+    if (a > b) { double q = a; a = b; b = q; }
+    *t0 = fmax(*t0, a); *t1 = fmin(*t1, b);
+    return *t1 >= *t0;
+}
+
+// Exact track-length deposition of one water segment by a 3-D voxel traversal in FP64, with the
+// reference's endpoint-snap tolerance and integrity counters (:3318-3400); representative rays keep their
+// clipped segments.
+__device__ void light_segment(const LightDiag& L, uint32_t gid, float Rin, float zmin, float x0, float y0,
+                              float z0, float vx, float vy, float vz, float dist, int particle_order) {
+    if (!(dist > 0.0f) || !isfinite(dist)) return;
+    const int nx = L.nx, ny = L.ny, nz = L.nz;
+    const float zmax = L.zmax;
+    if (nx <= 0 || ny <= 0 || nz <= 0 || !(zmax > zmin)) { atomicAdd(L.err_count, 1u); return; }
+    const double xmin = -(double)Rin, ymin = -(double)Rin;
+    double c0 = 0.0, c1 = 1.0;
+    if (!light_clip_axis(x0, (double)vx * (double)dist, -Rin, Rin, &c0, &c1) ||
+        !light_clip_axis(y0, (double)vy * (double)dist, -Rin, Rin, &c0, &c1) ||
+        !light_clip_axis(z0, (double)vz * (double)dist, zmin, zmax, &c0, &c1))
+        return;
+    const double ax = x0 + (double)vx * (double)dist * c0, ay = y0 + (double)vy * (double)dist * c0,
+                 az = z0 + (double)vz * (double)dist * c0;
+    const double x1 = x0 + (double)vx * (double)dist * c1, y1 = y0 + (double)vy * (double)dist * c1,
+                 z1 = z0 + (double)vz * (double)dist * c1;
+    const double clipped = dist * (c1 - c0);
+    if (!(clipped > 0.0f)) return;
+    atomicAdd(L.seg_total, clipped);
+    atomicAdd(L.seg_count, 1ull);
+    if ((int)gid < L.rep_rays && L.max_segments > 0) {
+        const int slot = L.tcount[gid];
+        if (slot < L.max_segments) {
+            const int q = (int)gid * L.max_segments + slot;
+            L.tx0[q] = (float)ax; L.ty0[q] = (float)ay; L.tz0[q] = (float)az;
+            L.tx1[q] = (float)x1; L.ty1[q] = (float)y1; L.tz1[q] = (float)z1;
+            L.torder[q] = particle_order;
+            L.tcount[gid] = slot + 1;
+        } else {
+            L.toverflow[gid] = 1;
+        }
+    }
+    const double dx = (2.0 * (double)Rin) / nx, dy = (2.0 * (double)Rin) / ny, dz = ((double)zmax - (double)zmin) / nz;
+    int ix = (int)floor((ax - xmin) / dx), iy = (int)floor((ay - ymin) / dy), iz = (int)floor((az - zmin) / dz);
+    if (ix < 0) ix = 0;
+    if (ix >= nx) ix = nx - 1;
+    if (iy < 0) iy = 0;
+    if (iy >= ny) iy = ny - 1;
+    if (iz < 0) iz = 0;
+    if (iz >= nz) iz = nz - 1;
+    const double sx = x1 - ax, sy = y1 - ay, sz = z1 - az;
+    const int stepx = (sx > 0.0f) ? 1 : ((sx < 0.0f) ? -1 : 0);
+    const int stepy = (sy > 0.0f) ? 1 : ((sy < 0.0f) ? -1 : 0);
+    const int stepz = (sz > 0.0f) ? 1 : ((sz < 0.0f) ? -1 : 0);
+    double bx = xmin + (double)(stepx > 0 ? ix + 1 : ix) * dx;
+    double by = ymin + (double)(stepy > 0 ? iy + 1 : iy) * dy;
+    double bz = zmin + (double)(stepz > 0 ? iz + 1 : iz) * dz;
+    double tmx = (stepx == 0) ? CLR_INF_F : (bx - ax) / sx;
+    double tmy = (stepy == 0) ? CLR_INF_F : (by - ay) / sy;
+    double tmz = (stepz == 0) ? CLR_INF_F : (bz - az) / sz;
+    if (tmx < 0.0f) tmx = 0.0f;
+    if (tmy < 0.0f) tmy = 0.0f;
+    if (tmz < 0.0f) tmz = 0.0f;
+    double u = 0.0, deposited = 0.0;
+    const float tol = 2.0e-6f;
+    const int max_steps = nx + ny + nz + 8;
+    for (int k = 0; k < max_steps && u < 1.0f; ++k) {
+        if (ix < 0 || ix >= nx || iy < 0 || iy >= ny || iz < 0 || iz >= nz) {
+            if (u >= 1.0f - tol) { atomicAdd(L.adj_count, 1u); u = 1.0f; break; }
+            atomicAdd(L.err_count, 1u);
+            break;
+        }
+        double un = fmin(1.0, fmin(tmx, fmin(tmy, tmz)));
+        if (un < 1.0f && un >= 1.0f - tol) { un = 1.0f; atomicAdd(L.adj_count, 1u); }
+        if (un < u) {
+            if (u - un <= tol) { un = u; atomicAdd(L.adj_count, 1u); }
+            else { atomicAdd(L.err_count, 1u); break; }
+        }
+        const double length = (un - u) * clipped;
+        if (length > 0.0f) {
+            const int q = (iz * ny + iy) * nx + ix;
+            atomicAdd(&L.total[q], (float)length);
+            if (particle_order > 0) atomicAdd(&L.post[q], (float)length);
+            deposited += length;
+        }
+        if (un >= 1.0f) { u = 1.0f; break; }
+        const double eps = 8.0 * 2.2204460492503131e-16 * fmax(1.0, fabs(un));
+        if (tmx <= un + eps) { ix += stepx; tmx = (xmin + (double)(stepx > 0 ? ix + 1 : ix) * dx - ax) / sx; }
+        if (tmy <= un + eps) { iy += stepy; tmy = (ymin + (double)(stepy > 0 ? iy + 1 : iy) * dy - ay) / sy; }
+        if (tmz <= un + eps) { iz += stepz; tmz = ((double)zmin + (double)(stepz > 0 ? iz + 1 : iz) * dz - az) / sz; }
+        u = un;
+    }
+    if (u < 1.0f - tol) atomicAdd(L.err_count, 1u);
+    atomicAdd(L.dep_total, deposited);
+}
+
+// A scatter-event site into its voxel (:3409-3438).
+__device__ void light_event(const LightDiag& L, uint32_t gid, float Rin, float zmin, float x, float y, float z) {
+    atomicAdd(L.event_total, 1ull);
+    const float zmax = L.zmax;
+    const float tol = 2.0e-6f * fmaxf(2.0f * Rin, zmax - zmin);
+    if (!isfinite(x) || !isfinite(y) || !isfinite(z) || x < -Rin - tol || x > Rin + tol || y < -Rin - tol ||
+        y > Rin + tol || z < zmin - tol || z > zmax + tol) {
+        const unsigned prev = atomicAdd(L.outside, 1u);
+        if (prev == 0u) {
+            L.outside[1] = __float_as_uint(x); L.outside[2] = __float_as_uint(y); L.outside[3] = __float_as_uint(z);
+            L.outside[4] = gid; L.outside[5] = __float_as_uint(tol); L.outside[6] = 1u;
+        }
+        atomicAdd(L.err_count, 1u);
+        return;
+    }
+    const int nx = L.nx, ny = L.ny, nz = L.nz;
+    int ix = (int)floorf(((x + Rin) / (2.0f * Rin)) * nx);
+    int iy = (int)floorf(((y + Rin) / (2.0f * Rin)) * ny);
+    int iz = (int)floorf(((z - zmin) / (zmax - zmin)) * nz);
+    int adjusted = 0;
+    if (ix < 0) { ix = 0; adjusted = 1; } else if (ix >= nx) { ix = nx - 1; adjusted = 1; }
+    if (iy < 0) { iy = 0; adjusted = 1; } else if (iy >= ny) { iy = ny - 1; adjusted = 1; }
+    if (iz < 0) { iz = 0; adjusted = 1; } else if (iz >= nz) { iz = nz - 1; adjusted = 1; }
+    if (adjusted) atomicAdd(L.adj_count, 1u);
+    const int q = (iz * ny + iy) * nx + ix;
+    atomicAdd(&L.event_weight[q], 1.0f);
+    atomicAdd(&L.event_count[q], 1u);
+}
+
 // Flight part. Returns WE_NONE when the iteration completed (the photon stays in the water),
 // WE_ENDED when the history ended, else the handler that completes the iteration (*ev_pidx is the
 // bin of a particle event). Position and direction are stored in r in every case.
 template <class S>
 __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S* opt, unsigned long long* cstats,
-                                            int* ev_pidx) {
+                                            int* ev_pidx, uint32_t gid) {
     const clr_scene_params& P = D.P;
     if (r.step >= (int)P.max_iterations) { r.pf = OP_ITERATION_LIMIT; r.pfs = OS_ITERATION_LIMIT; r.st = 4; return WE_ENDED; }
     r.step++;
@@ -505,6 +652,11 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
             do_particle = freep < tbound;
             travel = do_particle ? freep : tbound;
         }
+        if (D.light) {  // the segment about to be flown (:4763-4772): heat maps for every ray, voxels for the first
+            const LightDiag& LD = *D.light;
+            if (LD.vis > 0) light_heat_segment(LD, x, y, z, vx, vy, vz, travel, RIN, ZMIN);
+            if (LD.voxels && gid < (uint32_t)LD.max_rays) light_segment(LD, gid, RIN, ZMIN, x, y, z, vx, vy, vz, travel, r.ic);
+        }
         x += travel * vx; y += travel * vy; z += travel * vz;
         r.wp += travel;
         if (do_particle && !lazy) {
@@ -554,6 +706,7 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
                 if (uniform(st) >= pacc) { r.nulls++; break; }
             }
             r.ic++;
+            if (D.light && D.light->voxels && gid < (uint32_t)D.light->max_rays) light_event(*D.light, gid, RIN, ZMIN, x, y, z);
             const float vinx = vx, viny = vy, vinz = vz;
             const int COND = (P.event_model == 4 || P.event_model == 5);
             const float COHERENT = fminf(fmaxf(D.coherent_f, 0.0f), 1.0f);
@@ -883,9 +1036,10 @@ __device__ __forceinline__ bool water_side(const DevScene& D, Ray& r, S* st) {
 
 // One whole water iteration (flight part and its handler).
 template <class S, bool kWeighted>
-__device__ __forceinline__ bool water_step(const DevScene& D, Ray& r, S* st, S* opt, unsigned long long* cstats) {
+__device__ __forceinline__ bool water_step(const DevScene& D, Ray& r, S* st, S* opt, unsigned long long* cstats,
+                                           uint32_t gid) {
     int pidx = -1;
-    const int e = water_flight(D, r, st, opt, cstats, &pidx);
+    const int e = water_flight(D, r, st, opt, cstats, &pidx, gid);
     (void)kWeighted;
     switch (e) {
         case WE_NONE: return false;

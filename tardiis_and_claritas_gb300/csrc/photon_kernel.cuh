@@ -510,7 +510,8 @@ __global__ void __launch_bounds__(CLR_TRACE_THREADS) photon_kernel(const DevScen
             if (pick == PHASE_SOURCE) done = source_segment(D, r, L.source());
             else if (pick == PHASE_ENTRY) done = entry_segment(D, r, L.transport());
             else done = water_step<typename Mode::Stream, kWeighted>(D, r, L.transport(), L.optics(),
-                                                                      (sid == home) ? &wt->cstats[0] : &tallies[sid].c.cstats[0]);
+                                                                      (sid == home) ? &wt->cstats[0] : &tallies[sid].c.cstats[0],
+                                                                      gid);
             if (done) {
                 const long long tf = clock64();
                 finish_ray<Mode>(D, det, r, gid, sid, home, wt, tallies, kRecord ? records + rid : nullptr);

@@ -279,7 +279,7 @@ __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevSce
     } else if constexpr (Q == WQ_FLIGHT) {
         for (int k = 0; k < kFlightSteps; ++k) {
             int pidx = -1;
-            const int e = water_flight(D, r, L.transport(), L.optics(), cstats, &pidx);
+            const int e = water_flight(D, r, L.transport(), L.optics(), cstats, &pidx, m.gid);
             if (e == WE_NONE) continue;
             m.pidx = pidx;
             switch (e) {

@@ -12,8 +12,9 @@ adaptive stopping rule (:8818-8880) exactly as the reference's batch loop does.
 Two random streams are offered: ``rng="philox"`` (default; the fast production path) and
 ``rng="reference"`` (the reference's per-ray xorshift streams and seeds: per-ray outcomes equal the
 reference kernels'). Features outside the photon-transport path raise ``NotImplementedError``:
-light-history diagnostics and heat maps (``light_transport_config``, ``heatmap_size``) and population
-aggregation/fragmentation. Named materials (the reference's loess/kaolin PSD
+population aggregation/fragmentation. Light-history diagnostics and heat maps run on the device (scatter-event
+sites are the accepted particle collisions; absorption sites are not recorded). Named materials (the reference's
+loess/kaolin PSD
 tables) are not bundled: pass a ``scene.Particles`` as ``material`` or register one under a name.
 """
 from __future__ import annotations
@@ -353,8 +354,7 @@ class ClaritasForwardModel:
                  target_detector_score=None, min_rays=None, max_rays=None, min_rear_channel_score=None,
                  min_h170_score=None, stability_l1_tolerance=None, stability_window=3,
                  ray_id_start=0) -> ForwardResult:
-        if light_transport_config is not None or int(heatmap_size) > 0:
-            raise NotImplementedError("light-transport diagnostics and heat maps are outside this library")
+        light = self._light_setup(light_transport_config, heatmap_size)
         if collect_rays:
             raise NotImplementedError("collect_rays: use lib.Context.trace(run, records=True) for per-ray records")
         cfg = self.config
@@ -392,6 +392,8 @@ class ClaritasForwardModel:
             left -= sizes[-1]
         # Batches are traced in groups through one clr_trace_batch call; a fixed-count run is one group.
         group = len(sizes) if not adaptive else max(1, min(len(sizes), 64))
+        if adaptive and light is not None:
+            group = 1  # light diagnostics accumulate over traced batches: trace no batch past the stopping one
         tallies = []
         stop_at = None
         state = _StopState()
@@ -415,7 +417,103 @@ class ClaritasForwardModel:
             stop_reason = state.reason
         else:
             stop_reason = state.final_reason(adaptive, target, rear_target, h170_target, stability_l1_tolerance)
-        return self._result(tallies, requested, adaptive, max_n, stop_reason)
+        res = self._result(tallies, requested, adaptive, max_n, stop_reason)
+        if light is not None:
+            res.heatmap_xy, res.heatmap_zy, res.light_transport_diagnostics = self._light_results(
+                light, ray_id_start, res.n_rays)
+        return res
+
+    # ---- light-history diagnostics and heat maps (simulate's light_transport_config / heatmap_size,
+    # CLARITAS.py:7229-7300 and :9453-9580) ------------------------------------------------------------
+    def _light_setup(self, light_transport_config, heatmap_size):
+        vis = int(heatmap_size)
+        if vis < 0:
+            raise ValueError("heatmap_size must be >= 0")
+        ldc = dict(light_transport_config or {})
+        enabled = bool(ldc.get("enabled", False))
+        if not enabled and vis == 0:
+            prev = getattr(self._ctx, "_light", None) if self._ctx is not None else None
+            if prev is not None and (prev.enabled or prev.heatmap_size):
+                self._ctx.set_light()
+            return None
+        max_rays = int(ldc.get("max_rays", 0)) if enabled else 0
+        nx, ny, nz = ((int(ldc.get("nx", 1)), int(ldc.get("ny", 1)), int(ldc.get("nz", 1))) if enabled
+                      else (1, 1, 1))
+        rep = min(int(ldc.get("representative_rays", 0)), max_rays) if enabled else 0
+        max_seg = int(ldc.get("max_segments_per_ray", 0)) if enabled else 0
+        if enabled:
+            if max_rays < 1:
+                raise ValueError("light diagnostic max_rays must be >=1")
+            if min(nx, ny, nz) < 4:
+                raise ValueError("light diagnostic grid dimensions must each be >=4")
+            if rep < 0 or max_seg < 1:
+                raise ValueError("invalid representative-ray diagnostic configuration")
+        cfg = self.config
+        vg = S.vortex_surface_geometry(cfg.free_surface_model, cfg.zmean, cfg.tube_inner_radius_m,
+                                       cfg.vortex_wall_center_height_difference_m, cfg.vortex_core_radius_m,
+                                       cfg.gravity_m_s2)
+        zmax = max(float(vg["center_z"]), float(vg["wall_z"])) if enabled else cfg.zmean
+        voxels = nx * ny * nz if enabled else 1
+        nbytes = voxels * 20 + max(rep * max_seg, 1) * 32 + max(rep, 1) * 8 + 8
+        if enabled and nbytes > 1_000_000_000:
+            raise ValueError(f"light diagnostic allocation is too large ({nbytes / 1e9:.3g} GB); reduce grid "
+                             "dimensions, representative rays, or segments per ray")
+        self._context().set_light(enabled, nx, ny, nz, max_rays, rep, max_seg, vis, zmax, float(vg["wall_z"]))
+        return {"enabled": enabled, "vis": vis, "nx": nx, "ny": ny, "nz": nz, "max_rays": max_rays, "rep": rep,
+                "max_seg": max_seg, "zmax": zmax, "bytes": nbytes, "t0": __import__("time").perf_counter()}
+
+    def _light_results(self, light, ray_id_start: int, total_rays: int):
+        import time
+        a = self._context().read_light()
+        hm = (a["heatmap_xy"], a["heatmap_zy"]) if light["vis"] > 0 else (None, None)
+        if not light["enabled"]:
+            return hm[0], hm[1], None
+        cfg = self.config
+        total, post, ew = a["track_length"], a["post_scatter_track_length"], a["scatter_event_weight"]
+        ec = a["scatter_event_count"]
+        seg, dep = float(a["segment_length_total"]), float(a["deposited_length_total"])
+        ev_grid = int(np.sum(ec, dtype=np.uint64))
+        outside = None
+        if a["first_outside_set"]:
+            x, y, z, tol = a["first_outside_xyz_tol"]
+            outside = {"global_ray_id": int(a["first_outside_ray"]), "x_m": float(x), "y_m": float(y), "z_m": float(z),
+                       "coordinate_tolerance_m": float(tol),
+                       "x_bounds_m": [-cfg.tube_inner_radius_m, cfg.tube_inner_radius_m],
+                       "y_bounds_m": [-cfg.tube_inner_radius_m, cfg.tube_inner_radius_m],
+                       "z_bounds_m": [cfg.zmin, light["zmax"]]}
+        zeros = np.zeros_like(ec)
+        diag = {
+            "track_length_m": total, "post_scatter_track_length_m": post,
+            "absorption_event_count": zeros, "absorption_event_total": 0, "deposited_absorption_event_total": 0,
+            "absorption_event_closure_error": 0,
+            "absorption_grid_basis": "accepted extinction encounter site; not recorded by this library",
+            "scatter_event_weight": ew, "scatter_event_count": ec,
+            "nx": light["nx"], "ny": light["ny"], "nz": light["nz"],
+            "x_min_m": -cfg.tube_inner_radius_m, "x_max_m": cfg.tube_inner_radius_m,
+            "y_min_m": -cfg.tube_inner_radius_m, "y_max_m": cfg.tube_inner_radius_m,
+            "z_min_m": cfg.zmin, "z_max_m": light["zmax"],
+            "diagnostic_ray_limit": light["max_rays"],
+            "diagnostic_rays_processed": max(0, min(total_rays, light["max_rays"] - ray_id_start)),
+            "representative_ray_limit": light["rep"], "max_segments_per_ray": light["max_seg"],
+            "segment_count": int(a["segment_count"]), "scatter_event_total": int(a["scatter_event_total"]),
+            "deposited_scatter_event_total": ev_grid,
+            "scatter_event_closure_error": ev_grid - int(a["scatter_event_total"]),
+            "error_count": int(a["error_count"]), "hard_error_count": int(a["error_count"]),
+            "boundary_adjustment_count": int(a["boundary_adjustment_count"]),
+            "event_outside_count": int(a["event_outside_count"]), "first_outside_event": outside,
+            "nonfinite_count": sum(int(np.count_nonzero(~np.isfinite(v))) for v in (total, post, ew)),
+            "negative_value_count": sum(int(np.count_nonzero(v < 0)) for v in (total, post, ew)),
+            "diagnostic_memory_bytes": int(light["bytes"]),
+            "diagnostic_active_wall_time_s": float(time.perf_counter() - light["t0"]),
+            "segment_length_total_m": seg, "deposited_length_total_m": dep,
+            "deposition_closure_relative_error": abs(dep - seg) / max(abs(seg), 1e-30),
+            "grid_closure_relative_error": abs(float(np.sum(total, dtype=np.float64)) - seg) / max(abs(seg), 1e-30),
+            "trajectory_count": a["trajectory_count"], "trajectory_overflow": a["trajectory_overflow"],
+        }
+        for k in ("x0", "y0", "z0", "x1", "y1", "z1"):
+            diag[f"trajectory_{k}_m"] = a["trajectory_" + k]
+        diag["trajectory_particle_order"] = a["trajectory_order"]
+        return hm[0], hm[1], diag
 
     # ---- result assembly (formulas of CLARITAS.py:8882-8966 and :9600-9890) --------------------
     def _batch_scores(self, t):

@@ -72,6 +72,8 @@ def load(build_if_missing: bool = False):
                                     C.c_int64, C.c_void_p], C.c_int),
             "clr_read_sediment_field": ([C.c_void_p, C.c_void_p, P(C.c_int32), P(C.c_int32), P(C.c_int32),
                                          P(C.c_double)], C.c_int),
+            "clr_set_light_diagnostics": ([C.c_void_p, P(abi.LightConfig)], C.c_int),
+            "clr_read_light_diagnostics": ([C.c_void_p, P(abi.LightResult)], C.c_int),
         }
         for name, (argt, rest) in sig.items():
             f = getattr(lib, name)
@@ -87,7 +89,8 @@ def exported_symbols() -> list[str]:
             "clr_last_kernel_ms", "clr_last_launches", "clr_calibrate", "clr_mie_phase_noalloc", "clr_sweep_build",
             "clr_sweep_trace", "clr_sweep_read_particle_physics", "clr_mlp_create", "clr_mlp_destroy",
             "clr_mlp_last_error", "clr_mlp_set_params", "clr_mlp_get_params", "clr_mlp_forward", "clr_mlp_gradients",
-            "clr_mlp_train", "clr_mlp_last_ms", "clr_bf16_gemm_n256", "clr_read_sediment_field"]
+            "clr_mlp_train", "clr_mlp_last_ms", "clr_bf16_gemm_n256", "clr_read_sediment_field",
+            "clr_set_light_diagnostics", "clr_read_light_diagnostics"]
 
 
 class Context:
@@ -132,6 +135,43 @@ class Context:
                     "clr_read_sediment_field")
         return {"grid": g, "nr": int(nr.value), "nz": int(nz.value), "iterations": int(it.value),
                 "max_residual": float(res.value)}
+
+    def set_light(self, enabled: bool = False, nx: int = 1, ny: int = 1, nz: int = 1, max_rays: int = 0,
+                  representative_rays: int = 0, max_segments_per_ray: int = 0, heatmap_size: int = 0,
+                  zmax: float = 0.0, heat_zmax: float = 0.0):
+        """Light-history diagnostics (voxel track lengths, event sites, trajectories) and heat maps of the
+        following traces; all off by default."""
+        c = abi.LightConfig(int(bool(enabled)), int(nx), int(ny), int(nz), int(max_rays), int(representative_rays),
+                            int(max_segments_per_ray), int(heatmap_size), float(zmax), float(heat_zmax))
+        self._check(self.lib.clr_set_light_diagnostics(self.h, C.byref(c)), "clr_set_light_diagnostics")
+        self._light = c
+
+    def read_light(self) -> dict:
+        import numpy as np
+        c = self._light
+        vox = (c.nz, c.ny, c.nx) if c.enabled else (0, 0, 0)
+        rep = min(c.representative_rays, c.max_rays) if c.enabled else 0
+        seg = c.max_segments_per_ray if c.enabled else 0
+        vis = c.heatmap_size
+        a = {"track_length": np.zeros(vox, np.float32), "post_scatter_track_length": np.zeros(vox, np.float32),
+             "scatter_event_weight": np.zeros(vox, np.float32), "scatter_event_count": np.zeros(vox, np.uint32),
+             "heatmap_xy": np.zeros((vis, vis), np.float32), "heatmap_zy": np.zeros((vis, vis), np.float32)}
+        for k in ("x0", "y0", "z0", "x1", "y1", "z1"):
+            a["trajectory_" + k] = np.zeros((rep, seg), np.float32)
+        a["trajectory_order"] = np.zeros((rep, seg), np.int32)
+        a["trajectory_count"] = np.zeros(rep, np.int32)
+        a["trajectory_overflow"] = np.zeros(rep, np.int32)
+        r = abi.LightResult()
+        for name, arr in a.items():
+            if arr.size:
+                setattr(r, name, arr.ctypes.data_as(C.POINTER(np.ctypeslib.as_ctypes_type(arr.dtype))))
+        self._check(self.lib.clr_read_light_diagnostics(self.h, C.byref(r)), "clr_read_light_diagnostics")
+        for k in ("segment_length_total", "deposited_length_total", "segment_count", "scatter_event_total",
+                  "error_count", "boundary_adjustment_count", "event_outside_count", "first_outside_ray",
+                  "first_outside_set"):
+            a[k] = getattr(r, k)
+        a["first_outside_xyz_tol"] = list(r.first_outside_xyz_tol)
+        return a
 
     def trace(self, run: abi.RunParams, records: bool = False):
         import numpy as np

@@ -43,10 +43,16 @@ def test_model_takes_reference_keywords_and_validates():
 def test_unsupported_features_raise_explicitly():
     m = F.ClaritasForwardModel()
     parts = S.quartz_particles(100.0, n_bins=4)
-    with pytest.raises(NotImplementedError):
-        m.simulate(parts, 0.1, n_rays=10, light_transport_config={})
-    with pytest.raises(NotImplementedError):
-        m.simulate(parts, 0.1, n_rays=10, heatmap_size=8)
+    # light diagnostics are validated with the reference's rules before anything reaches the device
+    with pytest.raises(ValueError, match="max_rays must be >=1"):
+        m.simulate(parts, 0.1, n_rays=10, light_transport_config={"enabled": True, "nx": 8, "ny": 8, "nz": 8})
+    with pytest.raises(ValueError, match="grid dimensions"):
+        m.simulate(parts, 0.1, n_rays=10, light_transport_config={"enabled": True, "max_rays": 5, "nx": 3})
+    with pytest.raises(ValueError, match="representative-ray"):
+        m.simulate(parts, 0.1, n_rays=10, light_transport_config={"enabled": True, "max_rays": 5, "nx": 4, "ny": 4,
+                                                                 "nz": 4})
+    with pytest.raises(ValueError, match="heatmap_size"):
+        m.simulate(parts, 0.1, n_rays=10, heatmap_size=-1)
     with pytest.raises(NotImplementedError):
         m.simulate(parts, 0.1, n_rays=10, collect_rays=True)
     with pytest.raises(NotImplementedError, match="named PSD tables"):
