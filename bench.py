@@ -213,11 +213,14 @@ def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> di
     train = G.make_dataset(ctx, args.sur_train, args.sur_photons, sampler_seed=1000 + rank, seed_base=0)
     test = G.make_dataset(ctx, args.sur_test, 100 * args.sur_photons, sampler_seed=2000 + rank, seed_base=10 ** 6)
     data_s = time.perf_counter() - t0
-    ctx.close()
     model = G.Surrogate(local_rank, max_batch=65536, seed=rank)
     hist = model.fit(train, epochs=args.sur_epochs, batch=2048)
     err = G.judge(model, test)
     base = G.linear_baseline(train, test)
+    # surrogate-in-the-loop inversion of concentration (Monte Carlo as judge and fallback)
+    inv = G.inversion_study(ctx, model, n=args.inv_scenarios, photons=4_000_000, mc_only=args.inv_mc_only,
+                            sampler_seed=3000 + rank) if args.inv_scenarios > 0 else None
+    ctx.close()
     batch = 65536
     x = torch.randn(batch, 6, generator=torch.Generator().manual_seed(1)).to(dev)
     for _ in range(args.warmup):
@@ -269,7 +272,8 @@ def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> di
                           "mc": {"data_seconds_wall": data_s, "train_labels_device_s_per_scenario": mc_s_per_scen,
                                  "judge_device_s_per_scenario": mc_s_judge},
                           "speedup_vs_mc_at_training_photons": (value / world) * mc_s_per_scen,
-                          "speedup_vs_mc_at_judge_photons": (value / world) * mc_s_judge}}
+                          "speedup_vs_mc_at_judge_photons": (value / world) * mc_s_judge,
+                          "inversion": inv}}
     model.close()
     return line
 
@@ -424,6 +428,8 @@ def main():
     ap.add_argument("--sur-test", type=int, default=256, help="surrogate: judged held-out scenarios")
     ap.add_argument("--sur-photons", type=int, default=1_000_000, help="surrogate: photons per training scenario")
     ap.add_argument("--sur-epochs", type=int, default=400, help="surrogate: training epochs")
+    ap.add_argument("--inv-scenarios", type=int, default=1024, help="surrogate: scenarios of the inversion study")
+    ap.add_argument("--inv-mc-only", type=int, default=64, help="surrogate: of those, also inverted by MC alone")
     ap.add_argument("--rng", choices=["philox", "xorshift"], default="philox")
     ap.add_argument("--photons", type=int, default=0, help="override photons per step")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")

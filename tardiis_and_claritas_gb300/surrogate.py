@@ -206,3 +206,137 @@ def query_speed(model: Surrogate, batch: int = 65536, reps: int = 20) -> dict:
     e2e = (time.perf_counter() - t0) / reps
     dev = float(np.median(ms)) * 1e-3
     return {"batch": batch, "device_s_per_batch": dev, "queries_per_s": batch / dev, "e2e_queries_per_s": batch / e2e}
+
+
+# ---------------- surrogate-in-the-loop inversion (Monte Carlo as judge and fallback) ----------------
+def with_concentration(sc: S.SweepScenario, conc_mg_l: float) -> S.SweepScenario:
+    """The scenario with another concentration (everything else, photons and seed included, unchanged)."""
+    import dataclasses
+    parts = dataclasses.replace(sc.particles, concentration_kg_m3=float(conc_mg_l) * 1e-3)
+    params = dict(sc.params, concentration_mg_l=float(conc_mg_l))
+    return dataclasses.replace(sc, particles=parts, params=params)
+
+
+def _features_at(x: np.ndarray, log_c: np.ndarray) -> np.ndarray:
+    """Feature rows with the concentration replaced: log10 C and the optical depth (proportional to C)."""
+    out = x.copy()
+    out[..., 5] = x[..., 5] + (log_c - x[..., 0])
+    out[..., 0] = log_c
+    return out
+
+
+def surrogate_invert(model: Surrogate, x_known: np.ndarray, observed: np.ndarray, channels=(1,), lo: float = 0.0,
+                     hi: float = 4.0, grid: int = 401) -> np.ndarray:
+    """log10 concentration per scenario minimising the squared log-signal mismatch of the network over a grid
+    of candidates (one inference call for all scenarios), refined by a parabola through the best three."""
+    n = x_known.shape[0]
+    cand = np.linspace(lo, hi, grid)
+    xs = _features_at(np.repeat(x_known[:, None, :], grid, axis=1), np.broadcast_to(cand, (n, grid)))
+    pred = model.predict(xs.reshape(n * grid, 6)).reshape(n, grid, 3)
+    ch = list(channels)
+    err = np.sum((pred[:, :, ch] - observed[:, None, ch]) ** 2, axis=-1)
+    k = np.clip(np.argmin(err, axis=1), 1, grid - 2)
+    e0, e1, e2 = err[np.arange(n), k - 1], err[np.arange(n), k], err[np.arange(n), k + 1]
+    den = e0 - 2.0 * e1 + e2
+    step = np.where(den > 0, 0.5 * (e0 - e2) / np.where(den > 0, den, 1.0), 0.0)
+    return cand[k] + np.clip(step, -1.0, 1.0) * (cand[1] - cand[0])
+
+
+def mc_signals(ctx: L.Context, scs: list, seed_base: int) -> np.ndarray:
+    return monte_carlo(ctx, scs, seed_base=seed_base).y
+
+
+def mc_secant_invert(ctx: L.Context, scs: list, observed: np.ndarray, start: np.ndarray, channel: int = 1,
+                     tol: float = 0.005, max_iter: int = 8, seed_base: int = 5 * 10 ** 6, step: float = 0.1):
+    """Monte Carlo inversion of log10 concentration for one signal: secant iterations in log C, every
+    iteration one Monte Carlo run of all unfinished scenarios. Stops per scenario when the signal agrees
+    within `tol` (relative). Returns (log10 C, Monte Carlo evaluations per scenario)."""
+    n = len(scs)
+    x0 = np.asarray(start, dtype=float).copy()
+    f0 = mc_signals(ctx, [with_concentration(s, 10 ** c) for s, c in zip(scs, x0)], seed_base)[:, channel] \
+        - observed[:, channel]
+    evals = np.ones(n, dtype=int)
+    done = np.abs(10 ** f0 - 1.0) <= tol
+    # more particles lower the transmitted signal: step toward the observation
+    x1 = x0 + np.where(f0 < 0, -step, step) if channel == 1 else x0 + step
+    x = x0.copy()
+    xa, fa = x0.copy(), f0.copy()
+    xb = x1.copy()
+    for it in range(max_iter):
+        idx = np.nonzero(~done)[0]
+        if idx.size == 0:
+            break
+        fb_part = mc_signals(ctx, [with_concentration(scs[i], 10 ** xb[i]) for i in idx],
+                             seed_base + 100_000 * (it + 1))[:, channel] - observed[idx, channel]
+        evals[idx] += 1
+        fb = np.zeros(n)
+        fb[idx] = fb_part
+        for j, i in enumerate(idx):
+            x[i] = xb[i]
+            if abs(10 ** fb[i] - 1.0) <= tol:
+                done[i] = True
+                continue
+            den = fb[i] - fa[i]
+            nxt = xb[i] - fb[i] * (xb[i] - xa[i]) / den if abs(den) > 1e-12 else xb[i] + step
+            xa[i], fa[i] = xb[i], fb[i]
+            xb[i] = float(np.clip(nxt, -1.0, 5.0))
+    return x, evals
+
+
+def inversion_study(ctx: L.Context, model: Surrogate, n: int = 1024, photons: int = 4_000_000, tol: float = 0.01,
+                    sampler_seed: int = 3000, mc_only: int = 0, min_tau: float = 0.1) -> dict:
+    """Recover the concentration of n sweep scenarios from their transmitted signal (observed by Monte
+    Carlo at the true concentration): the surrogate proposes, the Monte Carlo at the proposal judges it,
+    and scenarios whose surrogate signal is off by more than `tol` fall back to Monte Carlo secant
+    iterations from the surrogate's proposal. The first `mc_only` scenarios are also inverted by Monte
+    Carlo alone from a mid-range start, for the cost of the method without the network."""
+    import time
+    # The transmitted signal carries the concentration only where the cell is not optically thin: scenarios
+    # are drawn from the sweep sampler and kept when their geometric optical depth is at least min_tau.
+    pool = S.sweep_workload(8 * n, sampler_seed=sampler_seed, photons=(photons, photons))
+    scs = [sc for sc in pool if optical_depth(sc) >= min_tau][:n]
+    n = len(scs)
+    true_log_c = np.log10([sc.params["concentration_mg_l"] for sc in scs])
+    t0 = time.perf_counter()
+    obs = monte_carlo(ctx, scs, seed_base=7 * 10 ** 6)
+    t_obs = time.perf_counter() - t0
+    x = features(scs)
+    t0 = time.perf_counter()
+    est = surrogate_invert(model, x, obs.y)
+    t_sur = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    proposals = [with_concentration(s, 10 ** c) for s, c in zip(scs, est)]
+    judge_mc = monte_carlo(ctx, proposals, seed_base=8 * 10 ** 6)
+    pred = model.predict(features(proposals))
+    t_judge = time.perf_counter() - t0
+    sur_err = np.abs(10 ** (pred[:, 1] - judge_mc.y[:, 1]) - 1.0)
+    bad = np.nonzero(sur_err > tol)[0]
+    final = est.copy()
+    fb_evals = np.zeros(n, dtype=int)
+    t0 = time.perf_counter()
+    if bad.size:
+        xb, ev = mc_secant_invert(ctx, [scs[i] for i in bad], obs.y[bad], est[bad], tol=0.5 * tol)
+        final[bad] = xb
+        fb_evals[bad] = ev
+    t_fb = time.perf_counter() - t0
+    rel_c = np.abs(10 ** (final - true_log_c) - 1.0)
+    out = {"scenarios": n, "photons": photons, "tolerance": tol, "min_optical_depth": min_tau,
+           "fallback_fraction": float(bad.size / n),
+           "surrogate_signal_error_median": float(np.median(sur_err)),
+           "concentration_rel_error_median": float(np.median(rel_c)),
+           "concentration_rel_error_p90": float(np.quantile(rel_c, 0.9)),
+           "mc_evaluations_per_scenario": float(1.0 + fb_evals.mean()),
+           "seconds": {"observations_mc": t_obs, "surrogate_search": t_sur, "judge_mc": t_judge,
+                       "fallback_mc": t_fb}}
+    if mc_only > 0:
+        m = min(mc_only, n)
+        t0 = time.perf_counter()
+        xm, ev = mc_secant_invert(ctx, scs[:m], obs.y[:m], np.full(m, 2.0), tol=0.5 * tol, max_iter=12)
+        t_mc = time.perf_counter() - t0
+        rel_m = np.abs(10 ** (xm - true_log_c[:m]) - 1.0)
+        out["mc_only"] = {"scenarios": m, "mc_evaluations_per_scenario": float(ev.mean()),
+                          "concentration_rel_error_median": float(np.median(rel_m)), "seconds": t_mc,
+                          "seconds_per_scenario": t_mc / m}
+        per_sur = (t_sur + t_judge + t_fb) / n
+        out["speedup_per_scenario_vs_mc_only"] = (t_mc / m) / per_sur if per_sur > 0 else None
+    return out

@@ -127,3 +127,20 @@ def test_surrogate_of_monte_carlo_beats_the_method_without_it(torch_cuda):
     speed = G.query_speed(model, batch=4096, reps=5)
     assert speed["queries_per_s"] > 1e3 * len(test.x) / test.mc_seconds
     model.close()
+
+
+def test_surrogate_in_the_loop_inversion(torch_cuda):
+    """Concentrations recovered from transmitted signals: the network proposes, the Monte Carlo judges and
+    takes over where the network is off by more than 1 %; the result is as accurate as a Monte Carlo-only
+    inversion and needs far fewer Monte Carlo runs."""
+    from tardiis_and_claritas_gb300 import lib as L, surrogate as G
+    ctx = L.Context(0)
+    train = G.make_dataset(ctx, 4096, 1_000_000, sampler_seed=41)
+    model = G.Surrogate(0, max_batch=8192, seed=1)
+    model.fit(train, epochs=300, batch=2048)
+    out = G.inversion_study(ctx, model, n=48, photons=2_000_000, mc_only=16, sampler_seed=43)
+    ctx.close()
+    model.close()
+    assert out["scenarios"] == 48
+    assert out["concentration_rel_error_median"] < 0.05, out
+    assert out["mc_evaluations_per_scenario"] < out["mc_only"]["mc_evaluations_per_scenario"], out
