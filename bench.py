@@ -203,7 +203,7 @@ def run_sweep(args, ctx, rank: int, world: int, local_rank: int, dist, dev) -> d
 
 def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> dict:
     """Surrogate workload: Monte Carlo training data from the batched sweep, training of the tensor-core
-    network, judgement against Monte Carlo with 100x the photons, then timed inference (a step = one
+    network, check against Monte Carlo with 100x the photons, then timed inference (a step = one
     batch of 65536 queries)."""
     import numpy as np
     import torch
@@ -215,9 +215,9 @@ def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> di
     data_s = time.perf_counter() - t0
     model = G.Surrogate(local_rank, max_batch=65536, seed=rank)
     hist = model.fit(train, epochs=args.sur_epochs, batch=2048)
-    err = G.judge(model, test)
+    err = G.mc_error(model, test)
     base = G.linear_baseline(train, test)
-    # surrogate-in-the-loop inversion of concentration (Monte Carlo as judge and fallback)
+    # surrogate-in-the-loop inversion of concentration (Monte Carlo as check and fallback)
     inv = G.inversion_study(ctx, model, n=args.inv_scenarios, photons=4_000_000, mc_only=args.inv_mc_only,
                             sampler_seed=3000 + rank) if args.inv_scenarios > 0 else None
     ctx.close()
@@ -248,14 +248,14 @@ def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> di
     peak = peaks.get("bf16_tflops") or 1900.0
     ach = flop_q * value / world / 1e12
     mc_s_per_scen = train.mc_seconds / len(train.x)
-    mc_s_judge = test.mc_seconds / len(test.x)
-    line = {"metric": "surrogate queries/s (error vs Monte Carlo judge stated)", "value": value,
+    mc_s_check = test.mc_seconds / len(test.x)
+    line = {"metric": "surrogate queries/s (error vs Monte Carlo stated)", "value": value,
             "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16 weights/activations, f32 accumulation", "data": "synthetic (seeded); labels from this MC",
             "config": {"workload": "surrogate MLP 6-256x4(SiLU)-3 of the sweep's detector signals (channels 9, 0, 17); "
                                    f"trained on {args.sur_train} sweep scenarios at {args.sur_photons:.0e} photons, "
-                                   f"judged on {args.sur_test} held-out scenarios at {100 * args.sur_photons:.0e} "
+                                   f"checked on {args.sur_test} held-out scenarios at {100 * args.sur_photons:.0e} "
                                    "photons; inference batch 65536",
                        "inference_batch": batch, "l2": "inputs resident (3 MB); weights L2-resident by design"},
             "e2e": {"value": speed["e2e_queries_per_s"] * world, "unit": "queries/s",
@@ -264,15 +264,15 @@ def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> di
             "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                          "peak_source": "bf16_tflops of MEASURED_PEAKS.json" if peaks.get("bf16_tflops") else "fallback",
                          "traffic": None, "flop_per_query": flop_q},
-            "surrogate": {"judge": err, "linear_baseline": base,
+            "surrogate": {"vs_mc": err, "linear_baseline": base,
                           "train": {"scenarios": len(train.x), "photons_each": args.sur_photons,
                                     "epochs": args.sur_epochs, "final_loss": hist[-1][2],
                                     "train_seconds": model.train_seconds,
                                     "ms_per_epoch": float(np.median([h[3] for h in hist]))},
                           "mc": {"data_seconds_wall": data_s, "train_labels_device_s_per_scenario": mc_s_per_scen,
-                                 "judge_device_s_per_scenario": mc_s_judge},
+                                 "check_device_s_per_scenario": mc_s_check},
                           "speedup_vs_mc_at_training_photons": (value / world) * mc_s_per_scen,
-                          "speedup_vs_mc_at_judge_photons": (value / world) * mc_s_judge,
+                          "speedup_vs_mc_at_check_photons": (value / world) * mc_s_check,
                           "inversion": inv}}
     model.close()
     return line
@@ -372,7 +372,7 @@ def run_reference_arm(args, rank: int, world: int):
         scs = S.sweep_workload(SWEEP_SCENARIOS, sampler_seed=2000, photons=(p, p))
         vals = [sweep_cpu_estimate(scs, threads, args.cpu_seconds) for _ in range(max(1, args.steps))]
         value = sum(v["value"] for v in vals) / len(vals)
-        line = {"impl": "reference", "metric": "surrogate queries/s (error vs Monte Carlo judge stated)",
+        line = {"impl": "reference", "metric": "surrogate queries/s (error vs Monte Carlo stated)",
                 "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32/f64", "data": "synthetic (seeded)",
@@ -425,7 +425,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["full", "small", "sweep", "surrogate"], default="full")
     ap.add_argument("--sur-train", type=int, default=16384, help="surrogate: training scenarios")
-    ap.add_argument("--sur-test", type=int, default=256, help="surrogate: judged held-out scenarios")
+    ap.add_argument("--sur-test", type=int, default=256, help="surrogate: held-out scenarios checked by Monte Carlo")
     ap.add_argument("--sur-photons", type=int, default=1_000_000, help="surrogate: photons per training scenario")
     ap.add_argument("--sur-epochs", type=int, default=400, help="surrogate: training epochs")
     ap.add_argument("--inv-scenarios", type=int, default=1024, help="surrogate: scenarios of the inversion study")

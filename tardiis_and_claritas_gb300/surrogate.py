@@ -1,9 +1,10 @@
-"""Surrogate of the detector signals, trained on batched Monte Carlo and judged by it.
+"""Surrogate of the detector signals, trained on batched Monte Carlo and checked against it.
 
 The reference answers every scenario query with a full Monte Carlo run (ClaritasForwardModel.simulate,
 CLARITAS/CLARITAS.py:7160). Here a small network (libclaritas_gb.so's clr_mlp: 6 -> 256 x4 SiLU -> 3, BF16
 tensor-core training and inference) maps the scenario parameters of the batched sweep to three detector
-signals, and the Monte Carlo stays both its training-data source and the judge of its error:
+signals, and the Monte Carlo stays both its training-data source and the reference its error is measured
+against:
 
   inputs  (6): log10 concentration [mg/L], log10 median diameter [um], sigma_g, stirrer rpm / 1000,
                particle refractive index, log10 geometric optical depth (radius x 3 C Q / (2 rho d_32),
@@ -151,26 +152,26 @@ class Surrogate:
         self.net.close()
 
 
-def judge(model: Surrogate, data: Dataset, min_hits: float = 2500.0) -> dict:
-    """Relative error of the surrogate's signals against Monte Carlo labels (the judge), per channel, over
-    scenarios whose judge count is at least `min_hits` (relative standard error <= 1/sqrt(min_hits): 2 % at
-    the default; the 90-degree aperture sees ~5e-5 of the photons, so 1e8 judge photons give ~5e3 counts)."""
+def mc_error(model: Surrogate, data: Dataset, min_hits: float = 2500.0) -> dict:
+    """Relative error of the surrogate's signals against Monte Carlo labels (the reference), per channel, over
+    scenarios whose Monte Carlo count is at least `min_hits` (relative standard error <= 1/sqrt(min_hits): 2 % at
+    the default; the 90-degree aperture sees ~5e-5 of the photons, so 1e8 reference photons give ~5e3 counts)."""
     pred = model.predict(data.x)
     out = {}
     for k, name in enumerate(SIGNAL_NAMES):
         ok = data.hits[:, k] >= min_hits
         rel = np.abs(10.0 ** (pred[ok, k] - data.y[ok, k]) - 1.0)
-        judge_se = 1.0 / np.sqrt(np.maximum(data.hits[ok, k], 1.0))
+        mc_se = 1.0 / np.sqrt(np.maximum(data.hits[ok, k], 1.0))
         out[name] = {"scenarios": int(ok.sum()), "median_rel_error": float(np.median(rel)) if ok.any() else None,
                      "p90_rel_error": float(np.quantile(rel, 0.9)) if ok.any() else None,
                      "within_1pct": float(np.mean(rel <= 0.01)) if ok.any() else None,
-                     "judge_median_rel_se": float(np.median(judge_se)) if ok.any() else None}
+                     "mc_median_rel_se": float(np.median(mc_se)) if ok.any() else None}
     return out
 
 
 def linear_baseline(train: Dataset, test: Dataset, min_hits: float = 2500.0) -> dict:
     """The method without the network: least squares on the same six features (plus their squares and a
-    constant), same judge and error measure."""
+    constant), same Monte Carlo reference and error measure."""
     def design(x):
         return np.hstack([np.ones((x.shape[0], 1)), x, x * x])
     coef, *_ = np.linalg.lstsq(design(train.x), train.y, rcond=None)
@@ -208,7 +209,7 @@ def query_speed(model: Surrogate, batch: int = 65536, reps: int = 20) -> dict:
     return {"batch": batch, "device_s_per_batch": dev, "queries_per_s": batch / dev, "e2e_queries_per_s": batch / e2e}
 
 
-# ---------------- surrogate-in-the-loop inversion (Monte Carlo as judge and fallback) ----------------
+# ---------------- surrogate-in-the-loop inversion (Monte Carlo as check and fallback) ----------------
 def with_concentration(sc: S.SweepScenario, conc_mg_l: float) -> S.SweepScenario:
     """The scenario with another concentration (everything else, photons and seed included, unchanged)."""
     import dataclasses
@@ -286,7 +287,7 @@ def mc_secant_invert(ctx: L.Context, scs: list, observed: np.ndarray, start: np.
 def inversion_study(ctx: L.Context, model: Surrogate, n: int = 1024, photons: int = 4_000_000, tol: float = 0.01,
                     sampler_seed: int = 3000, mc_only: int = 0, min_tau: float = 0.1) -> dict:
     """Recover the concentration of n sweep scenarios from their transmitted signal (observed by Monte
-    Carlo at the true concentration): the surrogate proposes, the Monte Carlo at the proposal judges it,
+    Carlo at the true concentration): the surrogate proposes, the Monte Carlo at the proposal checks it,
     and scenarios whose surrogate signal is off by more than `tol` fall back to Monte Carlo secant
     iterations from the surrogate's proposal. The first `mc_only` scenarios are also inverted by Monte
     Carlo alone from a mid-range start, for the cost of the method without the network."""
@@ -306,10 +307,10 @@ def inversion_study(ctx: L.Context, model: Surrogate, n: int = 1024, photons: in
     t_sur = time.perf_counter() - t0
     t0 = time.perf_counter()
     proposals = [with_concentration(s, 10 ** c) for s, c in zip(scs, est)]
-    judge_mc = monte_carlo(ctx, proposals, seed_base=8 * 10 ** 6)
+    check_mc = monte_carlo(ctx, proposals, seed_base=8 * 10 ** 6)
     pred = model.predict(features(proposals))
-    t_judge = time.perf_counter() - t0
-    sur_err = np.abs(10 ** (pred[:, 1] - judge_mc.y[:, 1]) - 1.0)
+    t_check = time.perf_counter() - t0
+    sur_err = np.abs(10 ** (pred[:, 1] - check_mc.y[:, 1]) - 1.0)
     bad = np.nonzero(sur_err > tol)[0]
     final = est.copy()
     fb_evals = np.zeros(n, dtype=int)
@@ -326,7 +327,7 @@ def inversion_study(ctx: L.Context, model: Surrogate, n: int = 1024, photons: in
            "concentration_rel_error_median": float(np.median(rel_c)),
            "concentration_rel_error_p90": float(np.quantile(rel_c, 0.9)),
            "mc_evaluations_per_scenario": float(1.0 + fb_evals.mean()),
-           "seconds": {"observations_mc": t_obs, "surrogate_search": t_sur, "judge_mc": t_judge,
+           "seconds": {"observations_mc": t_obs, "surrogate_search": t_sur, "check_mc": t_check,
                        "fallback_mc": t_fb}}
     if mc_only > 0:
         m = min(mc_only, n)
@@ -337,6 +338,6 @@ def inversion_study(ctx: L.Context, model: Surrogate, n: int = 1024, photons: in
         out["mc_only"] = {"scenarios": m, "mc_evaluations_per_scenario": float(ev.mean()),
                           "concentration_rel_error_median": float(np.median(rel_m)), "seconds": t_mc,
                           "seconds_per_scenario": t_mc / m}
-        per_sur = (t_sur + t_judge + t_fb) / n
+        per_sur = (t_sur + t_check + t_fb) / n
         out["speedup_per_scenario_vs_mc_only"] = (t_mc / m) / per_sur if per_sur > 0 else None
     return out

@@ -3,7 +3,7 @@
 Run on a machine with a GB300 (sm_103a) after oracle/ref_extract.py has written
 oracle/_ref/claritas_cuda_src.inc from the reference checkout:
 
-    python tests/golden/make_gpu_fixtures.py --out gpurun_out/gpu_ref_fixtures.npz
+    python tests/golden/make_gpu_fixtures.py --out tests/golden/gpu_ref_fixtures.npz
 
 It compiles oracle/ref_gpu_driver.cu (the reference's CUDA_SRC plus a launcher
 that replays the reference host's launch sequence) into
@@ -108,7 +108,7 @@ def run_scene(lib, name: str, n_rays: int = N_RAYS):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out", "gpu_ref_fixtures.npz"))
+    ap.add_argument("--out", default=os.path.join(ROOT, "tests", "golden", "gpu_ref_fixtures.npz"))
     ap.add_argument("--rays", type=int, default=N_RAYS)
     a = ap.parse_args()
     lib = load()

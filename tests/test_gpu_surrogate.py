@@ -105,7 +105,7 @@ def test_training_reduces_the_loss(torch_cuda):
 
 def test_surrogate_of_monte_carlo_beats_the_method_without_it(torch_cuda):
     """Trained on batched Monte Carlo of sweep scenarios, the network predicts held-out scenarios' signals
-    (judged by Monte Carlo with 100x the photons) better than a least-squares fit on the same features,
+    (checked by Monte Carlo with 100x the photons) better than a least-squares fit on the same features,
     and answers queries far faster than the Monte Carlo."""
     from tardiis_and_claritas_gb300 import lib as L, surrogate as G
     ctx = L.Context(0)
@@ -115,8 +115,8 @@ def test_surrogate_of_monte_carlo_beats_the_method_without_it(torch_cuda):
     model = G.Surrogate(0, max_batch=4096, seed=0)
     hist = model.fit(train, epochs=300, batch=1024)
     assert hist[-1][2] < 0.2 * hist[0][2]
-    # the 90-degree aperture sees ~5e-5 of the photons: judge scenarios with >= 400 counts there (5 % error)
-    err = G.judge(model, test, min_hits=400.0)
+    # the 90-degree aperture sees ~5e-5 of the photons: check scenarios with >= 400 counts there (5 % error)
+    err = G.mc_error(model, test, min_hits=400.0)
     base = G.linear_baseline(train, test, min_hits=400.0)
     assert err["signal_transmitted"]["scenarios"] >= 100, err
     assert err["signal_transmitted"]["median_rel_error"] < 0.5 * base["signal_transmitted"]["median_rel_error"], \
@@ -130,7 +130,7 @@ def test_surrogate_of_monte_carlo_beats_the_method_without_it(torch_cuda):
 
 
 def test_surrogate_in_the_loop_inversion(torch_cuda):
-    """Concentrations recovered from transmitted signals: the network proposes, the Monte Carlo judges and
+    """Concentrations recovered from transmitted signals: the network proposes, the Monte Carlo checks and
     takes over where the network is off by more than 1 %; the result is as accurate as a Monte Carlo-only
     inversion and needs far fewer Monte Carlo runs."""
     from tardiis_and_claritas_gb300 import lib as L, surrogate as G
