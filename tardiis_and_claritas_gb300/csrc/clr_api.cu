@@ -565,6 +565,7 @@ static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* 
         w.tallies = ctx->d_tally; w.records = d_records;
         w.ray = ctx->wave_ray; w.lane = ctx->wave_lane; w.meta = ctx->wave_meta; w.qbuf = ctx->wave_q;
         w.ctl = ctx->wave_ctl; w.cap = ctx->wave_cap; w.host_live = ctx->wave_live; w.flag_event = ctx->wave_ev;
+        w.light = d_light != nullptr;
     }
     CU(cudaEventRecord(ctx->ev0, st));
     ctx->last_passes = 0;

@@ -72,8 +72,9 @@ struct WaveLaunch {
     uint32_t* qbuf;                // [CLR_WQ_COUNT][2 * cap] queue rings
     WaveCtl* ctl;
     unsigned cap;                  // slots, a power of two
-    unsigned* host_live;           // pinned host word
+    unsigned* host_live;           // pinned host words: live, tail ready, photons in flight
     cudaEvent_t flag_event;
+    bool light;                    // light-history diagnostics on: the FLIGHT stage with its hooks
 };
 
 cudaError_t wave_run_xor(const WaveLaunch& w, int num_sms, cudaStream_t st, long long max_passes, int* passes);

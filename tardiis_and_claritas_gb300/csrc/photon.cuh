@@ -577,7 +577,7 @@ __device__ void light_event(const LightDiag& L, uint32_t gid, float Rin, float z
 // Flight part. Returns WE_NONE when the iteration completed (the photon stays in the water),
 // WE_ENDED when the history ended, else the handler that completes the iteration (*ev_pidx is the
 // bin of a particle event). Position and direction are stored in r in every case.
-template <class S>
+template <class S, bool kLight = true>
 __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S* opt, unsigned long long* cstats,
                                             int* ev_pidx, uint32_t gid) {
     const clr_scene_params& P = D.P;
@@ -652,7 +652,7 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
             do_particle = freep < tbound;
             travel = do_particle ? freep : tbound;
         }
-        if (D.light) {  // the segment about to be flown (:4763-4772): heat maps for every ray, voxels for the first
+        if (kLight && D.light) {  // the segment about to be flown (:4763-4772): heat maps for every ray, voxels for the first
             const LightDiag& LD = *D.light;
             if (LD.vis > 0) light_heat_segment(LD, x, y, z, vx, vy, vz, travel, RIN, ZMIN);
             if (LD.voxels && gid < (uint32_t)LD.max_rays) light_segment(LD, gid, RIN, ZMIN, x, y, z, vx, vy, vz, travel, r.ic);
@@ -706,7 +706,8 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
                 if (uniform(st) >= pacc) { r.nulls++; break; }
             }
             r.ic++;
-            if (D.light && D.light->voxels && gid < (uint32_t)D.light->max_rays) light_event(*D.light, gid, RIN, ZMIN, x, y, z);
+            if (kLight && D.light && D.light->voxels && gid < (uint32_t)D.light->max_rays)
+                light_event(*D.light, gid, RIN, ZMIN, x, y, z);
             const float vinx = vx, viny = vy, vinz = vz;
             const int COND = (P.event_model == 4 || P.event_model == 5);
             const float COHERENT = fminf(fmaxf(D.coherent_f, 0.0f), 1.0f);

@@ -270,7 +270,9 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
 }
 
 // ---------------- generic stage kernel (ENTRY, FLIGHT and the event handlers) ----------------
-template <class Mode, int Q>
+// kLight: the water flights carry the light-diagnostic hooks (a separate FLIGHT kernel, used only when
+// the diagnostics are on, keeps them out of the production kernel).
+template <class Mode, int Q, bool kLight = true>
 __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevScene& D, Ray& r,
                                                typename Mode::Lane& L, SlotMeta& m,
                                                unsigned long long* cstats) {
@@ -279,7 +281,8 @@ __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevSce
     } else if constexpr (Q == WQ_FLIGHT) {
         for (int k = 0; k < kFlightSteps; ++k) {
             int pidx = -1;
-            const int e = water_flight(D, r, L.transport(), L.optics(), cstats, &pidx, m.gid);
+            const int e = water_flight<typename Mode::Stream, kLight>(D, r, L.transport(), L.optics(), cstats, &pidx,
+                                                                       m.gid);
             if (e == WE_NONE) continue;
             m.pidx = pidx;
             switch (e) {
@@ -342,7 +345,7 @@ __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevSce
     }
 }
 
-template <class Mode, int Q>
+template <class Mode, int Q, bool kLight = false>
 __global__ void __launch_bounds__(kWaveThreads, stage_min_blocks(Q)) wave_stage_kernel(WaveLaunch w) {
     const WaveWindow win = wave_window(w, Q);
     if (win.n == 0) return;
@@ -363,7 +366,7 @@ __global__ void __launch_bounds__(kWaveThreads, stage_min_blocks(Q)) wave_stage_
             SlotMeta m = pool.meta[slot];
             const DevScene& D = w.scenes[m.sid];
             unsigned long long* cstats = (m.sid == 0) ? bs.cs : w.tallies[m.sid].c.cstats;
-            dest = wave_stage_body<Mode, Q>(w, D, r, L, m, cstats);
+            dest = wave_stage_body<Mode, Q, kLight>(w, D, r, L, m, cstats);
             pool.ray[slot] = r;
             pool.lane[slot] = L;
             if (Q == WQ_FLIGHT || dest == WQ_ACRYL || dest == WQ_COND) pool.meta[slot] = m;
@@ -532,7 +535,8 @@ struct WavePass {
         const StageK ks[CLR_WQ_COUNT] = {
             {(const void*)wave_gen_kernel<Mode>, kSmemTally, 0},
             {(const void*)wave_stage_kernel<Mode, WQ_ENTRY>, 0, 0},
-            {(const void*)wave_stage_kernel<Mode, WQ_FLIGHT>, 0, 0},
+            {w.light ? (const void*)wave_stage_kernel<Mode, WQ_FLIGHT, true>
+                     : (const void*)wave_stage_kernel<Mode, WQ_FLIGHT, false>, 0, 0},
             {(const void*)wave_stage_kernel<Mode, WQ_COND>, 0, 1},
             {(const void*)wave_stage_kernel<Mode, WQ_GEOM>, 0, 0},
             {(const void*)wave_stage_kernel<Mode, WQ_MORPH>, 0, 1},
