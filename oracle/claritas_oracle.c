@@ -3,7 +3,8 @@
  * Plain-C restatement of the reference's hot path (file CLARITAS/CLARITAS.py):
  *   precompute  _prepare_gpu_particle_physics :6036-6965 and its kernels
  *               (PSD normalisation :3607-3635, Mie :3488-3592, rates :3845-3921,
- *               sediment :3925-4038, grid finalisation :4203-4220)
+ *               sediment :3925-4038, meridional field solver :4040-4220 driven as
+               in :6451-6725, or the finalisation :4203-4220 of a supplied grid)
  *   transport   trace_kernel :4551-5104
  *   detectors   score_detectors_kernel :4378-4436 and helpers :4237-4376
  * The physics helpers live in oracle_transport_a.h / oracle_transport_b.h.
@@ -35,6 +36,9 @@ struct clo_state {
     unsigned char* moment_mode;
     double *trace_geom, *trace_wave;
     double *sed_A, *sed_B, *sed_norm, *sed_max, *sed_radial_log, *sed_major, *sed_grid;
+    double *sed_ws, *sed_wr;        /* settling velocity [n], radial slip table [n][n_radial] */
+    int solver_iterations;          /* meridional solver: iterations done, largest residual at the last check */
+    double solver_residual;
     char err[256];
 };
 
@@ -48,7 +52,8 @@ void clo_free(clo_state* s) {
     double* arrs[] = {s->d, s->wd, s->nidx, s->kidx, s->x, s->qext, s->qsca, s->qabs, s->qback, s->g, s->albedo,
                       s->theta, s->phase_cdf, s->radius, s->nden, s->mug, s->mus, s->mue, s->muw, s->muev, s->gcdf,
                       s->wcdf, s->pcdf, s->muscal, s->moment_a, s->moment_b, s->trace_geom, s->trace_wave, s->sed_A,
-                      s->sed_B, s->sed_norm, s->sed_max, s->sed_radial_log, s->sed_major, s->sed_grid};
+                      s->sed_B, s->sed_norm, s->sed_max, s->sed_radial_log, s->sed_major, s->sed_grid,
+                      s->sed_ws, s->sed_wr};
     for (size_t i = 0; i < sizeof arrs / sizeof arrs[0]; ++i) free(arrs[i]);
     free(s->nstop);
     free(s->moment_mode);
@@ -171,6 +176,255 @@ static double schiller_naumann(double v0, double d, double rho_w, double mu, dou
     double Re = fmax(K * v, 0.0), drag = 1.0 + 0.15 * pow(Re, 0.687);
     *out_Re = Re; *out_drag = drag;
     return v;
+}
+
+/* ---------------- meridional advection-diffusion field (:4040-4215, host sequence :6451-6725) ----------------
+ * Sediment model 3 without a supplied grid: per size bin, the stationary axisymmetric advection-diffusion of
+ * the sediment in the cell's secondary circulation on a cell-centred (r, z) grid, solved by red-black SOR
+ * with mass renormalisation every 20 iterations and at every check; the solve stops at the first check
+ * (after at least min(1000, max) iterations) where the largest relative residual over all bins is within
+ * tolerance. Bins are independent between checks, so they run in parallel; every sum keeps its order. */
+typedef struct { int FSM; double R, ZMIN, ZMEAN, DH, CORE, UPEAK; } m_geom;
+
+/* free-surface height and slope at radius r (:4046-4057) */
+static void m_surface(const m_geom* g, double r, double* zs, double* hp) {
+    double rr = fmin(fmax(r, 0.0), g->R), rr2 = rr * rr, R2 = g->R * g->R;
+    *zs = g->ZMEAN; *hp = 0.0;
+    if (!(g->DH > 0.0) || g->FSM == 0) return;
+    if (g->FSM == 1) { *zs = g->ZMEAN + g->DH * (rr2 / R2 - 0.5); *hp = 2.0 * g->DH * rr / R2; return; }
+    double a2 = g->CORE * g->CORE, Hinf = g->DH * (a2 + R2) / R2;
+    double hbar = Hinf * (1.0 - (a2 / R2) * log1p(R2 / a2));
+    *zs = g->ZMEAN - hbar + Hinf * rr2 / (a2 + rr2);
+    *hp = 2.0 * Hinf * a2 * rr / ((a2 + rr2) * (a2 + rr2));
+}
+/* velocity of the streamfunction psi = -2U r^2 (1 - r^2/R^2)^2 eta (1 - eta) (:4059-4073) */
+static void m_velocity(const m_geom* g, double r, double z, double* ur, double* uz) {
+    *ur = 0.0; *uz = 0.0;
+    if (!(g->UPEAK > 0.0) || !(g->R > 0.0) || !(g->DH > 0.0) || (g->FSM == 2 && !(g->CORE > 0.0))) return;
+    double rr = fmin(fmax(r, 0.0), g->R), R2 = g->R * g->R, rr2 = rr * rr, zs = g->ZMEAN, hp = 0.0;
+    m_surface(g, rr, &zs, &hp);
+    double H = zs - g->ZMIN;
+    if (!(H > 0.0)) return;
+    double eta = (z - g->ZMIN) / H;
+    if (eta < 0.0) eta = 0.0;
+    if (eta > 1.0) eta = 1.0;
+    double sq = rr2 / R2, f = eta * (1.0 - eta), fp = 1.0 - 2.0 * eta, A = 2.0 * g->UPEAK, om = 1.0 - sq;
+    *ur = A * rr * om * om * fp / H;
+    *uz = -A * (2.0 * om * (1.0 - 3.0 * sq) * f - rr * om * om * fp * eta * hp / H);
+}
+/* radial slip of bin p interpolated from its table (:4075-4082) */
+static double m_slip(const double* WR, int p, double r, double R, int NRAD) {
+    if (NRAD < 2 || !(R > 0.0)) return 0.0;
+    double q = fmin(fmax(r / R, 0.0), 1.0) * (double)(NRAD - 1);
+    int j = (int)floor(q);
+    double t = q - (double)j;
+    if (j >= NRAD - 1) { j = NRAD - 2; t = 1.0; }
+    const double* w = WR + (size_t)p * NRAD;
+    return (1.0 - t) * w[j] + t * w[j + 1];
+}
+/* a point inside the liquid (:4084-4089) */
+static int m_fluid(const m_geom* g, double r, double z) {
+    if (z < g->ZMIN) return 0;
+    double zs = g->ZMEAN, hp = 0.0;
+    m_surface(g, r, &zs, &hp);
+    return z < zs;
+}
+
+typedef struct {
+    int NR, NZ;
+    double dr, dz, target;
+    const unsigned char* act;
+} m_plane;
+
+/* mass renormalisation of one bin's plane (:4176-4187); 41 when the mass is not usable */
+static int m_normalize(const m_plane* P, double* G) {
+    double mass = 0.0;
+    for (int i = 0; i < P->NR; ++i) {
+        double rw = (double)i * P->dr, re = (double)(i + 1) * P->dr, vol = 0.5 * (re * re - rw * rw) * P->dz;
+        for (int k = 0; k < P->NZ; ++k) {
+            int c = i * P->NZ + k;
+            if (P->act[c]) mass += G[c] * vol;
+        }
+    }
+    if (!(mass > 0.0) || !(P->target > 0.0) || !isfinite(mass)) return 41;
+    double scale = P->target / mass;
+    for (int c = 0; c < P->NR * P->NZ; ++c)
+        if (P->act[c]) G[c] *= scale;
+    return 0;
+}
+/* neighbour sum of cell (i, k) */
+static inline double m_neigh(const m_plane* P, const double* const* A, const double* G, int i, int k, int c) {
+    const int NR = P->NR, NZ = P->NZ;
+    double num = 0.0;
+    if (i + 1 < NR) num += A[1][c] * G[(i + 1) * NZ + k];
+    if (i > 0) num += A[2][c] * G[(i - 1) * NZ + k];
+    if (k + 1 < NZ) num += A[3][c] * G[i * NZ + k + 1];
+    if (k > 0) num += A[4][c] * G[i * NZ + k - 1];
+    return num;
+}
+/* one colour of the SOR sweep (:4155-4169); a colour reads only the other colour, so order is free */
+static void m_relax(const m_plane* P, const double* const* A, double* G, int parity, double omega) {
+    for (int i = 0; i < P->NR; ++i)
+        for (int k = 0; k < P->NZ; ++k) {
+            int c = i * P->NZ + k;
+            if (!P->act[c] || ((i + k) & 1) != parity || !(A[0][c] > 0.0)) continue;
+            double target = m_neigh(P, A, G, i, k, c) / A[0][c], old = G[c];
+            double nv = (1.0 - omega) * old + omega * target;
+            if (!isfinite(nv) || nv < 1e-14) nv = 1e-14;
+            G[c] = nv;
+        }
+}
+/* largest relative residual of one bin (:4184-4193) */
+static double m_residual(const m_plane* P, const double* const* A, const double* G) {
+    double mr = 0.0;
+    for (int i = 0; i < P->NR; ++i)
+        for (int k = 0; k < P->NZ; ++k) {
+            int c = i * P->NZ + k;
+            if (!P->act[c] || !(A[0][c] > 0.0)) continue;
+            double num = m_neigh(P, A, G, i, k, c);
+            double den = fmax(fabs(A[0][c] * G[c]), 1e-30), q = fabs(A[0][c] * G[c] - num) / den;
+            if (q > mr) mr = q;
+        }
+    return mr;
+}
+
+static int meridional_solve(clo_state* S, const clr_sediment_spec* ss, const m_geom* g) {
+    const int n = S->n, NR = ss->meridional_nr, NZ = ss->meridional_nz, NRAD = S->n_radial;
+    const int max_it = ss->solver_max_iterations, every = ss->solver_check_interval;
+    if (NR < 2 || NZ < 2 || max_it < 1 || every < 1 || !(ss->grid_zmax > g->ZMIN)) {
+        snprintf(S->err, sizeof S->err, "bad meridional solver settings"); return -1;
+    }
+    const size_t plane = (size_t)NR * NZ;
+    m_plane P = {NR, NZ, g->R / (double)NR, (ss->grid_zmax - g->ZMIN) / (double)NZ,
+                 0.5 * g->R * g->R * (g->ZMEAN - g->ZMIN), NULL};
+    unsigned char* act = (unsigned char*)calloc(plane, 1);
+    double* G = zalloc(plane * n);
+    double* coef = zalloc(5 * plane * n);
+    double* res = zalloc(n);
+    int* bad = (int*)calloc((size_t)n, sizeof(int));
+    P.act = act;
+    /* liquid cells (:4091-4098) */
+    for (int i = 0; i < NR; ++i)
+        for (int k = 0; k < NZ; ++k)
+            act[i * NZ + k] = (unsigned char)m_fluid(g, ((double)i + 0.5) * P.dr, g->ZMIN + ((double)k + 0.5) * P.dz);
+    /* the model-2 drift-diffusion field starts the iteration (:4100-4112, sediment_local_scale :1560-1593) */
+    o_field F = {2, g->FSM, n, NRAD, 2, 2, S->sed_A, S->sed_B, S->sed_norm, S->sed_radial_log, NULL,
+                 (float)ss->grid_zmax, (float)g->R, (float)g->ZMIN, (float)g->CORE};
+    int rc = 0;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int p = 0; p < n; ++p) {
+        double* Gp = G + (size_t)p * plane;
+        double* A[5];
+        for (int q = 0; q < 5; ++q) A[q] = coef + ((size_t)p * 5 + q) * plane;
+        for (int i = 0; i < NR; ++i)
+            for (int k = 0; k < NZ; ++k) {
+                int c = i * NZ + k;
+                if (!act[c]) { Gp[c] = 0.0; continue; }
+                float x = (float)(((double)i + 0.5) * P.dr), z = (float)(g->ZMIN + ((double)k + 0.5) * P.dz);
+                Gp[c] = o_local_scale(&F, p, x, 0.0f, z);
+            }
+        /* upwind finite-volume coefficients with no-flux walls (:4114-4153) */
+        const double ws = S->sed_ws[p], Dt = ss->eddy_diffusivity;
+        for (int i = 0; i < NR; ++i)
+            for (int k = 0; k < NZ; ++k) {
+                int c = i * NZ + k;
+                if (!act[c]) continue;
+                double rc = ((double)i + 0.5) * P.dr, zc = g->ZMIN + ((double)k + 0.5) * P.dz;
+                double rw = (double)i * P.dr, re = (double)(i + 1) * P.dr, dz = P.dz, dr = P.dr;
+                double Az = 0.5 * (re * re - rw * rw), ap = 0.0, ur = 0.0, uz = 0.0, V, Fl, diff;
+                if (i + 1 < NR && act[(i + 1) * NZ + k] && m_fluid(g, re, zc)) {          /* east face */
+                    m_velocity(g, re, zc, &ur, &uz);
+                    V = ur + m_slip(S->sed_wr, p, re, g->R, NRAD); Fl = V * re * dz; diff = Dt * re * dz / dr;
+                    A[1][c] = diff + fmax(-Fl, 0.0); ap += diff + fmax(Fl, 0.0);
+                }
+                if (i > 0 && act[(i - 1) * NZ + k] && m_fluid(g, rw, zc)) {               /* west face */
+                    m_velocity(g, rw, zc, &ur, &uz);
+                    V = ur + m_slip(S->sed_wr, p, rw, g->R, NRAD); Fl = -V * rw * dz; diff = Dt * rw * dz / dr;
+                    A[2][c] = diff + fmax(-Fl, 0.0); ap += diff + fmax(Fl, 0.0);
+                }
+                double zf = zc + 0.5 * dz;
+                if (k + 1 < NZ && act[i * NZ + k + 1] && m_fluid(g, rc, zf)) {           /* top face */
+                    m_velocity(g, rc, zf, &ur, &uz);
+                    V = uz - ws; Fl = V * Az; diff = Dt * Az / dz;
+                    A[3][c] = diff + fmax(-Fl, 0.0); ap += diff + fmax(Fl, 0.0);
+                }
+                zf = zc - 0.5 * dz;
+                if (k > 0 && act[i * NZ + k - 1] && m_fluid(g, rc, zf)) {                /* bottom face */
+                    m_velocity(g, rc, zf, &ur, &uz);
+                    V = uz - ws; Fl = -V * Az; diff = Dt * Az / dz;
+                    A[4][c] = diff + fmax(-Fl, 0.0); ap += diff + fmax(Fl, 0.0);
+                }
+                A[0][c] = ap;
+            }
+        bad[p] = m_normalize(&P, Gp);
+    }
+    for (int p = 0; p < n; ++p) if (bad[p]) rc = bad[p];
+    const int min_it = max_it < 1000 ? max_it : 1000;
+    int iters = 0, last = 0;
+    double worst = 0.0;
+    for (int it0 = 0; !rc && it0 < max_it;) {
+        /* the next check: a multiple of the interval, or the last iteration */
+        int it1 = (it0 / every + 1) * every;
+        if (it1 > max_it) it1 = max_it;
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int p = 0; p < n; ++p) {
+            double* Gp = G + (size_t)p * plane;
+            const double* A[5];
+            for (int q = 0; q < 5; ++q) A[q] = coef + ((size_t)p * 5 + q) * plane;
+            for (int it = it0 + 1; it <= it1; ++it) {
+                m_relax(&P, A, Gp, 0, ss->solver_sor);
+                m_relax(&P, A, Gp, 1, ss->solver_sor);
+                if (it % 20 == 0 && m_normalize(&P, Gp)) bad[p] = 41;
+            }
+            if (m_normalize(&P, Gp)) bad[p] = 41;
+            res[p] = m_residual(&P, A, Gp);
+        }
+        for (int p = 0; p < n; ++p) if (bad[p]) rc = bad[p];
+        if (rc) break;
+        last = it1;
+        worst = 0.0;
+        for (int p = 0; p < n; ++p) worst = res[p] > worst ? res[p] : worst;
+        if (it1 >= min_it && worst <= ss->solver_tolerance) { iters = it1; break; }
+        it0 = it1;
+    }
+    if (iters == 0) iters = last ? last : max_it;
+    S->solver_iterations = iters;
+    S->solver_residual = worst;
+    if (!rc && worst > ss->solver_tolerance) rc = -7;
+    if (!rc) {
+        /* extend every column above the free surface with its highest liquid value (:4195-4201) */
+        for (int p = 0; p < n; ++p)
+            for (int i = 0; i < NR; ++i) {
+                double* col = G + (size_t)p * plane + (size_t)i * NZ;
+                int top = -1;
+                for (int k = NZ - 1; k >= 0; --k)
+                    if (act[i * NZ + k]) { top = k; break; }
+                if (top < 0) { for (int k = 0; k < NZ; ++k) col[k] = 1.0; continue; }
+                for (int k = top + 1; k < NZ; ++k) col[k] = col[top];
+            }
+        /* finalisation and majorants (:4203-4220) */
+        double mg = 0.0, mw = 0.0;
+        for (int p = 0; p < n; ++p) {
+            double mx = 0.0;
+            for (size_t c = 0; c < plane; ++c)
+                if (act[c] && G[(size_t)p * plane + c] > mx) mx = G[(size_t)p * plane + c];
+            if (!(mx > 0.0)) mx = 1.0;
+            S->sed_norm[p] = 1.0;
+            S->sed_max[p] = mx;
+        }
+        for (int i = 0; i < n; ++i) { mg += S->trace_geom[i] * S->sed_max[i]; mw += S->trace_wave[i] * S->sed_max[i]; }
+        S->sed_major[0] = mg; S->sed_major[1] = mw; S->sed_major[2] = mg + mw;
+        free(S->sed_grid);
+        S->sed_grid = G;
+        G = NULL;
+        S->grid_nr = NR; S->grid_nz = NZ;
+    } else if (rc == -7) {
+        snprintf(S->err, sizeof S->err, "meridional transport solver did not converge");
+    } else {
+        snprintf(S->err, sizeof S->err, "meridional normalization error %d", rc);
+    }
+    free(act); free(G); free(coef); free(res); free(bad);
+    return rc;
 }
 
 int clo_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, const clr_sediment_spec* ss, clo_state** out) {
@@ -366,6 +620,7 @@ int clo_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, const c
     S->n_radial = NRAD;
     S->sed_A = zalloc(n); S->sed_B = zalloc(n); S->sed_norm = zalloc(n); S->sed_max = zalloc(n);
     S->sed_radial_log = zalloc((size_t)n * NRAD); S->sed_major = zalloc(4);
+    S->sed_ws = zalloc(n); S->sed_wr = zalloc((size_t)n * NRAD);
     const int TM = sp->sediment_model, FSM = sp->free_surface_model;
     /* FP64 geometry as the reference passes it (float64 arguments, CLARITAS/CLARITAS.py:6413-6418);
        a spec without it widens the scene's FP32 values */
@@ -407,6 +662,7 @@ int clo_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, const c
             double ws = (TM == 2 || TM == 3) ? schiller_naumann(ws0, d, rho_w, mu, &sre, &sdrag) : ws0;
             double Bc = ws / Dt;
             S->sed_B[i] = Bc;
+            S->sed_ws[i] = ws;
             long long base = (long long)i * NRAD;
             double* RL = S->sed_radial_log + base;
             if (TM == 1) {
@@ -425,6 +681,7 @@ int clo_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, const c
                     double w0 = tau * acc, re = 0.0, drag = 1.0;
                     double wr = schiller_naumann(w0, d, rho_w, mu, &re, &drag);
                     wr_arr[j] = wr;
+                    S->sed_wr[base + j] = wr;
                     if (j > 0) total += 0.5 * (prev + wr) * drad;
                     prev = wr;
                 }
@@ -482,7 +739,11 @@ int clo_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, const c
     S->grid_nr = 2; S->grid_nz = 2; S->grid_zmax = (float)ss->grid_zmax;
     S->sed_grid = zalloc(1);
     S->sed_grid[0] = 1.0;
-    if (TM == 3) {
+    if (TM == 3 && !ss->grid) {
+        m_geom g = {FSM, R, ZMIN, ZMEAN, DH, CORE, ss->meridional_peak_speed};
+        int rc = meridional_solve(S, ss, &g);
+        if (rc) return rc;
+    } else if (TM == 3) {
         /* caller-supplied grid, every cell active: finalisation + majorants (:4203-4220) */
         if (!ss->grid || ss->grid_nr < 2 || ss->grid_nz < 2) { snprintf(S->err, sizeof S->err, "model 3 needs a grid"); return -1; }
         S->grid_nr = ss->grid_nr; S->grid_nz = ss->grid_nz;
@@ -505,6 +766,16 @@ int clo_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, const c
 }
 
 int clo_n_theta(clo_state* s) { return s ? s->nt : 0; }
+
+int clo_read_sediment_field(clo_state* S, double* grid, int* nr, int* nz, int* iterations, double* max_residual) {
+    if (!S) return -1;
+    if (nr) *nr = S->grid_nr;
+    if (nz) *nz = S->grid_nz;
+    if (iterations) *iterations = S->solver_iterations;
+    if (max_residual) *max_residual = S->solver_residual;
+    if (grid) memcpy(grid, S->sed_grid, (size_t)S->n * S->grid_nr * S->grid_nz * sizeof(double));
+    return 0;
+}
 
 int clo_read_physics(clo_state* S, clr_particle_physics* o) {
     if (!S || !o) return -1;

@@ -8,7 +8,8 @@
  *     (CLARITAS/CLARITAS.py:6036-6965): PSD normalisation (:6147-6169), Mie
  *     coefficients (:6186-6220), theta grid / phase pdf / phase cdf or the dummy
  *     table (:6221-6255), transport rates (:6278-6325), channel rate arrays
- *     (:6362-6375), sediment coefficients (:6399-6449), and for model 3 the grid
+ *     (:6362-6375), sediment coefficients (:6399-6449), and for model 3 either the
+ *     meridional solver's launch sequence (:6451-6725) or the grid
  *     finalisation/majorants (:6694-6725) on a caller-supplied grid;
  *   - one simulate() chunk (CLARITAS/CLARITAS.py:7631-7864): trace_kernel with
  *     the exact 234-argument list (:7638-7758), then score_detectors_kernel
@@ -57,6 +58,8 @@ struct RefState {
     std::vector<double> sed_sc, sed_sw, sed_bc, sed_bw, sed_major;
     std::vector<double> sed_grid;
     int grid_nr = 2, grid_nz = 2, n_radial = 65;
+    int solver_iterations = 0;
+    double solver_residual = 0.0;
     float grid_zmax = 0.f;
     std::string err;
 };
@@ -196,7 +199,78 @@ int clref_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, const
     if (err) { S->err = "sediment precompute error"; return err; }
     S->sed_grid.assign(1, 1.0);
     S->grid_nr = 2; S->grid_nz = 2; S->grid_zmax = (float)ss->grid_zmax;
-    if (sp->sediment_model == 3) {
+    if (sp->sediment_model == 3 && !ss->grid) {
+        // the reference's meridional solver kernels in its host's launch sequence (:6451-6725); a launch of
+        // T threads becomes a loop over t, a <<<n, 1>>> launch a loop over the bins
+        const int GNR = ss->meridional_nr, GNZ = ss->meridional_nz, FSM = sp->free_surface_model;
+        const int max_it = ss->solver_max_iterations, every = ss->solver_check_interval;
+        if (GNR < 2 || GNZ < 2 || max_it < 1 || every < 1) { S->err = "bad meridional solver settings"; return -1; }
+        const long long plane = (long long)GNR * GNZ, total = plane * n;
+        const double ZG = ss->grid_zmax;
+        S->grid_nr = GNR; S->grid_nz = GNZ;
+        S->sed_grid.assign((size_t)total, 0.0);
+        std::vector<unsigned char> active((size_t)plane, 0);
+        std::vector<double> ap((size_t)total), ae((size_t)total), aw((size_t)total), an((size_t)total),
+            as((size_t)total), res(n, 0.0);
+        double* G = S->sed_grid.data();
+        auto each = [](long long T, auto&& f) {
+#pragma omp parallel for schedule(static)
+            for (long long t = 0; t < T; ++t) { set_index(256, (unsigned)t); f(); }
+            set_index(1, 0);
+        };
+        auto per_bin = [&](auto&& f) {
+            for (int p = 0; p < n; ++p) { set_index(1, p); f(); }
+            set_index(1, 0);
+        };
+        each(plane, [&] { meridional_active_mask_kernel(GNR, GNZ, GR, GZMIN, ZG, GZMEAN, FSM, GDH, GCORE,
+                                                        active.data()); });
+        each(total, [&] { meridional_grid_initialize_kernel(n, GNR, GNZ, GR, GZMIN, ZG, FSM, GCORE, S->sed_A.data(),
+                                                            S->sed_B.data(), S->sed_norm.data(),
+                                                            S->sed_radial_log.data(), NR, active.data(), G); });
+        each(total, [&] { meridional_build_coefficients_kernel(n, GNR, GNZ, GR, GZMIN, ZG, GZMEAN, FSM, GDH, GCORE,
+                                                               ss->meridional_peak_speed, ss->eddy_diffusivity,
+                                                               S->sed_ws.data(), S->sed_radial_wr.data(), NR,
+                                                               active.data(), ap.data(), ae.data(), aw.data(),
+                                                               an.data(), as.data()); });
+        auto normalize = [&] {
+            per_bin([&] { meridional_normalize_kernel(n, GNR, GNZ, GR, GZMIN, ZG, GZMEAN, active.data(), G, &err); });
+        };
+        auto relax = [&](int parity) {
+            each(total, [&] { meridional_relax_kernel(n, GNR, GNZ, parity, ss->solver_sor, active.data(), ap.data(),
+                                                      ae.data(), aw.data(), an.data(), as.data(), G); });
+        };
+        normalize();
+        if (err) { S->err = "meridional initial normalization error"; return err; }
+        const int min_it = max_it < 1000 ? max_it : 1000;
+        int iters = 0, last = 0;
+        for (int it = 1; it <= max_it; ++it) {
+            relax(0);
+            relax(1);
+            if (it % 20 == 0) normalize();
+            if (it % every == 0 || it == max_it) {
+                normalize();
+                per_bin([&] { meridional_residual_kernel(n, GNR, GNZ, active.data(), ap.data(), ae.data(), aw.data(),
+                                                         an.data(), as.data(), G, res.data()); });
+                if (err) { S->err = "meridional normalization error"; return err; }
+                last = it;
+                double mx = 0.0;
+                for (double v : res) mx = v > mx ? v : mx;
+                if (it >= min_it && mx <= ss->solver_tolerance) { iters = it; break; }
+            }
+        }
+        if (iters == 0) iters = last ? last : max_it;
+        double mx = 0.0;
+        for (double v : res) mx = v > mx ? v : mx;
+        S->solver_iterations = iters;
+        S->solver_residual = mx;
+        if (mx > ss->solver_tolerance) { S->err = "meridional transport solver did not converge"; return -7; }
+        each((long long)n * GNR, [&] { meridional_extend_grid_kernel(n, GNR, GNZ, active.data(), G); });
+        per_bin([&] { meridional_finalize_kernel(n, GNR, GNZ, GR, GZMIN, ZG, active.data(), G, S->sed_norm.data(),
+                                                 S->sed_max.data(), S->sed_min.data(), S->sed_sc.data(),
+                                                 S->sed_sw.data(), S->sed_bc.data(), S->sed_bw.data()); });
+        meridional_majorants_kernel(n, S->trace_geom.data(), S->trace_wave.data(), S->sed_max.data(),
+                                    S->sed_major.data());
+    } else if (sp->sediment_model == 3) {
         if (!ss->grid || ss->grid_nr < 2 || ss->grid_nz < 2) { S->err = "model 3 needs a grid"; return -1; }
         S->grid_nr = ss->grid_nr; S->grid_nz = ss->grid_nz;
         const size_t plane = (size_t)ss->grid_nr * ss->grid_nz;
@@ -233,6 +307,17 @@ int clref_read_physics(clref_state* h, clr_particle_physics* o) {
 }
 
 int clref_n_theta(clref_state* h) { return h ? reinterpret_cast<RefState*>(h)->nt : 0; }
+
+int clref_read_sediment_field(clref_state* h, double* grid, int* nr, int* nz, int* iterations, double* max_residual) {
+    RefState* S = reinterpret_cast<RefState*>(h);
+    if (!S) return -1;
+    if (nr) *nr = S->grid_nr;
+    if (nz) *nz = S->grid_nz;
+    if (iterations) *iterations = S->solver_iterations;
+    if (max_residual) *max_residual = S->solver_residual;
+    if (grid) std::copy(S->sed_grid.begin(), S->sed_grid.end(), grid);
+    return 0;
+}
 
 /* Trace + score run->n_rays rays starting at global id run->ray_offset.
  * records (host memory, nullable) receives one clr_ray_record per ray. */

@@ -7,11 +7,14 @@ Run where the reference checkout is available (it is read, never modified):
 The host build of the reference (oracle/_ref/libclaritas_ref_host.so, recipe in
 oracle/Makefile) runs every scene of tests/parity_scenes.py; the fixture keeps
 the physics-table digests, the digest of all per-ray records, a compact integer
-view and the tallies. tests/test_oracle_cpu.py pins the C restatement
-(oracle/claritas_oracle.c) to this file bit for bit.
+view and the tallies, and for a scene whose sediment field the meridional solver
+makes, the field's digest, its first bin, the iteration count and final residual.
+tests/test_oracle_cpu.py pins the C restatement (oracle/claritas_oracle.c) to
+this file bit for bit.
 """
 from __future__ import annotations
 
+import hashlib
 import json
 import os
 import platform
@@ -46,6 +49,12 @@ def main():
         meta["scenes"][name] = {"records_sha256": PS.records_digest(rec), "physics_sha256": PS.physics_digests(ph),
                                 "event_counts": tal["event_counts"][:PS.EVENT_KEYS].tolist(),
                                 "conditional_stats": [int(v) for v in tal["conditional_stats"]]}
+        if name in PS.SOLVED_FIELD:
+            f = ref.sediment_field()
+            meta["scenes"][name]["field"] = {"nr": int(f["grid"].shape[1]), "nz": int(f["grid"].shape[2]),
+                                             "iterations": f["iterations"], "max_residual": f["max_residual"],
+                                             "sha256": hashlib.sha256(f["grid"].tobytes()).hexdigest()}
+            out[f"{name}/field_bin0"] = f["grid"][0]
         out[f"{name}/compact"] = PS.compact(rec, N_COMPACT).astype(np.int16)
         for k in PS.TALLY_KEYS:
             out[f"{name}/{k}"] = tal[k]

@@ -56,6 +56,10 @@ def _bind(lib, prefix):
     getattr(lib, p + "last_error").restype = C.c_char_p
     getattr(lib, p + "free").argtypes = [C.c_void_p]
     getattr(lib, p + "free").restype = None
+    getattr(lib, p + "read_sediment_field").argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_int),
+                                                        C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                                        C.POINTER(C.c_double)]
+    getattr(lib, p + "read_sediment_field").restype = C.c_int
     return lib
 
 
@@ -106,6 +110,15 @@ class OracleRun:
         getattr(self.lib, self.p + "read_physics")(self.h, C.byref(pp))
         arrays["phase_cdf"] = arrays["phase_cdf"].reshape(self.n_bins, self.n_theta)
         return arrays
+
+    def sediment_field(self) -> dict:
+        """The model-3 field [bins][nr][nz] with the solver's iterations and final largest residual."""
+        f = getattr(self.lib, self.p + "read_sediment_field")
+        nr, nz, it, res = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        f(self.h, None, C.byref(nr), C.byref(nz), C.byref(it), C.byref(res))
+        grid = np.zeros((self.n_bins, nr.value, nz.value))
+        f(self.h, grid.ctypes.data_as(C.c_void_p), None, None, None, None)
+        return {"grid": grid, "iterations": it.value, "max_residual": res.value}
 
     def trace(self, run: abi.RunParams, records: bool = False, threads: int = 0):
         T = abi.Tallies()

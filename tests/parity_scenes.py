@@ -57,10 +57,10 @@ SCENES = {
 }
 
 
-# Scenes the CPU oracle does not cover: the meridional field solver is pinned against the reference's own
-# solver kernels on the GPU only.
-GPU_ONLY = {"meridional_solver"}
-CPU_SCENES = [k for k in SCENES if k not in GPU_ONLY]
+# Every scene runs in the CPU oracle as well (the meridional field solver included).
+CPU_SCENES = list(SCENES)
+# Scenes whose sediment field the meridional solver makes (no supplied grid).
+SOLVED_FIELD = {"meridional_solver"}
 
 
 def build(name: str):

@@ -76,8 +76,38 @@ def test_oracle_matches_reference_fixture(gold, name):
         assert PS.physics_digests(ph) == m["physics_sha256"], f"{name}: physics tables differ"
 
 
+def test_oracle_meridional_field_matches_reference_fixture(gold):
+    """Sediment model 3 without a supplied field: the restated red-black SOR solver stops at the reference's
+    iteration with its residual, and gives the reference's field (bit for bit on the fixture's platform)."""
+    import hashlib
+    z, meta = gold
+    m = meta["scenes"]["meridional_solver"]["field"]
+    cfg, parts, grid = PS.build("meridional_solver")
+    orc = H.OracleRun("port", cfg, parts, grid=grid)
+    f = orc.sediment_field()
+    orc.close()
+    assert f["grid"].shape[1:] == (m["nr"], m["nz"])
+    assert f["iterations"] == m["iterations"]
+    np.testing.assert_allclose(f["grid"][0], z["meridional_solver/field_bin0"], rtol=1e-9, atol=0)
+    assert f["max_residual"] == pytest.approx(m["max_residual"], rel=1e-6)
+    if platform.machine() == meta["machine"]:
+        assert f["max_residual"] == m["max_residual"]
+        assert hashlib.sha256(f["grid"].tobytes()).hexdigest() == m["sha256"]
+    # columns above the free surface carry their highest liquid value; the field is positive everywhere
+    assert np.all(f["grid"] > 0.0) and np.all(np.isfinite(f["grid"]))
+
+
+def test_oracle_meridional_solver_reports_non_convergence():
+    """An iteration budget below the tolerance's need is an error, as in the reference's host."""
+    cfg, parts, _ = PS.build("meridional_solver")
+    cfg.meridional_solver_max_iterations = 250
+    with pytest.raises(RuntimeError, match="did not converge"):
+        H.OracleRun("port", cfg, parts)
+
+
 @pytest.mark.skipif(not H.reference_available(), reason="host build of the reference not present (no checkout)")
-@pytest.mark.parametrize("name", ["rough_spheroid", "absorbing_conditional", "scully_surface", "grid_sediment"])
+@pytest.mark.parametrize("name", ["rough_spheroid", "absorbing_conditional", "scully_surface", "grid_sediment",
+                                  "meridional_solver"])
 def test_oracle_matches_live_reference(name):
     """Larger run against the live host build of the reference, when it could be built here."""
     cfg, parts, grid = PS.build(name)
