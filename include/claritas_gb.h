@@ -199,6 +199,37 @@ typedef struct clr_ray_record {
 enum { CLR_PS_INTERACTIONS = 0, CLR_PS_GEOMETRIC, CLR_PS_WAVE, CLR_PS_COHERENT, CLR_PS_MORPHOLOGY,
        CLR_PS_ENTRY_REFLECTIONS, CLR_PS_INTERNAL_REFLECTIONS };
 
+/* indices into clr_tallies.path_mask_hits: the reference's per-ray event-history masks
+ * (_event_history_masks, CLARITAS/CLARITAS.py:5265-5321, in its key order), predicates over the ray's
+ * interaction (ic), geometric (g), wave (w), coherent (coh), morphology (mor) counts and its particle
+ * entry-reflection (per), internal-reflection (pir) and absorption (pabs) counts */
+#define CLR_N_PATH_MASKS 25
+enum {
+    CLR_PM_ANY_PARTICLE = 0,        /* ic > 0 */
+    CLR_PM_ANY_GEOMETRIC,           /* g > 0 */
+    CLR_PM_ANY_WAVE,                /* w > 0 */
+    CLR_PM_ANY_COHERENT_WAVE,       /* coh > 0 */
+    CLR_PM_ANY_MORPHOLOGY_WAVE,     /* mor > 0 */
+    CLR_PM_ANY_ENTRY_REFLECTION,    /* per > 0 */
+    CLR_PM_ANY_INTERNAL_REFLECTION, /* pir > 0 */
+    CLR_PM_BALLISTIC,               /* ic == 0 */
+    CLR_PM_SINGLE,                  /* ic == 1 */
+    CLR_PM_SINGLE_ENTRY_REFLECTION, /* ic == 1, per > 0 */
+    CLR_PM_MULTIPLE,                /* ic >= 2 */
+    CLR_PM_ORDER_2, CLR_PM_ORDER_3, CLR_PM_ORDER_4PLUS,
+    CLR_PM_EXACTLY_ONE_GEOMETRIC,   /* ic == 1, g == 1, w == 0 */
+    CLR_PM_EXACTLY_ONE_WAVE,        /* ic == 1, g == 0, w == 1 */
+    CLR_PM_SINGLE_COHERENT_ESCAPE,  /* ic == 1, coh == 1 */
+    CLR_PM_SINGLE_ENTRY_REFLECTION_ESCAPE,    /* ic == 1, per > 0 */
+    CLR_PM_SINGLE_INTERNAL_REFLECTION_ESCAPE, /* ic == 1, pir > 0 */
+    CLR_PM_SINGLE_TRANSMISSION_ESCAPE,        /* ic == 1, (g > 0 or mor > 0), per == pir == pabs == 0 */
+    CLR_PM_MIXED_GEOMETRIC_WAVE,    /* ic >= 2, g > 0, w > 0 */
+    CLR_PM_GEOMETRIC_ONLY_MULTIPLE, /* ic >= 2, g > 0, w == 0 */
+    CLR_PM_WAVE_ONLY_MULTIPLE,      /* ic >= 2, g == 0, w > 0 */
+    CLR_PM_MULTIPLE_ENTRY_REFLECTION,    /* ic >= 2, per > 0 */
+    CLR_PM_MULTIPLE_INTERNAL_REFLECTION  /* ic >= 2, pir > 0 */
+};
+
 /* indices into clr_tallies.event_counts (sums of per-ray counters over the run) */
 enum {
     CLR_EV_INTERACTIONS = 0, CLR_EV_GEOMETRIC, CLR_EV_WAVE, CLR_EV_COHERENT, CLR_EV_MORPHOLOGY,
@@ -273,6 +304,10 @@ typedef struct clr_tallies {
     int64_t order_hits[2][6][CLR_N_DETECTORS];            /* by particle-interaction count 0,1,2,3,4,5+ */
     int64_t geometric_order_hits[2][6][CLR_N_DETECTORS];  /* by geometric-event count 0,1,2,3,4,5+ */
     int64_t path_sums[CLR_N_PATH_SUMS][2][CLR_N_DETECTORS];  /* sums of per-ray counters (CLR_PS_*) */
+    int64_t path_mask_hits[2][CLR_N_PATH_MASKS][CLR_N_DETECTORS];  /* rays satisfying each CLR_PM_* mask */
+    /* by acrylic reflection count (cell inner + outer + bottom inner + outer reflections) 0,1,2,3,4+
+     * (:8114-8123) */
+    int64_t acrylic_order_hits[2][5][CLR_N_DETECTORS];
 } clr_tallies;
 
 /* Host copies of the particle-physics tables (diagnostics and parity checks).
@@ -354,6 +389,48 @@ typedef struct clr_light_result {
     uint32_t first_outside_ray, first_outside_set;
 } clr_light_result;
 int clr_read_light_diagnostics(clr_ctx* ctx, clr_light_result* out);
+
+/* Particle-event provenance of detected rays: the reference's causal partitions of its per-ray
+ * provenance arrays (first/last particle, geometric and wave bin, first/last event type and deflection,
+ * acrylic returns; trace_kernel :4625-4647, :4966-4979, :5005-5058, host :8063-8160, :8470-8481),
+ * counted on the device. While enabled (clr_set_path_provenance), every clr_trace / clr_trace_batch of
+ * the current scene adds its detected rays into one clr_path_provenance (reset at each call, summed over
+ * the runs of the call); the wavefront engine counts them, the persistent kernel refuses the run.
+ * Index [side]: 0 the native, 1 the mirrored detector id. Event type codes (:4625-4628): 1 geometric
+ * external reflection, 2 geometric transmission/refraction, 3 geometric internal-reflection path,
+ * 4 coherent Mie wave, 5..7 the morphology-wave 1..3; 0 none. */
+enum { CLR_PB_FIRST_PARTICLE = 0, CLR_PB_LAST_PARTICLE, CLR_PB_FIRST_GEOMETRIC, CLR_PB_LAST_GEOMETRIC,
+       CLR_PB_FIRST_WAVE, CLR_PB_LAST_WAVE, CLR_PB_COUNT };
+enum { CLR_WALL_ZERO_PARTICLE = 0, CLR_WALL_NO_ACRYLIC_RETURN, CLR_WALL_ACRYLIC_RETURN };
+#define CLR_N_EVENT_TYPES 8
+#define CLR_N_H170_ANGLE_BINS 6     /* last/first deflection bins [0,30,60,90,120,150,180.0001) deg */
+typedef struct clr_path_provenance {
+    int64_t bin_hits[CLR_PB_COUNT][2][CLR_MAX_BINS][CLR_N_DETECTORS];  /* rays by first/last bin (CLR_PB_*) */
+    int64_t first_type_hits[2][CLR_N_EVENT_TYPES][CLR_N_DETECTORS];   /* by type of the first event */
+    int64_t last_type_hits[2][CLR_N_EVENT_TYPES][CLR_N_DETECTORS];    /* by type of the last event */
+    int64_t wall_hits[2][3][CLR_N_DETECTORS];           /* CLR_WALL_*: no event / events, no return / return */
+    int64_t after_return_hits[2][CLR_N_DETECTORS];      /* a particle event after an acrylic return */
+    int64_t first_backscatter_hits[2][CLR_N_DETECTORS]; /* first event turned the ray back (cos < 0) */
+    int64_t first_source_hemisphere_hits[2][CLR_N_DETECTORS];  /* leaving the first event with vy < 0 */
+    double first_angle_sum[2][CLR_N_DETECTORS];         /* deflection (deg) sums and counts, first event */
+    int64_t first_angle_count[2][CLR_N_DETECTORS];
+    double last_angle_sum[2][CLR_N_DETECTORS];          /* and last event */
+    int64_t last_angle_count[2][CLR_N_DETECTORS];
+    double last_type_angle_sum[2][CLR_N_EVENT_TYPES][CLR_N_DETECTORS];  /* last deflection by last type */
+    int64_t last_type_angle_count[2][CLR_N_EVENT_TYPES][CLR_N_DETECTORS];
+    int64_t h170_last_angle_hits[2][CLR_N_EVENT_TYPES][CLR_N_H170_ANGLE_BINS];  /* detector 17; row 0: all */
+    int64_t h170_first_angle_hits[2][CLR_N_H170_ANGLE_BINS];
+} clr_path_provenance;
+int clr_set_path_provenance(clr_ctx* ctx, int enabled);
+int clr_read_path_provenance(clr_ctx* ctx, clr_path_provenance* out);
+/* Per-ray provenance of the last single-run trace that wrote per-ray records with provenance on (the
+ * reference's per-ray outputs :4601-4603, :4580; parity tests): out [n_rays][4] words per ray,
+ *   [0] bytes 0..3: first / last particle bin, first / last geometric bin (0xFF none)
+ *   [1] bytes 0, 1: first / last wave bin; bits 16-19 first and 20-23 last event type; bit 24 first event
+ *       backscatter; 25 first event into the source hemisphere (vy < 0); 26 an acrylic (or headspace)
+ *       return after a particle event; 27 a particle event after such a return
+ *   [2], [3]: first / last deflection (deg) as float bits, -1 before any event */
+int clr_read_path_provenance_records(clr_ctx* ctx, uint32_t* out, int64_t n_rays);
 
 /* Trace n_runs runs of the current scene in one engine execution (one persistent-kernel launch or
  * one sequence of wavefront passes): each run has its own photon range, seeds and tallies

@@ -321,8 +321,24 @@ int clref_read_sediment_field(clref_state* h, double* grid, int* nr, int* nz, in
 
 /* Trace + score run->n_rays rays starting at global id run->ray_offset.
  * records (host memory, nullable) receives one clr_ray_record per ray. */
+static int trace_impl(clref_state* h, const clr_run_params* run, clr_tallies* T, clr_ray_record* records,
+                      int32_t* prov, float* defl, int n_threads);
+
 int clref_trace(clref_state* h, const clr_run_params* run, clr_tallies* T, clr_ray_record* records,
                 int n_threads) {
+    return trace_impl(h, run, T, records, nullptr, nullptr, n_threads);
+}
+
+/* As clref_trace, and per ray the reference's provenance outputs: prov [n_rays][13] = its int outputs
+ * first_particle_event_type .. particle_after_acrylic_return_count (trace_kernel :4601-4603), defl
+ * [n_rays][2] = first_particle_deflection_deg, last_particle_deflection_deg (:4580). */
+int clref_trace_provenance(clref_state* h, const clr_run_params* run, clr_tallies* T, clr_ray_record* records,
+                           int32_t* prov, float* defl, int n_threads) {
+    return trace_impl(h, run, T, records, prov, defl, n_threads);
+}
+
+static int trace_impl(clref_state* h, const clr_run_params* run, clr_tallies* T, clr_ray_record* records,
+                      int32_t* prov, float* defl, int n_threads) {
     RefState* S = reinterpret_cast<RefState*>(h);
     if (!S || !run || !T) return -1;
     if (run->rng_mode != CLR_RNG_REFERENCE_XORSHIFT || run->weight_mode != CLR_WEIGHT_ANALOG) {
@@ -436,6 +452,9 @@ int clref_trace(clref_state* h, const clr_run_params* run, clr_tallies* T, clr_r
                 r.water_path = F[6][i]; r.acrylic_path = F[7][i];
                 clr_tally_add_ray_stats(T, &r);
                 if (records) records[start + i] = tmp;
+                if (prov)
+                    for (int k = 0; k < 13; ++k) prov[(start + i) * 13 + k] = I[35 + k][i];
+                if (defl) { defl[(start + i) * 2] = F[8][i]; defl[(start + i) * 2 + 1] = F[9][i]; }
             }
         }
     }

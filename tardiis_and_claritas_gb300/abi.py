@@ -18,6 +18,16 @@ N_CONDITIONAL_STATS = 10
 N_SUBCODES = 96
 IC_HIST = 1024
 N_PATH_SUMS = 7  # CLR_N_PATH_SUMS
+# CLR_PM_* in order: the reference's event-history mask keys (CLARITAS/CLARITAS.py:5287-5320)
+PATH_MASK_NAMES = (
+    "any_particle", "any_geometric", "any_wave", "any_coherent_wave", "any_morphology_wave",
+    "any_entry_reflection", "any_internal_reflection", "ballistic", "single_interaction",
+    "single_entry_reflection", "multiple_interaction", "interaction_order_2", "interaction_order_3",
+    "interaction_order_4plus", "exactly_one_geometric", "exactly_one_wave", "single_coherent_wave_escape",
+    "single_external_entry_reflection_escape", "single_internal_reflection_escape",
+    "single_surface_transmission_escape", "mixed_geometric_wave", "geometric_only_multiple", "wave_only_multiple",
+    "multiple_with_entry_reflection", "multiple_with_internal_reflection")
+N_PATH_MASKS = len(PATH_MASK_NAMES)  # CLR_N_PATH_MASKS
 ES_NAMES = ["ic", "gic", "wic", "wcoh", "wmorph", "pr", "cir", "cor", "top", "bir", "bor", "ctir", "ttir", "btir",
             "per", "pir"]
 RF_NAMES = ["entered", "ballistic", "entry_reflected", "internal_reflected", "absorbed", "cell_tir", "top_tir",
@@ -170,6 +180,7 @@ class Tallies(C.Structure):
         ("sched_stats", i64 * 16),
         ("order_hits", i64 * N_DETECTORS * 6 * 2), ("geometric_order_hits", i64 * N_DETECTORS * 6 * 2),
         ("path_sums", i64 * N_DETECTORS * 2 * N_PATH_SUMS),
+        ("path_mask_hits", i64 * N_DETECTORS * N_PATH_MASKS * 2), ("acrylic_order_hits", i64 * N_DETECTORS * 5 * 2),
     ]
 
     def as_dict(self) -> dict:
@@ -226,6 +237,41 @@ def records_to_numpy(buf, n: int):
 def record_dtype():
     import numpy as np
     return np.dtype([(nm, np.int32) for nm in RECORD_INT_FIELDS] + [(nm, np.float32) for nm in RECORD_FLOAT_FIELDS])
+
+
+# clr_path_provenance: CLR_PB_* rows of bin_hits, CLR_WALL_* rows of wall_hits, event type codes
+PROVENANCE_BIN_NAMES = ("first_particle_bin", "last_particle_bin", "first_geometric_bin", "last_geometric_bin",
+                        "first_wave_bin", "last_wave_bin")
+WALL_PATH_NAMES = ("zero_particle", "particle_no_acrylic_return", "particle_with_acrylic_return")
+N_EVENT_TYPES = 8  # CLR_N_EVENT_TYPES
+N_H170_ANGLE_BINS = 6  # CLR_N_H170_ANGLE_BINS
+PARTICLE_EVENT_TYPE_NAMES = {1: "geometric_external_entry_reflection", 2: "geometric_surface_transmission_refraction",
+                             3: "geometric_internal_reflection_path", 4: "coherent_mie_wave",
+                             5: "morphology_wave_external_entry_reflection",
+                             6: "morphology_wave_surface_transmission_refraction",
+                             7: "morphology_wave_internal_reflection_path"}
+
+
+class PathProvenance(C.Structure):
+    _fields_ = [
+        ("bin_hits", i64 * N_DETECTORS * MAX_BINS * 2 * len(PROVENANCE_BIN_NAMES)),
+        ("first_type_hits", i64 * N_DETECTORS * N_EVENT_TYPES * 2),
+        ("last_type_hits", i64 * N_DETECTORS * N_EVENT_TYPES * 2),
+        ("wall_hits", i64 * N_DETECTORS * 3 * 2),
+        ("after_return_hits", i64 * N_DETECTORS * 2),
+        ("first_backscatter_hits", i64 * N_DETECTORS * 2),
+        ("first_source_hemisphere_hits", i64 * N_DETECTORS * 2),
+        ("first_angle_sum", f64 * N_DETECTORS * 2), ("first_angle_count", i64 * N_DETECTORS * 2),
+        ("last_angle_sum", f64 * N_DETECTORS * 2), ("last_angle_count", i64 * N_DETECTORS * 2),
+        ("last_type_angle_sum", f64 * N_DETECTORS * N_EVENT_TYPES * 2),
+        ("last_type_angle_count", i64 * N_DETECTORS * N_EVENT_TYPES * 2),
+        ("h170_last_angle_hits", i64 * N_H170_ANGLE_BINS * N_EVENT_TYPES * 2),
+        ("h170_first_angle_hits", i64 * N_H170_ANGLE_BINS * 2),
+    ]
+
+    def as_dict(self) -> dict:
+        import numpy as np
+        return {name: np.ctypeslib.as_array(getattr(self, name)).copy() for name, _ in self._fields_}
 
 
 class LightConfig(C.Structure):

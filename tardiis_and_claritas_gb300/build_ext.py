@@ -21,8 +21,8 @@ BUILD_DIR = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libclaritas_gb.so")
 
-SOURCES = ["clr_api.cu", "precompute.cu", "trace_xor.cu", "trace_philox.cu", "calibrate.cu", "noalloc.cu",
-           "surrogate.cu"]
+SOURCES = ["clr_api.cu", "precompute.cu", "trace_xor.cu", "trace_philox.cu", "wave_xor.cu", "wave_philox.cu",
+           "calibrate.cu", "noalloc.cu", "surrogate.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"] + ARCH
 # Per-unit flags. The FP64 precompute and the xorshift parity kernels are compiled without
@@ -30,7 +30,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas"
 # which is the reference's, instead of by where the compiler happens to fuse a*b+c (that depends
 # on inlining and common-subexpression context, which necessarily differ between two programs).
 # The Philox production kernels keep contraction.
-UNIT_FLAGS: dict = {"precompute.cu": ["-fmad=false"], "trace_xor.cu": ["-fmad=false"]}
+UNIT_FLAGS: dict = {"precompute.cu": ["-fmad=false"], "trace_xor.cu": ["-fmad=false"], "wave_xor.cu": ["-fmad=false"]}
 if os.environ.get("CLR_ALL_NOFMA"):
     UNIT_FLAGS = {s: ["-fmad=false"] for s in SOURCES}
 

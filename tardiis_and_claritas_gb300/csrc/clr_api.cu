@@ -62,6 +62,12 @@ struct clr_ctx {
     LightDiag light{};
     LightDiag* d_light = nullptr;
     std::vector<void*> light_allocs;
+    // particle-event provenance partitions (clr_set_path_provenance): the partitions and the per-slot state
+    bool prov_on = false;
+    clr_path_provenance* d_prov = nullptr;
+    uint4* wave_prov = nullptr;
+    uint4* d_prov_rec = nullptr;  // per-ray provenance of the last single-run trace with records
+    long long prov_rec_cap = 0, prov_rec_n = 0;
 };
 
 static int fail(clr_ctx* c, int code, const char* fmt, ...) {
@@ -140,6 +146,9 @@ int clr_destroy(clr_ctx* ctx) {
     cudaFree(ctx->sw_scratch);
     cudaFree(ctx->sw_jobs);
     for (void* p : ctx->light_allocs) cudaFree(p);
+    cudaFree(ctx->d_prov);
+    cudaFree(ctx->wave_prov);
+    cudaFree(ctx->d_prov_rec);
     if (ctx->wave_live) cudaFreeHost(ctx->wave_live);
     if (ctx->wave_ev) cudaEventDestroy(ctx->wave_ev);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -465,6 +474,8 @@ static void tally_to_host(const DevTally& d, clr_tallies* out, int64_t n_rays) {
                 out->geometric_order_hits[side][o][j] = (int64_t)d.pd.geom_order[side][o][j];
             }
             for (int k = 0; k < CLR_N_PATH_SUMS; ++k) out->path_sums[k][side][j] = (int64_t)d.pd.sums[k][side][j];
+            for (int k = 0; k < CLR_N_PATH_MASKS; ++k) out->path_mask_hits[side][k][j] = (int64_t)d.pd.masks[side][k][j];
+            for (int k = 0; k < 5; ++k) out->acrylic_order_hits[side][k][j] = (int64_t)d.pd.acrylic_order[side][k][j];
         }
     out->device_error = (t.n_done == (unsigned long long)n_rays) ? 0 : 1;
 }
@@ -509,7 +520,7 @@ struct SceneRef {
 // Traces n runs in one engine execution (one launch of the persistent kernel or one sequence of
 // wavefront passes), each run with its own scene, photon range, seeds and tallies.
 static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* runs, int n, clr_tallies* outs,
-                      clr_ray_record* d_records, const LightDiag* d_light = nullptr) {
+                      clr_ray_record* d_records, const LightDiag* d_light = nullptr, bool prov = false) {
     if (!ctx || !runs || !outs || n < 1) return CLR_ERR_INVALID_ARGUMENT;
     if (d_records && n != 1) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "per-ray records need a single run");
     const clr_run_params& r0 = runs[0];
@@ -524,10 +535,26 @@ static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* 
         if (run->rng_mode != r0.rng_mode || run->weight_mode != r0.weight_mode || run->flags != r0.flags)
             return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "runs of one call must share rng_mode, weight_mode and flags");
     }
+    const bool persistent = (r0.flags & CLR_RUN_PERSISTENT_KERNEL) != 0;
+    if (prov && persistent)
+        return fail(ctx, CLR_ERR_UNSUPPORTED, "particle-event provenance is counted by the wavefront engine only");
     CU(cudaSetDevice(ctx->device));
     int rc = run_buffers_ready(ctx, n);
     if (rc != CLR_OK) return rc;
     cudaStream_t st = ctx->stream;
+    if (prov) CU(cudaMemsetAsync(ctx->d_prov, 0, sizeof(clr_path_provenance), st));
+    ctx->prov_rec_n = 0;
+    if (prov && d_records) {  // per-ray provenance beside the per-ray records
+        const long long need = std::max((long long)r0.n_rays, 1LL);
+        if (ctx->prov_rec_cap < need) {
+            cudaFree(ctx->d_prov_rec);
+            ctx->d_prov_rec = nullptr;
+            ctx->prov_rec_cap = 0;
+            CU(cudaMalloc((void**)&ctx->d_prov_rec, (size_t)need * sizeof(uint4)));
+            ctx->prov_rec_cap = need;
+        }
+        ctx->prov_rec_n = r0.n_rays;
+    }
     std::vector<DevScene> hs(n);
     std::vector<long long> cb(n + 1), rb(n + 1);
     const int chunk = r0.rays_per_item > 0 ? r0.rays_per_item : 256;
@@ -536,6 +563,7 @@ static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* 
     for (int i = 0; i < n; ++i) {
         fill_scene(*refs[i].sp, *refs[i].pb, runs + i, &hs[i]);
         hs[i].light = d_light;
+        hs[i].prov = prov ? ctx->d_prov : nullptr;
         max_iter = std::max(max_iter, (long long)refs[i].sp->max_iterations);
         cb[i + 1] = cb[i] + (runs[i].n_rays + chunk - 1) / chunk;
         rb[i + 1] = rb[i] + runs[i].n_rays;
@@ -555,7 +583,6 @@ static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* 
     long long blocks_needed = (cb[n] * 32 + CLR_TRACE_THREADS - 1) / CLR_TRACE_THREADS;  // a chunk per warp at most
     a.grid = (int)std::max(1LL, std::min(want, blocks_needed));
     if (r0.max_blocks > 0) a.grid = std::max(1, std::min(a.grid, r0.max_blocks));
-    const bool persistent = (r0.flags & CLR_RUN_PERSISTENT_KERNEL) != 0;
     WaveLaunch w{};
     if (!persistent) {
         rc = wave_pool_ready(ctx);
@@ -566,6 +593,8 @@ static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* 
         w.ray = ctx->wave_ray; w.lane = ctx->wave_lane; w.meta = ctx->wave_meta; w.qbuf = ctx->wave_q;
         w.ctl = ctx->wave_ctl; w.cap = ctx->wave_cap; w.host_live = ctx->wave_live; w.flag_event = ctx->wave_ev;
         w.light = d_light != nullptr;
+        w.prov = prov ? ctx->wave_prov : nullptr;
+        w.prov_rec = ctx->prov_rec_n > 0 ? ctx->d_prov_rec : nullptr;
     }
     CU(cudaEventRecord(ctx->ev0, st));
     ctx->last_passes = 0;
@@ -597,7 +626,8 @@ static int trace_current(clr_ctx* ctx, const clr_run_params* runs, int n, clr_ta
     if (!ctx->built) return fail(ctx, CLR_ERR_NOT_READY, "clr_build_particles must succeed before clr_trace");
     if (n < 1) return CLR_ERR_INVALID_ARGUMENT;
     std::vector<SceneRef> refs(n, SceneRef{&ctx->sp, &ctx->pb});
-    return trace_runs(ctx, refs.data(), runs, n, outs, d_records, ctx->light_on ? ctx->d_light : nullptr);
+    return trace_runs(ctx, refs.data(), runs, n, outs, d_records, ctx->light_on ? ctx->d_light : nullptr,
+                      ctx->prov_on);
 }
 
 // Zero the light-diagnostic buffers (trajectory coordinates to NaN and orders to -1, as the reference).
@@ -971,6 +1001,40 @@ int clr_set_light_diagnostics(clr_ctx* ctx, const clr_light_config* cfg) {
     return CLR_OK;
 }
 
+int clr_set_path_provenance(clr_ctx* ctx, int enabled) {
+    if (!ctx) return CLR_ERR_INVALID_ARGUMENT;
+    CU(cudaSetDevice(ctx->device));
+    CU(cudaStreamSynchronize(ctx->stream));
+    ctx->prov_on = false;
+    if (!enabled) return CLR_OK;
+    int rc = wave_pool_ready(ctx);
+    if (rc != CLR_OK) return rc;
+    if (!ctx->d_prov) CU(cudaMalloc((void**)&ctx->d_prov, sizeof(clr_path_provenance)));
+    if (!ctx->wave_prov) CU(cudaMalloc((void**)&ctx->wave_prov, (size_t)ctx->wave_cap * sizeof(uint4)));
+    CU(cudaMemset(ctx->d_prov, 0, sizeof(clr_path_provenance)));
+    ctx->prov_on = true;
+    return CLR_OK;
+}
+
+int clr_read_path_provenance(clr_ctx* ctx, clr_path_provenance* out) {
+    if (!ctx || !out) return CLR_ERR_INVALID_ARGUMENT;
+    if (!ctx->prov_on) return fail(ctx, CLR_ERR_NOT_READY, "particle-event provenance is off");
+    CU(cudaSetDevice(ctx->device));
+    CU(cudaMemcpyAsync(out, ctx->d_prov, sizeof(clr_path_provenance), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return CLR_OK;
+}
+
+int clr_read_path_provenance_records(clr_ctx* ctx, uint32_t* out, int64_t n_rays) {
+    if (!ctx || !out || n_rays < 0) return CLR_ERR_INVALID_ARGUMENT;
+    if (!ctx->prov_on || n_rays > ctx->prov_rec_n)
+        return fail(ctx, CLR_ERR_NOT_READY, "no per-ray provenance for %lld rays (the last trace kept %lld)",
+                    (long long)n_rays, ctx->prov_rec_n);
+    CU(cudaSetDevice(ctx->device));
+    if (n_rays) CU(cudaMemcpy(out, ctx->d_prov_rec, (size_t)n_rays * sizeof(uint4), cudaMemcpyDeviceToHost));
+    return CLR_OK;
+}
+
 int clr_read_light_diagnostics(clr_ctx* ctx, clr_light_result* o) {
     if (!ctx || !o) return CLR_ERR_INVALID_ARGUMENT;
     if (!ctx->light_on) return fail(ctx, CLR_ERR_NOT_READY, "light diagnostics are off");
@@ -1117,6 +1181,7 @@ int64_t clr_abi_sizeof(int which) {
         case 4: return (int64_t)sizeof(clr_ray_record);
         case 5: return (int64_t)sizeof(clr_tallies);
         case 6: return (int64_t)sizeof(clr_particle_physics);
+        case 7: return (int64_t)sizeof(clr_path_provenance);
         default: return -1;
     }
 }

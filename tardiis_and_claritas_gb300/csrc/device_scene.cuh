@@ -67,6 +67,7 @@ struct DevScene {
     float roulette_threshold, roulette_survival;
     int32_t pad;
     const LightDiag* light;     // null unless light-history diagnostics are on for this trace
+    clr_path_provenance* prov;  // provenance partitions of detected rays; null unless counted for this trace
 };
 
 // Tally counters shared by the per-warp shared-memory tally and the per-scenario device tally.
@@ -94,6 +95,8 @@ struct PathDiag {
     unsigned long long order[2][6][CLR_N_DETECTORS];       // by particle-interaction count 0,1,2,3,4,5+
     unsigned long long geom_order[2][6][CLR_N_DETECTORS];  // by geometric-event count 0,1,2,3,4,5+
     unsigned long long sums[CLR_N_PATH_SUMS][2][CLR_N_DETECTORS];  // per-ray counter sums (CLR_PS_*)
+    unsigned long long masks[2][CLR_N_PATH_MASKS][CLR_N_DETECTORS];  // event-history masks (CLR_PM_*)
+    unsigned long long acrylic_order[2][5][CLR_N_DETECTORS];         // by acrylic reflection count 0..3, 4+
 };
 
 // Per-scenario tallies in device memory: the core plus the high part of the histogram

@@ -75,6 +75,8 @@ struct WaveLaunch {
     unsigned* host_live;           // pinned host words: live, tail ready, photons in flight
     cudaEvent_t flag_event;
     bool light;                    // light-history diagnostics on: the FLIGHT stage with its hooks
+    uint4* prov;                   // [cap] particle-event provenance per slot; null unless counted
+    uint4* prov_rec;               // [n_rays] provenance of every ray, with per-ray records; nullable
 };
 
 cudaError_t wave_run_xor(const WaveLaunch& w, int num_sms, cudaStream_t st, long long max_passes, int* passes);

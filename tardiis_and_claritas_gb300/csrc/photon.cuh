@@ -738,6 +738,7 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
                     o_mie_direction(opt, D.phase_cdf, D.theta, D.nt, pidx, &vx, &vy, &vz);
                     if (COND) { atomicAdd(&cstats[4], 1ull); atomicAdd(&cstats[7], 1ull); }
                     apply_moment(D, pidx, vinx, viny, vinz, &vx, &vy, &vz);
+                    if constexpr (kLight) *ev_pidx = pidx;  // the diagnostic callers' provenance of the event
                     break;
                 }
                 r.wmorph++;

@@ -19,6 +19,7 @@
 #include <cstring>
 #pragma once
 #include "photon.cuh"
+#include "provenance.cuh"
 #include "kernels.h"
 
 namespace clr {
@@ -196,13 +197,49 @@ __device__ __forceinline__ void group_hist(const TallySink& sink, unsigned grp, 
     }
 }
 
+// The reference's event-history masks of one ray (_event_history_masks, CLARITAS/CLARITAS.py:5265-5321) as
+// bits in CLR_PM_* order.
+__device__ __forceinline__ unsigned path_mask_bits(const Ray& r) {
+    const int ic = r.ic, g = r.gic, w = r.wic, coh = r.wcoh, mor = r.wmorph;
+    const int per = r.pc.entry_reflections, pir = r.pc.internal_reflections, pabs = r.pc.absorptions;
+    const bool single = ic == 1, multiple = ic >= 2, surface = g > 0 || mor > 0;
+    unsigned m = 0u;
+    auto set = [&](int k, bool v) { m |= (v ? 1u : 0u) << k; };
+    set(CLR_PM_ANY_PARTICLE, ic > 0);
+    set(CLR_PM_ANY_GEOMETRIC, g > 0);
+    set(CLR_PM_ANY_WAVE, w > 0);
+    set(CLR_PM_ANY_COHERENT_WAVE, coh > 0);
+    set(CLR_PM_ANY_MORPHOLOGY_WAVE, mor > 0);
+    set(CLR_PM_ANY_ENTRY_REFLECTION, per > 0);
+    set(CLR_PM_ANY_INTERNAL_REFLECTION, pir > 0);
+    set(CLR_PM_BALLISTIC, ic == 0);
+    set(CLR_PM_SINGLE, single);
+    set(CLR_PM_SINGLE_ENTRY_REFLECTION, single && per > 0);
+    set(CLR_PM_MULTIPLE, multiple);
+    set(CLR_PM_ORDER_2, ic == 2);
+    set(CLR_PM_ORDER_3, ic == 3);
+    set(CLR_PM_ORDER_4PLUS, ic >= 4);
+    set(CLR_PM_EXACTLY_ONE_GEOMETRIC, single && g == 1 && w == 0);
+    set(CLR_PM_EXACTLY_ONE_WAVE, single && g == 0 && w == 1);
+    set(CLR_PM_SINGLE_COHERENT_ESCAPE, single && coh == 1);
+    set(CLR_PM_SINGLE_ENTRY_REFLECTION_ESCAPE, single && per > 0);
+    set(CLR_PM_SINGLE_INTERNAL_REFLECTION_ESCAPE, single && pir > 0);
+    set(CLR_PM_SINGLE_TRANSMISSION_ESCAPE, single && surface && per == 0 && pir == 0 && pabs == 0);
+    set(CLR_PM_MIXED_GEOMETRIC_WAVE, multiple && g > 0 && w > 0);
+    set(CLR_PM_GEOMETRIC_ONLY_MULTIPLE, multiple && g > 0 && w == 0);
+    set(CLR_PM_WAVE_ONLY_MULTIPLE, multiple && g == 0 && w > 0);
+    set(CLR_PM_MULTIPLE_ENTRY_REFLECTION, multiple && per > 0);
+    set(CLR_PM_MULTIPLE_INTERNAL_REFLECTION, multiple && pir > 0);
+    return m;
+}
+
 // Score finished histories and add them to the scenario tallies (:4390-4436, tallies :7849-7862,
 // per-ray statistics :8483-8508 and :8665-8735). Called by every lane whose photon finished in this
 // iteration; lanes are grouped by scenario so the frequent counters are reduced across the group first.
 template <class Mode>
 __device__ __forceinline__ void finish_ray(const DevScene& D, const DetTable& T, const Ray& r, uint32_t gid,
                                            int sid, int home, WarpTally* wt, DevTally* tallies,
-                                           clr_ray_record* rec) {
+                                           clr_ray_record* rec, const uint4* prov = nullptr) {
     const clr_scene_params& P = D.P;
     const int lane = threadIdx.x & 31;
     const unsigned act = __activemask();
@@ -272,16 +309,21 @@ __device__ __forceinline__ void finish_ray(const DevScene& D, const DetTable& T,
             const int oi = r.ic < 5 ? r.ic : 5, gi = r.gic < 5 ? r.gic : 5;
             const int pv[CLR_N_PATH_SUMS] = {r.ic, r.gic, r.wic, r.wcoh, r.wmorph, r.pc.entry_reflections,
                                             r.pc.internal_reflections};
+            const unsigned masks = path_mask_bits(r);
+            const int acr = r.cir + r.cor + r.bir + r.bor, ai = acr < 4 ? acr : 4;
 #pragma unroll
             for (int side = 0; side < 2; ++side) {
                 const int id = side ? mi : ni;
                 if (id < 0) continue;
                 atomicAdd(&pd.order[side][oi][id], 1ull);
                 atomicAdd(&pd.geom_order[side][gi][id], 1ull);
+                atomicAdd(&pd.acrylic_order[side][ai][id], 1ull);
 #pragma unroll
                 for (int k = 0; k < CLR_N_PATH_SUMS; ++k)
                     if (pv[k] > 0) atomicAdd(&pd.sums[k][side][id], (unsigned long long)pv[k]);
+                for (unsigned m = masks; m; m &= m - 1u) atomicAdd(&pd.masks[side][__ffs(m) - 1][id], 1ull);
             }
+            if (D.prov) prov_count(*D.prov, prov ? *prov : prov_init(), r.ic, ni, mi);
         }
         // legacy angular windows (:4429-4434)
         for (int mirror = 0; mirror < 2; ++mirror) {

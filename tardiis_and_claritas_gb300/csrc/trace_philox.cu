@@ -1,4 +1,4 @@
-// Instantiations of the photon kernel on the counter-based Philox stream (production mode).
+// Instantiations of the persistent photon kernel on the counter-based Philox stream (production mode).
 #include "wavefront.cuh"
 
 namespace clr {
@@ -7,9 +7,5 @@ cudaError_t launch_philox(const LaunchArgs& a) {
 }
 int occupancy_philox(bool records) {
     return records ? occupancy_t<PhiloxMode, true, false>() : occupancy_t<PhiloxMode, false, false>();
-}
-cudaError_t wave_run_philox(const WaveLaunch& w, int num_sms, cudaStream_t st, long long max_passes, int* passes) {
-    return w.records ? wave_run_t<PhiloxMode, true>(w, num_sms, st, max_passes, passes)
-                     : wave_run_t<PhiloxMode, false>(w, num_sms, st, max_passes, passes);
 }
 }  // namespace clr

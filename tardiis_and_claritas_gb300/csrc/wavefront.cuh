@@ -247,9 +247,11 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
                     drawn++;
                     if (source_segment(D, r, L.source())) {
                         finish_ray<Mode>(D, det, r, gid, sid, home, wt, w.tallies, w.records ? w.records + rid : nullptr);
+                        if (w.prov_rec) w.prov_rec[rid] = prov_init();
                     } else {
                         pool.ray[slot] = r;
                         pool.lane[slot] = L;
+                        if (w.prov) w.prov[slot] = prov_init();
                         SlotMeta m;
                         m.gid = gid; m.sid = sid; m.rid = rid; m.pidx = -1;
                         m.acr_caller = 0; m.acr_it = 0; m.acr_stuck = 0; m.acr_last = -1;
@@ -270,19 +272,26 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
 }
 
 // ---------------- generic stage kernel (ENTRY, FLIGHT and the event handlers) ----------------
-// kLight: the water flights carry the light-diagnostic hooks (a separate FLIGHT kernel, used only when
-// the diagnostics are on, keeps them out of the production kernel).
+// kLight: the water flights carry the diagnostic hooks, light history and particle-event provenance (a
+// separate FLIGHT kernel, used only when a diagnostic is on, keeps them out of the production kernel).
+// pv: the photon's provenance state, or null when provenance is not counted.
 template <class Mode, int Q, bool kLight = true>
 __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevScene& D, Ray& r,
                                                typename Mode::Lane& L, SlotMeta& m,
-                                               unsigned long long* cstats) {
+                                               unsigned long long* cstats, uint4* pv) {
     if constexpr (Q == WQ_ENTRY) {
         return entry_segment(D, r, L.transport()) ? WQ_FIN : WQ_FLIGHT;
     } else if constexpr (Q == WQ_FLIGHT) {
         for (int k = 0; k < kFlightSteps; ++k) {
             int pidx = -1;
+            const float vinx = r.vx, viny = r.vy, vinz = r.vz;
+            const int coh0 = r.wcoh;
             const int e = water_flight<typename Mode::Stream, kLight>(D, r, L.transport(), L.optics(), cstats, &pidx,
                                                                        m.gid);
+            if constexpr (kLight) {  // a coherent wave event completes inside the flight
+                if (pv && e == WE_NONE && r.wcoh != coh0)
+                    prov_event(*pv, r.ic, 4, pidx, vinx, viny, vinz, r.vx, r.vy, r.vz);
+            }
             if (e == WE_NONE) continue;
             m.pidx = pidx;
             switch (e) {
@@ -299,11 +308,24 @@ __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevSce
         }
         return WQ_FLIGHT;
     } else if constexpr (Q == WQ_COND || Q == WQ_GEOM) {
+        // counters and direction before the event: a closure changes them only when it completes
+        const int ic0 = r.ic, coh0 = r.wcoh, mor0 = r.wmorph;
+        const int per0 = r.pc.entry_reflections, pir0 = r.pc.internal_reflections;
+        const float vinx = r.vx, viny = r.vy, vinz = r.vz;
+        auto survived = [&]() {  // the event completed with the photon in the water (not a null proposal)
+            if (pv && r.ic == ic0)
+                prov_event(*pv, r.ic, prov_type(r.wcoh - coh0, r.wmorph - mor0, r.pc.entry_reflections - per0,
+                                                r.pc.internal_reflections - pir0),
+                           m.pidx, vinx, viny, vinz, r.vx, r.vy, r.vz);
+        };
         CondState cs;
         int v;
         if constexpr (Q == WQ_GEOM) {
             v = water_geom_visit(D, r, L.optics(), cstats, m.pidx);
-            if (v != 3) return v ? WQ_FIN : WQ_FLIGHT;
+            if (v != 3) {
+                if (v == 0) survived();
+                return v ? WQ_FIN : WQ_FLIGHT;
+            }
             m.cond_kind = CK_GEOM;
             cs = cond_start();
             v = closure_visit(D, r, L.optics(), cstats, m.pidx, CK_GEOM, &cs, kCondInline);
@@ -315,11 +337,20 @@ __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevSce
             m.cond_started = cs.started; m.cond_trial = cs.trial; m.cond_target = cs.target;
             return WQ_COND;
         }
+        if (v == 0) survived();
         return v ? WQ_FIN : WQ_FLIGHT;
     } else if constexpr (Q == WQ_MORPH) {
-        return water_morph(D, r, L.optics(), cstats, m.pidx) ? WQ_FIN : WQ_FLIGHT;
+        const int per0 = r.pc.entry_reflections, pir0 = r.pc.internal_reflections;
+        const float vinx = r.vx, viny = r.vy, vinz = r.vz;
+        const bool ended = water_morph(D, r, L.optics(), cstats, m.pidx);
+        if (pv && !ended)
+            prov_event(*pv, r.ic, prov_type(0, 1, r.pc.entry_reflections - per0, r.pc.internal_reflections - pir0),
+                       m.pidx, vinx, viny, vinz, r.vx, r.vy, r.vz);
+        return ended ? WQ_FIN : WQ_FLIGHT;
     } else if constexpr (Q == WQ_TOP) {
-        return water_top(D, r, L.transport()) ? WQ_FIN : WQ_FLIGHT;
+        const bool ended = water_top(D, r, L.transport());
+        if (pv && !ended) prov_return(*pv, r.ic);  // back from the headspace
+        return ended ? WQ_FIN : WQ_FLIGHT;
     } else {
         // SIDE, BOTTOM and ACRYL: a bounded piece of the acrylic traversal
         const int budget = wave_drawing(w) ? kAcrBudget : 0;
@@ -341,6 +372,7 @@ __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevSce
             m.acr_caller = caller; m.acr_it = as.it; m.acr_stuck = as.stuck; m.acr_last = as.last_surf;
             return WQ_ACRYL;
         }
+        if (pv && v == 0) prov_return(*pv, r.ic);  // back from the acrylic (or the headspace beyond it)
         return v ? WQ_FIN : WQ_FLIGHT;
     }
 }
@@ -366,7 +398,13 @@ __global__ void __launch_bounds__(kWaveThreads, stage_min_blocks(Q)) wave_stage_
             SlotMeta m = pool.meta[slot];
             const DevScene& D = w.scenes[m.sid];
             unsigned long long* cstats = (m.sid == 0) ? bs.cs : w.tallies[m.sid].c.cstats;
-            dest = wave_stage_body<Mode, Q, kLight>(w, D, r, L, m, cstats);
+            // only the diagnostic variants carry the provenance (ENTRY never changes it)
+            constexpr bool kProv = Q != WQ_ENTRY && kLight;
+            uint4 pvv;
+            uint4* pv = nullptr;
+            if (kProv && w.prov) { pvv = w.prov[slot]; pv = &pvv; }
+            dest = wave_stage_body<Mode, Q, kLight>(w, D, r, L, m, cstats, pv);
+            if (kProv && pv) w.prov[slot] = pvv;
             pool.ray[slot] = r;
             pool.lane[slot] = L;
             if (Q == WQ_FLIGHT || dest == WQ_ACRYL || dest == WQ_COND) pool.meta[slot] = m;
@@ -375,6 +413,12 @@ __global__ void __launch_bounds__(kWaveThreads, stage_min_blocks(Q)) wave_stage_
         wave_push(w, dest, slot);
     }
     warp_done(&bs, w.tallies, Q, done);
+}
+
+// The event-handler stage kernel: its provenance-counting variant when provenance is on.
+template <class Mode, int Q>
+const void* stage_fn(const void* prov) {
+    return prov ? (const void*)wave_stage_kernel<Mode, Q, true> : (const void*)wave_stage_kernel<Mode, Q, false>;
 }
 
 // ---------------- FIN: detector scoring and tallies; the slot becomes free ----------------
@@ -404,7 +448,9 @@ __global__ void __launch_bounds__(kWaveThreads) wave_fin_kernel(WaveLaunch w) {
         if (valid) {
             const Ray r = pool.ray[slot];
             const DevScene& D = w.scenes[m.sid];
-            finish_ray<Mode>(D, det, r, m.gid, m.sid, home, wt, w.tallies, kRecord ? w.records + m.rid : nullptr);
+            finish_ray<Mode>(D, det, r, m.gid, m.sid, home, wt, w.tallies, kRecord ? w.records + m.rid : nullptr,
+                             w.prov ? w.prov + slot : nullptr);
+            if (kRecord && w.prov_rec) w.prov_rec[m.rid] = w.prov ? w.prov[slot] : prov_init();
             done++;
         }
         wave_push(w, valid ? WQ_FREE : -1, slot);
@@ -417,17 +463,18 @@ __global__ void __launch_bounds__(kWaveThreads) wave_fin_kernel(WaveLaunch w) {
 // ---------------- TAIL: the last photons, each run to its end by one thread ----------------
 template <class Mode>
 __device__ __forceinline__ int tail_visit(const WaveLaunch& w, int q, const DevScene& D, Ray& r,
-                                          typename Mode::Lane& L, SlotMeta& m, unsigned long long* cstats) {
+                                          typename Mode::Lane& L, SlotMeta& m, unsigned long long* cstats,
+                                          uint4* pv) {
     switch (q) {
-        case WQ_ENTRY: return wave_stage_body<Mode, WQ_ENTRY>(w, D, r, L, m, cstats);
-        case WQ_FLIGHT: return wave_stage_body<Mode, WQ_FLIGHT>(w, D, r, L, m, cstats);
-        case WQ_COND: return wave_stage_body<Mode, WQ_COND>(w, D, r, L, m, cstats);
-        case WQ_GEOM: return wave_stage_body<Mode, WQ_GEOM>(w, D, r, L, m, cstats);
-        case WQ_MORPH: return wave_stage_body<Mode, WQ_MORPH>(w, D, r, L, m, cstats);
-        case WQ_TOP: return wave_stage_body<Mode, WQ_TOP>(w, D, r, L, m, cstats);
-        case WQ_BOTTOM: return wave_stage_body<Mode, WQ_BOTTOM>(w, D, r, L, m, cstats);
-        case WQ_SIDE: return wave_stage_body<Mode, WQ_SIDE>(w, D, r, L, m, cstats);
-        default: return wave_stage_body<Mode, WQ_ACRYL>(w, D, r, L, m, cstats);
+        case WQ_ENTRY: return wave_stage_body<Mode, WQ_ENTRY>(w, D, r, L, m, cstats, pv);
+        case WQ_FLIGHT: return wave_stage_body<Mode, WQ_FLIGHT>(w, D, r, L, m, cstats, pv);
+        case WQ_COND: return wave_stage_body<Mode, WQ_COND>(w, D, r, L, m, cstats, pv);
+        case WQ_GEOM: return wave_stage_body<Mode, WQ_GEOM>(w, D, r, L, m, cstats, pv);
+        case WQ_MORPH: return wave_stage_body<Mode, WQ_MORPH>(w, D, r, L, m, cstats, pv);
+        case WQ_TOP: return wave_stage_body<Mode, WQ_TOP>(w, D, r, L, m, cstats, pv);
+        case WQ_BOTTOM: return wave_stage_body<Mode, WQ_BOTTOM>(w, D, r, L, m, cstats, pv);
+        case WQ_SIDE: return wave_stage_body<Mode, WQ_SIDE>(w, D, r, L, m, cstats, pv);
+        default: return wave_stage_body<Mode, WQ_ACRYL>(w, D, r, L, m, cstats, pv);
     }
 }
 
@@ -455,12 +502,16 @@ __global__ void __launch_bounds__(kTailThreads) wave_tail_kernel(WaveLaunch w) {
         SlotMeta m = pool.meta[slot];
         const DevScene& D = w.scenes[m.sid];
         unsigned long long* cstats = w.tallies[m.sid].c.cstats;
+        uint4 pvv = prov_init();
+        uint4* pv = nullptr;
+        if (w.prov) { pvv = w.prov[slot]; pv = &pvv; }
         while (q != WQ_FIN) {
             ++visits[q];
-            q = tail_visit<Mode>(w, q, D, r, L, m, cstats);
+            q = tail_visit<Mode>(w, q, D, r, L, m, cstats, pv);
         }
         ++visits[WQ_FIN];
-        finish_ray<Mode>(D, det, r, m.gid, m.sid, -1, nullptr, w.tallies, kRecord ? w.records + m.rid : nullptr);
+        finish_ray<Mode>(D, det, r, m.gid, m.sid, -1, nullptr, w.tallies, kRecord ? w.records + m.rid : nullptr, pv);
+        if (kRecord && w.prov_rec) w.prov_rec[m.rid] = pvv;
     }
     for (int q = 1; q < CLR_WQ_COUNT; ++q)
         if (visits[q]) atomicAdd(&w.tallies[0].sched[q], visits[q]);
@@ -535,15 +586,15 @@ struct WavePass {
         const StageK ks[CLR_WQ_COUNT] = {
             {(const void*)wave_gen_kernel<Mode>, kSmemTally, 0},
             {(const void*)wave_stage_kernel<Mode, WQ_ENTRY>, 0, 0},
-            {w.light ? (const void*)wave_stage_kernel<Mode, WQ_FLIGHT, true>
+            {(w.light || w.prov) ? (const void*)wave_stage_kernel<Mode, WQ_FLIGHT, true>
                      : (const void*)wave_stage_kernel<Mode, WQ_FLIGHT, false>, 0, 0},
-            {(const void*)wave_stage_kernel<Mode, WQ_COND>, 0, 1},
-            {(const void*)wave_stage_kernel<Mode, WQ_GEOM>, 0, 0},
-            {(const void*)wave_stage_kernel<Mode, WQ_MORPH>, 0, 1},
-            {(const void*)wave_stage_kernel<Mode, WQ_TOP>, 0, 1},
-            {(const void*)wave_stage_kernel<Mode, WQ_BOTTOM>, 0, 1},
-            {(const void*)wave_stage_kernel<Mode, WQ_SIDE>, 0, 0},
-            {(const void*)wave_stage_kernel<Mode, WQ_ACRYL>, 0, 1},
+            {stage_fn<Mode, WQ_COND>(w.prov), 0, 1},
+            {stage_fn<Mode, WQ_GEOM>(w.prov), 0, 0},
+            {stage_fn<Mode, WQ_MORPH>(w.prov), 0, 1},
+            {stage_fn<Mode, WQ_TOP>(w.prov), 0, 1},
+            {stage_fn<Mode, WQ_BOTTOM>(w.prov), 0, 1},
+            {stage_fn<Mode, WQ_SIDE>(w.prov), 0, 0},
+            {stage_fn<Mode, WQ_ACRYL>(w.prov), 0, 1},
             {(const void*)wave_fin_kernel<Mode, kRecord>, kSmemTally, 0},
         };
         p.blockDim = dim3(kWaveThreads);

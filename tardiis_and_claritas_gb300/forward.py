@@ -353,7 +353,10 @@ class ClaritasForwardModel:
                  weight_mode="mass_fraction", collect_rays=False, heatmap_size=0, light_transport_config=None,
                  target_detector_score=None, min_rays=None, max_rays=None, min_rear_channel_score=None,
                  min_h170_score=None, stability_l1_tolerance=None, stability_window=3,
-                 ray_id_start=0) -> ForwardResult:
+                 ray_id_start=0, path_provenance=True) -> ForwardResult:
+        """The reference's simulate (CLARITAS.py:7160-7179). path_provenance (not a reference keyword): count
+        the particle-event provenance partitions of the path diagnostics (first/last bin, event type and
+        deflection, acrylic returns), which the reference always derives; off saves their device work."""
         light = self._light_setup(light_transport_config, heatmap_size)
         if collect_rays:
             raise NotImplementedError("collect_rays: use lib.Context.trace(run, records=True) for per-ray records")
@@ -384,6 +387,8 @@ class ClaritasForwardModel:
             raise ValueError("number of rays must be positive")
         self._prepare(material, concentration_g_per_L, weights, weight_mode)
         ctx = self._context()
+        prov = bool(path_provenance)
+        ctx.set_provenance(prov)
         batch = int(cfg.statistics_batch_rays)
         sizes = []
         left = max_n
@@ -392,9 +397,10 @@ class ClaritasForwardModel:
             left -= sizes[-1]
         # Batches are traced in groups through one clr_trace_batch call; a fixed-count run is one group.
         group = len(sizes) if not adaptive else max(1, min(len(sizes), 64))
-        if adaptive and light is not None:
-            group = 1  # light diagnostics accumulate over traced batches: trace no batch past the stopping one
+        if adaptive and (light is not None or prov):
+            group = 1  # diagnostics accumulate over traced batches: trace no batch past the stopping one
         tallies = []
+        prov_parts = []
         stop_at = None
         state = _StopState()
         start = 0
@@ -405,6 +411,8 @@ class ClaritasForwardModel:
                 runs.append(S.run_params(sizes[k], seed=seed, ray_offset=off, rng_mode=self.rng_mode))
                 off += sizes[k]
             got = ctx.trace_batch(runs)
+            if prov:
+                prov_parts.append(ctx.read_provenance())
             for t in got:
                 tallies.append(t)
                 if adaptive and state.after_batch(self, t, min_n, target, rear_target, h170_target,
@@ -417,7 +425,11 @@ class ClaritasForwardModel:
             stop_reason = state.reason
         else:
             stop_reason = state.final_reason(adaptive, target, rear_target, h170_target, stability_l1_tolerance)
-        res = self._result(tallies, requested, adaptive, max_n, stop_reason)
+        ctx.set_provenance(False)
+        prov_total = None
+        if prov_parts:
+            prov_total = {k: np.sum([q[k] for q in prov_parts], axis=0) for k in prov_parts[0]}
+        res = self._result(tallies, requested, adaptive, max_n, stop_reason, prov_total)
         if light is not None:
             res.heatmap_xy, res.heatmap_zy, res.light_transport_diagnostics = self._light_results(
                 light, ray_id_start, res.n_rays)
@@ -527,7 +539,7 @@ class ClaritasForwardModel:
         leg = 0.5 * (lnat + lmir) if cfg.symmetry_average_exact else lnat
         return sel, hw, pd, leg
 
-    def _result(self, tallies, requested, adaptive, max_n, stop_reason) -> ForwardResult:
+    def _result(self, tallies, requested, adaptive, max_n, stop_reason, prov=None) -> ForwardResult:
         cfg = self.config
         sym = avg = cfg.symmetry_average_exact
         tot = {k: np.sum([np.asarray(t[k]) for t in tallies], axis=0) for k in tallies[0]
@@ -718,7 +730,7 @@ class ClaritasForwardModel:
             mirror_detector_detection_fraction=float(mirror.sum() if ideal else pd_mir.sum()) / nrays,
             legacy_channel_score_per_ray=float(legacy_sym_total.sum()) / nrays,
             symmetry_variance_reduction=bool(sym), batch_diagnostics=rows, particle_diagnostics=dict(ph),
-            detector_particle_path_diagnostics=self._path_diagnostics(tot, hw_sym, avg))
+            detector_particle_path_diagnostics=self._path_diagnostics(tot, hw_sym, avg, prov))
 
     # The reference's detector particle-path diagnostics (simulate, CLARITAS.py:8019-8110 and :8972-9140) from
     # the device partitions of the detected rays; partitions that need per-ray provenance the device does not
@@ -732,7 +744,7 @@ class ClaritasForwardModel:
                     "accepted_coherent", "accepted_morphology", "accepted_absorptions", "accepted_scatterings",
                     "numerical_failures", "retry_exhaustions"]
 
-    def _path_diagnostics(self, tot: dict, denp: np.ndarray, avg: bool) -> dict:
+    def _path_diagnostics(self, tot: dict, denp: np.ndarray, avg: bool, prov: Optional[dict] = None) -> dict:
         def sym(native, mirror):
             return 0.5 * (native + mirror) if avg else native.copy()
         oh = np.asarray(tot["order_hits"], dtype=np.float64)            # [side][order][channel]
@@ -741,10 +753,31 @@ class ClaritasForwardModel:
         order, gorder = sym(oh[0], oh[1]), sym(gh[0], gh[1])            # [6][18]
         sums = sym(ps[:, 0, :], ps[:, 1, :])                            # [7][18]
         denp = np.asarray(denp, dtype=np.float64)
-        out = {"exact_particle_order_labels": list(self._ORDER_LABELS), "exact_particle_order_scores": order,
+        mh = np.asarray(tot["path_mask_hits"], dtype=np.float64)        # [side][mask][channel]
+        ah = np.asarray(tot["acrylic_order_hits"], dtype=np.float64)    # [side][order][channel]
+        masks, acr = sym(mh[0], mh[1]), sym(ah[0], ah[1])
+        # event-history mask scores and their fractions of the hard-aperture score (:8968-8977)
+        out = {"hardware_symmetry_scores": denp.copy()}
+        path = {}
+        for k, name in enumerate(abi.PATH_MASK_NAMES):
+            path[name] = masks[k]
+            out[name + "_scores"] = masks[k].copy()
+            out[name + "_fraction"] = np.divide(masks[k], denp, out=np.zeros_like(denp), where=denp > 0)
+        out["interaction_order_partition_closure_error_scores"] = path["any_particle"] - (
+            path["single_interaction"] + path["interaction_order_2"] + path["interaction_order_3"]
+            + path["interaction_order_4plus"])
+        out["multiple_branch_partition_closure_error_scores"] = path["multiple_interaction"] - (
+            path["mixed_geometric_wave"] + path["geometric_only_multiple"] + path["wave_only_multiple"])
+        out["single_branch_partition_closure_error_scores"] = path["single_interaction"] - (
+            path["single_external_entry_reflection_escape"] + path["single_internal_reflection_escape"]
+            + path["single_surface_transmission_escape"] + path["single_coherent_wave_escape"])
+        out["acrylic_reflection_order_labels"] = ["0", "1", "2", "3", "4+"]
+        out["acrylic_reflection_order_scores"] = acr
+        out["acrylic_reflection_order_partition_closure_error_scores"] = denp - acr.sum(axis=0)
+        out.update({"exact_particle_order_labels": list(self._ORDER_LABELS), "exact_particle_order_scores": order,
                "exact_geometric_order_labels": list(self._ORDER_LABELS), "exact_geometric_order_scores": gorder,
                "exact_particle_order_partition_closure_error_scores": denp - order.sum(axis=0),
-               "exact_geometric_order_partition_closure_error_scores": denp - gorder.sum(axis=0)}
+               "exact_geometric_order_partition_closure_error_scores": denp - gorder.sum(axis=0)})
         for k, key in enumerate(self._MEAN_KEYS):
             out[key] = np.divide(sums[k], denp, out=np.full(denp.shape, np.nan), where=denp > 0)
         cond = self.config.particle_event_model in ("hybrid_mie_exact_rate", "hybrid_mie_exact_rate_moment_constrained")
@@ -752,6 +785,58 @@ class ClaritasForwardModel:
         out["closure"] = ("Mie extinction and terminal outcomes; conditional finite-particle angular/path law"
                           if cond else self.config.particle_event_model + "; configured unconditional event law")
         out["conditional_max_trials"] = 16384
+        if prov is not None:
+            out.update(self._provenance_diagnostics(prov, denp, path["any_particle"], sym))
+        return out
+
+    def _provenance_diagnostics(self, pv: dict, denp: np.ndarray, any_particle: np.ndarray, sym) -> dict:
+        """The reference's causal outputs of the path diagnostics (CLARITAS.py:9008-9091, :9135-9150)."""
+        npart = int(np.asarray(self._physics["radius"]).size)
+
+        def nan_div(a, b):
+            return np.divide(a, b, out=np.full(np.shape(a), np.nan), where=b > 0)
+
+        def frac(a):
+            return np.divide(a, denp, out=np.zeros_like(a, dtype=np.float64), where=denp > 0)
+        out = {}
+        bh = np.asarray(pv["bin_hits"], dtype=np.float64)                 # [kind][side][bin][channel]
+        for k, name in enumerate(abi.PROVENANCE_BIN_NAMES):
+            out[name + "_scores"] = sym(bh[k, 0], bh[k, 1])[:npart]
+        for name in ("first_particle_bin", "last_particle_bin"):
+            out[name + "_partition_closure_error_scores"] = any_particle - out[name + "_scores"].sum(axis=0)
+        ft = np.asarray(pv["first_type_hits"], dtype=np.float64)
+        lt = np.asarray(pv["last_type_hits"], dtype=np.float64)
+        las = np.asarray(pv["last_type_angle_sum"], dtype=np.float64)
+        lac = np.asarray(pv["last_type_angle_count"], dtype=np.float64)
+        first_all, last_all = np.zeros_like(denp), np.zeros_like(denp)
+        for code, name in abi.PARTICLE_EVENT_TYPE_NAMES.items():
+            last, first = sym(lt[0, code], lt[1, code]), sym(ft[0, code], ft[1, code])
+            out[f"last_event_{name}_scores"], out[f"last_event_{name}_fraction"] = last, frac(last)
+            out[f"first_event_{name}_scores"], out[f"first_event_{name}_fraction"] = first, frac(first)
+            out[f"last_event_{name}_mean_deflection_deg_by_channel"] = nan_div(
+                sym(las[0, code], las[1, code]), sym(lac[0, code], lac[1, code]))
+            first_all, last_all = first_all + first, last_all + last
+        for key, field in (("first_event_backscatter", "first_backscatter_hits"),
+                           ("first_event_source_hemisphere", "first_source_hemisphere_hits")):
+            a = np.asarray(pv[field], dtype=np.float64)
+            out[key + "_scores"] = sym(a[0], a[1])
+            out[key + "_fraction"] = frac(out[key + "_scores"])
+        for which in ("first", "last"):
+            a = np.asarray(pv[which + "_angle_sum"], dtype=np.float64)
+            c = np.asarray(pv[which + "_angle_count"], dtype=np.float64)
+            out[f"mean_{which}_particle_deflection_deg_by_channel"] = nan_div(sym(a[0], a[1]), sym(c[0], c[1]))
+        out["causal_last_event_partition_closure_error_scores"] = any_particle - last_all
+        out["causal_first_event_partition_closure_error_scores"] = any_particle - first_all
+        out["H170_last_event_angle_bin_edges_deg"] = np.asarray([0.0, 30.0, 60.0, 90.0, 120.0, 150.0, 180.0001])
+        h = np.asarray(pv["h170_last_angle_hits"], dtype=np.float64)
+        out["H170_last_event_angle_histogram_scores_by_event_code"] = sym(h[0], h[1])
+        h = np.asarray(pv["h170_first_angle_hits"], dtype=np.float64)
+        out["H170_first_event_angle_histogram_scores"] = sym(h[0], h[1])
+        w = np.asarray(pv["wall_hits"], dtype=np.float64)
+        out["wall_path_scores"] = {name: sym(w[0, k], w[1, k]) for k, name in enumerate(abi.WALL_PATH_NAMES)}
+        out["wall_path_partition_closure_error_scores"] = denp - sum(out["wall_path_scores"].values())
+        a = np.asarray(pv["after_return_hits"], dtype=np.float64)
+        out["particle_after_acrylic_return_scores"] = sym(a[0], a[1])
         return out
 
     def close(self):

@@ -74,6 +74,9 @@ def load(build_if_missing: bool = False):
                                          P(C.c_double)], C.c_int),
             "clr_set_light_diagnostics": ([C.c_void_p, P(abi.LightConfig)], C.c_int),
             "clr_read_light_diagnostics": ([C.c_void_p, P(abi.LightResult)], C.c_int),
+            "clr_set_path_provenance": ([C.c_void_p, C.c_int], C.c_int),
+            "clr_read_path_provenance": ([C.c_void_p, P(abi.PathProvenance)], C.c_int),
+            "clr_read_path_provenance_records": ([C.c_void_p, C.c_void_p, C.c_int64], C.c_int),
         }
         for name, (argt, rest) in sig.items():
             f = getattr(lib, name)
@@ -90,7 +93,31 @@ def exported_symbols() -> list[str]:
             "clr_sweep_trace", "clr_sweep_read_particle_physics", "clr_mlp_create", "clr_mlp_destroy",
             "clr_mlp_last_error", "clr_mlp_set_params", "clr_mlp_get_params", "clr_mlp_forward", "clr_mlp_gradients",
             "clr_mlp_train", "clr_mlp_last_ms", "clr_bf16_gemm_n256", "clr_read_sediment_field",
-            "clr_set_light_diagnostics", "clr_read_light_diagnostics"]
+            "clr_set_light_diagnostics", "clr_read_light_diagnostics", "clr_set_path_provenance",
+            "clr_read_path_provenance", "clr_read_path_provenance_records"]
+
+
+def decode_provenance(raw):
+    """Unpack clr_read_path_provenance_records words into the reference's per-ray provenance columns."""
+    import numpy as np
+    raw = np.asarray(raw, np.uint32)
+    x, y = raw[:, 0], raw[:, 1]
+    prov = np.zeros((raw.shape[0], 13), np.int32)
+
+    def byte(v, k):
+        b = ((v >> (8 * k)) & 0xFF).astype(np.int32)
+        return np.where(b == 0xFF, -1, b)
+    prov[:, 0] = (y >> 16) & 0xF
+    prov[:, 1] = (y >> 20) & 0xF
+    prov[:, 2] = -1
+    prov[:, 3] = (y >> 24) & 1
+    prov[:, 4] = (y >> 25) & 1
+    prov[:, 5], prov[:, 6], prov[:, 7], prov[:, 8] = byte(x, 0), byte(x, 1), byte(x, 2), byte(x, 3)
+    prov[:, 9], prov[:, 10] = byte(y, 0), byte(y, 1)
+    prov[:, 11] = (y >> 26) & 1
+    prov[:, 12] = (y >> 27) & 1
+    defl = raw[:, 2:4].copy().view(np.float32)
+    return prov, defl
 
 
 class Context:
@@ -172,6 +199,28 @@ class Context:
             a[k] = getattr(r, k)
         a["first_outside_xyz_tol"] = list(r.first_outside_xyz_tol)
         return a
+
+    def set_provenance(self, enabled: bool):
+        """Count the particle-event provenance partitions of detected rays in the following traces (each
+        trace call resets them; the wavefront engine counts them)."""
+        self._check(self.lib.clr_set_path_provenance(self.h, int(bool(enabled))), "clr_set_path_provenance")
+
+    def read_provenance(self) -> dict:
+        """The provenance partitions of the last trace call (arrays indexed [.., side, ..], side 0 native)."""
+        p = abi.PathProvenance()
+        self._check(self.lib.clr_read_path_provenance(self.h, C.byref(p)), "clr_read_path_provenance")
+        return p.as_dict()
+
+    def read_provenance_records(self, n_rays: int):
+        """Per-ray provenance of the last trace with records, decoded: int32 [n][13] in the reference's
+        order (first/last event type, last order (not kept: -1), first backscatter, first source hemisphere,
+        first/last particle, geometric and wave bin (-1 none), acrylic return, particle after a return) and
+        float32 [n][2] first/last deflection."""
+        import numpy as np
+        raw = np.zeros((int(n_rays), 4), np.uint32)
+        self._check(self.lib.clr_read_path_provenance_records(self.h, raw.ctypes.data_as(C.c_void_p), int(n_rays)),
+                    "clr_read_path_provenance_records")
+        return decode_provenance(raw)
 
     def trace(self, run: abi.RunParams, records: bool = False):
         import numpy as np

@@ -70,3 +70,66 @@ def test_registered_material_takes_weights_on_its_grid():
     np.testing.assert_array_equal(p.weight, [1, 2, 3, 4, 5])
     with pytest.raises(ValueError, match="weights must have 5 entries"):
         m._particles("sand", 0.5, [1, 2], "mass_fraction")
+
+
+def test_path_diagnostics_report_every_partition():
+    """The facade turns the device partitions into the reference's path-diagnostics keys: mask scores and
+    fractions of the hard-aperture score, the closure errors, acrylic-reflection order (CLARITAS.py:8968-9161)."""
+    from tardiis_and_claritas_gb300 import abi
+    rng = np.random.default_rng(1)
+    m = F.ClaritasForwardModel()
+    tot = {"order_hits": rng.integers(0, 50, (2, 6, 18)), "geometric_order_hits": rng.integers(0, 50, (2, 6, 18)),
+           "path_sums": rng.integers(0, 50, (abi.N_PATH_SUMS, 2, 18)),
+           "path_mask_hits": rng.integers(0, 50, (2, abi.N_PATH_MASKS, 18)),
+           "acrylic_order_hits": rng.integers(0, 50, (2, 5, 18)), "conditional_stats": np.zeros(10, np.uint64)}
+    denp = 0.5 * (tot["order_hits"][0] + tot["order_hits"][1]).sum(axis=0)
+    denp[3] = 0.0
+    pd = m._path_diagnostics(tot, denp, True)
+    mask = 0.5 * (tot["path_mask_hits"][0] + tot["path_mask_hits"][1])
+    for k, name in enumerate(abi.PATH_MASK_NAMES):
+        np.testing.assert_array_equal(pd[name + "_scores"], mask[k])
+        assert pd[name + "_fraction"][3] == 0.0
+    i = abi.PATH_MASK_NAMES.index
+    np.testing.assert_allclose(pd["interaction_order_partition_closure_error_scores"],
+                               mask[i("any_particle")] - mask[[i("single_interaction"), i("interaction_order_2"),
+                                                              i("interaction_order_3"),
+                                                              i("interaction_order_4plus")]].sum(axis=0))
+    acr = 0.5 * (tot["acrylic_order_hits"][0] + tot["acrylic_order_hits"][1])
+    np.testing.assert_array_equal(pd["acrylic_reflection_order_scores"], acr)
+    np.testing.assert_allclose(pd["acrylic_reflection_order_partition_closure_error_scores"], denp - acr.sum(axis=0))
+    assert pd["acrylic_reflection_order_labels"] == ["0", "1", "2", "3", "4+"]
+    native = m._path_diagnostics(tot, denp, False)
+    np.testing.assert_array_equal(native["any_wave_scores"], tot["path_mask_hits"][0][i("any_wave")])
+
+
+def test_provenance_diagnostics_from_device_partitions():
+    """The causal outputs of the path diagnostics (CLARITAS.py:9008-9091, :9135-9150) from the device's
+    provenance partitions: bin scores cut to the material's bins, per-type scores and fractions, closures."""
+    from tardiis_and_claritas_gb300 import abi
+    rng = np.random.default_rng(2)
+    m = F.ClaritasForwardModel()
+    m._physics = {"radius": np.zeros(5)}
+    pv = {"bin_hits": np.zeros((6, 2, 64, 18), np.int64), "first_type_hits": rng.integers(0, 9, (2, 8, 18)),
+          "last_type_hits": rng.integers(0, 9, (2, 8, 18)), "wall_hits": rng.integers(0, 9, (2, 3, 18)),
+          "after_return_hits": rng.integers(0, 9, (2, 18)), "first_backscatter_hits": rng.integers(0, 9, (2, 18)),
+          "first_source_hemisphere_hits": rng.integers(0, 9, (2, 18)),
+          "first_angle_sum": rng.uniform(0, 90, (2, 18)), "first_angle_count": rng.integers(0, 3, (2, 18)),
+          "last_angle_sum": rng.uniform(0, 90, (2, 18)), "last_angle_count": rng.integers(0, 3, (2, 18)),
+          "last_type_angle_sum": rng.uniform(0, 90, (2, 8, 18)), "last_type_angle_count": rng.integers(0, 3, (2, 8, 18)),
+          "h170_last_angle_hits": rng.integers(0, 9, (2, 8, 6)), "h170_first_angle_hits": rng.integers(0, 9, (2, 6))}
+    pv["bin_hits"][0, :, :5] = rng.integers(0, 9, (2, 5, 18))
+    sym = lambda a, b: 0.5 * (a + b)  # noqa: E731
+    denp = rng.uniform(50, 100, 18)
+    anyp = sym(pv["bin_hits"][0, 0], pv["bin_hits"][0, 1]).sum(axis=0)
+    out = m._provenance_diagnostics(pv, denp, anyp, sym)
+    assert out["first_particle_bin_scores"].shape == (5, 18)
+    assert np.all(out["first_particle_bin_partition_closure_error_scores"] == 0.0)
+    for code, name in abi.PARTICLE_EVENT_TYPE_NAMES.items():
+        want = sym(pv["last_type_hits"][0, code], pv["last_type_hits"][1, code])
+        np.testing.assert_array_equal(out[f"last_event_{name}_scores"], want)
+        np.testing.assert_allclose(out[f"last_event_{name}_fraction"], want / denp)
+    cnt = sym(pv["first_angle_count"][0], pv["first_angle_count"][1])
+    mean = out["mean_first_particle_deflection_deg_by_channel"]
+    assert np.all(np.isnan(mean[cnt == 0])) and np.all(np.isfinite(mean[cnt > 0]))
+    assert set(out["wall_path_scores"]) == set(abi.WALL_PATH_NAMES)
+    assert out["H170_last_event_angle_histogram_scores_by_event_code"].shape == (8, 6)
