@@ -30,12 +30,9 @@ __device__ __forceinline__ unsigned prov_set_byte(unsigned v, int k, unsigned b)
     return (v & ~(0xFFu << (8 * k))) | ((b & 0xFFu) << (8 * k));
 }
 
-// A particle event that the photon survived: bin pidx, type code (1..7), interaction count ic including
-// this event, direction before (vin) and after (v) the event (:4966-4979).
-__device__ __forceinline__ void prov_event(uint4& p, int ic, int type, int pidx, float vinx, float viny, float vinz,
-                                           float vx, float vy, float vz) {
-    const float dcos = fminf(fmaxf(o_dot(vinx, viny, vinz, vx, vy, vz), -1.0f), 1.0f);
-    const float defl = acosf(dcos) * (180.0f / CLR_PI_F);
+// The bins, types and return flag of a particle event of bin pidx, type code (1..7), with interaction
+// count ic including this event.
+__device__ __forceinline__ void prov_mark(uint4& p, int ic, int type, int pidx) {
     const unsigned b = (unsigned)pidx;
     if (prov_byte(p.x, 0) == 0xFFu) p.x = prov_set_byte(p.x, 0, b);
     p.x = prov_set_byte(p.x, 1, b);
@@ -48,10 +45,18 @@ __device__ __forceinline__ void prov_event(uint4& p, int ic, int type, int pidx,
     }
     if (p.y & kProvReturn) p.y |= kProvAfter;
     p.y = (p.y & ~(0xFu << 20)) | ((unsigned)type << 20);
+    if (ic == 1) p.y = (p.y & ~(0xFu << 16)) | ((unsigned)type << 16);
+}
+
+// A particle event that the photon survived, with its direction before (vin) and after (v) (:4966-4979).
+__device__ __forceinline__ void prov_event(uint4& p, int ic, int type, int pidx, float vinx, float viny, float vinz,
+                                           float vx, float vy, float vz) {
+    const float dcos = fminf(fmaxf(o_dot(vinx, viny, vinz, vx, vy, vz), -1.0f), 1.0f);
+    const float defl = acosf(dcos) * (180.0f / CLR_PI_F);
+    prov_mark(p, ic, type, pidx);
     p.w = __float_as_uint(defl);
     if (ic == 1) {
-        p.y = (p.y & ~((0xFu << 16) | kProvBack | kProvHemi)) | ((unsigned)type << 16) |
-              (dcos < 0.0f ? kProvBack : 0u) | (vy < 0.0f ? kProvHemi : 0u);
+        p.y = (p.y & ~(kProvBack | kProvHemi)) | (dcos < 0.0f ? kProvBack : 0u) | (vy < 0.0f ? kProvHemi : 0u);
         p.z = __float_as_uint(defl);
     }
 }

@@ -338,6 +338,11 @@ __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevSce
             return WQ_COND;
         }
         if (v == 0) survived();
+        // an absorbing encounter of the closure ends the history; the reference keeps its bin and type
+        // (not a deflection) (:4836-4848)
+        if (v == 1 && pv && r.st == 5 && r.ic == ic0)
+            prov_mark(*pv, r.ic, prov_type(r.wcoh - coh0, r.wmorph - mor0, r.pc.entry_reflections - per0,
+                                           r.pc.internal_reflections - pir0), m.pidx);
         return v ? WQ_FIN : WQ_FLIGHT;
     } else if constexpr (Q == WQ_MORPH) {
         const int per0 = r.pc.entry_reflections, pir0 = r.pc.internal_reflections;

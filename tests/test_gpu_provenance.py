@@ -103,8 +103,11 @@ def test_provenance_per_ray_equals_reference(ctx, gold, name):
     got = prov.copy()
     cols = [c for c in range(13) if c != PP.LAST_ORDER]  # the device does not keep the last event's order
     np.testing.assert_array_equal(got[same][:, cols], want[same][:, cols], err_msg=name)
+    # deflections: the directions agree to a few ulp between the host's libm and the device's math, and near
+    # forward scattering acos turns one ulp of cos (6e-8) into ~0.02 deg
     wd = z[f"{name}/ray_defl"]
-    np.testing.assert_allclose(defl[same], wd[same], rtol=2e-6, atol=2e-4, err_msg=name)
+    np.testing.assert_allclose(defl[same], wd[same], rtol=1e-5, atol=0.05, err_msg=name)
+    assert np.mean(np.abs(defl[same] - wd[same]) <= 1e-4) > 0.99
     assert (want[same][:, PP.LAST_TYPE] > 0).sum() > 500  # enough rays with particle events
 
 
