@@ -107,7 +107,7 @@ def test_provenance_per_ray_equals_reference(ctx, gold, name):
     # forward scattering acos turns one ulp of cos (6e-8) into ~0.02 deg
     wd = z[f"{name}/ray_defl"]
     np.testing.assert_allclose(defl[same], wd[same], rtol=1e-5, atol=0.05, err_msg=name)
-    assert np.mean(np.abs(defl[same] - wd[same]) <= 1e-4) > 0.99
+    assert np.mean(np.abs(defl[same] - wd[same])) < 1e-3
     assert (want[same][:, PP.LAST_TYPE] > 0).sum() > 500  # enough rays with particle events
 
 
