@@ -466,27 +466,29 @@ __global__ void __launch_bounds__(kWaveThreads) wave_fin_kernel(WaveLaunch w) {
 }
 
 // ---------------- TAIL: the last photons, each run to its end by one thread ----------------
-template <class Mode>
+// kDiag: the stage bodies with the diagnostic hooks (light history, provenance); the production tail
+// carries none of them.
+template <class Mode, bool kDiag>
 __device__ __forceinline__ int tail_visit(const WaveLaunch& w, int q, const DevScene& D, Ray& r,
                                           typename Mode::Lane& L, SlotMeta& m, unsigned long long* cstats,
                                           uint4* pv) {
     switch (q) {
-        case WQ_ENTRY: return wave_stage_body<Mode, WQ_ENTRY>(w, D, r, L, m, cstats, pv);
-        case WQ_FLIGHT: return wave_stage_body<Mode, WQ_FLIGHT>(w, D, r, L, m, cstats, pv);
-        case WQ_COND: return wave_stage_body<Mode, WQ_COND>(w, D, r, L, m, cstats, pv);
-        case WQ_GEOM: return wave_stage_body<Mode, WQ_GEOM>(w, D, r, L, m, cstats, pv);
-        case WQ_MORPH: return wave_stage_body<Mode, WQ_MORPH>(w, D, r, L, m, cstats, pv);
-        case WQ_TOP: return wave_stage_body<Mode, WQ_TOP>(w, D, r, L, m, cstats, pv);
-        case WQ_BOTTOM: return wave_stage_body<Mode, WQ_BOTTOM>(w, D, r, L, m, cstats, pv);
-        case WQ_SIDE: return wave_stage_body<Mode, WQ_SIDE>(w, D, r, L, m, cstats, pv);
-        default: return wave_stage_body<Mode, WQ_ACRYL>(w, D, r, L, m, cstats, pv);
+        case WQ_ENTRY: return wave_stage_body<Mode, WQ_ENTRY, kDiag>(w, D, r, L, m, cstats, pv);
+        case WQ_FLIGHT: return wave_stage_body<Mode, WQ_FLIGHT, kDiag>(w, D, r, L, m, cstats, pv);
+        case WQ_COND: return wave_stage_body<Mode, WQ_COND, kDiag>(w, D, r, L, m, cstats, pv);
+        case WQ_GEOM: return wave_stage_body<Mode, WQ_GEOM, kDiag>(w, D, r, L, m, cstats, pv);
+        case WQ_MORPH: return wave_stage_body<Mode, WQ_MORPH, kDiag>(w, D, r, L, m, cstats, pv);
+        case WQ_TOP: return wave_stage_body<Mode, WQ_TOP, kDiag>(w, D, r, L, m, cstats, pv);
+        case WQ_BOTTOM: return wave_stage_body<Mode, WQ_BOTTOM, kDiag>(w, D, r, L, m, cstats, pv);
+        case WQ_SIDE: return wave_stage_body<Mode, WQ_SIDE, kDiag>(w, D, r, L, m, cstats, pv);
+        default: return wave_stage_body<Mode, WQ_ACRYL, kDiag>(w, D, r, L, m, cstats, pv);
     }
 }
 
 // Runs after the last pass, when every photon is drawn: the photons still queued (entries [snap, tail)
 // of every queue but FREE) are taken one per thread and carried through the same stage bodies, in the
 // same order, as the passes would carry them, then scored. Per-ray results are those of the passes.
-template <class Mode, bool kRecord>
+template <class Mode, bool kRecord, bool kDiag>
 __global__ void __launch_bounds__(kTailThreads) wave_tail_kernel(WaveLaunch w) {
     __shared__ DetTable det;
     det_table_init(&det);
@@ -509,14 +511,18 @@ __global__ void __launch_bounds__(kTailThreads) wave_tail_kernel(WaveLaunch w) {
         unsigned long long* cstats = w.tallies[m.sid].c.cstats;
         uint4 pvv = prov_init();
         uint4* pv = nullptr;
-        if (w.prov) { pvv = w.prov[slot]; pv = &pvv; }
+        if constexpr (kDiag) {
+            if (w.prov) { pvv = w.prov[slot]; pv = &pvv; }
+        }
         while (q != WQ_FIN) {
             ++visits[q];
-            q = tail_visit<Mode>(w, q, D, r, L, m, cstats, pv);
+            q = tail_visit<Mode, kDiag>(w, q, D, r, L, m, cstats, pv);
         }
         ++visits[WQ_FIN];
         finish_ray<Mode>(D, det, r, m.gid, m.sid, -1, nullptr, w.tallies, kRecord ? w.records + m.rid : nullptr, pv);
-        if (kRecord && w.prov_rec) w.prov_rec[m.rid] = pvv;
+        if constexpr (kDiag) {
+            if (kRecord && w.prov_rec) w.prov_rec[m.rid] = pvv;
+        }
     }
     for (int q = 1; q < CLR_WQ_COUNT; ++q)
         if (visits[q]) atomicAdd(&w.tallies[0].sched[q], visits[q]);
@@ -649,7 +655,8 @@ cudaError_t wave_run_t(const WaveLaunch& w, int num_sms, cudaStream_t st, long l
             // at most live[2] photons remain after the passes already queued: finish them in one launch
             const unsigned n = live[2];
             const int blocks = (int)std::max(1u, std::min(n, 65536u * kTailThreads) / kTailThreads + 1);
-            wave_tail_kernel<Mode, kRecord><<<blocks, kTailThreads, 0, st>>>(w);
+            if (w.light || w.prov) wave_tail_kernel<Mode, kRecord, true><<<blocks, kTailThreads, 0, st>>>(w);
+            else wave_tail_kernel<Mode, kRecord, false><<<blocks, kTailThreads, 0, st>>>(w);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             launched += 1;
             break;
