@@ -389,43 +389,45 @@ class ClaritasForwardModel:
         ctx = self._context()
         prov = bool(path_provenance)
         ctx.set_provenance(prov)
-        batch = int(cfg.statistics_batch_rays)
-        sizes = []
-        left = max_n
-        while left > 0:
-            sizes.append(min(batch, left))
-            left -= sizes[-1]
-        # Batches are traced in groups through one clr_trace_batch call; a fixed-count run is one group.
-        group = len(sizes) if not adaptive else max(1, min(len(sizes), 64))
-        if adaptive and (light is not None or prov):
-            group = 1  # diagnostics accumulate over traced batches: trace no batch past the stopping one
-        tallies = []
-        prov_parts = []
-        stop_at = None
-        state = _StopState()
-        start = 0
-        while start < len(sizes) and stop_at is None:
-            runs = []
-            off = ray_id_start + sum(sizes[:start])
-            for k in range(start, min(start + group, len(sizes))):
-                runs.append(S.run_params(sizes[k], seed=seed, ray_offset=off, rng_mode=self.rng_mode))
-                off += sizes[k]
-            got = ctx.trace_batch(runs)
-            if prov:
-                prov_parts.append(ctx.read_provenance())
-            for t in got:
-                tallies.append(t)
-                if adaptive and state.after_batch(self, t, min_n, target, rear_target, h170_target,
-                                                  stability_l1_tolerance, stability_window):
-                    stop_at = len(tallies)
-                    break
-            start += group
-        if stop_at is not None:
-            tallies = tallies[:stop_at]
-            stop_reason = state.reason
-        else:
-            stop_reason = state.final_reason(adaptive, target, rear_target, h170_target, stability_l1_tolerance)
-        ctx.set_provenance(False)
+        try:
+            batch = int(cfg.statistics_batch_rays)
+            sizes = []
+            left = max_n
+            while left > 0:
+                sizes.append(min(batch, left))
+                left -= sizes[-1]
+            # Batches are traced in groups through one clr_trace_batch call; a fixed-count run is one group.
+            group = len(sizes) if not adaptive else max(1, min(len(sizes), 64))
+            if adaptive and (light is not None or prov):
+                group = 1  # diagnostics accumulate over traced batches: trace no batch past the stopping one
+            tallies = []
+            prov_parts = []
+            stop_at = None
+            state = _StopState()
+            start = 0
+            while start < len(sizes) and stop_at is None:
+                runs = []
+                off = ray_id_start + sum(sizes[:start])
+                for k in range(start, min(start + group, len(sizes))):
+                    runs.append(S.run_params(sizes[k], seed=seed, ray_offset=off, rng_mode=self.rng_mode))
+                    off += sizes[k]
+                got = ctx.trace_batch(runs)
+                if prov:
+                    prov_parts.append(ctx.read_provenance())
+                for t in got:
+                    tallies.append(t)
+                    if adaptive and state.after_batch(self, t, min_n, target, rear_target, h170_target,
+                                                      stability_l1_tolerance, stability_window):
+                        stop_at = len(tallies)
+                        break
+                start += group
+            if stop_at is not None:
+                tallies = tallies[:stop_at]
+                stop_reason = state.reason
+            else:
+                stop_reason = state.final_reason(adaptive, target, rear_target, h170_target, stability_l1_tolerance)
+        finally:
+            ctx.set_provenance(False)
         prov_total = None
         if prov_parts:
             prov_total = {k: np.sum([q[k] for q in prov_parts], axis=0) for k in prov_parts[0]}
