@@ -8,9 +8,10 @@
  *   transport   trace_kernel :4551-5104
  *   detectors   score_detectors_kernel :4378-4436 and helpers :4237-4376
  * The physics helpers live in oracle_transport_a.h / oracle_transport_b.h.
- * Observational outputs of the reference that never feed a transport decision
- * (light-history grids, heatmaps, the particle_diag_* and deflection arrays)
- * are not restated. Built with -ffp-contract=off (oracle/Makefile).
+ * Of the observational outputs of the reference that never feed a transport decision, the per-ray
+ * provenance (first/last bin, event type and deflection, acrylic returns; clo_trace_provenance) is
+ * restated; the light-history grids, heatmaps, the particle_diag_* arrays and the remaining per-ray
+ * histories are not. Built with -ffp-contract=off (oracle/Makefile).
  */
 #define _GNU_SOURCE
 #include "claritas_oracle.h"
@@ -884,7 +885,25 @@ typedef struct {
     o_pcount pc;
     int steps, nulls;
     float wp, ap, ax, ay, az, avx, avy, avz;
+    /* particle-event provenance (:4625-4633): first/last event type and order, first-event backscatter and
+       source hemisphere, first/last particle, geometric and wave bin, acrylic returns after a particle
+       event and particle events after such a return, first/last deflection */
+    int first_evt, last_evt, last_order, first_back, first_hemi, bins[6], acr_returns, after_return;
+    float first_defl, last_defl;
 } o_ray;
+
+/* The bins and types of a particle event of type `type` in bin `pidx` (:4836-4848 for an absorbed
+   conditional encounter, :4972-4978 for a survived event). */
+static void o_prov_mark(o_ray* r, int type, int pidx) {
+    if (r->bins[0] < 0) r->bins[0] = pidx;
+    r->bins[1] = pidx;
+    if (type >= 1 && type <= 3) { if (r->bins[2] < 0) r->bins[2] = pidx; r->bins[3] = pidx; }
+    else if (type >= 4 && type <= 7) { if (r->bins[4] < 0) r->bins[4] = pidx; r->bins[5] = pidx; }
+    if (r->acr_returns > 0) r->after_return++;
+    if (r->ic == 1) r->first_evt = type;
+    r->last_evt = type;
+    r->last_order = r->ic;
+}
 
 static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32_t seed1, uint32_t seed2,
                         unsigned long long* cstats, o_ray* out) {
@@ -892,6 +911,8 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
     o_ray r;
     memset(&r, 0, sizeof r);
     r.ax = r.ay = r.az = r.avx = r.avy = r.avz = NAN;
+    for (int k = 0; k < 6; ++k) r.bins[k] = -1;
+    r.first_defl = r.last_defl = -1.0f;
     uint32_t state = seed0 + gid * 74729u + 13u, stOPT = seed1 + gid * 104729u + 29u, stSRC = seed2 + gid * 130363u + 43u;
     const int TM = P->sediment_model, FSM = P->free_surface_model;
     const float RIN = P->rin, ZMIN = P->zmin, ZMEAN = P->zmean, ZTOP = P->zwall_top, DH = P->vortex_delta_h,
@@ -1045,7 +1066,8 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
             }
             r.ic++;
             const float vinx = vx, viny = vy, vinz = vz;
-            int event_pidx = -1;
+            const int per0 = r.pc.entry_reflections, pir0 = r.pc.internal_reflections;
+            int event_pidx = -1, event_type = 0;
             float ipath = 0.0f;
             int use_wave = (LOCAL_WAVE > 0.0f && o_uniform(&state) * LOCAL_TOTAL >= LOCAL_GEOM);
             int sel = -1;
@@ -1069,7 +1091,8 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
                 r.pc.internal_reflections += h.pc.internal_reflections; r.pc.absorptions += h.pc.absorptions;
                 if (h.channel == 0) r.gic++;
                 else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
-                if (h.status == 2) { st = 5; break; }
+                event_type = h.event_type;
+                if (h.status == 2) { o_prov_mark(&r, event_type, sel); st = 5; break; }
             } else if (use_wave) {
                 if (COND) cstats[0]++;
                 r.wic++;
@@ -1082,6 +1105,7 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
                     r.wcoh++;
                     o_mie_direction(&stOPT, S->phase_cdf, S->theta, S->nt, pidx, &vx, &vy, &vz);
                     if (COND) { cstats[4]++; cstats[7]++; }
+                    event_type = 4;
                 } else {
                     r.wmorph++;
                     float fr = sqrtf(x * x + y * y);
@@ -1095,6 +1119,7 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
                     if (ps == 2) { st = 5; break; }
                     if (ps != 1) { if (COND) cstats[8]++; r.pf = ppc ? ppc : OP_OTHER; r.pfs = pps; st = 4; break; }
                     if (COND) { cstats[5]++; cstats[7]++; }
+                    event_type = (r.pc.entry_reflections > per0) ? 5 : ((r.pc.internal_reflections > pir0) ? 7 : 6);
                 }
             } else {
                 if (COND) cstats[0]++;
@@ -1124,6 +1149,7 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
                     r.gic--;
                     if (h.channel == 0) r.gic++;
                     else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
+                    event_type = h.event_type;
                 } else {
                     if (!accessible) { r.ic--; r.gic--; r.nulls++; continue; }
                     int ppc = 0, pps = 0, pmb = 0, pmo = 0;
@@ -1133,10 +1159,19 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
                     if (ps == 2) { st = 5; break; }
                     if (ps != 1) { if (COND) cstats[8]++; r.pf = ppc ? ppc : OP_OTHER; r.pfs = pps; st = 4; break; }
                     if (COND) { cstats[3]++; cstats[7]++; }
+                    event_type = (r.pc.entry_reflections > per0) ? 1 : ((r.pc.internal_reflections > pir0) ? 3 : 2);
                 }
             }
             if (event_pidx >= 0 && S->moment_mode[event_pidx])
                 o_moment(vinx, viny, vinz, &vx, &vy, &vz, (float)S->moment_a[event_pidx], (float)S->moment_b[event_pidx]);
+            /* provenance of the survived event (:4949-4979) */
+            {
+                const float dcos = fminf(fmaxf(o_dot(vinx, viny, vinz, vx, vy, vz), -1.0f), 1.0f);
+                const float defl = acosf(dcos) * (180.0f / O_PI_F);
+                o_prov_mark(&r, event_type, event_pidx);
+                r.last_defl = defl;
+                if (r.ic == 1) { r.first_defl = defl; r.first_back = dcos < 0.0f; r.first_hemi = vy < 0.0f; }
+            }
             continue;
         }
         if (axial) {
@@ -1159,7 +1194,7 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
                 x -= O_EPS_F * snx; y -= O_EPS_F * sny; z -= O_EPS_F * snz;
                 int hs = 0, hb = 0;
                 int hw = o_headspace(&state, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
-                if (hw == 1) continue;
+                if (hw == 1) { if (r.ic > 0) r.acr_returns++; continue; }
                 if (hw == 2) { st = 1; goto air_exit; }
                 if (hw == 3) { st = 7; goto done; }
                 if (hw == 4) { st = 6; goto done; }
@@ -1167,14 +1202,14 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
             } else {
                 int bs = 0, bb = 0;
                 int where = o_bottom_disc(&state, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &bs, &bb);
-                if (where == 1) continue;
+                if (where == 1) { if (r.ic > 0) r.acr_returns++; continue; }
                 if (where == 2) { st = 1; goto air_exit; }
                 if (where == 3) { st = 7; break; }
                 if (where == 5) { st = 8; break; }
                 if (where == 4) {
                     int hs = 0, hb = 0;
                     int hw = o_headspace(&state, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
-                    if (hw == 1) continue;
+                    if (hw == 1) { if (r.ic > 0) r.acr_returns++; continue; }
                     if (hw == 2) { st = 1; goto air_exit; }
                     if (hw == 3) { st = 7; goto done; }
                     if (hw == 4) { st = 6; goto done; }
@@ -1202,14 +1237,14 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
             int sub = 0, nb = 0;
             int where = o_acrylic_solid(&state, &C, C.n_air, C.n_bottom_ext, ZMIN, C.Zlow, &x, &y, &z, &vx, &vy, &vz,
                                         &r.ap, &bc, &sub, &nb);
-            if (where == 1) continue;
+            if (where == 1) { if (r.ic > 0) r.acr_returns++; continue; }
             if (where == 2) { st = 1; goto air_exit; }
             if (where == 3) { st = 7; break; }
             if (where == 5) { st = 8; break; }
             if (where == 4) {
                 int hs = 0, hb = 0;
                 int hw = o_headspace(&state, &C, &x, &y, &z, &vx, &vy, &vz, &r.ap, &bc, &hs, &hb);
-                if (hw == 1) continue;
+                if (hw == 1) { if (r.ic > 0) r.acr_returns++; continue; }
                 if (hw == 2) { st = 1; goto air_exit; }
                 if (hw == 3) { st = 7; goto done; }
                 if (hw == 4) { st = 6; goto done; }
@@ -1430,7 +1465,20 @@ static void tally_merge(clr_tallies* dst, const clr_tallies* src) {
     (void)d; (void)s;
 }
 
+static int trace_impl(clo_state* S, const clr_run_params* run, clr_tallies* T, clr_ray_record* records,
+                      int32_t* prov, float* defl, int n_threads);
+
 int clo_trace(clo_state* S, const clr_run_params* run, clr_tallies* T, clr_ray_record* records, int n_threads) {
+    return trace_impl(S, run, T, records, NULL, NULL, n_threads);
+}
+
+int clo_trace_provenance(clo_state* S, const clr_run_params* run, clr_tallies* T, clr_ray_record* records,
+                         int32_t* prov, float* defl, int n_threads) {
+    return trace_impl(S, run, T, records, prov, defl, n_threads);
+}
+
+static int trace_impl(clo_state* S, const clr_run_params* run, clr_tallies* T, clr_ray_record* records,
+                      int32_t* prov, float* defl, int n_threads) {
     if (!S || !run || !T) return -1;
     if (run->rng_mode != CLR_RNG_REFERENCE_XORSHIFT || run->weight_mode != CLR_WEIGHT_ANALOG) {
         snprintf(S->err, sizeof S->err, "the oracle restates xorshift streams and analog weights only");
@@ -1475,6 +1523,13 @@ int clo_trace(clo_state* S, const clr_run_params* run, clr_tallies* T, clr_ray_r
             rec->water_path = r.wp; rec->acrylic_path = r.ap;
             clr_tally_add_ray_stats(&L, rec);
             if (records) records[i] = tmp;
+            if (prov) {
+                const int32_t v[13] = {r.first_evt, r.last_evt, r.last_order, r.first_back, r.first_hemi, r.bins[0],
+                                       r.bins[1], r.bins[2], r.bins[3], r.bins[4], r.bins[5], r.acr_returns,
+                                       r.after_return};
+                memcpy(prov + i * 13, v, sizeof v);
+            }
+            if (defl) { defl[i * 2] = r.first_defl; defl[i * 2 + 1] = r.last_defl; }
         }
 #pragma omp critical
         {

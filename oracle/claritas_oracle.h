@@ -22,6 +22,12 @@ int clo_prepare(const clr_scene_params* scene, const clr_particle_spec* particle
                 clo_state** out);
 int clo_read_physics(clo_state* st, clr_particle_physics* out);
 int clo_n_theta(clo_state* st);
+/* as clo_trace, and per ray the provenance outputs of the reference (prov [n][13]: first/last event type,
+ * last event order, first backscatter, first source hemisphere, first/last particle, geometric and wave
+ * bin, acrylic returns after a particle event, particle events after a return; defl [n][2]: first/last
+ * deflection in degrees) */
+int clo_trace_provenance(clo_state* st, const clr_run_params* run, clr_tallies* out, clr_ray_record* records,
+                         int32_t* prov, float* defl, int n_threads);
 /* the sediment field [n_bins][nr][nz] of model 3 (solved or supplied) and the solver's iterations / residual */
 int clo_read_sediment_field(clo_state* st, double* grid, int* nr, int* nz, int* iterations, double* max_residual);
 int clo_trace(clo_state* st, const clr_run_params* run, clr_tallies* out, clr_ray_record* records, int n_threads);

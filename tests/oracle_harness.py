@@ -73,6 +73,9 @@ def load(kind: str = "port"):
         lib.clo_erfinv.argtypes = [C.c_double]
         lib.clo_erfinv.restype = C.c_double
         lib.clo_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        lib.clo_trace_provenance.argtypes = [C.c_void_p, C.POINTER(abi.RunParams), C.POINTER(abi.Tallies),
+                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        lib.clo_trace_provenance.restype = C.c_int
         prefix = "clo_"
     elif kind == "reference":
         if not reference_available():
@@ -136,7 +139,7 @@ class OracleRun:
         return T.as_dict(), rec
 
     def trace_provenance(self, run: abi.RunParams, threads: int = 0):
-        """Reference build only: tallies, per-ray records, and per ray the reference's provenance outputs
+        """Tallies, per-ray records, and per ray the reference's provenance outputs
         (int [n][13]: first/last event type, last event order, first backscatter, first source hemisphere,
         first/last particle, geometric and wave bin, acrylic returns after a particle event, particle events
         after a return) and deflections (float [n][2]: first, last)."""
@@ -145,11 +148,11 @@ class OracleRun:
         rec = np.zeros(n, dtype=abi.record_dtype())
         prov = np.zeros((n, 13), np.int32)
         defl = np.zeros((n, 2), np.float32)
-        rc = self.lib.clref_trace_provenance(self.h, C.byref(run), C.byref(T), rec.ctypes.data_as(C.c_void_p),
-                                             prov.ctypes.data_as(C.c_void_p), defl.ctypes.data_as(C.c_void_p),
-                                             int(threads))
+        rc = getattr(self.lib, self.p + "trace_provenance")(
+            self.h, C.byref(run), C.byref(T), rec.ctypes.data_as(C.c_void_p), prov.ctypes.data_as(C.c_void_p),
+            defl.ctypes.data_as(C.c_void_p), int(threads))
         if rc != 0:
-            raise RuntimeError(self.lib.clref_last_error(self.h).decode())
+            raise RuntimeError(getattr(self.lib, self.p + "last_error")(self.h).decode())
         return T.as_dict(), rec, prov, defl
 
     def close(self):
