@@ -233,6 +233,21 @@ __device__ __forceinline__ unsigned path_mask_bits(const Ray& r) {
     return m;
 }
 
+// The event-history masks and acrylic-reflection order of a detected ray (native id ni, mirrored mi), and its
+// provenance partitions when they are counted. One out-of-line copy shared by the kernels that score.
+__device__ __noinline__ void path_partitions_more(PathDiag& pd, clr_path_provenance* pt, const Ray& r,
+                                                  const uint4* prov, int ni, int mi) {
+    const unsigned masks = path_mask_bits(r);
+    const int acr = r.cir + r.cor + r.bir + r.bor, ai = acr < 4 ? acr : 4;
+    for (int side = 0; side < 2; ++side) {
+        const int id = side ? mi : ni;
+        if (id < 0) continue;
+        atomicAdd(&pd.acrylic_order[side][ai][id], 1ull);
+        for (unsigned m = masks; m; m &= m - 1u) atomicAdd(&pd.masks[side][__ffs(m) - 1][id], 1ull);
+    }
+    if (pt) prov_count(*pt, prov ? *prov : prov_init(), r.ic, ni, mi);
+}
+
 // Score finished histories and add them to the scenario tallies (:4390-4436, tallies :7849-7862,
 // per-ray statistics :8483-8508 and :8665-8735). Called by every lane whose photon finished in this
 // iteration; lanes are grouped by scenario so the frequent counters are reduced across the group first.
@@ -303,6 +318,26 @@ __device__ __forceinline__ void finish_ray(const DevScene& D, const DetTable& T,
             sink.add_d(5 * CLR_N_DETECTORS + mi, w);
             sink.add_d(7 * CLR_N_DETECTORS + mi, w * w);
         }
+        // particle-path partitions of the detected ray (one set per detector id it reaches); the less frequent
+        // ones (event-history masks, acrylic order, provenance) are counted out of line, so that the scoring
+        // code every finishing photon runs through stays as small as it was without them
+        {
+            PathDiag& pd = tallies[sid].pd;
+            const int oi = r.ic < 5 ? r.ic : 5, gi = r.gic < 5 ? r.gic : 5;
+            const int pv[CLR_N_PATH_SUMS] = {r.ic, r.gic, r.wic, r.wcoh, r.wmorph, r.pc.entry_reflections,
+                                            r.pc.internal_reflections};
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                const int id = side ? mi : ni;
+                if (id < 0) continue;
+                atomicAdd(&pd.order[side][oi][id], 1ull);
+                atomicAdd(&pd.geom_order[side][gi][id], 1ull);
+#pragma unroll
+                for (int k = 0; k < CLR_N_PATH_SUMS; ++k)
+                    if (pv[k] > 0) atomicAdd(&pd.sums[k][side][id], (unsigned long long)pv[k]);
+            }
+            if (ni >= 0 || mi >= 0) path_partitions_more(pd, D.prov, r, prov, ni, mi);
+        }
         // legacy angular windows (:4429-4434)
         for (int mirror = 0; mirror < 2; ++mirror) {
             float xx = mirror ? -x : x;
@@ -315,41 +350,6 @@ __device__ __forceinline__ void finish_ray(const DevScene& D, const DetTable& T,
                 if (fabsf(ang - deg) <= P.legacy_accept_deg) sink.add_u(CLR_OFF_HW(mirror ? 9 : 8, j), 1ull);
             }
         }
-    }
-    // particle-path partitions of the detected rays (one set per detector id a ray reaches): lanes of the
-    // scenario group whose partition keys agree are merged, one set of atomics per distinct key
-    {
-        PathDiag& pd = tallies[sid].pd;
-        const int oi = r.ic < 5 ? r.ic : 5, gi = r.gic < 5 ? r.gic : 5;
-        const int acr = r.cir + r.cor + r.bir + r.bor, ai = acr < 4 ? acr : 4;
-        const unsigned masks = path_mask_bits(r);
-        const int pv[CLR_N_PATH_SUMS] = {r.ic, r.gic, r.wic, r.wcoh, r.wmorph, r.pc.entry_reflections,
-                                        r.pc.internal_reflections};
-#pragma unroll
-        for (int side = 0; side < 2; ++side) {
-            const int id = side ? mi : ni;
-            const bool on = id >= 0;
-            const unsigned part = __ballot_sync(grp, on);
-            if (!on) continue;
-            const unsigned long long key = ((unsigned long long)masks << 16) | ((unsigned)id << 9) |
-                                           ((unsigned)oi << 6) | ((unsigned)gi << 3) | (unsigned)ai;
-            const unsigned same = __match_any_sync(part, key);
-            const bool head = lane == __ffs(same) - 1;
-            const unsigned long long n = (unsigned long long)__popc(same);
-            unsigned sums[CLR_N_PATH_SUMS];
-#pragma unroll
-            for (int k = 0; k < CLR_N_PATH_SUMS; ++k) sums[k] = __reduce_add_sync(same, (unsigned)pv[k]);
-            if (head) {
-                atomicAdd(&pd.order[side][oi][id], n);
-                atomicAdd(&pd.geom_order[side][gi][id], n);
-                atomicAdd(&pd.acrylic_order[side][ai][id], n);
-#pragma unroll
-                for (int k = 0; k < CLR_N_PATH_SUMS; ++k)
-                    if (sums[k]) atomicAdd(&pd.sums[k][side][id], (unsigned long long)sums[k]);
-                for (unsigned m = masks; m; m &= m - 1u) atomicAdd(&pd.masks[side][__ffs(m) - 1][id], n);
-            }
-        }
-        if (D.prov && (ni >= 0 || mi >= 0)) prov_count(*D.prov, prov ? *prov : prov_init(), r.ic, ni, mi);
     }
     // frequent counters: reduced over the scenario group, one atomic per group
     group_hist(sink, grp, CLR_OFF_STATUS, (st >= 0 && st < CLR_N_STATUS) ? st : 0, st >= 0 && st < CLR_N_STATUS);
