@@ -890,6 +890,8 @@ typedef struct {
        event and particle events after such a return, first/last deflection */
     int first_evt, last_evt, last_order, first_back, first_hemi, bins[6], acr_returns, after_return;
     float first_defl, last_defl;
+    /* path inside particles and its optical length over all events, water path at the last event (:4633) */
+    float ipath_total, iopl_total, wp_last;
 } o_ray;
 
 /* The bins and types of a particle event of type `type` in bin `pidx` (:4836-4848 for an absorbed
@@ -913,6 +915,7 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
     r.ax = r.ay = r.az = r.avx = r.avy = r.avz = NAN;
     for (int k = 0; k < 6; ++k) r.bins[k] = -1;
     r.first_defl = r.last_defl = -1.0f;
+    r.wp_last = -1.0f;
     uint32_t state = seed0 + gid * 74729u + 13u, stOPT = seed1 + gid * 104729u + 29u, stSRC = seed2 + gid * 130363u + 43u;
     const int TM = P->sediment_model, FSM = P->free_surface_model;
     const float RIN = P->rin, ZMIN = P->zmin, ZMEAN = P->zmean, ZTOP = P->zwall_top, DH = P->vortex_delta_h,
@@ -1092,7 +1095,14 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
                 if (h.channel == 0) r.gic++;
                 else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
                 event_type = h.event_type;
-                if (h.status == 2) { o_prov_mark(&r, event_type, sel); st = 5; break; }
+                ipath = h.path;
+                if (h.status == 2) {
+                    o_prov_mark(&r, event_type, sel);
+                    r.ipath_total += h.path;
+                    r.iopl_total += h.path * (float)S->nidx[sel];
+                    st = 5;
+                    break;
+                }
             } else if (use_wave) {
                 if (COND) cstats[0]++;
                 r.wic++;
@@ -1150,6 +1160,7 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
                     if (h.channel == 0) r.gic++;
                     else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
                     event_type = h.event_type;
+                    ipath = h.path;
                 } else {
                     if (!accessible) { r.ic--; r.gic--; r.nulls++; continue; }
                     int ppc = 0, pps = 0, pmb = 0, pmo = 0;
@@ -1168,8 +1179,11 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
             {
                 const float dcos = fminf(fmaxf(o_dot(vinx, viny, vinz, vx, vy, vz), -1.0f), 1.0f);
                 const float defl = acosf(dcos) * (180.0f / O_PI_F);
+                r.ipath_total += ipath;
+                if (event_pidx >= 0) r.iopl_total += ipath * (float)S->nidx[event_pidx];
                 o_prov_mark(&r, event_type, event_pidx);
                 r.last_defl = defl;
+                r.wp_last = r.wp;
                 if (r.ic == 1) { r.first_defl = defl; r.first_back = dcos < 0.0f; r.first_hemi = vy < 0.0f; }
             }
             continue;
@@ -1529,7 +1543,11 @@ static int trace_impl(clo_state* S, const clr_run_params* run, clr_tallies* T, c
                                        r.after_return};
                 memcpy(prov + i * 13, v, sizeof v);
             }
-            if (defl) { defl[i * 2] = r.first_defl; defl[i * 2 + 1] = r.last_defl; }
+            if (defl) {
+                float* d = defl + i * 5;
+                d[0] = r.first_defl; d[1] = r.last_defl; d[2] = r.ipath_total; d[3] = r.iopl_total;
+                d[4] = (r.last_order > 0 && r.wp_last >= 0.0f) ? fmaxf(r.wp - r.wp_last, 0.0f) : -1.0f;
+            }
         }
 #pragma omp critical
         {

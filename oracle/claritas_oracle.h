@@ -24,8 +24,8 @@ int clo_read_physics(clo_state* st, clr_particle_physics* out);
 int clo_n_theta(clo_state* st);
 /* as clo_trace, and per ray the provenance outputs of the reference (prov [n][13]: first/last event type,
  * last event order, first backscatter, first source hemisphere, first/last particle, geometric and wave
- * bin, acrylic returns after a particle event, particle events after a return; defl [n][2]: first/last
- * deflection in degrees) */
+ * bin, acrylic returns after a particle event, particle events after a return; defl [n][5]: first/last
+ * deflection in degrees, path and optical path inside particles, water path after the last event) */
 int clo_trace_provenance(clo_state* st, const clr_run_params* run, clr_tallies* out, clr_ray_record* records,
                          int32_t* prov, float* defl, int n_threads);
 /* the sediment field [n_bins][nr][nz] of model 3 (solved or supplied) and the solver's iterations / residual */

@@ -331,7 +331,7 @@ int clref_trace(clref_state* h, const clr_run_params* run, clr_tallies* T, clr_r
 
 /* As clref_trace, and per ray the reference's provenance outputs: prov [n_rays][13] = its int outputs
  * first_particle_event_type .. particle_after_acrylic_return_count (trace_kernel :4601-4603), defl
- * [n_rays][2] = first_particle_deflection_deg, last_particle_deflection_deg (:4580). */
+ * [n_rays][5] = first_particle_deflection_deg .. water_path_after_last_particle_event (:4580). */
 int clref_trace_provenance(clref_state* h, const clr_run_params* run, clr_tallies* T, clr_ray_record* records,
                            int32_t* prov, float* defl, int n_threads) {
     return trace_impl(h, run, T, records, prov, defl, n_threads);
@@ -454,7 +454,8 @@ static int trace_impl(clref_state* h, const clr_run_params* run, clr_tallies* T,
                 if (records) records[start + i] = tmp;
                 if (prov)
                     for (int k = 0; k < 13; ++k) prov[(start + i) * 13 + k] = I[35 + k][i];
-                if (defl) { defl[(start + i) * 2] = F[8][i]; defl[(start + i) * 2 + 1] = F[9][i]; }
+                if (defl)
+                    for (int k = 0; k < 5; ++k) defl[(start + i) * 5 + k] = F[8 + k][i];
             }
         }
     }

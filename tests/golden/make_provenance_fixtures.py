@@ -60,7 +60,8 @@ def main():
             rp[:, PP.ACR_RETURN] = rp[:, PP.ACR_RETURN] > 0  # counts kept as flags (the device keeps flags)
             rp[:, PP.AFTER_RETURN] = rp[:, PP.AFTER_RETURN] > 0
             out[f"{name}/ray_prov"] = np.clip(rp, -1, 127).astype(np.int8)
-            out[f"{name}/ray_defl"] = defl[:N_PER_RAY]
+            out[f"{name}/ray_defl"] = defl[:N_PER_RAY, :2]
+            out[f"{name}/ray_paths"] = defl[:N_PER_RAY, 2:]
         out[f"{name}/hw_native"] = tal["hw_native"]
         out[f"{name}/hw_mirror"] = tal["hw_mirror"]
         print(name, "detected", int(tal["hw_native"].sum()), "types", part["last_type_hits"].sum(axis=(0, 2)).tolist())

@@ -142,12 +142,13 @@ class OracleRun:
         """Tallies, per-ray records, and per ray the reference's provenance outputs
         (int [n][13]: first/last event type, last event order, first backscatter, first source hemisphere,
         first/last particle, geometric and wave bin, acrylic returns after a particle event, particle events
-        after a return) and deflections (float [n][2]: first, last)."""
+        after a return) and float [n][5]: first and last deflection (deg), path and optical path inside
+        particles, water path after the last event (-1 without one)."""
         T = abi.Tallies()
         n = int(run.n_rays)
         rec = np.zeros(n, dtype=abi.record_dtype())
         prov = np.zeros((n, 13), np.int32)
-        defl = np.zeros((n, 2), np.float32)
+        defl = np.zeros((n, 5), np.float32)
         rc = getattr(self.lib, self.p + "trace_provenance")(
             self.h, C.byref(run), C.byref(T), rec.ctypes.data_as(C.c_void_p), prov.ctypes.data_as(C.c_void_p),
             defl.ctypes.data_as(C.c_void_p), int(threads))

@@ -20,6 +20,8 @@ ACR_RETURN, AFTER_RETURN = 11, 12
 
 
 def partitions(ic, native_id, mirror_id, prov, defl, max_bins: int = 64) -> dict:
+    """defl: [n][2] first/last deflection, or [n][5] with the path inside particles, its optical length
+    and the water path after the last event, which add the causal path sums (:8142-8160)."""
     ic = np.asarray(ic)
     first_type, last_type = prov[:, FIRST_TYPE], prov[:, LAST_TYPE]
     first_angle = defl[:, 0].astype(np.float64)
@@ -45,6 +47,15 @@ def partitions(ic, native_id, mirror_id, prov, defl, max_bins: int = 64) -> dict
         "h170_last_angle_hits": np.zeros((2, N_TYPES, 6), np.int64),
         "h170_first_angle_hits": np.zeros((2, 6), np.int64),
     }
+    paths = defl.shape[1] >= 5
+    if paths:
+        ip, io, wa = (defl[:, k].astype(np.float64) for k in (2, 3, 4))
+        with np.errstate(invalid="ignore"):
+            path_valid = valid & np.isfinite(ip) & np.isfinite(io) & np.isfinite(wa) & (wa >= 0.0)
+        for k in ("causal_internal_path_sum", "causal_internal_opl_sum", "causal_post_last_water_path_sum",
+                  "causal_last_order_sum"):
+            out[k] = np.zeros((2, N_DET))
+        out["causal_path_count"] = np.zeros((2, N_DET), np.int64)
     for side, ids in enumerate((np.asarray(native_id), np.asarray(mirror_id))):
         ok = (ids >= 0) & (ids < N_DET)
         for k, col in enumerate(BIN_COLS):
@@ -65,6 +76,13 @@ def partitions(ic, native_id, mirror_id, prov, defl, max_bins: int = 64) -> dict
         np.add.at(out["first_angle_count"][side], ids[ok & fav], 1)
         np.add.at(out["last_angle_sum"][side], ids[ok & lav], last_angle[ok & lav])
         np.add.at(out["last_angle_count"][side], ids[ok & lav], 1)
+        if paths:
+            m = ok & path_valid
+            for k, v in (("causal_internal_path_sum", ip), ("causal_internal_opl_sum", io),
+                         ("causal_post_last_water_path_sum", wa),
+                         ("causal_last_order_sum", prov[:, LAST_ORDER].astype(np.float64))):
+                np.add.at(out[k][side], ids[m], v[m])
+            np.add.at(out["causal_path_count"][side], ids[m], 1)
         h = ok & (ids == 17)
         for b in range(6):
             lo, hi = H170_EDGES[b], H170_EDGES[b + 1]

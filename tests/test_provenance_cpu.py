@@ -92,7 +92,8 @@ def test_oracle_provenance_matches_reference_fixture(name):
         np.testing.assert_array_equal(rp[same], z[f"{name}/ray_prov"][same].astype(np.int32))
         if same_platform:
             assert same.all()
-            np.testing.assert_array_equal(defl[:n], z[f"{name}/ray_defl"])
+            np.testing.assert_array_equal(defl[:n, :2], z[f"{name}/ray_defl"])
+            np.testing.assert_array_equal(defl[:n, 2:], z[f"{name}/ray_paths"])
 
 
 @pytest.mark.skipif(not H.reference_available(), reason="host build of the reference not present (no checkout)")
