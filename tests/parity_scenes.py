@@ -57,15 +57,21 @@ SCENES = {
 }
 
 
+# The dense stress regime (the 20 g/L, 2 um clay case in the small cell, localized-vortex surface: optical
+# depth ~100, tens of thousands of events on the longest histories): CPU oracle only.
+CPU_ONLY = {
+    "dense_clay": (SCULLY, dict(concentration_mg_l=20000.0, n_bins=16, median_um=2.0, sigma_g=1.5, d_min_um=0.5,
+                                d_max_um=10.0), False),
+}
 # Every scene runs in the CPU oracle as well (the meridional field solver included).
-CPU_SCENES = list(SCENES)
+CPU_SCENES = list(SCENES) + list(CPU_ONLY)
 # Scenes whose sediment field the meridional solver makes (no supplied grid).
 SOLVED_FIELD = {"meridional_solver"}
 
 
 def build(name: str):
     """(config, particles, grid-or-None) of a parity scene."""
-    over, pk, needs_grid = SCENES[name]
+    over, pk, needs_grid = SCENES[name] if name in SCENES else CPU_ONLY[name]
     cfg = S.small_cell_config(**over)
     cfg.validate()
     parts = S.quartz_particles(**pk)
