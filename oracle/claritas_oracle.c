@@ -768,6 +768,28 @@ int clo_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, const c
 
 int clo_n_theta(clo_state* s) { return s ? s->nt : 0; }
 
+int clo_read_sediment(clo_state* S, double* A, double* B, double* norm, double* ws, double* radial_log,
+                      double* radial_slip) {
+    if (!S || !S->sed_A) return -1;
+    const size_t n = (size_t)S->n, nr = (size_t)S->n_radial;
+    if (A) memcpy(A, S->sed_A, n * sizeof(double));
+    if (B) memcpy(B, S->sed_B, n * sizeof(double));
+    if (norm) memcpy(norm, S->sed_norm, n * sizeof(double));
+    if (ws) memcpy(ws, S->sed_ws, n * sizeof(double));
+    if (radial_log) memcpy(radial_log, S->sed_radial_log, n * nr * sizeof(double));
+    if (radial_slip) memcpy(radial_slip, S->sed_wr, n * nr * sizeof(double));
+    return 0;
+}
+
+double clo_meridional_velocity(int fsm, double r, double z, double zmin, double zmean, double R, double dh, double core,
+                               double upeak, double* uz) {
+    m_geom g = {fsm, R, zmin, zmean, dh, core, upeak};
+    double ur = 0.0, w = 0.0;
+    m_velocity(&g, r, z, &ur, &w);
+    if (uz) *uz = w;
+    return ur;
+}
+
 int clo_read_sediment_field(clo_state* S, double* grid, int* nr, int* nz, int* iterations, double* max_residual) {
     if (!S) return -1;
     if (nr) *nr = S->grid_nr;

@@ -28,6 +28,14 @@ int clo_n_theta(clo_state* st);
  * deflection in degrees, path and optical path inside particles, water path after the last event) */
 int clo_trace_provenance(clo_state* st, const clr_run_params* run, clr_tallies* out, clr_ray_record* records,
                          int32_t* prov, float* defl, int n_threads);
+/* the sediment coefficients of models 1-3 per bin: radial log coefficient (A), vertical inverse length (B),
+ * normalisation, settling velocity, radial log lookup and (models 2, 3) radial slip velocity
+ * [n_bins][n_radial] (any pointer may be NULL) */
+int clo_read_sediment(clo_state* st, double* A, double* B, double* norm, double* ws, double* radial_log,
+                      double* radial_slip);
+/* the meridional secondary-circulation velocity (ur returned, uz through the pointer) at (r, z) */
+double clo_meridional_velocity(int fsm, double r, double z, double zmin, double zmean, double R, double dh, double core,
+                               double upeak, double* uz);
 /* the sediment field [n_bins][nr][nz] of model 3 (solved or supplied) and the solver's iterations / residual */
 int clo_read_sediment_field(clo_state* st, double* grid, int* nr, int* nz, int* iterations, double* max_residual);
 int clo_trace(clo_state* st, const clr_run_params* run, clr_tallies* out, clr_ray_record* records, int n_threads);
