@@ -790,6 +790,24 @@ double clo_meridional_velocity(int fsm, double r, double z, double zmin, double 
     return ur;
 }
 
+float clo_surface(int fsm, float x, float y, float zmean, float R, float dh, float core, float* normal) {
+    if (normal) o_surface_normal(x, y, R, fsm, dh, core, normal, normal + 1, normal + 2);
+    return o_surface_z(x, y, zmean, R, fsm, dh, core);
+}
+
+double clo_local_scale(clo_state* S, int pidx, float x, float y, float z) {
+    if (!S || pidx < 0 || pidx >= S->n) return -1.0;
+    const clr_scene_params* P = &S->sp;
+    o_field F = {P->sediment_model, P->free_surface_model, S->n, S->n_radial, S->grid_nr, S->grid_nz, S->sed_A, S->sed_B,
+                 S->sed_norm, S->sed_radial_log, S->sed_grid, S->grid_zmax, P->rin, P->zmin, P->vortex_core_radius};
+    return o_local_scale(&F, pidx, x, y, z);
+}
+
+int clo_meridional_fluid(int fsm, double r, double z, double zmin, double zmean, double R, double dh, double core) {
+    m_geom g = {fsm, R, zmin, zmean, dh, core, 0.0};
+    return m_fluid(&g, r, z);
+}
+
 int clo_read_sediment_field(clo_state* S, double* grid, int* nr, int* nz, int* iterations, double* max_residual) {
     if (!S) return -1;
     if (nr) *nr = S->grid_nr;

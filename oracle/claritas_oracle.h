@@ -36,6 +36,12 @@ int clo_read_sediment(clo_state* st, double* A, double* B, double* norm, double*
 /* the meridional secondary-circulation velocity (ur returned, uz through the pointer) at (r, z) */
 double clo_meridional_velocity(int fsm, double r, double z, double zmin, double zmean, double R, double dh, double core,
                                double upeak, double* uz);
+/* free-surface height at (x, y) and, when normal is not NULL, its unit normal (into the water) */
+float clo_surface(int fsm, float x, float y, float zmean, float R, float dh, float core, float* normal);
+/* the sediment concentration scale of bin pidx at a point, as the trace looks it up (FP32 position) */
+double clo_local_scale(clo_state* st, int pidx, float x, float y, float z);
+/* 1 when (r, z) lies in the liquid (above the bottom, below the free surface) */
+int clo_meridional_fluid(int fsm, double r, double z, double zmin, double zmean, double R, double dh, double core);
 /* the sediment field [n_bins][nr][nz] of model 3 (solved or supplied) and the solver's iterations / residual */
 int clo_read_sediment_field(clo_state* st, double* grid, int* nr, int* nz, int* iterations, double* max_residual);
 int clo_trace(clo_state* st, const clr_run_params* run, clr_tallies* out, clr_ray_record* records, int n_threads);

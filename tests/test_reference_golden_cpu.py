@@ -171,3 +171,64 @@ def test_parabolic_meridional_velocity(lib):
            + _velocity(lib, 1, rr, zz, upeak)[0] / rr
            + (_velocity(lib, 1, rr, zz + h, upeak)[1] - _velocity(lib, 1, rr, zz - h, upeak)[1]) / (2 * h))
     assert abs(div) < 2e-07, div
+
+
+def test_free_surface_height_and_normal(lib):
+    """The parabolic surface at r = 0 and 20 mm (the validation script's device geometry check, :1130-1160)."""
+    lib.clo_surface.restype = C.c_float
+    lib.clo_surface.argtypes = [C.c_int] + [C.c_float] * 6 + [C.c_void_p]
+    zs, normals = [], []
+    for x in (0.0, 0.02):
+        n = np.zeros(3, np.float32)
+        zs.append(lib.clo_surface(1, x, 0.0, ZMEAN, R, D, CORE, n.ctypes.data_as(C.c_void_p)))
+        normals.append(n.astype(np.float64))
+    close(zs, ZMEAN + D * (np.array([0.0, 0.02]) ** 2 / R ** 2 - 0.5), rtol=3e-06, atol=3e-07)
+    slopes = 2 * D * np.array([0.0, 0.02]) / R ** 2
+    want = np.column_stack([slopes, np.zeros(2), -np.ones(2)])
+    want /= np.linalg.norm(want, axis=1)[:, None]
+    close(np.abs(normals), np.abs(want), rtol=4e-06, atol=3e-07)
+    assert np.all(np.sign(np.asarray(normals)[:, 2]) == np.sign(np.asarray(normals)[0, 2]))
+
+
+@pytest.mark.parametrize("transport", ["stokes_drift_diffusion", "schiller_naumann_drift_diffusion"])
+def test_trace_field_lookup_matches_coefficients(lib, transport):
+    """The concentration scale the trace looks up (FP32 position, radial lookup, vertical decay) against the
+    coefficients it comes from, at the bottom and the beam plane on the axis and at 0.95 R (:1161-1225)."""
+    lib.clo_local_scale.restype = C.c_double
+    lib.clo_local_scale.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float]
+    cfg = S.ModelConfig(free_surface_model="parabolic_vortex", vortex_wall_center_height_difference_m=D,
+                        vortex_core_radius_m=CORE, sediment_transport_model=transport)
+    sp = cfg.to_scene_params()
+    ps = S.Particles(DIAM, np.ones(3), np.full(3, 1.54), np.zeros(3), 1.0, 2600.0).spec(cfg)
+    ss = cfg.sediment_spec()
+    ss.particle_density, ss.water_density, ss.water_viscosity, ss.gravity = 2600.0, 997.0, 8.9e-4, 9.81
+    ss.eddy_diffusivity, ss.n_quad, ss.n_radial = DT, 512, 129
+    ss.rin, ss.zmin, ss.zmean, ss.vortex_delta_h, ss.vortex_core_radius = R, ZMIN, ZMEAN, D, CORE
+    h = C.c_void_p()
+    assert lib.clo_prepare(C.byref(sp), C.byref(ps), C.byref(ss), C.byref(h)) == 0
+    b, norm = np.zeros(3), np.zeros(3)
+    rl = np.zeros((3, 129))
+    lib.clo_read_sediment(h, None, b.ctypes.data_as(C.c_void_p), norm.ctypes.data_as(C.c_void_p), None,
+                          rl.ctypes.data_as(C.c_void_p), None)
+    xyz = np.array([[0.0, 0.0, -0.093], [0.95 * R, 0.0, -0.093], [0.0, 0.0, 0.0], [0.95 * R, 0.0, 0.0]], np.float32)
+    rn = np.linspace(0.0, R, 129)
+    for p in range(3):
+        got = np.array([lib.clo_local_scale(h, p, *map(float, q)) for q in xyz])
+        log_r = np.array([np.interp(float(q[0]), rn, rl[p]) for q in xyz])
+        want = np.exp(log_r - b[p] * (xyz[:, 2].astype(np.float64) + 0.093)) / norm[p]
+        close(got, want, rtol=2e-05, atol=2e-07)
+        assert np.max(got) <= (1.0 / norm[p]) * (1 + 3e-06)
+    lib.clo_free(h)
+
+
+def test_meridional_liquid_cells():
+    """Cells of a 16 x 32 (r, z) grid are liquid exactly below the parabolic surface (:1265-1289)."""
+    lib, _ = H.load("port")
+    lib.clo_meridional_fluid.restype = C.c_int
+    lib.clo_meridional_fluid.argtypes = [C.c_int] + [C.c_double] * 7
+    nr, nz, ztop = 16, 32, 0.074
+    rr = (np.arange(nr) + 0.5) * R / nr
+    zz = ZMIN + (np.arange(nz) + 0.5) * (ztop - ZMIN) / nz
+    got = np.array([[lib.clo_meridional_fluid(1, r, z, ZMIN, ZMEAN, R, D, CORE) for z in zz] for r in rr], bool)
+    want = zz[None, :] < ZMEAN + D * (rr[:, None] ** 2 / R ** 2 - 0.5)
+    np.testing.assert_array_equal(got, want)
