@@ -527,6 +527,8 @@ class ClaritasForwardModel:
         for k in ("x0", "y0", "z0", "x1", "y1", "z1"):
             diag[f"trajectory_{k}_m"] = a["trajectory_" + k]
         diag["trajectory_particle_order"] = a["trajectory_order"]
+        # the event code of each kept segment's end is not recorded by this library: -1 throughout
+        diag["trajectory_event_code"] = np.full(np.shape(a["trajectory_order"]), -1, dtype=np.int32)
         return hm[0], hm[1], diag
 
     # ---- result assembly (formulas of CLARITAS.py:8882-8966 and :9600-9890) --------------------

@@ -10,6 +10,10 @@
 
 JSON and CSV values go through the reference's sanitiser rules (`_json_safe`, :11362-11375): arrays become
 lists, NumPy scalars Python scalars, non-finite floats None; JSON is written sorted with indent 2.
+
+The case-integrity policy (`resolved_failure_policy`, `production_integrity`, `diagnostic_integrity`,
+`enforce_case_integrity`; :11876-12070) judges a case by its failed-ray fraction (failed rays stay in the
+launched denominator) and, with light diagnostics, by their event reconciliation and track-length closure.
 """
 from __future__ import annotations
 
@@ -25,6 +29,160 @@ from .scene import DETECTOR_ANGLES_DEG, vortex_surface_geometry
 
 class CaseIntegrityError(RuntimeError):
     """A result field failed the reference's output integrity checks."""
+
+
+# The reference's case-integrity policy (CLARITAS/CLARITAS.py:46-51): "report" keeps going and reports,
+# "strict" stops on any diagnostic issue; a case whose failed-ray fraction exceeds the limit is fatal after
+# its results are exported. None disables a limit.
+DIAGNOSTIC_POLICY = "report"
+MAX_FAILED_RAY_FRACTION = 0.001
+MAX_UNEXPLAINED_EVENT_FRACTION = 0.001
+MAX_DIAGNOSTIC_CLOSURE_ERROR = 0.001
+ABORT_ON_SYSTEMIC_DIAGNOSTICS = False
+STRICT_DIAGNOSTIC_CLOSURE_ERROR = 2e-6
+
+
+def resolved_failure_policy(mode=None, **limits) -> dict:
+    """The policy in force (`_resolved_failure_policy`, :11876-11892); keywords override the module values."""
+    mode = DIAGNOSTIC_POLICY if mode is None else mode
+    if mode not in ("report", "strict"):
+        raise ValueError("DIAGNOSTIC_POLICY must be report or strict")
+    lim = {"max_failed_ray_fraction": MAX_FAILED_RAY_FRACTION,
+           "max_unexplained_event_fraction": MAX_UNEXPLAINED_EVENT_FRACTION,
+           "max_diagnostic_closure_error": MAX_DIAGNOSTIC_CLOSURE_ERROR,
+           "strict_closure_error": STRICT_DIAGNOSTIC_CLOSURE_ERROR}
+    lim.update(limits)
+    for key, value in lim.items():
+        if value is not None and (not np.isfinite(value) or value < 0):
+            raise ValueError(f"{key} must be finite and nonnegative, or None")
+    return dict(lim, mode=mode, abort_on_systemic_diagnostics=bool(ABORT_ON_SYSTEMIC_DIAGNOSTICS))
+
+
+def production_integrity(launched: int, failed: int, diagnostics: dict, policy: dict) -> dict:
+    """Failed-ray accounting of a case (`_production_integrity`, :11895-11920): failed rays stay in the
+    launched denominator (no renormalisation over successful rays); fatal beyond the policy's fraction."""
+    if launched <= 0 or failed < 0 or failed > launched:
+        raise ValueError("corrupted production ray counts")
+    if not diagnostics.get("count_closure_ok", True):
+        raise ValueError("production failure categories do not reconcile")
+    fraction = failed / launched
+    limit = policy["max_failed_ray_fraction"]
+    fatal = limit is not None and fraction > limit
+    return {
+        "launched_rays": int(launched), "failed_rays": int(failed), "failed_ray_fraction": fraction,
+        "normalization_rays": int(launched),
+        "failure_categories": diagnostics.get("code_counts", {}),
+        "failure_subcategories": diagnostics.get("subcode_counts", {}),
+        "failure_samples": diagnostics.get("samples", []),
+        "limitations": (["failed rays terminate without completion; valid histories and prefixes remain; "
+                         "no successful-ray renormalization"] if failed else []),
+        "fatal": bool(fatal),
+        "status": "systemic_failure" if fatal else ("limited" if failed else "ok"),
+    }
+
+
+def production_failure_diagnostics(res) -> dict:
+    """The failure categories of a ForwardResult in the form production_integrity takes."""
+    codes = {k: int(v) for k, v in dict(res.production_failure_code_counts).items() if int(v)}
+    subs = {k: int(v) for k, v in dict(getattr(res, "production_failure_subcode_counts", {}) or {}).items()
+            if int(v)}
+    return {"count_closure_ok": True, "code_counts": codes, "subcode_counts": subs}
+
+
+def enforce_case_integrity(production: dict, diagnostic: dict) -> None:
+    """`_enforce_case_integrity` (:11923-11927): raise once either report is fatal."""
+    if production["fatal"] or diagnostic.get("fatal", False):
+        raise CaseIntegrityError("case exceeded configured integrity policy; inspect persisted integrity reports "
+                                 "and run_summary.json")
+
+
+_DIAG_FIELDS = ("track_length_m", "post_scatter_track_length_m", "scatter_event_weight", "scatter_event_count")
+_TRAJ_FIELDS = ("trajectory_x0_m", "trajectory_y0_m", "trajectory_z0_m", "trajectory_x1_m", "trajectory_y1_m",
+                "trajectory_z1_m", "trajectory_particle_order", "trajectory_event_code")
+
+
+def diagnostic_integrity(diag: dict, policy: dict) -> dict:
+    """Integrity report of the light-history diagnostics (`_diagnostic_integrity`, :11930-12070): shapes and
+    bounds (corruption raises), field validity, event reconciliation (observed = deposited + rejected, grid
+    counts = deposited), track-length closure; limited / systemic / fatal by the policy."""
+    shape = (int(diag["nz"]), int(diag["ny"]), int(diag["nx"]))
+    if min(shape) <= 0:
+        raise ValueError("invalid diagnostic grid dimensions")
+    for axis in ("x", "y", "z"):
+        lo, hi = float(diag[axis + "_min_m"]), float(diag[axis + "_max_m"])
+        if not np.isfinite(lo) or not np.isfinite(hi) or hi <= lo:
+            raise ValueError("corrupted diagnostic grid bounds")
+    if int(diag["diagnostic_rays_processed"]) <= 0:
+        raise ValueError("invalid diagnostic launched-ray denominator")
+    valid = {}
+    for key in _DIAG_FIELDS:
+        a = np.asarray(diag[key])
+        if a.shape != shape:
+            raise ValueError(f"corrupted diagnostic shape: {key}: {a.shape}, expected {shape}")
+        valid[key] = bool(np.all(np.isfinite(a)) and np.all(a >= 0))
+    counts = np.asarray(diag["trajectory_count"])
+    nseg = int(diag["max_segments_per_ray"])
+    if counts.ndim != 1 or np.any(counts < 0) or np.any(counts > nseg):
+        raise ValueError("corrupted trajectory counts")
+    if np.asarray(diag["trajectory_overflow"]).shape != counts.shape:
+        raise ValueError("corrupted trajectory overflow shape")
+    for key in _TRAJ_FIELDS:
+        a = np.asarray(diag[key])
+        if a.shape != (len(counts), nseg):
+            raise ValueError(f"corrupted trajectory shape: {key}")
+        valid[key] = all(np.all(np.isfinite(a[i, :int(n)])) for i, n in enumerate(counts))
+    observed, deposited = int(diag["scatter_event_total"]), int(diag["deposited_scatter_event_total"])
+    rejected = int(diag.get("event_outside_count", 0))
+    if min(observed, deposited, rejected) < 0:
+        raise ValueError("corrupted diagnostic event counts")
+    discrepancy = deposited + rejected - observed
+    grid_discrepancy = (int(np.sum(diag["scatter_event_count"], dtype=np.uint64)) - deposited
+                        if valid["scatter_event_count"] else None)
+    unexplained = max(abs(discrepancy), abs(grid_discrepancy or 0)) / max(observed, 1)
+    closure, grid_closure = float(diag["deposition_closure_relative_error"]), float(diag["grid_closure_relative_error"])
+    issues = []
+    if rejected:
+        issues.append("rejected diagnostic events explicitly accounted")
+    if discrepancy or grid_discrepancy:
+        issues.append("unexplained diagnostic event discrepancy")
+    if int(diag.get("hard_error_count", diag.get("error_count", 0))):
+        issues.append("diagnostic traversal errors")
+    guard = int(diag.get("water_advance_guard_failure_count", 0))
+    if guard:
+        issues.append("water guard terminated rays")
+    unsafe = (not all(valid.values()) or int(diag.get("nonfinite_count", 0)) > 0
+              or int(diag.get("negative_value_count", 0)) > 0)
+    if unsafe:
+        issues.append("unsafe diagnostic fields; derived outputs skipped")
+    strict_limit = policy["strict_closure_error"]
+    if (not np.isfinite(closure) or not np.isfinite(grid_closure)
+            or (strict_limit is not None and max(closure, grid_closure) > strict_limit)):
+        issues.append("diagnostic track-length closure exceeds strict limit")
+    systemic = unsafe or not np.isfinite(closure) or not np.isfinite(grid_closure)
+    for value, limit in ((unexplained, policy["max_unexplained_event_fraction"]),
+                         (max(closure, grid_closure), policy["max_diagnostic_closure_error"])):
+        systemic = systemic or (limit is not None and value > limit)
+    return {
+        "policy": policy, "diagnostic_status": "limited" if issues else "ok",
+        "limitations": (["failed-ray history prefixes remain in diagnostics; failed rays stay in launched "
+                         "denominators"] if guard else []),
+        "issues": issues, "field_validity": valid, "derived_outputs_safe": not unsafe,
+        "observed_diagnostic_events": observed, "deposited_diagnostic_events": deposited,
+        "rejected_diagnostic_events": rejected, "reconciled_event_discrepancy": discrepancy,
+        "event_accounting_reconciled": discrepancy == 0 and grid_discrepancy == 0,
+        "deposited_grid_event_discrepancy": grid_discrepancy,
+        "deposited_only_event_discrepancy": deposited - observed,
+        "unexplained_event_fraction": unexplained,
+        "diagnostic_clipped_track_length_m": diag["segment_length_total_m"],
+        "physical_full_path_length_m": None,
+        "path_length_scope": "segment totals are clipped to diagnostic grid; full physical path is not collected",
+        "systemic_diagnostic_issue": bool(systemic),
+        "fatal": bool((policy["mode"] == "strict" and issues) or (policy["abort_on_systemic_diagnostics"] and systemic)),
+        "skipped_outputs": ([] if not unsafe else ["diagnostic cross-section CSVs, volume product, trajectories and "
+                                                  "diagnostic plots: unsafe fields"]),
+        "first_outside_event": diag.get("first_outside_event"),
+        "first_water_advance_guard_failure": diag.get("first_water_advance_guard_failure"),
+    }
 
 
 def json_safe(value):

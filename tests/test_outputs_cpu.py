@@ -58,3 +58,86 @@ def test_json_safe_rules(tmp_path):
     txt = (tmp_path / "x.json").read_text()
     assert json.loads(txt) == {"a": [0, 1, 2], "b": 2.5, "c": None, "d": [1, 2], "z": {"k": 4}}
     assert txt.index('"a"') < txt.index('"z"')  # sorted keys
+
+
+# ---- case-integrity policy (the reference's PolicyTests, CLARITAS/test_diagnostics.py) ----
+
+def _diag_fixture():
+    """A light-diagnostic result of a 2x2x2 grid: 9 observed events, 8 deposited, 1 outside the grid."""
+    a = np.ones((2, 2, 2), dtype=np.float32)
+    d = dict(nx=2, ny=2, nz=2, track_length_m=a, post_scatter_track_length_m=a.copy(), scatter_event_weight=a.copy(),
+             scatter_event_count=a.astype(np.uint32), scatter_event_total=9, deposited_scatter_event_total=8,
+             event_outside_count=1, deposition_closure_relative_error=1e-12, grid_closure_relative_error=1e-12,
+             segment_length_total_m=8.0, deposited_length_total_m=8.0, trajectory_count=np.zeros(0, dtype=int),
+             trajectory_overflow=np.zeros(0, dtype=int), max_segments_per_ray=4, nonfinite_count=0,
+             negative_value_count=0, hard_error_count=1, water_advance_guard_failure_count=1,
+             diagnostic_rays_processed=100)
+    for k in O._TRAJ_FIELDS:
+        d[k] = np.zeros((0, 4))
+    for k in ("x", "y", "z"):
+        d[k + "_min_m"], d[k + "_max_m"] = -0.049, 0.049
+    return d
+
+
+def test_one_failure_keeps_launched_denominator():
+    p = O.production_integrity(100_000_000, 1, {"count_closure_ok": True, "code_counts": {"water_guard": 1}},
+                               O.resolved_failure_policy())
+    O.enforce_case_integrity(p, O.diagnostic_integrity(_diag_fixture(), O.resolved_failure_policy()))
+    assert not p["fatal"] and p["normalization_rays"] == 100_000_000 and p["failed_ray_fraction"] == 1e-8
+    assert p["status"] == "limited"
+
+
+def test_rejected_events_reconcile():
+    r = O.diagnostic_integrity(_diag_fixture(), O.resolved_failure_policy())
+    assert r["reconciled_event_discrepancy"] == 0 and r["deposited_only_event_discrepancy"] == -1
+    assert not r["fatal"] and r["diagnostic_status"] == "limited"
+
+
+def test_unexplained_discrepancy_visible():
+    d = _diag_fixture()
+    d["event_outside_count"] = 0
+    r = O.diagnostic_integrity(d, O.resolved_failure_policy())
+    assert r["reconciled_event_discrepancy"] == -1 and not r["event_accounting_reconciled"] and not r["fatal"]
+    p = O.resolved_failure_policy()
+    p["abort_on_systemic_diagnostics"] = True
+    assert O.diagnostic_integrity(d, p)["fatal"]
+
+
+def test_strict_reports_then_stops():
+    p = O.resolved_failure_policy(mode="strict")
+    assert O.diagnostic_integrity(_diag_fixture(), p)["fatal"]
+    with pytest.raises(O.CaseIntegrityError):
+        O.enforce_case_integrity({"fatal": False}, O.diagnostic_integrity(_diag_fixture(), p))
+    d = _diag_fixture()
+    d.update(scatter_event_total=8, event_outside_count=0, hard_error_count=0, water_advance_guard_failure_count=0)
+    assert not O.diagnostic_integrity(d, p)["fatal"]
+    d["grid_closure_relative_error"] = 0.01
+    assert O.diagnostic_integrity(d, p)["fatal"]
+
+
+def test_unsafe_fields_are_reported():
+    d = _diag_fixture()
+    d["track_length_m"][0, 0, 0] = np.nan
+    r = O.diagnostic_integrity(d, O.resolved_failure_policy())
+    assert not r["derived_outputs_safe"] and r["skipped_outputs"] and not r["fatal"]
+    assert not r["field_validity"]["track_length_m"] and r["field_validity"]["scatter_event_count"]
+
+
+def test_shapes_and_counts_unrecoverable():
+    d = _diag_fixture()
+    d["track_length_m"] = np.zeros((1,))
+    with pytest.raises(ValueError):
+        O.diagnostic_integrity(d, O.resolved_failure_policy())
+    with pytest.raises(ValueError):
+        O.production_integrity(10, 1, {"count_closure_ok": False}, O.resolved_failure_policy())
+    with pytest.raises(ValueError):
+        O.resolved_failure_policy(mode="invalid")
+    with pytest.raises(ValueError):
+        O.resolved_failure_policy(max_failed_ray_fraction=-1.0)
+
+
+def test_systemic_ray_limit():
+    p = O.resolved_failure_policy()
+    assert O.production_integrity(100, 2, {}, p)["fatal"]
+    p["max_failed_ray_fraction"] = None
+    assert not O.production_integrity(100, 2, {}, p)["fatal"]
