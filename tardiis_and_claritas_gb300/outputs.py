@@ -81,12 +81,29 @@ def production_integrity(launched: int, failed: int, diagnostics: dict, policy: 
     }
 
 
-def production_failure_diagnostics(res) -> dict:
-    """The failure categories of a ForwardResult in the form production_integrity takes."""
-    codes = {k: int(v) for k, v in dict(res.production_failure_code_counts).items() if int(v)}
-    subs = {k: int(v) for k, v in dict(getattr(res, "production_failure_subcode_counts", {}) or {}).items()
-            if int(v)}
-    return {"count_closure_ok": True, "code_counts": codes, "subcode_counts": subs}
+def case_integrity(res, policy=None):
+    """The production and light-diagnostic integrity reports of a ForwardResult (the reference's case flow,
+    :13031-13036 and :12066-12068); the light report is the disabled one without light diagnostics."""
+    policy = resolved_failure_policy() if policy is None else policy
+    prod = production_integrity(int(res.n_rays), int(res.production_failure_count),
+                                res.production_failure_diagnostics, policy)
+    light = getattr(res, "light_transport_diagnostics", None)
+    diag = (diagnostic_integrity(light, policy) if light
+            else {"diagnostic_status": "disabled", "fatal": False, "skipped_outputs": []})
+    return prod, diag
+
+
+def write_case_integrity(out, res, policy=None):
+    """production_integrity_report.json (and light_transport_integrity_report.json with light diagnostics)
+    of one case; returns both reports. The caller exports the case first and then calls
+    enforce_case_integrity, as the reference does (:13204)."""
+    out = Path(out)
+    out.mkdir(parents=True, exist_ok=True)
+    prod, diag = case_integrity(res, policy)
+    write_json(out / "production_integrity_report.json", prod)
+    if diag.get("diagnostic_status") != "disabled":
+        write_json(out / "light_transport_integrity_report.json", diag)
+    return prod, diag
 
 
 def enforce_case_integrity(production: dict, diagnostic: dict) -> None:
@@ -344,5 +361,7 @@ def write_run_summary(out, material: str, concentration: float, wavelength_nm: f
     out.mkdir(parents=True, exist_ok=True)
     d = summary_dict(material, concentration, wavelength_nm, seed, gpu_name, runtime_s, res, cfg, out,
                      wavelength_assumptions)
+    if hasattr(res, "production_failure_diagnostics"):
+        d["production_integrity"], d["light_transport_diagnostics"] = case_integrity(res)
     write_json(out / "run_summary.json", d)
     return d

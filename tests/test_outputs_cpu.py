@@ -141,3 +141,24 @@ def test_systemic_ray_limit():
     assert O.production_integrity(100, 2, {}, p)["fatal"]
     p["max_failed_ray_fraction"] = None
     assert not O.production_integrity(100, 2, {}, p)["fatal"]
+
+
+def test_case_integrity_reports(tmp_path):
+    res = fake_result(n=200_000)
+    res.production_failure_count = 3
+    res.production_failure_diagnostics = {"code_counts": {"acrylic_bounce_limit": 3}, "subcode_counts": {}}
+    res.light_transport_diagnostics = None
+    prod, diag = O.write_case_integrity(tmp_path, res)
+    assert prod["failed_ray_fraction"] == 1.5e-5 and prod["status"] == "limited" and not prod["fatal"]
+    assert diag["diagnostic_status"] == "disabled"
+    back = json.loads((tmp_path / "production_integrity_report.json").read_text())
+    assert back["failure_categories"] == {"acrylic_bounce_limit": 3}
+    assert not (tmp_path / "light_transport_integrity_report.json").exists()
+    O.enforce_case_integrity(prod, diag)
+    res.light_transport_diagnostics = _diag_fixture()
+    res.production_failure_count = 1000  # 0.5 % > 0.1 %: the case is exported, then stops
+    prod, diag = O.write_case_integrity(tmp_path, res)
+    assert prod["fatal"] and diag["diagnostic_status"] == "limited"
+    assert (tmp_path / "light_transport_integrity_report.json").exists()
+    with pytest.raises(O.CaseIntegrityError):
+        O.enforce_case_integrity(prod, diag)
