@@ -140,3 +140,11 @@ def test_oracle_empty_run_and_precompute_errors():
     big = S.Particles([5e-3], [1.0], [1.5], [0.0], 1.0)
     with pytest.raises(RuntimeError, match="Mie"):
         H.OracleRun("port", cfg, big)
+
+
+def test_failure_categories_close(gold):
+    """Every failed history carries one failure code (the reference's closure check of its production failure
+    categories, CLARITAS/CLARITAS.py:9640-9655), in every scene of the reference fixture."""
+    z, meta = gold
+    for name in meta["scenes"]:
+        assert int(z[f"{name}/failure_code_counts"][1:].sum()) == int(z[f"{name}/status_counts"][4]), name
