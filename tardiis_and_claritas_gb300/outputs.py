@@ -113,6 +113,38 @@ def enforce_case_integrity(production: dict, diagnostic: dict) -> None:
                                  "and run_summary.json")
 
 
+def light_transport_cross_sections(diag: dict, cfg: dict) -> dict:
+    """Source-axis (x slab) and sensor-plane (z slab) sections of the light-history grids
+    (`_light_transport_cross_sections`, CLARITAS/CLARITAS.py:11645-11700): voxel centres, the slabs'
+    voxel indices (the nearest voxel when a slab is thinner than one), summed track length, post-scatter
+    track length and event counts, and the same as densities per diagnostic ray and unit volume."""
+    nx, ny, nz = (int(diag[k]) for k in ("nx", "ny", "nz"))
+
+    def centres(axis, n):
+        lo, hi = float(diag[axis + "_min_m"]), float(diag[axis + "_max_m"])
+        return np.linspace(lo, hi, n, endpoint=False) + (hi - lo) / (2 * n), (hi - lo) / n
+    (x, dx), (y, dy), (z, dz) = centres("x", nx), centres("y", ny), centres("z", nz)
+    rays = max(int(diag["diagnostic_rays_processed"]), 1)
+    vol = dx * dy * dz
+    xi = np.flatnonzero(np.abs(x) <= 0.5 * cfg["vertical_slice_thickness_m"])
+    zi = np.flatnonzero(np.abs(z) <= 0.5 * cfg["sensor_slice_thickness_m"])
+    if not len(xi):
+        xi = np.array([int(np.argmin(np.abs(x)))])
+    if not len(zi):
+        zi = np.array([int(np.argmin(np.abs(z)))])
+    total = np.asarray(diag["track_length_m"], dtype=float)        # [z][y][x]
+    post = np.asarray(diag["post_scatter_track_length_m"], dtype=float)
+    events = np.asarray(diag["scatter_event_count"], dtype=float)
+    q = {"x": x, "y": y, "z": z, "xi": xi, "zi": zi, "dx": dx, "dy": dy, "dz": dz, "voxel_volume": vol,
+         "vr": total[:, :, xi].sum(2), "vp": post[:, :, xi].sum(2), "ve": events[:, :, xi].sum(2),
+         "hr": total[zi].sum(0), "hp": post[zi].sum(0), "he": events[zi].sum(0)}
+    for k in ("vr", "vp", "ve"):
+        q[{"vr": "vd", "vp": "vpd", "ve": "ved"}[k]] = q[k] / (rays * vol * len(xi))
+    for k in ("hr", "hp", "he"):
+        q[{"hr": "hd", "hp": "hpd", "he": "hed"}[k]] = q[k] / (rays * vol * len(zi))
+    return q
+
+
 _DIAG_FIELDS = ("track_length_m", "post_scatter_track_length_m", "scatter_event_weight", "scatter_event_count")
 _TRAJ_FIELDS = ("trajectory_x0_m", "trajectory_y0_m", "trajectory_z0_m", "trajectory_x1_m", "trajectory_y1_m",
                 "trajectory_z1_m", "trajectory_particle_order", "trajectory_event_code")

@@ -162,3 +162,21 @@ def test_case_integrity_reports(tmp_path):
     assert (tmp_path / "light_transport_integrity_report.json").exists()
     with pytest.raises(O.CaseIntegrityError):
         O.enforce_case_integrity(prod, diag)
+
+
+def test_light_transport_cross_sections():
+    """The sections use every launched diagnostic history as denominator (the reference's check in
+    test_one_failure_keeps_launched_denominator) and pick the slabs around the axes."""
+    d = _diag_fixture()
+    rng = np.random.default_rng(3)
+    d.update(nx=6, ny=4, nz=5)
+    for k in O._DIAG_FIELDS:
+        d[k] = rng.uniform(0, 1, (5, 4, 6)).astype(np.float32)
+    q = O.light_transport_cross_sections(d, {"vertical_slice_thickness_m": 0.049, "sensor_slice_thickness_m": 0.049})
+    np.testing.assert_allclose(q["vd"], q["vr"] / (100 * q["dx"] * q["dy"] * q["dz"] * len(q["xi"])))
+    np.testing.assert_allclose(q["hed"], q["he"] / (100 * q["voxel_volume"] * len(q["zi"])))
+    assert q["vr"].shape == (5, 4) and q["hr"].shape == (4, 6)
+    np.testing.assert_array_equal(q["xi"], np.flatnonzero(np.abs(q["x"]) <= 0.0245))
+    thin = O.light_transport_cross_sections(d, {"vertical_slice_thickness_m": 1e-9, "sensor_slice_thickness_m": 1e-9})
+    assert len(thin["xi"]) == 1 and len(thin["zi"]) == 1
+    np.testing.assert_allclose(q["x"][0], -0.049 + 0.098 / 12)
