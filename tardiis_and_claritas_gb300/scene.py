@@ -199,10 +199,24 @@ class ModelConfig:
             raise ValueError("sediment_eddy_diffusivity_m2_s must be finite and >0")
         if not (np.isfinite(self.water_density_kg_per_m3) and 0.0 < self.water_density_kg_per_m3 < self.density_kg_per_m3):
             raise ValueError("water_density_kg_per_m3 must be positive and below particle density")
+        if not np.isfinite(self.water_dynamic_viscosity_pa_s) or self.water_dynamic_viscosity_pa_s <= 0.0:
+            raise ValueError("water_dynamic_viscosity_pa_s must be finite and >0")
+        if not np.isfinite(self.gravity_m_s2) or self.gravity_m_s2 <= 0.0:
+            raise ValueError("gravity_m_s2 must be finite and >0")
         if self.sediment_transport_quadrature_points < 64:
             raise ValueError("sediment_transport_quadrature_points must be >=64")
         if self.sediment_radial_lookup_points < 65:
             raise ValueError("sediment_radial_lookup_points must be >=65")
+        if not np.isfinite(self.meridional_circulation_ratio) or not (0.0 <= self.meridional_circulation_ratio <= 0.5):
+            raise ValueError("meridional_circulation_ratio must be finite and in [0,0.5]")
+        if self.meridional_grid_nr < 16 or self.meridional_grid_nz < 32:
+            raise ValueError("meridional solver grid must be at least 16 x 32")
+        if self.meridional_solver_max_iterations < 250 or self.meridional_solver_check_interval < 10:
+            raise ValueError("invalid meridional solver iteration controls")
+        if not np.isfinite(self.meridional_solver_tolerance) or not (0.0 < self.meridional_solver_tolerance < 1e-2):
+            raise ValueError("meridional_solver_tolerance must be in (0,1e-2)")
+        if not np.isfinite(self.meridional_solver_sor) or not (1.0 <= self.meridional_solver_sor < 1.95):
+            raise ValueError("meridional_solver_sor must be in [1,1.95)")
         vg = vortex_surface_geometry(self.free_surface_model, self.zmean, self.tube_inner_radius_m,
                                      self.vortex_wall_center_height_difference_m, self.vortex_core_radius_m,
                                      self.gravity_m_s2)
@@ -230,6 +244,23 @@ class ModelConfig:
             raise ValueError("chunk/batch sizes must be positive")
         if self.source_kind not in ("reference_led", "collimated_disc"):
             raise ValueError("source_kind must be 'reference_led' or 'collimated_disc'")
+        if self.aggregation_model not in ("none", "orthokinetic_compact", "orthokinetic_compact_fragmentation"):
+            raise ValueError("aggregation_model must be 'none', 'orthokinetic_compact', or "
+                             "'orthokinetic_compact_fragmentation'")
+        if not np.isfinite(self.aggregation_collision_exposure) or self.aggregation_collision_exposure < 0.0:
+            raise ValueError("aggregation_collision_exposure must be finite and >=0")
+        if not np.isfinite(self.fragmentation_breakup_exposure) or self.fragmentation_breakup_exposure < 0.0:
+            raise ValueError("fragmentation_breakup_exposure must be finite and >=0")
+        if not np.isfinite(self.fragmentation_reference_diameter_m) or self.fragmentation_reference_diameter_m <= 0.0:
+            raise ValueError("fragmentation_reference_diameter_m must be finite and >0")
+        if not np.isfinite(self.fragmentation_size_exponent) or not (0.0 <= self.fragmentation_size_exponent <= 6.0):
+            raise ValueError("fragmentation_size_exponent must be finite and in [0,6]")
+        if self.aggregation_model != "orthokinetic_compact_fragmentation" and self.fragmentation_breakup_exposure > 0.0:
+            raise ValueError("fragmentation_breakup_exposure requires aggregation_model=orthokinetic_compact_fragmentation")
+        if not (0.0 < self.aggregation_step_safety <= 0.25):
+            raise ValueError("aggregation_step_safety must be in (0,0.25]")
+        if self.aggregation_max_steps < 1:
+            raise ValueError("aggregation_max_steps must be >=1")
         if self.aggregation_model != "none":
             raise NotImplementedError("aggregation/fragmentation population balance is not part of this library")
 
@@ -329,11 +360,15 @@ def vortex_surface_geometry(model, zmean, R, delta_h, core_r, gravity=9.81):
     if not (g > 0.0 and np.isfinite(g)):
         raise ValueError("gravity must be finite and positive")
     R2 = R * R
+    if not (R2 > 0.0 and np.isfinite(R2)):
+        raise ValueError("vessel radius squared is outside the finite numerical range")
     if model == "flat" or D == 0.0:
         return dict(center_z=zmean, wall_z=zmean, h_inf=0.0, h_bar=0.0, angular_velocity_rad_s=0.0,
                     vtheta_peak_m_s=0.0, equivalent_rigid_body_rpm=0.0, equivalent_core_rpm=0.0)
     if model == "parabolic_vortex":
         omega = math.sqrt(2.0 * g * D / R2)
+        if not (np.isfinite(omega) and np.isfinite(omega * 60.0 / (2.0 * math.pi))):
+            raise ValueError("parabolic vortex derived angular velocity is non-finite")
         return dict(center_z=zmean - 0.5 * D, wall_z=zmean + 0.5 * D, h_inf=D, h_bar=0.5 * D,
                     angular_velocity_rad_s=omega, vtheta_peak_m_s=omega * R,
                     equivalent_rigid_body_rpm=omega * 60.0 / (2.0 * math.pi), equivalent_core_rpm=float("nan"))
@@ -342,9 +377,13 @@ def vortex_surface_geometry(model, zmean, R, delta_h, core_r, gravity=9.81):
     if not (a > 0.0):
         raise ValueError("localized Scully vortex requires positive core and vessel radii")
     a2 = a * a
+    if not (a2 > 0.0 and np.isfinite(a2)):
+        raise ValueError("localized Scully core radius squared is outside the finite numerical range")
     h_inf = D * (a2 + R2) / R2
     h_bar = h_inf * (1.0 - (a2 / R2) * math.log1p(R2 / a2))
     omega_c = math.sqrt(2.0 * g * h_inf / a2)
+    if not all(np.isfinite(q) for q in (h_inf, h_bar, omega_c)):
+        raise ValueError("localized Scully derived geometry or angular velocity is non-finite")
     return dict(center_z=zmean - h_bar, wall_z=zmean - h_bar + D, h_inf=h_inf, h_bar=h_bar,
                 angular_velocity_rad_s=omega_c, vtheta_peak_m_s=0.5 * omega_c * a,
                 equivalent_rigid_body_rpm=float("nan"), equivalent_core_rpm=omega_c * 60.0 / (2.0 * math.pi))

@@ -133,3 +133,31 @@ def test_provenance_diagnostics_from_device_partitions():
     assert np.all(np.isnan(mean[cnt == 0])) and np.all(np.isfinite(mean[cnt > 0]))
     assert set(out["wall_path_scores"]) == set(abi.WALL_PATH_NAMES)
     assert out["H170_last_event_angle_histogram_scores_by_event_code"].shape == (8, 6)
+
+
+@pytest.mark.parametrize("override", [
+    dict(free_surface_model="unknown", vortex_wall_center_height_difference_m=0.05),
+    dict(free_surface_model="parabolic_vortex", vortex_wall_center_height_difference_m=-0.01),
+    dict(free_surface_model="parabolic_vortex", vortex_wall_center_height_difference_m=float("nan")),
+    dict(sediment_eddy_diffusivity_m2_s=0.0), dict(water_density_kg_per_m3=2700.0),
+    dict(water_dynamic_viscosity_pa_s=0.0), dict(gravity_m_s2=float("inf")), dict(meridional_circulation_ratio=0.6),
+    dict(meridional_grid_nr=8), dict(meridional_solver_check_interval=5), dict(meridional_solver_tolerance=0.1),
+    dict(meridional_solver_sor=1.95), dict(aggregation_model="bogus"), dict(aggregation_collision_exposure=-1.0),
+    dict(fragmentation_size_exponent=7.0), dict(fragmentation_breakup_exposure=1.0),
+    dict(aggregation_step_safety=0.3), dict(aggregation_max_steps=0),
+])
+def test_fail_closed_configuration(override):
+    """Invalid settings are refused at construction, as in the reference's fail-closed configuration test
+    (CLARITAS/validate_claritas.py:437-551) and constructor (CLARITAS.py:5754-5999)."""
+    with pytest.raises(ValueError):
+        S.ModelConfig(**override).validate()
+
+
+def test_vortex_geometry_rejects_degenerate_inputs():
+    for radius in (0.0, float("nan")):
+        with pytest.raises(ValueError):
+            S.vortex_surface_geometry("parabolic_vortex", 0.05, radius, 0.05, -1.0)
+    with pytest.raises(ValueError):
+        S.vortex_surface_geometry("parabolic_vortex", 0.05, 1e-300, 1e300, -1.0)
+    with pytest.raises(ValueError):
+        S.vortex_surface_geometry("localized_scully_vortex", 0.05, 0.0465, 0.05, 1e-200)
