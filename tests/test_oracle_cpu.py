@@ -148,3 +148,36 @@ def test_failure_categories_close(gold):
     z, meta = gold
     for name in meta["scenes"]:
         assert int(z[f"{name}/failure_code_counts"][1:].sum()) == int(z[f"{name}/status_counts"][4]), name
+
+
+def test_oracle_meridional_solver_properties():
+    """The reference's validation of its meridional solver (CLARITAS/validate_claritas.py:1405-1460) on the
+    restated solver: at least 1000 iterations, converged, the normalised mass of every bin is the liquid
+    volume's, and the field is finite and non-negative in the liquid."""
+    cfg = S.ModelConfig(free_surface_model="parabolic_vortex", vortex_wall_center_height_difference_m=0.05,
+                        vortex_core_radius_m=0.02,
+                        sediment_transport_model="schiller_naumann_meridional_advection_diffusion",
+                        meridional_circulation_ratio=0.05, meridional_grid_nr=16, meridional_grid_nz=32,
+                        meridional_solver_max_iterations=3000, meridional_solver_check_interval=100,
+                        meridional_solver_tolerance=1e-05, meridional_solver_sor=1.5, particle_event_model="geometric")
+    parts = S.quartz_particles(500.0, n_bins=12)
+    orc = H.OracleRun("port", cfg, parts)
+    f = orc.sediment_field()
+    orc.close()
+    assert f["iterations"] >= 1000 and f["max_residual"] <= 1e-05
+    grid = f["grid"]
+    nr, nz = grid.shape[1:]
+    assert (nr, nz) == (16, 32)
+    rin, zmin, zmean, dh = (float(cfg.tube_inner_radius_m), float(cfg.zmin), float(cfg.zmean),
+                            float(cfg.vortex_wall_center_height_difference_m))
+    ztop = float(cfg.sediment_spec().grid_zmax)
+    r = (np.arange(nr) + 0.5) * rin / nr
+    z = zmin + (np.arange(nz) + 0.5) * (ztop - zmin) / nz
+    active = z[None, :] < (zmean + dh * (r * r / rin ** 2 - 0.5))[:, None]
+    dr, dz = rin / nr, (ztop - zmin) / nz
+    rw = np.arange(nr) * dr
+    vol = 0.5 * ((rw + dr) ** 2 - rw ** 2)[:, None] * dz
+    mass = np.sum(grid * active[None] * vol[None], axis=(1, 2))
+    np.testing.assert_allclose(mass, 0.5 * rin ** 2 * (zmean - zmin), rtol=4e-12, atol=2e-16)
+    vals = grid[:, active]
+    assert np.all(np.isfinite(vals)) and np.all(vals >= 0.0)
