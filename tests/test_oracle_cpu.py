@@ -181,3 +181,19 @@ def test_oracle_meridional_solver_properties():
     np.testing.assert_allclose(mass, 0.5 * rin ** 2 * (zmean - zmin), rtol=4e-12, atol=2e-16)
     vals = grid[:, active]
     assert np.all(np.isfinite(vals)) and np.all(vals >= 0.0)
+
+
+@pytest.mark.parametrize("vortex", ["parabolic_vortex", "localized_scully_vortex"])
+def test_oracle_full_ray_without_failures(vortex):
+    """The reference's full-ray validation case (CLARITAS/validate_claritas.py:1461-1540: stirred default cell,
+    Schiller-Naumann sediment, conditional closure, 2048 rays, seed 24630001) ends every history without a
+    production failure; absorbing bins exercise the closure."""
+    cfg = S.ModelConfig(free_surface_model=vortex, vortex_wall_center_height_difference_m=0.05, vortex_core_radius_m=0.02,
+                        sediment_transport_model="schiller_naumann_drift_diffusion", meridional_circulation_ratio=0.0,
+                        particle_event_model="hybrid_mie_exact_rate", hybrid_wave_scale=1.0, max_internal_bounces=4095)
+    orc = H.OracleRun("port", cfg, S.quartz_particles(500.0, n_bins=32, k=1e-4))
+    tal, _ = orc.trace(S.run_params(2048, seed=24630001))
+    orc.close()
+    assert int(tal["failure_code_counts"][1:].sum()) == 0 and int(tal["status_counts"][4]) == 0
+    assert int(tal["status_counts"][5]) > 0 and int(tal["conditional_stats"][0]) > 0
+    assert int(tal["status_counts"].sum()) == 2048
