@@ -333,15 +333,54 @@ class ClaritasForwardModel:
                                         max_residual=f["max_residual"])
         return parts
 
+    # the reference's diagnostic host keys (CLARITAS.py:6726-6767) that the library's tables provide
+    _HOST_KEYS = {"size_parameter": "size_parameter", "qext": "qext", "qsca": "qsca", "qabs": "qabs",
+                  "qback": "qback", "asymmetry_g": "asym_g", "single_scattering_albedo": "albedo",
+                  "radius_m": "radius", "number_density_by_bin": "number_density", "mu_geom_by_bin": "mu_geom_bin",
+                  "mu_sca_by_bin": "mu_sca_bin", "mu_ext_by_bin": "mu_ext_bin", "mu_wave_by_bin": "mu_wave_bin",
+                  "mu_event_by_bin": "mu_event_bin"}
+    # and its device tables (:6931-6965), here host copies
+    _DEVICE_KEYS = {"radius": "radius", "gcdf": "geometric_cdf", "wcdf": "wave_cdf", "phase_cdf": "phase_cdf",
+                    "theta": "theta", "qsca": "qsca", "qext": "qext", "mu_channels": "mu_scalars",
+                    "trace_geom_bin": "trace_geom_bin", "trace_wave_bin": "trace_wave_bin",
+                    "sed_majorants": "sed_majorants"}
+
     def _prepare_gpu_particle_physics(self, material, concentration_g_per_L, weights=None,
                                       weight_mode="mass_fraction") -> dict:
-        """The reference's physics preparation (CLARITAS.py:6036-6965): per-bin arrays of the population
-        (``d``, ``w``, ``nidx``, ``kidx``), the bin count, the phase-grid size and the tables (``host``)."""
+        """The reference's physics preparation (CLARITAS.py:6036-6965) and its return value (:6931-6965):
+        the population's per-bin arrays (``d``, ``w``, ``nidx``, ``kidx``), ``n``, ``ntheta``, the tables
+        under the reference's ``device`` keys (host copies: this library keeps its device tables inside the
+        context) and the diagnostics under its ``host`` keys, as far as the library computes them (the
+        population-balance and per-point sediment diagnostics are not part of it)."""
         parts = self._prepare(material, concentration_g_per_L, weights, weight_mode)
         ph = self._physics
+        n = int(parts.diameter_m.size)
+        device = {ref: np.asarray(ph[mine]).copy() for ref, mine in self._DEVICE_KEYS.items()}
+        device["phase_cdf"] = device["phase_cdf"].reshape(n, -1)
+        device["n"], device["k"] = parts.n_real.copy(), parts.k_imag.copy()
+        if self.config.sediment_transport_model == "schiller_naumann_meridional_advection_diffusion":
+            f = self._context().sediment_field()
+            device.update(sed_grid=f["grid"], sed_grid_nr=int(f["nr"]), sed_grid_nz=int(f["nz"]),
+                          sed_grid_zmax=float(self.config.sediment_spec().grid_zmax))
+        host = {ref: np.asarray(ph[mine]).copy() for ref, mine in self._HOST_KEYS.items()}
+        sg = math.pi * host["radius_m"] ** 2
+        host.update(diameter_m=parts.diameter_m.copy(), n_real=parts.n_real.copy(), k_imag=parts.k_imag.copy(),
+                    geometric_cross_section_m2=sg, scattering_cross_section_m2=host["qsca"] * sg,
+                    extinction_cross_section_m2=host["qext"] * sg)
+        theta, cdf = device["theta"], device["phase_cdf"]
+        for lo, hi in ((165.0, 175.0), (169.0, 171.0)):  # near-backscatter band probabilities (:6780-6799)
+            key = f"mie_phase_probability_{int(lo)}_{int(hi)}_by_bin"
+            if self.config.particle_event_model == "hybrid_mie_excess" and theta.size > 2:
+                at = lambda deg: np.array([np.interp(math.radians(deg), theta, row) for row in cdf])  # noqa: E731
+                host[key] = np.maximum(at(hi) - at(lo), 0.0)
+            else:
+                host[key] = np.zeros(n)
+        if self.config.sediment_transport_model == "schiller_naumann_meridional_advection_diffusion":
+            host.update(meridional_solver_iterations=int(self._meridional["iterations"]),
+                        meridional_solver_max_residual=float(self._meridional["max_residual"]),
+                        meridional_solver_tolerance=float(self.config.meridional_solver_tolerance))
         return dict(d=parts.diameter_m.copy(), w=parts.weight.copy(), nidx=parts.n_real.copy(),
-                    kidx=parts.k_imag.copy(), n=int(parts.diameter_m.size), device=self.device, host=ph,
-                    ntheta=int(ph["theta"].size))
+                    kidx=parts.k_imag.copy(), n=n, device=device, host=host, ntheta=int(theta.size))
 
     def phase_table_diagnostics(self, material, concentration_g_per_L, weights=None, weight_mode="mass_fraction"):
         """(theta [n_theta], cdf [n_bins, n_theta]) of the Mie phase tables (CLARITAS.py:7146)."""

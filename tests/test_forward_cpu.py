@@ -161,3 +161,71 @@ def test_vortex_geometry_rejects_degenerate_inputs():
         S.vortex_surface_geometry("parabolic_vortex", 0.05, 1e-300, 1e300, -1.0)
     with pytest.raises(ValueError):
         S.vortex_surface_geometry("localized_scully_vortex", 0.05, 0.0465, 0.05, 1e-200)
+
+
+class _OracleContext:
+    """A stand-in for lib.Context that prepares scenes in the CPU oracle (facade tests without a GPU)."""
+
+    def __init__(self):
+        import oracle_harness as H
+        self.lib, _ = H.load("port")
+        self.h = None
+
+    def set_scene(self, sp):
+        self.sp = sp
+
+    def build_particles(self, ps, ss):
+        import ctypes as C
+        self.h = C.c_void_p()
+        assert self.lib.clo_prepare(C.byref(self.sp), C.byref(ps), C.byref(ss), C.byref(self.h)) == 0
+        self.n_bins, self.n_theta = int(ps.n_bins), self.lib.clo_n_theta(self.h)
+
+    def physics(self):
+        import ctypes as C
+        from tardiis_and_claritas_gb300 import abi
+        pp, arrays = abi.alloc_physics(self.n_bins, self.n_theta)
+        self.lib.clo_read_physics(self.h, C.byref(pp))
+        return arrays
+
+    def sediment_field(self):
+        import ctypes as C
+        f = self.lib.clo_read_sediment_field
+        f.argtypes = [C.c_void_p, C.c_void_p] + [C.c_void_p] * 4
+        nr, nz, it, res = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        f(self.h, None, C.byref(nr), C.byref(nz), C.byref(it), C.byref(res))
+        g = np.zeros((self.n_bins, nr.value, nz.value))
+        f(self.h, g.ctypes.data_as(C.c_void_p), None, None, None, None)
+        return {"grid": g, "nr": nr.value, "nz": nz.value, "iterations": it.value, "max_residual": res.value}
+
+
+@pytest.mark.parametrize("transport", ["schiller_naumann_drift_diffusion",
+                                       "schiller_naumann_meridional_advection_diffusion"])
+def test_prepare_returns_the_reference_structure(transport):
+    """_prepare_gpu_particle_physics returns the reference's dict (CLARITAS.py:6931-6965): population arrays,
+    device tables under its keys, host diagnostics under its keys."""
+    m = F.ClaritasForwardModel(particle_event_model="hybrid_mie_excess", free_surface_model="parabolic_vortex",
+                               vortex_wall_center_height_difference_m=0.05, sediment_transport_model=transport,
+                               meridional_grid_nr=16, meridional_grid_nz=32)
+    ctx = _OracleContext()
+    ctx.set_scene(m.config.to_scene_params())
+    m._ctx = ctx
+    parts = S.quartz_particles(500.0, n_bins=8)
+    out = m._prepare_gpu_particle_physics(parts, 0.5)
+    assert set(out) == {"d", "w", "nidx", "kidx", "n", "device", "host", "ntheta"}
+    assert out["n"] == 8 and out["ntheta"] == out["device"]["theta"].size == out["device"]["phase_cdf"].shape[1]
+    dev, host = out["device"], out["host"]
+    for k in ("radius", "n", "k", "gcdf", "wcdf", "phase_cdf", "theta", "qsca", "qext", "mu_channels",
+              "trace_geom_bin", "trace_wave_bin", "sed_majorants"):
+        assert k in dev, k
+    np.testing.assert_allclose(host["scattering_cross_section_m2"],
+                               host["qsca"] * np.pi * host["radius_m"] ** 2, rtol=1e-15)
+    np.testing.assert_allclose(host["single_scattering_albedo"], host["qsca"] / host["qext"], rtol=1e-12)
+    band = host["mie_phase_probability_165_175_by_bin"]
+    assert band.shape == (8,) and np.all(band >= 0) and np.all(band < 1) and np.any(band > 0)
+    assert np.all(host["mie_phase_probability_169_171_by_bin"] <= band)
+    if transport.endswith("meridional_advection_diffusion"):
+        assert dev["sed_grid"].shape == (8, 16, 32) and dev["sed_grid_nr"] == 16
+        assert host["meridional_solver_iterations"] >= 1000
+        assert host["meridional_solver_max_residual"] <= host["meridional_solver_tolerance"]
+    else:
+        assert "sed_grid" not in dev and "meridional_solver_iterations" not in host
