@@ -187,6 +187,49 @@ class _OracleContext:
         self.lib.clo_read_physics(self.h, C.byref(pp))
         return arrays
 
+    def set_light(self, enabled=False, **kw):
+        assert not enabled and not kw.get("heatmap_size"), "light diagnostics are not restated by the oracle"
+
+    def set_provenance(self, enabled):
+        self.prov_on = bool(enabled)
+
+    def read_provenance(self):
+        return self.prov_acc
+
+    def close(self):
+        if self.h:
+            self.lib.clo_free(self.h)
+            self.h = None
+
+    def trace_batch(self, runs):
+        """Each run through the oracle, with the device-only partitions filled from its per-ray outputs
+        (the same partitions the device counts)."""
+        import ctypes as C
+        import provenance_partitions as PP
+        from tardiis_and_claritas_gb300 import abi
+        from path_partitions import partitions_from_records
+        out = []
+        self.prov_acc = None
+        for run in runs:
+            n = int(run.n_rays)
+            T = abi.Tallies()
+            rec = np.zeros(n, dtype=abi.record_dtype())
+            prov = np.zeros((n, 13), np.int32)
+            defl = np.zeros((n, 5), np.float32)
+            f = self.lib.clo_trace_provenance
+            assert f(self.h, C.byref(run), C.byref(T), rec.ctypes.data_as(C.c_void_p),
+                     prov.ctypes.data_as(C.c_void_p), defl.ctypes.data_as(C.c_void_p), 0) == 0
+            t = T.as_dict()
+            order, gorder, sums, masks, acr = partitions_from_records(rec)
+            t.update(order_hits=order, geometric_order_hits=gorder, path_sums=sums, path_mask_hits=masks,
+                     acrylic_order_hits=acr)
+            out.append(t)
+            if self.prov_on:
+                p = PP.partitions(rec["interaction_count"], rec["native_id"], rec["mirror_id"], prov, defl[:, :2])
+                p.pop("causal_path_count", None)
+                self.prov_acc = p if self.prov_acc is None else {k: self.prov_acc[k] + p[k] for k in p}
+        return out
+
     def sediment_field(self):
         import ctypes as C
         f = self.lib.clo_read_sediment_field
@@ -229,3 +272,57 @@ def test_prepare_returns_the_reference_structure(transport):
         assert host["meridional_solver_max_residual"] <= host["meridional_solver_tolerance"]
     else:
         assert "sed_grid" not in dev and "meridional_solver_iterations" not in host
+
+
+def test_simulate_on_the_oracle_engine(tmp_path):
+    """The whole facade on CPU: simulate() in statistics batches through a stand-in context that traces
+    with the oracle (the reference's streams), the ForwardResult, its path diagnostics with every closure
+    of the reference, and the per-case files with their integrity reports."""
+    from tardiis_and_claritas_gb300 import outputs as O
+    kw = {k: v for k, v in S.small_cell_config().__dict__.items() if k not in ("source_kind", "disc_beam_radius_m")}
+    kw["statistics_batch_rays"] = 4096
+    m = F.ClaritasForwardModel(rng="reference", **kw)
+    ctx = _OracleContext()
+    ctx.set_scene(m.config.to_scene_params())
+    m._ctx = ctx
+    m.register_material("quartz", S.quartz_particles(1.0, n_bins=16))
+    res = m.simulate("quartz", 2.0, n_rays=16384, seed=3)
+    assert res.n_rays == 16384 and res.production_failure_count == 0
+    hw = 0.5 * (res.hardware_native_hits + res.hardware_mirror_hits)
+    np.testing.assert_allclose(res.hardware_symmetry_scores, hw)
+    assert hw.sum() > 0 and np.isfinite(res.hardware_normalized_jackknife_se[hw > 0]).all()
+    pd = res.detector_particle_path_diagnostics
+    for key in ("exact_particle_order", "exact_geometric_order", "interaction_order", "multiple_branch",
+                "acrylic_reflection_order", "first_particle_bin", "last_particle_bin", "causal_last_event",
+                "causal_first_event", "wall_path"):
+        np.testing.assert_allclose(pd[key + "_partition_closure_error_scores"], 0.0, atol=1e-9, err_msg=key)
+    assert pd["first_particle_bin_scores"].shape == (16, 18)
+    np.testing.assert_allclose(pd["ballistic_scores"] + pd["any_particle_scores"], hw)
+    rows = O.write_detector_outputs(tmp_path, "quartz", 2.0, 860.0, 3, res)
+    assert len(rows) == 18
+    d = O.write_run_summary(tmp_path, "quartz", 2.0, 860.0, 3, "CPU oracle", 1.0, res, m.config)
+    assert d["production_integrity"]["status"] == "ok" and not d["production_integrity"]["fatal"]
+    prod, diag = O.write_case_integrity(tmp_path, res)
+    O.enforce_case_integrity(prod, diag)
+    m.close()
+
+
+def test_adaptive_simulate_on_the_oracle_engine():
+    """The adaptive stopping rule (CLARITAS.py:8818-8880) over statistics batches: it stops at the first batch
+    whose cumulative score reaches the target, and the provenance counts only the batches it kept."""
+    kw = {k: v for k, v in S.small_cell_config().__dict__.items() if k not in ("source_kind", "disc_beam_radius_m")}
+    kw["statistics_batch_rays"] = 2048
+    m = F.ClaritasForwardModel(rng="reference", **kw)
+    ctx = _OracleContext()
+    ctx.set_scene(m.config.to_scene_params())
+    m._ctx = ctx
+    m.register_material("quartz", S.quartz_particles(1.0, n_bins=16))
+    full = m.simulate("quartz", 2.0, n_rays=20480, seed=4)
+    per_batch = full.hardware_symmetry_scores.sum() / 10
+    res = m.simulate("quartz", 2.0, n_rays=2048, seed=4, target_detector_score=2.5 * per_batch, max_rays=20480)
+    assert res.stopped_adaptively and res.n_rays % 2048 == 0 and 2048 <= res.n_rays < 20480
+    assert res.hardware_symmetry_scores.sum() >= 2.5 * per_batch
+    pd = res.detector_particle_path_diagnostics
+    np.testing.assert_allclose(pd["wall_path_partition_closure_error_scores"], 0.0, atol=1e-9)
+    np.testing.assert_allclose(pd["first_particle_bin_partition_closure_error_scores"], 0.0, atol=1e-9)
+    m.close()
