@@ -58,3 +58,18 @@ def test_version_and_null_arguments(library):
 def test_resource_report_available(library):
     rep = build_ext.resource_report()
     assert "photon_kernel" in rep and "registers" in rep
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/claritas_gb.h is consumable from C (cgo, JNI, ctypes generators): it compiles as strict C99."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    src = tmp_path / "h.c"
+    src.write_text('#include "claritas_gb.h"\nint main(void) { clr_tallies t; clr_path_provenance p; '
+                   '(void)t; (void)p; return 0; }\n')
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        "-fsyntax-only", str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
