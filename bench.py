@@ -32,7 +32,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 # Work per photon of the wavefront engine on each workload (counter-based stream), summed over every
-# stage kernel of one ncu capture of a 4e6-photon trace (see profiles/wavefront_stages_full_scene.md):
+# stage kernel of one ncu capture of a 4e6-photon trace of the same scene:
 # warp instructions issued, FP64 flops executed (DFMA counted as 2) and DRAM bytes read + written.
 # The issue-slot roofline divides warp instructions issued per second by 4 schedulers x SMs x clock.
 PER_PHOTON = {"full": {"warp_inst": 423.5, "fp64_flops": 17.1, "dram_bytes": 981.8}, "small": None, "sweep": None}

@@ -482,18 +482,23 @@ int clr_last_launches(const clr_ctx* ctx, int64_t* launches, int64_t* passes);
 int clr_calibrate(clr_ctx* ctx, int which, double* ops_per_second);
 
 /* Allocation-free Mie tables (no reference counterpart; the reference always allocates through
- * CuPy). Computes, for n_bins <= CLR_NOALLOC_MAX_BINS (16) particle bins and
+ * CuPy). For callers that must not allocate device memory: a loop whose device memory belongs to
+ * another framework's pool, where a cudaMalloc/cudaFree per iteration would synchronise the device.
+ * Computes, for n_bins <= CLR_NOALLOC_MAX_BINS (16) particle bins and
  * 2 <= n_theta <= CLR_NOALLOC_MAX_THETA (4097) angles, the extinction and scattering efficiencies,
  * the asymmetry parameter, the theta grid and the per-bin phase CDF -- the same kernels and values as
  * clr_build_particles -- into caller-owned DEVICE buffers (d_qext, d_qsca, d_asym_g: [n_bins];
  * d_theta: [n_theta]; d_phase_cdf: [n_bins][n_theta]) on `stream` (a cudaStream_t, or NULL for the
  * context's stream). The inputs d_diameter_m, d_n_real, d_k_imag are device arrays of n_bins doubles.
  * No memory is allocated or freed: the scratch is a fixed set of file-scope device arrays (about 3 MB
- * per device) whose addresses are resolved on the first call for each device -- make that first call
- * before any stream capture. The scratch is shared by every context on a device, so calls must not
- * overlap on one device (serialise them). Only the error word is reset per call; the call synchronises
- * `stream` to read it and returns CLR_ERR_PRECOMPUTE with "error code k" on a Mie failure, and
- * CLR_ERR_INVALID_ARGUMENT (with the limits in the message) for sizes beyond the scratch. */
+ * per device, held by every device that loads the library until the process exits) whose addresses
+ * are resolved on the first call for each device and kept for the life of the process, so calls after
+ * a cudaDeviceReset of that device are not supported. The scratch is shared by every context on a
+ * device, so calls that overlap on one device race: serialise them. Only the error word is reset per
+ * call; the call then copies it to the host and synchronises `stream`, so it must not be called while
+ * `stream` is being captured into a CUDA graph. It returns CLR_ERR_PRECOMPUTE with "error code k" on a
+ * Mie failure (the scratch stays usable for the next call), and CLR_ERR_INVALID_ARGUMENT (with the
+ * limits in the message) for sizes beyond the scratch. */
 #define CLR_NOALLOC_MAX_BINS 16
 #define CLR_NOALLOC_MAX_THETA 4097
 int clr_mie_phase_noalloc(clr_ctx* ctx, const double* d_diameter_m, const double* d_n_real, const double* d_k_imag,

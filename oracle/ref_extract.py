@@ -7,7 +7,11 @@ the import works without a GPU) and writes that string, byte for byte, to
 ``oracle/_ref/claritas_cuda_src.inc``. Nothing it writes is committed:
 ``oracle/_ref/`` is git-ignored. Run from anywhere::
 
-    python oracle/ref_extract.py [--reference /root/reference]
+    python oracle/ref_extract.py [--reference DIR]
+
+The reference checkout is found by ``reference_root()``: the directory named by the
+CLARITAS_REFERENCE_DIR environment variable, else a checkout named ``reference`` beside
+this repository.
 """
 from __future__ import annotations
 
@@ -21,8 +25,16 @@ OUT_DIR = os.path.join(HERE, "_ref")
 OUT = os.path.join(OUT_DIR, "claritas_cuda_src.inc")
 
 
-def extract(reference_root: str = "/root/reference") -> str:
-    mod_dir = os.path.join(reference_root, "CLARITAS")
+def reference_root() -> str:
+    """The reference checkout: $CLARITAS_REFERENCE_DIR, else ``reference`` beside this repository."""
+    env = os.environ.get("CLARITAS_REFERENCE_DIR")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
+def extract(reference_root_dir: str | None = None) -> str:
+    mod_dir = os.path.join(reference_root_dir or reference_root(), "CLARITAS")
     if not os.path.isfile(os.path.join(mod_dir, "CLARITAS.py")):
         raise FileNotFoundError(f"reference module not found under {mod_dir}")
     sys.path.insert(0, mod_dir)
@@ -47,6 +59,6 @@ def extract(reference_root: str = "/root/reference") -> str:
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None, help="reference checkout (default: reference_root())")
     a = ap.parse_args()
     print(extract(a.reference))

@@ -16,6 +16,10 @@ from .build_ext import LIB_PATH
 _lock = threading.Lock()
 _lib = None
 
+# limits of clr_mie_phase_noalloc's fixed device scratch (CLR_NOALLOC_MAX_BINS / _THETA)
+NOALLOC_MAX_BINS = 16
+NOALLOC_MAX_THETA = 4097
+
 
 class ClaritasLibraryError(RuntimeError):
     pass

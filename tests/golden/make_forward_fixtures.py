@@ -11,7 +11,11 @@ import sys
 
 import numpy as np
 
-REF = "/root/reference/CLARITAS"
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
+from ref_extract import reference_root  # noqa: E402
+
+REF = os.path.join(reference_root(), "CLARITAS")
 
 
 def main() -> None:
