@@ -68,8 +68,19 @@ enum {
 /* photon weighting */
 enum {
     CLR_WEIGHT_ANALOG = 0,   /* reference semantics: absorption is terminal, every weight is 1 */
-    CLR_WEIGHT_IMPLICIT = 1  /* implicit capture at absorbing bins + Russian roulette below a threshold */
+    /* no reference counterpart (counter-based stream only): absorption is never sampled; at an absorbing
+       particle the photon scatters and its weight is multiplied by the survival probability (the particle
+       albedo in the conditional closure, exp(-alpha chord) per internal chord otherwise, exp(-mu_a d) per
+       water flight); below roulette_threshold Russian roulette keeps it with probability
+       w / roulette_survival at weight roulette_survival, else ends it with CLR_STATUS_ROULETTE. Detector
+       weight sums (clr_tallies.weight_*) are then unbiased estimates of the analog hit counts. */
+    CLR_WEIGHT_IMPLICIT = 1
 };
+
+/* photon end status (clr_tallies.status_counts): the reference's codes 0..8 (trace_kernel st,
+ * CLARITAS/CLARITAS.py:4617-5066: 1 left into the air, 2 water-boundary exit, 3 rejected at the source,
+ * 4 failure, 5 absorbed, 6 open top, 7 bottom exterior, 8 trapped), and one of this library's */
+#define CLR_STATUS_ROULETTE 9       /* weighted runs: ended by Russian roulette */
 
 /* source models */
 enum {
@@ -112,7 +123,11 @@ typedef struct clr_scene_params {
     int32_t source_kind;
     float disc_radius;              /* collimated disc beam radius */
     float disc_height;              /* beam axis height z (same frame) */
-    int32_t reserved[4];
+    /* absorption coefficient of the water itself (1/m; no reference counterpart, whose water does not
+     * absorb; 0 keeps the reference's transport and draw sequence). Analog runs end a photon at an
+     * exponential absorption distance (status 5), weighted runs multiply its weight by exp(-mu_a d). */
+    float water_absorption;
+    int32_t reserved[3];
 } clr_scene_params;
 
 /* Particle population and the inputs of the Mie/rate precompute
@@ -475,6 +490,12 @@ int clr_last_kernel_ms(const clr_ctx* ctx, float* ms);
  * nodes per pass plus one initialisation kernel; the persistent kernel is one launch) and the number
  * of wavefront passes (0 for the persistent kernel). No reference counterpart. */
 int clr_last_launches(const clr_ctx* ctx, int64_t* launches, int64_t* passes);
+
+/* Engine profile of the last clr_trace* / clr_sweep_trace call (no reference counterpart), the first n of:
+ * [0] wavefront pass graphs launched, [1] kernel launches, [2] photons handed to the tail kernel (0 when it
+ * did not run), [3] tail-kernel device time (ms, CUDA events around its launch), [4] the call's device time
+ * (ms, as clr_last_kernel_ms). */
+int clr_last_engine_stats(const clr_ctx* ctx, double* out, int n);
 
 /* Calibration kernels for roofline denominators (no reference counterpart): sustained
  * arithmetic throughput of this device in operations per second, counting a fused

@@ -642,7 +642,8 @@ int clo_prepare(const clr_scene_params* sp, const clr_particle_spec* ps, const c
             !(Dt > 0.0) || !(R > 0.0) || NQ < 64 || NRAD < 65) {
             snprintf(S->err, sizeof S->err, "sediment precompute error 31"); return 31;
         }
-        if (FSM < 0 || FSM > 2 || (DH > 0.0 && FSM == 0) || (FSM == 2 && !(CORE > 0.0))) {
+        /* surface model 3 (the Rankine vortex, new) is accepted with a supplied model-3 field only */
+        if (FSM < 0 || FSM > 3 || (FSM == 3 && TM != 3) || (DH > 0.0 && FSM == 0) || (FSM >= 2 && !(CORE > 0.0))) {
             snprintf(S->err, sizeof S->err, "sediment precompute error 32"); return 32;
         }
         double R2 = R * R, a2 = CORE * CORE, Hinf = 0.0, hbar = 0.0, omega2 = 0.0;
@@ -793,6 +794,11 @@ double clo_meridional_velocity(int fsm, double r, double z, double zmin, double 
 float clo_surface(int fsm, float x, float y, float zmean, float R, float dh, float core, float* normal) {
     if (normal) o_surface_normal(x, y, R, fsm, dh, core, normal, normal + 1, normal + 2);
     return o_surface_z(x, y, zmean, R, fsm, dh, core);
+}
+
+float clo_surface_hit(int fsm, float x, float y, float z, float vx, float vy, float vz, float zmean, float R, float dh,
+                      float core) {
+    return o_surface_hit(x, y, z, vx, vy, vz, zmean, R, fsm, dh, core);
 }
 
 double clo_local_scale(clo_state* S, int pidx, float x, float y, float z) {

@@ -38,6 +38,9 @@ double clo_meridional_velocity(int fsm, double r, double z, double zmin, double 
                                double upeak, double* uz);
 /* free-surface height at (x, y) and, when normal is not NULL, its unit normal (into the water) */
 float clo_surface(int fsm, float x, float y, float zmean, float R, float dh, float core, float* normal);
+/* first positive crossing of a ray with the free surface (FLT_MAX: none) */
+float clo_surface_hit(int fsm, float x, float y, float z, float vx, float vy, float vz, float zmean, float R, float dh,
+                      float core);
 /* the sediment concentration scale of bin pidx at a point, as the trace looks it up (FP32 position) */
 double clo_local_scale(clo_state* st, int pidx, float x, float y, float z);
 /* 1 when (r, z) lies in the liquid (above the bottom, below the free surface) */

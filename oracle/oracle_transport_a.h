@@ -328,10 +328,28 @@ static inline float o_scully_hbar(float R, float dh, float core) {
     float H = o_scully_hinf(R, dh, core);
     return H * (1.0f - (a2 / R2) * log1pf(R2 / a2));
 }
+/* Rankine vortex surface (model 3): new in this library, no reference lines to follow. Solid-body core
+ * r <= a and free vortex outside: z0 + k r^2 inside, z0 + k a^2 (2 - a^2/r^2) outside, with
+ * k = dh / (a^2 (2 - a^2/R^2)) and z0 = zmean - (k/R^2)(a^4/2 + 2 a^2 (R^2 - a^2) - 2 a^4 ln(R/a)) (volume
+ * conservation); a core wider than the tube is clamped to it. FP64 coefficients. */
+static inline void o_rankine(double zmean, double R, double dh, double core, double* k, double* a2, double* z0) {
+    double R2 = R * R, a = fmin(core, R);
+    *a2 = a * a;
+    *k = dh / (*a2 * (2.0 - *a2 / R2));
+    *z0 = zmean - (*k / R2) * (0.5 * *a2 * *a2 + 2.0 * *a2 * (R2 - *a2) - 2.0 * *a2 * *a2 * log(R / a));
+}
+static inline double o_rankine_z(double k, double a2, double z0, double q) {
+    return (q <= a2) ? z0 + k * q : z0 + k * a2 * (2.0 - a2 / q);
+}
 static inline float o_surface_z(float x, float y, float zmean, float R, int model, float dh, float core) {
     if (model == 0 || dh <= 0.0f) return zmean;
     float q = x * x + y * y;
     if (model == 1) return zmean + dh * (q / (R * R) - 0.5f);
+    if (model == 3) {
+        double k, a2, z0;
+        o_rankine(zmean, R, dh, core, &k, &a2, &z0);
+        return (float)o_rankine_z(k, a2, z0, (double)q);
+    }
     float a2 = core * core;
     float H = o_scully_hinf(R, dh, core);
     float hbar = o_scully_hbar(R, dh, core);
@@ -440,6 +458,51 @@ static double o_scully_bounded_root(double a3, double a2, double a1, double a0, 
     }
     return 1.0e300;
 }
+/* Rankine surface crossing (model 3, new): the ray's chord inside the tube split where it crosses the core
+ * cylinder; on each piece the first sign change of z(t) - zs(t) (a quadratic inside the core, the cubic
+ * q(t)(z(t) - z0 - 2 k a^2) + k a^4 outside) by the bounded-root search. */
+static float o_rankine_hit(float x, float y, float z, float vx, float vy, float vz, float zmean, float R, float dh,
+                           float core) {
+    double k, a2, z0;
+    o_rankine(zmean, R, dh, core, &k, &a2, &z0);
+    double X = x, Y = y, Z = z, VX = vx, VY = vy, VZ = vz, RR = (double)R * (double)R;
+    double Q2 = VX * VX + VY * VY, Q1 = 2.0 * (X * VX + Y * VY), Q0 = X * X + Y * Y;
+    if (!(Q2 > 0.0)) {
+        double t = (VZ != 0.0) ? (o_rankine_z(k, a2, z0, Q0) - Z) / VZ : 1.0e300;
+        return (t > 0.0 && Q0 <= RR * (1.0 + 2e-6) && t < 0.5 * (double)O_INF_F) ? (float)t : O_INF_F;
+    }
+    double dc = Q1 * Q1 - 4.0 * Q2 * (Q0 - RR);
+    if (dc < 0.0) return O_INF_F;
+    double q = -0.5 * (Q1 + copysign(sqrt(dc), Q1));
+    double ta = (q != 0.0) ? q / Q2 : -Q1 / (2.0 * Q2), tb = (q != 0.0) ? (Q0 - RR) / q : ta;
+    double lo = fmax(0.0, fmin(ta, tb)), hi = fmax(ta, tb);
+    if (!(hi > lo)) return O_INF_F;
+    double cuts[4];
+    int n = 0;
+    cuts[n++] = lo;
+    double dcore = Q1 * Q1 - 4.0 * Q2 * (Q0 - a2);
+    if (dcore > 0.0) {
+        q = -0.5 * (Q1 + copysign(sqrt(dcore), Q1));
+        ta = (q != 0.0) ? q / Q2 : -Q1 / (2.0 * Q2);
+        tb = (q != 0.0) ? (Q0 - a2) / q : ta;
+        double c1 = fmin(ta, tb), c2 = fmax(ta, tb);
+        if (c1 > lo && c1 < hi) cuts[n++] = c1;
+        if (c2 > lo && c2 < hi && c2 > c1) cuts[n++] = c2;
+    }
+    cuts[n++] = hi;
+    for (int i = 0; i < n - 1; ++i) {
+        double l = cuts[i], r = cuts[i + 1], m = 0.5 * (l + r), t;
+        double qm = Q0 + m * (Q1 + m * Q2);
+        if (qm <= a2) {
+            t = o_scully_bounded_root(0.0, -k * Q2, VZ - k * Q1, Z - z0 - k * Q0, l, r);
+        } else {
+            double L = Z - z0 - 2.0 * k * a2;
+            t = o_scully_bounded_root(VZ * Q2, L * Q2 + VZ * Q1, L * Q1 + VZ * Q0, L * Q0 + k * a2 * a2, l, r);
+        }
+        if (t > 0.0 && t < 0.5 * (double)O_INF_F) return (float)t;
+    }
+    return O_INF_F;
+}
 /* first positive ray/free-surface intersection (:1715-1765) */
 static float o_surface_hit(float x, float y, float z, float vx, float vy, float vz, float zmean, float R, int model,
                           float dh, float core) {
@@ -448,6 +511,7 @@ static float o_surface_hit(float x, float y, float z, float vx, float vy, float 
         float t = (zmean - z) / vz;
         return (t > 0.0f) ? t : O_INF_F;
     }
+    if (model == 3) return o_rankine_hit(x, y, z, vx, vy, vz, zmean, R, dh, core);
     if (model == 1) {
         float aa = dh / (R * R);
         double A = -(double)aa * ((double)vx * vx + (double)vy * vy);
@@ -496,6 +560,14 @@ static inline void o_surface_normal(float x, float y, float R, int model, float 
     if (model == 1) {
         float aa = dh / (R * R);
         *nx = 2.0f * aa * x; *ny = 2.0f * aa * y; *nz = -1.0f;
+        o_normalize(nx, ny, nz);
+        return;
+    }
+    if (model == 3) {  /* dz/dr = 2 k r in the core, 2 k a^4 / r^3 outside */
+        double k, ra2, z0, qq = (double)x * x + (double)y * y;
+        o_rankine(0.0, R, dh, core, &k, &ra2, &z0);
+        float fac = (float)((qq <= ra2) ? 2.0 * k : 2.0 * k * ra2 * ra2 / (qq * qq));
+        *nx = fac * x; *ny = fac * y; *nz = -1.0f;
         o_normalize(nx, ny, nz);
         return;
     }

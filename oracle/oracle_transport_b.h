@@ -429,6 +429,10 @@ static int o_sphere_accessible(double cx, double cy, double cz, double radius, f
         double q = rmin * rmin, R2 = R * R;
         if (model == 1) {
             zsurf = (double)Zmean + d * (q / R2 - 0.5);
+        } else if (model == 3) {
+            double rk, ra2, rz0;
+            o_rankine((double)Zmean, R, d, a, &rk, &ra2, &rz0);
+            zsurf = o_rankine_z(rk, ra2, rz0, q);
         } else {
             double a2 = a * a;
             double H = d * (a2 + R2) / R2;

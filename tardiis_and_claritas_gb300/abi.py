@@ -71,6 +71,8 @@ WEIGHT_ANALOG = 0
 WEIGHT_IMPLICIT = 1
 SOURCE_REFERENCE_LED = 0
 SOURCE_COLLIMATED_DISC = 1
+STATUS_ABSORBED = 5
+STATUS_ROULETTE = 9  # weighted runs: ended by Russian roulette (CLR_STATUS_ROULETTE)
 
 EV_NAMES = [
     "interactions", "geometric", "wave", "coherent", "morphology",
@@ -105,8 +107,8 @@ class SceneParams(C.Structure):
         ("max_axial_bounces", i32),
         ("max_iterations", f32),
         ("event_model", i32), ("conditional_retries", i32), ("sediment_model", i32),
-        ("source_kind", i32), ("disc_radius", f32), ("disc_height", f32),
-        ("reserved", i32 * 4),
+        ("source_kind", i32), ("disc_radius", f32), ("disc_height", f32), ("water_absorption", f32),
+        ("reserved", i32 * 3),
     ]
 
 

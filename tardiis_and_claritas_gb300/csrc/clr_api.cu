@@ -6,6 +6,7 @@
 // the message. Configuration errors that the reference raises as ValueError in
 // its constructor are rejected by the Python layer before reaching here; the
 // checks below guard the ABI itself.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <cstdarg>
@@ -43,7 +44,11 @@ struct clr_ctx {
     long long* wave_begin = nullptr;
     unsigned* wave_live = nullptr;  // pinned
     cudaEvent_t wave_ev = nullptr;
+    cudaEvent_t tail_ev[2] = {nullptr, nullptr};  // timing events around the tail kernel
     int last_passes = 0;
+    int last_tail = 0;
+    unsigned last_tail_photons = 0;
+    float last_tail_ms = 0.0f;
     long long last_launches = 0;
     int run_cap = 0;  // runs the per-run buffers hold
     // scenario sweep (clr_sweep_build): scene parameters and tables of every scenario, carved from one
@@ -151,6 +156,8 @@ int clr_destroy(clr_ctx* ctx) {
     cudaFree(ctx->d_prov_rec);
     if (ctx->wave_live) cudaFreeHost(ctx->wave_live);
     if (ctx->wave_ev) cudaEventDestroy(ctx->wave_ev);
+    for (cudaEvent_t e : ctx->tail_ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -166,11 +173,19 @@ static int check_scene(clr_ctx* ctx, const clr_scene_params& s) {
         return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "TARDIIS radial/source geometry is inconsistent");
     if (!(s.zwall_top > s.zmean && s.zmean > s.zmin))
         return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "wall top must lie above the water domain");
-    if (s.free_surface_model < 0 || s.free_surface_model > 2 || s.sediment_model < 0 || s.sediment_model > 3 ||
+    if (s.free_surface_model < 0 || s.free_surface_model > 3 || s.sediment_model < 0 || s.sediment_model > 3 ||
         s.event_model < 0 || s.event_model > 5)
         return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "model code out of range");
     if (s.source_kind != CLR_SOURCE_REFERENCE_LED && s.source_kind != CLR_SOURCE_COLLIMATED_DISC)
         return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "unknown source_kind %d", s.source_kind);
+    if (s.free_surface_model == 3 && s.vortex_delta_h > 0.0f && !(s.vortex_core_radius > 0.0f))
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "the Rankine vortex surface needs a positive core radius");
+    if (s.free_surface_model == 3 && (s.sediment_model == 1 || s.sediment_model == 2))
+        return fail(ctx, CLR_ERR_UNSUPPORTED,
+                    "the analytic drift-diffusion sediment fields are defined for the reference's free surfaces; "
+                    "with the Rankine vortex use a uniform or a supplied (r, z) field");
+    if (!(s.water_absorption >= 0.0f) || !std::isfinite(s.water_absorption))
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "water_absorption must be finite and nonnegative");
     return CLR_OK;
 }
 
@@ -199,6 +214,10 @@ static int check_particles(clr_ctx* ctx, const clr_scene_params& sp, const clr_p
             return fail(ctx, CLR_ERR_PRECOMPUTE, "sediment transport precompute failed with error code 33");
         if (sp.sediment_model == 3 && ss->grid && (ss->grid_nr < 2 || ss->grid_nz < 2))
             return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "a supplied model-3 grid needs at least 2 x 2 cells");
+        if (sp.sediment_model == 3 && !ss->grid && sp.free_surface_model == 3)
+            return fail(ctx, CLR_ERR_UNSUPPORTED,
+                        "the meridional field solver follows the reference's free surfaces; with the Rankine vortex "
+                        "supply the (r, z) field");
         if (sp.sediment_model == 3 && !ss->grid) {
             // the reference's constructor rules for the solver settings (:5867-5887)
             if (ss->meridional_nr < 16 || ss->meridional_nz < 32)
@@ -462,6 +481,7 @@ static void tally_to_host(const DevTally& d, clr_tallies* out, int64_t n_rays) {
     for (int k = 0; k < CLR_N_STATUS; ++k) out->status_counts[k] = (int64_t)t.status[k];
     for (int k = 0; k < CLR_N_FAILURE_CODES; ++k) out->failure_code_counts[k] = (int64_t)t.failure[k];
     for (int k = 0; k < CLR_N_EVENT_COUNTERS; ++k) out->event_counts[k] = (int64_t)t.events[k];
+    out->event_counts[CLR_EV_ROULETTE_KILLS] = (int64_t)t.status[CLR_STATUS_ROULETTE];
     for (int k = 0; k < CLR_N_CONDITIONAL_STATS; ++k) out->conditional_stats[k] = t.cstats[k];
     for (int k = 0; k < 16; ++k) { out->entered_sums[k] = (int64_t)t.entered_sums[k]; out->ray_flags[k] = (int64_t)t.ray_flags[k]; }
     for (int k = 0; k < CLR_N_SUBCODES; ++k) out->failure_subcode_counts[k] = (int64_t)t.subcodes[k];
@@ -492,6 +512,8 @@ static int wave_pool_ready(clr_ctx* ctx) {
     CU(cudaMalloc(&ctx->wave_ctl, sizeof(WaveCtl)));
     CU(cudaHostAlloc((void**)&ctx->wave_live, 4 * sizeof(unsigned), cudaHostAllocDefault));
     CU(cudaEventCreateWithFlags(&ctx->wave_ev, cudaEventDisableTiming));
+    CU(cudaEventCreate(&ctx->tail_ev[0]));
+    CU(cudaEventCreate(&ctx->tail_ev[1]));
     ctx->wave_cap = cap;
     return CLR_OK;
 }
@@ -530,8 +552,16 @@ static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* 
             return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "run %d: ray range exceeds uint32 global ids", i);
         if (run->rng_mode != CLR_RNG_REFERENCE_XORSHIFT && run->rng_mode != CLR_RNG_PHILOX)
             return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "run %d: unknown rng_mode %d", i, run->rng_mode);
+        if (run->weight_mode != CLR_WEIGHT_ANALOG && run->weight_mode != CLR_WEIGHT_IMPLICIT)
+            return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "run %d: unknown weight_mode %d", i, run->weight_mode);
         if (run->weight_mode == CLR_WEIGHT_IMPLICIT && run->rng_mode != CLR_RNG_PHILOX)
             return fail(ctx, CLR_ERR_UNSUPPORTED, "implicit-capture weighting runs on the Philox stream only");
+        if (run->weight_mode == CLR_WEIGHT_IMPLICIT &&
+            !(run->roulette_threshold >= 0.0f && run->roulette_survival > run->roulette_threshold &&
+              run->roulette_survival <= 1.0f))
+            return fail(ctx, CLR_ERR_INVALID_ARGUMENT,
+                        "run %d: Russian roulette needs 0 <= roulette_threshold < roulette_survival <= 1 (got %g, %g)",
+                        i, (double)run->roulette_threshold, (double)run->roulette_survival);
         if (run->rng_mode != r0.rng_mode || run->weight_mode != r0.weight_mode || run->flags != r0.flags)
             return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "runs of one call must share rng_mode, weight_mode and flags");
     }
@@ -592,6 +622,7 @@ static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* 
         w.tallies = ctx->d_tally; w.records = d_records;
         w.ray = ctx->wave_ray; w.lane = ctx->wave_lane; w.meta = ctx->wave_meta; w.qbuf = ctx->wave_q;
         w.ctl = ctx->wave_ctl; w.cap = ctx->wave_cap; w.host_live = ctx->wave_live; w.flag_event = ctx->wave_ev;
+        w.tail_begin = ctx->tail_ev[0]; w.tail_end = ctx->tail_ev[1];
         w.light = d_light != nullptr;
         w.prov = prov ? ctx->wave_prov : nullptr;
         w.prov_rec = ctx->prov_rec_n > 0 ? ctx->d_prov_rec : nullptr;
@@ -599,23 +630,31 @@ static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* 
     CU(cudaEventRecord(ctx->ev0, st));
     ctx->last_passes = 0;
     ctx->last_launches = 0;
+    ctx->last_tail = 0;
+    ctx->last_tail_photons = 0;
+    ctx->last_tail_ms = 0.0f;
     if (persistent) {
         if (cb[n] > 0) CU(launch_photon_kernel(a));
         ctx->last_launches = cb[n] > 0 ? 1 : 0;
     } else if (total > 0) {
         const long long max_passes = 100000 + 8LL * max_iter;
-        cudaError_t e = a.rng_mode == CLR_RNG_PHILOX ? wave_run_philox(w, ctx->num_sms, st, max_passes, &ctx->last_passes)
-                                                     : wave_run_xor(w, ctx->num_sms, st, max_passes, &ctx->last_passes);
+        WaveRunInfo info;
+        cudaError_t e = a.rng_mode == CLR_RNG_PHILOX ? wave_run_philox(w, ctx->num_sms, st, max_passes, &info)
+                                                     : wave_run_xor(w, ctx->num_sms, st, max_passes, &info);
         if (e == cudaErrorLaunchTimeout)
             return fail(ctx, CLR_ERR_DEVICE_TIMEOUT, "wavefront engine did not drain within %lld passes", max_passes);
         CU(e);
-        ctx->last_launches = 1 + (long long)ctx->last_passes * (1 + CLR_WQ_COUNT);
+        ctx->last_passes = info.passes;
+        ctx->last_tail = info.tail;
+        ctx->last_tail_photons = info.tail_photons;
+        ctx->last_launches = 1 + (long long)info.passes * (1 + CLR_WQ_COUNT) + info.tail;
     }
     CU(cudaEventRecord(ctx->ev1, st));
     std::vector<DevTally> ht(n);
     CU(cudaMemcpyAsync(ht.data(), ctx->d_tally, n * sizeof(DevTally), cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     CU(cudaEventElapsedTime(&ctx->last_kernel_ms, ctx->ev0, ctx->ev1));
+    if (ctx->last_tail) CU(cudaEventElapsedTime(&ctx->last_tail_ms, ctx->tail_ev[0], ctx->tail_ev[1]));
     for (int i = 0; i < n; ++i) tally_to_host(ht[i], outs + i, runs[i].n_rays);
     return CLR_OK;
 }
@@ -1144,6 +1183,14 @@ int clr_last_launches(const clr_ctx* ctx, int64_t* launches, int64_t* passes) {
     if (!ctx || !launches || !passes) return CLR_ERR_INVALID_ARGUMENT;
     *passes = ctx->last_passes;
     *launches = ctx->last_launches;
+    return CLR_OK;
+}
+
+int clr_last_engine_stats(const clr_ctx* ctx, double* out, int n) {
+    if (!ctx || !out || n < 1) return CLR_ERR_INVALID_ARGUMENT;
+    const double v[5] = {(double)ctx->last_passes, (double)ctx->last_launches, (double)ctx->last_tail_photons,
+                         (double)ctx->last_tail_ms, (double)ctx->last_kernel_ms};
+    for (int i = 0; i < n && i < 5; ++i) out[i] = v[i];
     return CLR_OK;
 }
 

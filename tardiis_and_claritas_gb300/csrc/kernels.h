@@ -74,13 +74,21 @@ struct WaveLaunch {
     unsigned cap;                  // slots, a power of two
     unsigned* host_live;           // pinned host words: live, tail ready, photons in flight
     cudaEvent_t flag_event;
+    cudaEvent_t tail_begin, tail_end;  // timing events recorded around the tail kernel
     bool light;                    // light-history diagnostics on: the FLIGHT stage with its hooks
     uint4* prov;                   // [cap] particle-event provenance per slot; null unless counted
     uint4* prov_rec;               // [n_rays] provenance of every ray, with per-ray records; nullable
 };
 
-cudaError_t wave_run_xor(const WaveLaunch& w, int num_sms, cudaStream_t st, long long max_passes, int* passes);
-cudaError_t wave_run_philox(const WaveLaunch& w, int num_sms, cudaStream_t st, long long max_passes, int* passes);
+// What one engine execution did: pass graphs launched, and whether (with how many photons) the tail kernel ran.
+struct WaveRunInfo {
+    int passes;
+    int tail;
+    unsigned tail_photons;
+};
+cudaError_t wave_run_xor(const WaveLaunch& w, int num_sms, cudaStream_t st, long long max_passes, WaveRunInfo* info);
+cudaError_t wave_run_philox(const WaveLaunch& w, int num_sms, cudaStream_t st, long long max_passes,
+                            WaveRunInfo* info);
 size_t wave_ray_bytes();
 size_t wave_lane_bytes(int rng_mode);
 

@@ -79,7 +79,7 @@ __device__ __forceinline__ int conditional_body(
     float radius, float aspect, int orientation, float kappa, int max_bounces, float coherent, const float* cdf,
     const float* theta, int nt, float x, float y, float z, float vx, float vy, float vz, float rin, float zmin,
     float zmean, int surface, float delta, float core, int max_trials, unsigned long long* stats, CondState* cs,
-    int budget) {
+    int budget, float* wmul) {
     Hist h;
     memset(&h, 0, sizeof h);
     h.failure = OP_OTHER; h.subcode = 9002;
@@ -93,7 +93,14 @@ __device__ __forceinline__ int conditional_body(
         if ((ki > 0.0f && (pabs <= 0.0 || albedo >= 1.0)) || (albedo > 0.0 && albedo < MINP) || (pabs > 0.0 && pabs < MINP)) {
             h.subcode = 9003; ++stats[8]; *out = h; return 1;
         }
-        cs->target = (albedo < 1.0 && uniform53(s) >= albedo);
+        if (wmul && albedo > 0.0) {
+            // implicit capture (weighted runs): the photon always scatters and carries the survival
+            // probability instead of drawing the absorbed/scattered outcome
+            *wmul *= (float)albedo;
+            cs->target = 0;
+        } else {
+            cs->target = (albedo < 1.0 && uniform53(s) >= albedo);
+        }
         cs->started = 1;
         cs->trial = 0;
     }
@@ -156,11 +163,11 @@ __device__ __noinline__ int conditional_interaction(
     float radius, float aspect, int orientation, float kappa, int max_bounces, float coherent, const float* cdf,
     const float* theta, int nt, float x, float y, float z, float vx, float vy, float vz, float rin, float zmin,
     float zmean, int surface, float delta, float core, int max_trials, unsigned long long* gstats,
-    CondState* cs, int budget) {
+    CondState* cs, int budget, float* wmul) {
     unsigned long long stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int done = conditional_body(s, out, pidx, qs, qe, nm, nr, ki, wl, rough, radius, aspect, orientation, kappa,
                                       max_bounces, coherent, cdf, theta, nt, x, y, z, vx, vy, vz, rin, zmin, zmean,
-                                      surface, delta, core, max_trials, stats, cs, budget);
+                                      surface, delta, core, max_trials, stats, cs, budget, wmul);
 #pragma unroll
     for (int i = 0; i < 10; ++i)
         if (stats[i]) atomicAdd(gstats + i, stats[i]);
@@ -399,6 +406,29 @@ __device__ __forceinline__ void apply_moment(const DevScene& D, int pidx, float 
                                              float* vy, float* vz) {
     if (D.any_moment && pidx >= 0 && D.moment_mode[pidx])
         moment_constraint(vinx, viny, vinz, vx, vy, vz, (float)D.moment_a[pidx], (float)D.moment_b[pidx]);
+}
+
+// ---------------- weighted transport (no reference counterpart) ----------------
+// With weight_mode == CLR_WEIGHT_IMPLICIT (counter-based stream only) absorption is never sampled: at an
+// absorbing particle the photon always scatters and its weight is multiplied by the survival
+// probability (the particle albedo in the conditional closure, exp(-alpha chord) per internal chord of a
+// sphere or spheroid, exp(-mu_a travel) per water flight). The detector tallies then sum weights, and the
+// expected tallies equal the analog ones. A photon whose weight falls below roulette_threshold survives
+// with probability w / roulette_survival and then carries roulette_survival, else it ends with status
+// CLR_STATUS_ROULETTE: an unbiased cut of the long, low-weight tail.
+__device__ __forceinline__ bool weighted_run(const DevScene& D) { return D.weight_mode == CLR_WEIGHT_IMPLICIT; }
+
+// Russian roulette after a weight change; true when the photon was killed.
+template <class S>
+__device__ __forceinline__ bool roulette(const DevScene& D, Ray& r, S* st) {
+    if (!(r.w < D.roulette_threshold)) return false;
+    if (uniform(st) * D.roulette_survival < r.w) {
+        r.w = D.roulette_survival;
+        return false;
+    }
+    r.w = 0.0f;
+    r.st = CLR_STATUS_ROULETTE;
+    return true;
 }
 
 // True when the straight segment of length t from (x, y, z) along v stays inside the water: the
@@ -652,6 +682,17 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
             do_particle = freep < tbound;
             travel = do_particle ? freep : tbound;
         }
+        // absorption by the water itself (no reference counterpart; skipped, with no draw, when mu_a is 0)
+        bool water_absorbed = false;
+        if (P.water_absorption > 0.0f) {
+            if (weighted_run(D)) {
+                r.w *= expf(-P.water_absorption * travel);
+                if (roulette(D, r, st)) { res = WE_ENDED; break; }
+            } else {
+                const float da = -logf(fmaxf(uniform(st), 1e-12f)) / P.water_absorption;
+                if (da < travel) { travel = da; water_absorbed = true; }
+            }
+        }
         if (kLight && D.light) {  // the segment about to be flown (:4763-4772): heat maps for every ray, voxels for the first
             const LightDiag& LD = *D.light;
             if (LD.vis > 0) light_heat_segment(LD, x, y, z, vx, vy, vz, travel, RIN, ZMIN);
@@ -659,6 +700,7 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
         }
         x += travel * vx; y += travel * vy; z += travel * vz;
         r.wp += travel;
+        if (water_absorbed) { r.st = 5; res = WE_ENDED; break; }
         if (do_particle && !lazy) {
             bool end_out;
             if constexpr (kCounterStream<S>) {
@@ -819,7 +861,7 @@ __device__ __forceinline__ int closure_visit(const DevScene& D, Ray& r, S* opt, 
         D.prad[pidx], P.spheroid_aspect, P.orientation_model, P.orientation_kappa, P.max_particle_bounces, COHERENT,
         D.phase_cdf, D.theta, D.nt, x, y, z, vx, vy, vz, P.rin, P.zmin, P.zmean, P.free_surface_model,
         P.vortex_delta_h, P.vortex_core_radius, kind == CK_GEOM ? P.conditional_retries - 1 : P.conditional_retries,
-        cstats, cs, budget);
+        cstats, cs, budget, (kind == CK_FLIGHT && weighted_run(D)) ? &r.w : nullptr);
     if (!done) return 2;
     bool ended = false;
     do {
@@ -836,6 +878,7 @@ __device__ __forceinline__ int closure_visit(const DevScene& D, Ray& r, S* opt, 
         else { r.wic++; if (h.channel == 1) r.wcoh++; else r.wmorph++; }
         if (kind == CK_FLIGHT && h.status == 2) { r.st = 5; ended = true; break; }
         apply_moment(D, pidx, vinx, viny, vinz, &vx, &vy, &vz);
+        if (kind == CK_FLIGHT && weighted_run(D) && roulette(D, r, opt)) ended = true;
     } while (false);
     r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
     return ended ? 1 : 0;
@@ -887,7 +930,7 @@ __device__ __forceinline__ int water_geom_visit(const DevScene& D, Ray& r, S* op
         if constexpr (kCounterStream<S>)
             ps = f_sphere_sampled(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, prad,
                                   P.max_particle_bounces, sgx, sgy, sgz, fcx, fcy, fcz, &x, &y, &z, &vx, &vy, &vz,
-                                  &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
+                                  &ipath, &r.pc, &ppc, &pps, &pmb, &pmo, weighted_run(D) ? &r.w : nullptr);
         else
             ps = o_sphere_sampled(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, prad,
                                   P.max_particle_bounces, sgx, sgy, sgz, dscx, dscy, dscz, &x, &y, &z, &vx, &vy, &vz,
@@ -896,6 +939,7 @@ __device__ __forceinline__ int water_geom_visit(const DevScene& D, Ray& r, S* op
         if (ps != 1) { if (COND) atomicAdd(&cstats[8], 1ull); r.pf = ppc ? ppc : OP_OTHER; r.pfs = pps; r.st = 4; res = 1; break; }
         if (COND) { atomicAdd(&cstats[3], 1ull); atomicAdd(&cstats[7], 1ull); }
         apply_moment(D, pidx, vinx, viny, vinz, &vx, &vy, &vz);
+        if (weighted_run(D) && roulette(D, r, opt)) res = 1;
     } while (false);
     r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
     return res;
@@ -924,11 +968,13 @@ __device__ __forceinline__ bool water_morph(const DevScene& D, Ray& r, S* opt, u
         int ppc = 0, pps = 0, pmb = 0, pmo = 0;
         int ps = o_spheroid_event(opt, P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha, D.prad[pidx],
                                   P.spheroid_aspect, P.orientation_model, P.orientation_kappa, ffx, ffy, ffz,
-                                  P.max_particle_bounces, &vx, &vy, &vz, &ipath, &r.pc, &ppc, &pps, &pmb, &pmo);
+                                  P.max_particle_bounces, &vx, &vy, &vz, &ipath, &r.pc, &ppc, &pps, &pmb, &pmo,
+                                  weighted_run(D) ? &r.w : nullptr);
         if (ps == 2) { r.st = 5; ended = true; break; }
         if (ps != 1) { if (COND) atomicAdd(&cstats[8], 1ull); r.pf = ppc ? ppc : OP_OTHER; r.pfs = pps; r.st = 4; ended = true; break; }
         if (COND) { atomicAdd(&cstats[5], 1ull); atomicAdd(&cstats[7], 1ull); }
         apply_moment(D, pidx, vinx, viny, vinz, &vx, &vy, &vz);
+        if (weighted_run(D) && roulette(D, r, opt)) ended = true;
     } while (false);
     r.vx = vx; r.vy = vy; r.vz = vz;
     return ended;

@@ -315,10 +315,47 @@ __device__ __forceinline__ float o_scully_hbar(float R, float dh, float core) {
     float H = o_scully_hinf(R, dh, core);
     return H * (1.0f - (a2 / R2) * log1pf(R2 / a2));
 }
+/* Rankine vortex (free-surface model 3; no reference counterpart). A stirrer turning the liquid inside
+ * the core r <= a as a solid body at angular speed W and a free vortex outside (v = W a^2 / r) give, from
+ * the radial pressure balance, a surface z0 + k r^2 inside and z0 + k a^2 (2 - a^2 / r^2) outside, with
+ * k = W^2 / (2 g): continuous with its slope at r = a. k follows from the wall-centre height difference
+ * dh = k a^2 (2 - a^2 / R^2), and z0 = zmean - hbar from volume conservation (the area mean of the surface
+ * over the disc r <= R is the rest height zmean):
+ *   hbar = (k / R^2) (a^4 / 2 + 2 a^2 (R^2 - a^2) - 2 a^4 ln(R / a)).
+ * A core at least as wide as the tube is a solid-body (parabolic) surface. Heights are functions of
+ * q = r^2, so every caller works with q. */
+struct RankineF {
+    float k, a2, z0;
+};
+__device__ __forceinline__ RankineF f_rankine(float zmean, float R, float dh, float core) {
+    const float R2 = R * R, a = fminf(core, R), a2 = a * a;
+    const float k = dh / (a2 * (2.0f - a2 / R2));
+    const float hbar = (k / R2) * (0.5f * a2 * a2 + 2.0f * a2 * (R2 - a2) - 2.0f * a2 * a2 * logf(R / a));
+    RankineF g = {k, a2, zmean - hbar};
+    return g;
+}
+__device__ __forceinline__ float f_rankine_z(const RankineF& g, float q) {
+    return (q <= g.a2) ? g.z0 + g.k * q : g.z0 + g.k * g.a2 * (2.0f - g.a2 / q);
+}
+struct RankineD {
+    double k, a2, z0;
+};
+__device__ __forceinline__ RankineD d_rankine(double zmean, double R, double dh, double core) {
+    const double R2 = R * R, a = fmin(core, R), a2 = a * a;
+    const double k = dh / (a2 * (2.0 - a2 / R2));
+    const double hbar = (k / R2) * (0.5 * a2 * a2 + 2.0 * a2 * (R2 - a2) - 2.0 * a2 * a2 * log(R / a));
+    RankineD g = {k, a2, zmean - hbar};
+    return g;
+}
+__device__ __forceinline__ double d_rankine_z(const RankineD& g, double q) {
+    return (q <= g.a2) ? g.z0 + g.k * q : g.z0 + g.k * g.a2 * (2.0 - g.a2 / q);
+}
+
 __device__ __forceinline__ float o_surface_z(float x, float y, float zmean, float R, int model, float dh, float core) {
     if (model == 0 || dh <= 0.0f) return zmean;
     float q = x * x + y * y;
     if (model == 1) return zmean + dh * (q / (R * R) - 0.5f);
+    if (model == 3) return f_rankine_z(f_rankine(zmean, R, dh, core), q);
     float a2 = core * core;
     float H = o_scully_hinf(R, dh, core);
     float hbar = o_scully_hbar(R, dh, core);
@@ -428,8 +465,55 @@ __device__ __noinline__ double o_scully_bounded_root(double a3, double a2, doubl
     return 1.0e300;
 }
 /* first positive ray/free-surface intersection (:1715-1765) */
+/* Rankine surface crossing (FP64): the ray's chord inside the tube is split where it crosses the core
+ * cylinder q(t) = a^2; on a piece inside the core the crossing solves the quadratic z(t) - z0 - k q(t) = 0,
+ * outside it the cubic q(t) (z(t) - z0 - 2 k a^2) + k a^4 = 0 (q > 0 there, so the sign is that of
+ * z(t) - zs: negative below the surface). The first sign change is found by the bounded-root search. */
+__device__ __noinline__ float o_rankine_hit(float x, float y, float z, float vx, float vy, float vz, float zmean,
+                                           float R, float dh, float core) {
+    const RankineD g = d_rankine(zmean, R, dh, core);
+    const double X = x, Y = y, Z = z, VX = vx, VY = vy, VZ = vz, RR = (double)R * (double)R;
+    const double Q2 = VX * VX + VY * VY, Q1 = 2.0 * (X * VX + Y * VY), Q0 = X * X + Y * Y;
+    if (!(Q2 > 0.0)) {
+        const double t = (VZ != 0.0) ? (d_rankine_z(g, Q0) - Z) / VZ : 1.0e300;
+        return (t > 0.0 && Q0 <= RR * (1.0 + 2e-6) && t < 0.5 * (double)CLR_INF_F) ? (float)t : CLR_INF_F;
+    }
+    const double dc = Q1 * Q1 - 4.0 * Q2 * (Q0 - RR);
+    if (dc < 0.0) return CLR_INF_F;
+    double q = -0.5 * (Q1 + copysign(sqrt(dc), Q1));
+    double ta = (q != 0.0) ? q / Q2 : -Q1 / (2.0 * Q2), tb = (q != 0.0) ? (Q0 - RR) / q : ta;
+    const double lo = fmax(0.0, fmin(ta, tb)), hi = fmax(ta, tb);
+    if (!(hi > lo)) return CLR_INF_F;
+    double cuts[4];
+    int n = 0;
+    cuts[n++] = lo;
+    const double dcore = Q1 * Q1 - 4.0 * Q2 * (Q0 - g.a2);
+    if (dcore > 0.0) {
+        q = -0.5 * (Q1 + copysign(sqrt(dcore), Q1));
+        ta = (q != 0.0) ? q / Q2 : -Q1 / (2.0 * Q2);
+        tb = (q != 0.0) ? (Q0 - g.a2) / q : ta;
+        const double c1 = fmin(ta, tb), c2 = fmax(ta, tb);
+        if (c1 > lo && c1 < hi) cuts[n++] = c1;
+        if (c2 > lo && c2 < hi && c2 > c1) cuts[n++] = c2;
+    }
+    cuts[n++] = hi;
+    for (int i = 0; i < n - 1; ++i) {
+        const double l = cuts[i], r = cuts[i + 1], m = 0.5 * (l + r);
+        const double qm = Q0 + m * (Q1 + m * Q2);
+        double t;
+        if (qm <= g.a2) {
+            t = o_scully_bounded_root(0.0, -g.k * Q2, VZ - g.k * Q1, Z - g.z0 - g.k * Q0, l, r);
+        } else {
+            const double L = Z - g.z0 - 2.0 * g.k * g.a2;
+            t = o_scully_bounded_root(VZ * Q2, L * Q2 + VZ * Q1, L * Q1 + VZ * Q0, L * Q0 + g.k * g.a2 * g.a2, l, r);
+        }
+        if (t > 0.0 && t < 0.5 * (double)CLR_INF_F) return (float)t;
+    }
+    return CLR_INF_F;
+}
 __device__ __noinline__ float o_surface_hit_curved(float x, float y, float z, float vx, float vy, float vz, float zmean,
                                                  float R, int model, float dh, float core) {
+    if (model == 3) return o_rankine_hit(x, y, z, vx, vy, vz, zmean, R, dh, core);
     if (model == 1) {
         float aa = dh / (R * R);
         double A = -(double)aa * ((double)vx * vx + (double)vy * vy);
@@ -507,8 +591,95 @@ __device__ __forceinline__ float f_quadratic_min_positive(float A, float B, floa
 __device__ __forceinline__ float f_cubic(float c3, float c2, float c1, float c0, float t) {
     return ((c3 * t + c2) * t + c1) * t + c0;
 }
+/* First sign change of the polynomial c3 t^3 + c2 t^2 + c1 t + c0 on (l, r], FP32: the piece is split at
+ * the polynomial's turning points and the first bracketing sub-piece bisected to FP32 resolution. */
+__device__ float f_first_poly_root(float c3, float c2, float c1, float c0, float l0, float r0) {
+    if (!(r0 > l0)) return CLR_INF_F;
+    float cuts[4];
+    int n = 0;
+    cuts[n++] = l0;
+    const float A = 3.0f * c3, B = 2.0f * c2, Cd = c1;
+    if (A != 0.0f) {
+        const float disc = B * B - 4.0f * A * Cd;
+        if (disc >= 0.0f) {
+            const float q = -0.5f * (B + copysignf(sqrtf(disc), B));
+            const float r1 = (q != 0.0f) ? q / A : -B / (2.0f * A);
+            const float r2 = (q != 0.0f) ? Cd / q : r1;
+            const float s1 = fminf(r1, r2), s2 = fmaxf(r1, r2);
+            if (s1 > l0 && s1 < r0) cuts[n++] = s1;
+            if (s2 > l0 && s2 < r0 && s2 != s1) cuts[n++] = s2;
+        }
+    } else if (B != 0.0f) {
+        const float r = -Cd / B;
+        if (r > l0 && r < r0) cuts[n++] = r;
+    }
+    cuts[n++] = r0;
+    for (int i = 0; i < n - 1; ++i) {
+        float l = cuts[i], r = cuts[i + 1];
+        float fl = ((c3 * l + c2) * l + c1) * l + c0;
+        const float fr = ((c3 * r + c2) * r + c1) * r + c0;
+        if (l > 0.0f && fl == 0.0f) return l;
+        if ((fl < 0.0f && fr > 0.0f) || (fl > 0.0f && fr < 0.0f)) {
+            for (int j = 0; j < 40; ++j) {
+                const float m = l + 0.5f * (r - l);
+                if (m == l || m == r) break;
+                const float fm = ((c3 * m + c2) * m + c1) * m + c0;
+                if (fm == 0.0f) { l = r = m; break; }
+                if ((fl < 0.0f) == (fm < 0.0f)) { l = m; fl = fm; } else r = m;
+            }
+            const float t = l + 0.5f * (r - l);
+            return t > 0.0f ? t : CLR_INF_F;
+        }
+        if (r > 0.0f && fr == 0.0f) return r;
+    }
+    return CLR_INF_F;
+}
+/* Rankine surface crossing in FP32 (counter-based stream): the pieces of o_rankine_hit. */
+__device__ __noinline__ float f_rankine_hit(float x, float y, float z, float vx, float vy, float vz, float zmean,
+                                            float R, float dh, float core) {
+    const RankineF g = f_rankine(zmean, R, dh, core);
+    const float RR = R * R;
+    const float Q2 = vx * vx + vy * vy, Q1 = 2.0f * (x * vx + y * vy), Q0 = x * x + y * y;
+    if (!(Q2 > 0.0f)) {
+        const float t = (vz != 0.0f) ? (f_rankine_z(g, Q0) - z) / vz : CLR_INF_F;
+        return (t > 0.0f && Q0 <= RR * (1.0f + 2e-6f)) ? t : CLR_INF_F;
+    }
+    const float dc = Q1 * Q1 - 4.0f * Q2 * (Q0 - RR);
+    if (dc < 0.0f) return CLR_INF_F;
+    float q = -0.5f * (Q1 + copysignf(sqrtf(dc), Q1));
+    float ta = (q != 0.0f) ? q / Q2 : -Q1 / (2.0f * Q2), tb = (q != 0.0f) ? (Q0 - RR) / q : ta;
+    const float lo = fmaxf(0.0f, fminf(ta, tb)), hi = fmaxf(ta, tb);
+    if (!(hi > lo) || !isfinite(hi)) return CLR_INF_F;
+    float cuts[4];
+    int n = 0;
+    cuts[n++] = lo;
+    const float dcore = Q1 * Q1 - 4.0f * Q2 * (Q0 - g.a2);
+    if (dcore > 0.0f) {
+        q = -0.5f * (Q1 + copysignf(sqrtf(dcore), Q1));
+        ta = (q != 0.0f) ? q / Q2 : -Q1 / (2.0f * Q2);
+        tb = (q != 0.0f) ? (Q0 - g.a2) / q : ta;
+        const float c1 = fminf(ta, tb), c2 = fmaxf(ta, tb);
+        if (c1 > lo && c1 < hi) cuts[n++] = c1;
+        if (c2 > lo && c2 < hi && c2 > c1) cuts[n++] = c2;
+    }
+    cuts[n++] = hi;
+    for (int i = 0; i < n - 1; ++i) {
+        const float l = cuts[i], r = cuts[i + 1], m = 0.5f * (l + r);
+        const float qm = Q0 + m * (Q1 + m * Q2);
+        float t;
+        if (qm <= g.a2) {
+            t = f_first_poly_root(0.0f, -g.k * Q2, vz - g.k * Q1, z - g.z0 - g.k * Q0, l, r);
+        } else {
+            const float L = z - g.z0 - 2.0f * g.k * g.a2;
+            t = f_first_poly_root(vz * Q2, L * Q2 + vz * Q1, L * Q1 + vz * Q0, L * Q0 + g.k * g.a2 * g.a2, l, r);
+        }
+        if (t < CLR_INF_F) return t;
+    }
+    return CLR_INF_F;
+}
 __device__ __noinline__ float f_surface_hit_curved(float x, float y, float z, float vx, float vy, float vz,
                                                    float zmean, float R, int model, float dh, float core) {
+    if (model == 3) return f_rankine_hit(x, y, z, vx, vy, vz, zmean, R, dh, core);
     if (model == 1) {
         const float aa = dh / (R * R);
         const float A = -aa * (vx * vx + vy * vy);
@@ -591,6 +762,14 @@ __device__ __forceinline__ void o_surface_normal(float x, float y, float R, int 
     if (model == 1) {
         float aa = dh / (R * R);
         *nx = 2.0f * aa * x; *ny = 2.0f * aa * y; *nz = -1.0f;
+        o_normalize(nx, ny, nz);
+        return;
+    }
+    if (model == 3) {  // dz/dr = 2 k r inside the core, 2 k a^4 / r^3 outside
+        const RankineF g = f_rankine(0.0f, R, dh, core);
+        const float q = x * x + y * y;
+        const float fac = (q <= g.a2) ? 2.0f * g.k : 2.0f * g.k * g.a2 * g.a2 / (q * q);
+        *nx = fac * x; *ny = fac * y; *nz = -1.0f;
         o_normalize(nx, ny, nz);
         return;
     }

@@ -440,6 +440,8 @@ __device__ int o_sphere_accessible(double cx, double cy, double cz, double radiu
         double q = rmin * rmin, R2 = R * R;
         if (model == 1) {
             zsurf = (double)Zmean + d * (q / R2 - 0.5);
+        } else if (model == 3) {
+            zsurf = d_rankine_z(d_rankine((double)Zmean, R, d, a), q);
         } else {
             double a2 = a * a;
             double H = d * (a2 + R2) / R2;
@@ -462,7 +464,7 @@ __device__ int o_sphere_sampled(S* s, float n_medium, float n_particle, float k_
                             float rough_alpha, float radius, int max_bounces, float gnx, float gny, float gnz,
                             double cx, double cy, double cz, float* x, float* y, float* z, float* vx, float* vy,
                             float* vz, float* internal_path, o_pcount* pc, int* pf, int* pfs, int* macro,
-                            int* micro) {
+                            int* micro, float* wmul = nullptr) {
     *pf = OP_OK; *pfs = OS_NONE; *macro = 0; *micro = 0;
     if (radius <= 0.0f) return 1;
     const int WD = 4096;
@@ -502,7 +504,9 @@ __device__ int o_sphere_sampled(S* s, float n_medium, float n_particle, float k_
             *pf = OP_MACRO_GEOMETRY; *pfs = OS_SPHERE_CHORD; return 0;
         }
         float chord_f = (float)chord;
-        if (alpha_abs > 0.0f) {
+        if (alpha_abs > 0.0f && wmul) {
+            *wmul *= expf(-alpha_abs * chord_f);  // implicit capture: the chord's survival probability
+        } else if (alpha_abs > 0.0f) {
             double dist = -log(open_uniform(s)) / (double)alpha_abs;
             if (dist < chord) {
                 qx += dist * dvx; qy += dist * dvy; qz += dist * dvz;
@@ -554,6 +558,8 @@ __device__ __forceinline__ int f_sphere_accessible(float cx, float cy, float cz,
         const float q = rmin * rmin, R2 = Rin * Rin;
         if (model == 1) {
             zsurf = Zmean + dh * (q / R2 - 0.5f);
+        } else if (model == 3) {
+            zsurf = f_rankine_z(f_rankine(Zmean, Rin, dh, core), q);
         } else {
             const float a2 = core * core;
             const float H = dh * (a2 + R2) / R2;
@@ -575,7 +581,7 @@ __device__ int f_sphere_sampled(S* s, float n_medium, float n_particle, float k_
                                 float rough_alpha, float radius, int max_bounces, float gnx, float gny, float gnz,
                                 float cx, float cy, float cz, float* x, float* y, float* z, float* vx, float* vy,
                                 float* vz, float* internal_path, o_pcount* pc, int* pf, int* pfs, int* macro,
-                                int* micro) {
+                                int* micro, float* wmul = nullptr) {
     const float FEPS = 1.1920928955078125e-7f;
     *pf = OP_OK; *pfs = OS_NONE; *macro = 0; *micro = 0;
     if (radius <= 0.0f) return 1;
@@ -615,7 +621,9 @@ __device__ int f_sphere_sampled(S* s, float n_medium, float n_particle, float k_
         if (!(arrival > 0.0f) || !isfinite(arrival) || !isfinite(tq2) || err > tol) {
             *pf = OP_MACRO_GEOMETRY; *pfs = OS_SPHERE_CHORD; return 0;
         }
-        if (alpha_abs > 0.0f) {
+        if (alpha_abs > 0.0f && wmul) {
+            *wmul *= expf(-alpha_abs * chord);  // implicit capture: the chord's survival probability
+        } else if (alpha_abs > 0.0f) {
             const float dist = -logf((float)open_uniform(s)) / alpha_abs;
             if (dist < chord) {
                 qx += dist * dvx; qy += dist * dvy; qz += dist * dvz;
@@ -657,13 +665,13 @@ template <class S>
 __device__ int o_sphere_fresh(S* s, float n_medium, float n_particle, float k_particle, float wavelength,
                           float rough_alpha, float radius, int max_bounces, float* x, float* y, float* z, float* vx,
                           float* vy, float* vz, float* internal_path, o_pcount* pc, int* pf, int* pfs, int* macro,
-                          int* micro) {
+                          int* micro, float* wmul = nullptr) {
     float rho, phi, gnx, gny, gnz;
     o_sphere_geometry(s, radius, *x, *y, *z, *vx, *vy, *vz, &rho, &phi, &gnx, &gny, &gnz);
     double cx = (double)(*x) - (double)radius * (double)gnx, cy = (double)(*y) - (double)radius * (double)gny,
            cz = (double)(*z) - (double)radius * (double)gnz;
     return o_sphere_sampled(s, n_medium, n_particle, k_particle, wavelength, rough_alpha, radius, max_bounces, gnx,
-                            gny, gnz, cx, cy, cz, x, y, z, vx, vy, vz, internal_path, pc, pf, pfs, macro, micro);
+                            gny, gnz, cx, cy, cz, x, y, z, vx, vy, vz, internal_path, pc, pf, pfs, macro, micro, wmul);
 }
 
 /* Mie inverse-CDF angle (:2624-2652). The CDF comparisons are done after a float cast. */
@@ -796,14 +804,15 @@ template <class S>
 __device__ __noinline__ int o_spheroid_event(S* s, float n_medium, float n_particle, float k_particle, float wavelength,
                             float rough_alpha, float r_equiv, float aspect, int orientation_model, float kappa,
                             float fx, float fy, float fz, int max_bounces, float* vx, float* vy, float* vz,
-                            float* internal_path, o_pcount* pc, int* pf, int* pfs, int* macro, int* micro) {
+                            float* internal_path, o_pcount* pc, int* pf, int* pfs, int* macro, int* micro,
+                            float* wmul = nullptr) {
     *pf = OP_OK; *pfs = OS_NONE; *macro = 0; *micro = 0;
     if (r_equiv <= 0.0f) return 1;
     if (!(aspect > 0.0f) || !isfinite(aspect)) { *pf = OP_SPHEROID_GEOMETRY; *pfs = OS_SPHEROID_ASPECT; return 0; }
     if (fabsf(aspect - 1.0f) < 1e-7f) {
         float lx = 0.0f, ly = 0.0f, lz = 0.0f, lvx = *vx, lvy = *vy, lvz = *vz, ip = 0.0f;
         int ps = o_sphere_fresh(s, n_medium, n_particle, k_particle, wavelength, rough_alpha, r_equiv, max_bounces, &lx,
-                                &ly, &lz, &lvx, &lvy, &lvz, &ip, pc, pf, pfs, macro, micro);
+                                &ly, &lz, &lvx, &lvy, &lvz, &ip, pc, pf, pfs, macro, micro, wmul);
         *internal_path += ip;
         if (ps == 1) { *vx = lvx; *vy = lvy; *vz = lvz; }
         return ps;
@@ -832,7 +841,9 @@ __device__ __noinline__ int o_spheroid_event(S* s, float n_medium, float n_parti
         *macro = bounce;
         float chord = o_spheroid_next(x, y, z, *vx, *vy, *vz, ux, uy, uz, invb2, delta, scale);
         if (chord <= 0.0f) { *pf = OP_SPHEROID_GEOMETRY; *pfs = OS_SPHEROID_CHORD; return 0; }
-        if (alpha_abs > 0.0f) {
+        if (alpha_abs > 0.0f && wmul) {
+            *wmul *= expf(-alpha_abs * chord);  // implicit capture: the chord's survival probability
+        } else if (alpha_abs > 0.0f) {
             double dist = -log(open_uniform(s)) / (double)alpha_abs;
             if (dist < (double)chord) { *internal_path += (float)dist; pc->absorptions++; return 2; }
         }

@@ -213,6 +213,11 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
     bool out = !wave_drawing(w);
     unsigned long long drawn = 0;
     int home = -1;  // scenario whose counts this warp keeps in shared memory (that of its first photon)
+    // A photon rejected at the collimator (most of them) changes only its end-status, failure-code-0 and
+    // done counters and the source-bore counters: without per-ray records those are counted in registers
+    // and added once per warp instead of running the whole scoring routine per photon.
+    const bool count_rejects = !w.records && !w.prov_rec;
+    unsigned rej = 0, rej_sbi = 0, rej_sbr = 0;
     for (unsigned base = wave_claim(w, WQ_FREE); base < win.n && !__all_sync(FULL, out); base = wave_claim(w, WQ_FREE)) {
         const unsigned i = base + lane;
         const bool valid = i < win.n;
@@ -246,8 +251,15 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
                     ray_reset(r);
                     drawn++;
                     if (source_segment(D, r, L.source())) {
-                        finish_ray<Mode>(D, det, r, gid, sid, home, wt, w.tallies, w.records ? w.records + rid : nullptr);
-                        if (w.prov_rec) w.prov_rec[rid] = prov_init();
+                        if (count_rejects && sid == home) {
+                            rej++;
+                            rej_sbi += (unsigned)r.sbi;
+                            rej_sbr += (unsigned)r.sbr;
+                        } else {
+                            finish_ray<Mode>(D, det, r, gid, sid, home, wt, w.tallies,
+                                             w.records ? w.records + rid : nullptr);
+                            if (w.prov_rec) w.prov_rec[rid] = prov_init();
+                        }
                     } else {
                         pool.ray[slot] = r;
                         pool.lane[slot] = L;
@@ -268,6 +280,16 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gen_kernel(WaveLaunch w) {
     }
     const unsigned long long sum = __reduce_add_sync(FULL, (unsigned)drawn);
     if (lane == 0 && sum) atomicAdd(&w.tallies[0].sched[WQ_FREE], sum);
+    const unsigned n_rej = __reduce_add_sync(FULL, rej);
+    const unsigned n_sbi = __reduce_add_sync(FULL, rej_sbi), n_sbr = __reduce_add_sync(FULL, rej_sbr);
+    if (lane == 0 && n_rej) {  // rejected photons end with status 3 and failure code 0 (r.pf is 0)
+        atomicAdd(&wt->status[3], (unsigned long long)n_rej);
+        atomicAdd(&wt->failure[0], (unsigned long long)n_rej);
+        atomicAdd(&wt->n_done, (unsigned long long)n_rej);
+        if (n_sbi) atomicAdd(&wt->events[CLR_EV_SOURCE_BORE_INTERACTIONS], (unsigned long long)n_sbi);
+        if (n_sbr) atomicAdd(&wt->events[CLR_EV_SOURCE_BORE_REFLECTIONS], (unsigned long long)n_sbr);
+    }
+    __syncwarp();
     if (home >= 0) flush_warp_tally(wt, w.tallies + home, lane);
 }
 
@@ -626,7 +648,10 @@ struct WavePass {
 // is already queued when it does, so the GPU does not idle on the read. Passes after the pool drained
 // find empty windows and return at once.
 template <class Mode, bool kRecord>
-cudaError_t wave_run_t(const WaveLaunch& w, int num_sms, cudaStream_t st, long long max_passes, int* passes_out) {
+cudaError_t wave_run_t(const WaveLaunch& w, int num_sms, cudaStream_t st, long long max_passes, WaveRunInfo* info) {
+    info->passes = 0;
+    info->tail = 0;
+    info->tail_photons = 0;
     WavePass<Mode, kRecord> P;
     cudaError_t e = P.build(w, num_sms);
     if (e != cudaSuccess) return e;
@@ -655,9 +680,13 @@ cudaError_t wave_run_t(const WaveLaunch& w, int num_sms, cudaStream_t st, long l
             // at most live[2] photons remain after the passes already queued: finish them in one launch
             const unsigned n = live[2];
             const int blocks = (int)std::max(1u, std::min(n, 65536u * kTailThreads) / kTailThreads + 1);
+            if (w.tail_begin && (e = cudaEventRecord(w.tail_begin, st)) != cudaSuccess) return e;
             if (w.light || w.prov) wave_tail_kernel<Mode, kRecord, true><<<blocks, kTailThreads, 0, st>>>(w);
             else wave_tail_kernel<Mode, kRecord, false><<<blocks, kTailThreads, 0, st>>>(w);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            if (w.tail_end && (e = cudaEventRecord(w.tail_end, st)) != cudaSuccess) return e;
+            info->tail = 1;
+            info->tail_photons = n;
             launched += 1;
             break;
         }
@@ -668,7 +697,7 @@ cudaError_t wave_run_t(const WaveLaunch& w, int num_sms, cudaStream_t st, long l
     }
     // wait for the passes queued after the flag read before the graph is destroyed
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
-    if (passes_out) *passes_out = (int)launched;
+    info->passes = (int)launched - info->tail;
     return cudaSuccess;
 }
 

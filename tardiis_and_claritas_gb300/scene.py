@@ -33,7 +33,8 @@ BORE_SURFACE_MODEL_CODES = {"absorbing": 0, "smooth_fresnel_nylon": 1}
 RING_FACE_SURFACE_MODEL_CODES = {"absorbing": 0, "smooth_fresnel_nylon": 1}
 PHOTODIODE_RESPONSE_MODEL_CODES = {"ideal_hard_aperture": 0, "sfh213_datasheet_fit": 1}
 SPHEROID_ORIENTATION_MODEL_CODES = {"isotropic": 0, "local_tangential_axial_vmf": 1}
-FREE_SURFACE_MODEL_CODES = {"flat": 0, "parabolic_vortex": 1, "localized_scully_vortex": 2}
+# "rankine_vortex" is this library's (no reference counterpart): see rankine_surface_coefficients
+FREE_SURFACE_MODEL_CODES = {"flat": 0, "parabolic_vortex": 1, "localized_scully_vortex": 2, "rankine_vortex": 3}
 SEDIMENT_TRANSPORT_MODEL_CODES = {
     "uniform": 0, "stokes_drift_diffusion": 1, "schiller_naumann_drift_diffusion": 2,
     "schiller_naumann_meridional_advection_diffusion": 3,
@@ -122,6 +123,7 @@ class ModelConfig:
     # new capabilities (no reference counterpart); defaults keep reference behaviour
     source_kind: str = "reference_led"
     disc_beam_radius_m: float = 1.0e-3
+    water_absorption_per_m: float = 0.0
 
     # ---- derived quantities (CLARITAS/CLARITAS.py:5660-5700) ----
     @property
@@ -195,6 +197,12 @@ class ModelConfig:
             np.isfinite(self.vortex_core_radius_m) and self.vortex_core_radius_m > 0.0
         ):
             raise ValueError("vortex_core_radius_m must be finite and >0 for localized_scully_vortex")
+        if self.free_surface_model == "rankine_vortex":
+            if not (np.isfinite(self.vortex_core_radius_m) and self.vortex_core_radius_m > 0.0):
+                raise ValueError("vortex_core_radius_m must be finite and >0 for rankine_vortex")
+            if self.sediment_transport_model in ("stokes_drift_diffusion", "schiller_naumann_drift_diffusion"):
+                raise ValueError("the analytic drift-diffusion sediment fields follow the reference's free surfaces; "
+                                 "with rankine_vortex use 'uniform' or a supplied meridional field")
         if not np.isfinite(self.sediment_eddy_diffusivity_m2_s) or self.sediment_eddy_diffusivity_m2_s <= 0.0:
             raise ValueError("sediment_eddy_diffusivity_m2_s must be finite and >0")
         if not (np.isfinite(self.water_density_kg_per_m3) and 0.0 < self.water_density_kg_per_m3 < self.density_kg_per_m3):
@@ -244,6 +252,8 @@ class ModelConfig:
             raise ValueError("chunk/batch sizes must be positive")
         if self.source_kind not in ("reference_led", "collimated_disc"):
             raise ValueError("source_kind must be 'reference_led' or 'collimated_disc'")
+        if not (np.isfinite(self.water_absorption_per_m) and self.water_absorption_per_m >= 0.0):
+            raise ValueError("water_absorption_per_m must be finite and nonnegative")
         if self.aggregation_model not in ("none", "orthokinetic_compact", "orthokinetic_compact_fragmentation"):
             raise ValueError("aggregation_model must be 'none', 'orthokinetic_compact', or "
                              "'orthokinetic_compact_fragmentation'")
@@ -300,6 +310,7 @@ class ModelConfig:
         s.source_kind = abi.SOURCE_COLLIMATED_DISC if self.source_kind == "collimated_disc" else abi.SOURCE_REFERENCE_LED
         s.disc_radius = self.disc_beam_radius_m
         s.disc_height = 0.0
+        s.water_absorption = float(self.water_absorption_per_m)
         return s
 
     def sediment_spec(self, grid: Optional[np.ndarray] = None, grid_zmax: Optional[float] = None):
@@ -345,11 +356,45 @@ class ModelConfig:
         return sp
 
 
+def rankine_surface_coefficients(zmean: float, R: float, delta_h: float, core_r: float):
+    """(k, a, z0) of the Rankine free surface z0 + k r^2 (r <= a), z0 + k a^2 (2 - a^2/r^2) (r > a).
+
+    The stirrer turns the core r <= a as a solid body at angular speed W and the liquid outside as a free
+    vortex (v = W a^2 / r); the radial pressure balance gives k = W^2 / (2 g), continuous with its slope at
+    r = a. k is set by the wall-centre height difference delta_h = k a^2 (2 - a^2/R^2), and z0 = zmean - hbar
+    by volume conservation, hbar = (k/R^2) (a^4/2 + 2 a^2 (R^2 - a^2) - 2 a^4 ln(R/a)). A core wider than the
+    tube is clamped to it (solid-body rotation, the parabolic surface). No reference counterpart.
+    """
+    R, a = float(R), min(float(core_r), float(R))
+    a2, R2 = a * a, R * R
+    k = float(delta_h) / (a2 * (2.0 - a2 / R2))
+    hbar = (k / R2) * (0.5 * a2 * a2 + 2.0 * a2 * (R2 - a2) - 2.0 * a2 * a2 * math.log(R / a))
+    return k, a, float(zmean) - hbar
+
+
+def rankine_surface(r, zmean: float, R: float, delta_h: float, core_r: float):
+    """Height of the Rankine free surface at radius r (array or scalar)."""
+    k, a, z0 = rankine_surface_coefficients(zmean, R, delta_h, core_r)
+    r = np.asarray(r, dtype=float)
+    q = r * r
+    return np.where(q <= a * a, z0 + k * q, z0 + k * a * a * (2.0 - a * a / np.maximum(q, 1e-300)))
+
+
+def stirrer_rankine_delta_h(rpm: float, core_radius_m: float, R: float, gravity: float = 9.81) -> float:
+    """Wall-minus-centre height of the Rankine surface of a stirrer whose core (radius a) turns at `rpm`:
+    k = W^2 / (2 g) with W = 2 pi rpm / 60, and delta_h = k a^2 (2 - a^2/R^2). No reference counterpart."""
+    w = float(rpm) * 2.0 * math.pi / 60.0
+    a = min(float(core_radius_m), float(R))
+    k = w * w / (2.0 * gravity)
+    return k * a * a * (2.0 - a * a / (float(R) * float(R)))
+
+
 def vortex_surface_geometry(model, zmean, R, delta_h, core_r, gravity=9.81):
     """Free-surface centre/wall heights and swirl of the selected surface model.
 
     Same arithmetic as the reference host helper (CLARITAS/CLARITAS.py:708-792), because the wall
-    height sets the sediment grid's upper edge and the constructor's geometry checks.
+    height sets the sediment grid's upper edge and the constructor's geometry checks. The Rankine
+    vortex (this library's model) reports its core angular speed.
     """
     model = str(model).strip().lower()
     zmean, R, D, a, g = float(zmean), float(R), float(delta_h), float(core_r), float(gravity)
@@ -372,6 +417,14 @@ def vortex_surface_geometry(model, zmean, R, delta_h, core_r, gravity=9.81):
         return dict(center_z=zmean - 0.5 * D, wall_z=zmean + 0.5 * D, h_inf=D, h_bar=0.5 * D,
                     angular_velocity_rad_s=omega, vtheta_peak_m_s=omega * R,
                     equivalent_rigid_body_rpm=omega * 60.0 / (2.0 * math.pi), equivalent_core_rpm=float("nan"))
+    if model == "rankine_vortex":
+        if not (a > 0.0):
+            raise ValueError("Rankine vortex requires a positive core radius")
+        k, ae, z0 = rankine_surface_coefficients(zmean, R, D, a)
+        omega = math.sqrt(2.0 * g * k)
+        return dict(center_z=z0, wall_z=z0 + D, h_inf=k * ae * ae * 2.0, h_bar=zmean - z0,
+                    angular_velocity_rad_s=omega, vtheta_peak_m_s=omega * ae,
+                    equivalent_rigid_body_rpm=float("nan"), equivalent_core_rpm=omega * 60.0 / (2.0 * math.pi))
     if model != "localized_scully_vortex":
         raise ValueError(f"unknown free-surface model {model!r}")
     if not (a > 0.0):
@@ -578,6 +631,8 @@ def rouse_radial_grid(cfg: ModelConfig, n_bins: int, nr: int = 64, nz: int = 64,
         dh = cfg.vortex_wall_center_height_difference_m
         if cfg.free_surface_model == "parabolic_vortex":
             return cfg.zmean + dh * (r * r / (R * R) - 0.5)
+        if cfg.free_surface_model == "rankine_vortex":
+            return rankine_surface(r, cfg.zmean, R, dh, cfg.vortex_core_radius_m)
         a2, R2 = cfg.vortex_core_radius_m ** 2, R * R
         return cfg.zmean - vg["h_bar"] + vg["h_inf"] * r * r / (a2 + r * r)
 
@@ -600,13 +655,21 @@ def rouse_radial_grid(cfg: ModelConfig, n_bins: int, nr: int = 64, nz: int = 64,
     return np.ascontiguousarray(np.broadcast_to(g, (n_bins, nr, nz))), zmax
 
 
-def full_scene_workload(n_photons: int = 100_000_000):
+def full_scene_workload(n_photons: int = 100_000_000, surface: str = "localized_scully_vortex", rpm: float = 600.0):
     """The full scene: three-component mixture at 500 mg/L in a (r, z) Rouse x radial-depletion field with a
-    stirred (600 rpm, 5 mm core) free surface, small cell. Returns (config, particles, grid)."""
+    stirred (600 rpm, 5 mm core) free surface, small cell. `surface` is the stirred surface: the Rankine
+    vortex ("rankine_vortex", this library's model of a stirrer) or the reference's localized Scully vortex
+    with the same core angular speed (the reference-supported stand-in). Returns (config, particles, grid,
+    grid_zmax)."""
     base = small_cell_config(particle_surface_rms_slope_deg=0.0, wave_surface_rms_height_m=0.0)
-    dh = stirrer_scully_delta_h(600.0, 0.005, base.tube_inner_radius_m)
+    if surface == "rankine_vortex":
+        dh = stirrer_rankine_delta_h(rpm, 0.005, base.tube_inner_radius_m)
+    elif surface == "localized_scully_vortex":
+        dh = stirrer_scully_delta_h(rpm, 0.005, base.tube_inner_radius_m)
+    else:
+        raise ValueError(f"unknown stirred surface {surface!r}")
     cfg = small_cell_config(particle_surface_rms_slope_deg=0.0, wave_surface_rms_height_m=0.0,
-                            free_surface_model="localized_scully_vortex", vortex_wall_center_height_difference_m=dh,
+                            free_surface_model=surface, vortex_wall_center_height_difference_m=dh,
                             vortex_core_radius_m=0.005,
                             sediment_transport_model="schiller_naumann_meridional_advection_diffusion")
     cfg.validate()
