@@ -71,6 +71,97 @@ __device__ __forceinline__ CondState cond_start() {
     return c;
 }
 
+// Inputs of a closure's candidate histories: the same for every trial of one closure.
+struct ClosureIn {
+    const float* cdf;
+    const float* theta;
+    double wave;
+    float nm, nr, ki, wl, rough, radius, aspect, kappa, coherent;
+    float x, y, z, vx, vy, vz, rin, zmin, zmean, delta, core;
+    int pidx, orientation, max_bounces, nt, surface;
+};
+
+// One candidate history of a closure (one iteration of the trial loop, :4505-4533). Returns -2 when the
+// sampled sphere does not fit in the water, -1 when the outcome is not the target, and 1 when the trial
+// ends the closure with *h: the target outcome, or a failure when h->status is neither 1 nor 2.
+template <class S>
+__device__ __forceinline__ int closure_trial(S* s, const ClosureIn& c, int target_absorbed, Hist* h) {
+    const float x = c.x, y = c.y, z = c.z, vx = c.vx, vy = c.vy, vz = c.vz, radius = c.radius;
+    memset(h, 0, sizeof *h);
+    h->x = x; h->y = y; h->z = z; h->vx = vx; h->vy = vy; h->vz = vz;
+    h->channel = (uniform53(s) < c.wave) ? ((c.coherent >= 1.0f || uniform53(s) < c.coherent) ? 1 : 2) : 0;
+    if (h->channel == 1) {
+        o_mie_direction(s, c.cdf, c.theta, c.nt, c.pidx, &h->vx, &h->vy, &h->vz);
+        h->status = 1;
+    } else if (h->channel == 2) {
+        float fr = sqrtf(x * x + y * y), fx = 1, fy = 0;
+        if (fr > 1e-12f) { fx = -y / fr; fy = x / fr; }
+        h->status = o_spheroid_event(s, c.nm, c.nr, c.ki, c.wl, c.rough, radius, c.aspect, c.orientation, c.kappa, fx,
+                                     fy, 0, c.max_bounces, &h->vx, &h->vy, &h->vz, &h->path, &h->pc, &h->failure,
+                                     &h->subcode, &h->macro, &h->micro);
+    } else {
+        float rho, phi, gx, gy, gz;
+        o_sphere_geometry(s, radius, x, y, z, vx, vy, vz, &rho, &phi, &gx, &gy, &gz);
+        if constexpr (kCounterStream<S>) {
+            const float fcx = x - radius * gx, fcy = y - radius * gy, fcz = z - radius * gz;
+            if (!f_sphere_accessible(fcx, fcy, fcz, radius, c.rin, c.zmin, c.zmean, c.surface, c.delta, c.core))
+                return -2;
+            h->status = f_sphere_sampled(s, c.nm, c.nr, c.ki, c.wl, c.rough, radius, c.max_bounces, gx, gy, gz, fcx,
+                                         fcy, fcz, &h->x, &h->y, &h->z, &h->vx, &h->vy, &h->vz, &h->path, &h->pc,
+                                         &h->failure, &h->subcode, &h->macro, &h->micro);
+        } else {
+            double dcx = (double)x - (double)radius * gx, dcy = (double)y - (double)radius * gy,
+                   dcz = (double)z - (double)radius * gz;
+            if (!o_sphere_accessible(dcx, dcy, dcz, radius, c.rin, c.zmin, c.zmean, c.surface, c.delta, c.core))
+                return -2;
+            h->status = o_sphere_sampled(s, c.nm, c.nr, c.ki, c.wl, c.rough, radius, c.max_bounces, gx, gy, gz, dcx,
+                                         dcy, dcz, &h->x, &h->y, &h->z, &h->vx, &h->vy, &h->vz, &h->path, &h->pc,
+                                         &h->failure, &h->subcode, &h->macro, &h->micro);
+        }
+    }
+    if (h->status != 1 && h->status != 2) return 1;
+    if ((h->status == 2) != target_absorbed) return -1;
+    return 1;
+}
+
+// Setup of a closure (argument checks and the absorbed/scattered target draw, :4491-4504). Returns 1 with
+// *out set when the closure ends here, else 0 with cs->target set.
+template <class S>
+__device__ __forceinline__ int closure_setup(S* s, Hist* out, double qs, double qe, float ki, int max_trials,
+                                             unsigned long long* stats, CondState* cs, float* wmul) {
+    Hist h;
+    memset(&h, 0, sizeof h);
+    h.failure = OP_OTHER; h.subcode = 9002;
+    double tol = 1e-10 * fmax(1.0, fmax(fabs(qs), fabs(qe)));
+    double albedo = (ki == 0.0f && fabs(qe - qs) <= tol) ? 1.0 : fmin(fmax(qs / qe, 0.0), 1.0);
+    if (max_trials == 0) { h.subcode = 9001; ++stats[9]; *out = h; return 1; }
+    if (!isfinite(qs) || !isfinite(qe) || qe <= 0.0 || qs < -tol || qs > qe + tol || max_trials < 1) { ++stats[8]; *out = h; return 1; }
+    double pabs = (ki == 0.0f && fabs(qe - qs) <= tol) ? 0.0 : fmin(fmax((qe - qs) / qe, 0.0), 1.0);
+    const double MINP = 2.3283064365386962890625e-10;
+    if ((ki > 0.0f && (pabs <= 0.0 || albedo >= 1.0)) || (albedo > 0.0 && albedo < MINP) || (pabs > 0.0 && pabs < MINP)) {
+        h.subcode = 9003; ++stats[8]; *out = h; return 1;
+    }
+    if (wmul && albedo > 0.0) {
+        // implicit capture (weighted runs): the photon always scatters and carries the survival
+        // probability instead of drawing the absorbed/scattered outcome
+        *wmul *= (float)albedo;
+        cs->target = 0;
+    } else {
+        cs->target = (albedo < 1.0 && uniform53(s) >= albedo);
+    }
+    cs->started = 1;
+    cs->trial = 0;
+    return 0;
+}
+
+__device__ __forceinline__ Hist closure_exhausted(unsigned long long* stats) {
+    Hist h;
+    memset(&h, 0, sizeof h);
+    h.failure = OP_OTHER; h.subcode = 9001;
+    ++stats[9];
+    return h;
+}
+
 // Runs the closure from *cs for at most `budget` trials (0: to its end). Returns 1 with *out set when
 // the closure finished, 0 when the budget ran out first (state in *cs).
 template <class S>
@@ -80,77 +171,30 @@ __device__ __forceinline__ int conditional_body(
     const float* theta, int nt, float x, float y, float z, float vx, float vy, float vz, float rin, float zmin,
     float zmean, int surface, float delta, float core, int max_trials, unsigned long long* stats, CondState* cs,
     int budget, float* wmul) {
-    Hist h;
-    memset(&h, 0, sizeof h);
-    h.failure = OP_OTHER; h.subcode = 9002;
-    double tol = 1e-10 * fmax(1.0, fmax(fabs(qs), fabs(qe)));
-    double albedo = (ki == 0.0f && fabs(qe - qs) <= tol) ? 1.0 : fmin(fmax(qs / qe, 0.0), 1.0);
-    if (!cs->started) {
-        if (max_trials == 0) { h.subcode = 9001; ++stats[9]; *out = h; return 1; }
-        if (!isfinite(qs) || !isfinite(qe) || qe <= 0.0 || qs < -tol || qs > qe + tol || max_trials < 1) { ++stats[8]; *out = h; return 1; }
-        double pabs = (ki == 0.0f && fabs(qe - qs) <= tol) ? 0.0 : fmin(fmax((qe - qs) / qe, 0.0), 1.0);
-        const double MINP = 2.3283064365386962890625e-10;
-        if ((ki > 0.0f && (pabs <= 0.0 || albedo >= 1.0)) || (albedo > 0.0 && albedo < MINP) || (pabs > 0.0 && pabs < MINP)) {
-            h.subcode = 9003; ++stats[8]; *out = h; return 1;
-        }
-        if (wmul && albedo > 0.0) {
-            // implicit capture (weighted runs): the photon always scatters and carries the survival
-            // probability instead of drawing the absorbed/scattered outcome
-            *wmul *= (float)albedo;
-            cs->target = 0;
-        } else {
-            cs->target = (albedo < 1.0 && uniform53(s) >= albedo);
-        }
-        cs->started = 1;
-        cs->trial = 0;
-    }
+    if (!cs->started && closure_setup(s, out, qs, qe, ki, max_trials, stats, cs, wmul)) return 1;
     const int target_absorbed = cs->target;
-    double wave = qs > 0.0 ? fmax(qs - 1.0, 0.0) / qs : 0.0;
+    ClosureIn c;
+    c.cdf = cdf; c.theta = theta; c.wave = qs > 0.0 ? fmax(qs - 1.0, 0.0) / qs : 0.0;
+    c.nm = nm; c.nr = nr; c.ki = ki; c.wl = wl; c.rough = rough; c.radius = radius; c.aspect = aspect;
+    c.kappa = kappa; c.coherent = coherent;
+    c.x = x; c.y = y; c.z = z; c.vx = vx; c.vy = vy; c.vz = vz; c.rin = rin; c.zmin = zmin; c.zmean = zmean;
+    c.delta = delta; c.core = core;
+    c.pidx = pidx; c.orientation = orientation; c.max_bounces = max_bounces; c.nt = nt; c.surface = surface;
     const int end = (budget > 0 && max_trials - cs->trial > budget) ? cs->trial + budget : max_trials;
+    Hist h;
     for (int trial = cs->trial; trial < end; ++trial) {
         ++stats[0];
-        memset(&h, 0, sizeof h);
-        h.x = x; h.y = y; h.z = z; h.vx = vx; h.vy = vy; h.vz = vz;
-        h.channel = (uniform53(s) < wave) ? ((coherent >= 1.0f || uniform53(s) < coherent) ? 1 : 2) : 0;
-        if (h.channel == 1) {
-            o_mie_direction(s, cdf, theta, nt, pidx, &h.vx, &h.vy, &h.vz);
-            h.status = 1;
-        } else if (h.channel == 2) {
-            float fr = sqrtf(x * x + y * y), fx = 1, fy = 0;
-            if (fr > 1e-12f) { fx = -y / fr; fy = x / fr; }
-            h.status = o_spheroid_event(s, nm, nr, ki, wl, rough, radius, aspect, orientation, kappa, fx, fy, 0,
-                                        max_bounces, &h.vx, &h.vy, &h.vz, &h.path, &h.pc, &h.failure, &h.subcode,
-                                        &h.macro, &h.micro);
-        } else {
-            float rho, phi, gx, gy, gz;
-            o_sphere_geometry(s, radius, x, y, z, vx, vy, vz, &rho, &phi, &gx, &gy, &gz);
-            if constexpr (kCounterStream<S>) {
-                const float fcx = x - radius * gx, fcy = y - radius * gy, fcz = z - radius * gz;
-                if (!f_sphere_accessible(fcx, fcy, fcz, radius, rin, zmin, zmean, surface, delta, core)) { ++stats[2]; continue; }
-                h.status = f_sphere_sampled(s, nm, nr, ki, wl, rough, radius, max_bounces, gx, gy, gz, fcx, fcy, fcz,
-                                            &h.x, &h.y, &h.z, &h.vx, &h.vy, &h.vz, &h.path, &h.pc, &h.failure,
-                                            &h.subcode, &h.macro, &h.micro);
-            } else {
-                double dcx = (double)x - (double)radius * gx, dcy = (double)y - (double)radius * gy,
-                       dcz = (double)z - (double)radius * gz;
-                if (!o_sphere_accessible(dcx, dcy, dcz, radius, rin, zmin, zmean, surface, delta, core)) { ++stats[2]; continue; }
-                h.status = o_sphere_sampled(s, nm, nr, ki, wl, rough, radius, max_bounces, gx, gy, gz, dcx, dcy, dcz,
-                                            &h.x, &h.y, &h.z, &h.vx, &h.vy, &h.vz, &h.path, &h.pc, &h.failure,
-                                            &h.subcode, &h.macro, &h.micro);
-            }
-        }
+        const int t = closure_trial(s, c, target_absorbed, &h);
+        if (t == -2) { ++stats[2]; continue; }
+        if (t == -1) { ++stats[1]; continue; }
         if (h.status != 1 && h.status != 2) { ++stats[8]; *out = h; return 1; }
-        if ((h.status == 2) != target_absorbed) { ++stats[1]; continue; }
         ++stats[3 + h.channel];
         ++stats[h.status == 2 ? 6 : 7];
         *out = h;
         return 1;
     }
     if (end < max_trials) { cs->trial = end; return 0; }
-    memset(&h, 0, sizeof h);
-    h.failure = OP_OTHER; h.subcode = 9001;
-    ++stats[9];
-    *out = h;
+    *out = closure_exhausted(stats);
     return 1;
 }
 
@@ -846,23 +890,12 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
 // geometric event whose sampled sphere does not fit in the water (CK_GEOM, :4890-4905).
 enum : int { CK_FLIGHT = 0, CK_GEOM = 1 };
 
-// Runs (part of) a closure. Returns 0 when the iteration ended with the photon in the water, 1 when the
-// history ended, 2 when the closure continues (state in *cs; with budget 0 it always finishes).
+// Completes the iteration of a finished closure with its result h: 0 when the photon continues in the
+// water, 1 when the history ended.
 template <class S>
-__device__ __forceinline__ int closure_visit(const DevScene& D, Ray& r, S* opt, unsigned long long* cstats, int pidx,
-                                             int kind, CondState* cs, int budget) {
-    const clr_scene_params& P = D.P;
+__device__ __forceinline__ int closure_finish(const DevScene& D, Ray& r, S* opt, int pidx, int kind, const Hist& h) {
     float x = r.x, y = r.y, z = r.z, vx = r.vx, vy = r.vy, vz = r.vz;
     const float vinx = vx, viny = vy, vinz = vz;
-    const float COHERENT = fminf(fmaxf(D.coherent_f, 0.0f), 1.0f);
-    Hist h;
-    const int done = conditional_interaction(
-        opt, &h, pidx, D.qsca[pidx], D.qext[pidx], P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha,
-        D.prad[pidx], P.spheroid_aspect, P.orientation_model, P.orientation_kappa, P.max_particle_bounces, COHERENT,
-        D.phase_cdf, D.theta, D.nt, x, y, z, vx, vy, vz, P.rin, P.zmin, P.zmean, P.free_surface_model,
-        P.vortex_delta_h, P.vortex_core_radius, kind == CK_GEOM ? P.conditional_retries - 1 : P.conditional_retries,
-        cstats, cs, budget, (kind == CK_FLIGHT && weighted_run(D)) ? &r.w : nullptr);
-    if (!done) return 2;
     bool ended = false;
     do {
         if (kind == CK_FLIGHT) {
@@ -882,6 +915,110 @@ __device__ __forceinline__ int closure_visit(const DevScene& D, Ray& r, S* opt, 
     } while (false);
     r.x = x; r.y = y; r.z = z; r.vx = vx; r.vy = vy; r.vz = vz;
     return ended ? 1 : 0;
+}
+
+// Runs (part of) a closure. Returns 0 when the iteration ended with the photon in the water, 1 when the
+// history ended, 2 when the closure continues (state in *cs; with budget 0 it always finishes).
+template <class S>
+__device__ __forceinline__ int closure_visit(const DevScene& D, Ray& r, S* opt, unsigned long long* cstats, int pidx,
+                                             int kind, CondState* cs, int budget) {
+    const clr_scene_params& P = D.P;
+    const float COHERENT = fminf(fmaxf(D.coherent_f, 0.0f), 1.0f);
+    Hist h;
+    const int done = conditional_interaction(
+        opt, &h, pidx, D.qsca[pidx], D.qext[pidx], P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha,
+        D.prad[pidx], P.spheroid_aspect, P.orientation_model, P.orientation_kappa, P.max_particle_bounces, COHERENT,
+        D.phase_cdf, D.theta, D.nt, r.x, r.y, r.z, r.vx, r.vy, r.vz, P.rin, P.zmin, P.zmean, P.free_surface_model,
+        P.vortex_delta_h, P.vortex_core_radius, kind == CK_GEOM ? P.conditional_retries - 1 : P.conditional_retries,
+        cstats, cs, budget, (kind == CK_FLIGHT && weighted_run(D)) ? &r.w : nullptr);
+    if (!done) return 2;
+    return closure_finish(D, r, opt, pidx, kind, h);
+}
+
+// Warp-cooperative closure (counter-based stream only; called by all 32 lanes of a warp with the same
+// photon). The setup draws from the photon's own stream, identically in every lane; then the warp runs 32
+// trials at a time, trial t on its own substream of the photon's Philox key (counter word 2 tagged with
+// the event number and t). The trials are independent and identically distributed, so the lowest-index
+// trial that ends the closure has the distribution of the serial loop's result, and the counters count
+// exactly the trials the serial loop would have run. Same returns as closure_visit; only lane 0 adds the
+// trial counters.
+__device__ __forceinline__ Hist shfl_hist(const Hist& h, int src) {
+    static_assert(sizeof(Hist) % 4 == 0, "Hist is moved as 32-bit words");
+    constexpr int kWords = (int)(sizeof(Hist) / 4);
+    uint32_t wv[kWords];
+    memcpy(wv, &h, sizeof(Hist));
+#pragma unroll
+    for (int k = 0; k < kWords; ++k) wv[k] = __shfl_sync(0xffffffffu, wv[k], src);
+    Hist o;
+    memcpy(&o, wv, sizeof(Hist));
+    return o;
+}
+__device__ __forceinline__ int closure_visit_warp(const DevScene& D, Ray& r, PhiloxStream* opt,
+                                                  unsigned long long* cstats, int pidx, int kind, CondState* cs,
+                                                  int budget) {
+    const clr_scene_params& P = D.P;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    unsigned long long stats[CLR_N_CONDITIONAL_STATS] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int max_trials = kind == CK_GEOM ? P.conditional_retries - 1 : P.conditional_retries;
+    Hist h;
+    int done = 0;
+    if (!cs->started)
+        done = closure_setup(opt, &h, D.qsca[pidx], D.qext[pidx], D.pk[pidx], max_trials, stats, cs,
+                             (kind == CK_FLIGHT && weighted_run(D)) ? &r.w : nullptr);
+    if (!done) {
+        const double qs = D.qsca[pidx];
+        ClosureIn c;
+        c.cdf = D.phase_cdf; c.theta = D.theta; c.wave = qs > 0.0 ? fmax(qs - 1.0, 0.0) / qs : 0.0;
+        c.nm = P.n_water; c.nr = D.pn[pidx]; c.ki = D.pk[pidx]; c.wl = P.wavelength; c.rough = P.rough_alpha;
+        c.radius = D.prad[pidx]; c.aspect = P.spheroid_aspect; c.kappa = P.orientation_kappa;
+        c.coherent = fminf(fmaxf(D.coherent_f, 0.0f), 1.0f);
+        c.x = r.x; c.y = r.y; c.z = r.z; c.vx = r.vx; c.vy = r.vy; c.vz = r.vz;
+        c.rin = P.rin; c.zmin = P.zmin; c.zmean = P.zmean; c.delta = P.vortex_delta_h; c.core = P.vortex_core_radius;
+        c.pidx = pidx; c.orientation = P.orientation_model; c.max_bounces = P.max_particle_bounces; c.nt = D.nt;
+        c.surface = P.free_surface_model;
+        const int end = (budget > 0 && max_trials - cs->trial > budget) ? cs->trial + budget : max_trials;
+        const uint32_t tag = 0x80000000u | (((uint32_t)r.ic & 0x1FFFFu) << 14);
+        for (int base = cs->trial; base < end && !done; base += 32) {
+            const int t = base + lane;
+            int res = 0;
+            if (t < end) {
+                PhiloxStream ts = *opt;
+                ts.c2 = tag | (uint32_t)t;
+                ts.draw = 0u;
+                ts.idx = 4;
+                res = closure_trial(&ts, c, cs->target, &h);
+            }
+            const unsigned term = __ballot_sync(FULL, res == 1);
+            const unsigned miss = __ballot_sync(FULL, res == -1), nofit = __ballot_sync(FULL, res == -2);
+            const int win = term ? __ffs(term) - 1 : 32;
+            const unsigned before = win < 32 ? ((1u << win) - 1u) : FULL;
+            stats[0] += (unsigned long long)(term ? win + 1 : min(32, end - base));
+            stats[1] += (unsigned long long)__popc(miss & before);
+            stats[2] += (unsigned long long)__popc(nofit & before);
+            if (term) {
+                h = shfl_hist(h, win);
+                if (h.status != 1 && h.status != 2) {
+                    ++stats[8];
+                } else {
+                    ++stats[3 + h.channel];
+                    ++stats[h.status == 2 ? 6 : 7];
+                }
+                done = 1;
+            }
+        }
+        if (!done) {
+            if (end < max_trials) cs->trial = end;
+            else { h = closure_exhausted(stats); done = 1; }
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < CLR_N_CONDITIONAL_STATS; ++i)
+            if (stats[i]) atomicAdd(cstats + i, stats[i]);
+    }
+    if (!done) return 2;
+    return closure_finish(D, r, opt, pidx, kind, h);
 }
 
 template <class S>

@@ -66,6 +66,8 @@ constexpr int kAcrBudget = 256;
 // (a closure can take 16384 trials, e.g. when no sampled sphere fits)
 constexpr int kCondInline = 8;
 constexpr int kCondBudget = 512;
+// trials per COND visit when a whole warp runs them (counter-based stream): 32 warp steps
+constexpr int kCondWarpBudget = 1024;
 
 template <class Mode>
 struct WavePool {
@@ -442,10 +444,64 @@ __global__ void __launch_bounds__(kWaveThreads, stage_min_blocks(Q)) wave_stage_
     warp_done(&bs, w.tallies, Q, done);
 }
 
+// COND stage of the counter-based stream without diagnostics: the photons of a warp's chunk are taken one
+// at a time and each one's closure trials run 32 at a time across the warp (closure_visit_warp), so a
+// closure of thousands of trials costs tens of warp steps instead of thousands of serial steps.
+template <class Mode>
+__global__ void __launch_bounds__(kWaveThreads, 1) wave_cond_warp_kernel(WaveLaunch w) {
+    const WaveWindow win = wave_window(w, WQ_COND);
+    if (win.n == 0) return;
+    const WavePool<Mode> pool = wave_pool<Mode>(w);
+    const uint32_t* ring = wave_ring(w, WQ_COND);
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    unsigned long long done = 0;
+    for (unsigned base = wave_claim(w, WQ_COND); base < win.n; base = wave_claim(w, WQ_COND)) {
+        const unsigned i = base + lane;
+        const bool valid = i < win.n;
+        const uint32_t my_slot = valid ? ring[(win.head + i) & wave_mask(w)] : 0u;
+        int my_dest = -1;
+        for (unsigned todo = __ballot_sync(FULL, valid); todo; todo &= todo - 1u) {
+            const int owner = __ffs(todo) - 1;
+            const uint32_t slot = __shfl_sync(FULL, my_slot, owner);
+            Ray r = pool.ray[slot];
+            typename Mode::Lane L = pool.lane[slot];
+            SlotMeta m = pool.meta[slot];
+            const DevScene& D = w.scenes[m.sid];
+            CondState cs;
+            cs.started = m.cond_started; cs.trial = m.cond_trial; cs.target = m.cond_target;
+            const int v = closure_visit_warp(D, r, L.optics(), w.tallies[m.sid].c.cstats, m.pidx, m.cond_kind, &cs,
+                                             kCondWarpBudget);
+            if (lane == owner) {
+                if (v == 2) { m.cond_started = cs.started; m.cond_trial = cs.trial; m.cond_target = cs.target; }
+                pool.ray[slot] = r;
+                pool.lane[slot] = L;
+                pool.meta[slot] = m;
+                my_dest = v == 2 ? WQ_COND : (v ? WQ_FIN : WQ_FLIGHT);
+                done++;
+            }
+            __syncwarp();
+        }
+        wave_push(w, my_dest, my_slot);
+    }
+    const unsigned long long sum = __reduce_add_sync(FULL, (unsigned)done);
+    if (lane == 0 && sum) atomicAdd(&w.tallies[0].sched[WQ_COND], sum);
+}
+
 // The event-handler stage kernel: its provenance-counting variant when provenance is on.
 template <class Mode, int Q>
 const void* stage_fn(const void* prov) {
     return prov ? (const void*)wave_stage_kernel<Mode, Q, true> : (const void*)wave_stage_kernel<Mode, Q, false>;
+}
+
+// The COND stage kernel: warp-cooperative closures on the counter-based stream without diagnostics, else
+// the per-lane stage kernel.
+template <class Mode>
+const void* cond_fn(const WaveLaunch& w) {
+    if constexpr (kCounterStream<typename Mode::Stream>) {
+        if (!w.prov && !w.light) return (const void*)wave_cond_warp_kernel<Mode>;
+    }
+    return stage_fn<Mode, WQ_COND>(w.prov);
 }
 
 // ---------------- FIN: detector scoring and tallies; the slot becomes free ----------------
@@ -621,7 +677,7 @@ struct WavePass {
             {(const void*)wave_stage_kernel<Mode, WQ_ENTRY>, 0, 0},
             {(w.light || w.prov) ? (const void*)wave_stage_kernel<Mode, WQ_FLIGHT, true>
                      : (const void*)wave_stage_kernel<Mode, WQ_FLIGHT, false>, 0, 0},
-            {stage_fn<Mode, WQ_COND>(w.prov), 0, 1},
+            {cond_fn<Mode>(w), 0, 1},
             {stage_fn<Mode, WQ_GEOM>(w.prov), 0, 0},
             {stage_fn<Mode, WQ_MORPH>(w.prov), 0, 1},
             {stage_fn<Mode, WQ_TOP>(w.prov), 0, 1},

@@ -82,3 +82,24 @@ def test_full_scene_philox_matches_xorshift(ctx):
     a, _ = ctx.trace(S.run_params(n, seed=41, rng_mode=abi.RNG_REFERENCE_XORSHIFT))
     b, _ = ctx.trace(S.run_params(n, seed=41, rng_mode=abi.RNG_PHILOX))
     _assert_agree(a, n, b, n, "full scene xorshift/philox")
+
+
+def test_warp_closures_match_serial_closures(ctx):
+    """The counter-based COND stage runs a closure's trials 32 at a time across a warp. Its closure
+    statistics (trials, rejected trials by reason, outcomes by channel) and tallies must match those of
+    the serial closures of the xorshift path on a scene where every absorbing-bin event is a closure."""
+    cfg, parts, grid = PS.build("absorbing_conditional")
+    _load(ctx, cfg, parts, grid)
+    n = 2_000_000
+    a, _ = ctx.trace(S.run_params(n, seed=71, rng_mode=abi.RNG_REFERENCE_XORSHIFT))
+    b, _ = ctx.trace(S.run_params(n, seed=72, rng_mode=abi.RNG_PHILOX))
+    _assert_agree(a, n, b, n, "absorbing_conditional xorshift/philox")
+    ca, cb = a["conditional_stats"].astype(float), b["conditional_stats"].astype(float)
+    closures_a, closures_b = ca[6] + ca[7] + ca[8] + ca[9], cb[6] + cb[7] + cb[8] + cb[9]
+    assert closures_a > 10_000 and closures_b > 10_000
+    # per closure: trials, rejected trials (outcome mismatch, no fit) and outcomes, as Poisson-like rates
+    for k, what in ((0, "trials"), (1, "mismatches"), (2, "no-fit"), (3, "geometric"), (4, "coherent"),
+                    (6, "absorbed"), (7, "scattered")):
+        ra, rb = ca[k] / closures_a, cb[k] / closures_b
+        se = np.sqrt(max(ca[k], 1.0)) / closures_a + np.sqrt(max(cb[k], 1.0)) / closures_b
+        assert abs(ra - rb) < 4.0 * se + 0.02 * max(ra, rb), (what, ra, rb, se)
