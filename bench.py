@@ -2,9 +2,11 @@
 """Benchmark of the photon-transport hot path (photons/s at fixed tally error).
 
 One "step" traces one batch of photons of the full-scene workload through the
-library's persistent photon kernel (transport + detector scoring + tallies in
-one launch). Photon counts are the same for GPU and CPU arms and both run the
-same estimator, so equal photon counts mean equal tally error.
+library's wavefront photon engine (transport, detector scoring and tallies; one
+CUDA graph of stage kernels per pass). Both arms run the same analog estimator;
+each line reports the per-channel standard error it reached and the figure of
+merit 1 / (relative SE^2 x time), so the speed ratio at equal tally error is
+measured, not assumed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload full|small|sweep]
   python bench.py --impl reference ...   # the reference's own CPU implementation
@@ -31,11 +33,42 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# Work per photon of the wavefront engine on each workload (counter-based stream), summed over every
-# stage kernel of one ncu capture of a 4e6-photon trace of the same scene:
-# warp instructions issued, FP64 flops executed (DFMA counted as 2) and DRAM bytes read + written.
-# The issue-slot roofline divides warp instructions issued per second by 4 schedulers x SMs x clock.
-PER_PHOTON = {"full": {"warp_inst": 423.5, "fp64_flops": 17.1, "dram_bytes": 981.8}, "small": None, "sweep": None}
+# Per photon of the wavefront engine on the full scene (counter-based stream), from ncu captures of a small
+# trace of the same scene summed over every stage kernel: warp instructions issued (the issue-slot cross-check
+# of the roofline, 4 schedulers x SMs x clock) and DRAM bytes read + written (the traffic figure). The
+# roofline's achieved work itself comes from the event counters of the timed traces (workcount.py).
+PER_PHOTON = {"full": {"warp_inst": 423.5, "dram_bytes": 981.8}}
+HEADLINE_CHANNELS = (0, 9, 17)  # transmitted, nephelometric (90 deg) and nearest-backscatter (170 deg) detectors
+
+
+def channel_error(tallies: list, seconds: float) -> dict:
+    """Per headline channel: native hits, relative standard error of the hit fraction (binomial; weighted
+    runs: from the weight sums) and the figure of merit 1 / (relative SE^2 x seconds). The ratio of two
+    arms' figures of merit is their speed ratio at equal tally error."""
+    import numpy as np
+    n = float(sum(int(t["n_rays"]) for t in tallies))
+    out = {}
+    for j in HEADLINE_CHANNELS:
+        hits = float(sum(int(t["hw_native"][j]) for t in tallies))
+        w = float(sum(float(t["weight_native"][j]) for t in tallies))
+        w2 = float(sum(float(t["weight_sq_native"][j]) for t in tallies))
+        mean = w / n if n else 0.0
+        var = max(w2 / n - mean * mean, 0.0) / n if n else 0.0
+        rel = float(np.sqrt(var) / mean) if mean > 0 else None
+        out[str(j)] = {"hits": int(hits), "mean_per_photon": mean, "rel_se": rel,
+                       "fom_per_s": (1.0 / (rel * rel * seconds)) if rel and seconds > 0 else None}
+    out["photons"] = int(n)
+    out["seconds"] = seconds
+    return out
+
+
+def equal_error_speedup(gpu: dict, cpu: dict) -> dict:
+    """Per headline channel: GPU figure of merit / CPU figure of merit (speed ratio at equal tally error)."""
+    out = {}
+    for j in HEADLINE_CHANNELS:
+        a, b = gpu[str(j)]["fom_per_s"], cpu[str(j)]["fom_per_s"]
+        out[str(j)] = (a / b) if a and b else None
+    return out
 
 
 def workload(name: str):
@@ -85,6 +118,7 @@ def sweep_cpu_estimate(scs: list, threads: int, seconds: float, n_sample: int = 
     import oracle_harness as H
     from tardiis_and_claritas_gb300 import scene as S
     kind = "reference" if H.reference_available() else "port"
+    build = "reference_fast" if kind == "reference" else "port"  # the reference's source built with -O3
     order = sorted(range(len(scs)), key=lambda i: optical_depth_proxy(scs[i]))
     m_s = min(n_sample, len(scs))
     ranks = sorted({round(k * (len(scs) - 1) / max(m_s - 1, 1)) for k in range(m_s)})
@@ -94,7 +128,7 @@ def sweep_cpu_estimate(scs: list, threads: int, seconds: float, n_sample: int = 
     for i in idx:
         sc = scs[i]
         t0 = time.perf_counter()
-        o = H.OracleRun(kind, sc.cfg, sc.particles)
+        o = H.OracleRun(build, sc.cfg, sc.particles)
         t_prep = time.perf_counter() - t0
         # grow the photon sample until it takes about its share of the time budget (or is the whole run)
         m = min(sc.n_photons, 2000)
@@ -144,6 +178,7 @@ def run_sweep(args, ctx, rank: int, world: int, local_rank: int, dist, dev) -> d
     sampler.start()
     build_ms, trace_ms, walls = [], [], []
     launches = passes = 0
+    all_tallies = []
     for k in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -156,6 +191,7 @@ def run_sweep(args, ctx, rank: int, world: int, local_rank: int, dist, dev) -> d
         nl, npass = ctx.last_launches()
         launches += nl
         passes += npass
+        all_tallies.extend(T)
     torch.cuda.synchronize()
     clocks = sampler.stop()
     dev_ms = float(sum(build_ms) + sum(trace_ms))
@@ -169,19 +205,18 @@ def run_sweep(args, ctx, rank: int, world: int, local_rank: int, dist, dev) -> d
     h2d = sum(int(p.n_bins) * (4 * 8 + 2 * 8 + 1) for p in parts) + SWEEP_SCENARIOS * (
         abi.C.sizeof(abi.SceneParams) + abi.C.sizeof(abi.RunParams) + 8)
     d2h = SWEEP_SCENARIOS * (abi.C.sizeof(abi.Tallies) + 8 * 8 + 4 * 8 + 4) + 4
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    sm_mhz = measured_peaks().get("sm_max_mhz") or 2070.0
-    issue_peak = 4.0 * sms * sm_mhz * 1e6
-    per = PER_PHOTON.get("sweep") if rng_mode == abi.RNG_PHILOX else None
+    from tardiis_and_claritas_gb300 import workcount as WC
     trace_s = float(sum(trace_ms)) * 1e-3 / args.steps
-    roofline = {"bound": "issue", "unit": "Twarp-inst/s", "peak": issue_peak / 1e12,
-                "peak_source": f"4 warp schedulers x {sms} SMs x {sm_mhz:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json)",
-                "achieved": None, "frac": None, "traffic": None,
+    # roofline of the sweep's trace from its own event counters (workcount.py) against the FP32 lane rate
+    wk = WC.work(all_tallies)
+    lane_peak = ctx.calibrate(0) / 2.0
+    ach = wk["fp32_ops"] / (float(sum(trace_ms)) * 1e-3)
+    roofline = {"bound": "fp32-issue", "unit": "Tops/s", "achieved": ach / 1e12, "peak": lane_peak / 1e12,
+                "frac": ach / lane_peak, "ops_per_photon": wk["ops_per_photon"],
+                "peak_source": "FP32 FFMA lane-operation rate measured in this run by the library's calibration kernel",
+                "work": "FP32-equivalent operations from the event counters of the timed sweep traces (workcount.py)",
+                "traffic": None,
                 "dominant": "the sweep's trace: all wavefront stage kernels over every scenario's photons"}
-    if per:
-        ach = per["warp_inst"] * n_photons / trace_s
-        roofline.update({"achieved": ach / 1e12, "frac": ach / issue_peak, "traffic": per["dram_bytes"] * n_photons,
-                         "traffic_unit": "bytes per sweep trace (ncu dram__bytes_read+write, scaled by photons)"})
     line = {"metric": "scenarios/s (at fixed tally error)", "value": value, "unit": "scenarios/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 transport, f64 Mie",
@@ -278,6 +313,99 @@ def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> di
     return line
 
 
+def _timed_traces(ctx, runs: list, flush) -> tuple:
+    """Device seconds and tallies of one trace per run, L2 flushed before each."""
+    import torch
+    ms, tallies = 0.0, []
+    for r in runs:
+        flush.zero_()
+        torch.cuda.synchronize()
+        T, _ = ctx.trace(r)
+        ms += ctx.last_kernel_ms()
+        tallies.append(T)
+    return ms * 1e-3, tallies
+
+
+def rankine_subrecord(ctx, args, rng_mode, flush) -> dict:
+    """The full scene as specified (a Rankine vortex from the 600 rpm stirrer with a 5 mm core) traced on the
+    GPU, with the CPU restatement of this library's Rankine surface as its CPU baseline (the reference has
+    no Rankine surface, so the headline line uses its localized-vortex stand-in)."""
+    from tardiis_and_claritas_gb300 import scene as S
+    cfg, parts, grid, zmax = S.full_scene_workload(surface="rankine_vortex")
+    ctx.set_scene(cfg.to_scene_params())
+    ctx.build_particles(parts.spec(cfg), cfg.sediment_spec(grid, zmax))
+    n, k = 100_000_000, 2
+    _timed_traces(ctx, [S.run_params(n // 10, seed=5, rng_mode=rng_mode)], flush)
+    secs, tallies = _timed_traces(ctx, [S.run_params(n, seed=11 + i, rng_mode=rng_mode) for i in range(k)], flush)
+    out = {"workload": "full scene with the Rankine free surface (600 rpm stirrer, 5 mm core, dip "
+                       f"{1e3 * cfg.vortex_wall_center_height_difference_m:.2f} mm), otherwise as the headline",
+           "photons_per_step": n, "steps": k, "value": n * k / secs, "unit": "photons/s",
+           "tally_error": channel_error(tallies, secs)}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_harness as H
+        o = H.OracleRun("port", cfg, parts, grid=grid, grid_zmax=zmax)
+        threads = os.cpu_count() or 1
+        m = 200_000
+        t = time.perf_counter()
+        T, _ = o.trace(S.run_params(m, seed=3), threads=threads)
+        dt = time.perf_counter() - t
+        o.close()
+        cpu_err = channel_error([T], dt)
+        out["cpu_baseline"] = {"value": m / dt, "unit": "photons/s", "cores": threads, "kind": "port",
+                               "sample": f"{m} photons, {dt:.1f} s", "tally_error": cpu_err}
+        out["equal_error_speedup"] = equal_error_speedup(out["tally_error"], cpu_err)
+    return out
+
+
+def weighted_subrecord(ctx, args) -> dict:
+    """The dense stress case (2 um clay, sigma_g 1.5, 20 g/L: optical depth above 100 across the cell; a
+    1200 rpm Rankine stirrer) with an absorption source (water absorbing 4 per metre; the reference's water
+    does not absorb) traced analog and weighted (implicit capture, Russian roulette below a weight of 1e-4,
+    survivors at 1e-3): photons/s and tally error of each, and the weighted estimator's gain at equal
+    error. A bounded number of photons per run (the specification's 1e9 would take minutes)."""
+    from tardiis_and_claritas_gb300 import abi, scene as S
+    dh = S.stirrer_rankine_delta_h(1200.0, 0.005, 0.0125)
+    cfg = S.small_cell_config(free_surface_model="rankine_vortex", vortex_wall_center_height_difference_m=dh,
+                              vortex_core_radius_m=0.005, particle_surface_rms_slope_deg=0.0,
+                              wave_surface_rms_height_m=0.0, water_absorption_per_m=4.0)
+    cfg.validate()
+    parts = S.quartz_particles(20000.0, n_bins=16, median_um=2.0, sigma_g=1.5, d_min_um=0.5, d_max_um=10.0)
+    ctx.set_scene(cfg.to_scene_params())
+    ctx.build_particles(parts.spec(cfg), cfg.sediment_spec())
+    import torch
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    n = 500_000
+    out = {"workload": "dense stress: 16-bin clay (median 2 um, sigma_g 1.5, 0.5-10 um) at 20 g/L, Rankine 1200 rpm, "
+                       "5 mm core, water absorption 4 /m, smooth spheres",
+           "photons_per_run": n}
+    for name, mode in (("analog", abi.WEIGHT_ANALOG), ("weighted", abi.WEIGHT_IMPLICIT)):
+        def mk(seed, mode=mode):
+            return S.run_params(n, seed=seed, rng_mode=abi.RNG_PHILOX, weight_mode=mode,
+                                roulette_threshold=1e-4, roulette_survival=1e-3)
+        _timed_traces(ctx, [mk(1)], flush)
+        secs, tallies = _timed_traces(ctx, [mk(2), mk(3)], flush)
+        t = tallies[-1]
+        out[name] = {"value": 2 * n / secs, "unit": "photons/s", "tally_error": channel_error(tallies, secs),
+                     "roulette_kills": int(t["event_counts"][abi.EV_NAMES.index("roulette_kills")]),
+                     "water_steps_per_photon": float(t["event_counts"][abi.EV_NAMES.index("water_steps")]) / n,
+                     "status_counts": [int(v) for v in t["status_counts"][:10]]}
+    out["weighted_gain_at_equal_error"] = equal_error_speedup(out["weighted"]["tally_error"],
+                                                              out["analog"]["tally_error"])
+    return out
+
+
+def sweep_subrecord(args, ctx, rank, world, local_rank, dev) -> dict:
+    """The 512-scenario batched sweep (scenarios/s) in the default line: two timed steps."""
+    sub = argparse.Namespace(**vars(args))
+    sub.steps, sub.warmup = 2, 1
+    line = run_sweep(sub, ctx, rank, world, local_rank, None, dev)
+    keep = ("metric", "value", "unit", "steps", "ms_per_step", "e2e", "roofline", "sweep", "cpu_baseline")
+    out = {k: line[k] for k in keep if k in line}
+    out["workload"] = SWEEP_WORKLOAD
+    return out
+
+
 def measured_peaks() -> dict:
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -338,9 +466,12 @@ class CpuReference:
         import oracle_harness as H
         cfg, parts, grid, zmax, _ = workload(name)
         self.kind = "reference" if H.reference_available() else "port"
-        self.o = H.OracleRun(self.kind, cfg, parts, grid=grid, grid_zmax=zmax)
+        # the reference's own source built for speed (-O3, contraction allowed); the port where it is absent
+        self.build = "reference_fast" if self.kind == "reference" else "port"
+        self.o = H.OracleRun(self.build, cfg, parts, grid=grid, grid_zmax=zmax)
         self.threads = threads
         self.probe = 20_000 if name == "full" else 200_000
+        self.tallies = []
 
     def sample_size(self, seconds: float) -> int:
         from tardiis_and_claritas_gb300 import scene as S
@@ -350,10 +481,13 @@ class CpuReference:
         return max(self.probe, int(self.probe * seconds / max(dt, 1e-3)))
 
     def time(self, n: int, seed: int) -> float:
+        """Seconds to trace n photons; the run's tallies are kept in self.tallies."""
         from tardiis_and_claritas_gb300 import scene as S
         t = time.perf_counter()
-        self.o.trace(S.run_params(n, seed=seed), threads=self.threads)
-        return time.perf_counter() - t
+        T, _ = self.o.trace(S.run_params(n, seed=seed), threads=self.threads)
+        dt = time.perf_counter() - t
+        self.tallies.append(T)
+        return dt
 
     def close(self):
         self.o.close()
@@ -403,16 +537,23 @@ def run_reference_arm(args, rank: int, world: int):
     n = ref.sample_size(args.cpu_seconds)
     for i in range(args.warmup):
         ref.time(max(n // 10, ref.probe), seed=100 + i)
+    ref.tallies = []
     total_t = sum(ref.time(n, seed=200 + k) for k in range(args.steps))
+    tallies = ref.tallies
     ref.close()
     total_n = n * args.steps
     value = total_n / total_t
+    cfg_line = workload_config(name, n, "reference xorshift")
+    cfg_line["gpu_arm_photons_per_step"] = n_gpu
     line = {"impl": "reference", "metric": "photons/s (at fixed tally error)", "value": value, "unit": "photons/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64",
-            "data": "synthetic (seeded)", "config": workload_config(name, n_gpu, "reference xorshift"),
+            "data": "synthetic (seeded)", "config": cfg_line,
             "cpu_baseline": {"value": value, "unit": "photons/s", "cores": threads, "kind": ref.kind,
+                             "build": "the reference's CUDA_SRC as host C++, -O3, OpenMP over photons"
+                             if ref.kind == "reference" else "the CPU restatement, -O2, OpenMP over photons",
                              "sample": f"{n} photons of the same workload per step, {args.steps} steps"},
+            "tally_error": channel_error(tallies, total_t),
             "e2e": {"value": value, "unit": "photons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -434,6 +575,8 @@ def main():
     ap.add_argument("--photons", type=int, default=0, help="override photons per step")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="full workload: skip the Rankine, sweep and weighted sub-records")
     ap.add_argument("--e2e-steps", type=int, default=3, help="steps of the end-to-end leg (0: skip it)")
     ap.add_argument("--engine", choices=["wavefront", "persistent"], default="wavefront",
                     help="photon engine (the persistent kernel is kept for comparison)")
@@ -455,6 +598,7 @@ def main():
     import numpy as np
     import torch
     from tardiis_and_claritas_gb300 import abi, lib as L, scene as S
+    from tardiis_and_claritas_gb300 import workcount as WC
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
@@ -508,14 +652,17 @@ def main():
     tallies = []
     wall0 = time.perf_counter()
     launches = passes = 0
+    tail_ms, tail_n = [], []
     for k in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         T, _ = ctx.trace(run(args.warmup + k))
         kernel_ms.append(ctx.last_kernel_ms())
-        nl, npass = ctx.last_launches()
-        launches += nl
-        passes += npass
+        es = ctx.engine_stats()
+        launches += es["launches"]
+        passes += es["passes"]
+        tail_ms.append(es["tail_ms"])
+        tail_n.append(es["tail_photons"])
         tallies.append(T)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
@@ -557,22 +704,38 @@ def main():
     launch_s = total_ms * 1e-3 / args.steps
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     sm_mhz = measured_peaks().get("sm_max_mhz") or 2070.0
-    issue_peak = 4.0 * sms * sm_mhz * 1e6  # warp instructions per second
-    per = PER_PHOTON.get(args.workload) if (rng_mode == abi.RNG_PHILOX and args.engine == "wavefront") else None
-    roofline = {"bound": "issue", "unit": "Twarp-inst/s", "peak": issue_peak / 1e12,
-                "peak_source": f"4 warp schedulers x {sms} SMs x {sm_mhz:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json)",
-                "achieved": None, "frac": None, "traffic": None,
+    # roofline: algorithmic FP32-equivalent operations from this run's own event counters (workcount.py)
+    # against the FP32 lane-operation rate of this GPU (its FFMA throughput, measured by the library's
+    # calibration kernel in this run, one FMA = one operation)
+    wk = WC.work(tallies)
+    lane_peak = fp32_peak / 2.0
+    ach = wk["fp32_ops"] / (total_ms * 1e-3)  # this GPU's work over the (max-over-ranks) device time
+    roofline = {"bound": "fp32-issue", "unit": "Tops/s", "achieved": ach / 1e12, "peak": lane_peak / 1e12,
+                "frac": ach / lane_peak,
+                "peak_source": "FP32 FFMA lane-operation rate measured in this run by the library's calibration "
+                               "kernel (MEASURED_PEAKS.json has no FP32 figure)",
+                "work": "FP32-equivalent operations counted from the event counters of the timed traces x the "
+                        "per-event table of workcount.py",
+                "ops_per_photon": wk["ops_per_photon"], "events_per_photon": wk["events_per_photon"],
+                "fp64": {"achieved_tflops": wk["fp64_flops"] / (total_ms * 1e-3) / 1e12,
+                         "peak_tflops": fp64_peak / 1e12,
+                         "frac": wk["fp64_flops"] / (total_ms * 1e-3) / fp64_peak,
+                         "peak_source": "measured DFMA loop (library calibration kernel, same GPU)"},
+                "traffic": None,
                 "dominant": "one trace: all wavefront stage kernels (they run concurrently inside each pass graph)"}
+    per = PER_PHOTON.get(args.workload) if (rng_mode == abi.RNG_PHILOX and args.engine == "wavefront") else None
     if per:
-        ach = per["warp_inst"] * n / launch_s
-        roofline.update({"achieved": ach / 1e12, "frac": ach / issue_peak, "traffic": per["dram_bytes"] * n,
-                         "traffic_unit": "bytes per trace (ncu dram__bytes_read+write, scaled by photons)"})
-        roofline["fp64"] = {"achieved_tflops": per["fp64_flops"] * n / launch_s / 1e12,
-                            "peak_tflops": fp64_peak / 1e12,
-                            "frac": per["fp64_flops"] * n / launch_s / fp64_peak,
-                            "peak_source": "measured DFMA loop (library calibration kernel, same GPU)"}
+        issue_peak = 4.0 * sms * sm_mhz * 1e6  # warp instructions per second
+        wi = per["warp_inst"] * n / launch_s
+        roofline["traffic"] = per["dram_bytes"] * n
+        roofline["traffic_unit"] = "DRAM bytes per trace (ncu dram__bytes_read+write per photon x photons)"
         roofline["hbm"] = {"achieved_gbs": per["dram_bytes"] * n / launch_s / 1e9,
                            "peak_gbs": measured_peaks().get("hbm_gbs")}
+        roofline["issue_slot_cross_check"] = {
+            "warp_inst_per_photon": per["warp_inst"], "achieved_twarp_inst_s": wi / 1e12,
+            "peak_twarp_inst_s": issue_peak / 1e12, "frac": wi / issue_peak,
+            "source": f"ncu smsp__inst_executed.sum per photon of a small trace; 4 schedulers x {sms} SMs x "
+                      f"{sm_mhz:.0f} MHz"}
     stage_names = ["gen", "entry", "flight", "cond", "geom", "morph", "top", "bottom", "side", "acryl", "fin"]
     cfg_line = workload_config(args.workload, n, args.rng)
     cfg_line["engine"] = args.engine
@@ -583,16 +746,28 @@ def main():
             "e2e": {"value": e2e, "unit": "photons/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "steps": e2e_steps, "includes": "scene upload, Mie/table/rate/field precompute, trace, tally readback"},
             "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline,
+            "tally_error": channel_error(tallies, total_ms * 1e-3),
             "engine": {"passes_per_trace": passes / args.steps, "wall_s": wall,
+                       "tail_ms_per_trace": float(np.mean(tail_ms)) if tail_ms else 0.0,
+                       "tail_photons_per_trace": float(np.mean(tail_n)) if tail_n else 0.0,
                        "stage_visits_per_photon": {stage_names[i]: float(sched[i] / (n * args.steps))
                                                    for i in range(len(stage_names))},
                        "fp32_peak_tflops": fp32_peak / 1e12}}
+    if args.workload == "full" and rank == 0 and not args.no_extras:
+        line["rankine"] = rankine_subrecord(ctx, args, rng_mode, flush)
+        line["sweep"] = sweep_subrecord(args, ctx, rank, world, local_rank, dev)
+        line["weighted"] = weighted_subrecord(ctx, args)
     if rank == 0 and world == 1 and not args.no_cpu:
         ref = CpuReference(args.workload, os.cpu_count() or 1)
         ns = ref.sample_size(args.cpu_seconds)
         dt = ref.time(ns, seed=8)
         line["cpu_baseline"] = {"value": ns / dt, "unit": "photons/s", "cores": ref.threads, "kind": ref.kind,
+                                "build": "the reference's CUDA_SRC as host C++, -O3, OpenMP over photons"
+                                if ref.kind == "reference" else "the CPU restatement, -O2, OpenMP over photons",
                                 "sample": f"{ns} photons of the same workload, {dt:.1f} s"}
+        cpu_err = channel_error(ref.tallies[-1:], dt)
+        line["cpu_baseline"]["tally_error"] = cpu_err
+        line["equal_error_speedup"] = equal_error_speedup(line["tally_error"], cpu_err)
         ref.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

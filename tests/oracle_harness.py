@@ -21,6 +21,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 PORT_SO = os.path.join(ORACLE_DIR, "_build", "libclaritas_oracle.so")
 REF_SO = os.path.join(ORACLE_DIR, "_ref", "libclaritas_ref_host.so")
+REF_FAST_SO = os.path.join(ORACLE_DIR, "_ref", "libclaritas_ref_host_fast.so")
 REF_SRC = os.path.join(ORACLE_DIR, "_ref", "claritas_cuda_src.inc")
 
 _libs: dict = {}
@@ -77,10 +78,14 @@ def load(kind: str = "port"):
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         lib.clo_trace_provenance.restype = C.c_int
         prefix = "clo_"
-    elif kind == "reference":
+    elif kind in ("reference", "reference_fast"):
         if not reference_available():
             raise FileNotFoundError("host build of the reference is not available")
-        lib = _bind(C.CDLL(REF_SO), "clref_")
+        so = REF_SO
+        if kind == "reference_fast":  # the timed CPU baseline: the same source built with -O3 and contraction
+            subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref_fast"], check=True)
+            so = REF_FAST_SO
+        lib = _bind(C.CDLL(so), "clref_")
         lib.clref_trace_provenance.argtypes = [C.c_void_p, C.POINTER(abi.RunParams), C.POINTER(abi.Tallies),
                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         lib.clref_trace_provenance.restype = C.c_int
