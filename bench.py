@@ -88,7 +88,8 @@ def workload_config(name: str, n: int, rng: str) -> dict:
                             "FP64 Mie phase tables (1801 angles), 860 nm",
                 "photons_per_step": n, "rng": rng, "l2": "flushed between steps (256 MiB write)"}
     return {"workload": "small plain MC: 64 lognormal quartz bins (median 20 um, sigma_g 1.6) at 100 mg/L, uniform, "
-                        "flat surface, r=12.5 mm cell, Mie tables 1801 angles, 860 nm",
+                        "flat surface, r=12.5 mm cell, 2 mm collimated disc beam at the sensor plane, Mie tables "
+                        "1801 angles, 860 nm",
             "photons_per_step": n, "rng": rng, "l2": "flushed between steps (256 MiB write)"}
 
 

@@ -979,6 +979,17 @@ static void o_trace_ray(const clo_state* S, uint32_t gid, uint32_t seed0, uint32
     memset(&bc, 0, sizeof bc);
     float x, y, z, vx = 0.0f, vy = 1.0f, vz = 0.0f;
     int st = 0;
+    /* collimated disc beam (new in this library, no reference lines to follow): a uniform disc of radius
+     * disc_radius centred on the 180-degree axis at height disc_height, launched along +y from the
+     * sensor-ring radius; the same two draws and arithmetic as the device's source_segment */
+    if (P->source_kind == CLR_SOURCE_COLLIMATED_DISC) {
+        float u1 = o_uniform(&stSRC), u2 = o_uniform(&stSRC);
+        float rr = P->disc_radius * sqrtf(u1);
+        float ph = 2.0f * O_PI_F * u2;
+        x = rr * cosf(ph);
+        z = P->disc_height + rr * sinf(ph);
+        y = -P->ring_in;
+    } else
     /* source (:4650-4697) */
     {
         float u1 = fmaxf(o_uniform(&stSRC), 1e-12f), u2 = o_uniform(&stSRC);

@@ -1165,7 +1165,29 @@ __device__ __noinline__ int o_acrylic_run(S* s, const o_cell* C, float n_side_ai
     const int it0 = as->it;
     const int end = (budget > 0 && cap - it0 > budget) ? it0 + budget : cap;
     int surf_next = 0;
-    for (int it = it0; it < end; ++it) {
+    int it = it0;
+    const float path0 = *acrylic_path;
+    for (; it < end; ++it) {
+        if constexpr (kCounterStream<S>) {
+            // Counter-based stream only (no reference counterpart): a long traversal whose ray meets the
+            // conserved-orbit trapped classifier (o_trapped: total internal reflection at every surface the
+            // ray can reach, from invariants that reflection keeps) can never escape and ends trapped at the
+            // bounce cap, as the classifier decides there. The remaining bounces are then accounted with the
+            // reflection mix and path per bounce of this visit, and the traversal goes straight to the cap.
+            if (it >= 512 && (it & 127) == 0 && it - it0 >= 128 &&
+                o_trapped(*x, *y, *z, *vx, *vy, *vz, n_water, n_acrylic, n_air, n_bottom_ext, Rin, Rout)) {
+                const long long done = it - it0, left = cap - it;
+                bc->cir += (int)((long long)bc->cir * left / done);
+                bc->cor += (int)((long long)bc->cor * left / done);
+                bc->bir += (int)((long long)bc->bir * left / done);
+                bc->bor += (int)((long long)bc->bor * left / done);
+                bc->ctir += (int)((long long)bc->ctir * left / done);
+                bc->btir += (int)((long long)bc->btir * left / done);
+                *acrylic_path += (*acrylic_path - path0) * (float)((double)left / (double)done);
+                it = cap;
+                break;
+            }
+        }
         *out_bounces = it;
         float t;
         if constexpr (kCounterStream<S>) {
@@ -1255,8 +1277,8 @@ __device__ __noinline__ int o_acrylic_run(S* s, const o_cell* C, float n_side_ai
         if (stuck >= 8) { *sub = OS_ACRYLIC_BOUNCE_LIMIT; return 0; }
         last_surf = surf;
     }
-    if (end < cap) {
-        as->it = end; as->stuck = stuck; as->last_surf = last_surf;
+    if (it < cap) {  // the budget ran out first (it == end)
+        as->it = it; as->stuck = stuck; as->last_surf = last_surf;
         return -1;
     }
     if (o_trapped(*x, *y, *z, *vx, *vy, *vz, n_water, n_acrylic, n_air, n_bottom_ext, Rin, Rout)) {

@@ -679,8 +679,11 @@ def full_scene_workload(n_photons: int = 100_000_000, surface: str = "localized_
 
 
 def small_plain_workload():
-    """The small plain-MC case: 64 lognormal bins (median 20 um, sigma_g 1.6) of quartz at 100 mg/L, uniform."""
-    cfg = small_cell_config(particle_surface_rms_slope_deg=0.0, wave_surface_rms_height_m=0.0)
+    """The small plain-MC case: 64 lognormal bins (median 20 um, sigma_g 1.6) of quartz at 100 mg/L, uniform,
+    lit by a 2 mm collimated disc beam through the 180-degree port at the sensor plane (20 mm above the
+    bottom; this library's source option, the reference has only its LED)."""
+    cfg = small_cell_config(particle_surface_rms_slope_deg=0.0, wave_surface_rms_height_m=0.0,
+                            source_kind="collimated_disc", disc_beam_radius_m=1.0e-3)
     cfg.validate()
     return cfg, quartz_particles(100.0), None, None
 

@@ -28,8 +28,11 @@ def ctx():
 
 
 def _z_binomial(a, na, b, nb):
+    """Two-proportion z statistic with the pooled standard error (the rate under the null hypothesis of
+    equal proportions), which stays valid when one sample sees few or no counts of a rare outcome."""
     pa, pb = a / na, b / nb
-    se = np.maximum(np.sqrt(pa * (1 - pa) / na + pb * (1 - pb) / nb), 1.0 / max(na, nb))
+    p = (a + b) / (na + nb)
+    se = np.maximum(np.sqrt(p * (1 - p) * (1.0 / na + 1.0 / nb)), 1.0 / (na + nb))
     return np.abs(pa - pb) / se
 
 
@@ -103,3 +106,64 @@ def test_warp_closures_match_serial_closures(ctx):
         ra, rb = ca[k] / closures_a, cb[k] / closures_b
         se = np.sqrt(max(ca[k], 1.0)) / closures_a + np.sqrt(max(cb[k], 1.0)) / closures_b
         assert abs(ra - rb) < 4.0 * se + 0.02 * max(ra, rb), (what, ra, rb, se)
+
+
+def test_early_trapped_classification_keeps_acrylic_statistics(ctx):
+    """On the counter-based stream a long acrylic traversal that meets the conserved-orbit trapped classifier
+    ends at once (its remaining bounces accounted with the reflection mix seen so far) instead of bouncing on
+    to the cap. The acrylic statistics must stay those of the bounce-by-bounce xorshift path: rays with a
+    wall TIR (binomial), the mean number of wall reflections and TIRs per entered ray (heavy-tailed: a few
+    rays run thousands of bounces, hence the wide bound), trapped rays (Poisson)."""
+    cfg, parts, grid, zmax = S.full_scene_workload()
+    _load(ctx, cfg, parts, grid, zmax)
+    n = 10_000_000
+    a, _ = ctx.trace(S.run_params(n, seed=81, rng_mode=abi.RNG_REFERENCE_XORSHIFT))
+    b, _ = ctx.trace(S.run_params(n, seed=82, rng_mode=abi.RNG_PHILOX))
+    rf_tir = 5  # CLR_RF_CELL_TIR
+    z = _z_binomial(np.array([a["ray_flags"][rf_tir]], float), n, np.array([b["ray_flags"][rf_tir]], float), n)
+    assert z[0] < 4.0, z
+    for k in (6, 7, 11):  # CLR_ES_CIR, CLR_ES_COR, CLR_ES_CTIR
+        ra = a["entered_sums"][k] / a["ray_flags"][0]
+        rb = b["entered_sums"][k] / b["ray_flags"][0]
+        assert abs(ra - rb) < 0.15 * max(ra, rb), (k, ra, rb)
+    ta, tb = float(a["status_counts"][8]), float(b["status_counts"][8])
+    assert abs(ta - tb) <= 4.0 * np.sqrt(max(ta + tb, 1.0)), (ta, tb)
+
+
+def test_c1_collimated_disc_beam_matches_cpu_oracle(ctx):
+    """The small plain case as specified: a 2 mm collimated disc beam (this library's source option) into
+    100 mg/L of 20 um quartz. Both streams on the GPU against the CPU restatement of the same source."""
+    import oracle_harness as H
+    cfg, parts, grid, zmax = S.small_plain_workload()
+    _load(ctx, cfg, parts, grid, zmax)
+    n_gpu, n_cpu = 4_000_000, 1_000_000
+    g, _ = ctx.trace(S.run_params(n_gpu, seed=91, rng_mode=abi.RNG_PHILOX))
+    x, _ = ctx.trace(S.run_params(n_gpu, seed=92, rng_mode=abi.RNG_REFERENCE_XORSHIFT))
+    orc = H.OracleRun("port", cfg, parts)
+    c, _ = orc.trace(S.run_params(n_cpu, seed=93))
+    orc.close()
+    assert g["status_counts"][3] == 0 and x["status_counts"][3] == 0  # no collimator: nothing rejected
+    _assert_agree(g, n_gpu, c, n_cpu, "C1 disc beam philox/oracle")
+    _assert_agree(x, n_gpu, c, n_cpu, "C1 disc beam xorshift/oracle")
+
+
+def test_dense_clay_matches_cpu_oracle(ctx):
+    """The dense stress regime (20 g/L of 2 um clay in the small cell under a localized vortex: optical depth
+    ~100, histories of thousands of events) on both GPU streams against the CPU restatement."""
+    import oracle_harness as H
+    cfg, parts, grid = PS.build("dense_clay")
+    _load(ctx, cfg, parts, grid)
+    n_gpu, n_cpu = 2_000_000, 100_000
+    g, _ = ctx.trace(S.run_params(n_gpu, seed=101, rng_mode=abi.RNG_PHILOX))
+    x, _ = ctx.trace(S.run_params(n_gpu, seed=102, rng_mode=abi.RNG_REFERENCE_XORSHIFT))
+    assert g["device_error"] == 0 and x["device_error"] == 0
+    orc = H.OracleRun("port", cfg, parts)
+    c, _ = orc.trace(S.run_params(n_cpu, seed=103))
+    orc.close()
+    _assert_agree(g, n_gpu, c, n_cpu, "dense clay philox/oracle")
+    _assert_agree(x, n_gpu, c, n_cpu, "dense clay xorshift/oracle")
+    _assert_agree(g, n_gpu, x, n_gpu, "dense clay philox/xorshift")
+    # the histories are long: mean free flights per photon agree within 5 % (a heavy-tailed mean)
+    fa = g["event_counts"][abi.EV_NAMES.index("water_steps")] / n_gpu
+    fc = c["event_counts"][abi.EV_NAMES.index("water_steps")] / n_cpu
+    assert abs(fa - fc) < 0.05 * fc, (fa, fc)
