@@ -26,7 +26,7 @@ from typing import Dict, Optional
 
 import numpy as np
 
-from . import abi, scene as S
+from . import abi, materials as M, scene as S
 
 DETECTOR_ANGLES_DEG = S.DETECTOR_ANGLES_DEG
 
@@ -296,9 +296,14 @@ class ClaritasForwardModel:
         elif material in self._materials:
             base = self._materials[material]
         else:
-            raise NotImplementedError(
-                f"material {material!r}: named PSD tables are not bundled; pass a scene.Particles or "
-                "register_material() one")
+            # the reference's named materials: raw PSD weights and per-bin n/k, with the constructor's
+            # optical-constants override, at the constructor's particle density (:6036-6052)
+            d, w_raw = M.get_material_psd_raw(material)
+            n, k = M.get_material_optical_constants(material, self.config.particle_optical_constants_by_material,
+                                                    self.config.n_particle)
+            base = S.Particles(d, w_raw, n, k, 0.0, float(self.config.density_kg_per_m3))
+            if weights is not None and np.asarray(weights).shape != d.shape:
+                raise ValueError(f"{material} requires {d.size} PSD weights")
         c = float(concentration_g_per_L)
         if not math.isfinite(c) or c < 0.0:
             raise ValueError("concentration must be finite and >=0")

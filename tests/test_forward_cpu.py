@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-from tardiis_and_claritas_gb300 import forward as F, scene as S
+from tardiis_and_claritas_gb300 import forward as F, materials as M, scene as S
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "forward_fixtures.npz")
 
@@ -55,8 +55,8 @@ def test_unsupported_features_raise_explicitly():
         m.simulate(parts, 0.1, n_rays=10, heatmap_size=-1)
     with pytest.raises(NotImplementedError):
         m.simulate(parts, 0.1, n_rays=10, collect_rays=True)
-    with pytest.raises(NotImplementedError, match="named PSD tables"):
-        m.simulate("loess", 0.1, n_rays=10)
+    with pytest.raises(ValueError, match="material must be 'loess' or 'kaolin'"):
+        m.simulate("basalt", 0.1, n_rays=10)
     with pytest.raises(ValueError, match="ray_id_start"):
         m.simulate(parts, 0.1, n_rays=10, ray_id_start=2 ** 32)
 
@@ -326,3 +326,22 @@ def test_adaptive_simulate_on_the_oracle_engine():
     np.testing.assert_allclose(pd["wall_path_partition_closure_error_scores"], 0.0, atol=1e-9)
     np.testing.assert_allclose(pd["first_particle_bin_partition_closure_error_scores"], 0.0, atol=1e-9)
     m.close()
+
+
+@pytest.mark.parametrize("material", ["loess", "kaolin"])
+def test_named_material_runs_through_the_facade(material):
+    """The reference's default call, simulate(material, concentration) with a named material (its run_one_case,
+    CLARITAS.py:13020): the bundled PSD and optical constants, traced here through the CPU restatement."""
+    m = F.ClaritasForwardModel(rng="reference", sediment_transport_model="uniform", free_surface_model="flat",
+                               vortex_wall_center_height_difference_m=0.0)
+    ctx = _OracleContext()
+    ctx.set_scene(m.config.to_scene_params())
+    m._ctx = ctx
+    prep = m._prepare_gpu_particle_physics(material, 0.5)
+    d, w = M.get_material_psd_raw(material)
+    n, k = M.get_material_optical_constants(material)
+    np.testing.assert_array_equal(prep["d"], d)
+    np.testing.assert_array_equal(prep["nidx"], n)
+    np.testing.assert_array_equal(prep["kidx"], k)
+    r = m.simulate(material, 0.5, n_rays=20_000, seed=3)
+    assert np.isfinite(r.normalized_hardware_symmetry_response).all() and r.hardware_native_hits.sum() > 0

@@ -49,3 +49,33 @@ def test_adaptive_stop_is_the_first_batch_meeting_the_target(model):
     assert len(rows) == 1 or rows[-2]["cumulative_selected_score"] < 2000.0
     fixed = model.simulate("quartz", 1.0, n_rays=res.n_rays, seed=5)
     np.testing.assert_array_equal(fixed.hardware_native_hits, res.hardware_native_hits)
+
+
+@pytest.mark.parametrize("material", ["loess", "kaolin"])
+def test_named_material_default_call(material):
+    """The reference's default call with a named material (run_one_case, CLARITAS.py:13020): the bundled
+    PSD and per-bin n/k give the CPU restatement's physics tables, and the GPU facade's tallies agree with
+    the facade driven through the CPU restatement (reference streams) within binomial errors."""
+    import oracle_harness as H
+    from test_forward_cpu import _OracleContext
+    kw = dict(sediment_transport_model="uniform", free_surface_model="flat", vortex_wall_center_height_difference_m=0.0,
+              statistics_batch_rays=250_000)
+    g = F.ClaritasForwardModel(**kw)
+    prep = g._prepare_gpu_particle_physics(material, 0.5)
+    c = F.ClaritasForwardModel(rng="reference", **kw)
+    ctx = _OracleContext()
+    ctx.set_scene(c.config.to_scene_params())
+    c._ctx = ctx
+    cprep = c._prepare_gpu_particle_physics(material, 0.5)
+    for k in ("qext", "qsca", "phase_cdf"):
+        np.testing.assert_allclose(prep["device"][k], cprep["device"][k], rtol=1e-9, atol=1e-12, err_msg=k)
+    n_g, n_c = 2_000_000, 200_000
+    rg = g.simulate(material, 0.5, n_rays=n_g, seed=11)
+    rc = c.simulate(material, 0.5, n_rays=n_c, seed=12)
+    g.close()
+    for a, b in ((rg.hardware_native_hits, rc.hardware_native_hits), (rg.hardware_mirror_hits, rc.hardware_mirror_hits)):
+        a, b = np.asarray(a, float), np.asarray(b, float)
+        p = (a + b) / (n_g + n_c)
+        se = np.maximum(np.sqrt(p * (1 - p) * (1 / n_g + 1 / n_c)), 1.0 / (n_g + n_c))
+        z = np.abs(a / n_g - b / n_c) / se
+        assert z.max() < 4.5 and np.sum(z > 3.0) <= 1, np.round(z, 2)
