@@ -361,24 +361,24 @@ def rankine_subrecord(ctx, args, rng_mode, flush) -> dict:
 
 def weighted_subrecord(ctx, args) -> dict:
     """The dense stress case (2 um clay, sigma_g 1.5, 20 g/L: optical depth above 100 across the cell; a
-    1200 rpm Rankine stirrer) with an absorption source (water absorbing 4 per metre; the reference's water
-    does not absorb) traced analog and weighted (implicit capture, Russian roulette below a weight of 1e-4,
+    1200 rpm Rankine stirrer) with the clay absorbing as the reference's kaolin table says (k 1e-4 to 8e-4 by
+    diameter), traced analog and weighted (implicit capture, Russian roulette below a weight of 1e-4,
     survivors at 1e-3): photons/s and tally error of each, and the weighted estimator's gain at equal
     error. A bounded number of photons per run (the specification's 1e9 would take minutes)."""
     from tardiis_and_claritas_gb300 import abi, scene as S
     dh = S.stirrer_rankine_delta_h(1200.0, 0.005, 0.0125)
     cfg = S.small_cell_config(free_surface_model="rankine_vortex", vortex_wall_center_height_difference_m=dh,
                               vortex_core_radius_m=0.005, particle_surface_rms_slope_deg=0.0,
-                              wave_surface_rms_height_m=0.0, water_absorption_per_m=4.0)
+                              wave_surface_rms_height_m=0.0)
     cfg.validate()
-    parts = S.quartz_particles(20000.0, n_bins=16, median_um=2.0, sigma_g=1.5, d_min_um=0.5, d_max_um=10.0)
+    parts = S.kaolin_clay_particles(20000.0, n_bins=16, median_um=2.0, sigma_g=1.5, d_min_um=0.5, d_max_um=10.0)
     ctx.set_scene(cfg.to_scene_params())
     ctx.build_particles(parts.spec(cfg), cfg.sediment_spec())
     import torch
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     n = 500_000
-    out = {"workload": "dense stress: 16-bin clay (median 2 um, sigma_g 1.5, 0.5-10 um) at 20 g/L, Rankine 1200 rpm, "
-                       "5 mm core, water absorption 4 /m, smooth spheres",
+    out = {"workload": "dense stress: 16-bin clay (median 2 um, sigma_g 1.5, 0.5-10 um) with the kaolin table's n and "
+                       "k at 20 g/L, Rankine 1200 rpm, 5 mm core, smooth spheres",
            "photons_per_run": n}
     for name, mode in (("analog", abi.WEIGHT_ANALOG), ("weighted", abi.WEIGHT_IMPLICIT)):
         def mk(seed, mode=mode):

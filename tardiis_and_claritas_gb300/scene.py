@@ -577,6 +577,20 @@ def quartz_particles(concentration_mg_l: float = 100.0, n_bins: int = 64, median
     return Particles(d, w, np.full(n_bins, n), np.full(n_bins, k), concentration_mg_l * 1e-3, density)
 
 
+def kaolin_clay_particles(concentration_mg_l: float, n_bins: int = 16, median_um: float = 2.0, sigma_g: float = 1.5,
+                          d_min_um: float = 0.5, d_max_um: float = 10.0, density: float = 2650.0) -> Particles:
+    """Lognormal clay whose per-bin n and k follow the reference's kaolin optical-constant table (bundled in
+    materials.npz), interpolated in log diameter and held constant beyond the table's ends."""
+    from . import materials as M
+    d, w = lognormal_mass_psd(n_bins, d_min_um * 1e-6, d_max_um * 1e-6, median_um * 1e-6, sigma_g)
+    td, _ = M.get_material_psd_raw("kaolin")
+    tn, tk = M.get_material_optical_constants("kaolin")
+    order = np.argsort(td)
+    x, xs = np.log(d), np.log(td[order])
+    return Particles(d, w, np.interp(x, xs, tn[order]), np.interp(x, xs, tk[order]), concentration_mg_l * 1e-3,
+                     density)
+
+
 def three_component_particles(concentration_mg_l: float = 500.0, bins_per_component: int = 21,
                               medians_um=(2.0, 20.0, 100.0), fractions=(0.3, 0.5, 0.2), sigma_g: float = 1.4,
                               n: float = 1.54, k: float = 0.0, density: float = 2650.0) -> Particles:

@@ -4,6 +4,8 @@ Run on a machine with a GB300 (sm_103a) after oracle/ref_extract.py has written
 oracle/_ref/claritas_cuda_src.inc from the reference checkout:
 
     python tests/golden/make_gpu_fixtures.py --out tests/golden/gpu_ref_fixtures.npz
+    python tests/golden/make_gpu_fixtures.py --scenes moment_constrained \
+        --out tests/golden/gpu_ref_moment_fixtures.npz
 
 It compiles oracle/ref_gpu_driver.cu (the reference's CUDA_SRC plus a launcher
 that replays the reference host's launch sequence) into
@@ -87,7 +89,7 @@ def field_of(lib, h, n_bins: int) -> dict:
 
 def run_scene(lib, name: str, n_rays: int = N_RAYS):
     cfg, parts, grid = PS.build(name)
-    sp, ps, ss = cfg.to_scene_params(), parts.spec(cfg), cfg.sediment_spec(grid)
+    sp, ps, ss = cfg.to_scene_params(), parts.spec(cfg, PS.moments(name, parts.diameter_m.size)), cfg.sediment_spec(grid)
     h = C.c_void_p()
     rc = lib.clrefgpu_prepare(C.byref(sp), C.byref(ps), C.byref(ss), C.byref(h))
     if rc != 0:
@@ -110,11 +112,12 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.join(ROOT, "tests", "golden", "gpu_ref_fixtures.npz"))
     ap.add_argument("--rays", type=int, default=N_RAYS)
+    ap.add_argument("--scenes", default="", help="comma-separated scene names (default: every parity scene)")
     a = ap.parse_args()
     lib = load()
     out = {}
     meta = {"n_rays": a.rays, "n_compact": N_COMPACT, "scenes": {}}
-    for name in PS.SCENES:
+    for name in (a.scenes.split(",") if a.scenes else PS.SCENES):
         t = time.time()
         ph, tal, rec, field = run_scene(lib, name, a.rays)
         meta["scenes"][name] = {"records_sha256": PS.records_digest(rec), "physics_sha256": PS.physics_digests(ph),

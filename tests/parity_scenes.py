@@ -63,15 +63,33 @@ CPU_ONLY = {
     "dense_clay": (SCULLY, dict(concentration_mg_l=20000.0, n_bins=16, median_um=2.0, sigma_g=1.5, d_min_um=0.5,
                                 d_max_um=10.0), False),
 }
+# The moment-constrained event law (model 5: the Mie two-moment post-outcome map of the reference,
+# apply_mie_moment_constraint, CLARITAS/CLARITAS.py:4459-4476) with per-bin moment coefficients; its GPU
+# golden fixture is a file of its own (gpu_ref_moment_fixtures.npz).
+MOMENT_SCENES = {
+    "moment_constrained": (dict(particle_event_model="hybrid_mie_exact_rate_moment_constrained"),
+                           dict(concentration_mg_l=2000.0), False),
+}
 # Every scene runs in the CPU oracle as well (the meridional field solver included).
 CPU_SCENES = list(SCENES) + list(CPU_ONLY)
 # Scenes whose sediment field the meridional solver makes (no supplied grid).
 SOLVED_FIELD = {"meridional_solver"}
 
 
+def moments(name: str, n_bins: int):
+    """Per-bin moment coefficients (a, b, mode) of a moment-constrained scene, else None: a fixed,
+    non-trivial map (a in [0.7, 1.3], |b| <= 0.15, the map off in every third bin)."""
+    if name not in MOMENT_SCENES:
+        return None
+    i = np.arange(n_bins, dtype=np.float64)
+    return {"a": 0.7 + 0.6 * (i / max(n_bins - 1, 1)), "b": 0.15 * np.sin(i),
+            "mode": (np.arange(n_bins) % 3 != 0).astype(np.uint8)}
+
+
 def build(name: str):
     """(config, particles, grid-or-None) of a parity scene."""
-    over, pk, needs_grid = SCENES[name] if name in SCENES else CPU_ONLY[name]
+    table = SCENES if name in SCENES else MOMENT_SCENES if name in MOMENT_SCENES else CPU_ONLY
+    over, pk, needs_grid = table[name]
     cfg = S.small_cell_config(**over)
     cfg.validate()
     parts = S.quartz_particles(**pk)

@@ -25,6 +25,7 @@ pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "gpu_ref_fixtures.npz")
 GOLD_FMA = os.path.join(os.path.dirname(__file__), "golden", "gpu_ref_fma_fixtures.npz")
+GOLD_MOMENT = os.path.join(os.path.dirname(__file__), "golden", "gpu_ref_moment_fixtures.npz")
 
 
 @pytest.fixture(scope="module")
@@ -40,7 +41,7 @@ def ctx():
 def prepare(ctx, name):
     cfg, parts, grid = PS.build(name)
     ctx.set_scene(cfg.to_scene_params())
-    ps, ss = parts.spec(cfg), cfg.sediment_spec(grid)
+    ps, ss = parts.spec(cfg, PS.moments(name, parts.diameter_m.size)), cfg.sediment_spec(grid)
     ctx.build_particles(ps, ss)
     return cfg, parts
 
@@ -79,6 +80,27 @@ def test_bit_exact_against_reference_kernels(ctx, gold, name, engine):
         np.testing.assert_array_equal(tal[k], z[f"{name}/{k}"], err_msg=f"{name}: {k}")
     assert tal["event_counts"][:PS.EVENT_KEYS].tolist() == m["event_counts"]
     assert [int(v) for v in tal["conditional_stats"]] == m["conditional_stats"]
+    assert PS.records_digest(rec) == m["records_sha256"], first_mismatch(rec, z[f"{name}/compact"])
+
+
+@pytest.mark.parametrize("engine", list(ENGINES))
+def test_moment_constrained_law_bit_exact(ctx, engine):
+    """Event model 5 with per-bin moment coefficients (the reference's apply_mie_moment_constraint,
+    CLARITAS.py:4459-4476): records, tables and tallies equal those of the reference's kernels."""
+    if not os.path.exists(GOLD_MOMENT):
+        pytest.skip("tests/golden/gpu_ref_moment_fixtures.npz not generated yet")
+    z = np.load(GOLD_MOMENT)
+    meta = json.loads(bytes(z["meta"]).decode())
+    name = "moment_constrained"
+    m = meta["scenes"][name]
+    prepare(ctx, name)
+    ph = ctx.physics()
+    mism = [k for k, v in PS.physics_digests(ph).items() if v != m["physics_sha256"][k]]
+    assert not mism, f"{name}: physics tables differ from the reference kernels: {mism}"
+    tal, rec = ctx.trace(S.run_params(meta["n_rays"], seed=m["seed"], flags=ENGINES[engine]), records=True)
+    for k in PS.TALLY_KEYS:
+        np.testing.assert_array_equal(tal[k], z[f"{name}/{k}"], err_msg=f"{name}: {k}")
+    assert tal["event_counts"][:PS.EVENT_KEYS].tolist() == m["event_counts"]
     assert PS.records_digest(rec) == m["records_sha256"], first_mismatch(rec, z[f"{name}/compact"])
 
 

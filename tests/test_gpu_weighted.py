@@ -151,3 +151,18 @@ def test_weighted_arguments_are_checked(ctx):
     r = S.run_params(1000, seed=1, rng_mode=abi.RNG_PHILOX, weight_mode=7)
     with pytest.raises(RuntimeError, match="unknown weight_mode"):
         ctx.trace(r)
+
+
+def test_weighted_unbiased_on_dense_absorbing_clay(ctx):
+    """The dense stress regime with absorbing clay (20 g/L, optical depth ~100, the reference's kaolin n and k):
+    long histories multiply many albedos, so Russian roulette at the default threshold fires, and the weight
+    sums still estimate the analog hit counts."""
+    cfg, _, _ = PS.build("dense_clay")
+    parts = S.kaolin_clay_particles(20000.0)
+    _load(ctx, cfg, parts)
+    n = 1_000_000
+    a, _ = ctx.trace(S.run_params(n, seed=51, rng_mode=abi.RNG_PHILOX))
+    w, _ = ctx.trace(_weighted(n, seed=52))
+    assert a["status_counts"][5] > 1000 and w["status_counts"][5] == 0
+    assert int(w["event_counts"][abi.EV_NAMES.index("roulette_kills")]) > 0
+    _assert_unbiased(a, n, w, n, "dense kaolin clay")

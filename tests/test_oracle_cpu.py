@@ -197,3 +197,23 @@ def test_oracle_full_ray_without_failures(vortex):
     assert int(tal["failure_code_counts"][1:].sum()) == 0 and int(tal["status_counts"][4]) == 0
     assert int(tal["status_counts"][5]) > 0 and int(tal["conditional_stats"][0]) > 0
     assert int(tal["status_counts"].sum()) == 2048
+
+
+@pytest.mark.skipif(not H.reference_available(), reason="host build of the reference not present (no checkout)")
+def test_oracle_moment_constrained_law_matches_live_reference():
+    """Event model 5 with per-bin moment coefficients (apply_mie_moment_constraint, CLARITAS.py:4459-4476):
+    the restatement against the reference's host build, bit for bit."""
+    cfg, parts, grid = PS.build("moment_constrained")
+    mom = PS.moments("moment_constrained", parts.diameter_m.size)
+    a = H.OracleRun("port", cfg, parts, grid=grid, moments=mom)
+    b = H.OracleRun("reference", cfg, parts, grid=grid, moments=mom)
+    run = S.run_params(50000, seed=PS.seed_of("moment_constrained"))
+    ta, ra = a.trace(run, records=True)
+    tb, rb = b.trace(run, records=True)
+    assert PS.records_digest(ra) == PS.records_digest(rb)
+    for k in PS.TALLY_KEYS:
+        np.testing.assert_array_equal(ta[k], tb[k])
+    # the map is active: the same run without the moments gives other records
+    c = H.OracleRun("port", cfg, parts, grid=grid)
+    tc, rc = c.trace(run, records=True)
+    assert PS.records_digest(rc) != PS.records_digest(ra)
