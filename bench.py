@@ -37,7 +37,7 @@ sys.path.insert(0, ROOT)
 # trace of the same scene summed over every stage kernel: warp instructions issued (the issue-slot cross-check
 # of the roofline, 4 schedulers x SMs x clock) and DRAM bytes read + written (the traffic figure). The
 # roofline's achieved work itself comes from the event counters of the timed traces (workcount.py).
-PER_PHOTON = {"full": {"warp_inst": 423.5, "dram_bytes": 981.8}}
+PER_PHOTON = {"full": {"warp_inst": 289.7, "dram_bytes": 889.0}}
 HEADLINE_CHANNELS = (0, 9, 17)  # transmitted, nephelometric (90 deg) and nearest-backscatter (170 deg) detectors
 
 
