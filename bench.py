@@ -579,6 +579,9 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="full workload: skip the Rankine, sweep and weighted sub-records")
     ap.add_argument("--e2e-steps", type=int, default=3, help="steps of the end-to-end leg (0: skip it)")
+    ap.add_argument("--tune", choices=["auto", "off"], default="auto",
+                    help="tune the wavefront engine's scheduling settings for this GPU and scene before timing "
+                         "(tallies are the same under any setting; the search is outside the timed region)")
     ap.add_argument("--engine", choices=["wavefront", "persistent"], default="wavefront",
                     help="photon engine (the persistent kernel is kept for comparison)")
     args = ap.parse_args()
@@ -642,6 +645,16 @@ def main():
         return S.run_params(n, seed=20261203, ray_offset=off, rng_mode=rng_mode,
                             flags=abi.RUN_PERSISTENT_KERNEL if args.engine == "persistent" else 0)
 
+    tuning = None
+    if args.tune == "auto" and args.engine == "wavefront":
+        from tardiis_and_claritas_gb300 import autotune as AT
+        props = torch.cuda.get_device_properties(dev)
+        # trial photons come from a range no timed step uses (after every rank's steps)
+        base = S.replica_ray_offset(world, 0, args.warmup + args.steps + max(args.e2e_steps, 0), n)
+        tuning = AT.tune(ctx, lambda i: S.run_params(n, seed=20261203, ray_offset=(base + i * n) % ((1 << 32) - n),
+                                                     rng_mode=rng_mode),
+                         key=AT.scene_key(sp, ps, ss), photons=n, device_name=props.name,
+                         sm_count=props.multi_processor_count)
     for w in range(args.warmup):
         ctx.trace(run(w))
     torch.cuda.synchronize()
@@ -753,7 +766,16 @@ def main():
                        "tail_photons_per_trace": float(np.mean(tail_n)) if tail_n else 0.0,
                        "stage_visits_per_photon": {stage_names[i]: float(sched[i] / (n * args.steps))
                                                    for i in range(len(stage_names))},
-                       "fp32_peak_tflops": fp32_peak / 1e12}}
+                       "fp32_peak_tflops": fp32_peak / 1e12,
+                       "settings": {"tuned": tuning["config"], "defaults": abi.ENGINE_DEFAULTS,
+                                    "gain_over_defaults": tuning["gain"], "trials": tuning["trials"],
+                                    "cached": tuning["cached"],
+                                    "search_s": None if tuning["cached"] else
+                                    tuning["trials"] * tuning["default_trace_s"],
+                                    "best_alternatives": sorted(tuning.get("landscape", []),
+                                                                key=lambda e: e["relative_time"])[:4]}
+                       if tuning else {"tuned": None, "defaults": abi.ENGINE_DEFAULTS}}}
+    ctx.set_engine_config(None)  # the sub-records run their own scenes at the default settings
     if args.workload == "full" and rank == 0 and not args.no_extras:
         line["rankine"] = rankine_subrecord(ctx, args, rng_mode, flush)
         line["sweep"] = sweep_subrecord(args, ctx, rank, world, local_rank, dev)

@@ -491,6 +491,26 @@ int clr_last_kernel_ms(const clr_ctx* ctx, float* ms);
  * of wavefront passes (0 for the persistent kernel). No reference counterpart. */
 int clr_last_launches(const clr_ctx* ctx, int64_t* launches, int64_t* passes);
 
+/* Settings of the wavefront engine (no reference counterpart; the reference launches one thread per ray).
+ * They change how the work is scheduled, never a photon's draws or arithmetic: integer tallies are the same
+ * for any settings. Zero selects the default. stage_blocks[q] caps the resident blocks per SM of the stage
+ * kernel of queue q (order GEN, ENTRY, FLIGHT, COND, GEOM, MORPH, TOP, BOTTOM, SIDE, ACRYL, FIN). */
+#define CLR_ENGINE_DEFAULT_FLIGHT_STEPS 4
+#define CLR_ENGINE_DEFAULT_TAIL_PHOTONS 65536
+#define CLR_ENGINE_DEFAULT_RARE_BATCH 8192
+#define CLR_ENGINE_DEFAULT_PASS_BATCH 8
+#define CLR_N_STAGES 11
+typedef struct clr_engine_config {
+    int32_t flight_steps;           /* water flights per FLIGHT visit, 1..64 */
+    int32_t tail_photons;           /* photons in flight at which the single-thread tail kernel takes over */
+    int32_t rare_batch;             /* queue length at which a rare stage (MORPH, TOP, BOTTOM) runs */
+    int32_t stage_blocks[CLR_N_STAGES];
+    int32_t pass_batch;             /* pass graphs queued between two reads of the live flag */
+    int32_t reserved[3];
+} clr_engine_config;
+/* Use `config` for the following traces of the context (NULL: back to the defaults). */
+int clr_set_engine_config(clr_ctx* ctx, const clr_engine_config* config);
+
 /* Engine profile of the last clr_trace* / clr_sweep_trace call (no reference counterpart), the first n of:
  * [0] wavefront pass graphs launched, [1] kernel launches, [2] photons handed to the tail kernel (0 when it
  * did not run), [3] tail-kernel device time (ms, CUDA events around its launch), [4] the call's device time
@@ -527,7 +547,8 @@ int clr_mie_phase_noalloc(clr_ctx* ctx, const double* d_diameter_m, const double
                           double* d_qsca, double* d_asym_g, double* d_theta, double* d_phase_cdf, void* stream);
 
 /* Sizes of the ABI structs as compiled into the library (0 scene, 1 particle spec, 2 sediment spec,
- * 3 run params, 4 ray record, 5 tallies, 6 particle physics); -1 for an unknown index.
+ * 3 run params, 4 ray record, 5 tallies, 6 particle physics, 7 path provenance, 8 engine config); -1 for an
+ * unknown index.
  * No reference counterpart: lets a binding check its struct mirror against the library. */
 int64_t clr_abi_sizeof(int which);
 

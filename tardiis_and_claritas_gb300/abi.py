@@ -276,6 +276,27 @@ class PathProvenance(C.Structure):
         return {name: np.ctypeslib.as_array(getattr(self, name)).copy() for name, _ in self._fields_}
 
 
+STAGE_NAMES = ("GEN", "ENTRY", "FLIGHT", "COND", "GEOM", "MORPH", "TOP", "BOTTOM", "SIDE", "ACRYL", "FIN")
+ENGINE_DEFAULTS = {"flight_steps": 4, "tail_photons": 65536, "rare_batch": 8192, "pass_batch": 8}
+
+
+class EngineConfig(C.Structure):
+    """clr_engine_config: scheduling settings of the wavefront engine (zero = default)."""
+    _fields_ = [("flight_steps", i32), ("tail_photons", i32), ("rare_batch", i32),
+                ("stage_blocks", i32 * len(STAGE_NAMES)), ("pass_batch", i32), ("reserved", i32 * 3)]
+
+    @classmethod
+    def from_dict(cls, d: dict | None) -> "EngineConfig":
+        c = cls()
+        for k, v in (d or {}).items():
+            if k == "stage_blocks":
+                for name, b in v.items():
+                    c.stage_blocks[STAGE_NAMES.index(name)] = int(b)
+            else:
+                setattr(c, k, int(v))
+        return c
+
+
 class LightConfig(C.Structure):
     _fields_ = [("enabled", i32), ("nx", i32), ("ny", i32), ("nz", i32), ("max_rays", i32),
                 ("representative_rays", i32), ("max_segments_per_ray", i32), ("heatmap_size", i32),

@@ -45,6 +45,7 @@ struct clr_ctx {
     unsigned* wave_live = nullptr;  // pinned
     cudaEvent_t wave_ev = nullptr;
     cudaEvent_t tail_ev[2] = {nullptr, nullptr};  // timing events around the tail kernel
+    clr_engine_config engine = {};  // zeros: defaults
     int last_passes = 0;
     int last_tail = 0;
     unsigned last_tail_photons = 0;
@@ -564,6 +565,10 @@ static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* 
                         i, (double)run->roulette_threshold, (double)run->roulette_survival);
         if (run->rng_mode != r0.rng_mode || run->weight_mode != r0.weight_mode || run->flags != r0.flags)
             return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "runs of one call must share rng_mode, weight_mode and flags");
+        // closure trials draw from substreams numbered in 14 bits of a counter word on the Philox stream
+        if (run->rng_mode == CLR_RNG_PHILOX && refs[i].sp && refs[i].sp->conditional_retries > 16384)
+            return fail(ctx, CLR_ERR_UNSUPPORTED, "run %d: the Philox stream allows at most 16384 closure trials "
+                        "(conditional_retries %d)", i, refs[i].sp->conditional_retries);
     }
     const bool persistent = (r0.flags & CLR_RUN_PERSISTENT_KERNEL) != 0;
     if (prov && persistent)
@@ -623,6 +628,12 @@ static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* 
         w.ray = ctx->wave_ray; w.lane = ctx->wave_lane; w.meta = ctx->wave_meta; w.qbuf = ctx->wave_q;
         w.ctl = ctx->wave_ctl; w.cap = ctx->wave_cap; w.host_live = ctx->wave_live; w.flag_event = ctx->wave_ev;
         w.tail_begin = ctx->tail_ev[0]; w.tail_end = ctx->tail_ev[1];
+        const clr_engine_config& ec = ctx->engine;
+        w.flight_steps = ec.flight_steps > 0 ? ec.flight_steps : CLR_ENGINE_DEFAULT_FLIGHT_STEPS;
+        w.tail_photons = ec.tail_photons > 0 ? (unsigned)ec.tail_photons : CLR_ENGINE_DEFAULT_TAIL_PHOTONS;
+        w.rare_batch = ec.rare_batch > 0 ? (unsigned)ec.rare_batch : CLR_ENGINE_DEFAULT_RARE_BATCH;
+        for (int q = 0; q < CLR_N_STAGES; ++q) w.stage_blocks[q] = std::max(0, ec.stage_blocks[q]);
+        w.pass_batch = ec.pass_batch > 0 ? ec.pass_batch : CLR_ENGINE_DEFAULT_PASS_BATCH;
         w.light = d_light != nullptr;
         w.prov = prov ? ctx->wave_prov : nullptr;
         w.prov_rec = ctx->prov_rec_n > 0 ? ctx->d_prov_rec : nullptr;
@@ -1186,6 +1197,25 @@ int clr_last_launches(const clr_ctx* ctx, int64_t* launches, int64_t* passes) {
     return CLR_OK;
 }
 
+int clr_set_engine_config(clr_ctx* ctx, const clr_engine_config* config) {
+    if (!ctx) return CLR_ERR_INVALID_ARGUMENT;
+    if (!config) {
+        ctx->engine = clr_engine_config{};
+        return CLR_OK;
+    }
+    const clr_engine_config& c = *config;
+    if (c.flight_steps < 0 || c.flight_steps > 64 || c.tail_photons < 0 || c.tail_photons > (1 << 23) ||
+        c.rare_batch < 0 || c.rare_batch > (1 << 21) || c.pass_batch < 0 || c.pass_batch > 64)
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT,
+                    "engine config: flight_steps 0..64, tail_photons 0..8388608, rare_batch 0..2097152, "
+                    "pass_batch 0..64");
+    for (int q = 0; q < CLR_N_STAGES; ++q)
+        if (c.stage_blocks[q] < 0 || c.stage_blocks[q] > 32)
+            return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "engine config: stage_blocks must be 0..32");
+    ctx->engine = c;
+    return CLR_OK;
+}
+
 int clr_last_engine_stats(const clr_ctx* ctx, double* out, int n) {
     if (!ctx || !out || n < 1) return CLR_ERR_INVALID_ARGUMENT;
     const double v[5] = {(double)ctx->last_passes, (double)ctx->last_launches, (double)ctx->last_tail_photons,
@@ -1229,6 +1259,7 @@ int64_t clr_abi_sizeof(int which) {
         case 5: return (int64_t)sizeof(clr_tallies);
         case 6: return (int64_t)sizeof(clr_particle_physics);
         case 7: return (int64_t)sizeof(clr_path_provenance);
+        case 8: return (int64_t)sizeof(clr_engine_config);
         default: return -1;
     }
 }

@@ -75,6 +75,13 @@ struct WaveLaunch {
     unsigned* host_live;           // pinned host words: live, tail ready, photons in flight
     cudaEvent_t flag_event;
     cudaEvent_t tail_begin, tail_end;  // timing events recorded around the tail kernel
+    // engine settings (clr_engine_config, defaults filled in): water flights per FLIGHT visit, photons in
+    // flight at which the tail kernel takes over, queue length at which a rare stage runs, and per stage a
+    // cap on resident blocks per SM (0: occupancy)
+    int flight_steps;
+    unsigned tail_photons, rare_batch;
+    int stage_blocks[CLR_WQ_COUNT];
+    int pass_batch;
     bool light;                    // light-history diagnostics on: the FLIGHT stage with its hooks
     uint4* prov;                   // [cap] particle-event provenance per slot; null unless counted
     uint4* prov_rec;               // [n_rays] provenance of every ray, with per-ray records; nullable

@@ -154,6 +154,13 @@ __device__ __forceinline__ int closure_setup(S* s, Hist* out, double qs, double 
     return 0;
 }
 
+// Counter word 2 of the substream of closure trial t (counter-based stream): a tag bit, the photon's
+// event number (17 bits) and t (14 bits; trials per closure are at most 16384, checked per run).
+constexpr int kClosureTrialBits = 14;
+__device__ __forceinline__ uint32_t closure_trial_tag(int ic) {
+    return 0x80000000u | (((uint32_t)ic & 0x1FFFFu) << kClosureTrialBits);
+}
+
 __device__ __forceinline__ Hist closure_exhausted(unsigned long long* stats) {
     Hist h;
     memset(&h, 0, sizeof h);
@@ -170,7 +177,7 @@ __device__ __forceinline__ int conditional_body(
     float radius, float aspect, int orientation, float kappa, int max_bounces, float coherent, const float* cdf,
     const float* theta, int nt, float x, float y, float z, float vx, float vy, float vz, float rin, float zmin,
     float zmean, int surface, float delta, float core, int max_trials, unsigned long long* stats, CondState* cs,
-    int budget, float* wmul) {
+    int budget, float* wmul, uint32_t trial_tag) {
     if (!cs->started && closure_setup(s, out, qs, qe, ki, max_trials, stats, cs, wmul)) return 1;
     const int target_absorbed = cs->target;
     ClosureIn c;
@@ -184,7 +191,18 @@ __device__ __forceinline__ int conditional_body(
     Hist h;
     for (int trial = cs->trial; trial < end; ++trial) {
         ++stats[0];
-        const int t = closure_trial(s, c, target_absorbed, &h);
+        int t;
+        if constexpr (kCounterStream<S>) {
+            // trial `trial` on its own substream, as the warp-cooperative closure draws it: the result of a
+            // photon does not depend on which of the two runs its closure
+            S ts = *s;
+            ts.c2 = trial_tag | (uint32_t)trial;
+            ts.draw = 0u;
+            ts.idx = 4;
+            t = closure_trial(&ts, c, target_absorbed, &h);
+        } else {
+            t = closure_trial(s, c, target_absorbed, &h);
+        }
         if (t == -2) { ++stats[2]; continue; }
         if (t == -1) { ++stats[1]; continue; }
         if (h.status != 1 && h.status != 2) { ++stats[8]; *out = h; return 1; }
@@ -207,11 +225,11 @@ __device__ __noinline__ int conditional_interaction(
     float radius, float aspect, int orientation, float kappa, int max_bounces, float coherent, const float* cdf,
     const float* theta, int nt, float x, float y, float z, float vx, float vy, float vz, float rin, float zmin,
     float zmean, int surface, float delta, float core, int max_trials, unsigned long long* gstats,
-    CondState* cs, int budget, float* wmul) {
+    CondState* cs, int budget, float* wmul, uint32_t trial_tag) {
     unsigned long long stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int done = conditional_body(s, out, pidx, qs, qe, nm, nr, ki, wl, rough, radius, aspect, orientation, kappa,
                                       max_bounces, coherent, cdf, theta, nt, x, y, z, vx, vy, vz, rin, zmin, zmean,
-                                      surface, delta, core, max_trials, stats, cs, budget, wmul);
+                                      surface, delta, core, max_trials, stats, cs, budget, wmul, trial_tag);
 #pragma unroll
     for (int i = 0; i < 10; ++i)
         if (stats[i]) atomicAdd(gstats + i, stats[i]);
@@ -930,7 +948,7 @@ __device__ __forceinline__ int closure_visit(const DevScene& D, Ray& r, S* opt, 
         D.prad[pidx], P.spheroid_aspect, P.orientation_model, P.orientation_kappa, P.max_particle_bounces, COHERENT,
         D.phase_cdf, D.theta, D.nt, r.x, r.y, r.z, r.vx, r.vy, r.vz, P.rin, P.zmin, P.zmean, P.free_surface_model,
         P.vortex_delta_h, P.vortex_core_radius, kind == CK_GEOM ? P.conditional_retries - 1 : P.conditional_retries,
-        cstats, cs, budget, (kind == CK_FLIGHT && weighted_run(D)) ? &r.w : nullptr);
+        cstats, cs, budget, (kind == CK_FLIGHT && weighted_run(D)) ? &r.w : nullptr, closure_trial_tag(r.ic));
     if (!done) return 2;
     return closure_finish(D, r, opt, pidx, kind, h);
 }
@@ -978,7 +996,7 @@ __device__ __forceinline__ int closure_visit_warp(const DevScene& D, Ray& r, Phi
         c.pidx = pidx; c.orientation = P.orientation_model; c.max_bounces = P.max_particle_bounces; c.nt = D.nt;
         c.surface = P.free_surface_model;
         const int end = (budget > 0 && max_trials - cs->trial > budget) ? cs->trial + budget : max_trials;
-        const uint32_t tag = 0x80000000u | (((uint32_t)r.ic & 0x1FFFFu) << 14);
+        const uint32_t tag = closure_trial_tag(r.ic);
         for (int base = cs->trial; base < end && !done; base += 32) {
             const int t = base + lane;
             int res = 0;

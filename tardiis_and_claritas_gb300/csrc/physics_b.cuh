@@ -1141,6 +1141,10 @@ typedef struct {
     int model; float dh, core;
 } o_cell;
 
+/* Bounces per window of the trapped-orbit test of long traversals (counter-based stream); the pieces a
+ * traversal is cut into must start at multiples of 2 kTrapWindow. */
+constexpr int kTrapWindow = 128;
+
 /* Loop state of a traversal of the acrylic solid, so that a traversal can run in bounded pieces. */
 typedef struct {
     int it, stuck, last_surf;
@@ -1166,24 +1170,32 @@ __device__ __noinline__ int o_acrylic_run(S* s, const o_cell* C, float n_side_ai
     const int end = (budget > 0 && cap - it0 > budget) ? it0 + budget : cap;
     int surf_next = 0;
     int it = it0;
-    const float path0 = *acrylic_path;
+    o_bcount snap = *bc;
+    float snap_path = *acrylic_path;
     for (; it < end; ++it) {
         if constexpr (kCounterStream<S>) {
             // Counter-based stream only (no reference counterpart): a long traversal whose ray meets the
             // conserved-orbit trapped classifier (o_trapped: total internal reflection at every surface the
             // ray can reach, from invariants that reflection keeps) can never escape and ends trapped at the
             // bounce cap, as the classifier decides there. The remaining bounces are then accounted with the
-            // reflection mix and path per bounce of this visit, and the traversal goes straight to the cap.
-            if (it >= 512 && (it & 127) == 0 && it - it0 >= 128 &&
-                o_trapped(*x, *y, *z, *vx, *vy, *vz, n_water, n_acrylic, n_air, n_bottom_ext, Rin, Rout)) {
-                const long long done = it - it0, left = cap - it;
-                bc->cir += (int)((long long)bc->cir * left / done);
-                bc->cor += (int)((long long)bc->cor * left / done);
-                bc->bir += (int)((long long)bc->bir * left / done);
-                bc->bor += (int)((long long)bc->bor * left / done);
-                bc->ctir += (int)((long long)bc->ctir * left / done);
-                bc->btir += (int)((long long)bc->btir * left / done);
-                *acrylic_path += (*acrylic_path - path0) * (float)((double)left / (double)done);
+            // reflection mix and path per bounce of the last kTrapWindow bounces, and the traversal goes
+            // straight to the cap. The test runs at bounces it = (2k+1) kTrapWindow only and its window
+            // starts at a multiple of 2 kTrapWindow: pieces of a traversal start at multiples of that too
+            // (budgets are multiples of it), so the window lies inside the running piece and the result of a
+            // photon does not depend on how its traversal was cut into pieces.
+            if ((it & (2 * kTrapWindow - 1)) == 0) {
+                snap = *bc;
+                snap_path = *acrylic_path;
+            } else if (it >= 512 && (it & (2 * kTrapWindow - 1)) == kTrapWindow &&
+                       o_trapped(*x, *y, *z, *vx, *vy, *vz, n_water, n_acrylic, n_air, n_bottom_ext, Rin, Rout)) {
+                const long long left = cap - it;
+                bc->cir += (int)((long long)(bc->cir - snap.cir) * left / kTrapWindow);
+                bc->cor += (int)((long long)(bc->cor - snap.cor) * left / kTrapWindow);
+                bc->bir += (int)((long long)(bc->bir - snap.bir) * left / kTrapWindow);
+                bc->bor += (int)((long long)(bc->bor - snap.bor) * left / kTrapWindow);
+                bc->ctir += (int)((long long)(bc->ctir - snap.ctir) * left / kTrapWindow);
+                bc->btir += (int)((long long)(bc->btir - snap.btir) * left / kTrapWindow);
+                *acrylic_path += (*acrylic_path - snap_path) * (float)((double)left / (double)kTrapWindow);
                 it = cap;
                 break;
             }

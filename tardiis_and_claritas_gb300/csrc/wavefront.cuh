@@ -41,18 +41,20 @@ namespace {
 enum : int { WQ_FREE = 0, WQ_ENTRY, WQ_FLIGHT, WQ_COND, WQ_GEOM, WQ_MORPH, WQ_TOP, WQ_BOTTOM, WQ_SIDE, WQ_ACRYL,
              WQ_FIN };
 static_assert(WQ_FIN + 1 == CLR_WQ_COUNT, "queue count");
+static_assert(CLR_WQ_COUNT == CLR_N_STAGES, "one engine setting per stage queue");
 
 constexpr int kWaveThreads = 256;
-// water flights per FLIGHT visit before the photon is re-queued (bounds lane imbalance in a warp)
-constexpr int kFlightSteps = 4;
-// Once every photon is drawn and at most kTailPhotons remain in flight, the passes stop and one tail
-// kernel runs each remaining photon to its end in a single thread: the longest histories (thousands of
-// flights in optically dense scenes) then cost one step each instead of a pass each.
-constexpr unsigned kTailPhotons = 65536;
+// Defaults of the engine settings (clr_engine_config; an autotuner may choose others per scene class):
+// water flights per FLIGHT visit before the photon is re-queued (bounds lane imbalance in a warp); the
+// photons in flight at or below which, once every photon is drawn, the passes stop and one tail kernel
+// runs each remaining photon to its end in a single thread (the longest histories, thousands of flights
+// in optically dense scenes, then cost one step each instead of a pass each).
+constexpr int kFlightSteps = CLR_ENGINE_DEFAULT_FLIGHT_STEPS;
+constexpr unsigned kTailPhotons = CLR_ENGINE_DEFAULT_TAIL_PHOTONS;
 constexpr int kTailThreads = 128;
 // Rare stages (few photons per pass, long serial work per photon) run only when their queue holds a
 // full batch, after kMaxSkips passes, or while the pool drains.
-constexpr unsigned kRareBatch = 8192;
+constexpr unsigned kRareBatch = CLR_ENGINE_DEFAULT_RARE_BATCH;
 constexpr unsigned kMaxSkips = 8;
 __host__ __device__ constexpr bool stage_is_rare(int q) {
     return q == WQ_MORPH || q == WQ_TOP || q == WQ_BOTTOM;
@@ -62,6 +64,7 @@ __host__ __device__ constexpr int stage_min_blocks(int q) { return q == WQ_COND 
 // acrylic bounces per visit of SIDE, BOTTOM and ACRYL (a traversal can take 16384), all of them
 // once every photon has been drawn
 constexpr int kAcrBudget = 256;
+static_assert(kAcrBudget % (2 * kTrapWindow) == 0, "traversal pieces start where no trapped-orbit window spans them");
 // closure trials per visit: a few inline in GEOM (most closures end in one or two), more per COND visit
 // (a closure can take 16384 trials, e.g. when no sampled sphere fits)
 constexpr int kCondInline = 8;
@@ -117,7 +120,7 @@ __global__ void wave_begin_kernel(WaveLaunch w) {
         if (q != WQ_FREE) pending |= n;
         bool run = n > 0;
         if (q == WQ_FREE) run = run && drawing;
-        else if (stage_is_rare(q) && n < kRareBatch && c->skips[q] < kMaxSkips && drawing) run = false;
+        else if (stage_is_rare(q) && n < w.rare_batch && c->skips[q] < kMaxSkips && drawing) run = false;
         c->snap[q] = run ? c->tail[q] : c->head[q];
         c->skips[q] = run ? 0u : c->skips[q] + (n > 0 ? 1u : 0u);
         c->claim[q] = 0u;
@@ -127,7 +130,7 @@ __global__ void wave_begin_kernel(WaveLaunch w) {
     // photons still in flight after this pass at the most (every queue but FREE), once all are drawn
     unsigned in_flight = 0;
     for (int q = 1; q < CLR_WQ_COUNT; ++q) in_flight += c->tail[q] - c->head[q];
-    c->tail_ready = (!drawing && in_flight <= kTailPhotons) ? 1u : 0u;
+    c->tail_ready = (!drawing && in_flight <= w.tail_photons) ? 1u : 0u;
     c->in_flight = in_flight;
 }
 
@@ -306,7 +309,7 @@ __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevSce
     if constexpr (Q == WQ_ENTRY) {
         return entry_segment(D, r, L.transport()) ? WQ_FIN : WQ_FLIGHT;
     } else if constexpr (Q == WQ_FLIGHT) {
-        for (int k = 0; k < kFlightSteps; ++k) {
+        for (int k = 0; k < w.flight_steps; ++k) {
             int pidx = -1;
             const float vinx = r.vx, viny = r.vy, vinz = r.vz;
             const int coh0 = r.wcoh;
@@ -689,7 +692,8 @@ struct WavePass {
         p.blockDim = dim3(kWaveThreads);
         for (int q = 0; q < CLR_WQ_COUNT; ++q) {
             dim3 g;
-            if ((e = grid_of(ks[q].fn, ks[q].smem, num_sms, ks[q].per_sm_cap, &g)) != cudaSuccess) return e;
+            const int cap = w.stage_blocks[q] > 0 ? w.stage_blocks[q] : ks[q].per_sm_cap;
+            if ((e = grid_of(ks[q].fn, ks[q].smem, num_sms, cap, &g)) != cudaSuccess) return e;
             p.func = const_cast<void*>(ks[q].fn);
             p.gridDim = g;
             p.sharedMemBytes = (unsigned)ks[q].smem;
@@ -713,7 +717,7 @@ cudaError_t wave_run_t(const WaveLaunch& w, int num_sms, cudaStream_t st, long l
     if (e != cudaSuccess) return e;
     wave_init_kernel<<<(w.cap + 255) / 256, 256, 0, st>>>(w);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    const int batch = 8;
+    const int batch = w.pass_batch > 0 ? w.pass_batch : CLR_ENGINE_DEFAULT_PASS_BATCH;
     long long launched = 0;
     volatile unsigned* live = w.host_live;  // [live, tail_ready, in_flight] of the pass before the read
     static_assert(offsetof(WaveCtl, tail_ready) == offsetof(WaveCtl, live) + sizeof(unsigned) &&

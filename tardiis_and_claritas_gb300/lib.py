@@ -54,6 +54,7 @@ def load(build_if_missing: bool = False):
             "clr_last_kernel_ms": ([C.c_void_p, P(C.c_float)], C.c_int),
             "clr_last_launches": ([C.c_void_p, P(C.c_int64), P(C.c_int64)], C.c_int),
             "clr_last_engine_stats": ([C.c_void_p, P(C.c_double), C.c_int], C.c_int),
+            "clr_set_engine_config": ([C.c_void_p, P(abi.EngineConfig)], C.c_int),
             "clr_mie_phase_noalloc": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
                                        C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p], C.c_int),
@@ -94,7 +95,8 @@ def load(build_if_missing: bool = False):
 def exported_symbols() -> list[str]:
     return ["clr_create", "clr_destroy", "clr_last_error", "clr_version", "clr_set_scene", "clr_build_particles",
             "clr_read_particle_physics", "clr_trace", "clr_trace_host_records", "clr_trace_batch", "clr_abi_sizeof",
-            "clr_last_kernel_ms", "clr_last_launches", "clr_last_engine_stats", "clr_calibrate", "clr_mie_phase_noalloc", "clr_sweep_build",
+            "clr_last_kernel_ms", "clr_last_launches", "clr_last_engine_stats", "clr_set_engine_config", "clr_calibrate",
+            "clr_mie_phase_noalloc", "clr_sweep_build",
             "clr_sweep_trace", "clr_sweep_read_particle_physics", "clr_mlp_create", "clr_mlp_destroy",
             "clr_mlp_last_error", "clr_mlp_set_params", "clr_mlp_get_params", "clr_mlp_forward", "clr_mlp_gradients",
             "clr_mlp_train", "clr_mlp_last_ms", "clr_bf16_gemm_n256", "clr_read_sediment_field",
@@ -297,6 +299,13 @@ class Context:
         self._check(self.lib.clr_last_engine_stats(self.h, v, 5), "clr_last_engine_stats")
         return {"passes": int(v[0]), "launches": int(v[1]), "tail_photons": int(v[2]), "tail_ms": float(v[3]),
                 "trace_ms": float(v[4])}
+
+    def set_engine_config(self, config: dict | None = None):
+        """Scheduling settings for the following traces ({} or None: defaults); keys as abi.EngineConfig,
+        stage_blocks as {stage name: blocks per SM}."""
+        c = abi.EngineConfig.from_dict(config)
+        self._check(self.lib.clr_set_engine_config(self.h, C.byref(c) if config is not None else None),
+                    "clr_set_engine_config")
 
     def mie_phase_noalloc(self, diameter_ptr: int, n_real_ptr: int, k_imag_ptr: int, n_bins: int, n_medium: float,
                           wavelength_m: float, n_theta: int, qext_ptr: int, qsca_ptr: int, asym_g_ptr: int,

@@ -43,7 +43,7 @@ def test_library_exports_every_declared_symbol(library):
 
 def test_struct_sizes_match(library):
     mirror = [abi.SceneParams, abi.ParticleSpec, abi.SedimentSpec, abi.RunParams, abi.RayRecord, abi.Tallies,
-              abi.ParticlePhysics, abi.PathProvenance]
+              abi.ParticlePhysics, abi.PathProvenance, abi.EngineConfig]
     for i, cls in enumerate(mirror):
         assert library.clr_abi_sizeof(i) == C.sizeof(cls), cls.__name__
     assert library.clr_abi_sizeof(99) == -1
