@@ -160,9 +160,11 @@ def run_sweep(args, ctx, rank: int, world: int, local_rank: int, dist, dev) -> d
     import torch
     from tardiis_and_claritas_gb300 import abi, scene as S
     scs = S.sweep_workload(SWEEP_SCENARIOS, sampler_seed=rank)
-    scenes, parts, seds = S.sweep_specs(scs)
-    n_photons = sum(sc.n_photons for sc in scs)
     rng_mode = abi.RNG_PHILOX if args.rng == "philox" else abi.RNG_REFERENCE_XORSHIFT
+    tables = args.tables if args.tables != "auto" else ("fast" if rng_mode == abi.RNG_PHILOX else "reference")
+    scenes, parts, seds = S.sweep_specs(scs, table_arithmetic=abi.TABLES_FAST if tables == "fast"
+                                        else abi.TABLES_REFERENCE)
+    n_photons = sum(sc.n_photons for sc in scs)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     def runs(step: int):
@@ -172,6 +174,14 @@ def run_sweep(args, ctx, rank: int, world: int, local_rank: int, dist, dev) -> d
     for w in range(args.warmup):
         ctx.sweep_build(scenes, parts, seds)
         ctx.sweep_trace(runs(w))
+    tuning = None
+    if args.tune == "auto":
+        from tardiis_and_claritas_gb300 import autotune as AT
+        props = torch.cuda.get_device_properties(dev)
+        # trials trace steps no timed step uses (their seeds follow the timed steps')
+        tuning = AT.tune(ctx, key=f"sweep{SWEEP_SCENARIOS}-seed{rank}-{args.rng}", photons=n_photons, reps=1,
+                         device=AT.device_key(props.major, props.minor, props.multi_processor_count),
+                         trace=lambda i: ctx.sweep_trace(runs(args.warmup + args.steps + 1 + i)))
     torch.cuda.synchronize()
     if dist:
         dist.barrier(device_ids=[local_rank])
@@ -223,7 +233,7 @@ def run_sweep(args, ctx, rank: int, world: int, local_rank: int, dist, dev) -> d
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 transport, f64 Mie",
             "data": "synthetic (seeded)",
             "config": {"workload": SWEEP_WORKLOAD, "scenarios": SWEEP_SCENARIOS, "photons_per_step": n_photons,
-                       "rng": args.rng, "l2": "flushed between steps (256 MiB write); tables exceed L2"},
+                       "rng": args.rng, "tables": tables, "l2": "flushed between steps (256 MiB write); tables exceed L2"},
             "e2e": {"value": e2e, "unit": "scenarios/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "steps": args.steps,
                     "includes": "host wall time of clr_sweep_build (scenario upload, batched Mie/phase tables, rates) "
@@ -231,7 +241,13 @@ def run_sweep(args, ctx, rank: int, world: int, local_rank: int, dist, dev) -> d
             "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline,
             "sweep": {"build_ms": float(np.mean(build_ms)), "trace_ms": float(np.mean(trace_ms)),
                       "photons_per_s": n_photons / trace_s, "passes_per_trace": passes / args.steps,
-                      "detected_native_total": int(sum(int(t["hw_native"].sum()) for t in T))}}
+                      "detected_native_total": int(sum(int(t["hw_native"].sum()) for t in T)),
+                      "engine_settings": {"tuned": tuning["config"], "gain_over_defaults": tuning["gain"],
+                                          "source": {"user": "tuning cache", "shipped": "the package's tuning "
+                                                     "table (same search, same GPU type)"}.get(tuning["cached"],
+                                                                                              "searched in this run"),
+                                          "trials": tuning["trials"]} if tuning else None}}
+    ctx.set_engine_config(None)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = sweep_cpu_estimate(scs, os.cpu_count() or 1, args.cpu_seconds)
     return line
@@ -404,6 +420,7 @@ def sweep_subrecord(args, ctx, rank, world, local_rank, dev) -> dict:
     keep = ("metric", "value", "unit", "steps", "ms_per_step", "e2e", "roofline", "sweep", "cpu_baseline")
     out = {k: line[k] for k in keep if k in line}
     out["workload"] = SWEEP_WORKLOAD
+    out["tables"] = line["config"]["tables"]
     return out
 
 
@@ -579,6 +596,9 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="full workload: skip the Rankine, sweep and weighted sub-records")
     ap.add_argument("--e2e-steps", type=int, default=3, help="steps of the end-to-end leg (0: skip it)")
+    ap.add_argument("--tables", choices=["auto", "reference", "fast"], default="auto",
+                    help="phase-table arithmetic of the sweep build (auto: fast on the Philox stream, the reference's "
+                         "order of operations on the parity stream)")
     ap.add_argument("--tune", choices=["auto", "off"], default="auto",
                     help="tune the wavefront engine's scheduling settings for this GPU and scene before timing "
                          "(tallies are the same under any setting; the search is outside the timed region)")
@@ -645,6 +665,8 @@ def main():
         return S.run_params(n, seed=20261203, ray_offset=off, rng_mode=rng_mode,
                             flags=abi.RUN_PERSISTENT_KERNEL if args.engine == "persistent" else 0)
 
+    for w in range(args.warmup):
+        ctx.trace(run(w))
     tuning = None
     if args.tune == "auto" and args.engine == "wavefront":
         from tardiis_and_claritas_gb300 import autotune as AT
@@ -653,10 +675,8 @@ def main():
         base = S.replica_ray_offset(world, 0, args.warmup + args.steps + max(args.e2e_steps, 0), n)
         tuning = AT.tune(ctx, lambda i: S.run_params(n, seed=20261203, ray_offset=(base + i * n) % ((1 << 32) - n),
                                                      rng_mode=rng_mode),
-                         key=AT.scene_key(sp, ps, ss), photons=n, device_name=props.name,
-                         sm_count=props.multi_processor_count)
-    for w in range(args.warmup):
-        ctx.trace(run(w))
+                         key=AT.scene_key(sp, ps, ss), photons=n,
+                         device=AT.device_key(props.major, props.minor, props.multi_processor_count))
     torch.cuda.synchronize()
     if dist:
         dist.barrier(device_ids=[local_rank])

@@ -150,7 +150,15 @@ typedef struct clr_particle_spec {
     double wavelength_m;
     double wave_rms_height_m;
     double hybrid_wave_scale;
+    /* Arithmetic of the phase tables (no reference counterpart): CLR_TABLES_REFERENCE (0) keeps the
+     * reference's order of operations (bit-identical tables, required by the parity stream's bit-exact
+     * contract); CLR_TABLES_FAST (1) evaluates the same sums with fused multiply-adds and two angles per
+     * Legendre recurrence, ~4x less FP64 work, tables equal to rounding. */
+    int32_t table_arithmetic;
+    int32_t reserved_spec;
 } clr_particle_spec;
+#define CLR_TABLES_REFERENCE 0
+#define CLR_TABLES_FAST 1
 
 /* Inputs of the sediment coefficient precompute (CLARITAS/CLARITAS.py:3940-4038) and,
  * for sediment model 3, an externally supplied (r,z) concentration-scale grid laid

@@ -118,7 +118,7 @@ class ParticleSpec(C.Structure):
         ("diameter_m", PD), ("weight", PD), ("n_real", PD), ("k_imag", PD),
         ("moment_a", PD), ("moment_b", PD), ("moment_mode", PU8),
         ("concentration_kg_m3", f64), ("density_kg_m3", f64), ("n_medium", f64), ("wavelength_m", f64),
-        ("wave_rms_height_m", f64), ("hybrid_wave_scale", f64),
+        ("wave_rms_height_m", f64), ("hybrid_wave_scale", f64), ("table_arithmetic", i32), ("reserved_spec", i32),
     ]
 
 
@@ -275,6 +275,9 @@ class PathProvenance(C.Structure):
         import numpy as np
         return {name: np.ctypeslib.as_array(getattr(self, name)).copy() for name, _ in self._fields_}
 
+
+TABLES_REFERENCE = 0  # CLR_TABLES_REFERENCE: the reference's order of operations (bit-identical tables)
+TABLES_FAST = 1  # CLR_TABLES_FAST: FMA, two angles per Legendre recurrence (equal to rounding)
 
 STAGE_NAMES = ("GEN", "ENTRY", "FLIGHT", "COND", "GEOM", "MORPH", "TOP", "BOTTOM", "SIDE", "ACRYL", "FIN")
 ENGINE_DEFAULTS = {"flight_steps": 4, "tail_photons": 65536, "rare_batch": 8192, "pass_batch": 8}

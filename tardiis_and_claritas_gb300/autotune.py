@@ -13,7 +13,8 @@ live, how often they meet the walls).
 `tune` runs a one-sweep coordinate search from the defaults: every candidate value of one setting is timed
 (device time of whole traces, the median of `reps`), a value is kept when it beats the incumbent by more
 than `min_gain`, and the winner is timed once more against the defaults, interleaved, before it is
-accepted. Results are cached in a JSON file by (GPU name, SM count, scene key, photons per trace).
+accepted. Results are cached in a JSON file by (compute capability and SM count, scene key, photons per
+trace); `engine_tuning.json` beside this file ships results of the same search for known GPUs and workloads.
 """
 from __future__ import annotations
 
@@ -90,6 +91,27 @@ def _candidates(cfg: dict, group: str) -> list[dict]:
     return out
 
 
+SHIPPED_TABLE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "engine_tuning.json")
+
+
+def device_key(major: int, minor: int, sm_count: int) -> str:
+    """The GPU part of a tuning key: compute capability and SM count (names differ between drivers)."""
+    return f"sm{int(major)}{int(minor)}x{int(sm_count)}"
+
+
+def entry_key(device: str, key: str, photons: int) -> str:
+    return f"{device}|{key}|{int(photons).bit_length()}"
+
+
+def load_shipped() -> dict:
+    """Settings this package ships, found by the same search on the GPUs named in their keys."""
+    try:
+        with open(SHIPPED_TABLE) as f:
+            return json.load(f).get("entries", {})
+    except (OSError, ValueError):
+        return {}
+
+
 def load_cache(path: str | None = None) -> dict:
     path = path or cache_path()
     try:
@@ -113,6 +135,7 @@ def search(time_config: Callable[[dict], float], *, reps: int = 2, min_gain: flo
     """Coordinate search over SPACE with `time_config(cfg) -> seconds` (one trace). Host-only logic: the
     GPU enters through time_config, so the search itself is tested on the CPU with a model of the cost."""
     trials = []
+    time_config({})  # untimed: the first trace of a context pays for its pool and graph set-up
 
     def med(cfg):
         ts = [time_config(cfg) for _ in range(reps)]
@@ -149,24 +172,33 @@ def search(time_config: Callable[[dict], float], *, reps: int = 2, min_gain: flo
             "landscape": [{"group": g, "config": c, "relative_time": round(r, 4)} for g, c, r in landscape]}
 
 
-def tune(ctx, make_run: Callable[[int], abi.RunParams], *, key: str, photons: int, device_name: str,
-         sm_count: int, reps: int = 2, use_cache: bool = True, cache_file: str | None = None) -> dict:
+def tune(ctx, make_run: Callable[[int], abi.RunParams] | None = None, *, key: str, photons: int, device: str,
+         reps: int = 2, use_cache: bool = True, cache_file: str | None = None,
+         trace: Callable[[int], object] | None = None) -> dict:
     """Tune the engine settings of `ctx`'s current scene and leave the winner set on the context.
 
-    make_run(i) returns the run of trial i (give disjoint photon ranges); key is scene_key(...) of the
-    scene the context holds. Returns {"config", "gain", "trace_s", "default_trace_s", "trials", "cached"}."""
-    entry_key = f"{device_name}|{sm_count}|{key}|{int(photons).bit_length()}"
-    entries = load_cache(cache_file) if use_cache else {}
-    if entry_key in entries:
-        res = dict(entries[entry_key])
-        ctx.set_engine_config(res["config"] or None)
-        res["cached"] = True
-        return res
+    make_run(i) returns the run of trial i (give disjoint photon ranges), or trace(i) runs trial i itself
+    (a batch or sweep trace of the context); key is scene_key(...) of the scene the context holds, or a name
+    of a workload; device is device_key(...). A result in the user's cache, else in the package's shipped
+    table, is used without a search. Returns {"config", "gain", "trace_s", "default_trace_s", "trials",
+    "landscape", "cached": "user" | "shipped" | False}."""
+    if trace is None:
+        if make_run is None:
+            raise ValueError("tune needs make_run or trace")
+        trace = lambda i: ctx.trace(make_run(i))  # noqa: E731
+    ek = entry_key(device, key, photons)
+    if use_cache:
+        for source, entries in (("user", load_cache(cache_file)), ("shipped", load_shipped())):
+            if ek in entries:
+                res = dict(entries[ek])
+                ctx.set_engine_config(res["config"] or None)
+                res["cached"] = source
+                return res
     counter = [0]
 
     def time_config(cfg: dict) -> float:
         ctx.set_engine_config(cfg or None)
-        ctx.trace(make_run(counter[0]))
+        trace(counter[0])
         counter[0] += 1
         return ctx.last_kernel_ms() * 1e-3
 
@@ -175,8 +207,7 @@ def tune(ctx, make_run: Callable[[int], abi.RunParams], *, key: str, photons: in
     res["cached"] = False
     if use_cache:
         entries = load_cache(cache_file)
-        entries[entry_key] = {k: res[k] for k in ("config", "gain", "trace_s", "default_trace_s", "trials",
-                                                  "landscape")}
+        entries[ek] = {k: res[k] for k in ("config", "gain", "trace_s", "default_trace_s", "trials", "landscape")}
         try:
             store_cache(entries, cache_file)
         except OSError:

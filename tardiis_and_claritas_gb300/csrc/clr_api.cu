@@ -203,6 +203,8 @@ static int check_particles(clr_ctx* ctx, const clr_scene_params& sp, const clr_p
     if (hybrid_model(sp) && ps->n_theta < 257) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "n_theta must be >= 257");
     if (!ps->diameter_m || !ps->weight || !ps->n_real || !ps->k_imag)
         return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "particle arrays must not be null");
+    if (ps->table_arithmetic != CLR_TABLES_REFERENCE && ps->table_arithmetic != CLR_TABLES_FAST)
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "unknown table_arithmetic %d", ps->table_arithmetic);
     if (ss->n_radial < 65 || ss->n_quad < 64) return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "sediment lookup sizes too small");
     if (sp.sediment_model != 0) {
         if (!(ss->particle_density > ss->water_density) || !(ss->water_density > 0.0) || !(ss->water_viscosity > 0.0) ||
@@ -827,6 +829,8 @@ static int sweep_build(clr_ctx* ctx, int ns, const clr_scene_params* sps, const 
         const clr_scene_params& sp = sps[i];
         int rc = check_scene(ctx, sp);
         if (rc == CLR_OK) rc = check_particles(ctx, sp, pss + i, sss + i);
+        if (rc == CLR_OK && pss[i].table_arithmetic != pss[0].table_arithmetic)
+            rc = fail(ctx, CLR_ERR_INVALID_ARGUMENT, "every scenario of a sweep must share table_arithmetic");
         if (rc != CLR_OK) {
             ctx->err = "scenario " + std::to_string(i) + ": " + ctx->err;
             return rc;
@@ -939,7 +943,8 @@ static int sweep_build(clr_ctx* ctx, int ns, const clr_scene_params* sps, const 
         b.theta = G.theta; b.theta_f = G.theta_f;
         b.cdf = P0.phase_cdf + tab; b.cdf_f = P0.phase_cdf_f + tab; b.err = P0.err;
         CU(enqueue_mie_tables(P0.d + c.b0, P0.nidx + c.b0, P0.kidx + c.b0, (int)nb, pss[c.s0].n_medium,
-                              pss[c.s0].wavelength_m, G.nt, hybrid_model(sps[c.s0]), c.cap, b, st));
+                              pss[c.s0].wavelength_m, G.nt, hybrid_model(sps[c.s0]), c.cap, b, st,
+                              pss[c.s0].table_arithmetic == CLR_TABLES_FAST));
     }
     {
         const size_t need = scene_rates_batch_scratch(ns);

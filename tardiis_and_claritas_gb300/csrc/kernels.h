@@ -158,10 +158,11 @@ struct MiePhaseBuffers {
 cudaError_t enqueue_mie_phase(const double* d, const double* nr, const double* k, int n, double n_medium,
                               double wavelength, int nt, const MiePhaseBuffers& b, cudaStream_t stream);
 // The same for a launch whose a_n/b_n rows are `order_cap` orders apart (mie_order_bound of its bins),
-// placeholder tables instead of the phase tables when `hybrid` is false, and no reset of the error word.
+// placeholder tables instead of the phase tables when `hybrid` is false, and no reset of the error word;
+// `fast_pdf` selects the FMA, two-angle phase pdf (CLR_TABLES_FAST) over the reference's order of operations.
 cudaError_t enqueue_mie_tables(const double* d, const double* nr, const double* k, int n, double n_medium,
                                double wavelength, int nt, bool hybrid, int order_cap, const MiePhaseBuffers& b,
-                               cudaStream_t stream);
+                               cudaStream_t stream, bool fast_pdf = false);
 // Orders the Mie kernel needs for these bins (host arithmetic, with slack), at most CLR_MIE_MAX_ORDER.
 int mie_order_bound(const double* d, const double* nr, const double* k, int n, double n_medium, double wavelength);
 // Precompute error code of a Mie launch whose order bound was too small (not a reference code).

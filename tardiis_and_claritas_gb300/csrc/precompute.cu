@@ -247,6 +247,103 @@ __global__ void __launch_bounds__(128) phase_pdf_kernel(const double* __restrict
     }
 }
 
+// Production variant of the phase pdf (CLR_TABLES_FAST; no reference counterpart). The same S1/S2 sums,
+// evaluated with fused multiply-adds on coefficients premultiplied by (2n+1)/(n(n+1)) (staged per block in
+// shared memory), and for two angles at once: theta_j and theta_{nt-1-j}, which is pi - theta_j on the
+// reference's grid to rounding. With pi_n(-mu) = (-1)^(n-1) pi_n(mu) and tau_n(-mu) = (-1)^n tau_n(mu), the
+// sums over odd and over even orders of a pi_n, b tau_n, a tau_n and b pi_n give S1 and S2 at mu and at
+// -mu: 8 FMAs per (bin, order) for both angles, against about 44 FP64 operations of the reference's order
+// of operations for the two. Tables differ from the reference-order ones by rounding only (tested).
+constexpr int kPdfFastGroup = 4;    // bins per block (one Legendre recurrence per angle serves them all)
+constexpr int kPdfFastChunk = 128;  // orders staged per block
+__global__ void __launch_bounds__(128) phase_pdf_fast_kernel(const double* __restrict__ theta, int nt,
+                                                             int n_particles, int order_cap,
+                                                             const int* __restrict__ nstop,
+                                                             const double* __restrict__ ab, double* __restrict__ pdf) {
+    __shared__ double4 AB[kPdfFastGroup][kPdfFastChunk];
+    __shared__ double2 RC[kPdfFastChunk];  // (2n+1)/n, (n+1)/n of the staged orders
+    const int g0 = blockIdx.y * kPdfFastGroup;
+    const int npair = (nt + 1) / 2;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = j < npair;
+    int ns[kPdfFastGroup];
+    int kmax = 0;
+#pragma unroll
+    for (int g = 0; g < kPdfFastGroup; ++g) {
+        ns[g] = (g0 + g < n_particles) ? nstop[g0 + g] : 0;
+        kmax = ns[g] > kmax ? ns[g] : kmax;
+    }
+    const double mu = active ? cos(theta[j]) : 0.0;
+    // per bin: odd-order sums P = a pi, Q = b tau, R = a tau, T = b pi (re, im), then the even-order ones
+    double acc[kPdfFastGroup][16];
+#pragma unroll
+    for (int g = 0; g < kPdfFastGroup; ++g)
+#pragma unroll
+        for (int i = 0; i < 16; ++i) acc[g][i] = 0.0;
+    const double4* ab4 = reinterpret_cast<const double4*>(ab);
+    double pi_nm1 = 0.0, pi_n = 1.0;
+    for (int k0 = 0; k0 < kmax; k0 += kPdfFastChunk) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < kPdfFastGroup * kPdfFastChunk; idx += blockDim.x) {
+            const int g = idx / kPdfFastChunk, kk = idx % kPdfFastChunk, k = k0 + kk;
+            double4 v = make_double4(0.0, 0.0, 0.0, 0.0);
+            if (k < ns[g]) {
+                const double4 q = ab4[(size_t)(g0 + g) * order_cap + k];
+                const double nf = (double)(k + 1);
+                const double c = (2.0 * nf + 1.0) / (nf * (nf + 1.0));
+                v = make_double4(c * q.x, c * q.y, c * q.z, c * q.w);
+            }
+            AB[g][kk] = v;
+        }
+        for (int kk = threadIdx.x; kk < kPdfFastChunk; kk += blockDim.x) {
+            const double nf = (double)(k0 + kk + 1);
+            RC[kk] = make_double2((2.0 * nf + 1.0) / nf, (nf + 1.0) / nf);
+        }
+        __syncthreads();
+        const int kend = min(kPdfFastChunk, kmax - k0);
+        // k0 is even, so order n = k0 + kk + 1 is odd for even kk: odd-order sums go to acc[g][0..7], even-order
+        // ones to acc[g][8..15]; the pair loop keeps every index a compile-time constant (registers, no stack).
+        // Orders past kend carry zero coefficients, so the pair's second half may run past it.
+        for (int kk = 0; kk < kend; kk += 2) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const double nf = (double)(k0 + kk + h + 1);
+                const double tau = fma(nf * mu, pi_n, -(nf + 1.0) * pi_nm1);
+#pragma unroll
+                for (int g = 0; g < kPdfFastGroup; ++g) {
+                    const double4 q = AB[g][kk + h];
+                    double* A = acc[g] + 8 * h;
+                    A[0] = fma(q.x, pi_n, A[0]); A[1] = fma(q.y, pi_n, A[1]);  // P
+                    A[2] = fma(q.z, tau, A[2]);  A[3] = fma(q.w, tau, A[3]);   // Q
+                    A[4] = fma(q.x, tau, A[4]);  A[5] = fma(q.y, tau, A[5]);   // R
+                    A[6] = fma(q.z, pi_n, A[6]); A[7] = fma(q.w, pi_n, A[7]);  // T
+                }
+                const double2 rc = RC[kk + h];
+                const double pi_np1 = fma(rc.x * mu, pi_n, -rc.y * pi_nm1);
+                pi_nm1 = pi_n; pi_n = pi_np1;
+            }
+        }
+    }
+    if (!active) return;
+    const int jm = nt - 1 - j;
+    const double sj = sin(theta[j]), sm = sin(theta[jm]);
+#pragma unroll
+    for (int g = 0; g < kPdfFastGroup; ++g) {
+        if (g0 + g >= n_particles) continue;
+        const double* o = acc[g];
+        const double* e = acc[g] + 8;
+        // S1(mu) = Po+Qo+Pe+Qe, S1(-mu) = Po-Qo-Pe+Qe, S2(mu) = Ro+To+Re+Te, S2(-mu) = -Ro+To+Re-Te
+        const double s1r = o[0] + o[2] + e[0] + e[2], s1i = o[1] + o[3] + e[1] + e[3];
+        const double s2r = o[4] + o[6] + e[4] + e[6], s2i = o[5] + o[7] + e[5] + e[7];
+        pdf[(size_t)(g0 + g) * nt + j] = 0.5 * (s1r * s1r + s1i * s1i + s2r * s2r + s2i * s2i) * sj;
+        if (jm != j) {
+            const double m1r = o[0] - o[2] - e[0] + e[2], m1i = o[1] - o[3] - e[1] + e[3];
+            const double m2r = -o[4] + o[6] + e[4] - e[6], m2i = -o[5] + o[7] + e[5] - e[7];
+            pdf[(size_t)(g0 + g) * nt + jm] = 0.5 * (m1r * m1r + m1i * m1i + m2r * m2r + m2i * m2i) * sm;
+        }
+    }
+}
+
 // Trapezoid CDF per bin, normalised and forced monotone (:3583-3592); also the float copy. One warp per
 // bin: the trapezoid areas and the normalised values are independent per angle and spread over the
 // lanes; the prefix sum and the monotone clamp stay serial on lane 0, so every value is the serial one.
@@ -1046,7 +1143,7 @@ static cudaError_t set_table_attributes() {
 // `b.pdf` n * nt values. The error word is not reset here.
 cudaError_t enqueue_mie_tables(const double* d, const double* nr, const double* k, int n, double n_medium,
                                double wavelength, int nt, bool hybrid, int order_cap, const MiePhaseBuffers& b,
-                               cudaStream_t st) {
+                               cudaStream_t st, bool fast_pdf) {
     cudaError_t e = set_table_attributes();
     if (e != cudaSuccess) return e;
     mie_coefficients_kernel<<<n, 32, mie_smem_bytes(order_cap), st>>>(d, nr, k, n_medium, wavelength, n, order_cap,
@@ -1054,9 +1151,14 @@ cudaError_t enqueue_mie_tables(const double* d, const double* nr, const double* 
                                                                       b.qback, b.g, b.albedo, b.err);
     if (hybrid) {
         theta_grid_kernel<<<(nt + 127) / 128, 128, 0, st>>>(b.theta, b.theta_f, nt);
-        dim3 grid((nt + 127) / 128, (n + PDF_GROUP - 1) / PDF_GROUP);
-        phase_pdf_kernel<<<grid, 128, pdf_smem_bytes(order_cap), st>>>(b.theta, nt, n, order_cap, b.nstop, b.ab,
-                                                                        b.pdf);
+        if (fast_pdf) {
+            dim3 grid(((nt + 1) / 2 + 127) / 128, (n + kPdfFastGroup - 1) / kPdfFastGroup);
+            phase_pdf_fast_kernel<<<grid, 128, 0, st>>>(b.theta, nt, n, order_cap, b.nstop, b.ab, b.pdf);
+        } else {
+            dim3 grid((nt + 127) / 128, (n + PDF_GROUP - 1) / PDF_GROUP);
+            phase_pdf_kernel<<<grid, 128, pdf_smem_bytes(order_cap), st>>>(b.theta, nt, n, order_cap, b.nstop,
+                                                                            b.ab, b.pdf);
+        }
         phase_cdf_kernel<<<n, 32, 0, st>>>(b.theta, b.pdf, nt, n, b.cdf, b.cdf_f, b.err);
     } else {
         dummy_phase_kernel<<<(n + 127) / 128, 128, 0, st>>>(b.theta, b.theta_f, b.cdf, b.cdf_f, n);
@@ -1191,7 +1293,8 @@ cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_par
     b.cdf = pb.phase_cdf; b.cdf_f = pb.phase_cdf_f; b.err = pb.err;
     const int em = sp.event_model;
     e = enqueue_mie_tables(pb.d, pb.nidx, pb.kidx, pb.n, ps.n_medium, ps.wavelength_m, pb.nt,
-                           em == 3 || em == 4 || em == 5, CLR_MIE_MAX_ORDER, b, st);
+                           em == 3 || em == 4 || em == 5, CLR_MIE_MAX_ORDER, b, st,
+                           ps.table_arithmetic == CLR_TABLES_FAST);
     if (e != cudaSuccess) return e;
     return enqueue_scene_rates(pb, sp, ps, ss, st);
 }

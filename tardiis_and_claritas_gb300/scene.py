@@ -473,8 +473,10 @@ class Particles:
         if not np.isfinite(c) or c < 0.0:
             raise ValueError("concentration must be finite and >=0")
 
-    def spec(self, cfg: ModelConfig, moments: Optional[dict] = None) -> abi.ParticleSpec:
+    def spec(self, cfg: ModelConfig, moments: Optional[dict] = None,
+             table_arithmetic: int = abi.TABLES_REFERENCE) -> abi.ParticleSpec:
         ps = abi.ParticleSpec()
+        ps.table_arithmetic = int(table_arithmetic)
         ps.n_bins = int(self.diameter_m.size)
         hybrid = cfg.particle_event_model in ("hybrid_mie_excess", "hybrid_mie_exact_rate",
                                               "hybrid_mie_exact_rate_moment_constrained")
@@ -748,10 +750,10 @@ def sweep_workload(n_scenarios: int = 512, sampler_seed: int = 0, n_bins: int = 
     return out
 
 
-def sweep_specs(scenarios: list) -> tuple[list, list, list]:
+def sweep_specs(scenarios: list, table_arithmetic: int = abi.TABLES_REFERENCE) -> tuple[list, list, list]:
     """ABI inputs of a sweep: (scene params, particle specs, sediment specs), one each per scenario."""
     scenes = [sc.cfg.to_scene_params() for sc in scenarios]
-    parts = [sc.particles.spec(sc.cfg) for sc in scenarios]
+    parts = [sc.particles.spec(sc.cfg, table_arithmetic=table_arithmetic) for sc in scenarios]
     seds = [sc.cfg.sediment_spec() for sc in scenarios]
     return scenes, parts, seds
 

@@ -82,14 +82,14 @@ def test_tune_caches_by_device_and_scene(tmp_path):
     cache = str(tmp_path / "t.json")
     ctx = _FakeCtx(_model({"flight_steps": 8}, 0.0, 3))
     mk = lambda i: S.run_params(10, seed=i)  # noqa: E731
-    res = AT.tune(ctx, mk, key=key, photons=10_000, device_name="gpu-a", sm_count=152, cache_file=cache)
+    res = AT.tune(ctx, mk, key=key, photons=10_000, device="sm103x152", cache_file=cache)
     assert res["config"] == {"flight_steps": 8} and not res["cached"]
     assert ctx.set_calls[-1] == {"flight_steps": 8}
     n_trials = len(ctx.set_calls)
-    res2 = AT.tune(ctx, mk, key=key, photons=12_000, device_name="gpu-a", sm_count=152, cache_file=cache)
-    assert res2["cached"] and len(ctx.set_calls) == n_trials + 1
+    res2 = AT.tune(ctx, mk, key=key, photons=12_000, device="sm103x152", cache_file=cache)
+    assert res2["cached"] == "user" and len(ctx.set_calls) == n_trials + 1
     # another GPU or another scene is tuned afresh
-    res3 = AT.tune(ctx, mk, key=key, photons=10_000, device_name="gpu-b", sm_count=152, cache_file=cache)
+    res3 = AT.tune(ctx, mk, key=key, photons=10_000, device="sm100x148", cache_file=cache)
     assert not res3["cached"]
     cfg2 = S.small_cell_config()
     assert AT.scene_key(cfg2.to_scene_params(), ps, ss) != key
@@ -101,3 +101,25 @@ def test_tune_caches_by_device_and_scene(tmp_path):
     assert AT.scene_key(sp, ps2, ss) == key
     d[0] *= 1.01
     assert AT.scene_key(sp, ps2, ss) != key
+
+
+def test_shipped_table_is_valid_and_used(tmp_path, monkeypatch):
+    entries = AT.load_shipped()
+    assert entries, "the package ships tuned settings"
+    for k, e in entries.items():
+        dev, work, bits = k.split("|")
+        assert dev.startswith("sm") and int(bits) > 0 and work
+        c = abi.EngineConfig.from_dict(e["config"])
+        assert 0 <= c.flight_steps <= 64 and 0 <= c.pass_batch <= 64 and all(0 <= b <= 32 for b in c.stage_blocks)
+        assert e["trace_s"] <= e["default_trace_s"]
+    key = next(iter(entries))
+    dev, work, bits = key.split("|")
+    ctx = _FakeCtx(_model({}, 0.0, 5))
+    res = AT.tune(ctx, lambda i: S.run_params(10, seed=i), key=work, photons=(1 << (int(bits) - 1)), device=dev,
+                  cache_file=str(tmp_path / "empty.json"))
+    assert res["cached"] == "shipped" and ctx.set_calls == [entries[key]["config"] or None]
+    # without the shipped table the same call searches
+    monkeypatch.setattr(AT, "SHIPPED_TABLE", str(tmp_path / "none.json"))
+    res = AT.tune(ctx, lambda i: S.run_params(10, seed=i), key=work, photons=(1 << (int(bits) - 1)), device=dev,
+                  cache_file=str(tmp_path / "empty2.json"))
+    assert res["cached"] is False and res["trials"] > 10

@@ -120,13 +120,13 @@ def test_tuner_picks_a_setting_and_leaves_it_set(ctx, tmp_path):
     n = 4_000_000
     mk = lambda i: S.run_params(n, seed=5, ray_offset=i * n, rng_mode=abi.RNG_PHILOX)  # noqa: E731
     cache = str(tmp_path / "tune.json")
-    res = AT.tune(ctx, mk, key=AT.scene_key(sp, ps, ss), photons=n, device_name="test", sm_count=1, reps=1,
+    res = AT.tune(ctx, mk, key=AT.scene_key(sp, ps, ss), photons=n, device="test", reps=1,
                   cache_file=cache)
     assert res["cached"] is False and res["trials"] > 10
     assert res["trace_s"] <= res["default_trace_s"] * 1.0001
-    again = AT.tune(ctx, mk, key=AT.scene_key(sp, ps, ss), photons=n, device_name="test", sm_count=1,
+    again = AT.tune(ctx, mk, key=AT.scene_key(sp, ps, ss), photons=n, device="test",
                     cache_file=cache)
-    assert again["cached"] is True and again["config"] == res["config"]
+    assert again["cached"] == "user" and again["config"] == res["config"]
     # the tuned context gives the default's tallies (up to contraction rounding, as above)
     run = S.run_params(500_000, seed=9, rng_mode=abi.RNG_PHILOX)
     tuned, _ = ctx.trace(run)
