@@ -348,6 +348,9 @@ def summary_dict(material: str, concentration: float, wavelength_nm: float, seed
         "single_scattering_albedo": mu_sca / mu_ext if mu_ext > 0 else None,
         "optical_depth_diameter": float(res.optical_depth_diameter),
         "geometric_optical_depth_diameter": float(res.geometric_optical_depth_diameter),
+        # the reference's batch driver runs a steady-state transport model exactly when its sediment
+        # distribution is "steady_state" (_resolved_sediment_config, :10080-10090)
+        "sediment_distribution": "steady_state" if cfg.sediment_transport_model != "uniform" else "uniform",
         "sediment_transport_model": res.sediment_transport_model,
         "steady_state_sediment_enabled": cfg.sediment_transport_model != "uniform",
         "sediment_eddy_diffusivity_m2_s": float(res.sediment_eddy_diffusivity_m2_s),
