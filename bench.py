@@ -264,11 +264,25 @@ def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> di
     t0 = time.perf_counter()
     train = G.make_dataset(ctx, args.sur_train, args.sur_photons, sampler_seed=1000 + rank, seed_base=0)
     test = G.make_dataset(ctx, args.sur_test, 100 * args.sur_photons, sampler_seed=2000 + rank, seed_base=10 ** 6)
+    # the precision judge: few held-out scenarios at many photons, so that the judge's own noise is a small
+    # part of the measured difference (a few scenarios per engine execution keeps each trace bounded)
+    judge = G.make_dataset(ctx, args.sur_judge, int(args.sur_judge_photons), sampler_seed=4000 + rank,
+                           seed_base=2 * 10 ** 6, chunk=8) if args.sur_judge > 0 else None
     data_s = time.perf_counter() - t0
     model = G.Surrogate(local_rank, max_batch=65536, seed=rank)
     hist = model.fit(train, epochs=args.sur_epochs, batch=2048)
     err = G.mc_error(model, test)
     base = G.linear_baseline(train, test)
+    judged = {"held_out_at_100x_photons": G.judged_error(model, test)}
+    if judge is not None:
+        judged["precision_judge"] = G.judged_error(model, judge)
+    # the same network trained with 1/(noise variance + floor^2) label weights, for comparison
+    model_u = G.Surrogate(local_rank, max_batch=65536, seed=rank)
+    model_u.fit(train, epochs=args.sur_epochs, batch=2048, weight_floor=G.WEIGHT_FLOOR_REL)
+    judged_u = {"held_out_at_100x_photons": G.judged_error(model_u, test)}
+    if judge is not None:
+        judged_u["precision_judge"] = G.judged_error(model_u, judge)
+    model_u.close()
     # surrogate-in-the-loop inversion of concentration (Monte Carlo as check and fallback)
     inv = G.inversion_study(ctx, model, n=args.inv_scenarios, photons=4_000_000, mc_only=args.inv_mc_only,
                             sampler_seed=3000 + rank) if args.inv_scenarios > 0 else None
@@ -308,7 +322,8 @@ def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> di
             "config": {"workload": "surrogate MLP 6-256x4(SiLU)-3 of the sweep's detector signals (channels 9, 0, 17); "
                                    f"trained on {args.sur_train} sweep scenarios at {args.sur_photons:.0e} photons, "
                                    f"checked on {args.sur_test} held-out scenarios at {100 * args.sur_photons:.0e} "
-                                   "photons; inference batch 65536",
+                                   f"photons and {args.sur_judge} at {args.sur_judge_photons:.0e}; inference batch "
+                                   "65536",
                        "inference_batch": batch, "l2": "inputs resident (3 MB); weights L2-resident by design"},
             "e2e": {"value": speed["e2e_queries_per_s"] * world, "unit": "queries/s",
                     "h2d_bytes_per_step": batch * 6 * 4, "d2h_bytes_per_step": batch * 3 * 4},
@@ -316,9 +331,14 @@ def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> di
             "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                          "peak_source": "bf16_tflops of MEASURED_PEAKS.json" if peaks.get("bf16_tflops") else "fallback",
                          "traffic": None, "flop_per_query": flop_q},
-            "surrogate": {"vs_mc": err, "linear_baseline": base,
+            "surrogate": {"vs_mc": err, "judged": judged,
+                          "weighted_loss": {"weight_floor": G.WEIGHT_FLOOR_REL, "judged": judged_u},
+                          "judge": {"scenarios": args.sur_judge, "photons_each": int(args.sur_judge_photons)},
+                          "linear_baseline": base,
                           "train": {"scenarios": len(train.x), "photons_each": args.sur_photons,
                                     "epochs": args.sur_epochs, "final_loss": hist[-1][2],
+                                    "kept_epoch": model.best_epoch, "validation_share": 0.05,
+                                    "loss": "unweighted mean squared error of the standardised log10 signals",
                                     "train_seconds": model.train_seconds,
                                     "ms_per_epoch": float(np.median([h[3] for h in hist]))},
                           "mc": {"data_seconds_wall": data_s, "train_labels_device_s_per_scenario": mc_s_per_scen,
@@ -583,8 +603,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["full", "small", "sweep", "surrogate"], default="full")
-    ap.add_argument("--sur-train", type=int, default=16384, help="surrogate: training scenarios")
+    ap.add_argument("--sur-train", type=int, default=262144, help="surrogate: training scenarios")
     ap.add_argument("--sur-test", type=int, default=256, help="surrogate: held-out scenarios checked by Monte Carlo")
+    ap.add_argument("--sur-judge", type=int, default=64, help="surrogate: held-out scenarios of the precision judge")
+    ap.add_argument("--sur-judge-photons", type=float, default=2e9,
+                    help="surrogate: photons per scenario of the precision judge")
     ap.add_argument("--sur-photons", type=int, default=1_000_000, help="surrogate: photons per training scenario")
     ap.add_argument("--sur-epochs", type=int, default=400, help="surrogate: training epochs")
     ap.add_argument("--inv-scenarios", type=int, default=1024, help="surrogate: scenarios of the inversion study")

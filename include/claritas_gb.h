@@ -595,6 +595,10 @@ int clr_mlp_gradients(clr_mlp* net, const float* d_x, const float* d_t, int64_t 
  * graph launch. mean_loss: the mean batch loss of the call. */
 int clr_mlp_train(clr_mlp* net, const float* d_x, const float* d_t, const int32_t* d_index, int64_t n_index,
                   int batch, float lr, float* mean_loss);
+/* Per-output loss weights for the following clr_mlp_gradients / clr_mlp_train calls: d_w[row][3] on the
+ * device, rows indexed like their d_t (the caller keeps it alive); NULL returns to the unweighted loss.
+ * The loss becomes sum w (y - t)^2 / (3 n); weights of 1/variance give each label its likelihood weight. */
+int clr_mlp_set_loss_weights(clr_mlp* net, const float* d_w);
 /* Device time of the last clr_mlp_forward / clr_mlp_train call (CUDA events on its stream), ms. */
 int clr_mlp_last_ms(const clr_mlp* net, float* ms);
 /* C[M][256] = A[M][K] . B[256][K]^T on the tensor cores: BF16 row-major operands (K a multiple of

@@ -71,15 +71,17 @@ def forward(params, x, bf16_round: bool = True):
         cache["h"].append(h)
 
 
-def loss_and_grad(params, x, t, bf16_round: bool = True):
-    """Mean squared error over the n x 3 outputs and its gradient (flat, like the parameters)."""
+def loss_and_grad(params, x, t, bf16_round: bool = True, w=None):
+    """(Weighted) mean squared error over the n x 3 outputs, sum w e^2 / (3 n), and its gradient (flat, like
+    the parameters); w = None is the unweighted loss."""
     R = bf16 if bf16_round else (lambda a: np.asarray(a, dtype=np.float64))
     L = unpack(params)
     y, c = forward(params, x, bf16_round)
     n = x.shape[0]
     e = y - t
-    loss = float(np.mean(e * e))
-    d = 2.0 * e / (3.0 * n)  # dL/dy
+    we = e if w is None else np.asarray(w, dtype=np.float64) * e
+    loss = float(np.mean(we * e))
+    d = 2.0 * we / (3.0 * n)  # dL/dy
     grads = [None] * len(L)
     for li in range(len(L) - 1, -1, -1):
         W, _ = L[li]

@@ -311,8 +311,10 @@ static cudaError_t launch_gemm(const GemmArgs& g, int grid_y, cudaStream_t st) {
 __device__ __forceinline__ float bfr(float x) { return __bfloat162float(__float2bfloat16(x)); }
 
 // rows of the batch by index (training) or copied (inference: idx null)
-__global__ void gather_kernel(const float* __restrict__ x, const float* __restrict__ t, const int32_t* __restrict__ idx,
-                              long long row0, int n, float* xb, float* tb) {
+// (w: per-output loss weights of the rows, nullable)
+__global__ void gather_kernel(const float* __restrict__ x, const float* __restrict__ t, const float* __restrict__ w,
+                              const int32_t* __restrict__ idx, long long row0, int n, float* xb, float* tb,
+                              float* wb) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const long long src = idx ? (long long)idx[row0 + r] : row0 + r;
@@ -321,6 +323,9 @@ __global__ void gather_kernel(const float* __restrict__ x, const float* __restri
     if (t && tb)
 #pragma unroll
         for (int i = 0; i < kOut; ++i) tb[r * kOut + i] = t[src * kOut + i];
+    if (w && wb)
+#pragma unroll
+        for (int i = 0; i < kOut; ++i) wb[r * kOut + i] = w[src * kOut + i];
 }
 
 // layer 1 (6 -> 256): one thread per (row, unit)
@@ -338,11 +343,13 @@ __global__ void layer1_kernel(const float* __restrict__ xb, int n, const bf16* _
     if (h1t) h1t[(long long)j * ldt + r] = h;
 }
 
-// Output layer (256 -> 3), one warp per row; with targets also the loss, dy = dL/dy and the gradient
-// through the output layer into the last hidden layer (dz4 = (dy . W5) * silu'(z4)).
+// Output layer (256 -> 3), one warp per row; with targets also the loss L = sum w (y - t)^2 / (3 n) (w = 1
+// without weights), dy = dL/dy and the gradient through the output layer into the last hidden layer
+// (dz4 = (dy . W5) * silu'(z4)).
 __global__ void head_kernel(const bf16* __restrict__ h4, const float* __restrict__ z4, int n,
                             const bf16* __restrict__ w5, const float* __restrict__ b5, const float* __restrict__ tb,
-                            float* y, float* dy, bf16* dz4, bf16* dz4t, long long ldt, float* loss_sum) {
+                            const float* __restrict__ wb, float* y, float* dy, bf16* dz4, bf16* dz4t, long long ldt,
+                            float* loss_sum) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= n) return;
     const int r = warp;
@@ -368,8 +375,9 @@ __global__ void head_kernel(const bf16* __restrict__ h4, const float* __restrict
 #pragma unroll
     for (int k = 0; k < kOut; ++k) {
         const float e = yv[k] - tb[r * kOut + k];
-        d[k] = scale * e;
-        l += e * e;
+        const float we = wb ? wb[r * kOut + k] * e : e;
+        d[k] = scale * we;
+        l += we * e;
     }
     if (lane == 0) {
 #pragma unroll
@@ -710,6 +718,8 @@ struct clr_mlp {
     bf16* dzt[5] = {};         // [256][cap]
     const bf16** d_dzt = nullptr;  // device array of dzt[1..4]
     float *xb = nullptr, *tb = nullptr, *dy = nullptr, *y = nullptr, *loss = nullptr;
+    float* wb = nullptr;          // [cap][3] loss weights of the batch rows
+    const float* d_w = nullptr;   // the caller's loss weights (clr_mlp_set_loss_weights), or null
     int* d_err = nullptr;
     long long steps = 0;
     float last_ms = 0.0f;
@@ -720,6 +730,7 @@ struct clr_mlp {
     const float* step_x = nullptr;
     const float* step_t = nullptr;
     const int32_t* step_idx = nullptr;
+    const float* step_w = nullptr;
     long long* d_row0 = nullptr;  // device copy of the batch's first index position (graph input)
     float* d_lr = nullptr;        // device scalars of the captured Adam step: lr, c1, c2
 };
@@ -768,6 +779,7 @@ static cudaError_t forward_rows(clr_mlp* m, int n, bool train, cudaStream_t st) 
 // Backward pass of the n rows of the last forward (targets in tb): gradients accumulate into grads.
 static cudaError_t backward_rows(clr_mlp* m, int n, cudaStream_t st) {
     head_kernel<<<(n * 32 + 255) / 256, 256, 0, st>>>(m->h[4], m->z[4], n, m->pa.w[5], m->params + kOffB5, m->tb,
+                                                      m->d_w ? m->wb : nullptr,
                                                       m->y, m->dy, m->dz[4], m->dzt[4], m->cap, m->loss);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -840,7 +852,7 @@ int clr_mlp_create(clr_mlp** out, int device, int max_batch, uint64_t seed) {
         MCU(F(&m->z[l], act)); MCU(H(&m->h[l], act)); MCU(H(&m->ht[l], act));
         MCU(H(&m->dz[l], act)); MCU(H(&m->dzt[l], act));
     }
-    MCU(F(&m->xb, (size_t)m->cap * kIn)); MCU(F(&m->tb, (size_t)m->cap * kOut));
+    MCU(F(&m->xb, (size_t)m->cap * kIn)); MCU(F(&m->tb, (size_t)m->cap * kOut)); MCU(F(&m->wb, (size_t)m->cap * kOut));
     MCU(F(&m->dy, (size_t)m->cap * kOut)); MCU(F(&m->y, (size_t)m->cap * kOut)); MCU(F(&m->loss, 4));
     MCU(malloc_tracked(m, (void**)&m->d_err, sizeof(int)));
     MCU(malloc_tracked(m, (void**)&m->d_dzt, 4 * sizeof(bf16*)));
@@ -935,7 +947,7 @@ int clr_mlp_gradients(clr_mlp* m, const float* d_x, const float* d_t, int64_t n,
     cudaStream_t st = m->stream;
     MCU(cudaMemsetAsync(m->grads, 0, kParams * sizeof(float), st));
     MCU(cudaMemsetAsync(m->loss, 0, sizeof(float), st));
-    gather_kernel<<<((int)n + 255) / 256, 256, 0, st>>>(d_x, d_t, nullptr, 0, (int)n, m->xb, m->tb);
+    gather_kernel<<<((int)n + 255) / 256, 256, 0, st>>>(d_x, d_t, m->d_w, nullptr, 0, (int)n, m->xb, m->tb, m->wb);
     MCU(cudaGetLastError());
     MCU(forward_rows(m, (int)n, true, st));
     MCU(backward_rows(m, (int)n, st));
@@ -954,8 +966,8 @@ int clr_mlp_gradients(clr_mlp* m, const float* d_x, const float* d_t, int64_t n,
 // Gathers batch rows by index, with the batch start read from device memory so the captured step
 // serves every batch of an epoch.
 __global__ void gather_dev_kernel(const float* __restrict__ x, const float* __restrict__ t,
-                                  const int32_t* __restrict__ idx, const long long* __restrict__ row0, int n,
-                                  float* xb, float* tb) {
+                                  const float* __restrict__ w, const int32_t* __restrict__ idx,
+                                  const long long* __restrict__ row0, int n, float* xb, float* tb, float* wb) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const long long src = (long long)idx[*row0 + r];
@@ -963,6 +975,9 @@ __global__ void gather_dev_kernel(const float* __restrict__ x, const float* __re
     for (int i = 0; i < kIn; ++i) xb[r * kIn + i] = bfr(x[src * kIn + i]);
 #pragma unroll
     for (int i = 0; i < kOut; ++i) tb[r * kOut + i] = t[src * kOut + i];
+    if (w)
+#pragma unroll
+        for (int i = 0; i < kOut; ++i) wb[r * kOut + i] = w[src * kOut + i];
 }
 
 __global__ void adam_dev_kernel(float* params, float* grads, float* m1, float* m2, const float* __restrict__ hp,
@@ -983,7 +998,8 @@ __global__ void adam_dev_kernel(float* params, float* grads, float* m1, float* m
 
 // One training step (gather, forward, backward, Adam) captured as a graph for batch size n.
 static int build_step_graph(clr_mlp* m, const float* d_x, const float* d_t, const int32_t* d_idx, int n) {
-    if (m->step_exec && m->step_n == n && m->step_x == d_x && m->step_t == d_t && m->step_idx == d_idx)
+    if (m->step_exec && m->step_n == n && m->step_x == d_x && m->step_t == d_t && m->step_idx == d_idx &&
+        m->step_w == m->d_w)
         return CLR_OK;
     if (m->step_exec) {
         cudaGraphExecDestroy(m->step_exec);
@@ -992,7 +1008,7 @@ static int build_step_graph(clr_mlp* m, const float* d_x, const float* d_t, cons
     cudaStream_t st = m->stream;
     cudaGraph_t graph;
     MCU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    gather_dev_kernel<<<(n + 255) / 256, 256, 0, st>>>(d_x, d_t, d_idx, m->d_row0, n, m->xb, m->tb);
+    gather_dev_kernel<<<(n + 255) / 256, 256, 0, st>>>(d_x, d_t, m->d_w, d_idx, m->d_row0, n, m->xb, m->tb, m->wb);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = forward_rows(m, n, true, st);
     if (e == cudaSuccess) e = backward_rows(m, n, st);
@@ -1007,7 +1023,7 @@ static int build_step_graph(clr_mlp* m, const float* d_x, const float* d_t, cons
     e = cudaGraphInstantiate(&m->step_exec, graph, 0);
     cudaGraphDestroy(graph);
     MCU(e);
-    m->step_n = n; m->step_x = d_x; m->step_t = d_t; m->step_idx = d_idx;
+    m->step_n = n; m->step_x = d_x; m->step_t = d_t; m->step_idx = d_idx; m->step_w = m->d_w;
     return CLR_OK;
 }
 
@@ -1039,6 +1055,12 @@ extern "C" int clr_mlp_train(clr_mlp* m, const float* d_x, const float* d_t, con
     if (rc != CLR_OK) return rc;
     MCU(cudaEventElapsedTime(&m->last_ms, m->ev0, m->ev1));
     if (mean_loss) *mean_loss = steps > 0 ? ls / (3.0f * (float)batch * (float)steps) : 0.0f;
+    return CLR_OK;
+}
+
+extern "C" int clr_mlp_set_loss_weights(clr_mlp* m, const float* d_w) {
+    if (!m) return CLR_ERR_INVALID_ARGUMENT;
+    m->d_w = d_w;
     return CLR_OK;
 }
 

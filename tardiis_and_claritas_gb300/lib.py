@@ -74,6 +74,7 @@ def load(build_if_missing: bool = False):
             "clr_mlp_train": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_float,
                                P(C.c_float)], C.c_int),
             "clr_mlp_last_ms": ([C.c_void_p, P(C.c_float)], C.c_int),
+            "clr_mlp_set_loss_weights": ([C.c_void_p, C.c_void_p], C.c_int),
             "clr_bf16_gemm_n256": ([C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p,
                                     C.c_int64, C.c_void_p], C.c_int),
             "clr_read_sediment_field": ([C.c_void_p, C.c_void_p, P(C.c_int32), P(C.c_int32), P(C.c_int32),
@@ -99,7 +100,7 @@ def exported_symbols() -> list[str]:
             "clr_mie_phase_noalloc", "clr_sweep_build",
             "clr_sweep_trace", "clr_sweep_read_particle_physics", "clr_mlp_create", "clr_mlp_destroy",
             "clr_mlp_last_error", "clr_mlp_set_params", "clr_mlp_get_params", "clr_mlp_forward", "clr_mlp_gradients",
-            "clr_mlp_train", "clr_mlp_last_ms", "clr_bf16_gemm_n256", "clr_read_sediment_field",
+            "clr_mlp_train", "clr_mlp_set_loss_weights", "clr_mlp_last_ms", "clr_bf16_gemm_n256", "clr_read_sediment_field",
             "clr_set_light_diagnostics", "clr_read_light_diagnostics", "clr_set_path_provenance",
             "clr_read_path_provenance", "clr_read_path_provenance_records"]
 
@@ -383,6 +384,11 @@ class Network:
         self._check(self.lib.clr_mlp_train(self.h, C.c_void_p(x_ptr), C.c_void_p(t_ptr), C.c_void_p(idx_ptr),
                                            int(n_index), int(batch), float(lr), C.byref(loss)), "clr_mlp_train")
         return float(loss.value)
+
+    def set_loss_weights(self, w_ptr: int):
+        """Per-output loss weights [rows][3] on the device for the following gradients/train calls (0: none)."""
+        self._check(self.lib.clr_mlp_set_loss_weights(self.h, C.c_void_p(w_ptr) if w_ptr else None),
+                    "clr_mlp_set_loss_weights")
 
     def last_ms(self) -> float:
         v = C.c_float()

@@ -81,6 +81,31 @@ def test_forward_and_gradients_match_the_oracle(torch_cuda):
     net.close()
 
 
+def test_weighted_gradients_match_the_oracle(torch_cuda):
+    """clr_mlp_set_loss_weights: the loss sum w (y-t)^2 / (3n) and its gradients, against the numpy oracle."""
+    torch = torch_cuda
+    from tardiis_and_claritas_gb300 import lib as L
+    net = L.Network(0, max_batch=1024, seed=1)
+    p = M.init_params(9)
+    net.set_params(p)
+    x, t = _data(512, 6)
+    w = np.random.default_rng(3).uniform(0.0, 4.0, size=(512, 3)).astype(np.float32)
+    w[::7] = 0.0  # rows that do not count
+    xd, td, wd = (torch.from_numpy(a).cuda() for a in (x, t, w))
+    net.set_loss_weights(wd.data_ptr())
+    loss, g = net.gradients(xd.data_ptr(), td.data_ptr(), 512)
+    loss_or, g_or = M.loss_and_grad(p, x, t, w=w)
+    assert abs(loss - loss_or) < 1e-3 * loss_or
+    a, b = g.astype(np.float64), g_or
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 2e-2
+    assert float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b))) > 0.9998
+    # unset: back to the unweighted loss
+    net.set_loss_weights(0)
+    loss_u, _ = net.gradients(xd.data_ptr(), td.data_ptr(), 512)
+    assert abs(loss_u - M.loss_and_grad(p, x, t)[0]) < 1e-3 * loss_u
+    net.close()
+
+
 def test_training_reduces_the_loss(torch_cuda):
     torch = torch_cuda
     from tardiis_and_claritas_gb300 import lib as L

@@ -5,6 +5,7 @@ import os
 import sys
 
 import numpy as np
+import pytest
 
 sys.path.insert(0, os.path.join(os.path.dirname(__file__), "..", "oracle"))
 import mlp_reference as M  # noqa: E402
@@ -28,12 +29,14 @@ def test_bf16_rounding_is_nearest_even():
     assert abs(r[6] - 3.140625) < 1e-12
 
 
-def test_oracle_gradient_matches_finite_differences():
+@pytest.mark.parametrize("weighted", [False, True])
+def test_oracle_gradient_matches_finite_differences(weighted):
     rng = np.random.default_rng(3)
     p = M.init_params(5).astype(np.float64)
     x = rng.normal(size=(16, 6))
     t = rng.normal(size=(16, 3))
-    loss, g = M.loss_and_grad(p, x, t, bf16_round=False)
+    w = rng.uniform(0.0, 3.0, size=(16, 3)) if weighted else None
+    loss, g = M.loss_and_grad(p, x, t, bf16_round=False, w=w)
     probe = np.concatenate([rng.choice(np.arange(0, 1536), 6), rng.choice(np.arange(1536, 1792), 3),
                             rng.choice(np.arange(1792, 67328), 8), rng.choice(np.arange(198912, M.N_PARAMS), 8)])
     eps = 1e-6
@@ -41,6 +44,6 @@ def test_oracle_gradient_matches_finite_differences():
         pp, pm = p.copy(), p.copy()
         pp[k] += eps
         pm[k] -= eps
-        fd = (M.loss_and_grad(pp, x, t, False)[0] - M.loss_and_grad(pm, x, t, False)[0]) / (2 * eps)
+        fd = (M.loss_and_grad(pp, x, t, False, w)[0] - M.loss_and_grad(pm, x, t, False, w)[0]) / (2 * eps)
         assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(fd)) + 1e-9, (k, fd, g[k])
     assert loss > 0
