@@ -507,6 +507,8 @@ int clr_last_launches(const clr_ctx* ctx, int64_t* launches, int64_t* passes);
 #define CLR_ENGINE_DEFAULT_TAIL_PHOTONS 65536
 #define CLR_ENGINE_DEFAULT_RARE_BATCH 8192
 #define CLR_ENGINE_DEFAULT_PASS_BATCH 8
+#define CLR_ENGINE_DEFAULT_ACR_BUDGET 256
+#define CLR_ENGINE_ACR_BUDGET_STEP 64
 #define CLR_N_STAGES 11
 typedef struct clr_engine_config {
     int32_t flight_steps;           /* water flights per FLIGHT visit, 1..64 */
@@ -514,7 +516,9 @@ typedef struct clr_engine_config {
     int32_t rare_batch;             /* queue length at which a rare stage (MORPH, TOP, BOTTOM) runs */
     int32_t stage_blocks[CLR_N_STAGES];
     int32_t pass_batch;             /* pass graphs queued between two reads of the live flag */
-    int32_t reserved[3];
+    int32_t acr_budget;             /* bounces per piece of an acrylic traversal while photons are drawn
+                                     * (a multiple of CLR_ENGINE_ACR_BUDGET_STEP) */
+    int32_t reserved[2];
 } clr_engine_config;
 /* Use `config` for the following traces of the context (NULL: back to the defaults). */
 int clr_set_engine_config(clr_ctx* ctx, const clr_engine_config* config);

@@ -280,13 +280,14 @@ TABLES_REFERENCE = 0  # CLR_TABLES_REFERENCE: the reference's order of operation
 TABLES_FAST = 1  # CLR_TABLES_FAST: FMA, two angles per Legendre recurrence (equal to rounding)
 
 STAGE_NAMES = ("GEN", "ENTRY", "FLIGHT", "COND", "GEOM", "MORPH", "TOP", "BOTTOM", "SIDE", "ACRYL", "FIN")
-ENGINE_DEFAULTS = {"flight_steps": 4, "tail_photons": 65536, "rare_batch": 8192, "pass_batch": 8}
+ENGINE_DEFAULTS = {"flight_steps": 4, "tail_photons": 65536, "rare_batch": 8192, "pass_batch": 8, "acr_budget": 256}
 
 
 class EngineConfig(C.Structure):
     """clr_engine_config: scheduling settings of the wavefront engine (zero = default)."""
     _fields_ = [("flight_steps", i32), ("tail_photons", i32), ("rare_batch", i32),
-                ("stage_blocks", i32 * len(STAGE_NAMES)), ("pass_batch", i32), ("reserved", i32 * 3)]
+                ("stage_blocks", i32 * len(STAGE_NAMES)), ("pass_batch", i32), ("acr_budget", i32),
+                ("reserved", i32 * 2)]
 
     @classmethod
     def from_dict(cls, d: dict | None) -> "EngineConfig":

@@ -33,6 +33,7 @@ SPACE: list[tuple[str, list[dict]]] = [
     ("pass_batch", [{"pass_batch": v} for v in (4, 16)]),
     ("tail_photons", [{"tail_photons": v} for v in (16384, 32768, 131072, 262144)]),
     ("rare_batch", [{"rare_batch": v} for v in (2048, 4096, 16384, 32768)]),
+    ("acr_budget", [{"acr_budget": v} for v in (64, 128, 512)]),
 ] + [(f"blocks:{stage}", [{"stage_blocks": {stage: b}} for b in blocks])
      for stage, blocks in (("FLIGHT", (1,)), ("GEN", (1, 2)), ("SIDE", (1, 2)), ("GEOM", (1,)), ("BOTTOM", (2,)),
                            ("TOP", (2,)), ("FIN", (1,)))]

@@ -636,6 +636,7 @@ static int trace_runs(clr_ctx* ctx, const SceneRef* refs, const clr_run_params* 
         w.rare_batch = ec.rare_batch > 0 ? (unsigned)ec.rare_batch : CLR_ENGINE_DEFAULT_RARE_BATCH;
         for (int q = 0; q < CLR_N_STAGES; ++q) w.stage_blocks[q] = std::max(0, ec.stage_blocks[q]);
         w.pass_batch = ec.pass_batch > 0 ? ec.pass_batch : CLR_ENGINE_DEFAULT_PASS_BATCH;
+        w.acr_budget = ec.acr_budget > 0 ? ec.acr_budget : CLR_ENGINE_DEFAULT_ACR_BUDGET;
         w.light = d_light != nullptr;
         w.prov = prov ? ctx->wave_prov : nullptr;
         w.prov_rec = ctx->prov_rec_n > 0 ? ctx->d_prov_rec : nullptr;
@@ -1217,6 +1218,9 @@ int clr_set_engine_config(clr_ctx* ctx, const clr_engine_config* config) {
     for (int q = 0; q < CLR_N_STAGES; ++q)
         if (c.stage_blocks[q] < 0 || c.stage_blocks[q] > 32)
             return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "engine config: stage_blocks must be 0..32");
+    if (c.acr_budget < 0 || c.acr_budget > 16384 || c.acr_budget % CLR_ENGINE_ACR_BUDGET_STEP)
+        return fail(ctx, CLR_ERR_INVALID_ARGUMENT, "engine config: acr_budget must be a multiple of %d up to 16384",
+                    CLR_ENGINE_ACR_BUDGET_STEP);
     ctx->engine = c;
     return CLR_OK;
 }

@@ -82,6 +82,7 @@ struct WaveLaunch {
     unsigned tail_photons, rare_batch;
     int stage_blocks[CLR_WQ_COUNT];
     int pass_batch;
+    int acr_budget;  // bounces per acrylic-traversal piece while photons are still drawn
     bool light;                    // light-history diagnostics on: the FLIGHT stage with its hooks
     uint4* prov;                   // [cap] particle-event provenance per slot; null unless counted
     uint4* prov_rec;               // [n_rays] provenance of every ray, with per-ray records; nullable

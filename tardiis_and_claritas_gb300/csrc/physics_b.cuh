@@ -1143,7 +1143,7 @@ typedef struct {
 
 /* Bounces per window of the trapped-orbit test of long traversals (counter-based stream); the pieces a
  * traversal is cut into must start at multiples of 2 kTrapWindow. */
-constexpr int kTrapWindow = 128;
+constexpr int kTrapWindow = 32;
 
 /* Loop state of a traversal of the acrylic solid, so that a traversal can run in bounded pieces. */
 typedef struct {
@@ -1179,10 +1179,10 @@ __device__ __noinline__ int o_acrylic_run(S* s, const o_cell* C, float n_side_ai
             // ray can reach, from invariants that reflection keeps) can never escape and ends trapped at the
             // bounce cap, as the classifier decides there. The remaining bounces are then accounted with the
             // reflection mix and path per bounce of the last kTrapWindow bounces, and the traversal goes
-            // straight to the cap. The test runs at bounces it = (2k+1) kTrapWindow only and its window
-            // starts at a multiple of 2 kTrapWindow: pieces of a traversal start at multiples of that too
-            // (budgets are multiples of it), so the window lies inside the running piece and the result of a
-            // photon does not depend on how its traversal was cut into pieces.
+            // straight to the cap. The test runs at bounces it = (2k+1) kTrapWindow (it >= 512) only and its
+            // window starts at a multiple of 2 kTrapWindow: pieces of a traversal start at multiples of that
+            // too (budgets are multiples of it), so the window lies inside the running piece and the result
+            // of a photon does not depend on how its traversal was cut into pieces.
             if ((it & (2 * kTrapWindow - 1)) == 0) {
                 snap = *bc;
                 snap_path = *acrylic_path;

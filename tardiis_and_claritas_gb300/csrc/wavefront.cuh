@@ -63,8 +63,9 @@ __host__ __device__ constexpr bool stage_is_rare(int q) {
 __host__ __device__ constexpr int stage_min_blocks(int q) { return q == WQ_COND ? 1 : 2; }
 // acrylic bounces per visit of SIDE, BOTTOM and ACRYL (a traversal can take 16384), all of them
 // once every photon has been drawn
-constexpr int kAcrBudget = 256;
-static_assert(kAcrBudget % (2 * kTrapWindow) == 0, "traversal pieces start where no trapped-orbit window spans them");
+constexpr int kAcrBudget = CLR_ENGINE_DEFAULT_ACR_BUDGET;
+static_assert(kAcrBudget % (2 * kTrapWindow) == 0 && CLR_ENGINE_ACR_BUDGET_STEP % (2 * kTrapWindow) == 0,
+              "traversal pieces start where no trapped-orbit window spans them");
 // closure trials per visit: a few inline in GEOM (most closures end in one or two), more per COND visit
 // (a closure can take 16384 trials, e.g. when no sampled sphere fits)
 constexpr int kCondInline = 8;
@@ -385,7 +386,7 @@ __device__ __forceinline__ int wave_stage_body(const WaveLaunch& w, const DevSce
         return ended ? WQ_FIN : WQ_FLIGHT;
     } else {
         // SIDE, BOTTOM and ACRYL: a bounded piece of the acrylic traversal
-        const int budget = wave_drawing(w) ? kAcrBudget : 0;
+        const int budget = wave_drawing(w) ? w.acr_budget : 0;
         o_acr_state as;
         int caller, v;
         if constexpr (Q == WQ_BOTTOM) {

@@ -1,7 +1,8 @@
 """GPU: the wavefront engine's scheduling settings change the trace time, never the tallies.
 
 clr_engine_config (flight steps per FLIGHT visit, pass graphs between flag reads, the tail-kernel
-threshold, the rare-stage batch and the blocks per SM of each stage kernel) decides only when and where a
+threshold, the rare-stage batch, the bounces per acrylic-traversal piece and the blocks per SM of each
+stage kernel) decides only when and where a
 photon's next stage runs; its draws come from its own counter (Philox) or its own state (the reference's
 per-ray xorshift), so every integer tally must be identical under any setting. Floating-point sums
 (photodiode, incidence, weights) are summed per warp in FP32 and then by atomics in launch order, so they
@@ -19,11 +20,11 @@ from tardiis_and_claritas_gb300 import abi, autotune as AT, scene as S
 pytestmark = pytest.mark.gpu
 
 EXTREMES = [
-    {"flight_steps": 1, "pass_batch": 2, "tail_photons": 1024, "rare_batch": 64,
+    {"flight_steps": 1, "pass_batch": 2, "tail_photons": 1024, "rare_batch": 64, "acr_budget": 64,
      "stage_blocks": {s: 1 for s in abi.STAGE_NAMES}},
-    {"flight_steps": 16, "pass_batch": 32, "tail_photons": 1 << 20, "rare_batch": 1 << 18,
+    {"flight_steps": 16, "pass_batch": 32, "tail_photons": 1 << 20, "rare_batch": 1 << 18, "acr_budget": 1024,
      "stage_blocks": {"GEN": 2, "SIDE": 2, "BOTTOM": 4, "TOP": 4}},
-    {"flight_steps": 3, "tail_photons": 1},
+    {"flight_steps": 3, "tail_photons": 1, "acr_budget": 192},
 ]
 FLOAT_KEYS = ("photodiode_native", "photodiode_mirror", "incidence_native_sum", "incidence_mirror_sum",
               "weight_native", "weight_mirror")
@@ -106,7 +107,8 @@ def test_production_stream_full_scene_identical_under_any_setting(ctx):
 
 def test_invalid_settings_rejected(ctx):
     for bad in ({"flight_steps": 65}, {"flight_steps": -1}, {"pass_batch": 100}, {"tail_photons": -5},
-                {"stage_blocks": {"FLIGHT": 33}}, {"rare_batch": 1 << 22}):
+                {"stage_blocks": {"FLIGHT": 33}}, {"rare_batch": 1 << 22}, {"acr_budget": 100},
+                {"acr_budget": 32768}):
         with pytest.raises(RuntimeError, match="engine config"):
             ctx.set_engine_config(bad)
     ctx.set_engine_config(None)
