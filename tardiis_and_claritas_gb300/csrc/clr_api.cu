@@ -324,6 +324,7 @@ int clr_build_particles(clr_ctx* ctx, const clr_particle_spec* ps, const clr_sed
     CU(D(&pb.pdf, (size_t)n * nt));
     CU(D(&pb.phase_cdf, (size_t)n * nt));
     CU(F(&pb.phase_cdf_f, (size_t)n * nt));
+    CU(dalloc(ctx, (void**)&pb.phase_guide, (size_t)n * (kPhaseGuide + 1) * sizeof(int)));
     CU(D(&pb.muscal, 8));
     CU(D(&pb.sed_major, 4));
     CU(D(&pb.sed_radial_log, (size_t)n * ss->n_radial));
@@ -445,6 +446,7 @@ static void fill_scene(const clr_scene_params& sp, const ParticleBuffers& pb, co
     memset(s, 0, sizeof *s);
     s->P = sp;
     s->gcdf = pb.gcdf_f; s->wcdf = pb.wcdf_f; s->phase_cdf = pb.phase_cdf_f; s->theta = pb.theta_f;
+    s->phase_guide = pb.phase_guide;
     s->pn = pb.pn_f; s->pk = pb.pk_f; s->prad = pb.prad_f;
     s->k = pb.kidx; s->qsca = pb.qsca; s->qext = pb.qext;
     s->moment_a = pb.moment_a; s->moment_b = pb.moment_b; s->moment_mode = pb.moment_mode;
@@ -767,6 +769,7 @@ static void sweep_carve(Arena& A, const SweepLayout& L, std::vector<ParticleBuff
     uint8_t* mm = A.take<uint8_t>(L.bins);
     double* cdf = A.take<double>(L.tabs);
     float* cdf_f = A.take<float>(L.tabs);
+    int* guide = A.take<int>((size_t)L.bins * (kPhaseGuide + 1));
     double* muscal = A.take<double>(8 * (size_t)ns);
     double* smaj = A.take<double>(4 * (size_t)ns);
     float* nmaj = A.take<float>(ns);
@@ -781,6 +784,7 @@ static void sweep_carve(Arena& A, const SweepLayout& L, std::vector<ParticleBuff
         pb.moment_mode = mm + L.bin_off[i];
         pb.phase_cdf = cdf + L.tab_off[i];
         pb.phase_cdf_f = cdf_f + L.tab_off[i];
+        pb.phase_guide = guide + (size_t)L.bin_off[i] * (kPhaseGuide + 1);
         pb.muscal = muscal + 8 * (size_t)i;
         pb.sed_major = smaj + 4 * (size_t)i;
         pb.node_major = nmaj + i;
@@ -943,6 +947,7 @@ static int sweep_build(clr_ctx* ctx, int ns, const clr_scene_params* sps, const 
         b.qabs = P0.qabs + c.b0; b.qback = P0.qback + c.b0; b.g = P0.g + c.b0; b.albedo = P0.albedo + c.b0;
         b.theta = G.theta; b.theta_f = G.theta_f;
         b.cdf = P0.phase_cdf + tab; b.cdf_f = P0.phase_cdf_f + tab; b.err = P0.err;
+        b.guide = P0.phase_guide + (size_t)c.b0 * (kPhaseGuide + 1);
         CU(enqueue_mie_tables(P0.d + c.b0, P0.nidx + c.b0, P0.kidx + c.b0, (int)nb, pss[c.s0].n_medium,
                               pss[c.s0].wavelength_m, G.nt, hybrid_model(sps[c.s0]), c.cap, b, st,
                               pss[c.s0].table_arithmetic == CLR_TABLES_FAST));

@@ -23,6 +23,11 @@ struct LightDiag {
     float *heat_xy, *heat_zy;                   // [vis][vis] (vis 0: none)
 };
 
+// Guide cells per bin of the inverse-CDF phase-angle search: guide[k] is the first angle index whose CDF
+// reaches k / kPhaseGuide (k = 0..kPhaseGuide), so a draw u in cell k = floor(u kPhaseGuide) searches only
+// [guide[k], guide[k+1]] and finds the index the whole-table search finds.
+constexpr int kPhaseGuide = 256;
+
 struct DevScene {
     clr_scene_params P;
     // particle tables (float copies are exact casts of the FP64 tables, which is what the
@@ -30,6 +35,7 @@ struct DevScene {
     const float* gcdf;
     const float* wcdf;
     const float* phase_cdf;     // [n_bins][nt]
+    const int* phase_guide;     // [n_bins][kPhaseGuide + 1], or null (whole-table search)
     const float* theta;         // [nt]
     const float* pn;            // (float)n_real
     const float* pk;            // (float)k_imag

@@ -115,6 +115,7 @@ struct ParticleBuffers {
     double* ab = nullptr;  // Mie a_n, b_n scratch: [n][CLR_MIE_MAX_ORDER][4] (a.re, a.im, b.re, b.im)
     double *theta = nullptr, *pdf = nullptr, *phase_cdf = nullptr;
     float *theta_f = nullptr, *phase_cdf_f = nullptr;
+    int* phase_guide = nullptr;  // [n][kPhaseGuide + 1]
     double *radius = nullptr, *nden = nullptr, *mug = nullptr, *mus = nullptr, *mue = nullptr, *muw = nullptr,
            *muev = nullptr, *gcdf = nullptr, *wcdf = nullptr, *pcdf = nullptr, *muscal = nullptr;
     float *gcdf_f = nullptr, *wcdf_f = nullptr, *pn_f = nullptr, *pk_f = nullptr, *prad_f = nullptr;
@@ -154,6 +155,7 @@ struct MiePhaseBuffers {
     double* pdf;      // [n][nt] scratch
     double* cdf;      // [n][nt]
     float* cdf_f;     // [n][nt]
+    int* guide = nullptr;  // [n][kPhaseGuide + 1] search guide of cdf_f, or null (not built)
     int* err;         // error word, cleared by the call
 };
 cudaError_t enqueue_mie_phase(const double* d, const double* nr, const double* k, int n, double n_medium,

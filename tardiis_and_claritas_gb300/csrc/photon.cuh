@@ -75,6 +75,7 @@ __device__ __forceinline__ CondState cond_start() {
 struct ClosureIn {
     const float* cdf;
     const float* theta;
+    const int* guide;
     double wave;
     float nm, nr, ki, wl, rough, radius, aspect, kappa, coherent;
     float x, y, z, vx, vy, vz, rin, zmin, zmean, delta, core;
@@ -91,7 +92,7 @@ __device__ __forceinline__ int closure_trial(S* s, const ClosureIn& c, int targe
     h->x = x; h->y = y; h->z = z; h->vx = vx; h->vy = vy; h->vz = vz;
     h->channel = (uniform53(s) < c.wave) ? ((c.coherent >= 1.0f || uniform53(s) < c.coherent) ? 1 : 2) : 0;
     if (h->channel == 1) {
-        o_mie_direction(s, c.cdf, c.theta, c.nt, c.pidx, &h->vx, &h->vy, &h->vz);
+        o_mie_direction(s, c.cdf, c.theta, c.nt, c.pidx, &h->vx, &h->vy, &h->vz, c.guide);
         h->status = 1;
     } else if (h->channel == 2) {
         float fr = sqrtf(x * x + y * y), fx = 1, fy = 0;
@@ -175,13 +176,13 @@ template <class S>
 __device__ __forceinline__ int conditional_body(
     S* s, Hist* out, int pidx, double qs, double qe, float nm, float nr, float ki, float wl, float rough,
     float radius, float aspect, int orientation, float kappa, int max_bounces, float coherent, const float* cdf,
-    const float* theta, int nt, float x, float y, float z, float vx, float vy, float vz, float rin, float zmin,
-    float zmean, int surface, float delta, float core, int max_trials, unsigned long long* stats, CondState* cs,
+    const float* theta, const int* guide, int nt, float x, float y, float z, float vx, float vy, float vz, float rin,
+    float zmin, float zmean, int surface, float delta, float core, int max_trials, unsigned long long* stats, CondState* cs,
     int budget, float* wmul, uint32_t trial_tag) {
     if (!cs->started && closure_setup(s, out, qs, qe, ki, max_trials, stats, cs, wmul)) return 1;
     const int target_absorbed = cs->target;
     ClosureIn c;
-    c.cdf = cdf; c.theta = theta; c.wave = qs > 0.0 ? fmax(qs - 1.0, 0.0) / qs : 0.0;
+    c.cdf = cdf; c.theta = theta; c.guide = guide; c.wave = qs > 0.0 ? fmax(qs - 1.0, 0.0) / qs : 0.0;
     c.nm = nm; c.nr = nr; c.ki = ki; c.wl = wl; c.rough = rough; c.radius = radius; c.aspect = aspect;
     c.kappa = kappa; c.coherent = coherent;
     c.x = x; c.y = y; c.z = z; c.vx = vx; c.vy = vy; c.vz = vz; c.rin = rin; c.zmin = zmin; c.zmean = zmean;
@@ -223,13 +224,13 @@ template <class S>
 __device__ __noinline__ int conditional_interaction(
     S* s, Hist* out, int pidx, double qs, double qe, float nm, float nr, float ki, float wl, float rough,
     float radius, float aspect, int orientation, float kappa, int max_bounces, float coherent, const float* cdf,
-    const float* theta, int nt, float x, float y, float z, float vx, float vy, float vz, float rin, float zmin,
-    float zmean, int surface, float delta, float core, int max_trials, unsigned long long* gstats,
+    const float* theta, const int* guide, int nt, float x, float y, float z, float vx, float vy, float vz, float rin,
+    float zmin, float zmean, int surface, float delta, float core, int max_trials, unsigned long long* gstats,
     CondState* cs, int budget, float* wmul, uint32_t trial_tag) {
     unsigned long long stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int done = conditional_body(s, out, pidx, qs, qe, nm, nr, ki, wl, rough, radius, aspect, orientation, kappa,
-                                      max_bounces, coherent, cdf, theta, nt, x, y, z, vx, vy, vz, rin, zmin, zmean,
-                                      surface, delta, core, max_trials, stats, cs, budget, wmul, trial_tag);
+                                      max_bounces, coherent, cdf, theta, guide, nt, x, y, z, vx, vy, vz, rin, zmin,
+                                      zmean, surface, delta, core, max_trials, stats, cs, budget, wmul, trial_tag);
 #pragma unroll
     for (int i = 0; i < 10; ++i)
         if (stats[i]) atomicAdd(gstats + i, stats[i]);
@@ -839,7 +840,7 @@ __device__ __forceinline__ int water_flight(const DevScene& D, Ray& r, S* st, S*
                 int coherent = (COHERENT >= 1.0f) || (uniform(opt) < COHERENT);
                 if (coherent) {
                     r.wcoh++;
-                    o_mie_direction(opt, D.phase_cdf, D.theta, D.nt, pidx, &vx, &vy, &vz);
+                    o_mie_direction(opt, D.phase_cdf, D.theta, D.nt, pidx, &vx, &vy, &vz, D.phase_guide);
                     if (COND) { atomicAdd(&cstats[4], 1ull); atomicAdd(&cstats[7], 1ull); }
                     apply_moment(D, pidx, vinx, viny, vinz, &vx, &vy, &vz);
                     if constexpr (kLight) *ev_pidx = pidx;  // the diagnostic callers' provenance of the event
@@ -946,7 +947,8 @@ __device__ __forceinline__ int closure_visit(const DevScene& D, Ray& r, S* opt, 
     const int done = conditional_interaction(
         opt, &h, pidx, D.qsca[pidx], D.qext[pidx], P.n_water, D.pn[pidx], D.pk[pidx], P.wavelength, P.rough_alpha,
         D.prad[pidx], P.spheroid_aspect, P.orientation_model, P.orientation_kappa, P.max_particle_bounces, COHERENT,
-        D.phase_cdf, D.theta, D.nt, r.x, r.y, r.z, r.vx, r.vy, r.vz, P.rin, P.zmin, P.zmean, P.free_surface_model,
+        D.phase_cdf, D.theta, D.phase_guide, D.nt, r.x, r.y, r.z, r.vx, r.vy, r.vz, P.rin, P.zmin, P.zmean,
+        P.free_surface_model,
         P.vortex_delta_h, P.vortex_core_radius, kind == CK_GEOM ? P.conditional_retries - 1 : P.conditional_retries,
         cstats, cs, budget, (kind == CK_FLIGHT && weighted_run(D)) ? &r.w : nullptr, closure_trial_tag(r.ic));
     if (!done) return 2;
@@ -987,7 +989,8 @@ __device__ __forceinline__ int closure_visit_warp(const DevScene& D, Ray& r, Phi
     if (!done) {
         const double qs = D.qsca[pidx];
         ClosureIn c;
-        c.cdf = D.phase_cdf; c.theta = D.theta; c.wave = qs > 0.0 ? fmax(qs - 1.0, 0.0) / qs : 0.0;
+        c.cdf = D.phase_cdf; c.theta = D.theta; c.guide = D.phase_guide;
+        c.wave = qs > 0.0 ? fmax(qs - 1.0, 0.0) / qs : 0.0;
         c.nm = P.n_water; c.nr = D.pn[pidx]; c.ki = D.pk[pidx]; c.wl = P.wavelength; c.rough = P.rough_alpha;
         c.radius = D.prad[pidx]; c.aspect = P.spheroid_aspect; c.kappa = P.orientation_kappa;
         c.coherent = fminf(fmaxf(D.coherent_f, 0.0f), 1.0f);

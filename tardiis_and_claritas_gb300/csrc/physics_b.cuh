@@ -3,6 +3,7 @@
 // bottom disc. Same conventions as physics_a.cuh.
 #pragma once
 #include "physics_a.cuh"
+#include "device_scene.cuh"
 
 namespace clr {
 namespace {  // header-only device code: internal linkage in every translation unit
@@ -684,9 +685,18 @@ __device__ __forceinline__ int o_sample_cdf(S* s, const float* cdf, int n) {
     return lo;
 }
 template <class S>
-__device__ __forceinline__ float o_mie_theta(S* s, const float* cdf, const float* theta, int nt, int pidx) {
+__device__ __forceinline__ float o_mie_theta(S* s, const float* cdf, const float* theta, int nt, int pidx,
+                                             const int* guide) {
     float u = uniform(s);
     int base = pidx * nt, lo = 0, hi = nt - 1;
+    if (guide) {
+        // u * kPhaseGuide is exact (a power of two): k/G <= u < (k+1)/G, so the first index with u <= cdf lies
+        // between the first indices with cdf >= k/G and cdf >= (k+1)/G, and the search below finds it there
+        const int k = min((int)(u * (float)kPhaseGuide), kPhaseGuide - 1);
+        const int* g = guide + pidx * (kPhaseGuide + 1);
+        lo = __ldg(g + k);
+        hi = __ldg(g + k + 1);
+    }
     while (lo < hi) { int mid = (lo + hi) >> 1; if (u <= __ldg(cdf + base + mid)) hi = mid; else lo = mid + 1; }
     int j = lo;
     if (j <= 0) return theta[0];
@@ -697,8 +707,8 @@ __device__ __forceinline__ float o_mie_theta(S* s, const float* cdf, const float
 }
 template <class S>
 __device__ __forceinline__ void o_mie_direction(S* s, const float* cdf, const float* theta, int nt, int pidx, float* vx,
-                            float* vy, float* vz) {
-    float th = o_mie_theta(s, cdf, theta, nt, pidx);
+                            float* vy, float* vz, const int* guide = nullptr) {
+    float th = o_mie_theta(s, cdf, theta, nt, pidx, guide);
     float phi = 2.0f * CLR_PI_F * uniform(s);
     float e1x, e1y, e1z, e2x, e2y, e2z;
     o_perp_basis(*vx, *vy, *vz, &e1x, &e1y, &e1z, &e2x, &e2y, &e2z);

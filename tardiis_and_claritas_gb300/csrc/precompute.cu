@@ -392,6 +392,19 @@ __global__ void __launch_bounds__(32) phase_cdf_kernel(const double* __restrict_
     for (int j = lane; j < nt; j += 32) cdf_f[base + j] = (float)cdf[base + j];
 }
 
+// guide[p][k] = the first index j of bin p with cdf_f[j] >= k / kPhaseGuide (nt - 1 when none), found by the
+// photon kernels' own search, so that a search restricted to [guide[k], guide[k+1]] returns its index
+__global__ void phase_guide_kernel(const float* __restrict__ cdf_f, int nt, int n_particles, int* __restrict__ guide) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n_particles * (kPhaseGuide + 1)) return;
+    const int p = (int)(t / (kPhaseGuide + 1)), k = (int)(t % (kPhaseGuide + 1));
+    const float u = (float)k / (float)kPhaseGuide;
+    const float* c = cdf_f + (size_t)p * nt;
+    int lo = 0, hi = nt - 1;
+    while (lo < hi) { const int mid = (lo + hi) >> 1; if (u <= c[mid]) hi = mid; else lo = mid + 1; }
+    guide[t] = lo;
+}
+
 __global__ void dummy_phase_kernel(double* theta, float* theta_f, double* cdf, float* cdf_f, int n_particles) {
     int p = blockDim.x * blockIdx.x + threadIdx.x;
     if (p == 0) { theta[0] = 0.0; theta[1] = PD_PI; theta_f[0] = 0.0f; theta_f[1] = (float)PD_PI; }
@@ -1163,6 +1176,10 @@ cudaError_t enqueue_mie_tables(const double* d, const double* nr, const double* 
     } else {
         dummy_phase_kernel<<<(n + 127) / 128, 128, 0, st>>>(b.theta, b.theta_f, b.cdf, b.cdf_f, n);
     }
+    if (b.guide) {
+        const long long cells = (long long)n * (kPhaseGuide + 1);
+        phase_guide_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(b.cdf_f, hybrid ? nt : 2, n, b.guide);
+    }
     return cudaGetLastError();
 }
 
@@ -1290,7 +1307,7 @@ cudaError_t enqueue_particle_precompute(ParticleBuffers& pb, const clr_scene_par
     b.ab = ab_scratch ? ab_scratch : pb.ab;
     b.nstop = pb.nstop; b.x = pb.x; b.qext = pb.qext; b.qsca = pb.qsca; b.qabs = pb.qabs; b.qback = pb.qback;
     b.g = pb.g; b.albedo = pb.albedo; b.theta = pb.theta; b.theta_f = pb.theta_f; b.pdf = pb.pdf;
-    b.cdf = pb.phase_cdf; b.cdf_f = pb.phase_cdf_f; b.err = pb.err;
+    b.cdf = pb.phase_cdf; b.cdf_f = pb.phase_cdf_f; b.guide = pb.phase_guide; b.err = pb.err;
     const int em = sp.event_model;
     e = enqueue_mie_tables(pb.d, pb.nidx, pb.kidx, pb.n, ps.n_medium, ps.wavelength_m, pb.nt,
                            em == 3 || em == 4 || em == 5, CLR_MIE_MAX_ORDER, b, st,
