@@ -44,27 +44,26 @@ static_assert(WQ_FIN + 1 == CLR_WQ_COUNT, "queue count");
 static_assert(CLR_WQ_COUNT == CLR_N_STAGES, "one engine setting per stage queue");
 
 constexpr int kWaveThreads = 256;
-// Defaults of the engine settings (clr_engine_config; an autotuner may choose others per scene class):
-// water flights per FLIGHT visit before the photon is re-queued (bounds lane imbalance in a warp); the
-// photons in flight at or below which, once every photon is drawn, the passes stop and one tail kernel
-// runs each remaining photon to its end in a single thread (the longest histories, thousands of flights
-// in optically dense scenes, then cost one step each instead of a pass each).
-constexpr int kFlightSteps = CLR_ENGINE_DEFAULT_FLIGHT_STEPS;
-constexpr unsigned kTailPhotons = CLR_ENGINE_DEFAULT_TAIL_PHOTONS;
+// Engine settings (WaveLaunch, from clr_engine_config; defaults CLR_ENGINE_DEFAULT_*, chosen per GPU and
+// scene by the tuner): flight_steps water flights per FLIGHT visit before the photon is re-queued (bounds
+// lane imbalance in a warp); tail_photons, the photons in flight at or below which, once every photon is
+// drawn, the passes stop and one tail kernel runs each remaining photon to its end in a single thread (the
+// longest histories, thousands of flights in optically dense scenes, then cost one step each instead of a
+// pass each); rare_batch, the queue length at which a rare stage runs (below); acr_budget, the bounces per
+// piece of an acrylic traversal; pass_batch and stage_blocks on the host side.
 constexpr int kTailThreads = 128;
-// Rare stages (few photons per pass, long serial work per photon) run only when their queue holds a
-// full batch, after kMaxSkips passes, or while the pool drains.
-constexpr unsigned kRareBatch = CLR_ENGINE_DEFAULT_RARE_BATCH;
+// Rare stages (few photons per pass, long serial work per photon) run only when their queue holds
+// rare_batch photons, after kMaxSkips passes, or while the pool drains.
 constexpr unsigned kMaxSkips = 8;
 __host__ __device__ constexpr bool stage_is_rare(int q) {
     return q == WQ_MORPH || q == WQ_TOP || q == WQ_BOTTOM;
 }
 // minimum resident blocks per SM (register budget) per stage
 __host__ __device__ constexpr int stage_min_blocks(int q) { return q == WQ_COND ? 1 : 2; }
-// acrylic bounces per visit of SIDE, BOTTOM and ACRYL (a traversal can take 16384), all of them
-// once every photon has been drawn
-constexpr int kAcrBudget = CLR_ENGINE_DEFAULT_ACR_BUDGET;
-static_assert(kAcrBudget % (2 * kTrapWindow) == 0 && CLR_ENGINE_ACR_BUDGET_STEP % (2 * kTrapWindow) == 0,
+// acrylic bounces per visit of SIDE, BOTTOM and ACRYL while photons are drawn (acr_budget; a traversal can
+// take 16384), all of them once every photon has been drawn
+static_assert(CLR_ENGINE_DEFAULT_ACR_BUDGET % (2 * kTrapWindow) == 0 &&
+                  CLR_ENGINE_ACR_BUDGET_STEP % (2 * kTrapWindow) == 0,
               "traversal pieces start where no trapped-orbit window spans them");
 // closure trials per visit: a few inline in GEOM (most closures end in one or two), more per COND visit
 // (a closure can take 16384 trials, e.g. when no sampled sphere fits)
