@@ -277,12 +277,14 @@ def run_surrogate(args, rank: int, world: int, local_rank: int, dist, dev) -> di
     if judge is not None:
         judged["precision_judge"] = G.judged_error(model, judge)
     # the same network trained with 1/(noise variance + floor^2) label weights, for comparison
-    model_u = G.Surrogate(local_rank, max_batch=65536, seed=rank)
-    model_u.fit(train, epochs=args.sur_epochs, batch=2048, weight_floor=G.WEIGHT_FLOOR_REL)
-    judged_u = {"held_out_at_100x_photons": G.judged_error(model_u, test)}
-    if judge is not None:
-        judged_u["precision_judge"] = G.judged_error(model_u, judge)
-    model_u.close()
+    judged_u = None
+    if getattr(args, "sur_compare_weighted", True):
+        model_u = G.Surrogate(local_rank, max_batch=65536, seed=rank)
+        model_u.fit(train, epochs=args.sur_epochs, batch=2048, weight_floor=G.WEIGHT_FLOOR_REL)
+        judged_u = {"held_out_at_100x_photons": G.judged_error(model_u, test)}
+        if judge is not None:
+            judged_u["precision_judge"] = G.judged_error(model_u, judge)
+        model_u.close()
     # surrogate-in-the-loop inversion of concentration (Monte Carlo as check and fallback)
     inv = G.inversion_study(ctx, model, n=args.inv_scenarios, photons=4_000_000, mc_only=args.inv_mc_only,
                             sampler_seed=3000 + rank) if args.inv_scenarios > 0 else None
@@ -430,6 +432,26 @@ def weighted_subrecord(ctx, args) -> dict:
     out["weighted_gain_at_equal_error"] = equal_error_speedup(out["weighted"]["tally_error"],
                                                               out["analog"]["tally_error"])
     return out
+
+
+def surrogate_subrecord(args, rank, world, local_rank, dev) -> dict:
+    """The surrogate (C4) in the default line, reduced: 16384 training scenarios at 1e6 photons (the full
+    C4 size, 262144, is `--workload surrogate`), judged on 128 held-out scenarios at 1e8 photons with the
+    judge's noise removed, and timed inference on 65536-query batches. About 90 s of GPU."""
+    sub = argparse.Namespace(**vars(args))
+    sub.steps, sub.warmup = 10, 3
+    sub.sur_train, sub.sur_test, sub.sur_photons, sub.sur_epochs = 16384, 128, 1_000_000, 400
+    sub.sur_judge, sub.inv_scenarios, sub.sur_compare_weighted = 0, 0, False
+    line = run_surrogate(sub, rank, world, local_rank, None, dev)
+    sur = line["surrogate"]
+    return {"metric": line["metric"], "value": line["value"], "unit": line["unit"], "e2e": line["e2e"],
+            "roofline": line["roofline"], "workload": line["config"]["workload"],
+            "judged_error": sur["judged"]["held_out_at_100x_photons"], "median_error": sur["vs_mc"],
+            "linear_baseline": sur["linear_baseline"], "train": sur["train"], "mc": sur["mc"],
+            "speedup_vs_mc_at_training_photons": sur["speedup_vs_mc_at_training_photons"],
+            "speedup_vs_mc_at_check_photons": sur["speedup_vs_mc_at_check_photons"],
+            "reduced": "16384 training scenarios of the C4 sampler (C4: 262144) and 128 judge scenarios at 1e8 "
+                       "photons (C4: 4096); the full size runs with --workload surrogate"}
 
 
 def sweep_subrecord(args, ctx, rank, world, local_rank, dev) -> dict:
@@ -823,6 +845,10 @@ def main():
         line["rankine"] = rankine_subrecord(ctx, args, rng_mode, flush)
         line["sweep"] = sweep_subrecord(args, ctx, rank, world, local_rank, dev)
         line["weighted"] = weighted_subrecord(ctx, args)
+        try:
+            line["surrogate"] = surrogate_subrecord(args, rank, world, local_rank, dev)
+        except Exception as e:  # the headline line must not depend on the sub-record
+            line["surrogate"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0 and world == 1 and not args.no_cpu:
         ref = CpuReference(args.workload, os.cpu_count() or 1)
         ns = ref.sample_size(args.cpu_seconds)
