@@ -47,3 +47,38 @@ def test_oracle_gradient_matches_finite_differences(weighted):
         fd = (M.loss_and_grad(pp, x, t, False, w)[0] - M.loss_and_grad(pm, x, t, False, w)[0]) / (2 * eps)
         assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(fd)) + 1e-9, (k, fd, g[k])
     assert loss > 0
+
+
+class _KnownErrorModel:
+    """A stand-in surrogate whose prediction is the true signal times (1 + e), e ~ N(bias, s)."""
+
+    def __init__(self, truth_log10, s, bias, seed):
+        rng = np.random.default_rng(seed)
+        self.pred = truth_log10 + np.log10(1.0 + bias + s * rng.standard_normal(truth_log10.shape))
+
+    def predict(self, x):
+        return self.pred
+
+
+@pytest.mark.parametrize("s_true,hits", [(0.01, 2e4), (0.02, 5e3), (0.005, 1e5)])
+def test_judged_error_removes_the_judge_noise(s_true, hits):
+    """surrogate.judged_error: prediction/MC - 1 has variance s^2 + sigma_judge^2; the estimator recovers s
+    (within a few bootstrap standard errors) although the judge's own noise is as large as s."""
+    from tardiis_and_claritas_gb300 import surrogate as G
+    rng = np.random.default_rng(1)
+    m = 400
+    rate = 10.0 ** rng.uniform(-5, -3, size=(m, 3))
+    photons = np.full(m, 2.0 * hits / 1e-4)
+    lam = rate * photons[:, None]
+    counts = rng.poisson(2.0 * lam) / 2.0  # symmetric score: (native + mirror) / 2
+    y = np.log10((counts + 0.5) / photons[:, None])
+    judge = G.Dataset(x=np.zeros((m, 6)), y=y, hits=counts, photons=photons, mc_seconds=0.0)
+    model = _KnownErrorModel(np.log10(rate), s_true, 0.0, seed=2)
+    out = G.judged_error(model, judge, min_hits=100.0, boot=500)
+    for name in G.SIGNAL_NAMES:
+        r = out[name]
+        assert r["scenarios"] > 100
+        assert abs(r["rms_rel_error"] - s_true) < 4.0 * r["rms_rel_error_se"] + 0.15 * s_true, (name, r)
+        assert abs(r["mean_bias"]) < 4.0 * r["mean_bias_se"] + 1e-4, (name, r)
+        # the raw difference overstates the error by the judge's noise
+        assert r["raw_rms_rel_difference"] > r["rms_rel_error"]
